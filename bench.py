@@ -1,0 +1,364 @@
+#!/usr/bin/env python
+"""Benchmark: site-steps/s of the CAC step on the C2 workload (EAM Cu, 1,000,000
+atoms + 20,000 elements, FP64) on one GB300 per rank.
+
+A step is one full Verlet step of the reference's loop (verlet.cpp:163-218):
+NVE half-kick and drift of atoms and nodes, rebuild decision (every 10 steps,
+1 A trigger), ghost refresh or rebuild, EAM density + embedding derivative +
+force passes over the atom list, nodal densities and integration-point forces
+over the element lists with the shape-function gather onto the nodes, and the
+final half-kick.  site-steps/s = (atoms + Gauss integration points) * steps / s.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--mode fp64|exact|mixed]
+  python bench.py --impl reference ...   # the reference algorithm on the host cores
+
+Multi-GPU (torchrun): replicas only -- every rank runs its own C2 system, no
+collective on the data path; value = all ranks' site-steps / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "site-steps/s on 1 GB300: mixed+surrogate vs plain FP64 at ≤1e-4 rel force err"
+UNIT = "site-steps/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=50)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--mode", default="fp64", choices=["fp64", "exact", "mixed"])
+    p.add_argument("--small", action="store_true", help="the 8,000-atom C2 sample (profiling)")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+# ----------------------------------------------------------------------------- ranks
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=ws)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(ws, v):
+    if ws <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ----------------------------------------------------------------------------- clocks
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------- CPU legs
+
+def _cpu_worker(args):
+    """One host core: the CPU restatement of the reference on a C2-structured
+    sample replica (8,000 atoms + 160 elements), timed over ``steps`` steps."""
+    seed, steps, warm, eam = args
+    sys.path.insert(0, ROOT)
+    from cac_code_gb300 import workloads as W
+    from oracle import oracle as O
+    m, cfg = W.c2_sample(seed=seed)
+    o = O.Oracle(m, **W.oracle_kwargs(cfg, eam))
+    o.setup()
+    if m.natoms:
+        o.atom_list()
+    if m.nelements:
+        o.elem_lists()
+    o.run(warm)
+    t0 = time.perf_counter()
+    o.run(steps)
+    dt = time.perf_counter() - t0
+    return W.metric_sites(m, cfg) * steps / dt, dt
+
+
+def cpu_leg(cores, steps, warm, eam):
+    from oracle import oracle as O
+    O.build()
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_cpu_worker, [(100 + k, steps, warm, eam) for k in range(cores)])
+    return sum(r[0] for r in res), max(r[1] for r in res)
+
+
+# ----------------------------------------------------------------------------- arms
+
+def algorithmic_bytes_force_atoms(natoms, mean_neigh):
+    """EAM force pass over the atom list (bytes per launch): x_i 24 + list 4n +
+    fp_i 8 + f_i 24."""
+    return natoms * (24 + 4 * mean_neigh + 8 + 24)
+
+
+def run_ours(a, ws, rank, local):
+    import numpy as np
+    from cac_code_gb300 import build, cacg
+    from cac_code_gb300 import workloads as W
+    build.build_library()
+    tmp = tempfile.mkdtemp(prefix="cacbench_")
+    eam = W.write_eam(os.path.join(tmp, "Cu_analytic_2000.eam"))
+
+    cpu = None
+    if rank == 0 and ws == 1 and not a.no_cpu_baseline:
+        # before the first GPU call: spawn the host-core sample
+        cores = os.cpu_count() or 1
+        val, wall = cpu_leg(cores, 3, 1, eam)
+        cpu = {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{cores} independent 8,000-atom + 160-element C2-structured replicas "
+                         f"(CPU restatement of the reference, oracle/cac_oracle.c), 3 timed steps "
+                         f"each after 1 warm-up, {wall:.1f} s"}
+
+    m, cfg = (W.c2_sample(seed=5) if a.small else W.c2_eam())
+    sites = W.metric_sites(m, cfg)
+    s = cacg.System(local)
+    W.configure_system(s, m, cfg, eam)
+    mode = {"fp64": cacg.FP64, "exact": cacg.FP64_EXACT, "mixed": cacg.MIXED}[a.mode]
+    s.set_precision(mode)
+    s.init()
+    s.setup()
+    s.neighbor_build()
+    if m.nelements:
+        s.neighbor_ebuild()
+        s.neighbor_nbuild()
+    c0 = s.counts()
+    s.run(max(a.warmup, 3))
+    s.set_timing(True)
+
+    clocks = ClockSampler(local)
+    barrier(ws)
+    clocks.start()
+    l0 = s.counts()["launches"]
+    t0 = time.perf_counter()
+    s.run(a.steps)
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    barrier(ws)
+    tm = s.timing()
+    c1 = s.counts()
+    launches = c1["launches"] - l0
+    dev_ms = float(tm[0])
+    ms_max = allmax(ws, dev_ms)
+    value = ws * sites * a.steps / (ms_max * 1e-3)
+
+    # dominant kernel: EAM force pass over the atom list (phase 3), one launch per step
+    mean_neigh = c0["atom_entries"] / max(c0["nlocal"], 1)
+    phase = {"integrate+comm": tm[1], "atom_rho": tm[2], "atom_force": tm[3],
+             "element": tm[4], "final": tm[5]}
+    k_ms = tm[3] / a.steps
+    abytes = algorithmic_bytes_force_atoms(c0["nlocal"], mean_neigh)
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak, peak_src = 6790.0, "fallback 6.8 TB/s"
+    if os.path.exists(peaks_path):
+        try:
+            peak = float(json.load(open(peaks_path))["hbm_gbs"])
+            peak_src = "measured (MEASURED_PEAKS.json hbm_gbs)"
+        except Exception:
+            pass
+    achieved = abytes / (k_ms * 1e-3) / 1e9 if k_ms > 0 else 0.0
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        try:
+            tj = json.load(open(tpath))
+            per_atom = tj.get("k_eam_force_atoms_bytes_per_atom")
+            if per_atom:
+                traffic = per_atom * c0["nlocal"]
+        except Exception:
+            traffic = None
+    fp64_peak = s.fp64_peak()
+
+    # e2e through the C ABI with host-resident state: push x,v (atoms + nodes)
+    # from pinned host memory, one step, read x,v,f back, every step
+    e2e = None
+    if not a.no_e2e:
+        try:
+            import torch
+            pin = torch.cuda.is_available()
+        except Exception:
+            pin = False
+        n = c1["nlocal"]
+        ne = c1["enlocal"]
+
+        def host(shape):
+            if pin:
+                import torch
+                return torch.empty(shape, dtype=torch.float64).pin_memory().numpy()
+            return np.empty(shape, dtype=np.float64)
+        hx, hv, hf = host((n, 3)), host((n, 3)), host((n, 3))
+        hnx, hnv = host((ne, 8, 3)), host((ne, 8, 3))
+        s.get_state_into(hx, hv, hf)
+        el = s.elements()
+        hnx[...] = el["nodex"]
+        hnv[...] = el["nodev"]
+        s.set_timing(False)
+        e_steps = max(5, min(a.steps, 20))
+        barrier(ws)
+        t0 = time.perf_counter()
+        for _ in range(e_steps):
+            s.put_atoms(hx, hv)
+            s.put_nodes(hnx, hnv)
+            s.run(1)
+            s.get_state_into(hx, hv, hf)
+        e_wall = time.perf_counter() - t0
+        e_wall = allmax(ws, e_wall)
+        e2e = {"value": ws * sites * e_steps / e_wall, "unit": UNIT,
+               "h2d_bytes_per_step": int(hx.nbytes + hv.nbytes + hnx.nbytes + hnv.nbytes),
+               "d2h_bytes_per_step": int(hx.nbytes + hv.nbytes + hf.nbytes),
+               "steps": e_steps}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps,
+            "warmup": max(a.warmup, 3), "ms_per_step": ms_max / a.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if a.mode != "mixed" else "f32+f64", "data": "synthetic",
+            "config": {
+                "workload": ("C2 sample: EAM Cu 8,000 atoms + 160 elements" if a.small else
+                             "C2: EAM Cu CAC slab, 1,000,000 atoms + 20,000 elements (10 sites/edge), FP64"),
+                "mode": a.mode, "atoms": c0["nlocal"], "ghost_atoms": c0["nghost"],
+                "elements": c0["enlocal"], "ghost_elements": c0["enghost"],
+                "gauss_points": cfg["gauss_per_element"] * c0["enlocal"],
+                "integration_rows": c0["ip_rows"], "sites": sites,
+                "atom_list_mean": round(mean_neigh, 2),
+                "ip_list_mean": round(c0["ip_entries"] / max(c0["ip_rows"], 1), 2),
+                "rebuild": "every 10 steps if any displacement > skin/2 (check yes)",
+                "rebuilds_in_timed_region": c1["rebuilds"] - c0["rebuilds"],
+                "l2": "inputs larger than L2 (positions+lists >> 129 MB resident)",
+                "parallelism": f"replicas{ws}",
+                "phase_ms_per_step": {k: round(v / a.steps, 4) for k, v in phase.items()},
+                "wall_s": round(wall, 3)},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "k_eam_force_atoms (EAM force pass over the atom list)",
+                         "algorithmic_bytes_per_launch": abytes, "kernel_ms": k_ms,
+                         "peak_source": peak_src,
+                         "fp64_peak_flops_measured": fp64_peak,
+                         "note": "FP64 pair math is ALU-bound on GB300; see fp64_peak"},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "clocks": clk,
+            "gpu_launches": launches,
+        }
+        print(json.dumps(line), flush=True)
+    s.close()
+
+
+def run_reference(a, ws, rank):
+    if rank != 0:
+        return
+    from cac_code_gb300 import workloads as W
+    tmp = tempfile.mkdtemp(prefix="cacref_bench_")
+    eam = W.write_eam(os.path.join(tmp, "Cu_analytic_2000.eam"))
+    cores = os.cpu_count() or 1
+    steps = max(1, min(a.steps, 3))
+    val, wall = cpu_leg(cores, steps, 1, eam)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": ws,
+        "steps": steps, "warmup": 1, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "C2: EAM Cu CAC slab, sampled on the host cores",
+                   "parallelism": f"{cores} host processes"},
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{cores} independent 8,000-atom + 160-element C2-structured "
+                                   f"replicas, {steps} timed steps each, {wall:.1f} s; the "
+                                   f"reference's own binary is x86-only here, so its CPU "
+                                   f"restatement (bit-identical outputs) is timed"},
+        "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    a = parse()
+    ws, rank, local = dist_init()
+    if a.impl == "reference":
+        run_reference(a, ws, rank)
+    else:
+        run_ours(a, ws, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,287 @@
+"""ctypes binding of libcacg.so (include/cacg.h) and a thin Python mirror of the
+reference's objects for the CAC force path.
+
+``System`` is one CAC system resident on one GPU.  Its methods are the
+reference entry points the C ABI replaces:
+
+================================  ==========================================
+System method                     reference routine
+================================  ==========================================
+command / file                    Input::execute_command / Input::file
+init / setup                      CAC::init / Verlet::setup (without its abort)
+neighbor_build/ebuild/nbuild      Neighbor::build / ebuild / nbuild
+pair_compute / pair_ecompute      Pair::compute / Pair::ecompute
+fix_nve_initial/final             FixNVE::(e)initial_integrate / (e)final_integrate
+run                               Verlet::run
+================================  ==========================================
+
+There is no CPU fallback: a missing library or GPU raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Dict, Optional
+
+import numpy as np
+
+from . import build as _build
+
+FP64_EXACT, FP64, MIXED = 0, 1, 2
+_STATUS = {0: "ok", -1: "invalid", -2: "state", -3: "cuda", -4: "overflow", -5: "io",
+           -6: "nomem", -7: "timeout"}
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+_lp = ctypes.POINTER(ctypes.c_longlong)
+
+EXPORTED = [
+    "cacg_create", "cacg_destroy", "cacg_error", "cacg_version", "cacg_command", "cacg_file",
+    "cacg_set_box", "cacg_set_masses", "cacg_set_atoms", "cacg_set_element_types",
+    "cacg_set_elements", "cacg_set_precision", "cacg_init", "cacg_setup",
+    "cacg_neighbor_build", "cacg_neighbor_ebuild", "cacg_neighbor_nbuild",
+    "cacg_pair_compute", "cacg_pair_ecompute", "cacg_fix_nve_initial_integrate",
+    "cacg_fix_nve_final_integrate", "cacg_run", "cacg_get_counts", "cacg_get_atoms",
+    "cacg_get_elements", "cacg_get_atom_list", "cacg_get_elem_list", "cacg_get_ip_list",
+    "cacg_get_cut", "cacg_set_timing", "cacg_get_timing", "cacg_measure_fp64_peak",
+    "cacg_put_atoms", "cacg_put_nodes",
+]
+
+
+class CacgError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"[{_STATUS.get(status, status)}] {msg}")
+        self.status = status
+
+
+_LIB: Optional[ctypes.CDLL] = None
+
+
+def load(build_if_missing: bool = False) -> ctypes.CDLL:
+    """Load libcacg.so from the package directory (built in-tree)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(_build.LIB):
+        if not build_if_missing:
+            raise FileNotFoundError(
+                f"{_build.LIB} is missing: run cac_code_gb300.build.build_library() first")
+        _build.build_library()
+    lib = ctypes.CDLL(_build.LIB)
+    lib.cacg_error.restype = ctypes.c_char_p
+    lib.cacg_error.argtypes = [ctypes.c_void_p]
+    lib.cacg_version.restype = ctypes.c_char_p
+    lib.cacg_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int]
+    for name in ("cacg_destroy", "cacg_init", "cacg_setup", "cacg_neighbor_build",
+                 "cacg_neighbor_ebuild", "cacg_neighbor_nbuild", "cacg_pair_ecompute",
+                 "cacg_fix_nve_initial_integrate", "cacg_fix_nve_final_integrate"):
+        getattr(lib, name).argtypes = [ctypes.c_void_p]
+    lib.cacg_command.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+    lib.cacg_file.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+    lib.cacg_run.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.cacg_set_precision.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.cacg_set_timing.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.cacg_pair_compute.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+    lib.cacg_get_cut.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp]
+    _LIB = lib
+    return lib
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp) if a is not None else None
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip) if a is not None else None
+
+
+class System:
+    """One CAC system on one GPU, driven through the C ABI."""
+
+    def __init__(self, device: int = 0):
+        self._L = load()
+        h = ctypes.c_void_p()
+        rc = self._L.cacg_create(ctypes.byref(h), device)
+        if rc != 0:
+            raise CacgError(rc, "cacg_create failed (no CUDA device visible?)")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._L.cacg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ok(self, rc: int):
+        if rc != 0:
+            raise CacgError(rc, self._L.cacg_error(self.h).decode())
+
+    # ---- input ----
+    def command(self, line: str):
+        self._ok(self._L.cacg_command(self.h, line.encode()))
+
+    def commands(self, text: str):
+        for line in text.splitlines():
+            self.command(line)
+
+    def file(self, path: str):
+        self._ok(self._L.cacg_file(self.h, path.encode()))
+
+    def set_precision(self, mode: int):
+        self._ok(self._L.cacg_set_precision(self.h, mode))
+
+    # ---- direct state ----
+    def set_box(self, lo, hi, periodic):
+        lo = np.ascontiguousarray(lo, dtype=np.float64)
+        hi = np.ascontiguousarray(hi, dtype=np.float64)
+        per = np.ascontiguousarray([1 if p else 0 for p in periodic], dtype=np.int32)
+        self._ok(self._L.cacg_set_box(self.h, _d(lo), _d(hi), _i(per)))
+
+    def set_masses(self, mass):
+        m = np.ascontiguousarray(mass, dtype=np.float64)
+        self._ok(self._L.cacg_set_masses(self.h, len(m), _d(m)))
+
+    def set_atoms(self, x, v=None, type_=None):
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
+        v = None if v is None else np.ascontiguousarray(v, dtype=np.float64).reshape(-1, 3)
+        t = None if type_ is None else np.ascontiguousarray(type_, dtype=np.int32)
+        self._ok(self._L.cacg_set_atoms(self.h, x.shape[0], _d(x), _d(v), _i(t)))
+
+    def set_element_types(self, etypes):
+        nae = np.ascontiguousarray([et.nae for et in etypes], dtype=np.int32).reshape(-1)
+        numint = np.ascontiguousarray([len(et.intp) for et in etypes], dtype=np.int32)
+        intp = np.ascontiguousarray(np.concatenate([et.intp for et in etypes]), dtype=np.int32)
+        w = np.ascontiguousarray(np.concatenate([et.weight for et in etypes]), dtype=np.float64)
+        self._ok(self._L.cacg_set_element_types(self.h, len(etypes), _i(nae), _i(numint),
+                                                _i(intp), _d(w)))
+
+    def set_elements(self, etype, centre, nodex, nodev=None):
+        et = np.ascontiguousarray(etype, dtype=np.int32)
+        c = np.ascontiguousarray(centre, dtype=np.float64)
+        nx = np.ascontiguousarray(nodex, dtype=np.float64)
+        nv = None if nodev is None else np.ascontiguousarray(nodev, dtype=np.float64)
+        self._ok(self._L.cacg_set_elements(self.h, len(et), _i(et), _d(c), _d(nx), _d(nv)))
+
+    def load_model(self, model):
+        """Upload a lattice.Model (the same data read_data would deliver)."""
+        self.set_box(model.boxlo, model.boxhi, model.periodic)
+        self.set_masses([model.mass])
+        self.set_atoms(model.atom_x, model.atom_v, np.ones(model.natoms, dtype=np.int32))
+        if model.nelements:
+            self.set_element_types(model.etypes)
+            self.set_elements(model.elem_type, model.element_centres(), model.nodex, model.nodev)
+
+    # ---- path ----
+    def init(self):
+        self._ok(self._L.cacg_init(self.h))
+
+    def setup(self):
+        self._ok(self._L.cacg_setup(self.h))
+
+    def neighbor_build(self):
+        self._ok(self._L.cacg_neighbor_build(self.h))
+
+    def neighbor_ebuild(self):
+        self._ok(self._L.cacg_neighbor_ebuild(self.h))
+
+    def neighbor_nbuild(self):
+        self._ok(self._L.cacg_neighbor_nbuild(self.h))
+
+    def pair_compute(self, eflag: int = 0, vflag: int = 0):
+        self._ok(self._L.cacg_pair_compute(self.h, eflag, vflag))
+
+    def pair_ecompute(self):
+        self._ok(self._L.cacg_pair_ecompute(self.h))
+
+    def fix_nve_initial_integrate(self):
+        self._ok(self._L.cacg_fix_nve_initial_integrate(self.h))
+
+    def fix_nve_final_integrate(self):
+        self._ok(self._L.cacg_fix_nve_final_integrate(self.h))
+
+    def run(self, n: int):
+        self._ok(self._L.cacg_run(self.h, n))
+
+    # ---- state out ----
+    def counts(self) -> Dict[str, int]:
+        c = np.zeros(13, dtype=np.int64)
+        self._ok(self._L.cacg_get_counts(self.h, c.ctypes.data_as(_lp), 13))
+        keys = ["nlocal", "nghost", "atom_entries", "enlocal", "enghost", "elem_entries",
+                "ip_rows", "ip_entries", "rebuilds", "nstencil", "step", "sites", "launches"]
+        return dict(zip(keys, (int(v) for v in c)))
+
+    def atoms(self, all_: bool = False) -> Dict[str, np.ndarray]:
+        c = self.counts()
+        nl = c["nlocal"]
+        n = nl + (c["nghost"] if all_ else 0)
+        x = np.zeros((n, 3)); v = np.zeros((nl, 3)); f = np.zeros((nl, 3))
+        tag = np.zeros(n, dtype=np.int32)
+        self._ok(self._L.cacg_get_atoms(self.h, 1 if all_ else 0, _d(x), _d(v), _d(f), _i(tag)))
+        return {"x": x, "v": v, "f": f, "tag": tag}
+
+    def elements(self, all_: bool = False) -> Dict[str, np.ndarray]:
+        c = self.counts()
+        nl = c["enlocal"]
+        n = nl + (c["enghost"] if all_ else 0)
+        cx = np.zeros((n, 3)); nx = np.zeros((n, 8, 3))
+        nv = np.zeros((nl, 8, 3)); nf = np.zeros((nl, 8, 3))
+        tag = np.zeros(n, dtype=np.int32)
+        self._ok(self._L.cacg_get_elements(self.h, 1 if all_ else 0, _d(cx), _d(nx), _d(nv),
+                                           _d(nf), _i(tag)))
+        return {"x": cx, "nodex": nx, "nodev": nv, "nodef": nf, "tag": tag}
+
+    def atom_list(self):
+        c = self.counts()
+        num = np.zeros(c["nlocal"], dtype=np.int32)
+        nb = np.zeros(max(c["atom_entries"], 1), dtype=np.int32)
+        self._ok(self._L.cacg_get_atom_list(self.h, _i(num), _i(nb)))
+        return num, nb[:c["atom_entries"]]
+
+    def elem_lists(self):
+        c = self.counts()
+        enum = np.zeros(c["enlocal"], dtype=np.int32)
+        eneigh = np.zeros(max(c["elem_entries"], 1), dtype=np.int32)
+        self._ok(self._L.cacg_get_elem_list(self.h, _i(enum), _i(eneigh)))
+        ipn = np.zeros(c["ip_rows"], dtype=np.int32)
+        ipj = np.zeros(max(c["ip_entries"], 1), dtype=np.int32)
+        ipnj = np.zeros(max(c["ip_entries"], 1), dtype=np.int32)
+        self._ok(self._L.cacg_get_ip_list(self.h, _i(ipn), _i(ipj), _i(ipnj)))
+        return enum, eneigh[:c["elem_entries"]], ipn, ipj[:c["ip_entries"]], ipnj[:c["ip_entries"]]
+
+    def cut(self, what: int) -> float:
+        v = ctypes.c_double()
+        self._ok(self._L.cacg_get_cut(self.h, what, ctypes.byref(v)))
+        return v.value
+
+    def cuts(self) -> np.ndarray:
+        return np.array([self.cut(i) for i in range(6)])
+
+    def set_timing(self, enable: bool = True):
+        self._ok(self._L.cacg_set_timing(self.h, 1 if enable else 0))
+
+    def timing(self) -> np.ndarray:
+        """[total, integrate+comm/rebuild, atom pass 1, atom pass 2, element, final]"""
+        ms = np.zeros(8)
+        self._ok(self._L.cacg_get_timing(self.h, _d(ms), 8))
+        return ms[:6]
+
+    def put_atoms(self, x, v):
+        """Push host-owned owned-atom x, v (float64 [nlocal][3], C order)."""
+        self._ok(self._L.cacg_put_atoms(self.h, _d(x), _d(v)))
+
+    def put_nodes(self, nodex, nodev):
+        self._ok(self._L.cacg_put_nodes(self.h, _d(nodex), _d(nodev)))
+
+    def get_state_into(self, x, v, f):
+        """Read owned-atom x, v, f into caller-provided float64 [nlocal][3] buffers."""
+        self._ok(self._L.cacg_get_atoms(self.h, 0, _d(x), _d(v), _d(f), None))
+
+    def fp64_peak(self) -> float:
+        v = ctypes.c_double()
+        self._ok(self._L.cacg_measure_fp64_peak(self.h, ctypes.byref(v)))
+        return v.value

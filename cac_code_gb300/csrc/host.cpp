@@ -1,0 +1,2015 @@
+// Host side of libcacg.so: the C ABI in include/cacg.h.
+//
+// The handle mirrors the reference's objects for this path -- Domain box,
+// Atom/Element arrays, Neighbor settings and lists, Pair tables, FixNVE -- but
+// the arrays live on the GPU from cacg_init on.  Host code does only what the
+// reference does once per rebuild on scalars (cutoffs, bin geometry, swap
+// slabs, element-size maximum) and drives the kernels on one stream.
+//
+// Parsing follows the reference's command and file formats so an input
+// script written for the reference runs unchanged:
+//   Input::execute_command  input.cpp:362-404
+//   ReadData::command       read_data.cpp:70-246, 277-367, 379-688
+//   PairLJCut::settings/coeff/init_one  pair_lj_cut.cpp:75-198
+//   PairEAM::coeff/read_file/file2array/array2spline  pair_eam.cpp:119-580
+//   Neighbor::set/modify_params/init/setup_bins  neighbor.cpp:188-481, 828-976
+//   Element tables  element.cpp:725-906, 1170-1423
+//   CommBrick::setup  comm_brick.cpp:182-367
+#include "../../include/cacg.h"
+#include "internal.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+using namespace cacg;
+
+namespace {
+
+struct ApiError {
+  int code;
+  std::string msg;
+};
+
+[[noreturn]] void fail(int code, const char *fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  throw ApiError{code, buf};
+}
+
+struct SwapDef {
+  int dim = 0, pbc = 0;
+  double lo = 0, hi = 0;
+  double mlo[MAXT + 1] = {}, mhi[MAXT + 1] = {};
+  int nsend = 0, firstrecv = 0, send_off = 0;
+  int ensend = 0, efirstrecv = 0, esend_off = 0;
+  double d[3] = {0, 0, 0};
+};
+
+double numeric(const std::string &s) {
+  char *end = nullptr;
+  double v = strtod(s.c_str(), &end);
+  if (end == s.c_str() || *end) fail(CACG_EINVAL, "Expected floating point parameter instead of '%s'", s.c_str());
+  return v;
+}
+
+int inumeric(const std::string &s) {
+  char *end = nullptr;
+  long v = strtol(s.c_str(), &end, 10);
+  if (end == s.c_str() || *end) fail(CACG_EINVAL, "Expected integer parameter instead of '%s'", s.c_str());
+  return (int) v;
+}
+
+// Force::bounds: "*", "n", "*n", "n*", "m*n" over 1..nmax (force.cpp:182-210)
+void bounds(const std::string &s, int nmax, int &lo, int &hi) {
+  size_t p = s.find('*');
+  if (p == std::string::npos) {
+    lo = hi = inumeric(s);
+  } else if (s.size() == 1) {
+    lo = 1;
+    hi = nmax;
+  } else if (p == 0) {
+    lo = 1;
+    hi = inumeric(s.substr(1));
+  } else if (p == s.size() - 1) {
+    lo = inumeric(s.substr(0, p));
+    hi = nmax;
+  } else {
+    lo = inumeric(s.substr(0, p));
+    hi = inumeric(s.substr(p + 1));
+  }
+  if (lo < 1 || hi > nmax || lo > hi) fail(CACG_EINVAL, "Numeric index is out of bounds");
+}
+
+std::vector<std::string> split_words(const std::string &line) {
+  std::vector<std::string> w;
+  std::istringstream is(line);
+  std::string t;
+  while (is >> t) w.push_back(t);
+  return w;
+}
+
+void shape8(double px, double py, double pz, double *N) {
+  // element.cpp:1340-1347, evaluated left to right
+  N[0] = 0.125 * (1 - px) * (1 - py) * (1 - pz);
+  N[1] = 0.125 * (1 + px) * (1 - py) * (1 - pz);
+  N[2] = 0.125 * (1 + px) * (1 + py) * (1 - pz);
+  N[3] = 0.125 * (1 - px) * (1 + py) * (1 - pz);
+  N[4] = 0.125 * (1 - px) * (1 - py) * (1 + pz);
+  N[5] = 0.125 * (1 + px) * (1 - py) * (1 + pz);
+  N[6] = 0.125 * (1 + px) * (1 + py) * (1 + pz);
+  N[7] = 0.125 * (1 - px) * (1 + py) * (1 + pz);
+}
+
+template <class T>
+void upload(DBuf<T> &b, const std::vector<T> &h, cudaStream_t s) {
+  b.ensure(h.size() > 0 ? h.size() : 1, s);
+  if (!h.empty())
+    check(cudaMemcpyAsync(b.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s),
+          "upload");
+}
+
+}  // namespace
+
+struct LJTabHost {
+  double lj1[(MAXT + 1) * (MAXT + 1)];
+  double lj2[(MAXT + 1) * (MAXT + 1)];
+  double cutsq[(MAXT + 1) * (MAXT + 1)];
+};
+
+struct cacg_context {
+  std::string err;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+
+  // units (update.cpp:83-132)
+  double ftm2v = 1.0, dt = 0.005, skin = 0.3;
+  bool metal = false;
+  // neighbor settings (neighbor.cpp:45-55 defaults)
+  int every = 1, delay = 10, dist_check = 1, oneatom = 2000, pgsize = 100000;
+  double binsize_user = 0.0;
+  int nsplit = 2;
+  int mode = CACG_FP64_EXACT;
+  bool fix_nve = false;
+
+  // box
+  double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0}, prd[3] = {0, 0, 0};
+  int periodic[3] = {1, 1, 1};
+  bool box_set = false;
+
+  // atoms (host staging until init)
+  int ntypes = 0;
+  double amass[MAXT + 1] = {};
+  std::vector<double> h_x, h_v;
+  std::vector<int> h_type, h_tag;
+  int nlocal = 0, nghost = 0;
+
+  // element types
+  int netypes = 0;
+  int nae[MAXT + 1][3] = {};
+  int numint[MAXT + 1] = {};
+  std::vector<int> intp[MAXT + 1];
+  std::vector<double> weight[MAXT + 1];
+  double emass[MAXT + 1] = {};
+  std::vector<double> h_ex, h_nodex, h_nodev;
+  std::vector<int> h_etype, h_etag;
+  int enlocal = 0, enghost = 0;
+
+  // pair
+  int pair_style = 0;  // 1 lj/cut, 2 eam
+  double cut_global = 0.0;
+  double eps[MAXT + 1][MAXT + 1] = {}, sig[MAXT + 1][MAXT + 1] = {}, cutp[MAXT + 1][MAXT + 1] = {};
+  int setflag[MAXT + 1][MAXT + 1] = {};
+  LJTabHost ljtab;
+  // eam
+  int nr = 0, nrho = 0;
+  double dr = 0, drho = 0, rdr = 0, rdrho = 0, cutforcesq = 0, eam_mass = 0, eam_cut = 0;
+  std::vector<double> frho_sp, rhor_sp, z2r_sp;
+
+  // derived cutoffs
+  double cutneighmax = 0, cutneighmaxsq = 0, triggersq = 0;
+  double esize[MAXT + 1] = {}, max_size = 0.0;
+  double cut_all = 0, cut_allsq = 0, cut_ele = 0, cut_elesq = 0, cut_subele = 0, cut_subelesq = 0;
+  double cutghost[3] = {}, cutghostmulti[MAXT + 1] = {};
+  std::vector<SwapDef> swaps;
+  BinGeom bins{};
+  std::vector<int> stencil;
+
+  // element tables (host)
+  int nsub = 0;
+  std::vector<int> int_off, inter_off, inter_num, numint_v, node_list, sub_first, list_isub;
+  std::vector<double> spa_int, w_all, spa_inter, spa_csub, spa_isub;
+  std::vector<int> h_site_base, h_row_first, h_eroot;
+  int nrows = 0, nsites = 0;
+
+  // device arrays: atoms
+  DBuf<double4> d_x;
+  DBuf<double> d_v, d_f, d_xhold, d_rho, d_fp, d_mass;
+  DBuf<int> d_type, d_tag, d_root, d_send;
+  DBuf<int> d_abin, d_bcount, d_bstart, d_bmem, d_stencil;
+  DBuf<double4> d_bx;
+  DBuf<int> d_num, d_list;
+  int maxneigh = 64, stride = 0;
+  // elements
+  DBuf<double> d_ex, d_nodex, d_nodev, d_nodef, d_nodexhold, d_erho, d_emass, d_diag, d_fip,
+      d_site_fp;
+  DBuf<int> d_etype, d_etag, d_eroot, d_esend;
+  DBuf<int> d_ebin, d_ebcount, d_ebstart, d_ebmem;
+  DBuf<double4> d_ebx, d_site_x, d_subc;
+  DBuf<int> d_enum, d_elist;
+  int maxeneigh = 32, estride = 0;
+  DBuf<int> d_row_elem, d_row_jj, d_row_first, d_site_base, d_ipnum, d_ipent;
+  int maxip = 128, rowstride = 0;
+  // tables
+  DBuf<double> d_spa_int, d_weight, d_spa_inter, d_spa_csub, d_spa_isub, d_frho, d_rhor, d_z2r;
+  DBuf<int> d_int_off, d_inter_off, d_numint, d_inter_num, d_node_list, d_list_isub,
+      d_sub_first;
+  DBuf<LJTabHost> d_ljtab;
+  // scratch
+  DBuf<int> d_flags, d_pos, d_scan, d_misc;
+  int *h_pin = nullptr;  // pinned readback slots
+
+  // state
+  bool inited = false, setup_done = false, list_built = false, elists_built = false;
+  long long ntimestep = 0, launches = 0;
+  int ago = 0, nrebuild = 0;
+  cudaEvent_t ev[10] = {};
+  double t_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  bool timing = false;
+  std::vector<cudaEvent_t> pev;  // per-step phase events
+  void mark(size_t k) {
+    if (!timing) return;
+    while (pev.size() <= k) {
+      cudaEvent_t e;
+      check(cudaEventCreate(&e), "event");
+      pev.push_back(e);
+    }
+    check(cudaEventRecord(pev[k], stream), "event record");
+  }
+
+  ~cacg_context();
+
+  // ---- helpers ----
+  void sync() { check(cudaStreamSynchronize(stream), "sync"); }
+  ElemTables etab() const {
+    ElemTables t;
+    t.spa_int = d_spa_int.p;
+    t.weight = d_weight.p;
+    t.spa_inter = d_spa_inter.p;
+    t.int_off = d_int_off.p;
+    t.inter_off = d_inter_off.p;
+    t.numint = d_numint.p;
+    t.inter_num = d_inter_num.p;
+    t.node_list = d_node_list.p;
+    t.spa_center_sub = d_spa_csub.p;
+    t.spa_inter_sub = d_spa_isub.p;
+    t.list_inter_sub = d_list_isub.p;
+    t.sub_first = d_sub_first.p;
+    t.nsub = nsub;
+    return t;
+  }
+  EamTables eamtab() const {
+    EamTables e;
+    e.frho = d_frho.p;
+    e.rhor = d_rhor.p;
+    e.z2r = d_z2r.p;
+    e.nr = nr;
+    e.nrho = nrho;
+    e.rdr = rdr;
+    e.rdrho = rdrho;
+    e.cutforcesq = cutforcesq;
+    return e;
+  }
+
+  // ---- commands ----
+  void command(const std::string &line);
+  void read_data(const std::string &path);
+  void read_eam(const std::string &path);
+  void set_units(const std::string &style);
+
+  // ---- path ----
+  void init();
+  void element_tables();
+  void element_size();
+  void setup_cut();
+  void comm_setup();
+  void setup_bins();
+  void borders();
+  void forward_comm();
+  void pbc();
+  void neighbor_build();
+  void neighbor_ebuild();
+  void neighbor_nbuild();
+  void pair_compute();
+  void pair_compute_pass(int pass);
+  void pair_ecompute();
+  void nve_initial();
+  void nve_final();
+  int decide();
+  void rebuild();
+  void run(int n);
+  void setup();
+  void require_init() {
+    if (!inited) init();
+  }
+};
+
+cacg_context::~cacg_context() {
+  DBuf<double4> *b4[] = {&d_x, &d_bx, &d_ebx, &d_site_x, &d_subc};
+  for (auto *b : b4) b->release();
+  DBuf<double> *bd[] = {&d_v, &d_f, &d_xhold, &d_rho, &d_fp, &d_mass, &d_ex, &d_nodex, &d_nodev,
+                        &d_nodef, &d_nodexhold, &d_erho, &d_emass, &d_diag, &d_fip, &d_site_fp,
+                        &d_spa_int, &d_weight, &d_spa_inter, &d_spa_csub, &d_spa_isub, &d_frho,
+                        &d_rhor, &d_z2r};
+  for (auto *b : bd) b->release();
+  DBuf<int> *bi[] = {&d_type, &d_tag, &d_root, &d_send, &d_abin, &d_bcount, &d_bstart, &d_bmem,
+                     &d_stencil, &d_num, &d_list, &d_etype, &d_etag, &d_eroot, &d_esend,
+                     &d_ebin, &d_ebcount, &d_ebstart, &d_ebmem, &d_enum, &d_elist,
+                     &d_row_elem, &d_row_jj, &d_row_first, &d_site_base, &d_ipnum, &d_ipent,
+                     &d_int_off, &d_inter_off, &d_numint, &d_inter_num, &d_node_list,
+                     &d_list_isub, &d_sub_first, &d_flags, &d_pos, &d_scan, &d_misc};
+  for (auto *b : bi) b->release();
+  d_ljtab.release();
+  for (auto &e : ev)
+    if (e) cudaEventDestroy(e);
+  for (auto &e : pev) cudaEventDestroy(e);
+  if (h_pin) cudaFreeHost(h_pin);
+  if (stream) cudaStreamDestroy(stream);
+}
+
+// ------------------------------------------------------------------ commands
+
+void cacg_context::set_units(const std::string &style) {
+  if (style == "lj") {
+    metal = false;
+    ftm2v = 1.0;
+    dt = 0.005;
+    skin = 0.3;
+  } else if (style == "metal") {
+    metal = true;
+    ftm2v = 1.0 / 1.0364269e-4;
+    dt = 0.001;
+    skin = 2.0;
+  } else {
+    fail(CACG_EINVAL, "Illegal units command");
+  }
+}
+
+void cacg_context::command(const std::string &raw) {
+  std::string line = raw;
+  size_t hash = line.find('#');
+  if (hash != std::string::npos) line = line.substr(0, hash);
+  auto w = split_words(line);
+  if (w.empty()) return;
+  const std::string &c = w[0];
+  std::vector<std::string> a(w.begin() + 1, w.end());
+  if (c == "units") {
+    if (a.size() != 1) fail(CACG_EINVAL, "Illegal units command");
+    if (box_set) fail(CACG_EINVAL, "Units command after simulation box is defined");
+    set_units(a[0]);
+  } else if (c == "dimension") {
+    if (a.size() != 1 || a[0] != "3") fail(CACG_EINVAL, "Only 3d CAC is supported");
+  } else if (c == "atom_style") {
+    if (a.empty() || a[0] != "atomic") fail(CACG_EINVAL, "Only atom_style atomic is supported");
+  } else if (c == "newton" || c == "processors") {
+    // single GPU: no processor grid; newton flag unused by the full lists
+  } else if (c == "boundary") {
+    if (a.size() != 3) fail(CACG_EINVAL, "Illegal boundary command");
+    for (int d = 0; d < 3; d++) {
+      char c0 = a[d][0], c1 = a[d].size() == 1 ? a[d][0] : a[d][1];
+      if (!strchr("pfsm", c0) || !strchr("pfsm", c1)) fail(CACG_EINVAL, "Illegal boundary command");
+      if ((c0 == 'p') != (c1 == 'p')) fail(CACG_EINVAL, "Both sides of boundary must be periodic");
+      if (c0 == 's' || c0 == 'm' || c1 == 's' || c1 == 'm')
+        fail(CACG_EINVAL, "Shrink-wrapped boundaries are not supported");
+      periodic[d] = c0 == 'p';
+    }
+  } else if (c == "timestep") {
+    if (a.size() != 1) fail(CACG_EINVAL, "Illegal timestep command");
+    dt = numeric(a[0]);
+  } else if (c == "elementsplit") {
+    if (a.size() != 1) fail(CACG_EINVAL, "Illegal element_split command");
+    nsplit = inumeric(a[0]);
+    if (nsplit < 1) fail(CACG_EINVAL, "Illegal element_split command");
+  } else if (c == "neighbor") {
+    if (a.size() != 2) fail(CACG_EINVAL, "Illegal neighbor command");
+    skin = numeric(a[0]);
+    if (skin < 0.0) fail(CACG_EINVAL, "Illegal neighbor command");
+    if (a[1] != "bin") fail(CACG_EINVAL, "Only neighbor style bin is supported");
+  } else if (c == "neigh_modify") {
+    size_t i = 0;
+    while (i < a.size()) {
+      if (i + 1 >= a.size()) fail(CACG_EINVAL, "Illegal neigh_modify command");
+      const std::string &k = a[i], &v = a[i + 1];
+      if (k == "every") {
+        every = inumeric(v);
+        if (every <= 0) fail(CACG_EINVAL, "Illegal neigh_modify command");
+      } else if (k == "delay") {
+        delay = inumeric(v);
+        if (delay < 0) fail(CACG_EINVAL, "Illegal neigh_modify command");
+      } else if (k == "check") {
+        if (v == "yes") dist_check = 1;
+        else if (v == "no") dist_check = 0;
+        else fail(CACG_EINVAL, "Illegal neigh_modify command");
+      } else if (k == "binsize") {
+        binsize_user = numeric(v);
+        if (binsize_user <= 0.0) binsize_user = 0.0;
+      } else if (k == "one") {
+        oneatom = inumeric(v);
+      } else if (k == "page") {
+        pgsize = inumeric(v);
+      } else {
+        fail(CACG_EINVAL, "Illegal neigh_modify command");
+      }
+      i += 2;
+    }
+  } else if (c == "read_data") {
+    if (a.size() < 1) fail(CACG_EINVAL, "Illegal read_data command");
+    read_data(a[0]);
+  } else if (c == "pair_style") {
+    if (a.empty()) fail(CACG_EINVAL, "Illegal pair_style command");
+    if (a[0] == "lj/cut") {
+      if (a.size() != 2) fail(CACG_EINVAL, "Illegal pair_style command");
+      pair_style = 1;
+      cut_global = numeric(a[1]);
+    } else if (a[0] == "eam") {
+      if (a.size() != 1) fail(CACG_EINVAL, "Illegal pair_style command");
+      pair_style = 2;
+    } else {
+      fail(CACG_EINVAL, "Unknown pair style %s", a[0].c_str());
+    }
+    inited = false;
+  } else if (c == "pair_coeff") {
+    if (!box_set) fail(CACG_EINVAL, "Pair_coeff command before simulation box is defined");
+    if (pair_style == 0) fail(CACG_EINVAL, "Pair_coeff command before pair_style is defined");
+    int ilo, ihi, jlo, jhi;
+    int nt = ntypes > 0 ? ntypes : 1;
+    if (pair_style == 1) {
+      if (a.size() < 4 || a.size() > 5) fail(CACG_EINVAL, "Incorrect args for pair coefficients");
+      bounds(a[0], nt, ilo, ihi);
+      bounds(a[1], nt, jlo, jhi);
+      double e = numeric(a[2]), s = numeric(a[3]);
+      double cc = a.size() == 5 ? numeric(a[4]) : cut_global;
+      int count = 0;
+      for (int i = ilo; i <= ihi; i++)
+        for (int j = std::max(jlo, i); j <= jhi; j++) {
+          eps[i][j] = e;
+          sig[i][j] = s;
+          cutp[i][j] = cc;
+          setflag[i][j] = 1;
+          count++;
+        }
+      if (count == 0) fail(CACG_EINVAL, "Incorrect args for pair coefficients");
+    } else {
+      if (a.size() != 3) fail(CACG_EINVAL, "Incorrect args for pair coefficients");
+      bounds(a[0], nt, ilo, ihi);
+      bounds(a[1], nt, jlo, jhi);
+      read_eam(a[2]);
+      int count = 0;
+      for (int i = ilo; i <= ihi; i++)
+        for (int j = std::max(jlo, i); j <= jhi; j++)
+          if (i == j) {
+            setflag[i][i] = 1;
+            amass[i] = eam_mass;  // PairEAM::coeff sets the type mass (pair_eam.cpp:152-161)
+            count++;
+          }
+      if (count == 0) fail(CACG_EINVAL, "Incorrect args for pair coefficients");
+    }
+    inited = false;
+  } else if (c == "fix") {
+    if (a.size() < 3) fail(CACG_EINVAL, "Illegal fix command");
+    if (a[2] != "nve") fail(CACG_EINVAL, "Only fix nve is on this path");
+    if (a[1] != "all") fail(CACG_EINVAL, "fix nve applies to group all here");
+    fix_nve = true;
+  } else if (c == "run") {
+    if (a.size() < 1) fail(CACG_EINVAL, "Illegal run command");
+    run(inumeric(a[0]));
+  } else if (c == "thermo" || c == "thermo_style" || c == "dump" || c == "velocity" ||
+             c == "region" || c == "group") {
+    // output and setup commands outside this path are accepted and ignored
+  } else {
+    fail(CACG_EINVAL, "Unknown command: %s", raw.c_str());
+  }
+}
+
+// ------------------------------------------------------------------ read_data
+
+namespace {
+
+void remap(double *x, const double *lo, const double *hi, const double *prd, const int *per) {
+  // Domain::remap, domain.cpp:389-476
+  for (int d = 0; d < 3; d++) {
+    if (!per[d]) continue;
+    while (x[d] < lo[d]) x[d] += prd[d];
+    while (x[d] >= hi[d]) x[d] -= prd[d];
+    x[d] = std::max(x[d], lo[d]);
+  }
+}
+
+bool blank(const std::string &s) { return s.find_first_not_of(" \t\r\n") == std::string::npos; }
+
+std::string trim(const std::string &s) {
+  size_t a = s.find_first_not_of(" \t\r\n");
+  if (a == std::string::npos) return "";
+  size_t b = s.find_last_not_of(" \t\r\n");
+  return s.substr(a, b - a + 1);
+}
+
+}  // namespace
+
+void cacg_context::read_data(const std::string &path) {
+  std::ifstream in(path);
+  if (!in) fail(CACG_EIO, "Cannot open file %s", path.c_str());
+  std::string line;
+  std::getline(in, line);  // first line skipped
+  long long natoms = 0, nelem = 0;
+  int nat = 0, net = 0;
+  double blo[3] = {0, 0, 0}, bhi[3] = {0, 0, 0};
+  std::string keyword;
+  // header (read_data.cpp:277-367)
+  while (std::getline(in, line)) {
+    std::string l = line;
+    size_t hash = l.find('#');
+    if (hash != std::string::npos) l = l.substr(0, hash);
+    if (blank(l)) continue;
+    if (l.find("atoms") != std::string::npos) natoms = atoll(l.c_str());
+    else if (l.find("elements") != std::string::npos) nelem = atoll(l.c_str());
+    else if (l.find("xlo xhi") != std::string::npos) sscanf(l.c_str(), "%lg %lg", &blo[0], &bhi[0]);
+    else if (l.find("ylo yhi") != std::string::npos) sscanf(l.c_str(), "%lg %lg", &blo[1], &bhi[1]);
+    else if (l.find("zlo zhi") != std::string::npos) sscanf(l.c_str(), "%lg %lg", &blo[2], &bhi[2]);
+    else if (l.find("atom types") != std::string::npos) nat = atoi(l.c_str());
+    else if (l.find("element types") != std::string::npos) net = atoi(l.c_str());
+    else {
+      keyword = trim(l);
+      break;
+    }
+  }
+  if (nat < 1 || nat > MAXT) fail(CACG_EINVAL, "unsupported number of atom types %d", nat);
+  if (net > MAXT) fail(CACG_EINVAL, "unsupported number of element types %d", net);
+  for (int d = 0; d < 3; d++) {
+    if (!(blo[d] < bhi[d])) fail(CACG_EINVAL, "Box bounds are invalid");
+    lo[d] = blo[d];
+    hi[d] = bhi[d];
+    prd[d] = hi[d] - lo[d];
+  }
+  box_set = true;
+  ntypes = nat;
+  netypes = net;
+  h_x.clear(); h_v.clear(); h_type.clear(); h_tag.clear();
+  h_ex.clear(); h_nodex.clear(); h_nodev.clear(); h_etype.clear(); h_etag.clear();
+  std::vector<int> eid_to_index;
+  auto next_lines = [&](long long n, std::vector<std::string> &out) {
+    out.clear();
+    // one blank line follows the keyword (parse_keyword reads it)
+    std::getline(in, line);
+    while ((long long) out.size() < n) {
+      if (!std::getline(in, line)) fail(CACG_EIO, "Unexpected end of data file");
+      out.push_back(line);
+    }
+  };
+  std::vector<std::string> rows;
+  while (!keyword.empty()) {
+    if (keyword == "Masses") {
+      next_lines(nat, rows);
+      for (auto &r : rows) {
+        int t;
+        double m;
+        if (sscanf(r.c_str(), "%d %lg", &t, &m) != 2 || t < 1 || t > nat)
+          fail(CACG_EINVAL, "Invalid type for mass set");
+        if (m <= 0.0) fail(CACG_EINVAL, "Invalid mass value");
+        amass[t] = m;
+      }
+    } else if (keyword == "NAAE") {
+      next_lines(net, rows);
+      for (auto &r : rows) {
+        int t, nx, ny, nz;
+        if (sscanf(r.c_str(), "%d %d %d %d", &t, &nx, &ny, &nz) != 4)
+          fail(CACG_EINVAL, "Invalid nae line in data file");
+        if (t < 1 || t > net) fail(CACG_EINVAL, "Invalid type for nae set");
+        if (nx < 2 || ny < 2 || nz < 2) fail(CACG_EINVAL, "Invalid naae values");
+        nae[t][0] = nx;
+        nae[t][1] = ny;
+        nae[t][2] = nz;
+      }
+    } else if (keyword == "Numint") {
+      next_lines(net, rows);
+      for (auto &r : rows) {
+        int t, n;
+        if (sscanf(r.c_str(), "%d %d", &t, &n) != 2) fail(CACG_EINVAL, "Invalid numint line in data file");
+        if (t < 1 || t > net) fail(CACG_EINVAL, "Invalid type for numint set");
+        numint[t] = n;
+        intp[t].assign(3 * (size_t) n, 0);
+        weight[t].assign((size_t) n, 0.0);
+      }
+    } else if (keyword == "Intp") {
+      long long tot = 0;
+      for (int t = 1; t <= net; t++) tot += numint[t];
+      next_lines(tot, rows);
+      for (auto &r : rows) {
+        auto w = split_words(r);
+        if (w.size() < 6) fail(CACG_EINVAL, "Invalid Intp line in data file");
+        int t = atoi(w[0].c_str()), m = atoi(w[1].c_str()) - 1;
+        if (t < 1 || t > net || m < 0 || m >= numint[t]) fail(CACG_EINVAL, "Invalid Intp index");
+        intp[t][3 * m] = atoi(w[2].c_str());
+        intp[t][3 * m + 1] = atoi(w[3].c_str());
+        intp[t][3 * m + 2] = atoi(w[4].c_str());
+        weight[t][m] = atof(w[5].c_str());
+      }
+    } else if (keyword == "Atoms") {
+      next_lines(natoms, rows);
+      for (auto &r : rows) {
+        auto w = split_words(r);
+        if (w.size() != 5 && w.size() != 8) fail(CACG_EINVAL, "Incorrect atom format in data file");
+        double x[3] = {atof(w[2].c_str()), atof(w[3].c_str()), atof(w[4].c_str())};
+        remap(x, lo, hi, prd, periodic);
+        int t = atoi(w[1].c_str());
+        if (t < 1 || t > nat) fail(CACG_EINVAL, "Invalid atom type in Atoms section of data file");
+        bool inside = true;
+        for (int d = 0; d < 3; d++) {
+          double l = lo[d], h = hi[d];
+          if (periodic[d]) {
+            l -= prd[d] * 1.0e-6;
+            h += prd[d] * 1.0e-6;
+          }
+          inside = inside && x[d] >= l && x[d] < h;
+        }
+        if (!inside) fail(CACG_EINVAL, "Did not assign all atoms correctly");
+        h_tag.push_back(atoi(w[0].c_str()));
+        h_type.push_back(t);
+        for (int d = 0; d < 3; d++) {
+          h_x.push_back(x[d]);
+          h_v.push_back(0.0);
+        }
+      }
+    } else if (keyword == "Elements") {
+      next_lines(nelem, rows);
+      for (auto &r : rows) {
+        auto w = split_words(r);
+        if (w.size() != 5 && w.size() != 8) fail(CACG_EINVAL, "Incorrect element format in data file");
+        double x[3] = {atof(w[2].c_str()), atof(w[3].c_str()), atof(w[4].c_str())};
+        remap(x, lo, hi, prd, periodic);
+        int t = atoi(w[1].c_str());
+        if (t < 1 || t > net) fail(CACG_EINVAL, "Invalid atom type in Elements section of data file");
+        int id = atoi(w[0].c_str());
+        if (id >= (int) eid_to_index.size()) eid_to_index.resize(id + 1, -1);
+        eid_to_index[id] = (int) h_etype.size();
+        h_etag.push_back(id);
+        h_etype.push_back(t);
+        for (int d = 0; d < 3; d++) h_ex.push_back(x[d]);
+      }
+      h_nodex.assign(24 * h_etype.size(), 0.0);
+      h_nodev.assign(24 * h_etype.size(), 0.0);
+    } else if (keyword == "Nodes") {
+      next_lines(nelem * NPE, rows);
+      for (auto &r : rows) {
+        auto w = split_words(r);
+        if (w.size() != 6 && w.size() != 9) fail(CACG_EINVAL, "Incorrect node format in data file");
+        int id = atoi(w[0].c_str()), k = atoi(w[1].c_str()) - 1;
+        if (id < 0 || id >= (int) eid_to_index.size() || eid_to_index[id] < 0 || k < 0 || k >= NPE)
+          fail(CACG_EINVAL, "Invalid node line in data file");
+        int e = eid_to_index[id];
+        for (int d = 0; d < 3; d++) h_nodex[24 * e + 3 * k + d] = atof(w[2 + d].c_str());
+        if (w.size() == 9)
+          for (int d = 0; d < 3; d++) h_nodev[24 * e + 3 * k + d] = atof(w[5 + d].c_str());
+      }
+    } else {
+      fail(CACG_EINVAL, "Unknown identifier in data file: %s", keyword.c_str());
+    }
+    keyword.clear();
+    while (std::getline(in, line)) {
+      if (!blank(line) && line.find_first_not_of(" \t") != std::string::npos &&
+          line[line.find_first_not_of(" \t")] != '#') {
+        keyword = trim(line.substr(0, line.find('#')));
+        break;
+      }
+    }
+  }
+  if ((long long) h_type.size() != natoms) fail(CACG_EINVAL, "Did not assign all atoms correctly");
+  if ((long long) h_etype.size() != nelem) fail(CACG_EINVAL, "Did not assign all elements correctly");
+  nlocal = (int) h_type.size();
+  enlocal = (int) h_etype.size();
+  inited = setup_done = list_built = elists_built = false;
+}
+
+// PairEAM::read_file + file2array + array2spline (pair_eam.cpp:197-580)
+void cacg_context::read_eam(const std::string &path) {
+  FILE *fp = fopen(path.c_str(), "r");
+  if (!fp) fail(CACG_EIO, "Cannot open EAM potential file %s", path.c_str());
+  char buf[1024];
+  int tmp, nrho_f, nr_f;
+  double mass, drho_f, dr_f, cut;
+  if (!fgets(buf, sizeof(buf), fp) || !fgets(buf, sizeof(buf), fp)) {
+    fclose(fp);
+    fail(CACG_EIO, "EAM file truncated");
+  }
+  sscanf(buf, "%d %lg", &tmp, &mass);
+  if (!fgets(buf, sizeof(buf), fp)) {
+    fclose(fp);
+    fail(CACG_EIO, "EAM file truncated");
+  }
+  sscanf(buf, "%d %lg %d %lg %lg", &nrho_f, &drho_f, &nr_f, &dr_f, &cut);
+  if (nrho_f < 5 || nr_f < 5) {
+    fclose(fp);
+    fail(CACG_EINVAL, "EAM tables too short");
+  }
+  auto grab = [&](int n, std::vector<double> &v) {
+    v.assign((size_t) n + 1, 0.0);
+    int i = 0;
+    while (i < n) {
+      if (!fgets(buf, sizeof(buf), fp)) return false;
+      char *p = strtok(buf, " \t\n\r\f");
+      if (!p) continue;
+      v[1 + i++] = atof(p);
+      while ((p = strtok(nullptr, " \t\n\r\f")) && i < n) v[1 + i++] = atof(p);
+    }
+    return true;
+  };
+  std::vector<double> F, R, Z;
+  bool ok = grab(nrho_f, F) && grab(nr_f, R) && grab(nr_f, Z);
+  fclose(fp);
+  if (!ok) fail(CACG_EIO, "EAM file truncated");
+  eam_mass = mass;
+  eam_cut = cut;
+  dr = dr_f;
+  drho = drho_f;
+  double rmax = (nr_f - 1) * dr_f, rhomax = (nrho_f - 1) * drho_f;
+  nr = (int) (rmax / dr + 0.5);
+  nrho = (int) (rhomax / drho + 0.5);
+  const double sixth = 1.0 / 6.0;
+  auto regrid = [&](int n, double delta, int nfile, double dfile, const std::vector<double> &src) {
+    std::vector<double> dst((size_t) n + 1, 0.0);
+    for (int m = 1; m <= n; m++) {
+      double r = (m - 1) * delta;
+      double p = r / dfile + 1.0;
+      int k = (int) p;
+      k = std::min(k, nfile - 2);
+      k = std::max(k, 2);
+      p -= k;
+      p = std::min(p, 2.0);
+      double cof1 = -sixth * p * (p - 1.0) * (p - 2.0);
+      double cof2 = 0.5 * (p * p - 1.0) * (p - 2.0);
+      double cof3 = -0.5 * p * (p + 1.0) * (p - 2.0);
+      double cof4 = sixth * p * (p * p - 1.0);
+      dst[m] = cof1 * src[k - 1] + cof2 * src[k] + cof3 * src[k + 1] + cof4 * src[k + 2];
+    }
+    return dst;
+  };
+  auto interpolate = [](int n, double delta, const std::vector<double> &f) {
+    std::vector<double> sp((size_t) (n + 1) * 7, 0.0);
+    auto S = [&](int m, int k) -> double & { return sp[(size_t) m * 7 + k]; };
+    for (int m = 1; m <= n; m++) S(m, 6) = f[m];
+    S(1, 5) = S(2, 6) - S(1, 6);
+    S(2, 5) = 0.5 * (S(3, 6) - S(1, 6));
+    S(n - 1, 5) = 0.5 * (S(n, 6) - S(n - 2, 6));
+    S(n, 5) = S(n, 6) - S(n - 1, 6);
+    for (int m = 3; m <= n - 2; m++)
+      S(m, 5) = ((S(m - 2, 6) - S(m + 2, 6)) + 8.0 * (S(m + 1, 6) - S(m - 1, 6))) / 12.0;
+    for (int m = 1; m <= n - 1; m++) {
+      S(m, 4) = 3.0 * (S(m + 1, 6) - S(m, 6)) - 2.0 * S(m, 5) - S(m + 1, 5);
+      S(m, 3) = S(m, 5) + S(m + 1, 5) - 2.0 * (S(m + 1, 6) - S(m, 6));
+    }
+    S(n, 4) = 0.0;
+    S(n, 3) = 0.0;
+    for (int m = 1; m <= n; m++) {
+      S(m, 2) = S(m, 5) / delta;
+      S(m, 1) = 2.0 * S(m, 4) / delta;
+      S(m, 0) = 3.0 * S(m, 3) / delta;
+    }
+    return sp;
+  };
+  auto frho = regrid(nrho, drho, nrho_f, drho_f, F);
+  auto rhor = regrid(nr, dr, nr_f, dr_f, R);
+  auto z2r = regrid(nr, dr, nr_f, dr_f, Z);
+  rdr = 1.0 / dr;
+  rdrho = 1.0 / drho;
+  frho_sp = interpolate(nrho, drho, frho);
+  rhor_sp = interpolate(nr, dr, rhor);
+  z2r_sp = interpolate(nr, dr, z2r);
+  cutforcesq = cut * cut;
+}
+
+// ------------------------------------------------------------------ init
+
+// Element tables: inter_ele/shape_array_inter_ele (element.cpp:1361-1423),
+// intp_pcoord/shape_array_int (1170-1191, 1326-1354), sub-elements (725-906),
+// find_node_list (1296-1319).
+void cacg_context::element_tables() {
+  int_off.assign(MAXT + 1, 0);
+  inter_off.assign(MAXT + 1, 0);
+  inter_num.assign(MAXT + 1, 0);
+  numint_v.assign(MAXT + 1, 0);
+  node_list.assign((MAXT + 1) * NPE, 0);
+  spa_int.clear();
+  w_all.clear();
+  spa_inter.clear();
+  int ioff = 0, roff = 0;
+  std::vector<std::vector<double>> pcs(MAXT + 1);
+  for (int t = 1; t <= netypes; t++) {
+    int nx = nae[t][0], ny = nae[t][1], nz = nae[t][2];
+    inter_num[t] = nx * ny * nz;
+    inter_off[t] = roff;
+    double inx = 2 / ((double) nx - 1), iny = 2 / ((double) ny - 1), inz = 2 / ((double) nz - 1);
+    double N[8];
+    for (int ii = 0; ii < nx; ii++)
+      for (int jj = 0; jj < ny; jj++)
+        for (int kk = 0; kk < nz; kk++) {
+          double px = inx * (double) ii - 1, py = iny * (double) jj - 1, pz = inz * (double) kk - 1;
+          pcs[t].push_back(px);
+          pcs[t].push_back(py);
+          pcs[t].push_back(pz);
+          shape8(px, py, pz, N);
+          spa_inter.insert(spa_inter.end(), N, N + 8);
+        }
+    roff += inter_num[t];
+    numint_v[t] = numint[t];
+    int_off[t] = ioff;
+    double dx = 2 / ((double) nx - 1), dy = 2 / ((double) ny - 1), dz = 2 / ((double) nz - 1);
+    for (int m = 0; m < numint[t]; m++) {
+      double px = dx * ((double) intp[t][3 * m]) - 1;
+      double py = dy * ((double) intp[t][3 * m + 1]) - 1;
+      double pz = dz * ((double) intp[t][3 * m + 2]) - 1;
+      shape8(px, py, pz, N);
+      spa_int.insert(spa_int.end(), N, N + 8);
+      w_all.push_back(weight[t][m]);
+    }
+    ioff += numint[t];
+    if (pair_style == 2) {
+      for (int q = 0; q < NPE; q++) {
+        int kk;
+        for (kk = 0; kk < numint[t]; kk++)
+          if (std::fabs(spa_int[(size_t) (int_off[t] + kk) * NPE + q] - 1.0) < 0.01) {
+            node_list[t * NPE + q] = kk;
+            break;
+          }
+        if (kk == numint[t]) fail(CACG_EINVAL, "didn't contain all node integration point");
+      }
+    }
+  }
+  // sub-elements: type-1 geometry (element.cpp:786-787, 835-836)
+  int ns = nsplit;
+  nsub = ns * ns * ns;
+  double ls = 2.0 / ns;
+  std::vector<double> pc((size_t) nsub * NPE * 3);
+  auto PC = [&](int i, int l, int d) -> double & { return pc[((size_t) i * NPE + l) * 3 + d]; };
+  const double c0[8][3] = {{-1.0, -1.0, -1.0}, {ls - 1.0, -1.0, -1.0}, {ls - 1.0, ls - 1.0, -1.0},
+                           {-1.0, ls - 1.0, -1.0}, {-1.0, -1.0, ls - 1.0}, {ls - 1.0, -1.0, ls - 1.0},
+                           {ls - 1.0, ls - 1.0, ls - 1.0}, {-1.0, ls - 1.0, ls - 1.0}};
+  for (int l = 0; l < NPE; l++)
+    for (int d = 0; d < 3; d++) PC(0, l, d) = c0[l][d];
+  int in = 0;
+  for (int ii = 0; ii < ns; ii++)
+    for (int jj = 0; jj < ns; jj++)
+      for (int kk = 0; kk < ns; kk++) {
+        if (ii == 0 && jj == 0 && kk == 0) continue;
+        in++;
+        for (int l = 0; l < NPE; l++) {
+          PC(in, l, 0) = PC(0, l, 0) + ii * ls;
+          PC(in, l, 1) = PC(0, l, 1) + jj * ls;
+          PC(in, l, 2) = PC(0, l, 2) + kk * ls;
+        }
+      }
+  spa_csub.assign((size_t) nsub * NPE, 0.0);
+  sub_first.assign((size_t) nsub + 1, 0);
+  list_isub.clear();
+  spa_isub.clear();
+  const std::vector<double> &pinter = pcs[1];
+  int ninter = inter_num[1];
+  for (int i = 0; i < nsub; i++) {
+    double c[3] = {0.0, 0.0, 0.0};
+    for (int l = 0; l < NPE; l++)
+      for (int d = 0; d < 3; d++) c[d] += PC(i, l, d);
+    for (int d = 0; d < 3; d++) c[d] = c[d] / NPE;
+    shape8(c[0], c[1], c[2], &spa_csub[(size_t) i * NPE]);
+    double blo[3] = {PC(i, 0, 0), PC(i, 0, 1), PC(i, 0, 2)};
+    double bhi[3] = {PC(i, 1, 0), PC(i, 3, 1), PC(i, 4, 2)};
+    for (int d = 0; d < 3; d++) {
+      if (blo[d] < -0.99) blo[d] = -1.01;
+      if (bhi[d] > 0.99) bhi[d] = 1.01;
+    }
+    sub_first[i] = (int) list_isub.size();
+    double N[8];
+    for (int j = 0; j < ninter; j++) {
+      const double *p = &pinter[3 * (size_t) j];
+      if (p[0] > blo[0] && p[0] <= bhi[0] && p[1] > blo[1] && p[1] <= bhi[1] && p[2] > blo[2] &&
+          p[2] <= bhi[2]) {
+        shape8(p[0], p[1], p[2], N);
+        spa_isub.insert(spa_isub.end(), N, N + 8);
+        list_isub.push_back(j);
+      }
+    }
+  }
+  sub_first[nsub] = (int) list_isub.size();
+  if ((int) list_isub.size() != ninter)
+    fail(CACG_EINVAL, "sub atom total donot match total atom number");
+  cudaStream_t s = stream;
+  upload(d_spa_int, spa_int, s);
+  upload(d_weight, w_all, s);
+  upload(d_spa_inter, spa_inter, s);
+  upload(d_spa_csub, spa_csub, s);
+  upload(d_spa_isub, spa_isub, s);
+  upload(d_int_off, int_off, s);
+  upload(d_inter_off, inter_off, s);
+  upload(d_numint, numint_v, s);
+  upload(d_inter_num, inter_num, s);
+  upload(d_node_list, node_list, s);
+  upload(d_list_isub, list_isub, s);
+  upload(d_sub_first, sub_first, s);
+}
+
+// Element::element_size (element.cpp:567-625): running maximum of the body
+// diagonals over local elements, per type the value reached at its last
+// element, max_size never decreases.
+void cacg_context::element_size() {
+  if (enlocal == 0) return;
+  d_diag.ensure(enlocal, stream);
+  d_misc.ensure(16, stream);
+  check(cudaMemsetAsync(d_misc.p + 8, 0, sizeof(int), stream), "memset");
+  launch_elem_diag(d_nodex.p, d_ex.p, enlocal, d_diag.p, d_misc.p + 8, stream);
+  launches++;
+  std::vector<double> diag(enlocal);
+  check(cudaMemcpyAsync(diag.data(), d_diag.p, sizeof(double) * enlocal, cudaMemcpyDeviceToHost, stream), "diag");
+  check(cudaMemcpyAsync(h_pin + 8, d_misc.p + 8, sizeof(int), cudaMemcpyDeviceToHost, stream), "bad");
+  std::vector<int> et(enlocal);
+  check(cudaMemcpyAsync(et.data(), d_etype.p, sizeof(int) * enlocal, cudaMemcpyDeviceToHost, stream), "etype");
+  sync();
+  double mx[MAXT + 1] = {};
+  double length = 0.0;
+  for (int i = 0; i < enlocal; i++) {
+    length = std::max(length, diag[i]);
+    mx[et[i]] = length;
+  }
+  for (int t = 1; t <= netypes; t++) {
+    esize[t] = mx[t];
+    max_size = std::max(max_size, esize[t]);
+  }
+  if (h_pin[8]) fail(CACG_EINVAL, "element data has error");
+}
+
+void cacg_context::setup_cut() {
+  // Neighbor::setup_cut, neighbor.cpp:284-293
+  cut_all = cutneighmax + max_size;
+  cut_allsq = cut_all * cut_all;
+  cut_ele = cutneighmax + max_size / 2;
+  cut_elesq = cut_ele * cut_ele;
+  cut_subele = cutneighmax + max_size / (2 * nsplit);
+  cut_subelesq = cut_subele * cut_subele;
+}
+
+// CommBrick::setup for one sub-domain spanning the box (comm_brick.cpp:182-367)
+void cacg_context::comm_setup() {
+  double cut = cutneighmax;
+  for (int d = 0; d < 3; d++) cutghost[d] = cut_all;
+  for (int t = 1; t <= netypes; t++) cutghostmulti[t] = cut + esize[t];
+  int maxneed[3];
+  for (int d = 0; d < 3; d++) {
+    maxneed[d] = (int) (cutghost[d] * 1 / prd[d]) + 1;
+    if (!periodic[d]) maxneed[d] = std::min(maxneed[d], 0);
+  }
+  swaps.clear();
+  for (int dim = 0; dim < 3; dim++)
+    for (int ineed = 0; ineed < 2 * maxneed[dim]; ineed++) {
+      SwapDef w;
+      w.dim = dim;
+      double sublo = lo[dim], subhi = hi[dim];
+      if (ineed % 2 == 0) {
+        w.lo = ineed < 2 ? -1.0e20 : 0.5 * (sublo + subhi);
+        w.hi = sublo + cutghost[dim];
+        for (int t = 1; t <= netypes; t++) {
+          w.mlo[t] = ineed < 2 ? -1.0e20 : 0.5 * (sublo + subhi);
+          w.mhi[t] = sublo + cutghostmulti[t];
+        }
+        w.pbc = 1;
+      } else {
+        w.lo = subhi - cutghost[dim];
+        w.hi = ineed < 2 ? 1.0e20 : 0.5 * (sublo + subhi);
+        for (int t = 1; t <= netypes; t++) {
+          w.mlo[t] = subhi - cutghostmulti[t];
+          w.mhi[t] = ineed < 2 ? 1.0e20 : 0.5 * (sublo + subhi);
+        }
+        w.pbc = -1;
+      }
+      // AtomVecAtomic::pack_border / pack_comm: dx = pbc[d]*prd[d]
+      for (int d = 0; d < 3; d++) w.d[d] = (d == dim ? w.pbc : 0) * prd[d];
+      swaps.push_back(w);
+    }
+}
+
+// Neighbor::setup_bins + stencil_half_bin_3d_no_newton (neighbor.cpp:768-976)
+void cacg_context::setup_bins() {
+  double bsublo[3], bsubhi[3], bbox[3];
+  for (int d = 0; d < 3; d++) {
+    bsublo[d] = lo[d] - cutghost[d] - max_size / 2.0;
+    bsubhi[d] = hi[d] + cutghost[d] + max_size / 2.0;
+    bbox[d] = hi[d] - lo[d];
+  }
+  double binsize_optimal = binsize_user > 0.0 ? binsize_user : 0.5 * cutneighmax;
+  if (binsize_optimal == 0.0) binsize_optimal = bbox[0];
+  double binsizeinv = 1.0 / binsize_optimal;
+  for (int d = 0; d < 3; d++)
+    if (bbox[d] * binsizeinv > 2147483647.0) fail(CACG_EINVAL, "Domain too large for neighbor bins");
+  double binsize[3];
+  for (int d = 0; d < 3; d++) {
+    bins.nbin[d] = (int) (bbox[d] * binsizeinv);
+    if (bins.nbin[d] == 0) bins.nbin[d] = 1;
+    binsize[d] = bbox[d] / bins.nbin[d];
+    bins.bininv[d] = 1.0 / binsize[d];
+    bins.lo[d] = lo[d];
+    bins.hi[d] = hi[d];
+  }
+  for (int d = 0; d < 3; d++)
+    if (binsize_optimal * bins.bininv[d] > 100)
+      fail(CACG_EINVAL, "Cannot use neighbor bins - box size << cutoff");
+  for (int d = 0; d < 3; d++) {
+    double coord = bsublo[d] - 1.0e-6 * bbox[d];
+    int mlo_ = (int) ((coord - lo[d]) * bins.bininv[d]);
+    if (coord < lo[d]) mlo_ = mlo_ - 1;
+    coord = bsubhi[d] + 1.0e-6 * bbox[d];
+    int mhi_ = (int) ((coord - lo[d]) * bins.bininv[d]);
+    mlo_ -= 1;
+    mhi_ += 1;
+    bins.mlo[d] = mlo_;
+    bins.mbin[d] = mhi_ - mlo_ + 1;
+  }
+  long long bb = (long long) bins.mbin[0] * bins.mbin[1] * bins.mbin[2];
+  if (bb > 2147483647LL) fail(CACG_EINVAL, "Too many neighbor bins");
+  bins.mbins = (int) bb;
+  int sx = (int) (cutneighmax * bins.bininv[0]);
+  if (sx * binsize[0] < cutneighmax) sx++;
+  int sy = (int) (cutneighmax * bins.bininv[1]);
+  if (sy * binsize[1] < cutneighmax) sy++;
+  int sz = (int) (cutneighmax * bins.bininv[2]);
+  if (sz * binsize[2] < cutneighmax) sz++;
+  auto bin_distance = [&](int i, int j, int k) {
+    double dx, dy, dz;
+    if (i > 0) dx = (i - 1) * binsize[0];
+    else if (i == 0) dx = 0.0;
+    else dx = (i + 1) * binsize[0];
+    if (j > 0) dy = (j - 1) * binsize[1];
+    else if (j == 0) dy = 0.0;
+    else dy = (j + 1) * binsize[1];
+    if (k > 0) dz = (k - 1) * binsize[2];
+    else if (k == 0) dz = 0.0;
+    else dz = (k + 1) * binsize[2];
+    return dx * dx + dy * dy + dz * dz;
+  };
+  stencil.clear();
+  for (int k = -sz; k <= sz; k++)
+    for (int j = -sy; j <= sy; j++)
+      for (int i = -sx; i <= sx; i++)
+        if (bin_distance(i, j, k) < cutneighmaxsq)
+          stencil.push_back(k * bins.mbin[1] * bins.mbin[0] + j * bins.mbin[0] + i);
+  upload(d_stencil, stencil, stream);
+}
+
+void cacg_context::init() {
+  if (!box_set) fail(CACG_ESTATE, "Init before the box is defined (read_data or cacg_set_box)");
+  if (pair_style == 0) fail(CACG_ESTATE, "No pair style defined");
+  int nt = std::max(ntypes, 1);
+  for (int i = 1; i <= nt; i++)
+    if (!setflag[i][i]) fail(CACG_EINVAL, "All pair coeffs are not set");
+  if (netypes > 1 && enlocal > 0)
+    fail(CACG_EINVAL, "Element forces use type-1 tables only (pair_lj_cut.cpp:327-331); one element type");
+  for (int i = 1; i <= nt; i++)
+    if (amass[i] <= 0.0) fail(CACG_EINVAL, "Not all atom masses are set");
+  if (!h_pin) check(cudaMallocHost(&h_pin, 64 * sizeof(int)), "pinned");
+
+  // Neighbor::init cutoffs (neighbor.cpp:335-374): per-type cutoff is 0, so the
+  // list cutoff is the neighbor command's value
+  cutneighmax = skin;
+  cutneighmaxsq = cutneighmax * cutneighmax;
+  triggersq = 0.25 * skin * skin;
+
+  // Pair::init -> init_one (pair.cpp:102-155, pair_lj_cut.cpp:140-198)
+  if (pair_style == 1) {
+    memset(&ljtab, 0, sizeof(ljtab));
+    for (int i = 1; i <= nt; i++)
+      for (int j = i; j <= nt; j++) {
+        double e = eps[i][j], s = sig[i][j], c = cutp[i][j];
+        if (!setflag[i][j]) {
+          e = std::sqrt(eps[i][i] * eps[j][j]);  // geometric mixing (pair.cpp:174-199)
+          s = std::sqrt(sig[i][i] * sig[j][j]);
+          c = std::sqrt(cutp[i][i] * cutp[j][j]);
+        }
+        double l1 = 48.0 * e * std::pow(s, 12.0), l2 = 24.0 * e * std::pow(s, 6.0);
+        int a = i * (MAXT + 1) + j, b = j * (MAXT + 1) + i;
+        ljtab.lj1[a] = ljtab.lj1[b] = l1;
+        ljtab.lj2[a] = ljtab.lj2[b] = l2;
+        ljtab.cutsq[a] = ljtab.cutsq[b] = c * c;
+      }
+    d_ljtab.ensure(1, stream);
+    check(cudaMemcpyAsync(d_ljtab.p, &ljtab, sizeof(ljtab), cudaMemcpyHostToDevice, stream), "ljtab");
+  } else {
+    upload(d_frho, frho_sp, stream);
+    upload(d_rhor, rhor_sp, stream);
+    upload(d_z2r, z2r_sp, stream);
+  }
+  // element masses: NAAE gives nae^3 * m(type 1) (element.cpp:1104) and
+  // pair_coeff eam resets it from the potential file (element.cpp:1117-1123)
+  for (int t = 1; t <= netypes; t++)
+    emass[t] = nae[t][0] * nae[t][1] * nae[t][2] * (pair_style == 2 ? eam_mass : amass[1]);
+
+  // upload per-particle state (owned particles only; ghosts come from borders)
+  cudaStream_t s = stream;
+  int na = std::max(nlocal, 1);
+  d_x.ensure(na, s);
+  d_v.ensure(3 * (size_t) na, s);
+  d_f.ensure(3 * (size_t) na, s);
+  d_xhold.ensure(3 * (size_t) na, s);
+  d_type.ensure(na, s);
+  d_tag.ensure(na, s);
+  d_root.ensure(na, s);
+  if (nlocal) {
+    std::vector<double4> x4(nlocal);
+    for (int i = 0; i < nlocal; i++) x4[i] = make_double4(h_x[3 * i], h_x[3 * i + 1], h_x[3 * i + 2], 0.0);
+    std::vector<int> root(nlocal);
+    for (int i = 0; i < nlocal; i++) root[i] = i;
+    check(cudaMemcpyAsync(d_x.p, x4.data(), sizeof(double4) * nlocal, cudaMemcpyHostToDevice, s), "x");
+    check(cudaMemcpyAsync(d_v.p, h_v.data(), sizeof(double) * 3 * nlocal, cudaMemcpyHostToDevice, s), "v");
+    check(cudaMemsetAsync(d_f.p, 0, sizeof(double) * 3 * nlocal, s), "f");
+    check(cudaMemcpyAsync(d_type.p, h_type.data(), sizeof(int) * nlocal, cudaMemcpyHostToDevice, s), "type");
+    check(cudaMemcpyAsync(d_tag.p, h_tag.data(), sizeof(int) * nlocal, cudaMemcpyHostToDevice, s), "tag");
+    check(cudaMemcpyAsync(d_root.p, root.data(), sizeof(int) * nlocal, cudaMemcpyHostToDevice, s), "root");
+  }
+  std::vector<double> massv(MAXT + 1, 0.0), emassv(MAXT + 1, 0.0);
+  for (int t = 0; t <= MAXT; t++) {
+    massv[t] = amass[t];
+    emassv[t] = emass[t];
+  }
+  upload(d_mass, massv, s);
+  upload(d_emass, emassv, s);
+  nghost = 0;
+  int ne = std::max(enlocal, 1);
+  d_ex.ensure(3 * (size_t) ne, s);
+  d_nodex.ensure(24 * (size_t) ne, s);
+  d_nodev.ensure(24 * (size_t) ne, s);
+  d_nodef.ensure(24 * (size_t) ne, s);
+  d_nodexhold.ensure(24 * (size_t) ne, s);
+  d_etype.ensure(ne, s);
+  d_etag.ensure(ne, s);
+  d_eroot.ensure(ne, s);
+  if (enlocal) {
+    std::vector<int> root(enlocal);
+    for (int i = 0; i < enlocal; i++) root[i] = i;
+    check(cudaMemcpyAsync(d_ex.p, h_ex.data(), sizeof(double) * 3 * enlocal, cudaMemcpyHostToDevice, s), "ex");
+    check(cudaMemcpyAsync(d_nodex.p, h_nodex.data(), sizeof(double) * 24 * enlocal, cudaMemcpyHostToDevice, s), "nodex");
+    check(cudaMemcpyAsync(d_nodev.p, h_nodev.data(), sizeof(double) * 24 * enlocal, cudaMemcpyHostToDevice, s), "nodev");
+    check(cudaMemsetAsync(d_nodef.p, 0, sizeof(double) * 24 * enlocal, s), "nodef");
+    check(cudaMemcpyAsync(d_etype.p, h_etype.data(), sizeof(int) * enlocal, cudaMemcpyHostToDevice, s), "etype");
+    check(cudaMemcpyAsync(d_etag.p, h_etag.data(), sizeof(int) * enlocal, cudaMemcpyHostToDevice, s), "etag");
+    check(cudaMemcpyAsync(d_eroot.p, root.data(), sizeof(int) * enlocal, cudaMemcpyHostToDevice, s), "eroot");
+    element_tables();
+    // integration-point rows of the owned elements (NodeNeighList rows, node_neigh_list.h:23-27)
+    h_row_first.assign(enlocal + 1, 0);
+    std::vector<int> re, rj;
+    for (int e = 0; e < enlocal; e++) {
+      h_row_first[e] = (int) re.size();
+      for (int jj = 0; jj < numint[h_etype[e]]; jj++) {
+        re.push_back(e);
+        rj.push_back(jj);
+      }
+    }
+    h_row_first[enlocal] = (int) re.size();
+    nrows = (int) re.size();
+    upload(d_row_elem, re, s);
+    upload(d_row_jj, rj, s);
+    upload(d_row_first, h_row_first, s);
+    element_size();
+  } else {
+    nrows = 0;
+  }
+  enghost = 0;
+  cut_all = cutneighmax + max_size;
+  cut_ele = cutneighmax + max_size / 2;
+  cut_allsq = cut_all * cut_all;
+  cut_elesq = cut_ele * cut_ele;
+  inited = true;
+  setup_done = list_built = elists_built = false;
+}
+
+// ------------------------------------------------------------------ ghosts
+
+void cacg_context::borders() {
+  cudaStream_t s = stream;
+  d_misc.ensure(16, s);
+  // atoms (comm_brick.cpp:657-801)
+  nghost = 0;
+  size_t send_total = 0;
+  int nfirst = 0, nlast = 0;
+  for (size_t iw = 0; iw < swaps.size(); iw++) {
+    SwapDef &w = swaps[iw];
+    if (iw == 0 || swaps[iw - 1].dim != w.dim) nlast = 0;
+    if (w.pbc == 1) {
+      nfirst = nlast;
+      nlast = nlocal + nghost;
+    }
+    int n = nlast - nfirst;
+    d_flags.ensure(std::max(n, 1), s);
+    d_pos.ensure(std::max(n, 1), s);
+    launch_border_flags_atoms(d_x.p, nfirst, nlast, w.dim, w.lo, w.hi, d_flags.p, s);
+    scan_exclusive(d_flags.p, d_pos.p, n, d_misc.p, d_scan, s);
+    launches += 2;
+    check(cudaMemcpyAsync(h_pin, d_misc.p, sizeof(int), cudaMemcpyDeviceToHost, s), "count");
+    sync();
+    int cnt = n > 0 ? h_pin[0] : 0;
+    int n0 = nlocal + nghost;
+    d_x.ensure((size_t) n0 + cnt, s, true);
+    d_type.ensure((size_t) n0 + cnt, s, true);
+    d_tag.ensure((size_t) n0 + cnt, s, true);
+    d_root.ensure((size_t) n0 + cnt, s, true);
+    d_send.ensure(send_total + cnt + 1, s, true);
+    launch_border_scatter_atoms(d_x.p, d_type.p, d_tag.p, d_root.p, d_send.p + send_total,
+                                d_flags.p, d_pos.p, nfirst, nlast, n0, w.d[0], w.d[1], w.d[2], s);
+    launches++;
+    w.nsend = cnt;
+    w.firstrecv = n0;
+    w.send_off = (int) send_total;
+    send_total += cnt;
+    nghost += cnt;
+  }
+  // elements (comm_brick.cpp:804-905)
+  enghost = 0;
+  send_total = 0;
+  nfirst = nlast = 0;
+  for (size_t iw = 0; iw < swaps.size(); iw++) {
+    SwapDef &w = swaps[iw];
+    if (iw == 0 || swaps[iw - 1].dim != w.dim) nlast = 0;
+    if (w.pbc == 1) {
+      nfirst = nlast;
+      nlast = enlocal + enghost;
+    }
+    int n = nlast - nfirst;
+    if (enlocal == 0) {
+      w.ensend = 0;
+      w.efirstrecv = enlocal + enghost;
+      w.esend_off = 0;
+      continue;
+    }
+    d_flags.ensure(std::max(n, 1), s);
+    d_pos.ensure(std::max(n, 1), s);
+    launch_border_flags_elems(d_ex.p, d_etype.p, nfirst, nlast, w.dim, w.mlo, w.mhi, d_flags.p, s);
+    scan_exclusive(d_flags.p, d_pos.p, n, d_misc.p, d_scan, s);
+    launches += 2;
+    check(cudaMemcpyAsync(h_pin, d_misc.p, sizeof(int), cudaMemcpyDeviceToHost, s), "count");
+    sync();
+    int cnt = n > 0 ? h_pin[0] : 0;
+    int n0 = enlocal + enghost;
+    d_ex.ensure(3 * ((size_t) n0 + cnt), s, true);
+    d_nodex.ensure(24 * ((size_t) n0 + cnt), s, true);
+    d_etype.ensure((size_t) n0 + cnt, s, true);
+    d_etag.ensure((size_t) n0 + cnt, s, true);
+    d_eroot.ensure((size_t) n0 + cnt, s, true);
+    d_esend.ensure(send_total + cnt + 1, s, true);
+    launch_border_scatter_elems(d_ex.p, d_nodex.p, d_etype.p, d_etag.p, d_eroot.p,
+                                d_esend.p + send_total, d_flags.p, d_pos.p, nfirst, nlast, n0,
+                                w.d[0], w.d[1], w.d[2], s);
+    launches++;
+    w.ensend = cnt;
+    w.efirstrecv = n0;
+    w.esend_off = (int) send_total;
+    send_total += cnt;
+    enghost += cnt;
+  }
+  // per-element site offsets (types of ghosts from their roots)
+  int nall_e = enlocal + enghost;
+  if (enlocal) {
+    h_eroot.resize(nall_e);
+    check(cudaMemcpyAsync(h_eroot.data(), d_eroot.p, sizeof(int) * nall_e, cudaMemcpyDeviceToHost, s), "eroot");
+    sync();
+    h_site_base.assign(nall_e + 1, 0);
+    int acc = 0;
+    for (int e = 0; e < nall_e; e++) {
+      h_site_base[e] = acc;
+      acc += inter_num[h_etype[h_eroot[e]]];
+    }
+    h_site_base[nall_e] = acc;
+    nsites = acc;
+    upload(d_site_base, h_site_base, s);
+  } else {
+    nsites = 0;
+  }
+}
+
+// CommBrick::forward_comm / eforward_comm: ghost positions from their sources,
+// swap by swap (comm_brick.cpp:1017-1112)
+void cacg_context::forward_comm() {
+  for (auto &w : swaps) {
+    if (nlocal && w.nsend) {
+      launch_forward_atoms(d_x.p, d_send.p + w.send_off, w.nsend, w.firstrecv, w.d[0], w.d[1], w.d[2], stream);
+      launches++;
+    }
+    if (enlocal && w.ensend) {
+      launch_forward_elems(d_nodex.p, d_esend.p + w.esend_off, w.ensend, w.efirstrecv, w.d[0], w.d[1], w.d[2], stream);
+      launches++;
+    }
+  }
+}
+
+void cacg_context::pbc() {
+  launch_pbc_atoms(d_x.p, nlocal, lo, hi, prd, periodic, stream);
+  launch_pbc_elems(d_ex.p, d_nodex.p, enlocal, lo, hi, prd, periodic, stream);
+  launches += 2;
+}
+
+// ------------------------------------------------------------------ lists
+
+void cacg_context::neighbor_build() {
+  cudaStream_t s = stream;
+  int nall = nlocal + nghost;
+  if (nlocal == 0) {
+    list_built = true;
+    return;
+  }
+  d_misc.ensure(16, s);
+  d_abin.ensure(nall, s);
+  check(cudaMemsetAsync(d_misc.p + 1, 0, sizeof(int) * 2, s), "memset");
+  launch_coord2bin_atoms(d_x.p, nall, bins, d_abin.p, d_misc.p + 1, s);
+  build_bins(d_abin.p, nall, bins.mbins, d_bcount, d_bstart, d_bmem, d_scan, s);
+  d_bx.ensure(nall, s);
+  launch_gather_bin_x_atoms(d_bmem.p, d_x.p, d_bx.p, nall, s);
+  launches += 7;
+  stride = (nlocal + 31) / 32 * 32;
+  d_num.ensure(nlocal, s);
+  for (int attempt = 0; attempt < 3; attempt++) {
+    d_list.ensure((size_t) maxneigh * stride, s);
+    check(cudaMemsetAsync(d_misc.p + 2, 0, sizeof(int), s), "memset");
+    launch_atom_list(d_x.p, d_abin.p, d_bstart.p, d_bmem.p, d_bx.p, d_stencil.p,
+                     (int) stencil.size(), bins.mbins, nlocal, cutneighmaxsq, maxneigh, stride,
+                     d_num.p, d_list.p, d_misc.p + 2, s);
+    launches++;
+    check(cudaMemcpyAsync(h_pin + 1, d_misc.p + 1, sizeof(int) * 2, cudaMemcpyDeviceToHost, s), "ovf");
+    sync();
+    if (h_pin[1]) fail(CACG_EINVAL, "%d atoms outside the bin grid (lost atoms)", h_pin[1]);
+    if (h_pin[2] == 0) break;
+    if (h_pin[2] > oneatom || attempt == 2)
+      fail(CACG_EOVERFLOW, "Neighbor list overflow, boost neigh_modify one");
+    maxneigh = (h_pin[2] + 8 + 7) / 8 * 8;
+  }
+  launch_hold_atoms(d_x.p, d_xhold.p, nlocal, s);
+  launches++;
+  list_built = true;
+}
+
+void cacg_context::neighbor_ebuild() {
+  cudaStream_t s = stream;
+  setup_cut();
+  if (enlocal == 0) {
+    elists_built = true;
+    return;
+  }
+  int nall = enlocal + enghost;
+  if (dist_check)
+    check(cudaMemcpyAsync(d_nodexhold.p, d_nodex.p, sizeof(double) * 24 * enlocal, cudaMemcpyDeviceToDevice, s), "hold");
+  d_ebin.ensure(nall, s);
+  check(cudaMemsetAsync(d_misc.p + 3, 0, sizeof(int) * 2, s), "memset");
+  launch_coord2bin_elems(d_ex.p, nall, bins, d_ebin.p, d_misc.p + 3, s);
+  build_bins(d_ebin.p, nall, bins.mbins, d_ebcount, d_ebstart, d_ebmem, d_scan, s);
+  d_ebx.ensure(nall, s);
+  launch_gather_bin_x_elems(d_ebmem.p, d_ex.p, d_ebx.p, nall, s);
+  launches += 7;
+  estride = (enlocal + 31) / 32 * 32;
+  d_enum.ensure(enlocal, s);
+  for (int attempt = 0; attempt < 3; attempt++) {
+    d_elist.ensure((size_t) maxeneigh * estride, s);
+    check(cudaMemsetAsync(d_misc.p + 4, 0, sizeof(int), s), "memset");
+    launch_elem_list(d_ex.p, d_ebin.p, d_ebstart.p, d_ebmem.p, d_ebx.p, d_stencil.p,
+                     (int) stencil.size(), bins.mbins, enlocal, cut_allsq, maxeneigh, estride,
+                     d_enum.p, d_elist.p, d_misc.p + 4, s);
+    launches++;
+    check(cudaMemcpyAsync(h_pin + 3, d_misc.p + 3, sizeof(int) * 2, cudaMemcpyDeviceToHost, s), "ovf");
+    sync();
+    if (h_pin[3]) fail(CACG_EINVAL, "%d elements outside the bin grid (lost elements)", h_pin[3]);
+    if (h_pin[4] == 0) break;
+    if (h_pin[4] > oneatom || attempt == 2)
+      fail(CACG_EOVERFLOW, "Neighbor list overflow, boost neigh_modify one");
+    maxeneigh = (h_pin[4] + 8 + 7) / 8 * 8;
+  }
+  elists_built = false;
+}
+
+void cacg_context::neighbor_nbuild() {
+  cudaStream_t s = stream;
+  if (enlocal == 0) {
+    elists_built = true;
+    return;
+  }
+  int nall = enlocal + enghost;
+  ElemTables t = etab();
+  d_site_x.ensure(std::max(nsites, 1), s);
+  launch_sites(d_nodex.p, d_etype.p, d_site_base.p, nall, t, d_site_x.p, s);
+  d_subc.ensure((size_t) nall * nsub, s);
+  launch_sub_centres(d_nodex.p, nall, t, d_subc.p, s);
+  launches += 2;
+  rowstride = (nrows + 31) / 32 * 32;
+  d_ipnum.ensure(std::max(nrows, 1), s);
+  for (int attempt = 0; attempt < 3; attempt++) {
+    d_ipent.ensure((size_t) maxip * rowstride, s);
+    check(cudaMemsetAsync(d_misc.p + 5, 0, sizeof(int), s), "memset");
+    launch_ip_list(d_nodex.p, d_ex.p, d_etype.p, d_row_elem.p, d_row_jj.p, nrows, d_enum.p,
+                   d_elist.p, estride, d_subc.p, d_site_x.p, d_site_base.p, t, cut_elesq,
+                   cut_subelesq, cutneighmaxsq, maxip, rowstride, d_ipnum.p, d_ipent.p,
+                   d_misc.p + 5, s);
+    launches++;
+    check(cudaMemcpyAsync(h_pin + 5, d_misc.p + 5, sizeof(int), cudaMemcpyDeviceToHost, s), "ovf");
+    sync();
+    if (h_pin[5] == 0) break;
+    if (h_pin[5] > oneatom || attempt == 2)
+      fail(CACG_EOVERFLOW, "Neighbor list overflow, boost neigh_modify one");
+    maxip = (h_pin[5] + 8 + 7) / 8 * 8;
+  }
+  d_fip.ensure(3 * (size_t) std::max(nrows, 1), s);
+  elists_built = true;
+}
+
+// ------------------------------------------------------------------ forces
+
+void cacg_context::pair_compute() {
+  pair_compute_pass(1);
+  pair_compute_pass(2);
+}
+
+// pass 1: LJ forces, or EAM densities + F'(rho) + ghost copy; pass 2: EAM forces
+void cacg_context::pair_compute_pass(int pass) {
+  if (nlocal == 0) return;
+  if (!list_built) fail(CACG_ESTATE, "Pair::compute before the atom neighbor list is built");
+  cudaStream_t s = stream;
+  bool exact = mode == CACG_FP64_EXACT;
+  if (pair_style == 1) {
+    if (pass != 1) return;
+    if (exact) fp64_exact::lj_atoms(d_x.p, d_type.p, d_num.p, d_list.p, stride, nlocal, d_ljtab.p, d_f.p, s);
+    else fp64_fma::lj_atoms(d_x.p, d_type.p, d_num.p, d_list.p, stride, nlocal, d_ljtab.p, d_f.p, s);
+    launches++;
+    return;
+  }
+  EamTables e = eamtab();
+  if (pass == 1) {
+    int nall = nlocal + nghost;
+    d_rho.ensure(nall, s);
+    d_fp.ensure(nall, s);
+    if (exact) fp64_exact::eam_rho_atoms(d_x.p, d_num.p, d_list.p, stride, nlocal, e, d_rho.p, d_fp.p, s);
+    else fp64_fma::eam_rho_atoms(d_x.p, d_num.p, d_list.p, stride, nlocal, e, d_rho.p, d_fp.p, s);
+    // forward_comm_pair: ghost fp = owner fp (comm_brick.cpp:941-971)
+    launch_copy_root(d_fp.p, 1, d_root.p, nlocal, nghost, s);
+    launches += 2;
+  } else {
+    if (exact) fp64_exact::eam_force_atoms(d_x.p, d_num.p, d_list.p, stride, nlocal, e, d_fp.p, d_f.p, s);
+    else fp64_fma::eam_force_atoms(d_x.p, d_num.p, d_list.p, stride, nlocal, e, d_fp.p, d_f.p, s);
+    launches++;
+  }
+}
+
+void cacg_context::pair_ecompute() {
+  if (enlocal == 0) return;
+  if (!elists_built) fail(CACG_ESTATE, "Pair::ecompute before the node neighbor list is built");
+  cudaStream_t s = stream;
+  bool exact = mode == CACG_FP64_EXACT;
+  int nall = enlocal + enghost;
+  ElemTables t = etab();
+  // sites of every local and ghost element at the current node positions
+  launch_sites(d_nodex.p, d_etype.p, d_site_base.p, nall, t, d_site_x.p, s);
+  launches++;
+  if (pair_style == 1) {
+    int a = 1 * (MAXT + 1) + 1;
+    if (exact)
+      fp64_exact::lj_ip(d_nodex.p, d_etype.p, d_row_elem.p, d_row_jj.p, nrows, d_ipnum.p, d_ipent.p,
+                        rowstride, d_site_x.p, t, ljtab.lj1[a], ljtab.lj2[a], ljtab.cutsq[a], d_fip.p, s);
+    else
+      fp64_fma::lj_ip(d_nodex.p, d_etype.p, d_row_elem.p, d_row_jj.p, nrows, d_ipnum.p, d_ipent.p,
+                      rowstride, d_site_x.p, t, ljtab.lj1[a], ljtab.lj2[a], ljtab.cutsq[a], d_fip.p, s);
+    launches++;
+  } else {
+    EamTables e = eamtab();
+    d_erho.ensure((size_t) NPE * nall, s);
+    d_site_fp.ensure(std::max(nsites, 1), s);
+    if (exact) {
+      fp64_exact::eam_erho(d_nodex.p, d_etype.p, d_row_first.p, enlocal, d_ipnum.p, d_ipent.p, rowstride, d_site_x.p, t, e, d_erho.p, s);
+    } else {
+      fp64_fma::eam_erho(d_nodex.p, d_etype.p, d_row_first.p, enlocal, d_ipnum.p, d_ipent.p, rowstride, d_site_x.p, t, e, d_erho.p, s);
+    }
+    // eforward_comm_pair: ghost nodal densities from their owners (comm_brick.cpp:978-1010)
+    launch_copy_root(d_erho.p, NPE, d_eroot.p, enlocal, enghost, s);
+    if (exact) {
+      fp64_exact::eam_site_fp(d_erho.p, d_etype.p, d_site_base.p, nall, t, e, d_site_fp.p, s);
+      fp64_exact::eam_ip(d_nodex.p, d_erho.p, d_etype.p, d_row_elem.p, d_row_jj.p, nrows, d_ipnum.p, d_ipent.p,
+                         rowstride, d_site_x.p, d_site_fp.p, t, e, d_fip.p, s);
+    } else {
+      fp64_fma::eam_site_fp(d_erho.p, d_etype.p, d_site_base.p, nall, t, e, d_site_fp.p, s);
+      fp64_fma::eam_ip(d_nodex.p, d_erho.p, d_etype.p, d_row_elem.p, d_row_jj.p, nrows, d_ipnum.p, d_ipent.p,
+                       rowstride, d_site_x.p, d_site_fp.p, t, e, d_fip.p, s);
+    }
+    launches += 4;
+  }
+  if (exact) fp64_exact::gather_nodef(d_fip.p, d_etype.p, d_row_first.p, enlocal, t, d_nodef.p, s);
+  else fp64_fma::gather_nodef(d_fip.p, d_etype.p, d_row_first.p, enlocal, t, d_nodef.p, s);
+  launches++;
+}
+
+// ------------------------------------------------------------------ integrate
+
+void cacg_context::nve_initial() {
+  double dtf = 0.5 * dt * ftm2v;
+  launch_nve_atoms_initial(d_x.p, d_v.p, d_f.p, d_type.p, d_mass.p, nlocal, dt, dtf, stream);
+  launch_nve_nodes_initial(d_ex.p, d_nodex.p, d_nodev.p, d_nodef.p, d_etype.p, d_emass.p, enlocal, dt, dtf, stream);
+  launches += 2;
+}
+
+void cacg_context::nve_final() {
+  double dtf = 0.5 * dt * ftm2v;
+  launch_nve_atoms_final(d_v.p, d_f.p, d_type.p, d_mass.p, nlocal, dtf, stream);
+  launch_nve_nodes_final(d_nodev.p, d_nodef.p, d_etype.p, d_emass.p, enlocal, dtf, stream);
+  launches += 2;
+}
+
+// Neighbor::decide (neighbor.cpp:1150-1163); ago counts steps since setup and
+// is not reset by a rebuild, as in the reference
+int cacg_context::decide() {
+  ago++;
+  if (ago >= delay && ago % every == 0) {
+    if (dist_check == 0) return 1;
+    d_misc.ensure(16, stream);
+    check(cudaMemsetAsync(d_misc.p + 6, 0, sizeof(int), stream), "memset");
+    launch_check_distance(d_x.p, d_xhold.p, nlocal, d_nodex.p, d_nodexhold.p, enlocal, triggersq,
+                          d_misc.p + 6, stream);
+    launches++;
+    check(cudaMemcpyAsync(h_pin + 6, d_misc.p + 6, sizeof(int), cudaMemcpyDeviceToHost, stream), "flag");
+    sync();
+    return h_pin[6] ? 1 : 0;
+  }
+  return 0;
+}
+
+void cacg_context::rebuild() {
+  nrebuild++;
+  pbc();
+  if (enlocal) element_size();
+  setup_cut();
+  comm_setup();
+  setup_bins();
+  borders();
+  if (nlocal) neighbor_build();
+  if (enlocal) {
+    neighbor_ebuild();
+    neighbor_nbuild();
+  }
+}
+
+void cacg_context::setup() {
+  require_init();
+  comm_setup();
+  setup_bins();
+  borders();
+  ago = 0;
+  setup_done = true;
+  list_built = elists_built = false;
+}
+
+void cacg_context::run(int n) {
+  if (n < 0) fail(CACG_EINVAL, "Illegal run command");
+  if (!setup_done) setup();
+  if (!list_built) neighbor_build();
+  if (!elists_built && enlocal) {
+    neighbor_ebuild();
+    neighbor_nbuild();
+  }
+  if (!fix_nve) fail(CACG_ESTATE, "run without fix nve");
+  for (int k = 0; k < 8; k++) t_ms[k] = 0.0;
+  for (auto &e : ev)
+    if (!e) check(cudaEventCreate(&e), "event");
+  check(cudaEventRecord(ev[0], stream), "ev");
+  const size_t P = 6;  // phase marks per step
+  for (int step = 0; step < n; step++) {
+    size_t b = (size_t) step * P;
+    ntimestep++;
+    mark(b);
+    nve_initial();
+    int nflag = decide();
+    if (nflag == 0) forward_comm();
+    else rebuild();
+    mark(b + 1);
+    pair_compute_pass(1);
+    mark(b + 2);
+    pair_compute_pass(2);
+    mark(b + 3);
+    pair_ecompute();
+    mark(b + 4);
+    nve_final();
+    mark(b + 5);
+  }
+  check(cudaEventRecord(ev[1], stream), "ev");
+  check(cudaEventSynchronize(ev[1]), "ev sync");
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ev[0], ev[1]);
+  t_ms[0] = ms;
+  if (timing && n > 0) {
+    for (int step = 0; step < n; step++) {
+      size_t b = (size_t) step * P;
+      for (size_t k = 0; k < P - 1; k++) {
+        float d = 0;
+        check(cudaEventElapsedTime(&d, pev[b + k], pev[b + k + 1]), "elapsed");
+        t_ms[1 + k] += d;
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ ABI
+
+#define API_BEGIN                 \
+  if (!h) return CACG_EINVAL;     \
+  try {                           \
+    check(cudaSetDevice(h->device), "cudaSetDevice");
+#define API_END                                                              \
+  return CACG_OK;                                                            \
+  }                                                                          \
+  catch (const ApiError &e) {                                                \
+    h->err = e.msg;                                                          \
+    return e.code;                                                           \
+  }                                                                          \
+  catch (const CudaError &e) {                                               \
+    h->err = std::string(e.where) + ": " + cudaGetErrorString(e.code);       \
+    return e.code == cudaErrorMemoryAllocation ? CACG_ENOMEM : CACG_ECUDA;   \
+  }
+
+extern "C" {
+
+const char *cacg_version(void) { return "cacg 0.1 (sm_103a)"; }
+
+int cacg_create(cacg_handle *out, int device) {
+  if (!out) return CACG_EINVAL;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return CACG_ECUDA;
+  if (device < 0 || device >= n) return CACG_EINVAL;
+  cacg_context *h = new cacg_context();
+  h->device = device;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete h;
+    return CACG_ECUDA;
+  }
+  *out = h;
+  return CACG_OK;
+}
+
+int cacg_destroy(cacg_handle h) {
+  if (!h) return CACG_EINVAL;
+  cudaSetDevice(h->device);
+  cudaStreamSynchronize(h->stream);
+  delete h;
+  return CACG_OK;
+}
+
+const char *cacg_error(cacg_handle h) { return h ? h->err.c_str() : "null handle"; }
+
+int cacg_command(cacg_handle h, const char *line) {
+  API_BEGIN
+  if (!line) fail(CACG_EINVAL, "null command");
+  h->command(line);
+  API_END
+}
+
+int cacg_file(cacg_handle h, const char *path) {
+  API_BEGIN
+  std::ifstream in(path ? path : "");
+  if (!in) fail(CACG_EIO, "Cannot open input script %s", path ? path : "(null)");
+  std::string line, acc;
+  while (std::getline(in, line)) {
+    // '&' continues a line (input.cpp:119-125)
+    size_t e = line.find_last_not_of(" \t\r\n");
+    if (e != std::string::npos && line[e] == '&') {
+      acc += line.substr(0, e) + " ";
+      continue;
+    }
+    acc += line;
+    h->command(acc);
+    acc.clear();
+  }
+  if (!acc.empty()) h->command(acc);
+  API_END
+}
+
+int cacg_set_box(cacg_handle h, const double *lo, const double *hi, const int *periodic) {
+  API_BEGIN
+  if (!lo || !hi || !periodic) fail(CACG_EINVAL, "null argument");
+  for (int d = 0; d < 3; d++) {
+    if (!(lo[d] < hi[d])) fail(CACG_EINVAL, "Box bounds are invalid");
+    h->lo[d] = lo[d];
+    h->hi[d] = hi[d];
+    h->prd[d] = hi[d] - lo[d];
+    h->periodic[d] = periodic[d] ? 1 : 0;
+  }
+  h->box_set = true;
+  h->inited = false;
+  API_END
+}
+
+int cacg_set_masses(cacg_handle h, int ntypes, const double *mass) {
+  API_BEGIN
+  if (ntypes < 1 || ntypes > MAXT || !mass) fail(CACG_EINVAL, "bad mass table");
+  h->ntypes = ntypes;
+  for (int t = 1; t <= ntypes; t++) {
+    if (mass[t - 1] <= 0.0) fail(CACG_EINVAL, "Invalid mass value");
+    h->amass[t] = mass[t - 1];
+  }
+  h->inited = false;
+  API_END
+}
+
+int cacg_set_atoms(cacg_handle h, int n, const double *x, const double *v, const int *type) {
+  API_BEGIN
+  if (n < 0 || (n > 0 && !x)) fail(CACG_EINVAL, "bad atom arrays");
+  h->nlocal = n;
+  h->h_x.assign(x, x + 3 * (size_t) n);
+  h->h_v.assign(3 * (size_t) n, 0.0);
+  if (v) h->h_v.assign(v, v + 3 * (size_t) n);
+  h->h_type.assign(n, 1);
+  if (type)
+    for (int i = 0; i < n; i++) {
+      if (type[i] < 1 || type[i] > std::max(h->ntypes, 1)) fail(CACG_EINVAL, "Invalid atom type");
+      h->h_type[i] = type[i];
+    }
+  h->h_tag.resize(n);
+  for (int i = 0; i < n; i++) h->h_tag[i] = i + 1;
+  h->inited = false;
+  API_END
+}
+
+int cacg_set_element_types(cacg_handle h, int ntypes, const int *nae, const int *numint,
+                           const int *intp, const double *weight) {
+  API_BEGIN
+  if (ntypes < 1 || ntypes > MAXT || !nae || !numint || !intp || !weight) fail(CACG_EINVAL, "bad element types");
+  h->netypes = ntypes;
+  int off = 0;
+  for (int t = 1; t <= ntypes; t++) {
+    for (int d = 0; d < 3; d++) h->nae[t][d] = nae[3 * (t - 1) + d];
+    if (h->nae[t][0] < 2 || h->nae[t][1] < 2 || h->nae[t][2] < 2) fail(CACG_EINVAL, "Invalid naae values");
+    h->numint[t] = numint[t - 1];
+    h->intp[t].assign(intp + 3 * off, intp + 3 * (off + numint[t - 1]));
+    h->weight[t].assign(weight + off, weight + off + numint[t - 1]);
+    off += numint[t - 1];
+  }
+  h->inited = false;
+  API_END
+}
+
+int cacg_set_elements(cacg_handle h, int n, const int *etype, const double *centre,
+                      const double *nodex, const double *nodev) {
+  API_BEGIN
+  if (n < 0 || (n > 0 && (!etype || !centre || !nodex))) fail(CACG_EINVAL, "bad element arrays");
+  h->enlocal = n;
+  h->h_etype.resize(n);
+  for (int i = 0; i < n; i++) {
+    if (etype[i] < 1 || etype[i] > h->netypes) fail(CACG_EINVAL, "Invalid element type");
+    h->h_etype[i] = etype[i];
+  }
+  h->h_ex.assign(centre, centre + 3 * (size_t) n);
+  h->h_nodex.assign(nodex, nodex + 24 * (size_t) n);
+  h->h_nodev.assign(24 * (size_t) n, 0.0);
+  if (nodev) h->h_nodev.assign(nodev, nodev + 24 * (size_t) n);
+  h->h_etag.resize(n);
+  for (int i = 0; i < n; i++) h->h_etag[i] = i + 1;
+  h->inited = false;
+  API_END
+}
+
+int cacg_set_precision(cacg_handle h, int mode) {
+  API_BEGIN
+  if (mode != CACG_FP64_EXACT && mode != CACG_FP64 && mode != CACG_MIXED) fail(CACG_EINVAL, "unknown precision mode");
+  h->mode = mode;
+  API_END
+}
+
+int cacg_init(cacg_handle h) {
+  API_BEGIN
+  h->init();
+  API_END
+}
+
+int cacg_setup(cacg_handle h) {
+  API_BEGIN
+  h->setup();
+  API_END
+}
+
+int cacg_neighbor_build(cacg_handle h) {
+  API_BEGIN
+  if (!h->setup_done) h->setup();
+  h->neighbor_build();
+  API_END
+}
+
+int cacg_neighbor_ebuild(cacg_handle h) {
+  API_BEGIN
+  if (!h->setup_done) h->setup();
+  h->neighbor_ebuild();
+  API_END
+}
+
+int cacg_neighbor_nbuild(cacg_handle h) {
+  API_BEGIN
+  if (!h->setup_done) h->setup();
+  h->neighbor_nbuild();
+  API_END
+}
+
+int cacg_pair_compute(cacg_handle h, int eflag, int vflag) {
+  API_BEGIN
+  (void) eflag;
+  (void) vflag;
+  h->pair_compute();
+  h->sync();
+  API_END
+}
+
+int cacg_pair_ecompute(cacg_handle h) {
+  API_BEGIN
+  h->pair_ecompute();
+  h->sync();
+  API_END
+}
+
+int cacg_fix_nve_initial_integrate(cacg_handle h) {
+  API_BEGIN
+  h->require_init();
+  h->nve_initial();
+  API_END
+}
+
+int cacg_fix_nve_final_integrate(cacg_handle h) {
+  API_BEGIN
+  h->require_init();
+  h->nve_final();
+  API_END
+}
+
+int cacg_run(cacg_handle h, int nsteps) {
+  API_BEGIN
+  h->run(nsteps);
+  API_END
+}
+
+int cacg_get_counts(cacg_handle h, long long *c, int n) {
+  API_BEGIN
+  long long v[13] = {h->nlocal, h->nghost, 0, h->enlocal, h->enghost, 0, h->nrows, 0,
+                     h->nrebuild, (long long) h->stencil.size(), h->ntimestep, h->nsites,
+                     h->launches};
+  if (h->list_built && h->nlocal) {
+    std::vector<int> num(h->nlocal);
+    check(cudaMemcpyAsync(num.data(), h->d_num.p, sizeof(int) * h->nlocal, cudaMemcpyDeviceToHost, h->stream), "num");
+    h->sync();
+    for (int x : num) v[2] += x;
+  }
+  if (h->enlocal && h->d_enum.p) {
+    std::vector<int> num(h->enlocal);
+    check(cudaMemcpyAsync(num.data(), h->d_enum.p, sizeof(int) * h->enlocal, cudaMemcpyDeviceToHost, h->stream), "enum");
+    h->sync();
+    for (int x : num) v[5] += x;
+  }
+  if (h->elists_built && h->nrows) {
+    std::vector<int> num(h->nrows);
+    check(cudaMemcpyAsync(num.data(), h->d_ipnum.p, sizeof(int) * h->nrows, cudaMemcpyDeviceToHost, h->stream), "ipnum");
+    h->sync();
+    for (int x : num) v[7] += x;
+  }
+  for (int i = 0; i < n && i < 13; i++) c[i] = v[i];
+  API_END
+}
+
+int cacg_get_atoms(cacg_handle h, int all, double *x, double *v, double *f, int *tag) {
+  API_BEGIN
+  if (!h->inited) fail(CACG_ESTATE, "no device state yet (cacg_init)");
+  int n = all ? h->nlocal + h->nghost : h->nlocal;
+  cudaStream_t s = h->stream;
+  if (x && n) {
+    std::vector<double4> x4(n);
+    check(cudaMemcpyAsync(x4.data(), h->d_x.p, sizeof(double4) * n, cudaMemcpyDeviceToHost, s), "x");
+    h->sync();
+    for (int i = 0; i < n; i++) {
+      x[3 * i] = x4[i].x;
+      x[3 * i + 1] = x4[i].y;
+      x[3 * i + 2] = x4[i].z;
+    }
+  }
+  if (v && h->nlocal) check(cudaMemcpyAsync(v, h->d_v.p, sizeof(double) * 3 * h->nlocal, cudaMemcpyDeviceToHost, s), "v");
+  if (f && h->nlocal) check(cudaMemcpyAsync(f, h->d_f.p, sizeof(double) * 3 * h->nlocal, cudaMemcpyDeviceToHost, s), "f");
+  if (tag && n) check(cudaMemcpyAsync(tag, h->d_tag.p, sizeof(int) * n, cudaMemcpyDeviceToHost, s), "tag");
+  h->sync();
+  API_END
+}
+
+int cacg_get_elements(cacg_handle h, int all, double *centre, double *nodex, double *nodev,
+                      double *nodef, int *tag) {
+  API_BEGIN
+  if (!h->inited) fail(CACG_ESTATE, "no device state yet (cacg_init)");
+  int n = all ? h->enlocal + h->enghost : h->enlocal;
+  cudaStream_t s = h->stream;
+  if (centre && n) check(cudaMemcpyAsync(centre, h->d_ex.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s), "ex");
+  if (nodex && n) check(cudaMemcpyAsync(nodex, h->d_nodex.p, sizeof(double) * 24 * n, cudaMemcpyDeviceToHost, s), "nodex");
+  if (nodev && h->enlocal) check(cudaMemcpyAsync(nodev, h->d_nodev.p, sizeof(double) * 24 * h->enlocal, cudaMemcpyDeviceToHost, s), "nodev");
+  if (nodef && h->enlocal) check(cudaMemcpyAsync(nodef, h->d_nodef.p, sizeof(double) * 24 * h->enlocal, cudaMemcpyDeviceToHost, s), "nodef");
+  if (tag && n) check(cudaMemcpyAsync(tag, h->d_etag.p, sizeof(int) * n, cudaMemcpyDeviceToHost, s), "etag");
+  h->sync();
+  API_END
+}
+
+int cacg_get_atom_list(cacg_handle h, int *numneigh, int *neigh) {
+  API_BEGIN
+  if (!h->list_built) fail(CACG_ESTATE, "atom list not built");
+  int n = h->nlocal;
+  if (!n) return CACG_OK;
+  std::vector<int> num(n), lst((size_t) h->maxneigh * h->stride);
+  check(cudaMemcpyAsync(num.data(), h->d_num.p, sizeof(int) * n, cudaMemcpyDeviceToHost, h->stream), "num");
+  check(cudaMemcpyAsync(lst.data(), h->d_list.p, sizeof(int) * lst.size(), cudaMemcpyDeviceToHost, h->stream), "list");
+  h->sync();
+  size_t o = 0;
+  for (int i = 0; i < n; i++) {
+    if (numneigh) numneigh[i] = num[i];
+    for (int k = 0; k < num[i]; k++)
+      if (neigh) neigh[o++] = lst[(size_t) k * h->stride + i];
+  }
+  API_END
+}
+
+int cacg_get_elem_list(cacg_handle h, int *numneigh, int *neigh) {
+  API_BEGIN
+  int n = h->enlocal;
+  if (!n) return CACG_OK;
+  if (!h->d_enum.p) fail(CACG_ESTATE, "element list not built");
+  std::vector<int> num(n), lst((size_t) h->maxeneigh * h->estride);
+  check(cudaMemcpyAsync(num.data(), h->d_enum.p, sizeof(int) * n, cudaMemcpyDeviceToHost, h->stream), "enum");
+  check(cudaMemcpyAsync(lst.data(), h->d_elist.p, sizeof(int) * lst.size(), cudaMemcpyDeviceToHost, h->stream), "elist");
+  h->sync();
+  size_t o = 0;
+  for (int i = 0; i < n; i++) {
+    if (numneigh) numneigh[i] = num[i];
+    for (int k = 0; k < num[i]; k++)
+      if (neigh) neigh[o++] = lst[(size_t) k * h->estride + i];
+  }
+  API_END
+}
+
+int cacg_get_ip_list(cacg_handle h, int *numneigh, int *jelem, int *jsite) {
+  API_BEGIN
+  if (!h->elists_built) fail(CACG_ESTATE, "node neighbor list not built");
+  int n = h->nrows;
+  if (!n) return CACG_OK;
+  std::vector<int> num(n), lst((size_t) h->maxip * h->rowstride);
+  check(cudaMemcpyAsync(num.data(), h->d_ipnum.p, sizeof(int) * n, cudaMemcpyDeviceToHost, h->stream), "ipnum");
+  check(cudaMemcpyAsync(lst.data(), h->d_ipent.p, sizeof(int) * lst.size(), cudaMemcpyDeviceToHost, h->stream), "ipent");
+  h->sync();
+  size_t o = 0;
+  const std::vector<int> &sb = h->h_site_base;
+  for (int r = 0; r < n; r++) {
+    if (numneigh) numneigh[r] = num[r];
+    for (int k = 0; k < num[r]; k++) {
+      int sid = lst[(size_t) k * h->rowstride + r];
+      int e = (int) (std::upper_bound(sb.begin(), sb.end(), sid) - sb.begin()) - 1;
+      if (jelem) jelem[o] = e;
+      if (jsite) jsite[o] = sid - sb[e];
+      o++;
+    }
+  }
+  API_END
+}
+
+int cacg_get_cut(cacg_handle h, int what, double *value) {
+  API_BEGIN
+  if (!value) fail(CACG_EINVAL, "null argument");
+  double v[6] = {h->cutneighmax, h->cut_all, h->cut_ele, h->cut_subele, h->max_size, (double) h->nsub};
+  if (what < 0 || what > 5) fail(CACG_EINVAL, "unknown cutoff index");
+  *value = v[what];
+  API_END
+}
+
+int cacg_set_timing(cacg_handle h, int enable) {
+  API_BEGIN
+  h->timing = enable != 0;
+  API_END
+}
+
+int cacg_get_timing(cacg_handle h, double *ms, int n) {
+  API_BEGIN
+  for (int i = 0; i < n && i < 8; i++) ms[i] = h->t_ms[i];
+  API_END
+}
+
+int cacg_put_atoms(cacg_handle h, const double *x, const double *v) {
+  API_BEGIN
+  if (!h->inited) fail(CACG_ESTATE, "no device state yet (cacg_init)");
+  int n = h->nlocal;
+  if (n && x) {
+    // interleave into the device's padded layout through a staging copy
+    static thread_local std::vector<double4> x4;
+    x4.resize(n);
+    for (int i = 0; i < n; i++) x4[i] = make_double4(x[3 * i], x[3 * i + 1], x[3 * i + 2], 0.0);
+    check(cudaMemcpyAsync(h->d_x.p, x4.data(), sizeof(double4) * n, cudaMemcpyHostToDevice, h->stream), "put x");
+    h->sync();
+  }
+  if (n && v) check(cudaMemcpyAsync(h->d_v.p, v, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, h->stream), "put v");
+  API_END
+}
+
+int cacg_put_nodes(cacg_handle h, const double *nodex, const double *nodev) {
+  API_BEGIN
+  if (!h->inited) fail(CACG_ESTATE, "no device state yet (cacg_init)");
+  int n = h->enlocal;
+  if (n && nodex) check(cudaMemcpyAsync(h->d_nodex.p, nodex, sizeof(double) * 24 * n, cudaMemcpyHostToDevice, h->stream), "put nodex");
+  if (n && nodev) check(cudaMemcpyAsync(h->d_nodev.p, nodev, sizeof(double) * 24 * n, cudaMemcpyHostToDevice, h->stream), "put nodev");
+  API_END
+}
+
+int cacg_measure_fp64_peak(cacg_handle h, double *flops) {
+  API_BEGIN
+  if (!flops) fail(CACG_EINVAL, "null argument");
+  *flops = fp64_fma_rate(h->stream);
+  API_END
+}
+
+}  // extern "C"

@@ -1,0 +1,201 @@
+// Internal declarations shared by the host orchestration (host.cpp) and the
+// CUDA kernels (k_*.cu) of libcacg.so.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace cacg {
+
+constexpr int NPE = 8;    // nodes per 3-d element (element.cpp:41)
+constexpr int MAXT = 8;   // atom / element types supported
+
+// Error from a CUDA call, turned into CACG_ECUDA at the ABI boundary.
+struct CudaError {
+  cudaError_t code;
+  const char *where;
+};
+
+inline void check(cudaError_t e, const char *where) {
+  if (e != cudaSuccess) throw CudaError{e, where};
+}
+
+// Growable device array.  Growth keeps contents when asked (ghost appends).
+template <class T>
+struct DBuf {
+  T *p = nullptr;
+  size_t cap = 0;
+  void ensure(size_t n, cudaStream_t s, bool keep = false) {
+    if (n <= cap) return;
+    size_t ncap = cap ? cap : 256;
+    while (ncap < n) ncap = ncap + ncap / 2 + 256;
+    T *q = nullptr;
+    check(cudaMalloc(&q, ncap * sizeof(T)), "cudaMalloc");
+    if (keep && p && cap) check(cudaMemcpyAsync(q, p, cap * sizeof(T), cudaMemcpyDeviceToDevice, s), "grow copy");
+    if (p) {
+      check(cudaStreamSynchronize(s), "grow sync");
+      cudaFree(p);
+    }
+    p = q;
+    cap = ncap;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+// Bin geometry of Neighbor::setup_bins (neighbor.cpp:828-976); coord2bin uses
+// the domain box lo/hi as bboxlo/bboxhi.
+struct BinGeom {
+  double lo[3], hi[3];
+  double bininv[3];
+  int nbin[3];
+  int mlo[3];
+  int mbin[3];
+  int mbins;
+};
+
+// Shape-function and sub-element tables on the device (element.cpp:725-1423).
+struct ElemTables {
+  const double *spa_int;        // [sum numint][8], rows of type t start at int_off[t]
+  const double *weight;         // [sum numint]
+  const double *spa_inter;      // [sum ninter][8], type t starts at inter_off[t]
+  const int *int_off;           // [MAXT+1]
+  const int *inter_off;         // [MAXT+1]
+  const int *numint;            // [MAXT+1]
+  const int *inter_num;         // [MAXT+1]
+  const int *node_list;         // [(MAXT+1)*8]
+  const double *spa_center_sub; // [nsub][8]
+  const double *spa_inter_sub;  // [total][8]
+  const int *list_inter_sub;    // [total]
+  const int *sub_first;         // [nsub+1]
+  int nsub;
+};
+
+struct EamTables {
+  const double *frho;  // [(nrho+1)*7]
+  const double *rhor;  // [(nr+1)*7]
+  const double *z2r;   // [(nr+1)*7]
+  int nr, nrho;
+  double rdr, rdrho, cutforcesq;
+};
+
+// ---- scan / compaction (k_comm.cu) ----
+void scan_exclusive(const int *in, int *out, int n, int *total, DBuf<int> &scratch,
+                    cudaStream_t s);
+
+// ---- ghosts, wrap, bins (k_comm.cu) ----
+void launch_border_flags_atoms(const double4 *x, int nfirst, int nlast, int dim, double lo,
+                               double hi, int *flags, cudaStream_t s);
+void launch_border_flags_elems(const double *ex, const int *etype, int nfirst, int nlast,
+                               int dim, const double *mlo, const double *mhi, int *flags,
+                               cudaStream_t s);
+void launch_border_scatter_atoms(double4 *x, int *type, int *tag, int *root, int *sendlist,
+                                 const int *flags, const int *pos, int nfirst, int nlast,
+                                 int n0, double dx, double dy, double dz, cudaStream_t s);
+void launch_border_scatter_elems(double *ex, double *nodex, int *etype, int *etag, int *eroot,
+                                 int *sendlist, const int *flags, const int *pos, int nfirst,
+                                 int nlast, int n0, double dx, double dy, double dz,
+                                 cudaStream_t s);
+void launch_forward_atoms(double4 *x, const int *sendlist, int n, int first, double dx,
+                          double dy, double dz, cudaStream_t s);
+void launch_forward_elems(double *nodex, const int *sendlist, int n, int first, double dx,
+                          double dy, double dz, cudaStream_t s);
+void launch_copy_root(double *a, int width, const int *root, int gfirst, int gn,
+                      cudaStream_t s);
+void launch_pbc_atoms(double4 *x, int n, const double *lo, const double *hi,
+                      const double *prd, const int *periodic, cudaStream_t s);
+void launch_pbc_elems(double *ex, double *nodex, int n, const double *lo, const double *hi,
+                      const double *prd, const int *periodic, cudaStream_t s);
+void launch_coord2bin_atoms(const double4 *x, int n, const BinGeom &g, int *bin, int *oob,
+                            cudaStream_t s);
+void launch_coord2bin_elems(const double *ex, int n, const BinGeom &g, int *bin, int *oob,
+                            cudaStream_t s);
+// counting sort by bin, members of a bin in ascending index order
+void build_bins(const int *bin, int n, int mbins, DBuf<int> &count, DBuf<int> &start,
+                DBuf<int> &members, DBuf<int> &scratch, cudaStream_t s);
+void launch_gather_bin_x_atoms(const int *members, const double4 *x, double4 *bx, int n,
+                               cudaStream_t s);
+void launch_gather_bin_x_elems(const int *members, const double *ex, double4 *bx, int n,
+                               cudaStream_t s);
+
+// ---- neighbor lists (k_neigh.cu) ----
+void launch_atom_list(const double4 *x, const int *bin, const int *bstart, const int *bmem,
+                      const double4 *bx, const int *stencil, int nstencil, int mbins, int nlocal,
+                      double cutsq, int maxneigh, int stride, int *num, int *list,
+                      int *overflow, cudaStream_t s);
+void launch_elem_list(const double *ex, const int *bin, const int *bstart, const int *bmem,
+                      const double4 *bx, const int *stencil, int nstencil, int mbins, int nlocal,
+                      double cutsq, int maxneigh, int stride, int *num, int *list,
+                      int *overflow, cudaStream_t s);
+void launch_sites(const double *nodex, const int *etype, const int *site_base, int nelem,
+                  ElemTables t, double4 *site_x, cudaStream_t s);
+void launch_sub_centres(const double *nodex, int nelem, ElemTables t, double4 *subc,
+                        cudaStream_t s);
+void launch_ip_list(const double *nodex, const double *ex, const int *etype,
+                    const int *row_elem, const int *row_jj, int nrows, const int *enum_,
+                    const int *elist, int estride, const double4 *subc, const double4 *site_x,
+                    const int *site_base, ElemTables t, double cut_elesq, double cut_subelesq,
+                    double cutsq, int maxip, int rowstride, int *ipnum, int *ipent,
+                    int *overflow, cudaStream_t s);
+
+// ---- forces: same kernels in two translation units (force_fp64.cuh) ----
+// fp64_exact (k_force_exact.cu, -fmad=false) and fp64_fma (k_force_fma.cu).
+#define CACG_FORCE_DECLS                                                                   \
+  void lj_atoms(const double4 *x, const int *type, const int *num, const int *list,         \
+                int stride, int nlocal, const void *tab, double *f, cudaStream_t s);        \
+  void eam_rho_atoms(const double4 *x, const int *num, const int *list, int stride,         \
+                     int nlocal, EamTables e, double *rho, double *fp, cudaStream_t s);     \
+  void eam_force_atoms(const double4 *x, const int *num, const int *list, int stride,       \
+                       int nlocal, EamTables e, const double *fp, double *f,                \
+                       cudaStream_t s);                                                     \
+  void lj_ip(const double *nodex, const int *etype, const int *row_elem, const int *row_jj, \
+             int nrows, const int *ipnum, const int *ipent, int rowstride,                  \
+             const double4 *site_x, ElemTables t, double lj1, double lj2, double cutsq,      \
+             double *fip, cudaStream_t s);                                                  \
+  void eam_erho(const double *nodex, const int *etype, const int *row_first, int nlocal_e,  \
+                const int *ipnum, const int *ipent, int rowstride, const double4 *site_x,   \
+                ElemTables t, EamTables e, double *erho, cudaStream_t s);                   \
+  void eam_site_fp(const double *erho, const int *etype, const int *site_base, int nelem,   \
+                   ElemTables t, EamTables e, double *site_fp, cudaStream_t s);             \
+  void eam_ip(const double *nodex, const double *erho, const int *etype,                    \
+              const int *row_elem, const int *row_jj, int nrows, const int *ipnum,          \
+              const int *ipent, int rowstride, const double4 *site_x,                       \
+              const double *site_fp, ElemTables t, EamTables e, double *fip,                \
+              cudaStream_t s);                                                              \
+  void gather_nodef(const double *fip, const int *etype, const int *row_first,              \
+                    int nlocal_e, ElemTables t, double *nodef, cudaStream_t s);
+
+namespace fp64_exact {
+CACG_FORCE_DECLS
+}
+namespace fp64_fma {
+CACG_FORCE_DECLS
+}
+
+// ---- integration and reductions (k_nve.cu) ----
+void launch_nve_atoms_initial(double4 *x, double *v, const double *f, const int *type,
+                              const double *mass, int n, double dtv, double dtf,
+                              cudaStream_t s);
+void launch_nve_atoms_final(double *v, const double *f, const int *type, const double *mass,
+                            int n, double dtf, cudaStream_t s);
+void launch_nve_nodes_initial(double *ex, double *nodex, double *nodev, const double *nodef,
+                              const int *etype, const double *emass, int n, double dtv,
+                              double dtf, cudaStream_t s);
+void launch_nve_nodes_final(double *nodev, const double *nodef, const int *etype,
+                            const double *emass, int n, double dtf, cudaStream_t s);
+void launch_check_distance(const double4 *x, const double *xhold, int n,
+                           const double *nodex, const double *nodexhold, int ne,
+                           double triggersq, int *flag, cudaStream_t s);
+void launch_hold_atoms(const double4 *x, double *xhold, int n, cudaStream_t s);
+void launch_elem_diag(const double *nodex, const double *ex, int n, double *diag,
+                      int *centre_bad, cudaStream_t s);
+double fp64_fma_rate(cudaStream_t s);
+
+}  // namespace cacg

@@ -1,0 +1,233 @@
+// Velocity-Verlet for atoms and element nodes, rebuild check and element-size
+// reduction (sm_103a).  Compiled without contraction so the updates are the
+// reference's own multiply-then-add sequences (FixNVE, fix_nve.cpp:54-242).
+#include "internal.h"
+
+namespace cacg {
+
+namespace {
+
+inline int nblk(long long n, int t) { return (int) ((n + t - 1) / t); }
+
+// FixNVE::initial_integrate, fix_nve.cpp:54-98 (per-type mass branch)
+__global__ void k_nve_atoms_initial(double4 *__restrict__ x, double *__restrict__ v,
+                                    const double *__restrict__ f, const int *__restrict__ type,
+                                    const double *__restrict__ mass, int n, double dtv,
+                                    double dtf) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double dtfm = dtf / mass[type[i]];
+  double vx = v[3 * i] + dtfm * f[3 * i];
+  double vy = v[3 * i + 1] + dtfm * f[3 * i + 1];
+  double vz = v[3 * i + 2] + dtfm * f[3 * i + 2];
+  v[3 * i] = vx;
+  v[3 * i + 1] = vy;
+  v[3 * i + 2] = vz;
+  double4 p = x[i];
+  p.x = p.x + dtv * vx;
+  p.y = p.y + dtv * vy;
+  p.z = p.z + dtv * vz;
+  x[i] = p;
+}
+
+// FixNVE::final_integrate, fix_nve.cpp:181-212
+__global__ void k_nve_atoms_final(double *__restrict__ v, const double *__restrict__ f,
+                                  const int *__restrict__ type, const double *__restrict__ mass,
+                                  int n, double dtf) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double dtfm = dtf / mass[type[i]];
+  v[3 * i] = v[3 * i] + dtfm * f[3 * i];
+  v[3 * i + 1] = v[3 * i + 1] + dtfm * f[3 * i + 1];
+  v[3 * i + 2] = v[3 * i + 2] + dtfm * f[3 * i + 2];
+}
+
+// FixNVE::einitial_integrate, fix_nve.cpp:100-157: nodal mass M_e/8, then the
+// centre is recomputed as the mean of the nodes
+__global__ void k_nve_nodes_initial(double *__restrict__ ex, double *__restrict__ nodex,
+                                    double *__restrict__ nodev,
+                                    const double *__restrict__ nodef,
+                                    const int *__restrict__ etype,
+                                    const double *__restrict__ emass, int n, double dtv,
+                                    double dtf) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double inv_npe = 1 / (double) NPE;
+  double dtfm = dtf / (inv_npe * emass[etype[i]]);
+  double c[3] = {0.0, 0.0, 0.0};
+  for (int q = 0; q < NPE; q++) {
+    for (int d = 0; d < 3; d++) {
+      size_t k = 24 * (size_t) i + 3 * q + d;
+      double vv = nodev[k] + dtfm * nodef[k];
+      nodev[k] = vv;
+      nodex[k] = nodex[k] + dtv * vv;
+    }
+  }
+  for (int q = 0; q < NPE; q++)
+    for (int d = 0; d < 3; d++) c[d] += nodex[24 * (size_t) i + 3 * q + d];
+  for (int d = 0; d < 3; d++) ex[3 * i + d] = c[d] / NPE;
+}
+
+// FixNVE::efinal_integrate, fix_nve.cpp:216-242
+__global__ void k_nve_nodes_final(double *__restrict__ nodev, const double *__restrict__ nodef,
+                                  const int *__restrict__ etype,
+                                  const double *__restrict__ emass, int n, double dtf) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * 24) return;
+  int i = t / 24;
+  const double inv_npe = 1 / (double) NPE;
+  double dtfm = dtf / (inv_npe * emass[etype[i]]);
+  nodev[t] = nodev[t] + dtfm * nodef[t];
+}
+
+// Neighbor::check_distance, neighbor.cpp:1176-1217
+__global__ void k_check_distance(const double4 *__restrict__ x, const double *__restrict__ xh,
+                                 int n, const double *__restrict__ nodex,
+                                 const double *__restrict__ nodexh, int ne, double triggersq,
+                                 int *__restrict__ flag) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  bool hit = false;
+  if (t < n) {
+    double4 p = x[t];
+    double dx = p.x - xh[3 * t], dy = p.y - xh[3 * t + 1], dz = p.z - xh[3 * t + 2];
+    hit = dx * dx + dy * dy + dz * dz > triggersq;
+  } else if (t < n + ne * NPE) {
+    size_t k = 3 * (size_t) (t - n);
+    double dx = nodex[k] - nodexh[k], dy = nodex[k + 1] - nodexh[k + 1],
+           dz = nodex[k + 2] - nodexh[k + 2];
+    hit = dx * dx + dy * dy + dz * dz > triggersq;
+  }
+  if (__any_sync(0xffffffffu, hit) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
+__global__ void k_hold_atoms(const double4 *__restrict__ x, double *__restrict__ xh, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double4 p = x[i];
+  xh[3 * i] = p.x;
+  xh[3 * i + 1] = p.y;
+  xh[3 * i + 2] = p.z;
+}
+
+// Per-element longest body diagonal (Element::element_size, element.cpp:567-625)
+// and the centre-versus-node-mean check (element.cpp:608-622).
+__global__ void k_elem_diag(const double *__restrict__ nodex, const double *__restrict__ ex,
+                            int n, double *__restrict__ diag, int *__restrict__ bad) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double *nx = nodex + 24 * (size_t) i;
+  double length = 0.0;
+  for (int j = 0; j < 4; j++) {
+    int o = j < 2 ? j + 6 : j + 2;
+    double lx = nx[3 * j] - nx[3 * o], ly = nx[3 * j + 1] - nx[3 * o + 1],
+           lz = nx[3 * j + 2] - nx[3 * o + 2];
+    double l = sqrt(lx * lx + ly * ly + lz * lz);
+    length = length > l ? length : l;
+  }
+  diag[i] = length;
+  double c[3] = {0.0, 0.0, 0.0};
+  for (int q = 0; q < NPE; q++)
+    for (int d = 0; d < 3; d++) c[d] += nx[3 * q + d];
+  for (int d = 0; d < 3; d++) c[d] = c[d] / NPE;
+  double dist = (c[0] - ex[3 * i]) * (c[0] - ex[3 * i]) +
+                (c[1] - ex[3 * i + 1]) * (c[1] - ex[3 * i + 1]) +
+                (c[2] - ex[3 * i + 2]) * (c[2] - ex[3 * i + 2]);
+  if (dist > 0.01) atomicAdd(bad, 1);
+}
+
+// Dependent chains of FP64 fused multiply-adds: 8 independent chains per
+// thread keep the FP64 pipe busy; the result is written so nothing is elided.
+__global__ void k_fma_loop(double *out, int iters) {
+  double a0 = threadIdx.x * 1e-9, a1 = a0 + 1e-9, a2 = a0 + 2e-9, a3 = a0 + 3e-9;
+  double a4 = a0 + 4e-9, a5 = a0 + 5e-9, a6 = a0 + 6e-9, a7 = a0 + 7e-9;
+  const double b = 0.999999, c = 1e-7;
+  for (int k = 0; k < iters; k++) {
+    a0 = fma(a0, b, c); a1 = fma(a1, b, c); a2 = fma(a2, b, c); a3 = fma(a3, b, c);
+    a4 = fma(a4, b, c); a5 = fma(a5, b, c); a6 = fma(a6, b, c); a7 = fma(a7, b, c);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
+
+}  // namespace
+
+void launch_nve_atoms_initial(double4 *x, double *v, const double *f, const int *type,
+                              const double *mass, int n, double dtv, double dtf,
+                              cudaStream_t s) {
+  if (n <= 0) return;
+  k_nve_atoms_initial<<<nblk(n, 256), 256, 0, s>>>(x, v, f, type, mass, n, dtv, dtf);
+  check(cudaGetLastError(), "nve_atoms_initial");
+}
+
+void launch_nve_atoms_final(double *v, const double *f, const int *type, const double *mass,
+                            int n, double dtf, cudaStream_t s) {
+  if (n <= 0) return;
+  k_nve_atoms_final<<<nblk(n, 256), 256, 0, s>>>(v, f, type, mass, n, dtf);
+  check(cudaGetLastError(), "nve_atoms_final");
+}
+
+void launch_nve_nodes_initial(double *ex, double *nodex, double *nodev, const double *nodef,
+                              const int *etype, const double *emass, int n, double dtv,
+                              double dtf, cudaStream_t s) {
+  if (n <= 0) return;
+  k_nve_nodes_initial<<<nblk(n, 128), 128, 0, s>>>(ex, nodex, nodev, nodef, etype, emass, n,
+                                                    dtv, dtf);
+  check(cudaGetLastError(), "nve_nodes_initial");
+}
+
+void launch_nve_nodes_final(double *nodev, const double *nodef, const int *etype,
+                            const double *emass, int n, double dtf, cudaStream_t s) {
+  if (n <= 0) return;
+  k_nve_nodes_final<<<nblk((long long) n * 24, 256), 256, 0, s>>>(nodev, nodef, etype, emass,
+                                                                   n, dtf);
+  check(cudaGetLastError(), "nve_nodes_final");
+}
+
+void launch_check_distance(const double4 *x, const double *xhold, int n,
+                           const double *nodex, const double *nodexhold, int ne,
+                           double triggersq, int *flag, cudaStream_t s) {
+  long long tot = (long long) n + (long long) ne * NPE;
+  if (tot <= 0) return;
+  k_check_distance<<<nblk(tot, 256), 256, 0, s>>>(x, xhold, n, nodex, nodexhold, ne,
+                                                   triggersq, flag);
+  check(cudaGetLastError(), "check_distance");
+}
+
+void launch_hold_atoms(const double4 *x, double *xhold, int n, cudaStream_t s) {
+  if (n <= 0) return;
+  k_hold_atoms<<<nblk(n, 256), 256, 0, s>>>(x, xhold, n);
+  check(cudaGetLastError(), "hold_atoms");
+}
+
+void launch_elem_diag(const double *nodex, const double *ex, int n, double *diag,
+                      int *centre_bad, cudaStream_t s) {
+  if (n <= 0) return;
+  k_elem_diag<<<nblk(n, 128), 128, 0, s>>>(nodex, ex, n, diag, centre_bad);
+  check(cudaGetLastError(), "elem_diag");
+}
+
+double fp64_fma_rate(cudaStream_t s) {
+  int dev = 0;
+  check(cudaGetDevice(&dev), "getdevice");
+  int nsm = 0;
+  check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "attr");
+  const int threads = 256, blocks = nsm * 8, iters = 4096;
+  double *out = nullptr;
+  check(cudaMalloc(&out, sizeof(double) * threads * blocks), "malloc fma");
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  k_fma_loop<<<blocks, threads, 0, s>>>(out, iters);  // warm-up
+  cudaEventRecord(a, s);
+  k_fma_loop<<<blocks, threads, 0, s>>>(out, iters);
+  cudaEventRecord(b, s);
+  check(cudaEventSynchronize(b), "fma sync");
+  float ms = 0;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(out);
+  double flops = 2.0 * 8.0 * (double) iters * threads * blocks;
+  return ms > 0 ? flops / (ms * 1e-3) : 0.0;
+}
+
+}  // namespace cacg

@@ -1,0 +1,127 @@
+/*
+ * cacg.h -- C ABI of the GB300 CAC force path (libcacg.so).
+ *
+ * One handle owns one CAC system resident on one GPU: atoms (x, v, f, type),
+ * 8-node elements (nodes, centres, velocities, forces), their ghost images,
+ * bins, the three neighbor lists and the pair-style tables.  Every entry
+ * point returns 0 on success or a negative status; cacg_error() gives the
+ * message.  Plain pointers and sizes only; host arrays are caller-owned and
+ * copied in or out.  One host thread per handle.
+ *
+ * Each entry point replaces the reference routine named beside it (file:line in
+ * fangyuanxiao/CAC_Code).  Where the reference is a C++ virtual (Pair,
+ * Neighbor, Fix), the plug-in shim that calls this ABI is shown in
+ * INTEGRATION.md.
+ */
+#ifndef CACG_H
+#define CACG_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct cacg_context *cacg_handle;
+
+/* status codes */
+#define CACG_OK 0
+#define CACG_EINVAL (-1)     /* bad argument or command (error->all in the reference) */
+#define CACG_ESTATE (-2)     /* call out of order (e.g. forces before lists) */
+#define CACG_ECUDA (-3)      /* CUDA runtime error */
+#define CACG_EOVERFLOW (-4)  /* neighbor list overflow that regrowing could not fix */
+#define CACG_EIO (-5)        /* file could not be read */
+#define CACG_ENOMEM (-6)     /* device allocation failed */
+#define CACG_ETIMEOUT (-7)   /* a bounded device wait ran out */
+
+/* precision modes (cacg_set_precision) */
+#define CACG_FP64_EXACT 0    /* reference operation order, no contraction: bit-identical */
+#define CACG_FP64 1          /* FP64 with fused multiply-add */
+#define CACG_MIXED 2         /* FP32 pair terms, FP64 accumulation and integration */
+
+/* ---- lifetime (CAC::CAC / CAC::~CAC, cac.cpp:29-148) ---- */
+int cacg_create(cacg_handle *out, int device);
+int cacg_destroy(cacg_handle h);
+const char *cacg_error(cacg_handle h);
+const char *cacg_version(void);
+
+/* ---- input commands (Input::execute_command, input.cpp:362-404) ----
+ * Accepts: units lj|metal, boundary, dimension 3, timestep, elementsplit,
+ * read_data FILE, pair_style lj/cut RC | eam, pair_coeff, neighbor SKIN bin,
+ * neigh_modify every/delay/check/binsize/one/page, fix ID all nve, run N. */
+int cacg_command(cacg_handle h, const char *line);
+/* Input::file, input.cpp:95-194: every line of an input script */
+int cacg_file(cacg_handle h, const char *path);
+
+/* ---- direct state (ReadData::command sections, read_data.cpp:166-211) ---- */
+int cacg_set_box(cacg_handle h, const double *lo, const double *hi, const int *periodic);
+int cacg_set_masses(cacg_handle h, int ntypes, const double *mass);         /* Masses */
+int cacg_set_atoms(cacg_handle h, int n, const double *x, const double *v,
+                   const int *type);                                          /* Atoms */
+int cacg_set_element_types(cacg_handle h, int ntypes, const int *nae,
+                           const int *numint, const int *intp,
+                           const double *weight);                 /* NAAE, Numint, Intp */
+int cacg_set_elements(cacg_handle h, int n, const int *etype, const double *centre,
+                      const double *nodex, const double *nodev);      /* Elements, Nodes */
+int cacg_set_precision(cacg_handle h, int mode);
+
+/* ---- init and setup ---- */
+int cacg_init(cacg_handle h);       /* CAC::init, cac.cpp:202-213 (tables, cutoffs) */
+int cacg_setup(cacg_handle h);      /* Verlet::setup through comm->borders, verlet.cpp:70-90 */
+
+/* ---- neighbor (Neighbor::build/ebuild/nbuild, neighbor.h:74-76) ---- */
+int cacg_neighbor_build(cacg_handle h);    /* neighbor.cpp:984-1018 half_bin_no_newton (full) */
+int cacg_neighbor_ebuild(cacg_handle h);   /* neighbor.cpp:1022-1062 element_neighbor */
+int cacg_neighbor_nbuild(cacg_handle h);   /* neighbor.cpp:1096-1106 node_neighbor */
+
+/* ---- pair (Pair::compute / Pair::ecompute, pair.h:82-105) ---- */
+int cacg_pair_compute(cacg_handle h, int eflag, int vflag);  /* atoms: f = sum over list */
+int cacg_pair_ecompute(cacg_handle h);  /* integration points -> nodef (zeroed first) */
+
+/* ---- FixNVE (fix_nve.cpp:54-242), atoms and nodes ---- */
+int cacg_fix_nve_initial_integrate(cacg_handle h);
+int cacg_fix_nve_final_integrate(cacg_handle h);
+
+/* ---- Verlet::run, verlet.cpp:149-219 (atoms also get Pair::compute) ---- */
+int cacg_run(cacg_handle h, int nsteps);
+
+/* ---- host-owned state in (drop-in callers keep Atom::x/v and Element::nodex/nodev,
+   atom.h:40, element.h:25, in host memory and push them every step) ---- */
+int cacg_put_atoms(cacg_handle h, const double *x, const double *v);      /* [nlocal][3] */
+int cacg_put_nodes(cacg_handle h, const double *nodex, const double *nodev); /* [n][8][3] */
+
+/* ---- state out ---- */
+/* counts: 0 nlocal 1 nghost 2 atom-list entries 3 elem nlocal 4 elem nghost
+   5 element-list entries 6 integration-point rows 7 ip-list entries
+   8 rebuilds so far 9 stencil bins 10 step number 11 interpolated sites
+   12 kernel launches issued */
+int cacg_get_counts(cacg_handle h, long long *counts, int n);
+/* Atom::x/v/f (atom.h:40); all != 0 includes ghosts for x and tag */
+int cacg_get_atoms(cacg_handle h, int all, double *x, double *v, double *f, int *tag);
+/* Element::x/nodex/nodev/nodef (element.h:25) */
+int cacg_get_elements(cacg_handle h, int all, double *centre, double *nodex, double *nodev,
+                      double *nodef, int *tag);
+/* NeighList ilist/numneigh/firstneigh (neigh_list.h:26-33), indices in the
+   reference's local+ghost numbering, rows concatenated */
+int cacg_get_atom_list(cacg_handle h, int *numneigh, int *neigh);
+int cacg_get_elem_list(cacg_handle h, int *numneigh, int *neigh);
+/* NodeNeighList numneigh/firstneigh/nfirstneigh (node_neigh_list.h:23-27) */
+int cacg_get_ip_list(cacg_handle h, int *numneigh, int *jelem, int *jsite);
+/* 0 cutneighmax 1 cut_all 2 cut_ele 3 cut_subele 4 max_size 5 nsubele */
+int cacg_get_cut(cacg_handle h, int what, double *value);
+
+/* ---- measurement ---- */
+/* Phase timing of the last cacg_run from CUDA events on the handle's stream
+   (recorded only after cacg_set_timing(h, 1)): ms[0] total, [1] integrate +
+   rebuild decision + ghost refresh or rebuild, [2] atom pass 1 (LJ force or
+   EAM density), [3] atom pass 2 (EAM force), [4] element forces and nodal
+   gather, [5] final integrate; each summed over the steps of the run. */
+int cacg_set_timing(cacg_handle h, int enable);
+int cacg_get_timing(cacg_handle h, double *ms, int n);
+/* Device-time of a FP64 fused-multiply-add loop on this GPU, for the FP64 roof:
+   returns achieved FP64 FLOP/s in *flops. */
+int cacg_measure_fp64_peak(cacg_handle h, double *flops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
