@@ -42,7 +42,8 @@ def parse():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--mode", default="fp64", choices=["fp64", "exact", "mixed"])
-    p.add_argument("--small", action="store_true", help="the 8,000-atom C2 sample (profiling)")
+    p.add_argument("--size", default="full", choices=["full", "medium", "small"],
+                   help="full C2; medium = 360,000-atom slab (profiling, > L2); small = 8,000 atoms")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     return p.parse_args()
@@ -185,13 +186,18 @@ def run_ours(a, ws, rank, local):
     if rank == 0 and ws == 1 and not a.no_cpu_baseline:
         # before the first GPU call: spawn the host-core sample
         cores = os.cpu_count() or 1
-        val, wall = cpu_leg(cores, 3, 1, eam)
+        val, wall = cpu_leg(cores, 60, 2, eam)
         cpu = {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"{cores} independent 8,000-atom + 160-element C2-structured replicas "
-                         f"(CPU restatement of the reference, oracle/cac_oracle.c), 3 timed steps "
-                         f"each after 1 warm-up, {wall:.1f} s"}
+                         f"(CPU restatement of the reference, oracle/cac_oracle.c, -O3), 60 timed "
+                         f"steps each after 2 warm-up, {wall:.1f} s"}
 
-    m, cfg = (W.c2_sample(seed=5) if a.small else W.c2_eam())
+    if a.size == "small":
+        m, cfg = W.c2_sample(seed=5)
+    elif a.size == "medium":
+        m, cfg = W.c2_eam(cells=(25, 60, 60), layers=50)
+    else:
+        m, cfg = W.c2_eam()
     sites = W.metric_sites(m, cfg)
     s = cacg.System(local)
     W.configure_system(s, m, cfg, eam)
@@ -296,8 +302,10 @@ def run_ours(a, ws, rank, local):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if a.mode != "mixed" else "f32+f64", "data": "synthetic",
             "config": {
-                "workload": ("C2 sample: EAM Cu 8,000 atoms + 160 elements" if a.small else
-                             "C2: EAM Cu CAC slab, 1,000,000 atoms + 20,000 elements (10 sites/edge), FP64"),
+                "workload": {"small": "C2 sample: EAM Cu 8,000 atoms + 160 elements",
+                             "medium": "C2 medium: EAM Cu 360,000 atoms + 7,200 elements",
+                             "full": "C2: EAM Cu CAC slab, 1,000,000 atoms + 20,000 elements "
+                                     "(10 sites/edge), FP64"}[a.size],
                 "mode": a.mode, "atoms": c0["nlocal"], "ghost_atoms": c0["nghost"],
                 "elements": c0["enlocal"], "ghost_elements": c0["enghost"],
                 "gauss_points": cfg["gauss_per_element"] * c0["enlocal"],
@@ -333,8 +341,8 @@ def run_reference(a, ws, rank):
     tmp = tempfile.mkdtemp(prefix="cacref_bench_")
     eam = W.write_eam(os.path.join(tmp, "Cu_analytic_2000.eam"))
     cores = os.cpu_count() or 1
-    steps = max(1, min(a.steps, 3))
-    val, wall = cpu_leg(cores, steps, 1, eam)
+    steps = max(1, min(a.steps, 200))
+    val, wall = cpu_leg(cores, steps, max(1, min(a.warmup, 5)), eam)
     line = {
         "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": ws,
         "steps": steps, "warmup": 1, "ms_per_step": None, "higher_is_better": True,

@@ -194,6 +194,7 @@ struct cacg_context {
 
   // device arrays: atoms
   DBuf<double4> d_x;
+  DBuf<float4> d_xh, d_site_h;  // float copies for the FP32 cutoff pre-tests
   DBuf<double> d_v, d_f, d_xhold, d_rho, d_fp, d_mass;
   DBuf<int> d_type, d_tag, d_root, d_send;
   DBuf<int> d_abin, d_bcount, d_bstart, d_bmem, d_stencil;
@@ -271,6 +272,34 @@ struct cacg_context {
     return e;
   }
 
+  // Float threshold for the FP32 pre-test of a pair against cutsq: any pair
+  // with exact rsq < cutsq has float rsq <= the returned value.  Coordinates
+  // are bounded by the box plus the ghost margin plus a motion allowance; each
+  // float coordinate is within u|x| (u = 2^-24) of the double, the float
+  // difference within a further u|dx|, and the float sum of squares within 3u.
+  float cut_pass(double cutsq) const {
+    double X = 0.0;
+    for (int d = 0; d < 3; d++)
+      X = std::max(X, std::max(std::fabs(lo[d]), std::fabs(hi[d])) + cutghost[d] + max_size +
+                          10.0 * skin + 1.0);
+    const double u = std::ldexp(1.0, -24);
+    const double rn = std::max(cutneighmax, std::sqrt(cutsq));
+    const double delta = 2.0 * u * X * 1.001 + u * (rn + 1.0);
+    const double guard = 4.0 * u * cutsq + (1.0 + 4.0 * u) * (2.0 * std::sqrt(3.0) * rn * delta +
+                                                              3.0 * delta * delta);
+    float c = (float) (cutsq + guard);
+    return std::nextafter(std::nextafter(c, 3.0e38f), 3.0e38f);
+  }
+  float atom_cut_pass() const {
+    if (pair_style == 2) return cut_pass(cutforcesq);
+    double mx = 0.0;
+    int nt = std::max(ntypes, 1);
+    for (int i = 1; i <= nt; i++)
+      for (int j = 1; j <= nt; j++) mx = std::max(mx, ljtab.cutsq[i * (MAXT + 1) + j]);
+    return cut_pass(mx);
+  }
+  bool fast() const { return mode != CACG_FP64_EXACT; }
+
   // ---- commands ----
   void command(const std::string &line);
   void read_data(const std::string &path);
@@ -307,6 +336,8 @@ struct cacg_context {
 cacg_context::~cacg_context() {
   DBuf<double4> *b4[] = {&d_x, &d_bx, &d_ebx, &d_site_x, &d_subc};
   for (auto *b : b4) b->release();
+  d_xh.release();
+  d_site_h.release();
   DBuf<double> *bd[] = {&d_v, &d_f, &d_xhold, &d_rho, &d_fp, &d_mass, &d_ex, &d_nodex, &d_nodev,
                         &d_nodef, &d_nodexhold, &d_erho, &d_emass, &d_diag, &d_fip, &d_site_fp,
                         &d_spa_int, &d_weight, &d_spa_inter, &d_spa_csub, &d_spa_isub, &d_frho,
@@ -1384,7 +1415,7 @@ void cacg_context::neighbor_nbuild() {
   int nall = enlocal + enghost;
   ElemTables t = etab();
   d_site_x.ensure(std::max(nsites, 1), s);
-  launch_sites(d_nodex.p, d_etype.p, d_site_base.p, nall, t, d_site_x.p, s);
+  launch_sites(d_nodex.p, d_etype.p, d_site_base.p, nall, t, d_site_x.p, nullptr, s);
   d_subc.ensure((size_t) nall * nsub, s);
   launch_sub_centres(d_nodex.p, nall, t, d_subc.p, s);
   launches += 2;
@@ -1421,27 +1452,33 @@ void cacg_context::pair_compute_pass(int pass) {
   if (nlocal == 0) return;
   if (!list_built) fail(CACG_ESTATE, "Pair::compute before the atom neighbor list is built");
   cudaStream_t s = stream;
-  bool exact = mode == CACG_FP64_EXACT;
+  bool exact = !fast();
+  int nall = nlocal + nghost;
+  if (pass == 1 && !exact) {
+    d_xh.ensure(nall, s);
+    launch_split_hi(d_x.p, d_xh.p, nall, s);
+    launches++;
+  }
+  const float cp = exact ? 0.f : atom_cut_pass();
   if (pair_style == 1) {
     if (pass != 1) return;
     if (exact) fp64_exact::lj_atoms(d_x.p, d_type.p, d_num.p, d_list.p, stride, nlocal, d_ljtab.p, d_f.p, s);
-    else fp64_fma::lj_atoms(d_x.p, d_type.p, d_num.p, d_list.p, stride, nlocal, d_ljtab.p, d_f.p, s);
+    else fp64_fma::lj_atoms(d_x.p, d_xh.p, d_type.p, d_num.p, d_list.p, stride, nlocal, d_ljtab.p, cp, d_f.p, s);
     launches++;
     return;
   }
   EamTables e = eamtab();
   if (pass == 1) {
-    int nall = nlocal + nghost;
     d_rho.ensure(nall, s);
     d_fp.ensure(nall, s);
     if (exact) fp64_exact::eam_rho_atoms(d_x.p, d_num.p, d_list.p, stride, nlocal, e, d_rho.p, d_fp.p, s);
-    else fp64_fma::eam_rho_atoms(d_x.p, d_num.p, d_list.p, stride, nlocal, e, d_rho.p, d_fp.p, s);
+    else fp64_fma::eam_rho_atoms(d_x.p, d_xh.p, d_num.p, d_list.p, stride, nlocal, e, cp, d_rho.p, d_fp.p, s);
     // forward_comm_pair: ghost fp = owner fp (comm_brick.cpp:941-971)
     launch_copy_root(d_fp.p, 1, d_root.p, nlocal, nghost, s);
     launches += 2;
   } else {
     if (exact) fp64_exact::eam_force_atoms(d_x.p, d_num.p, d_list.p, stride, nlocal, e, d_fp.p, d_f.p, s);
-    else fp64_fma::eam_force_atoms(d_x.p, d_num.p, d_list.p, stride, nlocal, e, d_fp.p, d_f.p, s);
+    else fp64_fma::eam_force_atoms(d_x.p, d_xh.p, d_num.p, d_list.p, stride, nlocal, e, cp, d_fp.p, d_f.p, s);
     launches++;
   }
 }
@@ -1450,11 +1487,12 @@ void cacg_context::pair_ecompute() {
   if (enlocal == 0) return;
   if (!elists_built) fail(CACG_ESTATE, "Pair::ecompute before the node neighbor list is built");
   cudaStream_t s = stream;
-  bool exact = mode == CACG_FP64_EXACT;
+  bool exact = !fast();
   int nall = enlocal + enghost;
   ElemTables t = etab();
   // sites of every local and ghost element at the current node positions
-  launch_sites(d_nodex.p, d_etype.p, d_site_base.p, nall, t, d_site_x.p, s);
+  if (!exact) d_site_h.ensure(std::max(nsites, 1), s);
+  launch_sites(d_nodex.p, d_etype.p, d_site_base.p, nall, t, d_site_x.p, exact ? nullptr : d_site_h.p, s);
   launches++;
   if (pair_style == 1) {
     int a = 1 * (MAXT + 1) + 1;
@@ -1463,16 +1501,18 @@ void cacg_context::pair_ecompute() {
                         rowstride, d_site_x.p, t, ljtab.lj1[a], ljtab.lj2[a], ljtab.cutsq[a], d_fip.p, s);
     else
       fp64_fma::lj_ip(d_nodex.p, d_etype.p, d_row_elem.p, d_row_jj.p, nrows, d_ipnum.p, d_ipent.p,
-                      rowstride, d_site_x.p, t, ljtab.lj1[a], ljtab.lj2[a], ljtab.cutsq[a], d_fip.p, s);
+                      rowstride, d_site_x.p, d_site_h.p, t, ljtab.lj1[a], ljtab.lj2[a], ljtab.cutsq[a],
+                      cut_pass(ljtab.cutsq[a]), d_fip.p, s);
     launches++;
   } else {
     EamTables e = eamtab();
+    const float cp = exact ? 0.f : cut_pass(cutforcesq);
     d_erho.ensure((size_t) NPE * nall, s);
     d_site_fp.ensure(std::max(nsites, 1), s);
     if (exact) {
       fp64_exact::eam_erho(d_nodex.p, d_etype.p, d_row_first.p, enlocal, d_ipnum.p, d_ipent.p, rowstride, d_site_x.p, t, e, d_erho.p, s);
     } else {
-      fp64_fma::eam_erho(d_nodex.p, d_etype.p, d_row_first.p, enlocal, d_ipnum.p, d_ipent.p, rowstride, d_site_x.p, t, e, d_erho.p, s);
+      fp64_fma::eam_erho(d_nodex.p, d_etype.p, d_row_first.p, enlocal, d_ipnum.p, d_ipent.p, rowstride, d_site_x.p, d_site_h.p, t, e, cp, d_erho.p, s);
     }
     // eforward_comm_pair: ghost nodal densities from their owners (comm_brick.cpp:978-1010)
     launch_copy_root(d_erho.p, NPE, d_eroot.p, enlocal, enghost, s);
@@ -1483,7 +1523,7 @@ void cacg_context::pair_ecompute() {
     } else {
       fp64_fma::eam_site_fp(d_erho.p, d_etype.p, d_site_base.p, nall, t, e, d_site_fp.p, s);
       fp64_fma::eam_ip(d_nodex.p, d_erho.p, d_etype.p, d_row_elem.p, d_row_jj.p, nrows, d_ipnum.p, d_ipent.p,
-                       rowstride, d_site_x.p, d_site_fp.p, t, e, d_fip.p, s);
+                       rowstride, d_site_x.p, d_site_h.p, d_site_fp.p, t, e, cp, d_fip.p, s);
     }
     launches += 4;
   }

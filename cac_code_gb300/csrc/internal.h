@@ -134,8 +134,10 @@ void launch_elem_list(const double *ex, const int *bin, const int *bstart, const
                       const double4 *bx, const int *stencil, int nstencil, int mbins, int nlocal,
                       double cutsq, int maxneigh, int stride, int *num, int *list,
                       int *overflow, cudaStream_t s);
+// site_h (may be null): float copy of each site for the FP32 pre-tests
 void launch_sites(const double *nodex, const int *etype, const int *site_base, int nelem,
-                  ElemTables t, double4 *site_x, cudaStream_t s);
+                  ElemTables t, double4 *site_x, float4 *site_h, cudaStream_t s);
+void launch_split_hi(const double4 *x, float4 *xh, int n, cudaStream_t s);
 void launch_sub_centres(const double *nodex, int nelem, ElemTables t, double4 *subc,
                         cudaStream_t s);
 void launch_ip_list(const double *nodex, const double *ex, const int *etype,
@@ -175,9 +177,35 @@ void launch_ip_list(const double *nodex, const double *ex, const int *etype,
 namespace fp64_exact {
 CACG_FORCE_DECLS
 }
+// fp64_fma (k_force_fma.cu): FP32 pre-test against cut_pass on the float
+// copies (xh, site_h), Newton-refined reciprocals, weight-0 rows skipped.
 namespace fp64_fma {
-CACG_FORCE_DECLS
-}
+void lj_atoms(const double4 *x, const float4 *xh, const int *type, const int *num,
+              const int *list, int stride, int nlocal, const void *tab, float cut_pass,
+              double *f, cudaStream_t s);
+void eam_rho_atoms(const double4 *x, const float4 *xh, const int *num, const int *list,
+                   int stride, int nlocal, EamTables e, float cut_pass, double *rho,
+                   double *fp, cudaStream_t s);
+void eam_force_atoms(const double4 *x, const float4 *xh, const int *num, const int *list,
+                     int stride, int nlocal, EamTables e, float cut_pass, const double *fp,
+                     double *f, cudaStream_t s);
+void lj_ip(const double *nodex, const int *etype, const int *row_elem, const int *row_jj,
+           int nrows, const int *ipnum, const int *ipent, int rowstride, const double4 *site_x,
+           const float4 *site_h, ElemTables t, double lj1, double lj2, double cutsq,
+           float cut_pass, double *fip, cudaStream_t s);
+void eam_erho(const double *nodex, const int *etype, const int *row_first, int nlocal_e,
+              const int *ipnum, const int *ipent, int rowstride, const double4 *site_x,
+              const float4 *site_h, ElemTables t, EamTables e, float cut_pass, double *erho,
+              cudaStream_t s);
+void eam_site_fp(const double *erho, const int *etype, const int *site_base, int nelem,
+                 ElemTables t, EamTables e, double *site_fp, cudaStream_t s);
+void eam_ip(const double *nodex, const double *erho, const int *etype, const int *row_elem,
+            const int *row_jj, int nrows, const int *ipnum, const int *ipent, int rowstride,
+            const double4 *site_x, const float4 *site_h, const double *site_fp, ElemTables t,
+            EamTables e, float cut_pass, double *fip, cudaStream_t s);
+void gather_nodef(const double *fip, const int *etype, const int *row_first, int nlocal_e,
+                  ElemTables t, double *nodef, cudaStream_t s);
+}  // namespace fp64_fma
 
 // ---- integration and reductions (k_nve.cu) ----
 void launch_nve_atoms_initial(double4 *x, double *v, const double *f, const int *type,

@@ -84,7 +84,7 @@ k_elem_list(const double *__restrict__ ex, const int *__restrict__ bin,
 // element.cpp:1226-1272): x = sum_k N_k x_k in node order.  One block per element.
 __global__ void k_sites(const double *__restrict__ nodex, const int *__restrict__ etype,
                         const int *__restrict__ site_base, ElemTables t,
-                        double4 *__restrict__ site_x) {
+                        double4 *__restrict__ site_x, float4 *__restrict__ site_h) {
   __shared__ double nx[24];
   const int e = blockIdx.x;
   if (threadIdx.x < 24) nx[threadIdx.x] = nodex[24 * (size_t) e + threadIdx.x];
@@ -104,7 +104,15 @@ __global__ void k_sites(const double *__restrict__ nodex, const int *__restrict_
       c += s * nx[3 * k + 2];
     }
     site_x[base + nj] = make_double4(a, b, c, 0.0);
+    if (site_h) site_h[base + nj] = make_float4((float) a, (float) b, (float) c, 0.f);
   }
+}
+
+__global__ void k_split_hi(const double4 *__restrict__ x, float4 *__restrict__ xh, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double4 p = x[i];
+  xh[i] = make_float4((float) p.x, (float) p.y, (float) p.z, 0.f);
 }
 
 // Sub-element centres (full_node_neighbor.cpp:137-143)
@@ -233,10 +241,16 @@ void launch_elem_list(const double *ex, const int *bin, const int *bstart, const
 }
 
 void launch_sites(const double *nodex, const int *etype, const int *site_base, int nelem,
-                  ElemTables t, double4 *site_x, cudaStream_t s) {
+                  ElemTables t, double4 *site_x, float4 *site_h, cudaStream_t s) {
   if (nelem <= 0) return;
-  k_sites<<<nelem, 128, 0, s>>>(nodex, etype, site_base, t, site_x);
+  k_sites<<<nelem, 128, 0, s>>>(nodex, etype, site_base, t, site_x, site_h);
   check(cudaGetLastError(), "sites");
+}
+
+void launch_split_hi(const double4 *x, float4 *xh, int n, cudaStream_t s) {
+  if (n <= 0) return;
+  k_split_hi<<<nblk(n, 256), 256, 0, s>>>(x, xh, n);
+  check(cudaGetLastError(), "split_hi");
 }
 
 void launch_sub_centres(const double *nodex, int nelem, ElemTables t, double4 *subc,
