@@ -46,6 +46,7 @@ def parse():
                    help="full C2; medium = 360,000-atom slab (profiling, > L2); small = 8,000 atoms")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-modes", action="store_true", help="skip timing the other precision modes")
     return p.parse_args()
 
 
@@ -295,6 +296,40 @@ def run_ours(a, ws, rank, local):
                "d2h_bytes_per_step": int(hx.nbytes + hv.nbytes + hf.nbytes),
                "steps": e_steps}
 
+    # the other precision modes on the same system: timing and force error
+    # against the FP64 forces of the same configuration
+    modes = {}
+    if not a.no_modes and ws == 1:
+        def forces():
+            s.pair_compute()
+            s.pair_ecompute()
+            return s.atoms()["f"].copy(), s.elements()["nodef"].copy()
+        s.set_precision(mode)
+        f_ref, nf_ref = forces()
+        for name, mcode in (("exact", cacg.FP64_EXACT), ("fp64", cacg.FP64), ("mixed", cacg.MIXED)):
+            if mcode == mode:
+                continue
+            s.set_precision(mcode)
+            f_m, nf_m = forces()
+            s.set_timing(True)
+            s.run(2)
+            s.run(a.steps)
+            tmm = s.timing()
+            err = {}
+            for key, (fa, fb) in {"atoms": (f_m, f_ref), "nodes": (nf_m, nf_ref)}.items():
+                fa = fa.reshape(-1, 3)
+                fb = fb.reshape(-1, 3)
+                if fb.size:
+                    d = np.linalg.norm(fa - fb, axis=1)
+                    n_ = np.linalg.norm(fb, axis=1)
+                    err[key] = {"rms_rel": float(np.sqrt((d ** 2).mean() / (n_ ** 2).mean())),
+                                "max_rel": float(d.max() / n_.max())}
+            modes[name] = {"value": sites * a.steps / (tmm[0] * 1e-3),
+                           "ms_per_step": tmm[0] / a.steps,
+                           "phase_ms_per_step": [round(v / a.steps, 4) for v in tmm[1:6]],
+                           "force_err_vs_" + a.mode: err}
+        s.set_precision(mode)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps,
@@ -329,6 +364,7 @@ def run_ours(a, ws, rank, local):
             "e2e": e2e,
             "clocks": clk,
             "gpu_launches": launches,
+            "other_modes": modes,
         }
         print(json.dumps(line), flush=True)
     s.close()

@@ -195,6 +195,11 @@ struct cacg_context {
   // device arrays: atoms
   DBuf<double4> d_x;
   DBuf<float4> d_xh, d_site_h;  // float copies for the FP32 cutoff pre-tests
+  // mixed precision: low parts of the double-single coordinates, element node
+  // offsets, FP32 spline and shape tables
+  DBuf<float4> d_xl, d_rhor_val4, d_ftab;
+  DBuf<float> d_u, d_shape_f, d_ljf;
+  DBuf<double> d_cutsq64;
   DBuf<double> d_v, d_f, d_xhold, d_rho, d_fp, d_mass;
   DBuf<int> d_type, d_tag, d_root, d_send;
   DBuf<int> d_abin, d_bcount, d_bstart, d_bmem, d_stencil;
@@ -309,6 +314,7 @@ struct cacg_context {
   // ---- path ----
   void init();
   void element_tables();
+  void mixed_tables();
   void element_size();
   void setup_cut();
   void comm_setup();
@@ -321,6 +327,8 @@ struct cacg_context {
   void neighbor_nbuild();
   void pair_compute();
   void pair_compute_pass(int pass);
+  void pair_compute_mixed(int pass);
+  void pair_ecompute_mixed();
   void pair_ecompute();
   void nve_initial();
   void nve_final();
@@ -338,6 +346,13 @@ cacg_context::~cacg_context() {
   for (auto *b : b4) b->release();
   d_xh.release();
   d_site_h.release();
+  d_xl.release();
+  d_rhor_val4.release();
+  d_ftab.release();
+  d_u.release();
+  d_shape_f.release();
+  d_ljf.release();
+  d_cutsq64.release();
   DBuf<double> *bd[] = {&d_v, &d_f, &d_xhold, &d_rho, &d_fp, &d_mass, &d_ex, &d_nodex, &d_nodev,
                         &d_nodef, &d_nodexhold, &d_erho, &d_emass, &d_diag, &d_fip, &d_site_fp,
                         &d_spa_int, &d_weight, &d_spa_inter, &d_spa_csub, &d_spa_isub, &d_frho,
@@ -934,6 +949,38 @@ void cacg_context::element_tables() {
   upload(d_node_list, node_list, s);
   upload(d_list_isub, list_isub, s);
   upload(d_sub_first, sub_first, s);
+  std::vector<float> shf((size_t) inter_num[1] * NPE);
+  for (size_t k = 0; k < shf.size(); k++) shf[k] = (float) spa_inter[(size_t) inter_off[1] * NPE + k];
+  upload(d_shape_f, shf, s);
+}
+
+// FP32 copies of the tables the mixed-precision kernels read from shared memory
+void cacg_context::mixed_tables() {
+  const int T = (MAXT + 1) * (MAXT + 1);
+  if (pair_style == 1) {
+    std::vector<float> lf(3 * T, 0.f);
+    std::vector<double> c64(T, 0.0);
+    for (int k = 0; k < T; k++) {
+      lf[k] = (float) ljtab.lj1[k];
+      lf[T + k] = (float) ljtab.lj2[k];
+      lf[2 * T + k] = (float) ljtab.cutsq[k];
+      c64[k] = ljtab.cutsq[k];
+    }
+    upload(d_ljf, lf, stream);
+    upload(d_cutsq64, c64, stream);
+  } else if (pair_style == 2) {
+    std::vector<float4> val(nr + 1), ft(3 * (size_t) (nr + 1));
+    for (int m = 0; m <= nr; m++) {
+      const double *c = &rhor_sp[(size_t) m * 7];
+      const double *z = &z2r_sp[(size_t) m * 7];
+      val[m] = make_float4((float) c[3], (float) c[4], (float) c[5], (float) c[6]);
+      ft[3 * m] = make_float4((float) c[0], (float) c[1], (float) c[2], (float) z[0]);
+      ft[3 * m + 1] = make_float4((float) z[1], (float) z[2], (float) z[3], (float) z[4]);
+      ft[3 * m + 2] = make_float4((float) z[5], (float) z[6], 0.f, 0.f);
+    }
+    upload(d_rhor_val4, val, stream);
+    upload(d_ftab, ft, stream);
+  }
 }
 
 // Element::element_size (element.cpp:567-625): running maximum of the body
@@ -1123,6 +1170,7 @@ void cacg_context::init() {
     upload(d_rhor, rhor_sp, stream);
     upload(d_z2r, z2r_sp, stream);
   }
+  mixed_tables();
   // element masses: NAAE gives nae^3 * m(type 1) (element.cpp:1104) and
   // pair_coeff eam resets it from the potential file (element.cpp:1117-1123)
   for (int t = 1; t <= netypes; t++)
@@ -1454,6 +1502,10 @@ void cacg_context::pair_compute_pass(int pass) {
   cudaStream_t s = stream;
   bool exact = !fast();
   int nall = nlocal + nghost;
+  if (mode == CACG_MIXED) {
+    pair_compute_mixed(pass);
+    return;
+  }
   if (pass == 1 && !exact) {
     d_xh.ensure(nall, s);
     launch_split_hi(d_x.p, d_xh.p, nall, s);
@@ -1483,16 +1535,128 @@ void cacg_context::pair_compute_pass(int pass) {
   }
 }
 
+// Mixed precision, atoms: double-single coordinates, FP32 pair terms, FP64 sums
+void cacg_context::pair_compute_mixed(int pass) {
+  cudaStream_t s = stream;
+  int nall = nlocal + nghost;
+  const float eps = 1.0e-4f;
+  mixed::MixedAtoms m{};
+  m.x = d_x.p;
+  m.num = d_num.p;
+  m.list = d_list.p;
+  m.stride = stride;
+  m.nlocal = nlocal;
+  if (pass == 1) {
+    d_xh.ensure(nall, s);
+    d_xl.ensure(nall, s);
+    mixed::split_hilo(d_x.p, d_xh.p, d_xl.p, nall, s);
+    launches++;
+  }
+  m.xh = d_xh.p;
+  m.xl = d_xl.p;
+  if (pair_style == 1) {
+    if (pass != 1) return;
+    m.cutsq_f = 0.f;
+    m.band_lo = 1.0f - eps;
+    m.band_hi = 1.0f + eps;
+    const int T = (MAXT + 1) * (MAXT + 1);
+    mixed::lj_atoms(m, d_type.p, d_ljf.p, d_ljf.p + T, d_ljf.p + 2 * T, d_cutsq64.p, d_f.p, s);
+    launches++;
+    return;
+  }
+  EamTables e = eamtab();
+  m.cutsq = cutforcesq;
+  m.cutsq_f = (float) cutforcesq;
+  m.band_lo = m.cutsq_f * (1.0f - eps);
+  m.band_hi = m.cutsq_f * (1.0f + eps);
+  if (pass == 1) {
+    d_rho.ensure(nall, s);
+    d_fp.ensure(nall, s);
+    mixed::eam_rho_atoms(m, d_rhor_val4.p, e, d_rho.p, d_fp.p, s);
+    launch_copy_root(d_fp.p, 1, d_root.p, nlocal, nghost, s);
+    launches += 2;
+  } else {
+    mixed::eam_force_atoms(m, d_ftab.p, e, d_fp.p, d_f.p, s);
+    launches++;
+  }
+}
+
+// Mixed precision, elements: sites interpolated in FP32 from node offsets,
+// FP32 pair terms, FP64 sums and FP64 nodal gather
+void cacg_context::pair_ecompute_mixed() {
+  cudaStream_t s = stream;
+  int nall = enlocal + enghost;
+  ElemTables t = etab();
+  d_u.ensure((size_t) 24 * nall, s);
+  mixed::elem_rel(d_nodex.p, d_ex.p, nall, d_u.p, s);
+  launches++;
+  const float eps = 1.0e-3f;
+  mixed::MixedElems m{};
+  m.nodex = d_nodex.p;
+  m.ex = d_ex.p;
+  m.u = d_u.p;
+  m.etype = d_etype.p;
+  m.row_elem = d_row_elem.p;
+  m.row_jj = d_row_jj.p;
+  m.row_first = d_row_first.p;
+  m.ipnum = d_ipnum.p;
+  m.ipent = d_ipent.p;
+  m.site_base = d_site_base.p;
+  m.nrows = nrows;
+  m.rowstride = rowstride;
+  m.nall = nall;
+  m.nlocal_e = enlocal;
+  m.spa_int = d_spa_int.p;
+  m.weight = d_weight.p;
+  m.int_off = d_int_off.p;
+  m.node_list = d_node_list.p;
+  m.shape = d_shape_f.p;
+  m.ninter = inter_num[1];
+  const double *spa64 = d_spa_inter.p + (size_t) inter_off[1] * NPE;
+  if (pair_style == 1) {
+    int a = 1 * (MAXT + 1) + 1;
+    m.cutsq = ljtab.cutsq[a];
+    m.cutsq_f = (float) m.cutsq;
+    m.band_lo = m.cutsq_f * (1.0f - eps);
+    m.band_hi = m.cutsq_f * (1.0f + eps);
+    EamTables e{};
+    mixed::ip_pass(m, 0, spa64, nullptr, e, (float) ljtab.lj1[a], (float) ljtab.lj2[a], d_fip.p, s);
+    launches++;
+  } else {
+    EamTables e = eamtab();
+    m.cutsq = cutforcesq;
+    m.cutsq_f = (float) cutforcesq;
+    m.band_lo = m.cutsq_f * (1.0f - eps);
+    m.band_hi = m.cutsq_f * (1.0f + eps);
+    d_erho.ensure((size_t) NPE * nall, s);
+    mixed::ip_pass(m, 1, spa64, d_rhor_val4.p, e, 0.f, 0.f, d_erho.p, s);
+    launch_copy_root(d_erho.p, NPE, d_eroot.p, enlocal, enghost, s);
+    m.erho = d_erho.p;
+    mixed::ip_pass(m, 2, spa64, d_ftab.p, e, 0.f, 0.f, d_fip.p, s);
+    launches += 3;
+  }
+  fp64_fma::gather_nodef(d_fip.p, d_etype.p, d_row_first.p, enlocal, t, d_nodef.p, s);
+  launches++;
+}
+
 void cacg_context::pair_ecompute() {
   if (enlocal == 0) return;
   if (!elists_built) fail(CACG_ESTATE, "Pair::ecompute before the node neighbor list is built");
+  if (mode == CACG_MIXED) {
+    pair_ecompute_mixed();
+    return;
+  }
   cudaStream_t s = stream;
   bool exact = !fast();
   int nall = enlocal + enghost;
   ElemTables t = etab();
   // sites of every local and ghost element at the current node positions
-  if (!exact) d_site_h.ensure(std::max(nsites, 1), s);
-  launch_sites(d_nodex.p, d_etype.p, d_site_base.p, nall, t, d_site_x.p, exact ? nullptr : d_site_h.p, s);
+  if (exact) {
+    launch_sites(d_nodex.p, d_etype.p, d_site_base.p, nall, t, d_site_x.p, nullptr, s);
+  } else {
+    d_site_h.ensure(std::max(nsites, 1), s);
+    fp64_fma::sites(d_nodex.p, d_etype.p, d_site_base.p, nall, t, d_site_x.p, d_site_h.p, s);
+  }
   launches++;
   if (pair_style == 1) {
     int a = 1 * (MAXT + 1) + 1;

@@ -205,7 +205,45 @@ void eam_ip(const double *nodex, const double *erho, const int *etype, const int
             EamTables e, float cut_pass, double *fip, cudaStream_t s);
 void gather_nodef(const double *fip, const int *etype, const int *row_first, int nlocal_e,
                   ElemTables t, double *nodef, cudaStream_t s);
+void sites(const double *nodex, const int *etype, const int *site_base, int nelem, ElemTables t,
+           double4 *site_x, float4 *site_h, cudaStream_t s);
 }  // namespace fp64_fma
+
+// ---- mixed precision (k_mixed.cu): FP32 pair terms, FP64 accumulation ----
+namespace mixed {
+struct MixedAtoms {
+  const double4 *x;
+  const float4 *xh, *xl;  // double-single coordinates
+  const int *num, *list;
+  int stride, nlocal;
+  float cutsq_f, band_lo, band_hi;  // FP32 test; [band_lo, band_hi] re-tested in FP64
+  double cutsq;
+};
+struct MixedElems {
+  const double *nodex, *ex, *erho;
+  const float *u;  // [nall][24] node offsets from the element centre
+  const int *etype, *row_elem, *row_jj, *row_first, *ipnum, *ipent, *site_base;
+  int nrows, rowstride, nall, nlocal_e;
+  const double *spa_int, *weight;
+  const int *int_off, *node_list;
+  const float *shape;  // [ninter][8]
+  int ninter;
+  float cutsq_f, band_lo, band_hi;
+  double cutsq;
+};
+void split_hilo(const double4 *x, float4 *xh, float4 *xl, int n, cudaStream_t s);
+void elem_rel(const double *nodex, const double *ex, int n, float *u, cudaStream_t s);
+void eam_rho_atoms(const MixedAtoms &m, const float4 *rhor_val, const EamTables &e,
+                   double *rho, double *fp, cudaStream_t s);
+void eam_force_atoms(const MixedAtoms &m, const float4 *ftab, const EamTables &e,
+                     const double *fp, double *f, cudaStream_t s);
+void lj_atoms(const MixedAtoms &m, const int *type, const float *lj1, const float *lj2,
+              const float *cutsq_t, const double *cutsq64, double *f, cudaStream_t s);
+// pass 0: LJ forces -> out[3*rows]; 1: EAM nodal densities -> out[8*nlocal_e];
+// 2: EAM forces -> out[3*rows]
+void ip_pass(const MixedElems &m, int pass, const double *spa_inter64, const float4 *tab,
+             const EamTables &e, float lj1, float lj2, double *out, cudaStream_t s);
+}  // namespace mixed
 
 // ---- integration and reductions (k_nve.cu) ----
 void launch_nve_atoms_initial(double4 *x, double *v, const double *f, const int *type,

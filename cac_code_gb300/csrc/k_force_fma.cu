@@ -359,7 +359,42 @@ __global__ void k_gather_nodef(const double *__restrict__ fip, const int *__rest
   nodef[tid] = acc;
 }
 
+// site positions with fused multiply-adds (the exact mode uses k_sites in
+// k_neigh.cu, built without contraction); also writes the float copy
+__global__ void k_sites_fma(const double *__restrict__ nodex, const int *__restrict__ etype,
+                            const int *__restrict__ site_base, ElemTables t,
+                            double4 *__restrict__ site_x, float4 *__restrict__ site_h) {
+  __shared__ double nx[24];
+  const int e = blockIdx.x;
+  if (threadIdx.x < 24) nx[threadIdx.x] = nodex[24 * (size_t) e + threadIdx.x];
+  __syncthreads();
+  const int ty = etype[e];
+  const int nint = t.inter_num[ty];
+  const double *S0 = t.spa_inter + (size_t) t.inter_off[ty] * NPE;
+  const int base = site_base[e];
+  for (int nj = threadIdx.x; nj < nint; nj += blockDim.x) {
+    const double *S = S0 + (size_t) nj * NPE;
+    double a = 0, b = 0, c = 0;
+#pragma unroll
+    for (int k = 0; k < NPE; k++) {
+      double w = S[k];
+      a += w * nx[3 * k];
+      b += w * nx[3 * k + 1];
+      c += w * nx[3 * k + 2];
+    }
+    site_x[base + nj] = make_double4(a, b, c, 0.0);
+    site_h[base + nj] = make_float4((float) a, (float) b, (float) c, 0.f);
+  }
+}
+
 }  // namespace
+
+void sites(const double *nodex, const int *etype, const int *site_base, int nelem, ElemTables t,
+           double4 *site_x, float4 *site_h, cudaStream_t s) {
+  if (nelem <= 0) return;
+  k_sites_fma<<<nelem, 128, 0, s>>>(nodex, etype, site_base, t, site_x, site_h);
+  check(cudaGetLastError(), "sites_fma");
+}
 
 void lj_atoms(const double4 *x, const float4 *xh, const int *type, const int *num,
               const int *list, int stride, int nlocal, const void *tab, float cut_pass,

@@ -174,10 +174,12 @@ k_eam_force_atoms(AtomArgs a, const float4 *__restrict__ ftab, int nr, float rdr
   }
 }
 
+// band_lo/band_hi are relative factors here: a pair with rsq in
+// [band_lo, band_hi] * cutsq(type pair) is decided in FP64
 __global__ void __launch_bounds__(256)
 k_lj_atoms(AtomArgs a, const int *__restrict__ type, const float *__restrict__ lj1,
            const float *__restrict__ lj2, const float *__restrict__ cutsq_t,
-           double *__restrict__ f) {
+           const double *__restrict__ cutsq64, double *__restrict__ f) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.nlocal; i += gridDim.x * blockDim.x) {
     const float4 hi = a.xh[i], li = a.xl[i];
     const int it = type[i];
@@ -192,8 +194,7 @@ k_lj_atoms(AtomArgs a, const int *__restrict__ type, const float *__restrict__ l
       int ij = it * (MAXT + 1) + type[j];
       float cs = cutsq_t[ij];
       bool in = rsq < cs;
-      if (rsq >= a.band_lo * cs && rsq <= a.band_hi * cs)
-        in = inside64(a.x[i], a.x[j], (double) a.cutsq * (double) cs / (double) a.cutsq_f);
+      if (rsq >= a.band_lo * cs && rsq <= a.band_hi * cs) in = inside64(a.x[i], a.x[j], cutsq64[ij]);
       if (in) {
         float r2inv = __frcp_rn(rsq);
         float r6inv = r2inv * r2inv * r2inv;
@@ -468,12 +469,12 @@ void eam_force_atoms(const MixedAtoms &m, const float4 *ftab, const EamTables &e
 }
 
 void lj_atoms(const MixedAtoms &m, const int *type, const float *lj1, const float *lj2,
-              const float *cutsq_t, double *f, cudaStream_t s) {
+              const float *cutsq_t, const double *cutsq64, double *f, cudaStream_t s) {
   if (m.nlocal <= 0) return;
   AtomArgs a{m.x, m.xh, m.xl, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
              m.band_hi, m.cutsq};
   int g = persistent_grid((const void *) k_lj_atoms, 256, 0, m.nlocal);
-  k_lj_atoms<<<g, 256, 0, s>>>(a, type, lj1, lj2, cutsq_t, f);
+  k_lj_atoms<<<g, 256, 0, s>>>(a, type, lj1, lj2, cutsq_t, cutsq64, f);
   check(cudaGetLastError(), "lj_atoms_mixed");
 }
 
