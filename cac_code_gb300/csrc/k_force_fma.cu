@@ -179,6 +179,10 @@ k_eam_force_atoms(const double4 *__restrict__ x, const float4 *__restrict__ xh,
   f[3 * i + 2] = fz;
 }
 
+// Positions are interpolated without contraction (explicit round-to-nearest
+// multiply and add), exactly as the exact mode: element coordinates reach
+// |x| ~ 1e3, and a fused rounding there would move a site by ~1e-13, which the
+// stiff pair forces amplify beyond the 1e-12 FP64 tolerance.
 __device__ __forceinline__ void ip_position(const double *__restrict__ N,
                                             const double *__restrict__ nx, double &ix,
                                             double &iy, double &iz) {
@@ -187,9 +191,9 @@ __device__ __forceinline__ void ip_position(const double *__restrict__ N,
   iz = 0;
 #pragma unroll
   for (int k = 0; k < NPE; k++) {
-    ix += N[k] * nx[3 * k];
-    iy += N[k] * nx[3 * k + 1];
-    iz += N[k] * nx[3 * k + 2];
+    ix = __dadd_rn(ix, __dmul_rn(N[k], nx[3 * k]));
+    iy = __dadd_rn(iy, __dmul_rn(N[k], nx[3 * k + 1]));
+    iz = __dadd_rn(iz, __dmul_rn(N[k], nx[3 * k + 2]));
   }
 }
 
@@ -299,14 +303,10 @@ k_eam_ip(const double *__restrict__ nodex, const double *__restrict__ erho,
     const double *N = t.spa_int + ((size_t) t.int_off[ty] + jj) * NPE;
     const double *nx = nodex + 24 * (size_t) e;
     const double *er = erho + NPE * (size_t) e;
-    double ix = 0, iy = 0, iz = 0, rhoi = 0;
+    double ix, iy, iz, rhoi = 0;
+    ip_position(N, nx, ix, iy, iz);
 #pragma unroll
-    for (int k = 0; k < NPE; k++) {
-      ix += N[k] * nx[3 * k];
-      iy += N[k] * nx[3 * k + 1];
-      iz += N[k] * nx[3 * k + 2];
-      rhoi += N[k] * er[k];
-    }
+    for (int k = 0; k < NPE; k++) rhoi += N[k] * er[k];
     double p;
     int m = rhoindex(rhoi, eam, p);
     const double fpi = spline_deriv(eam.frho + 7 * m, p);
@@ -374,14 +374,8 @@ __global__ void k_sites_fma(const double *__restrict__ nodex, const int *__restr
   const int base = site_base[e];
   for (int nj = threadIdx.x; nj < nint; nj += blockDim.x) {
     const double *S = S0 + (size_t) nj * NPE;
-    double a = 0, b = 0, c = 0;
-#pragma unroll
-    for (int k = 0; k < NPE; k++) {
-      double w = S[k];
-      a += w * nx[3 * k];
-      b += w * nx[3 * k + 1];
-      c += w * nx[3 * k + 2];
-    }
+    double a, b, c;
+    ip_position(S, nx, a, b, c);
     site_x[base + nj] = make_double4(a, b, c, 0.0);
     site_h[base + nj] = make_float4((float) a, (float) b, (float) c, 0.f);
   }

@@ -87,3 +87,36 @@ def test_exact_mode_matches_oracle_larger_slab(cacg_lib, oracle_lib):
     o.run(cfg["steps"])
     assert bits_equal(out["s1_x"], o.atoms()["x"].reshape(-1))
     assert bits_equal(out["s1_nodex"], o.elements()["nodex"].reshape(-1))
+
+
+def test_fma_mode_large_coordinates(cacg_lib, oracle_lib):
+    """Elements far from the origin (|x| up to ~200 A): the fast FP64 mode must
+    still agree with the reference arithmetic within 1e-12 of the force scale."""
+    from cac_code_gb300 import workloads as W
+    import os
+    import tempfile
+    eam = W.write_eam(os.path.join(tempfile.mkdtemp(), "Cu.eam"), n=2000)
+    m, cfg = W.c2_sample(seed=9)
+    s = cacg.System(0)
+    try:
+        W.configure_system(s, m, cfg, eam)
+        s.set_precision(cacg.FP64)
+        s.init()
+        s.setup()
+        s.neighbor_build()
+        s.neighbor_ebuild()
+        s.neighbor_nbuild()
+        s.pair_compute()
+        s.pair_ecompute()
+        f = s.atoms()["f"]
+        nf = s.elements()["nodef"]
+    finally:
+        s.close()
+    o = oracle_lib.Oracle(m, **W.oracle_kwargs(cfg, eam))
+    o.setup()
+    o.atom_list()
+    fr = o.atom_forces()
+    o.elem_lists()
+    nfr = o.elem_forces()
+    assert np.abs(f - fr).max() <= FP64_TOL * np.abs(fr).max()
+    assert np.abs(nf - nfr).max() <= FP64_TOL * np.abs(nfr).max()
