@@ -197,14 +197,16 @@ struct cacg_context {
   DBuf<float4> d_xh, d_site_h;  // float copies for the FP32 cutoff pre-tests
   // mixed precision: low parts of the double-single coordinates, element node
   // offsets, FP32 spline and shape tables
-  DBuf<float4> d_xl, d_rhor_val4, d_ftab;
-  DBuf<float> d_u, d_shape_f, d_ljf;
+  DBuf<float4> d_xl, d_rhor_val4, d_ftab, d_site_l;
+  DBuf<float2> d_shape_hl;
+  DBuf<float> d_u, d_shape_f, d_ljf, d_site_rho;
   DBuf<double> d_cutsq64;
   DBuf<double> d_v, d_f, d_xhold, d_rho, d_fp, d_mass;
   DBuf<int> d_type, d_tag, d_root, d_send;
   DBuf<int> d_abin, d_bcount, d_bstart, d_bmem, d_stencil;
   DBuf<double4> d_bx;
   DBuf<int> d_num, d_list;
+  DBuf<int> d_snum, d_slist;  // per-step short lists (FP32 guarded cutoff test)
   int maxneigh = 64, stride = 0;
   // elements
   DBuf<double> d_ex, d_nodex, d_nodev, d_nodef, d_nodexhold, d_erho, d_emass, d_diag, d_fip,
@@ -215,6 +217,7 @@ struct cacg_context {
   DBuf<int> d_enum, d_elist;
   int maxeneigh = 32, estride = 0;
   DBuf<int> d_row_elem, d_row_jj, d_row_first, d_site_base, d_ipnum, d_ipent;
+  DBuf<int> d_sipnum, d_sipent;
   int maxip = 128, rowstride = 0;
   // tables
   DBuf<double> d_spa_int, d_weight, d_spa_inter, d_spa_csub, d_spa_isub, d_frho, d_rhor, d_z2r;
@@ -351,6 +354,9 @@ cacg_context::~cacg_context() {
   d_ftab.release();
   d_u.release();
   d_shape_f.release();
+  d_site_l.release();
+  d_shape_hl.release();
+  d_site_rho.release();
   d_ljf.release();
   d_cutsq64.release();
   DBuf<double> *bd[] = {&d_v, &d_f, &d_xhold, &d_rho, &d_fp, &d_mass, &d_ex, &d_nodex, &d_nodev,
@@ -363,7 +369,8 @@ cacg_context::~cacg_context() {
                      &d_ebin, &d_ebcount, &d_ebstart, &d_ebmem, &d_enum, &d_elist,
                      &d_row_elem, &d_row_jj, &d_row_first, &d_site_base, &d_ipnum, &d_ipent,
                      &d_int_off, &d_inter_off, &d_numint, &d_inter_num, &d_node_list,
-                     &d_list_isub, &d_sub_first, &d_flags, &d_pos, &d_scan, &d_misc};
+                     &d_list_isub, &d_sub_first, &d_flags, &d_pos, &d_scan, &d_misc,
+                     &d_snum, &d_slist, &d_sipnum, &d_sipent};
   for (auto *b : bi) b->release();
   d_ljtab.release();
   for (auto &e : ev)
@@ -950,8 +957,14 @@ void cacg_context::element_tables() {
   upload(d_list_isub, list_isub, s);
   upload(d_sub_first, sub_first, s);
   std::vector<float> shf((size_t) inter_num[1] * NPE);
-  for (size_t k = 0; k < shf.size(); k++) shf[k] = (float) spa_inter[(size_t) inter_off[1] * NPE + k];
+  std::vector<float2> shl((size_t) inter_num[1] * NPE);
+  for (size_t k = 0; k < shf.size(); k++) {
+    double v = spa_inter[(size_t) inter_off[1] * NPE + k];
+    shf[k] = (float) v;
+    shl[k] = make_float2((float) v, (float) (v - (double) (float) v));
+  }
   upload(d_shape_f, shf, s);
+  upload(d_shape_hl, shl, s);
 }
 
 // FP32 copies of the tables the mixed-precision kernels read from shared memory
@@ -1506,16 +1519,21 @@ void cacg_context::pair_compute_pass(int pass) {
     pair_compute_mixed(pass);
     return;
   }
-  if (pass == 1 && !exact) {
+  const float cp = atom_cut_pass();
+  if (pass == 1) {
+    // float copies and the short list of this step (both FP64 modes)
     d_xh.ensure(nall, s);
     launch_split_hi(d_x.p, d_xh.p, nall, s);
-    launches++;
+    d_snum.ensure(nlocal, s);
+    d_slist.ensure((size_t) maxneigh * stride, s);
+    fp64_fma::filter_atoms(d_xh.p, d_num.p, d_list.p, stride, nlocal, cp, d_snum.p, d_slist.p, s);
+    launches += 2;
   }
-  const float cp = exact ? 0.f : atom_cut_pass();
+  const int *num = d_snum.p, *lst = d_slist.p;
   if (pair_style == 1) {
     if (pass != 1) return;
-    if (exact) fp64_exact::lj_atoms(d_x.p, d_type.p, d_num.p, d_list.p, stride, nlocal, d_ljtab.p, d_f.p, s);
-    else fp64_fma::lj_atoms(d_x.p, d_xh.p, d_type.p, d_num.p, d_list.p, stride, nlocal, d_ljtab.p, cp, d_f.p, s);
+    if (exact) fp64_exact::lj_atoms(d_x.p, d_type.p, num, lst, stride, nlocal, d_ljtab.p, d_f.p, s);
+    else fp64_fma::lj_atoms(d_x.p, d_xh.p, d_type.p, num, lst, stride, nlocal, d_ljtab.p, cp, d_f.p, s);
     launches++;
     return;
   }
@@ -1523,14 +1541,14 @@ void cacg_context::pair_compute_pass(int pass) {
   if (pass == 1) {
     d_rho.ensure(nall, s);
     d_fp.ensure(nall, s);
-    if (exact) fp64_exact::eam_rho_atoms(d_x.p, d_num.p, d_list.p, stride, nlocal, e, d_rho.p, d_fp.p, s);
-    else fp64_fma::eam_rho_atoms(d_x.p, d_xh.p, d_num.p, d_list.p, stride, nlocal, e, cp, d_rho.p, d_fp.p, s);
+    if (exact) fp64_exact::eam_rho_atoms(d_x.p, num, lst, stride, nlocal, e, d_rho.p, d_fp.p, s);
+    else fp64_fma::eam_rho_atoms(d_x.p, d_xh.p, num, lst, stride, nlocal, e, cp, d_rho.p, d_fp.p, s);
     // forward_comm_pair: ghost fp = owner fp (comm_brick.cpp:941-971)
     launch_copy_root(d_fp.p, 1, d_root.p, nlocal, nghost, s);
     launches += 2;
   } else {
-    if (exact) fp64_exact::eam_force_atoms(d_x.p, d_num.p, d_list.p, stride, nlocal, e, d_fp.p, d_f.p, s);
-    else fp64_fma::eam_force_atoms(d_x.p, d_xh.p, d_num.p, d_list.p, stride, nlocal, e, cp, d_fp.p, d_f.p, s);
+    if (exact) fp64_exact::eam_force_atoms(d_x.p, num, lst, stride, nlocal, e, d_fp.p, d_f.p, s);
+    else fp64_fma::eam_force_atoms(d_x.p, d_xh.p, num, lst, stride, nlocal, e, cp, d_fp.p, d_f.p, s);
     launches++;
   }
 }
@@ -1581,38 +1599,35 @@ void cacg_context::pair_compute_mixed(int pass) {
   }
 }
 
-// Mixed precision, elements: sites interpolated in FP32 from node offsets,
-// FP32 pair terms, FP64 sums and FP64 nodal gather
+// Mixed precision, elements: sites and integration points in double-single
+// FP32 (hi/lo float pairs), FP32 pair terms, FP64 sums and FP64 nodal gather
 void cacg_context::pair_ecompute_mixed() {
   cudaStream_t s = stream;
   int nall = enlocal + enghost;
   ElemTables t = etab();
-  d_u.ensure((size_t) 24 * nall, s);
-  mixed::elem_rel(d_nodex.p, d_ex.p, nall, d_u.p, s);
+  d_site_h.ensure(std::max(nsites, 1), s);
+  d_site_l.ensure(std::max(nsites, 1), s);
+  mixed::sites_ds(d_nodex.p, d_etype.p, d_site_base.p, d_inter_num.p, d_shape_hl.p, nall,
+                  d_site_h.p, d_site_l.p, s);
   launches++;
-  const float eps = 1.0e-3f;
+  const float eps = 1.0e-4f;
   mixed::MixedElems m{};
   m.nodex = d_nodex.p;
-  m.ex = d_ex.p;
-  m.u = d_u.p;
+  m.site_h = d_site_h.p;
+  m.site_l = d_site_l.p;
   m.etype = d_etype.p;
   m.row_elem = d_row_elem.p;
   m.row_jj = d_row_jj.p;
   m.row_first = d_row_first.p;
   m.ipnum = d_ipnum.p;
   m.ipent = d_ipent.p;
-  m.site_base = d_site_base.p;
   m.nrows = nrows;
   m.rowstride = rowstride;
-  m.nall = nall;
   m.nlocal_e = enlocal;
   m.spa_int = d_spa_int.p;
   m.weight = d_weight.p;
   m.int_off = d_int_off.p;
   m.node_list = d_node_list.p;
-  m.shape = d_shape_f.p;
-  m.ninter = inter_num[1];
-  const double *spa64 = d_spa_inter.p + (size_t) inter_off[1] * NPE;
   if (pair_style == 1) {
     int a = 1 * (MAXT + 1) + 1;
     m.cutsq = ljtab.cutsq[a];
@@ -1620,7 +1635,7 @@ void cacg_context::pair_ecompute_mixed() {
     m.band_lo = m.cutsq_f * (1.0f - eps);
     m.band_hi = m.cutsq_f * (1.0f + eps);
     EamTables e{};
-    mixed::ip_pass(m, 0, spa64, nullptr, e, (float) ljtab.lj1[a], (float) ljtab.lj2[a], d_fip.p, s);
+    mixed::ip_pass(m, 0, nullptr, e, (float) ljtab.lj1[a], (float) ljtab.lj2[a], d_fip.p, s);
     launches++;
   } else {
     EamTables e = eamtab();
@@ -1629,11 +1644,15 @@ void cacg_context::pair_ecompute_mixed() {
     m.band_lo = m.cutsq_f * (1.0f - eps);
     m.band_hi = m.cutsq_f * (1.0f + eps);
     d_erho.ensure((size_t) NPE * nall, s);
-    mixed::ip_pass(m, 1, spa64, d_rhor_val4.p, e, 0.f, 0.f, d_erho.p, s);
+    d_site_rho.ensure(std::max(nsites, 1), s);
+    mixed::ip_pass(m, 1, d_rhor_val4.p, e, 0.f, 0.f, d_erho.p, s);
     launch_copy_root(d_erho.p, NPE, d_eroot.p, enlocal, enghost, s);
+    mixed::site_rho(d_erho.p, d_etype.p, d_site_base.p, d_inter_num.p, d_shape_f.p, nall,
+                    d_site_rho.p, s);
     m.erho = d_erho.p;
-    mixed::ip_pass(m, 2, spa64, d_ftab.p, e, 0.f, 0.f, d_fip.p, s);
-    launches += 3;
+    m.site_rho = d_site_rho.p;
+    mixed::ip_pass(m, 2, d_ftab.p, e, 0.f, 0.f, d_fip.p, s);
+    launches += 4;
   }
   fp64_fma::gather_nodef(d_fip.p, d_etype.p, d_row_first.p, enlocal, t, d_nodef.p, s);
   launches++;
@@ -1650,43 +1669,47 @@ void cacg_context::pair_ecompute() {
   bool exact = !fast();
   int nall = enlocal + enghost;
   ElemTables t = etab();
-  // sites of every local and ghost element at the current node positions
-  if (exact) {
-    launch_sites(d_nodex.p, d_etype.p, d_site_base.p, nall, t, d_site_x.p, nullptr, s);
-  } else {
-    d_site_h.ensure(std::max(nsites, 1), s);
-    fp64_fma::sites(d_nodex.p, d_etype.p, d_site_base.p, nall, t, d_site_x.p, d_site_h.p, s);
-  }
-  launches++;
+  // sites of every local and ghost element at the current node positions,
+  // with their float copies, then this step's short lists of the rows
+  d_site_h.ensure(std::max(nsites, 1), s);
+  if (exact) launch_sites(d_nodex.p, d_etype.p, d_site_base.p, nall, t, d_site_x.p, d_site_h.p, s);
+  else fp64_fma::sites(d_nodex.p, d_etype.p, d_site_base.p, nall, t, d_site_x.p, d_site_h.p, s);
+  const double csq = pair_style == 1 ? ljtab.cutsq[1 * (MAXT + 1) + 1] : cutforcesq;
+  const float cp = cut_pass(csq);
+  d_sipnum.ensure(std::max(nrows, 1), s);
+  d_sipent.ensure((size_t) maxip * rowstride, s);
+  fp64_fma::filter_rows(d_nodex.p, d_etype.p, d_row_elem.p, d_row_jj.p, nrows, d_ipnum.p, d_ipent.p,
+                        rowstride, d_site_h.p, t, cp, exact ? 0 : 1, d_sipnum.p, d_sipent.p, s);
+  launches += 2;
+  const int *ipn = d_sipnum.p, *ipe = d_sipent.p;
   if (pair_style == 1) {
     int a = 1 * (MAXT + 1) + 1;
     if (exact)
-      fp64_exact::lj_ip(d_nodex.p, d_etype.p, d_row_elem.p, d_row_jj.p, nrows, d_ipnum.p, d_ipent.p,
+      fp64_exact::lj_ip(d_nodex.p, d_etype.p, d_row_elem.p, d_row_jj.p, nrows, ipn, ipe,
                         rowstride, d_site_x.p, t, ljtab.lj1[a], ljtab.lj2[a], ljtab.cutsq[a], d_fip.p, s);
     else
-      fp64_fma::lj_ip(d_nodex.p, d_etype.p, d_row_elem.p, d_row_jj.p, nrows, d_ipnum.p, d_ipent.p,
+      fp64_fma::lj_ip(d_nodex.p, d_etype.p, d_row_elem.p, d_row_jj.p, nrows, ipn, ipe,
                       rowstride, d_site_x.p, d_site_h.p, t, ljtab.lj1[a], ljtab.lj2[a], ljtab.cutsq[a],
-                      cut_pass(ljtab.cutsq[a]), d_fip.p, s);
+                      cp, d_fip.p, s);
     launches++;
   } else {
     EamTables e = eamtab();
-    const float cp = exact ? 0.f : cut_pass(cutforcesq);
     d_erho.ensure((size_t) NPE * nall, s);
     d_site_fp.ensure(std::max(nsites, 1), s);
     if (exact) {
-      fp64_exact::eam_erho(d_nodex.p, d_etype.p, d_row_first.p, enlocal, d_ipnum.p, d_ipent.p, rowstride, d_site_x.p, t, e, d_erho.p, s);
+      fp64_exact::eam_erho(d_nodex.p, d_etype.p, d_row_first.p, enlocal, ipn, ipe, rowstride, d_site_x.p, t, e, d_erho.p, s);
     } else {
-      fp64_fma::eam_erho(d_nodex.p, d_etype.p, d_row_first.p, enlocal, d_ipnum.p, d_ipent.p, rowstride, d_site_x.p, d_site_h.p, t, e, cp, d_erho.p, s);
+      fp64_fma::eam_erho(d_nodex.p, d_etype.p, d_row_first.p, enlocal, ipn, ipe, rowstride, d_site_x.p, d_site_h.p, t, e, cp, d_erho.p, s);
     }
     // eforward_comm_pair: ghost nodal densities from their owners (comm_brick.cpp:978-1010)
     launch_copy_root(d_erho.p, NPE, d_eroot.p, enlocal, enghost, s);
     if (exact) {
       fp64_exact::eam_site_fp(d_erho.p, d_etype.p, d_site_base.p, nall, t, e, d_site_fp.p, s);
-      fp64_exact::eam_ip(d_nodex.p, d_erho.p, d_etype.p, d_row_elem.p, d_row_jj.p, nrows, d_ipnum.p, d_ipent.p,
+      fp64_exact::eam_ip(d_nodex.p, d_erho.p, d_etype.p, d_row_elem.p, d_row_jj.p, nrows, ipn, ipe,
                          rowstride, d_site_x.p, d_site_fp.p, t, e, d_fip.p, s);
     } else {
       fp64_fma::eam_site_fp(d_erho.p, d_etype.p, d_site_base.p, nall, t, e, d_site_fp.p, s);
-      fp64_fma::eam_ip(d_nodex.p, d_erho.p, d_etype.p, d_row_elem.p, d_row_jj.p, nrows, d_ipnum.p, d_ipent.p,
+      fp64_fma::eam_ip(d_nodex.p, d_erho.p, d_etype.p, d_row_elem.p, d_row_jj.p, nrows, ipn, ipe,
                        rowstride, d_site_x.p, d_site_h.p, d_site_fp.p, t, e, cp, d_fip.p, s);
     }
     launches += 4;

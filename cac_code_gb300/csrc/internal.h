@@ -207,6 +207,13 @@ void gather_nodef(const double *fip, const int *etype, const int *row_first, int
                   ElemTables t, double *nodef, cudaStream_t s);
 void sites(const double *nodex, const int *etype, const int *site_base, int nelem, ElemTables t,
            double4 *site_x, float4 *site_h, cudaStream_t s);
+// per-step short lists (FP32 guarded cutoff test), used by both FP64 modes
+void filter_atoms(const float4 *xh, const int *num, const int *list, int stride, int nlocal,
+                  float cut_pass, int *snum, int *slist, cudaStream_t s);
+void filter_rows(const double *nodex, const int *etype, const int *row_elem, const int *row_jj,
+                 int nrows, const int *ipnum, const int *ipent, int rowstride,
+                 const float4 *site_h, ElemTables t, float cut_pass, int only_needed, int *snum,
+                 int *sent, cudaStream_t s);
 }  // namespace fp64_fma
 
 // ---- mixed precision (k_mixed.cu): FP32 pair terms, FP64 accumulation ----
@@ -220,19 +227,21 @@ struct MixedAtoms {
   double cutsq;
 };
 struct MixedElems {
-  const double *nodex, *ex, *erho;
-  const float *u;  // [nall][24] node offsets from the element centre
-  const int *etype, *row_elem, *row_jj, *row_first, *ipnum, *ipent, *site_base;
-  int nrows, rowstride, nall, nlocal_e;
+  const double *nodex, *erho;
+  const float4 *site_h, *site_l;  // double-single site positions of this step
+  const float *site_rho;          // FP32 site densities (EAM force pass)
+  const int *etype, *row_elem, *row_jj, *row_first, *ipnum, *ipent;
+  int nrows, rowstride, nlocal_e;
   const double *spa_int, *weight;
   const int *int_off, *node_list;
-  const float *shape;  // [ninter][8]
-  int ninter;
   float cutsq_f, band_lo, band_hi;
   double cutsq;
 };
 void split_hilo(const double4 *x, float4 *xh, float4 *xl, int n, cudaStream_t s);
-void elem_rel(const double *nodex, const double *ex, int n, float *u, cudaStream_t s);
+void sites_ds(const double *nodex, const int *etype, const int *site_base, const int *inter_num,
+              const float2 *shape_hl, int nelem, float4 *site_h, float4 *site_l, cudaStream_t s);
+void site_rho(const double *erho, const int *etype, const int *site_base, const int *inter_num,
+              const float *shape, int nelem, float *rho, cudaStream_t s);
 void eam_rho_atoms(const MixedAtoms &m, const float4 *rhor_val, const EamTables &e,
                    double *rho, double *fp, cudaStream_t s);
 void eam_force_atoms(const MixedAtoms &m, const float4 *ftab, const EamTables &e,
@@ -241,8 +250,8 @@ void lj_atoms(const MixedAtoms &m, const int *type, const float *lj1, const floa
               const float *cutsq_t, const double *cutsq64, double *f, cudaStream_t s);
 // pass 0: LJ forces -> out[3*rows]; 1: EAM nodal densities -> out[8*nlocal_e];
 // 2: EAM forces -> out[3*rows]
-void ip_pass(const MixedElems &m, int pass, const double *spa_inter64, const float4 *tab,
-             const EamTables &e, float lj1, float lj2, double *out, cudaStream_t s);
+void ip_pass(const MixedElems &m, int pass, const float4 *tab, const EamTables &e, float lj1,
+             float lj2, double *out, cudaStream_t s);
 }  // namespace mixed
 
 // ---- integration and reductions (k_nve.cu) ----

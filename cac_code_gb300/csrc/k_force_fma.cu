@@ -89,7 +89,6 @@ k_lj_atoms(const double4 *__restrict__ x, const float4 *__restrict__ xh,
   double fx = 0.0, fy = 0.0, fz = 0.0;
   for (int k = 0; k < n; k++) {
     int j = __ldg(list + (size_t) k * stride + i);
-    if (rsq_f(hi, __ldg(xh + j)) > cut_pass) continue;
     double4 xj = x[j];
     double dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
     double rsq = dx * dx + dy * dy + dz * dz;
@@ -122,7 +121,6 @@ k_eam_rho_atoms(const double4 *__restrict__ x, const float4 *__restrict__ xh,
   double r = 0.0;
   for (int k = 0; k < n; k++) {
     int j = __ldg(list + (size_t) k * stride + i);
-    if (rsq_f(hi, __ldg(xh + j)) > cut_pass) continue;
     double4 xj = x[j];
     double dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
     double rsq = dx * dx + dy * dy + dz * dz;
@@ -152,7 +150,6 @@ k_eam_force_atoms(const double4 *__restrict__ x, const float4 *__restrict__ xh,
   double fx = 0.0, fy = 0.0, fz = 0.0;
   for (int k = 0; k < n; k++) {
     int j = __ldg(list + (size_t) k * stride + i);
-    if (rsq_f(hi, __ldg(xh + j)) > cut_pass) continue;
     double4 xj = x[j];
     double dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
     double rsq = dx * dx + dy * dy + dz * dz;
@@ -215,7 +212,6 @@ k_lj_ip(const double *__restrict__ nodex, const int *__restrict__ etype,
     const int n = ipnum[r];
     for (int k = 0; k < n; k++) {
       int sid = __ldg(ipent + (size_t) k * rowstride + r);
-      if (rsq_f(hi, __ldg(site_h + sid)) > cut_pass) continue;
       double4 s = site_x[sid];
       double dx = ix - s.x, dy = iy - s.y, dz = iz - s.z;
       double rsq = dx * dx + dy * dy + dz * dz;
@@ -253,7 +249,6 @@ k_eam_erho(const double *__restrict__ nodex, const int *__restrict__ etype,
   const int n = ipnum[r];
   for (int k = 0; k < n; k++) {
     int sid = __ldg(ipent + (size_t) k * rowstride + r);
-    if (rsq_f(hi, __ldg(site_h + sid)) > cut_pass) continue;
     double4 s = site_x[sid];
     double dx = ix - s.x, dy = iy - s.y, dz = iz - s.z;
     double rsq = dx * dx + dy * dy + dz * dz;
@@ -314,7 +309,6 @@ k_eam_ip(const double *__restrict__ nodex, const double *__restrict__ erho,
     const int n = ipnum[r];
     for (int k = 0; k < n; k++) {
       int sid = __ldg(ipent + (size_t) k * rowstride + r);
-      if (rsq_f(hi, __ldg(site_h + sid)) > cut_pass) continue;
       double4 s = site_x[sid];
       double dx = ix - s.x, dy = iy - s.y, dz = iz - s.z;
       double rsq = dx * dx + dy * dy + dz * dz;
@@ -359,6 +353,57 @@ __global__ void k_gather_nodef(const double *__restrict__ fip, const int *__rest
   nodef[tid] = acc;
 }
 
+// Per-step short lists: the entries of a row whose FP32 distance passes the
+// guarded cutoff test (any entry inside the cutoff in exact arithmetic passes),
+// in list order.  Both EAM passes and the element passes then iterate mostly
+// interacting pairs, so the FP64 branch seldom diverges inside a warp.
+__global__ void __launch_bounds__(128)
+k_filter_atoms(const float4 *__restrict__ xh, const int *__restrict__ num,
+               const int *__restrict__ list, int stride, int nlocal, float cut_pass,
+               int *__restrict__ snum, int *__restrict__ slist) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nlocal) return;
+  const float4 hi = xh[i];
+  const int n = num[i];
+  int m = 0;
+  for (int k = 0; k < n; k++) {
+    int j = __ldg(list + (size_t) k * stride + i);
+    if (rsq_f(hi, __ldg(xh + j)) <= cut_pass) slist[(size_t) m++ * stride + i] = j;
+  }
+  snum[i] = m;
+}
+
+// rows: all rows (mode 0), rows of nonzero weight or node rows (mode 1)
+__global__ void __launch_bounds__(128)
+k_filter_rows(const double *__restrict__ nodex, const int *__restrict__ etype,
+              const int *__restrict__ row_elem, const int *__restrict__ row_jj, int nrows,
+              const int *__restrict__ ipnum, const int *__restrict__ ipent, int rowstride,
+              const float4 *__restrict__ site_h, ElemTables t, float cut_pass, int only_needed,
+              int *__restrict__ snum, int *__restrict__ sent) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  const int e = row_elem[r], jj = row_jj[r], ty = etype[e];
+  if (only_needed && t.weight[t.int_off[ty] + jj] == 0.0) {
+    bool node = false;
+    for (int q = 0; q < NPE; q++) node = node || t.node_list[ty * NPE + q] == jj;
+    if (!node) {
+      snum[r] = 0;
+      return;
+    }
+  }
+  const double *N = t.spa_int + ((size_t) t.int_off[ty] + jj) * NPE;
+  double ix, iy, iz;
+  ip_position(N, nodex + 24 * (size_t) e, ix, iy, iz);
+  const float4 hi = make_float4((float) ix, (float) iy, (float) iz, 0.f);
+  const int n = ipnum[r];
+  int m = 0;
+  for (int k = 0; k < n; k++) {
+    int sid = __ldg(ipent + (size_t) k * rowstride + r);
+    if (rsq_f(hi, __ldg(site_h + sid)) <= cut_pass) sent[(size_t) m++ * rowstride + r] = sid;
+  }
+  snum[r] = m;
+}
+
 // site positions with fused multiply-adds (the exact mode uses k_sites in
 // k_neigh.cu, built without contraction); also writes the float copy
 __global__ void k_sites_fma(const double *__restrict__ nodex, const int *__restrict__ etype,
@@ -382,6 +427,25 @@ __global__ void k_sites_fma(const double *__restrict__ nodex, const int *__restr
 }
 
 }  // namespace
+
+void filter_atoms(const float4 *xh, const int *num, const int *list, int stride, int nlocal,
+                  float cut_pass, int *snum, int *slist, cudaStream_t s) {
+  if (nlocal <= 0) return;
+  k_filter_atoms<<<nblk(nlocal, 128), 128, 0, s>>>(xh, num, list, stride, nlocal, cut_pass,
+                                                  snum, slist);
+  check(cudaGetLastError(), "filter_atoms");
+}
+
+void filter_rows(const double *nodex, const int *etype, const int *row_elem, const int *row_jj,
+                 int nrows, const int *ipnum, const int *ipent, int rowstride,
+                 const float4 *site_h, ElemTables t, float cut_pass, int only_needed, int *snum,
+                 int *sent, cudaStream_t s) {
+  if (nrows <= 0) return;
+  k_filter_rows<<<nblk(nrows, 128), 128, 0, s>>>(nodex, etype, row_elem, row_jj, nrows, ipnum,
+                                                ipent, rowstride, site_h, t, cut_pass,
+                                                only_needed, snum, sent);
+  check(cudaGetLastError(), "filter_rows");
+}
 
 void sites(const double *nodex, const int *etype, const int *site_base, int nelem, ElemTables t,
            double4 *site_x, float4 *site_h, cudaStream_t s) {

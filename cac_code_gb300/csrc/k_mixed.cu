@@ -5,8 +5,8 @@
 // evaluated in FP32 where the spec allows it:
 //  * atom coordinates are double-single pairs (hi = float(x), lo = float(x-hi)),
 //    so a pair vector (hi_i-hi_j)+(lo_i-lo_j) is good to ~1e-6 A at any box size;
-//  * element sites are interpolated in FP32 from node offsets to the element
-//    centre, the centre-to-centre offset taken in FP64 once per neighbor element;
+//  * element sites and integration points are interpolated once per step in
+//    double-single FP32 arithmetic (k_sites_ds), stored as hi/lo float pairs;
 //  * r, 1/r and the rho(r), r*phi(r) splines are FP32, the spline coefficients
 //    FP32 in shared memory, loaded once by each resident block (persistent grid);
 //  * the cutoff test is made in FP32 and re-made in FP64 inside a thin guard
@@ -61,15 +61,6 @@ __global__ void k_split_hilo(const double4 *__restrict__ x, float4 *__restrict__
   float hx = (float) p.x, hy = (float) p.y, hz = (float) p.z;
   xh[i] = make_float4(hx, hy, hz, 0.f);
   xl[i] = make_float4((float) (p.x - hx), (float) (p.y - hy), (float) (p.z - hz), 0.f);
-}
-
-// node offsets from the element centre, FP32 (element-relative coordinates)
-__global__ void k_elem_rel(const double *__restrict__ nodex, const double *__restrict__ ex,
-                           int n, float *__restrict__ u) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n * 24) return;
-  int e = t / 24, c = t % 3;
-  u[t] = (float) (nodex[t] - ex[3 * e + c]);
 }
 
 __device__ __forceinline__ void pair_vec(const float4 &hi, const float4 &li, const float4 &hj,
@@ -217,148 +208,175 @@ k_lj_atoms(AtomArgs a, const int *__restrict__ type, const float *__restrict__ l
 }
 
 // ---------------------------------------------------------------- elements
+//
+// Sites are computed once per step in double-single FP32 arithmetic (a value is
+// an unevaluated sum hi + lo of two floats; products and sums use error-free
+// transformations: TwoProduct via fma and Knuth's TwoSum), so a site carries
+// ~44 bits from the FP64 nodes without a single FP64 instruction per site.
+
+__device__ __forceinline__ void ds_split(double x, float &h, float &l) {
+  h = (float) x;
+  l = (float) (x - (double) h);
+}
+
+// (ah, al) += (bh + bl) * (ch + cl), dropping bl*cl
+__device__ __forceinline__ void ds_acc_prod(float &ah, float &al, float bh, float bl, float ch,
+                                            float cl) {
+  float p = __fmul_rn(bh, ch);
+  float e = __fmaf_rn(bh, ch, -p);
+  e = __fmaf_rn(bh, cl, e);
+  e = __fmaf_rn(bl, ch, e);
+  float s = __fadd_rn(ah, p);
+  float v = __fsub_rn(s, ah);
+  float err = __fadd_rn(__fsub_rn(ah, __fsub_rn(s, v)), __fsub_rn(p, v));
+  al = __fadd_rn(al, __fadd_rn(e, err));
+  ah = s;
+}
+
+__device__ __forceinline__ void ds_norm(float &h, float &l) {
+  float s = __fadd_rn(h, l);
+  l = __fsub_rn(l, __fsub_rn(s, h));
+  h = s;
+}
+
+// one block per element: nodes split into double-single once, then every site
+// of the element interpolated in double-single; also writes the per-site
+// element index used by the density interpolation
+__global__ void k_sites_ds(const double *__restrict__ nodex, const int *__restrict__ etype,
+                           const int *__restrict__ site_base, const int *__restrict__ inter_num,
+                           const float2 *__restrict__ shape_hl, float4 *__restrict__ site_h,
+                           float4 *__restrict__ site_l) {
+  __shared__ float nh[24], nl[24];
+  const int e = blockIdx.x;
+  if (threadIdx.x < 24) ds_split(nodex[24 * (size_t) e + threadIdx.x], nh[threadIdx.x], nl[threadIdx.x]);
+  __syncthreads();
+  const int nint = inter_num[etype[e]];
+  const int base = site_base[e];
+  for (int nj = threadIdx.x; nj < nint; nj += blockDim.x) {
+    const float2 *S = shape_hl + (size_t) nj * NPE;
+    float xh = 0.f, xl = 0.f, yh = 0.f, yl = 0.f, zh = 0.f, zl = 0.f;
+#pragma unroll
+    for (int k = 0; k < NPE; k++) {
+      float2 w = S[k];
+      ds_acc_prod(xh, xl, w.x, w.y, nh[3 * k], nl[3 * k]);
+      ds_acc_prod(yh, yl, w.x, w.y, nh[3 * k + 1], nl[3 * k + 1]);
+      ds_acc_prod(zh, zl, w.x, w.y, nh[3 * k + 2], nl[3 * k + 2]);
+    }
+    ds_norm(xh, xl);
+    ds_norm(yh, yl);
+    ds_norm(zh, zl);
+    site_h[base + nj] = make_float4(xh, yh, zh, 0.f);
+    site_l[base + nj] = make_float4(xl, yl, zl, 0.f);
+  }
+}
+
+// density at every site, rho_s = sum_k N_k erho_k (FP32; pair_eam.cpp:1060-1065)
+__global__ void k_site_rho(const double *__restrict__ erho, const int *__restrict__ etype,
+                           const int *__restrict__ site_base, const int *__restrict__ inter_num,
+                           const float *__restrict__ shape, float *__restrict__ site_rho) {
+  __shared__ float er[NPE];
+  const int e = blockIdx.x;
+  if (threadIdx.x < NPE) er[threadIdx.x] = (float) erho[NPE * (size_t) e + threadIdx.x];
+  __syncthreads();
+  const int nint = inter_num[etype[e]];
+  const int base = site_base[e];
+  for (int nj = threadIdx.x; nj < nint; nj += blockDim.x) {
+    const float *S = shape + (size_t) nj * NPE;
+    float r = 0.f;
+#pragma unroll
+    for (int k = 0; k < NPE; k++) r += S[k] * er[k];
+    site_rho[base + nj] = r;
+  }
+}
 
 struct ElemArgs {
-  const double *nodex, *ex, *erho;
-  const float *u;           // [nall][24] node offsets from the centre
-  const int *etype, *row_elem, *row_jj, *row_first, *ipnum, *ipent, *site_base;
-  int nrows, rowstride, nall, nlocal_e;
+  const double *nodex, *erho;
+  const float4 *site_h, *site_l;
+  const float *site_rho;
+  const int *etype, *row_elem, *row_jj, *row_first, *ipnum, *ipent;
+  int nrows, rowstride, nlocal_e;
   const double *spa_int, *weight;
   const int *int_off, *node_list;
-  const float *shape;       // [ninter][8] FP32 site shape functions (type 1)
-  int ninter;
   float cutsq_f, band_lo, band_hi;
   double cutsq;
 };
 
-// locate the element owning site id `sid` (site_base ascending), starting from
-// the current range; entries of a row come grouped by element
-__device__ __forceinline__ int site_elem(const int *__restrict__ sb, int nall, int sid) {
-  int lo = 0, hi = nall;  // sb[lo] <= sid < sb[hi]
-  while (hi - lo > 1) {
-    int mid = (lo + hi) >> 1;
-    if (__ldg(sb + mid) <= sid) lo = mid;
-    else hi = mid;
-  }
-  return lo;
-}
-
-__device__ __forceinline__ void site_rel(const float *__restrict__ S, const float *__restrict__ u,
-                                         float &x, float &y, float &z) {
-  x = 0.f;
-  y = 0.f;
-  z = 0.f;
+// integration-point position in double-single from the FP64 nodes
+__device__ __forceinline__ void ip_ds(const double *__restrict__ N, const double *__restrict__ nx,
+                                      float4 &h, float4 &l) {
+  float xh = 0.f, xl = 0.f, yh = 0.f, yl = 0.f, zh = 0.f, zl = 0.f;
 #pragma unroll
   for (int k = 0; k < NPE; k++) {
-    x += S[k] * u[3 * k];
-    y += S[k] * u[3 * k + 1];
-    z += S[k] * u[3 * k + 2];
+    float wh, wl, ah, al, bh, bl, ch, cl;
+    ds_split(N[k], wh, wl);
+    ds_split(nx[3 * k], ah, al);
+    ds_split(nx[3 * k + 1], bh, bl);
+    ds_split(nx[3 * k + 2], ch, cl);
+    ds_acc_prod(xh, xl, wh, wl, ah, al);
+    ds_acc_prod(yh, yl, wh, wl, bh, bl);
+    ds_acc_prod(zh, zl, wh, wl, ch, cl);
   }
+  ds_norm(xh, xl);
+  ds_norm(yh, yl);
+  ds_norm(zh, zl);
+  h = make_float4(xh, yh, zh, 0.f);
+  l = make_float4(xl, yl, zl, 0.f);
 }
 
-// FP64 position of a site, for the guard-band re-test
-__device__ __forceinline__ void site64(const double *__restrict__ S, const double *__restrict__ nx,
-                                       double &x, double &y, double &z) {
-  x = 0;
-  y = 0;
-  z = 0;
-  for (int k = 0; k < NPE; k++) {
-    x += S[k] * nx[3 * k];
-    y += S[k] * nx[3 * k + 1];
-    z += S[k] * nx[3 * k + 2];
-  }
-}
-
-// One thread per integration point (row); node rows of weight 0 are skipped
-// unless `node_rows` (EAM nodal density pass), which visits only node rows.
+// One thread per integration point.  DENSITY: node rows -> erho (EAM);
+// otherwise rows of nonzero weight -> forces (LJ or EAM).
 template <bool EAM, bool DENSITY>
 __global__ void __launch_bounds__(256)
-k_ip(ElemArgs a, const double *__restrict__ spa_inter64, const float4 *__restrict__ tab,
-     int nr, float rdr, const double *__restrict__ frho, int nrho, double rdrho,
-     float lj1, float lj2, double *__restrict__ out) {
-  extern __shared__ float4 smem[];
-  float *s_shape = (float *) smem;                       // ninter*8 floats
-  float4 *s_tab = smem + 2 * a.ninter;                   // EAM table after the shapes
-  for (int k = threadIdx.x; k < a.ninter * NPE; k += blockDim.x) s_shape[k] = a.shape[k];
+k_ip(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr,
+     const double *__restrict__ frho, int nrho, double rdrho, float lj1, float lj2,
+     double *__restrict__ out) {
+  extern __shared__ float4 s_tab[];
   const int ntab = EAM ? (DENSITY ? (nr + 1) : 3 * (nr + 1)) : 0;
   for (int m = threadIdx.x; m < ntab; m += blockDim.x) s_tab[m] = tab[m];
   __syncthreads();
   const int nitems = DENSITY ? a.nlocal_e * NPE : a.nrows;
   for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < nitems; it += gridDim.x * blockDim.x) {
-    int r, e, ty;
-    const double *N64;
+    int r, e, ty, jj;
     if (DENSITY) {
       e = it / NPE;
-      int q = it % NPE;
       ty = a.etype[e];
-      int jj = a.node_list[ty * NPE + q];
+      jj = a.node_list[ty * NPE + it % NPE];
       r = a.row_first[e] + jj;
-      N64 = a.spa_int + ((size_t) a.int_off[ty] + jj) * NPE;
     } else {
       r = it;
       e = a.row_elem[r];
       ty = a.etype[e];
-      int jj = a.row_jj[r];
+      jj = a.row_jj[r];
       if (a.weight[a.int_off[ty] + jj] == 0.0) {
         out[3 * r] = out[3 * r + 1] = out[3 * r + 2] = 0.0;
         continue;
       }
-      N64 = a.spa_int + ((size_t) a.int_off[ty] + jj) * NPE;
     }
-    const float *ue = a.u + 24 * (size_t) e;
-    float ipx = 0.f, ipy = 0.f, ipz = 0.f;
+    const double *N64 = a.spa_int + ((size_t) a.int_off[ty] + jj) * NPE;
+    const double *nxe = a.nodex + 24 * (size_t) e;
+    float4 ih, il;
+    ip_ds(N64, nxe, ih, il);
     double fpi = 0.0;
-    double rhoi = 0.0;
+    if (EAM && !DENSITY) {
+      double rhoi = 0.0;
 #pragma unroll
-    for (int k = 0; k < NPE; k++) {
-      float nk = (float) N64[k];
-      ipx += nk * ue[3 * k];
-      ipy += nk * ue[3 * k + 1];
-      ipz += nk * ue[3 * k + 2];
-      if (EAM && !DENSITY) rhoi += N64[k] * a.erho[NPE * (size_t) e + k];
+      for (int k = 0; k < NPE; k++) rhoi += N64[k] * a.erho[NPE * (size_t) e + k];
+      fpi = fprime64(rhoi, frho, nrho, rdrho);
     }
-    if (EAM && !DENSITY) fpi = fprime64(rhoi, frho, nrho, rdrho);
-    const double cex = a.ex[3 * e], cey = a.ex[3 * e + 1], cez = a.ex[3 * e + 2];
-    int j = -1, sb0 = 0, sb1 = 0;
-    float ox = 0.f, oy = 0.f, oz = 0.f;
-    float uj[24];
-    float erj[NPE];
-    double acc = 0.0, fx = 0.0, fy = 0.0, fz = 0.f;
+    double acc = 0.0, fx = 0.0, fy = 0.0, fz = 0.0;
     float part = 0.f, px = 0.f, py = 0.f, pz = 0.f;
     const int n = a.ipnum[r];
     for (int k = 0; k < n; k++) {
       int sid = __ldg(a.ipent + (size_t) k * a.rowstride + r);
-      if (sid < sb0 || sid >= sb1) {
-        j = site_elem(a.site_base, a.nall, sid);
-        sb0 = __ldg(a.site_base + j);
-        sb1 = __ldg(a.site_base + j + 1);
-        ox = (float) (cex - a.ex[3 * j]);
-        oy = (float) (cey - a.ex[3 * j + 1]);
-        oz = (float) (cez - a.ex[3 * j + 2]);
-        for (int q = 0; q < 24; q++) uj[q] = a.u[24 * (size_t) j + q];
-        if (EAM && !DENSITY)
-          for (int q = 0; q < NPE; q++) erj[q] = (float) a.erho[NPE * (size_t) j + q];
-      }
-      const int nj = sid - sb0;
-      const float *S = s_shape + nj * NPE;
-      float sx, sy, sz;
-      site_rel(S, uj, sx, sy, sz);
-      float dx = ox + (ipx - sx), dy = oy + (ipy - sy), dz = oz + (ipz - sz);
+      float4 sh = __ldg(a.site_h + sid), sl = __ldg(a.site_l + sid);
+      float dx, dy, dz;
+      pair_vec(ih, il, sh, sl, dx, dy, dz);
       float rsq = dx * dx + dy * dy + dz * dz;
       bool in = rsq < a.cutsq_f;
       if (rsq >= a.band_lo && rsq <= a.band_hi) {
-        // FP64 re-test from the nodes, exactly as the FP64 path positions them
-        double ix, iy, iz, jx, jy, jz;
-        site64(N64, a.nodex + 24 * (size_t) e, ix, iy, iz);
-        site64(spa_inter64 + (size_t) nj * NPE, a.nodex + 24 * (size_t) j, jx, jy, jz);
-        double ddx = ix - jx, ddy = iy - jy, ddz = iz - jz;
-        if (DENSITY) {
-          const double *nxq = a.nodex + 24 * (size_t) e;
-          int q = it % NPE;
-          ddx = nxq[3 * q] - jx;
-          ddy = nxq[3 * q + 1] - jy;
-          ddz = nxq[3 * q + 2] - jz;
-        }
+        double ddx = ((double) ih.x + il.x) - ((double) sh.x + sl.x);
+        double ddy = ((double) ih.y + il.y) - ((double) sh.y + sl.y);
+        double ddz = ((double) ih.z + il.z) - ((double) sh.z + sl.z);
         in = ddx * ddx + ddy * ddy + ddz * ddz < a.cutsq;
       }
       if (in) {
@@ -371,12 +389,7 @@ k_ip(ElemArgs a, const double *__restrict__ spa_inter64, const float4 *__restric
             float4 c = s_tab[m];
             part += ((c.x * p + c.y) * p + c.z) * p + c.w;
           } else {
-            double rhoj = 0.0;
-            float rj = 0.f;
-#pragma unroll
-            for (int q = 0; q < NPE; q++) rj += S[q] * erj[q];
-            rhoj = (double) rj;
-            float fpj = (float) fprime64(rhoj, frho, nrho, rdrho);
+            float fpj = (float) fprime64((double) __ldg(a.site_rho + sid), frho, nrho, rdrho);
             float4 t0 = s_tab[3 * m], t1 = s_tab[3 * m + 1], t2 = s_tab[3 * m + 2];
             float rhoip = (t0.x * p + t0.y) * p + t0.z;
             float z2p = (t0.w * p + t1.x) * p + t1.y;
@@ -407,7 +420,7 @@ k_ip(ElemArgs a, const double *__restrict__ spa_inter64, const float4 *__restric
       }
     }
     if (DENSITY) {
-      out[it] = acc + (double) part;
+      out[NPE * (size_t) e + it % NPE] = acc + (double) part;
     } else {
       out[3 * r] = fx + (double) px;
       out[3 * r + 1] = fy + (double) py;
@@ -437,12 +450,6 @@ void split_hilo(const double4 *x, float4 *xh, float4 *xl, int n, cudaStream_t s)
   if (n <= 0) return;
   k_split_hilo<<<nblk(n, 256), 256, 0, s>>>(x, xh, xl, n);
   check(cudaGetLastError(), "split_hilo");
-}
-
-void elem_rel(const double *nodex, const double *ex, int n, float *u, cudaStream_t s) {
-  if (n <= 0) return;
-  k_elem_rel<<<nblk((long long) n * 24, 256), 256, 0, s>>>(nodex, ex, n, u);
-  check(cudaGetLastError(), "elem_rel");
 }
 
 void eam_rho_atoms(const MixedAtoms &m, const float4 *rhor_val, const EamTables &e,
@@ -478,32 +485,38 @@ void lj_atoms(const MixedAtoms &m, const int *type, const float *lj1, const floa
   check(cudaGetLastError(), "lj_atoms_mixed");
 }
 
-void ip_pass(const MixedElems &m, int pass, const double *spa_inter64, const float4 *tab,
-             const EamTables &e, float lj1, float lj2, double *out, cudaStream_t s) {
-  ElemArgs a{m.nodex, m.ex, m.erho, m.u, m.etype, m.row_elem, m.row_jj, m.row_first,
-             m.ipnum, m.ipent, m.site_base, m.nrows, m.rowstride, m.nall, m.nlocal_e,
-             m.spa_int, m.weight, m.int_off, m.node_list, m.shape, m.ninter, m.cutsq_f,
-             m.band_lo, m.band_hi, m.cutsq};
-  size_t smem_shape = sizeof(float4) * 2 * (size_t) m.ninter;
-  long long work;
+void sites_ds(const double *nodex, const int *etype, const int *site_base, const int *inter_num,
+              const float2 *shape_hl, int nelem, float4 *site_h, float4 *site_l, cudaStream_t s) {
+  if (nelem <= 0) return;
+  k_sites_ds<<<nelem, 128, 0, s>>>(nodex, etype, site_base, inter_num, shape_hl, site_h, site_l);
+  check(cudaGetLastError(), "sites_ds");
+}
+
+void site_rho(const double *erho, const int *etype, const int *site_base, const int *inter_num,
+              const float *shape, int nelem, float *rho, cudaStream_t s) {
+  if (nelem <= 0) return;
+  k_site_rho<<<nelem, 128, 0, s>>>(erho, etype, site_base, inter_num, shape, rho);
+  check(cudaGetLastError(), "site_rho");
+}
+
+void ip_pass(const MixedElems &m, int pass, const float4 *tab, const EamTables &e, float lj1,
+             float lj2, double *out, cudaStream_t s) {
+  ElemArgs a{m.nodex, m.erho, m.site_h, m.site_l, m.site_rho, m.etype, m.row_elem, m.row_jj,
+             m.row_first, m.ipnum, m.ipent, m.nrows, m.rowstride, m.nlocal_e, m.spa_int,
+             m.weight, m.int_off, m.node_list, m.cutsq_f, m.band_lo, m.band_hi, m.cutsq};
   if (pass == 0) {  // LJ forces
-    work = m.nrows;
-    size_t smem = smem_shape;
-    int g = persistent_grid((const void *) k_ip<false, false>, 256, smem, work);
-    k_ip<false, false><<<g, 256, smem, s>>>(a, spa_inter64, tab, 0, 0.f, nullptr, 0, 0.0,
-                                           lj1, lj2, out);
+    int g = persistent_grid((const void *) k_ip<false, false>, 256, 0, m.nrows);
+    k_ip<false, false><<<g, 256, 0, s>>>(a, tab, 0, 0.f, nullptr, 0, 0.0, lj1, lj2, out);
   } else if (pass == 1) {  // EAM nodal densities
-    work = (long long) m.nlocal_e * NPE;
-    size_t smem = smem_shape + sizeof(float4) * (e.nr + 1);
-    int g = persistent_grid((const void *) k_ip<true, true>, 256, smem, work);
-    k_ip<true, true><<<g, 256, smem, s>>>(a, spa_inter64, tab, e.nr, (float) e.rdr, e.frho,
-                                         e.nrho, e.rdrho, 0.f, 0.f, out);
+    size_t smem = sizeof(float4) * (e.nr + 1);
+    int g = persistent_grid((const void *) k_ip<true, true>, 256, smem, (long long) m.nlocal_e * NPE);
+    k_ip<true, true><<<g, 256, smem, s>>>(a, tab, e.nr, (float) e.rdr, e.frho, e.nrho, e.rdrho,
+                                         0.f, 0.f, out);
   } else {  // EAM forces
-    work = m.nrows;
-    size_t smem = smem_shape + sizeof(float4) * 3 * (e.nr + 1);
-    int g = persistent_grid((const void *) k_ip<true, false>, 256, smem, work);
-    k_ip<true, false><<<g, 256, smem, s>>>(a, spa_inter64, tab, e.nr, (float) e.rdr, e.frho,
-                                          e.nrho, e.rdrho, 0.f, 0.f, out);
+    size_t smem = sizeof(float4) * 3 * (e.nr + 1);
+    int g = persistent_grid((const void *) k_ip<true, false>, 256, smem, m.nrows);
+    k_ip<true, false><<<g, 256, smem, s>>>(a, tab, e.nr, (float) e.rdr, e.frho, e.nrho, e.rdrho,
+                                          0.f, 0.f, out);
   }
   check(cudaGetLastError(), "ip_pass_mixed");
 }
