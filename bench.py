@@ -350,6 +350,7 @@ def run_ours(a, ws, rank, local):
                 "elements": c0["enlocal"], "ghost_elements": c0["enghost"],
                 "gauss_points": cfg["gauss_per_element"] * c0["enlocal"],
                 "integration_rows": c0["ip_rows"], "sites": sites,
+                "interpolated_sites": c0["sites"], "sites_referenced": c0["sites_needed"],
                 "atom_list_mean": round(mean_neigh, 2),
                 "ip_list_mean": round(c0["ip_entries"] / max(c0["ip_rows"], 1), 2),
                 "rebuild": "every 10 steps if any displacement > skin/2 (check yes)",

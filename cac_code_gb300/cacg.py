@@ -209,10 +209,11 @@ class System:
 
     # ---- state out ----
     def counts(self) -> Dict[str, int]:
-        c = np.zeros(13, dtype=np.int64)
-        self._ok(self._L.cacg_get_counts(self.h, c.ctypes.data_as(_lp), 13))
+        c = np.zeros(15, dtype=np.int64)
+        self._ok(self._L.cacg_get_counts(self.h, c.ctypes.data_as(_lp), 15))
         keys = ["nlocal", "nghost", "atom_entries", "enlocal", "enghost", "elem_entries",
-                "ip_rows", "ip_entries", "rebuilds", "nstencil", "step", "sites", "launches"]
+                "ip_rows", "ip_entries", "rebuilds", "nstencil", "step", "sites", "launches",
+                "sites_needed", "force_rows"]
         return dict(zip(keys, (int(v) for v in c)))
 
     def atoms(self, all_: bool = False) -> Dict[str, np.ndarray]:

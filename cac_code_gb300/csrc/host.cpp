@@ -218,6 +218,8 @@ struct cacg_context {
   int maxeneigh = 32, estride = 0;
   DBuf<int> d_row_elem, d_row_jj, d_row_first, d_site_base, d_ipnum, d_ipent;
   DBuf<int> d_sipnum, d_sipent;
+  DBuf<int> d_force_rows, d_need, d_need_elem, d_site_flag, d_site_pos;
+  int nforce = 0, nneed = 0;
   int maxip = 128, rowstride = 0;
   // tables
   DBuf<double> d_spa_int, d_weight, d_spa_inter, d_spa_csub, d_spa_isub, d_frho, d_rhor, d_z2r;
@@ -370,7 +372,8 @@ cacg_context::~cacg_context() {
                      &d_row_elem, &d_row_jj, &d_row_first, &d_site_base, &d_ipnum, &d_ipent,
                      &d_int_off, &d_inter_off, &d_numint, &d_inter_num, &d_node_list,
                      &d_list_isub, &d_sub_first, &d_flags, &d_pos, &d_scan, &d_misc,
-                     &d_snum, &d_slist, &d_sipnum, &d_sipent};
+                     &d_snum, &d_slist, &d_sipnum, &d_sipent, &d_force_rows, &d_need,
+                     &d_need_elem, &d_site_flag, &d_site_pos};
   for (auto *b : bi) b->release();
   d_ljtab.release();
   for (auto &e : ev)
@@ -1254,6 +1257,12 @@ void cacg_context::init() {
     upload(d_row_elem, re, s);
     upload(d_row_jj, rj, s);
     upload(d_row_first, h_row_first, s);
+    // rows of nonzero weight: the only ones whose force reaches the nodes
+    std::vector<int> fr;
+    for (int r = 0; r < nrows; r++)
+      if (weight[h_etype[re[r]]][rj[r]] != 0.0) fr.push_back(r);
+    nforce = (int) fr.size();
+    upload(d_force_rows, fr, s);
     element_size();
   } else {
     nrows = 0;
@@ -1498,6 +1507,21 @@ void cacg_context::neighbor_nbuild() {
     maxip = (h_pin[5] + 8 + 7) / 8 * 8;
   }
   d_fip.ensure(3 * (size_t) std::max(nrows, 1), s);
+  check(cudaMemsetAsync(d_fip.p, 0, sizeof(double) * 3 * std::max(nrows, 1), s), "fip");
+  // the sites any list references: the per-step site kernels compute only these
+  d_site_flag.ensure(std::max(nsites, 1), s);
+  d_site_pos.ensure(std::max(nsites, 1), s);
+  check(cudaMemsetAsync(d_site_flag.p, 0, sizeof(int) * std::max(nsites, 1), s), "flag");
+  fp64_fma::mark_sites(d_ipnum.p, d_ipent.p, nrows, rowstride, d_site_flag.p, s);
+  scan_exclusive(d_site_flag.p, d_site_pos.p, nsites, d_misc.p + 7, d_scan, s);
+  check(cudaMemcpyAsync(h_pin + 7, d_misc.p + 7, sizeof(int), cudaMemcpyDeviceToHost, s), "nneed");
+  sync();
+  nneed = h_pin[7];
+  d_need.ensure(std::max(nneed, 1), s);
+  d_need_elem.ensure(std::max(nneed, 1), s);
+  fp64_fma::need_compact(d_site_flag.p, d_site_pos.p, nsites, d_site_base.p, nall, d_need.p,
+                         d_need_elem.p, s);
+  launches += 4;
   elists_built = true;
 }
 
@@ -1607,8 +1631,8 @@ void cacg_context::pair_ecompute_mixed() {
   ElemTables t = etab();
   d_site_h.ensure(std::max(nsites, 1), s);
   d_site_l.ensure(std::max(nsites, 1), s);
-  mixed::sites_ds(d_nodex.p, d_etype.p, d_site_base.p, d_inter_num.p, d_shape_hl.p, nall,
-                  d_site_h.p, d_site_l.p, s);
+  mixed::sites_ds_needed(d_nodex.p, d_site_base.p, d_need.p, d_need_elem.p, nneed, d_shape_hl.p,
+                         d_site_h.p, d_site_l.p, s);
   launches++;
   const float eps = 1.0e-4f;
   mixed::MixedElems m{};
@@ -1628,6 +1652,8 @@ void cacg_context::pair_ecompute_mixed() {
   m.weight = d_weight.p;
   m.int_off = d_int_off.p;
   m.node_list = d_node_list.p;
+  m.rows = d_force_rows.p;
+  m.nforce = nforce;
   if (pair_style == 1) {
     int a = 1 * (MAXT + 1) + 1;
     m.cutsq = ljtab.cutsq[a];
@@ -1647,8 +1673,8 @@ void cacg_context::pair_ecompute_mixed() {
     d_site_rho.ensure(std::max(nsites, 1), s);
     mixed::ip_pass(m, 1, d_rhor_val4.p, e, 0.f, 0.f, d_erho.p, s);
     launch_copy_root(d_erho.p, NPE, d_eroot.p, enlocal, enghost, s);
-    mixed::site_rho(d_erho.p, d_etype.p, d_site_base.p, d_inter_num.p, d_shape_f.p, nall,
-                    d_site_rho.p, s);
+    mixed::site_rho_needed(d_erho.p, d_site_base.p, d_need.p, d_need_elem.p, nneed, d_shape_f.p,
+                           d_site_rho.p, s);
     m.erho = d_erho.p;
     m.site_rho = d_site_rho.p;
     mixed::ip_pass(m, 2, d_ftab.p, e, 0.f, 0.f, d_fip.p, s);
@@ -1672,8 +1698,9 @@ void cacg_context::pair_ecompute() {
   // sites of every local and ghost element at the current node positions,
   // with their float copies, then this step's short lists of the rows
   d_site_h.ensure(std::max(nsites, 1), s);
-  if (exact) launch_sites(d_nodex.p, d_etype.p, d_site_base.p, nall, t, d_site_x.p, d_site_h.p, s);
-  else fp64_fma::sites(d_nodex.p, d_etype.p, d_site_base.p, nall, t, d_site_x.p, d_site_h.p, s);
+  // contraction-free in both modes: bit-identical to the all-sites kernel
+  fp64_fma::sites_needed(d_nodex.p, d_etype.p, d_site_base.p, d_need.p, d_need_elem.p, nneed, t,
+                         d_site_x.p, d_site_h.p, s);
   const double csq = pair_style == 1 ? ljtab.cutsq[1 * (MAXT + 1) + 1] : cutforcesq;
   const float cp = cut_pass(csq);
   d_sipnum.ensure(std::max(nrows, 1), s);
@@ -1688,9 +1715,9 @@ void cacg_context::pair_ecompute() {
       fp64_exact::lj_ip(d_nodex.p, d_etype.p, d_row_elem.p, d_row_jj.p, nrows, ipn, ipe,
                         rowstride, d_site_x.p, t, ljtab.lj1[a], ljtab.lj2[a], ljtab.cutsq[a], d_fip.p, s);
     else
-      fp64_fma::lj_ip(d_nodex.p, d_etype.p, d_row_elem.p, d_row_jj.p, nrows, ipn, ipe,
+      fp64_fma::lj_ip(d_nodex.p, d_etype.p, d_row_elem.p, d_row_jj.p, nforce, ipn, ipe,
                       rowstride, d_site_x.p, d_site_h.p, t, ljtab.lj1[a], ljtab.lj2[a], ljtab.cutsq[a],
-                      cp, d_fip.p, s);
+                      cp, d_force_rows.p, d_fip.p, s);
     launches++;
   } else {
     EamTables e = eamtab();
@@ -1708,9 +1735,11 @@ void cacg_context::pair_ecompute() {
       fp64_exact::eam_ip(d_nodex.p, d_erho.p, d_etype.p, d_row_elem.p, d_row_jj.p, nrows, ipn, ipe,
                          rowstride, d_site_x.p, d_site_fp.p, t, e, d_fip.p, s);
     } else {
-      fp64_fma::eam_site_fp(d_erho.p, d_etype.p, d_site_base.p, nall, t, e, d_site_fp.p, s);
-      fp64_fma::eam_ip(d_nodex.p, d_erho.p, d_etype.p, d_row_elem.p, d_row_jj.p, nrows, ipn, ipe,
-                       rowstride, d_site_x.p, d_site_h.p, d_site_fp.p, t, e, cp, d_fip.p, s);
+      fp64_fma::site_fp_needed(d_erho.p, d_etype.p, d_site_base.p, d_need.p, d_need_elem.p, nneed,
+                               t, e, d_site_fp.p, s);
+      fp64_fma::eam_ip(d_nodex.p, d_erho.p, d_etype.p, d_row_elem.p, d_row_jj.p, nforce, ipn, ipe,
+                       rowstride, d_site_x.p, d_site_h.p, d_site_fp.p, t, e, cp, d_force_rows.p,
+                       d_fip.p, s);
     }
     launches += 4;
   }
@@ -2064,9 +2093,9 @@ int cacg_run(cacg_handle h, int nsteps) {
 
 int cacg_get_counts(cacg_handle h, long long *c, int n) {
   API_BEGIN
-  long long v[13] = {h->nlocal, h->nghost, 0, h->enlocal, h->enghost, 0, h->nrows, 0,
+  long long v[15] = {h->nlocal, h->nghost, 0, h->enlocal, h->enghost, 0, h->nrows, 0,
                      h->nrebuild, (long long) h->stencil.size(), h->ntimestep, h->nsites,
-                     h->launches};
+                     h->launches, h->nneed, h->nforce};
   if (h->list_built && h->nlocal) {
     std::vector<int> num(h->nlocal);
     check(cudaMemcpyAsync(num.data(), h->d_num.p, sizeof(int) * h->nlocal, cudaMemcpyDeviceToHost, h->stream), "num");
@@ -2085,7 +2114,7 @@ int cacg_get_counts(cacg_handle h, long long *c, int n) {
     h->sync();
     for (int x : num) v[7] += x;
   }
-  for (int i = 0; i < n && i < 13; i++) c[i] = v[i];
+  for (int i = 0; i < n && i < 15; i++) c[i] = v[i];
   API_END
 }
 

@@ -192,7 +192,7 @@ void eam_force_atoms(const double4 *x, const float4 *xh, const int *num, const i
 void lj_ip(const double *nodex, const int *etype, const int *row_elem, const int *row_jj,
            int nrows, const int *ipnum, const int *ipent, int rowstride, const double4 *site_x,
            const float4 *site_h, ElemTables t, double lj1, double lj2, double cutsq,
-           float cut_pass, double *fip, cudaStream_t s);
+           float cut_pass, const int *rows, double *fip, cudaStream_t s);
 void eam_erho(const double *nodex, const int *etype, const int *row_first, int nlocal_e,
               const int *ipnum, const int *ipent, int rowstride, const double4 *site_x,
               const float4 *site_h, ElemTables t, EamTables e, float cut_pass, double *erho,
@@ -202,11 +202,22 @@ void eam_site_fp(const double *erho, const int *etype, const int *site_base, int
 void eam_ip(const double *nodex, const double *erho, const int *etype, const int *row_elem,
             const int *row_jj, int nrows, const int *ipnum, const int *ipent, int rowstride,
             const double4 *site_x, const float4 *site_h, const double *site_fp, ElemTables t,
-            EamTables e, float cut_pass, double *fip, cudaStream_t s);
+            EamTables e, float cut_pass, const int *rows, double *fip, cudaStream_t s);
 void gather_nodef(const double *fip, const int *etype, const int *row_first, int nlocal_e,
                   ElemTables t, double *nodef, cudaStream_t s);
 void sites(const double *nodex, const int *etype, const int *site_base, int nelem, ElemTables t,
            double4 *site_x, float4 *site_h, cudaStream_t s);
+// the sites any integration-point list references (computed per rebuild)
+void mark_sites(const int *ipnum, const int *ipent, int nrows, int rowstride, int *flag,
+                cudaStream_t s);
+void need_compact(const int *flag, const int *pos, int nsites, const int *site_base, int nall,
+                  int *need, int *need_elem, cudaStream_t s);
+void sites_needed(const double *nodex, const int *etype, const int *site_base, const int *need,
+                  const int *need_elem, int nneed, ElemTables t, double4 *site_x, float4 *site_h,
+                  cudaStream_t s);
+void site_fp_needed(const double *erho, const int *etype, const int *site_base, const int *need,
+                    const int *need_elem, int nneed, ElemTables t, EamTables e, double *site_fp,
+                    cudaStream_t s);
 // per-step short lists (FP32 guarded cutoff test), used by both FP64 modes
 void filter_atoms(const float4 *xh, const int *num, const int *list, int stride, int nlocal,
                   float cut_pass, int *snum, int *slist, cudaStream_t s);
@@ -234,6 +245,8 @@ struct MixedElems {
   int nrows, rowstride, nlocal_e;
   const double *spa_int, *weight;
   const int *int_off, *node_list;
+  const int *rows;  // rows of nonzero weight (force passes), count nforce
+  int nforce;
   float cutsq_f, band_lo, band_hi;
   double cutsq;
 };
@@ -242,6 +255,12 @@ void sites_ds(const double *nodex, const int *etype, const int *site_base, const
               const float2 *shape_hl, int nelem, float4 *site_h, float4 *site_l, cudaStream_t s);
 void site_rho(const double *erho, const int *etype, const int *site_base, const int *inter_num,
               const float *shape, int nelem, float *rho, cudaStream_t s);
+void sites_ds_needed(const double *nodex, const int *site_base, const int *need,
+                     const int *need_elem, int nneed, const float2 *shape_hl, float4 *site_h,
+                     float4 *site_l, cudaStream_t s);
+void site_rho_needed(const double *erho, const int *site_base, const int *need,
+                     const int *need_elem, int nneed, const float *shape, float *rho,
+                     cudaStream_t s);
 void eam_rho_atoms(const MixedAtoms &m, const float4 *rhor_val, const EamTables &e,
                    double *rho, double *fp, cudaStream_t s);
 void eam_force_atoms(const MixedAtoms &m, const float4 *ftab, const EamTables &e,

@@ -199,9 +199,11 @@ k_lj_ip(const double *__restrict__ nodex, const int *__restrict__ etype,
         const int *__restrict__ row_elem, const int *__restrict__ row_jj, int nrows,
         const int *__restrict__ ipnum, const int *__restrict__ ipent, int rowstride,
         const double4 *__restrict__ site_x, const float4 *__restrict__ site_h, ElemTables t,
-        double lj1, double lj2, double cutsq, float cut_pass, double *__restrict__ fip) {
+        double lj1, double lj2, double cutsq, float cut_pass, const int *__restrict__ rows,
+        double *__restrict__ fip) {
   int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nrows) return;
+  if (rows) r = rows[r];
   const int e = row_elem[r], jj = row_jj[r], ty = etype[e];
   double fx = 0, fy = 0, fz = 0;
   if (t.weight[t.int_off[ty] + jj] != 0.0) {
@@ -289,9 +291,10 @@ k_eam_ip(const double *__restrict__ nodex, const double *__restrict__ erho,
          const int *__restrict__ row_jj, int nrows, const int *__restrict__ ipnum,
          const int *__restrict__ ipent, int rowstride, const double4 *__restrict__ site_x,
          const float4 *__restrict__ site_h, const double *__restrict__ site_fp, ElemTables t,
-         EamTables eam, float cut_pass, double *__restrict__ fip) {
+         EamTables eam, float cut_pass, const int *__restrict__ rows, double *__restrict__ fip) {
   int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nrows) return;
+  if (rows) r = rows[r];
   const int e = row_elem[r], jj = row_jj[r], ty = etype[e];
   double fx = 0, fy = 0, fz = 0;
   if (t.weight[t.int_off[ty] + jj] != 0.0) {
@@ -404,6 +407,68 @@ k_filter_rows(const double *__restrict__ nodex, const int *__restrict__ etype,
   snum[r] = m;
 }
 
+// Sites referenced by any integration-point list (built once per rebuild):
+// flag every entry's site, then the host compacts the flags into `need` and the
+// owning element of each needed site into `need_elem`.
+__global__ void k_mark_sites(const int *__restrict__ ipnum, const int *__restrict__ ipent,
+                             int nrows, int rowstride, int *__restrict__ flag) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  const int n = ipnum[r];
+  for (int k = 0; k < n; k++) flag[__ldg(ipent + (size_t) k * rowstride + r)] = 1;
+}
+
+__global__ void k_need_compact(const int *__restrict__ flag, const int *__restrict__ pos,
+                               int nsites, const int *__restrict__ site_base, int nall,
+                               int *__restrict__ need, int *__restrict__ need_elem) {
+  int sid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (sid >= nsites || !flag[sid]) return;
+  int lo = 0, hi = nall;  // site_base[lo] <= sid < site_base[hi]
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (site_base[mid] <= sid) lo = mid;
+    else hi = mid;
+  }
+  need[pos[sid]] = sid;
+  need_elem[pos[sid]] = lo;
+}
+
+// positions of the needed sites, contraction-free (both FP64 modes), one thread
+// per site; consecutive needed sites mostly share their element's nodes in L1
+__global__ void k_sites_needed(const double *__restrict__ nodex, const int *__restrict__ etype,
+                               const int *__restrict__ site_base, const int *__restrict__ need,
+                               const int *__restrict__ need_elem, int nneed, ElemTables t,
+                               double4 *__restrict__ site_x, float4 *__restrict__ site_h) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nneed) return;
+  const int sid = need[q], j = need_elem[q];
+  const int nj = sid - site_base[j];
+  const double *S = t.spa_inter + ((size_t) t.inter_off[etype[j]] + nj) * NPE;
+  double a, b, c;
+  ip_position(S, nodex + 24 * (size_t) j, a, b, c);
+  site_x[sid] = make_double4(a, b, c, 0.0);
+  site_h[sid] = make_float4((float) a, (float) b, (float) c, 0.f);
+}
+
+// F'(rho) of the needed sites (pair_eam.cpp:1060-1076)
+__global__ void k_site_fp_needed(const double *__restrict__ erho, const int *__restrict__ etype,
+                                 const int *__restrict__ site_base, const int *__restrict__ need,
+                                 const int *__restrict__ need_elem, int nneed, ElemTables t,
+                                 EamTables eam, double *__restrict__ site_fp) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nneed) return;
+  const int sid = need[q], j = need_elem[q];
+  const int nj = sid - site_base[j];
+  const double *S = t.spa_inter + ((size_t) t.inter_off[etype[j]] + nj) * NPE;
+  const double *er = erho + NPE * (size_t) j;
+  double rho = 0;
+#pragma unroll
+  for (int k = 0; k < NPE; k++) rho += S[k] * er[k];
+  double p;
+  int m = rhoindex(rho, eam, p);
+  site_fp[sid] = spline_deriv(eam.frho + 7 * m, p);
+}
+
 // site positions with fused multiply-adds (the exact mode uses k_sites in
 // k_neigh.cu, built without contraction); also writes the float copy
 __global__ void k_sites_fma(const double *__restrict__ nodex, const int *__restrict__ etype,
@@ -447,6 +512,39 @@ void filter_rows(const double *nodex, const int *etype, const int *row_elem, con
   check(cudaGetLastError(), "filter_rows");
 }
 
+void mark_sites(const int *ipnum, const int *ipent, int nrows, int rowstride, int *flag,
+                cudaStream_t s) {
+  if (nrows <= 0) return;
+  k_mark_sites<<<nblk(nrows, 128), 128, 0, s>>>(ipnum, ipent, nrows, rowstride, flag);
+  check(cudaGetLastError(), "mark_sites");
+}
+
+void need_compact(const int *flag, const int *pos, int nsites, const int *site_base, int nall,
+                  int *need, int *need_elem, cudaStream_t s) {
+  if (nsites <= 0) return;
+  k_need_compact<<<nblk(nsites, 256), 256, 0, s>>>(flag, pos, nsites, site_base, nall, need,
+                                                  need_elem);
+  check(cudaGetLastError(), "need_compact");
+}
+
+void sites_needed(const double *nodex, const int *etype, const int *site_base, const int *need,
+                  const int *need_elem, int nneed, ElemTables t, double4 *site_x, float4 *site_h,
+                  cudaStream_t s) {
+  if (nneed <= 0) return;
+  k_sites_needed<<<nblk(nneed, 128), 128, 0, s>>>(nodex, etype, site_base, need, need_elem,
+                                                 nneed, t, site_x, site_h);
+  check(cudaGetLastError(), "sites_needed");
+}
+
+void site_fp_needed(const double *erho, const int *etype, const int *site_base, const int *need,
+                    const int *need_elem, int nneed, ElemTables t, EamTables e, double *site_fp,
+                    cudaStream_t s) {
+  if (nneed <= 0) return;
+  k_site_fp_needed<<<nblk(nneed, 128), 128, 0, s>>>(erho, etype, site_base, need, need_elem,
+                                                   nneed, t, e, site_fp);
+  check(cudaGetLastError(), "site_fp_needed");
+}
+
 void sites(const double *nodex, const int *etype, const int *site_base, int nelem, ElemTables t,
            double4 *site_x, float4 *site_h, cudaStream_t s) {
   if (nelem <= 0) return;
@@ -484,11 +582,11 @@ void eam_force_atoms(const double4 *x, const float4 *xh, const int *num, const i
 void lj_ip(const double *nodex, const int *etype, const int *row_elem, const int *row_jj,
            int nrows, const int *ipnum, const int *ipent, int rowstride, const double4 *site_x,
            const float4 *site_h, ElemTables t, double lj1, double lj2, double cutsq,
-           float cut_pass, double *fip, cudaStream_t s) {
+           float cut_pass, const int *rows, double *fip, cudaStream_t s) {
   if (nrows <= 0) return;
   k_lj_ip<<<nblk(nrows, 128), 128, 0, s>>>(nodex, etype, row_elem, row_jj, nrows, ipnum, ipent,
                                           rowstride, site_x, site_h, t, lj1, lj2, cutsq,
-                                          cut_pass, fip);
+                                          cut_pass, rows, fip);
   check(cudaGetLastError(), "lj_ip_fma");
 }
 
@@ -513,11 +611,11 @@ void eam_site_fp(const double *erho, const int *etype, const int *site_base, int
 void eam_ip(const double *nodex, const double *erho, const int *etype, const int *row_elem,
             const int *row_jj, int nrows, const int *ipnum, const int *ipent, int rowstride,
             const double4 *site_x, const float4 *site_h, const double *site_fp, ElemTables t,
-            EamTables e, float cut_pass, double *fip, cudaStream_t s) {
+            EamTables e, float cut_pass, const int *rows, double *fip, cudaStream_t s) {
   if (nrows <= 0) return;
   k_eam_ip<<<nblk(nrows, 128), 128, 0, s>>>(nodex, erho, etype, row_elem, row_jj, nrows, ipnum,
                                            ipent, rowstride, site_x, site_h, site_fp, t, e,
-                                           cut_pass, fip);
+                                           cut_pass, rows, fip);
   check(cudaGetLastError(), "eam_ip_fma");
 }
 

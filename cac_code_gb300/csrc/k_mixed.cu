@@ -270,6 +270,52 @@ __global__ void k_sites_ds(const double *__restrict__ nodex, const int *__restri
   }
 }
 
+// double-single positions of the needed sites only (one thread per site)
+__global__ void k_sites_ds_needed(const double *__restrict__ nodex,
+                                  const int *__restrict__ site_base, const int *__restrict__ need,
+                                  const int *__restrict__ need_elem, int nneed,
+                                  const float2 *__restrict__ shape_hl,
+                                  float4 *__restrict__ site_h, float4 *__restrict__ site_l) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nneed) return;
+  const int sid = need[q], j = need_elem[q];
+  const int nj = sid - site_base[j];
+  const float2 *S = shape_hl + (size_t) nj * NPE;
+  const double *nx = nodex + 24 * (size_t) j;
+  float xh = 0.f, xl = 0.f, yh = 0.f, yl = 0.f, zh = 0.f, zl = 0.f;
+#pragma unroll
+  for (int k = 0; k < NPE; k++) {
+    float2 w = S[k];
+    float ah, al, bh, bl, ch, cl;
+    ds_split(nx[3 * k], ah, al);
+    ds_split(nx[3 * k + 1], bh, bl);
+    ds_split(nx[3 * k + 2], ch, cl);
+    ds_acc_prod(xh, xl, w.x, w.y, ah, al);
+    ds_acc_prod(yh, yl, w.x, w.y, bh, bl);
+    ds_acc_prod(zh, zl, w.x, w.y, ch, cl);
+  }
+  ds_norm(xh, xl);
+  ds_norm(yh, yl);
+  ds_norm(zh, zl);
+  site_h[sid] = make_float4(xh, yh, zh, 0.f);
+  site_l[sid] = make_float4(xl, yl, zl, 0.f);
+}
+
+__global__ void k_site_rho_needed(const double *__restrict__ erho,
+                                  const int *__restrict__ site_base, const int *__restrict__ need,
+                                  const int *__restrict__ need_elem, int nneed,
+                                  const float *__restrict__ shape, float *__restrict__ site_rho) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nneed) return;
+  const int sid = need[q], j = need_elem[q];
+  const float *S = shape + (size_t) (sid - site_base[j]) * NPE;
+  const double *er = erho + NPE * (size_t) j;
+  float r = 0.f;
+#pragma unroll
+  for (int k = 0; k < NPE; k++) r += S[k] * (float) er[k];
+  site_rho[sid] = r;
+}
+
 // density at every site, rho_s = sum_k N_k erho_k (FP32; pair_eam.cpp:1060-1065)
 __global__ void k_site_rho(const double *__restrict__ erho, const int *__restrict__ etype,
                            const int *__restrict__ site_base, const int *__restrict__ inter_num,
@@ -297,6 +343,8 @@ struct ElemArgs {
   int nrows, rowstride, nlocal_e;
   const double *spa_int, *weight;
   const int *int_off, *node_list;
+  const int *rows;
+  int nforce;
   float cutsq_f, band_lo, band_hi;
   double cutsq;
 };
@@ -334,7 +382,7 @@ k_ip(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr,
   const int ntab = EAM ? (DENSITY ? (nr + 1) : 3 * (nr + 1)) : 0;
   for (int m = threadIdx.x; m < ntab; m += blockDim.x) s_tab[m] = tab[m];
   __syncthreads();
-  const int nitems = DENSITY ? a.nlocal_e * NPE : a.nrows;
+  const int nitems = DENSITY ? a.nlocal_e * NPE : a.nforce;
   for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < nitems; it += gridDim.x * blockDim.x) {
     int r, e, ty, jj;
     if (DENSITY) {
@@ -343,14 +391,10 @@ k_ip(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr,
       jj = a.node_list[ty * NPE + it % NPE];
       r = a.row_first[e] + jj;
     } else {
-      r = it;
+      r = a.rows[it];  // rows of nonzero weight only; the others stay zero
       e = a.row_elem[r];
       ty = a.etype[e];
       jj = a.row_jj[r];
-      if (a.weight[a.int_off[ty] + jj] == 0.0) {
-        out[3 * r] = out[3 * r + 1] = out[3 * r + 2] = 0.0;
-        continue;
-      }
     }
     const double *N64 = a.spa_int + ((size_t) a.int_off[ty] + jj) * NPE;
     const double *nxe = a.nodex + 24 * (size_t) e;
@@ -492,6 +536,24 @@ void sites_ds(const double *nodex, const int *etype, const int *site_base, const
   check(cudaGetLastError(), "sites_ds");
 }
 
+void sites_ds_needed(const double *nodex, const int *site_base, const int *need,
+                     const int *need_elem, int nneed, const float2 *shape_hl, float4 *site_h,
+                     float4 *site_l, cudaStream_t s) {
+  if (nneed <= 0) return;
+  k_sites_ds_needed<<<nblk(nneed, 128), 128, 0, s>>>(nodex, site_base, need, need_elem, nneed,
+                                                    shape_hl, site_h, site_l);
+  check(cudaGetLastError(), "sites_ds_needed");
+}
+
+void site_rho_needed(const double *erho, const int *site_base, const int *need,
+                     const int *need_elem, int nneed, const float *shape, float *rho,
+                     cudaStream_t s) {
+  if (nneed <= 0) return;
+  k_site_rho_needed<<<nblk(nneed, 128), 128, 0, s>>>(erho, site_base, need, need_elem, nneed,
+                                                    shape, rho);
+  check(cudaGetLastError(), "site_rho_needed");
+}
+
 void site_rho(const double *erho, const int *etype, const int *site_base, const int *inter_num,
               const float *shape, int nelem, float *rho, cudaStream_t s) {
   if (nelem <= 0) return;
@@ -503,9 +565,10 @@ void ip_pass(const MixedElems &m, int pass, const float4 *tab, const EamTables &
              float lj2, double *out, cudaStream_t s) {
   ElemArgs a{m.nodex, m.erho, m.site_h, m.site_l, m.site_rho, m.etype, m.row_elem, m.row_jj,
              m.row_first, m.ipnum, m.ipent, m.nrows, m.rowstride, m.nlocal_e, m.spa_int,
-             m.weight, m.int_off, m.node_list, m.cutsq_f, m.band_lo, m.band_hi, m.cutsq};
+             m.weight, m.int_off, m.node_list, m.rows, m.nforce, m.cutsq_f, m.band_lo,
+             m.band_hi, m.cutsq};
   if (pass == 0) {  // LJ forces
-    int g = persistent_grid((const void *) k_ip<false, false>, 256, 0, m.nrows);
+    int g = persistent_grid((const void *) k_ip<false, false>, 256, 0, m.nforce);
     k_ip<false, false><<<g, 256, 0, s>>>(a, tab, 0, 0.f, nullptr, 0, 0.0, lj1, lj2, out);
   } else if (pass == 1) {  // EAM nodal densities
     size_t smem = sizeof(float4) * (e.nr + 1);
@@ -514,7 +577,7 @@ void ip_pass(const MixedElems &m, int pass, const float4 *tab, const EamTables &
                                          0.f, 0.f, out);
   } else {  // EAM forces
     size_t smem = sizeof(float4) * 3 * (e.nr + 1);
-    int g = persistent_grid((const void *) k_ip<true, false>, 256, smem, m.nrows);
+    int g = persistent_grid((const void *) k_ip<true, false>, 256, smem, m.nforce);
     k_ip<true, false><<<g, 256, smem, s>>>(a, tab, e.nr, (float) e.rdr, e.frho, e.nrho, e.rdrho,
                                           0.f, 0.f, out);
   }
