@@ -198,9 +198,9 @@ struct cacg_context {
   // mixed precision: low parts of the double-single coordinates, element node
   // offsets, FP32 spline and shape tables
   DBuf<float4> d_xl, d_rhor_val4, d_ftab, d_site_l;
-  DBuf<float2> d_shape_hl;
+  DBuf<float2> d_shape_hl, d_node_hl, d_spa_int_hl;
   DBuf<float> d_u, d_shape_f, d_ljf, d_site_rho;
-  DBuf<double> d_cutsq64;
+  DBuf<double> d_cutsq64, d_stage;
   DBuf<double> d_v, d_f, d_xhold, d_rho, d_fp, d_mass;
   DBuf<int> d_type, d_tag, d_root, d_send;
   DBuf<int> d_abin, d_bcount, d_bstart, d_bmem, d_stencil;
@@ -358,9 +358,12 @@ cacg_context::~cacg_context() {
   d_shape_f.release();
   d_site_l.release();
   d_shape_hl.release();
+  d_node_hl.release();
+  d_spa_int_hl.release();
   d_site_rho.release();
   d_ljf.release();
   d_cutsq64.release();
+  d_stage.release();
   DBuf<double> *bd[] = {&d_v, &d_f, &d_xhold, &d_rho, &d_fp, &d_mass, &d_ex, &d_nodex, &d_nodev,
                         &d_nodef, &d_nodexhold, &d_erho, &d_emass, &d_diag, &d_fip, &d_site_fp,
                         &d_spa_int, &d_weight, &d_spa_inter, &d_spa_csub, &d_spa_isub, &d_frho,
@@ -968,6 +971,10 @@ void cacg_context::element_tables() {
   }
   upload(d_shape_f, shf, s);
   upload(d_shape_hl, shl, s);
+  std::vector<float2> sihl(spa_int.size());
+  for (size_t k = 0; k < spa_int.size(); k++)
+    sihl[k] = make_float2((float) spa_int[k], (float) (spa_int[k] - (double) (float) spa_int[k]));
+  upload(d_spa_int_hl, sihl, s);
 }
 
 // FP32 copies of the tables the mixed-precision kernels read from shared memory
@@ -1631,8 +1638,11 @@ void cacg_context::pair_ecompute_mixed() {
   ElemTables t = etab();
   d_site_h.ensure(std::max(nsites, 1), s);
   d_site_l.ensure(std::max(nsites, 1), s);
-  mixed::sites_ds_needed(d_nodex.p, d_site_base.p, d_need.p, d_need_elem.p, nneed, d_shape_hl.p,
+  d_node_hl.ensure((size_t) 24 * nall, s);
+  mixed::node_split(d_nodex.p, nall, d_node_hl.p, s);
+  mixed::sites_ds_needed(d_node_hl.p, d_site_base.p, d_need.p, d_need_elem.p, nneed, d_shape_hl.p,
                          d_site_h.p, d_site_l.p, s);
+  launches++;
   launches++;
   const float eps = 1.0e-4f;
   mixed::MixedElems m{};
@@ -1654,6 +1664,8 @@ void cacg_context::pair_ecompute_mixed() {
   m.node_list = d_node_list.p;
   m.rows = d_force_rows.p;
   m.nforce = nforce;
+  m.node_hl = d_node_hl.p;
+  m.spa_int_hl = d_spa_int_hl.p;
   if (pair_style == 1) {
     int a = 1 * (MAXT + 1) + 1;
     m.cutsq = ljtab.cutsq[a];
@@ -2124,14 +2136,9 @@ int cacg_get_atoms(cacg_handle h, int all, double *x, double *v, double *f, int 
   int n = all ? h->nlocal + h->nghost : h->nlocal;
   cudaStream_t s = h->stream;
   if (x && n) {
-    std::vector<double4> x4(n);
-    check(cudaMemcpyAsync(x4.data(), h->d_x.p, sizeof(double4) * n, cudaMemcpyDeviceToHost, s), "x");
-    h->sync();
-    for (int i = 0; i < n; i++) {
-      x[3 * i] = x4[i].x;
-      x[3 * i + 1] = x4[i].y;
-      x[3 * i + 2] = x4[i].z;
-    }
+    h->d_stage.ensure(3 * (size_t) n, s);
+    launch_unpack4to3(h->d_x.p, h->d_stage.p, n, s);
+    check(cudaMemcpyAsync(x, h->d_stage.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s), "x");
   }
   if (v && h->nlocal) check(cudaMemcpyAsync(v, h->d_v.p, sizeof(double) * 3 * h->nlocal, cudaMemcpyDeviceToHost, s), "v");
   if (f && h->nlocal) check(cudaMemcpyAsync(f, h->d_f.p, sizeof(double) * 3 * h->nlocal, cudaMemcpyDeviceToHost, s), "f");
@@ -2240,15 +2247,13 @@ int cacg_put_atoms(cacg_handle h, const double *x, const double *v) {
   API_BEGIN
   if (!h->inited) fail(CACG_ESTATE, "no device state yet (cacg_init)");
   int n = h->nlocal;
+  cudaStream_t s = h->stream;
   if (n && x) {
-    // interleave into the device's padded layout through a staging copy
-    static thread_local std::vector<double4> x4;
-    x4.resize(n);
-    for (int i = 0; i < n; i++) x4[i] = make_double4(x[3 * i], x[3 * i + 1], x[3 * i + 2], 0.0);
-    check(cudaMemcpyAsync(h->d_x.p, x4.data(), sizeof(double4) * n, cudaMemcpyHostToDevice, h->stream), "put x");
-    h->sync();
+    h->d_stage.ensure(3 * (size_t) n, s);
+    check(cudaMemcpyAsync(h->d_stage.p, x, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s), "put x");
+    launch_pack3to4(h->d_stage.p, h->d_x.p, n, s);
   }
-  if (n && v) check(cudaMemcpyAsync(h->d_v.p, v, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, h->stream), "put v");
+  if (n && v) check(cudaMemcpyAsync(h->d_v.p, v, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s), "put v");
   API_END
 }
 

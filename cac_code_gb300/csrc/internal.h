@@ -249,13 +249,16 @@ struct MixedElems {
   int nforce;
   float cutsq_f, band_lo, band_hi;
   double cutsq;
+  const float2 *node_hl;     // [nall][24] double-single node coordinates
+  const float2 *spa_int_hl;  // double-single integration-point shape functions
 };
 void split_hilo(const double4 *x, float4 *xh, float4 *xl, int n, cudaStream_t s);
 void sites_ds(const double *nodex, const int *etype, const int *site_base, const int *inter_num,
               const float2 *shape_hl, int nelem, float4 *site_h, float4 *site_l, cudaStream_t s);
 void site_rho(const double *erho, const int *etype, const int *site_base, const int *inter_num,
               const float *shape, int nelem, float *rho, cudaStream_t s);
-void sites_ds_needed(const double *nodex, const int *site_base, const int *need,
+void node_split(const double *nodex, int n, float2 *hl, cudaStream_t s);
+void sites_ds_needed(const float2 *node_hl, const int *site_base, const int *need,
                      const int *need_elem, int nneed, const float2 *shape_hl, float4 *site_h,
                      float4 *site_l, cudaStream_t s);
 void site_rho_needed(const double *erho, const int *site_base, const int *need,
@@ -291,5 +294,7 @@ void launch_hold_atoms(const double4 *x, double *xhold, int n, cudaStream_t s);
 void launch_elem_diag(const double *nodex, const double *ex, int n, double *diag,
                       int *centre_bad, cudaStream_t s);
 double fp64_fma_rate(cudaStream_t s);
+void launch_pack3to4(const double *in, double4 *out, int n, cudaStream_t s);
+void launch_unpack4to3(const double4 *in, double *out, int n, cudaStream_t s);
 
 }  // namespace cacg

@@ -79,7 +79,7 @@ struct AtomArgs {
   double cutsq;
 };
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(512, 2)
 k_eam_rho_atoms(AtomArgs a, const float4 *__restrict__ rhor_val, int nr, float rdr,
                 const double *__restrict__ frho, int nrho, double rdrho,
                 double *__restrict__ rho, double *__restrict__ fp) {
@@ -116,7 +116,7 @@ k_eam_rho_atoms(AtomArgs a, const float4 *__restrict__ rhor_val, int nr, float r
 }
 
 // force table per knot: rho'(r) c0..c2 (x,y,z of f0), r*phi c0..c6 (w of f0, f1, f2.xy)
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(512, 2)
 k_eam_force_atoms(AtomArgs a, const float4 *__restrict__ ftab, int nr, float rdr,
                   const double *__restrict__ fp, double *__restrict__ f) {
   extern __shared__ float4 s_tab[];  // 3 float4 per knot
@@ -167,7 +167,7 @@ k_eam_force_atoms(AtomArgs a, const float4 *__restrict__ ftab, int nr, float rdr
 
 // band_lo/band_hi are relative factors here: a pair with rsq in
 // [band_lo, band_hi] * cutsq(type pair) is decided in FP64
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(512, 2)
 k_lj_atoms(AtomArgs a, const int *__restrict__ type, const float *__restrict__ lj1,
            const float *__restrict__ lj2, const float *__restrict__ cutsq_t,
            const double *__restrict__ cutsq64, double *__restrict__ f) {
@@ -270,8 +270,17 @@ __global__ void k_sites_ds(const double *__restrict__ nodex, const int *__restri
   }
 }
 
+// node coordinates as double-single pairs, once per element and step
+__global__ void k_node_split(const double *__restrict__ nodex, int n, float2 *__restrict__ hl) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * 24) return;
+  float h, l;
+  ds_split(nodex[t], h, l);
+  hl[t] = make_float2(h, l);
+}
+
 // double-single positions of the needed sites only (one thread per site)
-__global__ void k_sites_ds_needed(const double *__restrict__ nodex,
+__global__ void k_sites_ds_needed(const float2 *__restrict__ node_hl,
                                   const int *__restrict__ site_base, const int *__restrict__ need,
                                   const int *__restrict__ need_elem, int nneed,
                                   const float2 *__restrict__ shape_hl,
@@ -281,18 +290,15 @@ __global__ void k_sites_ds_needed(const double *__restrict__ nodex,
   const int sid = need[q], j = need_elem[q];
   const int nj = sid - site_base[j];
   const float2 *S = shape_hl + (size_t) nj * NPE;
-  const double *nx = nodex + 24 * (size_t) j;
+  const float2 *nx = node_hl + 24 * (size_t) j;
   float xh = 0.f, xl = 0.f, yh = 0.f, yl = 0.f, zh = 0.f, zl = 0.f;
 #pragma unroll
   for (int k = 0; k < NPE; k++) {
     float2 w = S[k];
-    float ah, al, bh, bl, ch, cl;
-    ds_split(nx[3 * k], ah, al);
-    ds_split(nx[3 * k + 1], bh, bl);
-    ds_split(nx[3 * k + 2], ch, cl);
-    ds_acc_prod(xh, xl, w.x, w.y, ah, al);
-    ds_acc_prod(yh, yl, w.x, w.y, bh, bl);
-    ds_acc_prod(zh, zl, w.x, w.y, ch, cl);
+    float2 a = __ldg(nx + 3 * k), b = __ldg(nx + 3 * k + 1), c = __ldg(nx + 3 * k + 2);
+    ds_acc_prod(xh, xl, w.x, w.y, a.x, a.y);
+    ds_acc_prod(yh, yl, w.x, w.y, b.x, b.y);
+    ds_acc_prod(zh, zl, w.x, w.y, c.x, c.y);
   }
   ds_norm(xh, xl);
   ds_norm(yh, yl);
@@ -347,22 +353,21 @@ struct ElemArgs {
   int nforce;
   float cutsq_f, band_lo, band_hi;
   double cutsq;
+  const float2 *node_hl, *spa_int_hl;
 };
 
-// integration-point position in double-single from the FP64 nodes
-__device__ __forceinline__ void ip_ds(const double *__restrict__ N, const double *__restrict__ nx,
+// integration-point position in double-single from the split nodes and the
+// split integration-point shape functions
+__device__ __forceinline__ void ip_ds(const float2 *__restrict__ N, const float2 *__restrict__ nx,
                                       float4 &h, float4 &l) {
   float xh = 0.f, xl = 0.f, yh = 0.f, yl = 0.f, zh = 0.f, zl = 0.f;
 #pragma unroll
   for (int k = 0; k < NPE; k++) {
-    float wh, wl, ah, al, bh, bl, ch, cl;
-    ds_split(N[k], wh, wl);
-    ds_split(nx[3 * k], ah, al);
-    ds_split(nx[3 * k + 1], bh, bl);
-    ds_split(nx[3 * k + 2], ch, cl);
-    ds_acc_prod(xh, xl, wh, wl, ah, al);
-    ds_acc_prod(yh, yl, wh, wl, bh, bl);
-    ds_acc_prod(zh, zl, wh, wl, ch, cl);
+    float2 w = N[k];
+    float2 a = nx[3 * k], b = nx[3 * k + 1], c = nx[3 * k + 2];
+    ds_acc_prod(xh, xl, w.x, w.y, a.x, a.y);
+    ds_acc_prod(yh, yl, w.x, w.y, b.x, b.y);
+    ds_acc_prod(zh, zl, w.x, w.y, c.x, c.y);
   }
   ds_norm(xh, xl);
   ds_norm(yh, yl);
@@ -374,7 +379,7 @@ __device__ __forceinline__ void ip_ds(const double *__restrict__ N, const double
 // One thread per integration point.  DENSITY: node rows -> erho (EAM);
 // otherwise rows of nonzero weight -> forces (LJ or EAM).
 template <bool EAM, bool DENSITY>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(512, 2)
 k_ip(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr,
      const double *__restrict__ frho, int nrho, double rdrho, float lj1, float lj2,
      double *__restrict__ out) {
@@ -397,9 +402,8 @@ k_ip(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr,
       jj = a.row_jj[r];
     }
     const double *N64 = a.spa_int + ((size_t) a.int_off[ty] + jj) * NPE;
-    const double *nxe = a.nodex + 24 * (size_t) e;
     float4 ih, il;
-    ip_ds(N64, nxe, ih, il);
+    ip_ds(a.spa_int_hl + ((size_t) a.int_off[ty] + jj) * NPE, a.node_hl + 24 * (size_t) e, ih, il);
     double fpi = 0.0;
     if (EAM && !DENSITY) {
       double rhoi = 0.0;
@@ -502,8 +506,8 @@ void eam_rho_atoms(const MixedAtoms &m, const float4 *rhor_val, const EamTables 
   AtomArgs a{m.x, m.xh, m.xl, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
              m.band_hi, m.cutsq};
   size_t smem = sizeof(float4) * (e.nr + 1);
-  int g = persistent_grid((const void *) k_eam_rho_atoms, 256, smem, m.nlocal);
-  k_eam_rho_atoms<<<g, 256, smem, s>>>(a, rhor_val, e.nr, (float) e.rdr, e.frho, e.nrho,
+  int g = persistent_grid((const void *) k_eam_rho_atoms, 512, smem, m.nlocal);
+  k_eam_rho_atoms<<<g, 512, smem, s>>>(a, rhor_val, e.nr, (float) e.rdr, e.frho, e.nrho,
                                        e.rdrho, rho, fp);
   check(cudaGetLastError(), "eam_rho_atoms_mixed");
 }
@@ -514,8 +518,8 @@ void eam_force_atoms(const MixedAtoms &m, const float4 *ftab, const EamTables &e
   AtomArgs a{m.x, m.xh, m.xl, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
              m.band_hi, m.cutsq};
   size_t smem = sizeof(float4) * 3 * (e.nr + 1);
-  int g = persistent_grid((const void *) k_eam_force_atoms, 256, smem, m.nlocal);
-  k_eam_force_atoms<<<g, 256, smem, s>>>(a, ftab, e.nr, (float) e.rdr, fp, f);
+  int g = persistent_grid((const void *) k_eam_force_atoms, 512, smem, m.nlocal);
+  k_eam_force_atoms<<<g, 512, smem, s>>>(a, ftab, e.nr, (float) e.rdr, fp, f);
   check(cudaGetLastError(), "eam_force_atoms_mixed");
 }
 
@@ -524,8 +528,8 @@ void lj_atoms(const MixedAtoms &m, const int *type, const float *lj1, const floa
   if (m.nlocal <= 0) return;
   AtomArgs a{m.x, m.xh, m.xl, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
              m.band_hi, m.cutsq};
-  int g = persistent_grid((const void *) k_lj_atoms, 256, 0, m.nlocal);
-  k_lj_atoms<<<g, 256, 0, s>>>(a, type, lj1, lj2, cutsq_t, cutsq64, f);
+  int g = persistent_grid((const void *) k_lj_atoms, 512, 0, m.nlocal);
+  k_lj_atoms<<<g, 512, 0, s>>>(a, type, lj1, lj2, cutsq_t, cutsq64, f);
   check(cudaGetLastError(), "lj_atoms_mixed");
 }
 
@@ -536,11 +540,17 @@ void sites_ds(const double *nodex, const int *etype, const int *site_base, const
   check(cudaGetLastError(), "sites_ds");
 }
 
-void sites_ds_needed(const double *nodex, const int *site_base, const int *need,
+void node_split(const double *nodex, int n, float2 *hl, cudaStream_t s) {
+  if (n <= 0) return;
+  k_node_split<<<nblk((long long) n * 24, 256), 256, 0, s>>>(nodex, n, hl);
+  check(cudaGetLastError(), "node_split");
+}
+
+void sites_ds_needed(const float2 *node_hl, const int *site_base, const int *need,
                      const int *need_elem, int nneed, const float2 *shape_hl, float4 *site_h,
                      float4 *site_l, cudaStream_t s) {
   if (nneed <= 0) return;
-  k_sites_ds_needed<<<nblk(nneed, 128), 128, 0, s>>>(nodex, site_base, need, need_elem, nneed,
+  k_sites_ds_needed<<<nblk(nneed, 128), 128, 0, s>>>(node_hl, site_base, need, need_elem, nneed,
                                                     shape_hl, site_h, site_l);
   check(cudaGetLastError(), "sites_ds_needed");
 }
@@ -566,19 +576,19 @@ void ip_pass(const MixedElems &m, int pass, const float4 *tab, const EamTables &
   ElemArgs a{m.nodex, m.erho, m.site_h, m.site_l, m.site_rho, m.etype, m.row_elem, m.row_jj,
              m.row_first, m.ipnum, m.ipent, m.nrows, m.rowstride, m.nlocal_e, m.spa_int,
              m.weight, m.int_off, m.node_list, m.rows, m.nforce, m.cutsq_f, m.band_lo,
-             m.band_hi, m.cutsq};
+             m.band_hi, m.cutsq, m.node_hl, m.spa_int_hl};
   if (pass == 0) {  // LJ forces
-    int g = persistent_grid((const void *) k_ip<false, false>, 256, 0, m.nforce);
-    k_ip<false, false><<<g, 256, 0, s>>>(a, tab, 0, 0.f, nullptr, 0, 0.0, lj1, lj2, out);
+    int g = persistent_grid((const void *) k_ip<false, false>, 512, 0, m.nforce);
+    k_ip<false, false><<<g, 512, 0, s>>>(a, tab, 0, 0.f, nullptr, 0, 0.0, lj1, lj2, out);
   } else if (pass == 1) {  // EAM nodal densities
     size_t smem = sizeof(float4) * (e.nr + 1);
-    int g = persistent_grid((const void *) k_ip<true, true>, 256, smem, (long long) m.nlocal_e * NPE);
-    k_ip<true, true><<<g, 256, smem, s>>>(a, tab, e.nr, (float) e.rdr, e.frho, e.nrho, e.rdrho,
+    int g = persistent_grid((const void *) k_ip<true, true>, 512, smem, (long long) m.nlocal_e * NPE);
+    k_ip<true, true><<<g, 512, smem, s>>>(a, tab, e.nr, (float) e.rdr, e.frho, e.nrho, e.rdrho,
                                          0.f, 0.f, out);
   } else {  // EAM forces
     size_t smem = sizeof(float4) * 3 * (e.nr + 1);
-    int g = persistent_grid((const void *) k_ip<true, false>, 256, smem, m.nforce);
-    k_ip<true, false><<<g, 256, smem, s>>>(a, tab, e.nr, (float) e.rdr, e.frho, e.nrho, e.rdrho,
+    int g = persistent_grid((const void *) k_ip<true, false>, 512, smem, m.nforce);
+    k_ip<true, false><<<g, 512, smem, s>>>(a, tab, e.nr, (float) e.rdr, e.frho, e.nrho, e.rdrho,
                                           0.f, 0.f, out);
   }
   check(cudaGetLastError(), "ip_pass_mixed");

@@ -135,6 +135,22 @@ __global__ void k_elem_diag(const double *__restrict__ nodex, const double *__re
   if (dist > 0.01) atomicAdd(bad, 1);
 }
 
+// [n][3] <-> double4 layout changes for host transfers, done on the device so
+// that a host-resident caller moves plain arrays with one DMA each way
+__global__ void k_pack3to4(const double *__restrict__ in, double4 *__restrict__ out, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = make_double4(in[3 * i], in[3 * i + 1], in[3 * i + 2], 0.0);
+}
+
+__global__ void k_unpack4to3(const double4 *__restrict__ in, double *__restrict__ out, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double4 p = in[i];
+  out[3 * i] = p.x;
+  out[3 * i + 1] = p.y;
+  out[3 * i + 2] = p.z;
+}
+
 // Dependent chains of FP64 fused multiply-adds: 8 independent chains per
 // thread keep the FP64 pipe busy; the result is written so nothing is elided.
 __global__ void k_fma_loop(double *out, int iters) {
@@ -203,6 +219,18 @@ void launch_elem_diag(const double *nodex, const double *ex, int n, double *diag
   if (n <= 0) return;
   k_elem_diag<<<nblk(n, 128), 128, 0, s>>>(nodex, ex, n, diag, centre_bad);
   check(cudaGetLastError(), "elem_diag");
+}
+
+void launch_pack3to4(const double *in, double4 *out, int n, cudaStream_t s) {
+  if (n <= 0) return;
+  k_pack3to4<<<nblk(n, 256), 256, 0, s>>>(in, out, n);
+  check(cudaGetLastError(), "pack3to4");
+}
+
+void launch_unpack4to3(const double4 *in, double *out, int n, cudaStream_t s) {
+  if (n <= 0) return;
+  k_unpack4to3<<<nblk(n, 256), 256, 0, s>>>(in, out, n);
+  check(cudaGetLastError(), "unpack4to3");
 }
 
 double fp64_fma_rate(cudaStream_t s) {
