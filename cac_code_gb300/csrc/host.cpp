@@ -1603,6 +1603,10 @@ void cacg_context::pair_compute_mixed(int pass) {
   }
   m.xh = d_xh.p;
   m.xl = d_xl.p;
+  d_snum.ensure(std::max(nlocal, 1), s);
+  d_slist.ensure((size_t) maxneigh * stride, s);
+  m.snum = d_snum.p;
+  m.slist = d_slist.p;
   if (pair_style == 1) {
     if (pass != 1) return;
     m.cutsq_f = 0.f;
@@ -1642,7 +1646,13 @@ void cacg_context::pair_ecompute_mixed() {
   mixed::node_split(d_nodex.p, nall, d_node_hl.p, s);
   mixed::sites_ds_needed(d_node_hl.p, d_site_base.p, d_need.p, d_need_elem.p, nneed, d_shape_hl.p,
                          d_site_h.p, d_site_l.p, s);
-  launches++;
+  // short lists of the rows this step (node rows and rows of nonzero weight)
+  const double csq = pair_style == 1 ? ljtab.cutsq[1 * (MAXT + 1) + 1] : cutforcesq;
+  d_sipnum.ensure(std::max(nrows, 1), s);
+  d_sipent.ensure((size_t) maxip * rowstride, s);
+  fp64_fma::filter_rows(d_nodex.p, d_etype.p, d_row_elem.p, d_row_jj.p, nrows, d_ipnum.p, d_ipent.p,
+                        rowstride, d_site_h.p, t, cut_pass(csq), 1, d_sipnum.p, d_sipent.p, s);
+  launches += 2;
   launches++;
   const float eps = 1.0e-4f;
   mixed::MixedElems m{};
@@ -1653,8 +1663,8 @@ void cacg_context::pair_ecompute_mixed() {
   m.row_elem = d_row_elem.p;
   m.row_jj = d_row_jj.p;
   m.row_first = d_row_first.p;
-  m.ipnum = d_ipnum.p;
-  m.ipent = d_ipent.p;
+  m.ipnum = d_sipnum.p;
+  m.ipent = d_sipent.p;
   m.nrows = nrows;
   m.rowstride = rowstride;
   m.nlocal_e = enlocal;

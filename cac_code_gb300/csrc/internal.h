@@ -236,6 +236,7 @@ struct MixedAtoms {
   int stride, nlocal;
   float cutsq_f, band_lo, band_hi;  // FP32 test; [band_lo, band_hi] re-tested in FP64
   double cutsq;
+  int *snum, *slist;  // EAM: short list written by the density pass, read by the force pass
 };
 struct MixedElems {
   const double *nodex, *erho;

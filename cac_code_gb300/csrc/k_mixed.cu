@@ -77,6 +77,7 @@ struct AtomArgs {
   int stride, nlocal;
   float cutsq_f, band_lo, band_hi;  // [band_lo, band_hi]: decide in FP64
   double cutsq;
+  int *snum, *slist;  // short list written by the density pass, read by the force pass
 };
 
 __global__ void __launch_bounds__(512, 2)
@@ -91,24 +92,28 @@ k_eam_rho_atoms(AtomArgs a, const float4 *__restrict__ rhor_val, int nr, float r
     const int n = a.num[i];
     double acc = 0.0;
     float part = 0.f;
+    int ns = 0, cnt = 0;
     for (int k = 0; k < n; k++) {
       int j = __ldg(a.list + (size_t) k * a.stride + i);
       float dx, dy, dz;
       pair_vec(hi, li, __ldg(a.xh + j), __ldg(a.xl + j), dx, dy, dz);
       float rsq = dx * dx + dy * dy + dz * dz;
+      if (rsq > a.band_hi) continue;
+      a.slist[(size_t) ns++ * a.stride + i] = j;
       bool in = rsq < a.cutsq_f;
-      if (rsq >= a.band_lo && rsq <= a.band_hi) in = inside64(a.x[i], a.x[j], a.cutsq);
+      if (rsq >= a.band_lo) in = inside64(a.x[i], a.x[j], a.cutsq);
       if (in) {
         float p;
         int m = findex(sqrtf(rsq), rdr, nr, p);
         float4 c = s_val[m];
         part += ((c.x * p + c.y) * p + c.z) * p + c.w;
-      }
-      if ((k & (CHUNK - 1)) == CHUNK - 1) {
-        acc += (double) part;
-        part = 0.f;
+        if ((++cnt & (CHUNK - 1)) == 0) {
+          acc += (double) part;
+          part = 0.f;
+        }
       }
     }
+    a.snum[i] = ns;
     acc += (double) part;
     rho[i] = acc;
     fp[i] = fprime64(acc, frho, nrho, rdrho);
@@ -125,11 +130,12 @@ k_eam_force_atoms(AtomArgs a, const float4 *__restrict__ ftab, int nr, float rdr
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.nlocal; i += gridDim.x * blockDim.x) {
     const float4 hi = a.xh[i], li = a.xl[i];
     const float fpi = (float) fp[i];
-    const int n = a.num[i];
+    const int n = a.snum[i];
     double fx = 0.0, fy = 0.0, fz = 0.0;
     float px = 0.f, py = 0.f, pz = 0.f;
+    int cnt = 0;
     for (int k = 0; k < n; k++) {
-      int j = __ldg(a.list + (size_t) k * a.stride + i);
+      int j = __ldg(a.slist + (size_t) k * a.stride + i);
       float dx, dy, dz;
       pair_vec(hi, li, __ldg(a.xh + j), __ldg(a.xl + j), dx, dy, dz);
       float rsq = dx * dx + dy * dy + dz * dz;
@@ -151,12 +157,12 @@ k_eam_force_atoms(AtomArgs a, const float4 *__restrict__ ftab, int nr, float rdr
         px += dx * fpair;
         py += dy * fpair;
         pz += dz * fpair;
-      }
-      if ((k & (CHUNK - 1)) == CHUNK - 1) {
-        fx += (double) px;
-        fy += (double) py;
-        fz += (double) pz;
-        px = py = pz = 0.f;
+        if ((++cnt & (CHUNK - 1)) == 0) {
+          fx += (double) px;
+          fy += (double) py;
+          fz += (double) pz;
+          px = py = pz = 0.f;
+        }
       }
     }
     f[3 * i] = fx + (double) px;
@@ -504,7 +510,7 @@ void eam_rho_atoms(const MixedAtoms &m, const float4 *rhor_val, const EamTables 
                    double *rho, double *fp, cudaStream_t s) {
   if (m.nlocal <= 0) return;
   AtomArgs a{m.x, m.xh, m.xl, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
-             m.band_hi, m.cutsq};
+             m.band_hi, m.cutsq, m.snum, m.slist};
   size_t smem = sizeof(float4) * (e.nr + 1);
   int g = persistent_grid((const void *) k_eam_rho_atoms, 512, smem, m.nlocal);
   k_eam_rho_atoms<<<g, 512, smem, s>>>(a, rhor_val, e.nr, (float) e.rdr, e.frho, e.nrho,
@@ -516,7 +522,7 @@ void eam_force_atoms(const MixedAtoms &m, const float4 *ftab, const EamTables &e
                      const double *fp, double *f, cudaStream_t s) {
   if (m.nlocal <= 0) return;
   AtomArgs a{m.x, m.xh, m.xl, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
-             m.band_hi, m.cutsq};
+             m.band_hi, m.cutsq, m.snum, m.slist};
   size_t smem = sizeof(float4) * 3 * (e.nr + 1);
   int g = persistent_grid((const void *) k_eam_force_atoms, 512, smem, m.nlocal);
   k_eam_force_atoms<<<g, 512, smem, s>>>(a, ftab, e.nr, (float) e.rdr, fp, f);
@@ -527,7 +533,7 @@ void lj_atoms(const MixedAtoms &m, const int *type, const float *lj1, const floa
               const float *cutsq_t, const double *cutsq64, double *f, cudaStream_t s) {
   if (m.nlocal <= 0) return;
   AtomArgs a{m.x, m.xh, m.xl, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
-             m.band_hi, m.cutsq};
+             m.band_hi, m.cutsq, m.snum, m.slist};
   int g = persistent_grid((const void *) k_lj_atoms, 512, 0, m.nlocal);
   k_lj_atoms<<<g, 512, 0, s>>>(a, type, lj1, lj2, cutsq_t, cutsq64, f);
   check(cudaGetLastError(), "lj_atoms_mixed");
