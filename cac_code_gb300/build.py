@@ -33,6 +33,7 @@ UNITS = [
     ("k_force_exact.cu", ["-fmad=false"]),
     ("k_force_fma.cu", ["-fmad=true"]),
     ("k_mixed.cu", ["-fmad=true"]),
+    ("k_thermo.cu", ["-fmad=true"]),
 ]
 
 

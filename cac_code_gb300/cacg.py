@@ -44,7 +44,7 @@ EXPORTED = [
     "cacg_fix_nve_final_integrate", "cacg_run", "cacg_get_counts", "cacg_get_atoms",
     "cacg_get_elements", "cacg_get_atom_list", "cacg_get_elem_list", "cacg_get_ip_list",
     "cacg_get_cut", "cacg_set_timing", "cacg_get_timing", "cacg_measure_fp64_peak",
-    "cacg_put_atoms", "cacg_put_nodes",
+    "cacg_put_atoms", "cacg_put_nodes", "cacg_compute_thermo",
 ]
 
 
@@ -261,6 +261,14 @@ class System:
 
     def cuts(self) -> np.ndarray:
         return np.array([self.cut(i) for i in range(6)])
+
+    def thermo(self) -> Dict[str, object]:
+        """Energies (pe/ke of atoms and elements), virial and kinetic tensors, volume."""
+        out = np.zeros(17)
+        self._ok(self._L.cacg_compute_thermo(self.h, _d(out), 17))
+        return {"pe_atoms": out[0], "pe_elements": out[1], "ke_atoms": out[2],
+                "ke_nodes": out[3], "virial": out[4:10].copy(), "kinetic_tensor": out[10:16].copy(),
+                "volume": out[16], "etotal": out[0] + out[1] + out[2] + out[3]}
 
     def set_timing(self, enable: bool = True):
         self._ok(self._L.cacg_set_timing(self.h, 1 if enable else 0))

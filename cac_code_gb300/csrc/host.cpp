@@ -200,7 +200,8 @@ struct cacg_context {
   DBuf<float4> d_xl, d_rhor_val4, d_ftab, d_site_l;
   DBuf<float2> d_shape_hl, d_node_hl, d_spa_int_hl;
   DBuf<float> d_u, d_shape_f, d_ljf, d_site_rho;
-  DBuf<double> d_cutsq64, d_stage;
+  DBuf<double> d_cutsq64, d_stage, d_part, d_lj5;
+  std::vector<double> h_lj5;
   DBuf<double> d_v, d_f, d_xhold, d_rho, d_fp, d_mass;
   DBuf<int> d_type, d_tag, d_root, d_send;
   DBuf<int> d_abin, d_bcount, d_bstart, d_bmem, d_stencil;
@@ -337,6 +338,7 @@ struct cacg_context {
   void pair_ecompute();
   void nve_initial();
   void nve_final();
+  void compute_thermo(double *out);
   int decide();
   void rebuild();
   void run(int n);
@@ -364,6 +366,8 @@ cacg_context::~cacg_context() {
   d_ljf.release();
   d_cutsq64.release();
   d_stage.release();
+  d_part.release();
+  d_lj5.release();
   DBuf<double> *bd[] = {&d_v, &d_f, &d_xhold, &d_rho, &d_fp, &d_mass, &d_ex, &d_nodex, &d_nodev,
                         &d_nodef, &d_nodexhold, &d_erho, &d_emass, &d_diag, &d_fip, &d_site_fp,
                         &d_spa_int, &d_weight, &d_spa_inter, &d_spa_csub, &d_spa_isub, &d_frho,
@@ -1188,6 +1192,25 @@ void cacg_context::init() {
       }
     d_ljtab.ensure(1, stream);
     check(cudaMemcpyAsync(d_ljtab.p, &ljtab, sizeof(ljtab), cudaMemcpyHostToDevice, stream), "ljtab");
+    // energy coefficients lj3 = 4 eps sigma^12, lj4 = 4 eps sigma^6 (pair_lj_cut.cpp:151-152)
+    const int T = (MAXT + 1) * (MAXT + 1);
+    std::vector<double> lj5(5 * T, 0.0);
+    for (int i = 1; i <= nt; i++)
+      for (int j = 1; j <= nt; j++) {
+        double e = eps[std::min(i, j)][std::max(i, j)], sg = sig[std::min(i, j)][std::max(i, j)];
+        if (!setflag[std::min(i, j)][std::max(i, j)]) {
+          e = std::sqrt(eps[i][i] * eps[j][j]);
+          sg = std::sqrt(sig[i][i] * sig[j][j]);
+        }
+        int k = i * (MAXT + 1) + j;
+        lj5[k] = ljtab.lj1[k];
+        lj5[T + k] = ljtab.lj2[k];
+        lj5[2 * T + k] = 4.0 * e * std::pow(sg, 12.0);
+        lj5[3 * T + k] = 4.0 * e * std::pow(sg, 6.0);
+        lj5[4 * T + k] = ljtab.cutsq[k];
+      }
+    upload(d_lj5, lj5, stream);
+    h_lj5 = lj5;
   } else {
     upload(d_frho, frho_sp, stream);
     upload(d_rhor, rhor_sp, stream);
@@ -1770,6 +1793,88 @@ void cacg_context::pair_ecompute() {
   launches++;
 }
 
+// ------------------------------------------------------------------ thermo
+
+void cacg_context::compute_thermo(double *out) {
+  if (!setup_done || (nlocal && !list_built) || (enlocal && !elists_built))
+    fail(CACG_ESTATE, "thermo before the neighbor lists are built");
+  cudaStream_t s = stream;
+  for (int k = 0; k < 17; k++) out[k] = 0.0;
+  auto reduce = [&](int nblocks, double *acc) {
+    std::vector<double> h((size_t) nblocks * 7);
+    check(cudaMemcpyAsync(h.data(), d_part.p, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, s), "part");
+    sync();
+    for (int b = 0; b < nblocks; b++)
+      for (int k = 0; k < 7; k++) acc[k] += h[(size_t) b * 7 + k];
+  };
+  const double mvv2e = metal ? 1.0364269e-4 : 1.0;  // force->mvv2e (update.cpp:90,110)
+  double q[7];
+  if (nlocal) {
+    int nb = thermo::partial_blocks(nlocal);
+    d_part.ensure((size_t) nb * 7, s);
+    int nall = nlocal + nghost;
+    if (pair_style == 1) {
+      thermo::atoms_lj(d_x.p, d_type.p, d_num.p, d_list.p, stride, nlocal, d_lj5.p, d_part.p, s);
+    } else {
+      EamTables e = eamtab();
+      d_rho.ensure(nall, s);
+      d_fp.ensure(nall, s);
+      fp64_exact::eam_rho_atoms(d_x.p, d_num.p, d_list.p, stride, nlocal, e, d_rho.p, d_fp.p, s);
+      launch_copy_root(d_fp.p, 1, d_root.p, nlocal, nghost, s);
+      thermo::atoms_eam(d_x.p, d_num.p, d_list.p, stride, nlocal, e, d_rho.p, d_fp.p, d_part.p, s);
+    }
+    for (double &v : q) v = 0.0;
+    reduce(nb, q);
+    out[0] = q[0];
+    for (int k = 0; k < 6; k++) out[4 + k] += q[1 + k];
+    nb = thermo::partial_blocks(nlocal);
+    thermo::kinetic(d_v.p, d_type.p, d_mass.p, nlocal, 1, 1.0, d_part.p, s);
+    for (double &v : q) v = 0.0;
+    reduce(nb, q);
+    out[2] = q[0] * mvv2e;
+    for (int k = 0; k < 6; k++) out[10 + k] += q[1 + k] * mvv2e;
+  }
+  if (enlocal) {
+    int nall = enlocal + enghost;
+    ElemTables t = etab();
+    EamTables e = eamtab();
+    d_site_x.ensure(std::max(nsites, 1), s);
+    d_site_h.ensure(std::max(nsites, 1), s);
+    fp64_fma::sites_needed(d_nodex.p, d_etype.p, d_site_base.p, d_need.p, d_need_elem.p, nneed, t,
+                           d_site_x.p, d_site_h.p, s);
+    if (pair_style == 2) {
+      d_erho.ensure((size_t) NPE * nall, s);
+      d_site_fp.ensure(std::max(nsites, 1), s);
+      fp64_exact::eam_erho(d_nodex.p, d_etype.p, d_row_first.p, enlocal, d_ipnum.p, d_ipent.p, rowstride,
+                           d_site_x.p, t, e, d_erho.p, s);
+      launch_copy_root(d_erho.p, NPE, d_eroot.p, enlocal, enghost, s);
+      fp64_fma::site_fp_needed(d_erho.p, d_etype.p, d_site_base.p, d_need.p, d_need_elem.p, nneed, t,
+                               e, d_site_fp.p, s);
+    }
+    int nb = thermo::partial_blocks(nforce);
+    d_part.ensure((size_t) std::max(nb, thermo::partial_blocks((long long) enlocal * NPE)) * 7, s);
+    // elements carry one species: the 1-1 pair coefficients (pair_lj_cut.cpp:295-330)
+    const int T = (MAXT + 1) * (MAXT + 1), a = 1 * (MAXT + 1) + 1;
+    double l5[5] = {0, 0, 0, 0, 0};
+    if (pair_style == 1)
+      for (int k = 0; k < 5; k++) l5[k] = h_lj5[(size_t) k * T + a];
+    thermo::ip(d_nodex.p, d_erho.p, d_etype.p, d_row_elem.p, d_row_jj.p, d_force_rows.p, nforce,
+               d_ipnum.p, d_ipent.p, rowstride, d_site_x.p, d_site_fp.p, t, e, pair_style == 2,
+               l5[0], l5[1], l5[2], l5[3], l5[4], d_part.p, s);
+    for (double &v : q) v = 0.0;
+    reduce(nb, q);
+    out[1] = q[0];
+    for (int k = 0; k < 6; k++) out[4 + k] += q[1 + k];
+    nb = thermo::partial_blocks((long long) enlocal * NPE);
+    thermo::kinetic(d_nodev.p, d_etype.p, d_emass.p, enlocal * NPE, NPE, 1.0 / NPE, d_part.p, s);
+    for (double &v : q) v = 0.0;
+    reduce(nb, q);
+    out[3] = q[0] * mvv2e;
+    for (int k = 0; k < 6; k++) out[10 + k] += q[1 + k] * mvv2e;
+  }
+  out[16] = prd[0] * prd[1] * prd[2];
+}
+
 // ------------------------------------------------------------------ integrate
 
 void cacg_context::nve_initial() {
@@ -2244,6 +2349,15 @@ int cacg_get_cut(cacg_handle h, int what, double *value) {
 int cacg_set_timing(cacg_handle h, int enable) {
   API_BEGIN
   h->timing = enable != 0;
+  API_END
+}
+
+int cacg_compute_thermo(cacg_handle h, double *out, int n) {
+  API_BEGIN
+  if (!out || n < 1) fail(CACG_EINVAL, "bad output array");
+  double v[17];
+  h->compute_thermo(v);
+  for (int i = 0; i < n && i < 17; i++) out[i] = v[i];
   API_END
 }
 

@@ -277,6 +277,22 @@ void ip_pass(const MixedElems &m, int pass, const float4 *tab, const EamTables &
              float lj2, double *out, cudaStream_t s);
 }  // namespace mixed
 
+// ---- energy, virial, kinetic energy (k_thermo.cu); 7 partial sums per block ----
+namespace thermo {
+int partial_blocks(long long n);
+void atoms_lj(const double4 *x, const int *type, const int *num, const int *list, int stride,
+              int n, const double *lj, double *part, cudaStream_t s);
+void atoms_eam(const double4 *x, const int *num, const int *list, int stride, int n,
+               EamTables e, const double *rho, const double *fp, double *part, cudaStream_t s);
+void ip(const double *nodex, const double *erho, const int *etype, const int *row_elem,
+        const int *row_jj, const int *rows, int nforce, const int *ipnum, const int *ipent,
+        int rowstride, const double4 *site_x, const double *site_fp, ElemTables t, EamTables e,
+        int eam, double lj1, double lj2, double lj3, double lj4, double ljcutsq, double *part,
+        cudaStream_t s);
+void kinetic(const double *v, const int *type, const double *mass, int n, int per_item,
+             double scale, double *part, cudaStream_t s);
+}  // namespace thermo
+
 // ---- integration and reductions (k_nve.cu) ----
 void launch_nve_atoms_initial(double4 *x, double *v, const double *f, const int *type,
                               const double *mass, int n, double dtv, double dtf,

@@ -301,7 +301,12 @@ def write_data(model: Model, path: str, with_velocities: bool = False) -> None:
 
 @dataclasses.dataclass
 class AnalyticEAM:
-    """f(r)=exp(-beta(r/re-1)); phi = Morse(D, alpha, r0); F(rho) = -A*sqrt(rho)."""
+    """f(r)=exp(-beta(r/re-1)); phi = Morse(D, alpha, r0); F(rho) = -A*sqrt(rho).
+
+    With ``taper`` > 0, f and phi are multiplied by psi(x) = x^4 / (1 + x^4),
+    x = (r - cut) / taper (zero beyond the cutoff), so both vanish smoothly
+    there and the total energy is conserved in NVE.
+    """
     re: float = 2.556
     beta: float = 6.0
     D: float = 0.3429
@@ -310,27 +315,38 @@ class AnalyticEAM:
     A: float = 1.2
     cut: float = 5.5
     mass: float = 63.546
+    taper: float = 0.0
+
+    def _psi(self, r):
+        if self.taper <= 0.0:
+            return 1.0
+        x = (np.asarray(r, dtype=np.float64) - self.cut) / self.taper
+        x4 = x ** 4
+        return np.where(x < 0.0, x4 / (1.0 + x4), 0.0)
 
     def density(self, r):
-        return np.exp(-self.beta * (np.asarray(r) / self.re - 1.0))
+        return np.exp(-self.beta * (np.asarray(r) / self.re - 1.0)) * self._psi(r)
 
     def pair(self, r):
         e = np.exp(-self.alpha * (np.asarray(r) - self.r0))
-        return self.D * (e * e - 2.0 * e)
+        return self.D * (e * e - 2.0 * e) * self._psi(r)
 
     def embed(self, rho):
         return -self.A * np.sqrt(np.maximum(np.asarray(rho), 0.0))
 
 
 def write_eam_funcfl(pot: AnalyticEAM, path: str, nrho: int = 2000, drho: Optional[float] = None,
-                     nr: int = 2000, rho_max: Optional[float] = None) -> None:
+                     nr: int = 2000, rho_max: Optional[float] = None,
+                     r_max: Optional[float] = None) -> None:
     """Tabulate ``pot`` in the file variant PairEAM::read_file reads.
 
-    Grid r = (m-1)*dr, m = 1..nr with (nr-1)*dr = cut (file2array then regrids to
-    nr-1 points, pair_eam.cpp:338-339).  The third table holds r*phi(r) directly,
-    as the reference uses it without the Z-product conversion (pair_eam.cpp:487).
+    Grid r = (m-1)*dr, m = 1..nr with (nr-1)*dr = r_max (default: the cutoff;
+    file2array then regrids to nr-1 points, pair_eam.cpp:338-339, so the last
+    interval below the cutoff is clamped unless r_max extends past it).  The
+    third table holds r*phi(r) directly, as the reference uses it without the
+    Z-product conversion (pair_eam.cpp:487).
     """
-    dr = pot.cut / (nr - 1)
+    dr = (pot.cut if r_max is None else r_max) / (nr - 1)
     r = np.arange(nr) * dr
     if rho_max is None:
         rho_max = 40.0

@@ -109,6 +109,16 @@ int cacg_get_ip_list(cacg_handle h, int *numneigh, int *jelem, int *jsite);
 /* 0 cutneighmax 1 cut_all 2 cut_ele 3 cut_subele 4 max_size 5 nsubele */
 int cacg_get_cut(cacg_handle h, int what, double *value);
 
+/* ---- thermo (the reference's compute pe/temp/pressure are stubs,
+   compute_pe.cpp:16-49; these are the standard pair-style energies) ----
+   FP64 at the current positions: out[0] potential energy of atoms, [1] of
+   elements (integration-point weights), [2] kinetic energy of atoms, [3] of
+   nodes (nodal mass M_e/8), [4..9] pair virial sum r_a f_b (xx yy zz xy xz yz,
+   atoms + weighted integration points), [10..15] kinetic tensor sum m v_a v_b,
+   [16] box volume.  Energies in the unit style's energy unit.  Returns the
+   number filled (n <= 17). */
+int cacg_compute_thermo(cacg_handle h, double *out, int n);
+
 /* ---- measurement ---- */
 /* Phase timing of the last cacg_run from CUDA events on the handle's stream
    (recorded only after cacg_set_timing(h, 1)): ms[0] total, [1] integrate +

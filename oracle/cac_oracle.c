@@ -120,6 +120,7 @@ struct orc_sys {
   /* pair */
   int pair_style;    /* 0 none, 1 lj/cut, 2 eam */
   double lj1[MAXTYPES + 1][MAXTYPES + 1], lj2[MAXTYPES + 1][MAXTYPES + 1];
+  double lj3[MAXTYPES + 1][MAXTYPES + 1], lj4[MAXTYPES + 1][MAXTYPES + 1];
   double cutsq[MAXTYPES + 1][MAXTYPES + 1];
   /* eam */
   int nr, nrho;
@@ -345,6 +346,8 @@ int orc_set_lj(orc_sys *s, int ntypes, const double *eps, const double *sigma,
       double c = cut[(i - 1) * ntypes + (j - 1)];
       s->lj1[i][j] = 48.0 * e * pow(sg, 12.0);
       s->lj2[i][j] = 24.0 * e * pow(sg, 6.0);
+      s->lj3[i][j] = 4.0 * e * pow(sg, 12.0);
+      s->lj4[i][j] = 4.0 * e * pow(sg, 6.0);
       s->cutsq[i][j] = c * c;
     }
   return 0;
@@ -1394,6 +1397,197 @@ int orc_elem_forces(orc_sys *s) {
   if (s->pair_style == 1) lj_ecompute(s);
   else if (s->pair_style == 2) eam_ecompute(s);
   else return fail(s, "no pair style");
+  return 0;
+}
+
+/* ---- energy and virial (standard lj/cut and eam definitions; the reference's
+   compute pe/temp/pressure are stubs, compute_pe.cpp:16-49) ---- */
+
+static double spl_value(const double *c, double p) { return ((c[3] * p + c[4]) * p + c[5]) * p + c[6]; }
+static double spl_deriv(const double *c, double p) { return (c[0] * p + c[1]) * p + c[2]; }
+
+static const double *r_coef(orc_sys *s, const double *tab, double r, double *p) {
+  double q = r * s->rdr + 1.0;
+  int m = (int) q;
+  m = m < s->nr - 1 ? m : s->nr - 1;
+  q -= m;
+  *p = q < 1.0 ? q : 1.0;
+  return tab + 7 * m;
+}
+
+static const double *rho_coef(orc_sys *s, double rho, double *p) {
+  double q = rho * s->rdrho + 1.0;
+  int m = (int) q;
+  m = m < s->nrho - 1 ? m : s->nrho - 1;
+  m = 1 > m ? 1 : m;
+  q -= m;
+  *p = q < 1.0 ? q : 1.0;
+  return s->frho_spline + 7 * m;
+}
+
+static void add_vir(double *v, double w, double dx, double dy, double dz, double fpair) {
+  v[0] += w * dx * dx * fpair;
+  v[1] += w * dy * dy * fpair;
+  v[2] += w * dz * dz * fpair;
+  v[3] += w * dx * dy * fpair;
+  v[4] += w * dx * dz * fpair;
+  v[5] += w * dy * dz * fpair;
+}
+
+/* position of integration site nj of element j */
+static void site_pos(orc_sys *s, int j, int nj, double *out) {
+  const double *M = s->spa_inter[s->etype[j]] + NPE * nj;
+  const double *nxj = s->nodex + 24 * j;
+  out[0] = out[1] = out[2] = 0.0;
+  for (int kk = 0; kk < NPE; kk++)
+    for (int d = 0; d < 3; d++) out[d] += M[kk] * nxj[3 * kk + d];
+}
+
+/* out: pe atoms, pe elements, ke atoms, ke nodes, virial[6], kinetic tensor[6],
+   volume.  Pair energies are halved (full lists); integration points carry
+   their weight.  EAM densities are recomputed at the current positions. */
+int orc_thermo(orc_sys *s, double *out) {
+  if (!s->have_list && s->nlocal) return fail(s, "atom neighbor list not built");
+  if (!s->have_elists && s->enlocal) return fail(s, "element lists not built");
+  for (int k = 0; k < 17; k++) out[k] = 0.0;
+  double *vir = out + 4, p;
+  if (s->pair_style == 2 && s->nlocal) {
+    int nall = s->nlocal + s->nghost;
+    for (int i = 0; i < nall; i++) s->rho[i] = 0.0;
+    for (int i = 0; i < s->nlocal; i++) {
+      const int *jl = s->neigh.v + s->firstneigh[i];
+      for (int jj = 0; jj < s->numneigh[i]; jj++) {
+        int j = jl[jj];
+        double dx = s->x[3 * i] - s->x[3 * j], dy = s->x[3 * i + 1] - s->x[3 * j + 1],
+               dz = s->x[3 * i + 2] - s->x[3 * j + 2];
+        double rsq = dx * dx + dy * dy + dz * dz;
+        if (rsq < s->cutforcesq) {
+          const double *c = r_coef(s, s->rhor_spline, sqrt(rsq), &p);
+          s->rho[i] += spl_value(c, p);
+        }
+      }
+      const double *c = rho_coef(s, s->rho[i], &p);
+      s->fp[i] = spl_deriv(c, p);
+    }
+    forward_fp(s);
+  }
+  for (int i = 0; i < s->nlocal; i++) {
+    int it = s->type[i];
+    double e = 0.0;
+    if (s->pair_style == 2) {
+      const double *c = rho_coef(s, s->rho[i], &p);
+      e = spl_value(c, p);
+    }
+    const int *jl = s->neigh.v + s->firstneigh[i];
+    for (int jj = 0; jj < s->numneigh[i]; jj++) {
+      int j = jl[jj], jt = s->type[j];
+      double dx = s->x[3 * i] - s->x[3 * j], dy = s->x[3 * i + 1] - s->x[3 * j + 1],
+             dz = s->x[3 * i + 2] - s->x[3 * j + 2];
+      double rsq = dx * dx + dy * dy + dz * dz;
+      if (s->pair_style == 1 && rsq < s->cutsq[it][jt]) {
+        double r2inv = 1.0 / rsq, r6inv = r2inv * r2inv * r2inv;
+        e += 0.5 * r6inv * (s->lj3[it][jt] * r6inv - s->lj4[it][jt]);
+        add_vir(vir, 0.5, dx, dy, dz, r6inv * (s->lj1[it][jt] * r6inv - s->lj2[it][jt]) * r2inv);
+      } else if (s->pair_style == 2 && rsq < s->cutforcesq) {
+        double r = sqrt(rsq);
+        const double *cr = r_coef(s, s->rhor_spline, r, &p);
+        const double *z = r_coef(s, s->z2r_spline, r, &p);
+        double phi = spl_value(z, p) / r;
+        double phip = spl_deriv(z, p) / r - phi / r;
+        e += 0.5 * phi;
+        add_vir(vir, 0.5, dx, dy, dz, -((s->fp[i] + s->fp[j]) * spl_deriv(cr, p) + phip) / r);
+      }
+    }
+    out[0] += e;
+  }
+  if (s->enlocal && s->pair_style == 2) {
+    int nall = s->enlocal + s->enghost;
+    for (int i = 0; i < nall * NPE; i++) s->erho[i] = 0.0;
+    for (int i = 0; i < s->enlocal; i++) {
+      int t = s->etype[i];
+      for (int jj = 0; jj < NPE; jj++) {
+        int nt = s->elist[i] + s->node_list[t][jj];
+        const double *xi = s->nodex + 24 * i + 3 * jj;
+        int base = s->ip_first.v[nt];
+        for (int ll = 0; ll < s->ip_num.v[nt]; ll++) {
+          double xj[3];
+          site_pos(s, s->ip_j.v[base + ll], s->ip_nj.v[base + ll], xj);
+          double dx = xi[0] - xj[0], dy = xi[1] - xj[1], dz = xi[2] - xj[2];
+          double rsq = dx * dx + dy * dy + dz * dz;
+          if (rsq < s->cutforcesq) {
+            const double *c = r_coef(s, s->rhor_spline, sqrt(rsq), &p);
+            s->erho[NPE * i + jj] += spl_value(c, p);
+          }
+        }
+      }
+    }
+    forward_erho(s);
+  }
+  for (int i = 0; i < s->enlocal; i++) {
+    int t = s->etype[i];
+    int np = s->elist[i];
+    for (int jj = 0; jj < s->numint[t]; jj++, np++) {
+      double w = s->weight[t][jj];
+      if (w == 0.0) continue;
+      const double *N = s->spa_int[t] + NPE * jj;
+      double xi[3] = {0, 0, 0}, rhoi = 0.0;
+      for (int kk = 0; kk < NPE; kk++) {
+        for (int d = 0; d < 3; d++) xi[d] += N[kk] * s->nodex[24 * i + 3 * kk + d];
+        if (s->pair_style == 2) rhoi += N[kk] * s->erho[NPE * i + kk];
+      }
+      double e = 0.0, fpi = 0.0;
+      if (s->pair_style == 2) {
+        const double *c = rho_coef(s, rhoi, &p);
+        fpi = spl_deriv(c, p);
+        e = spl_value(c, p);
+      }
+      int base = s->ip_first.v[np];
+      for (int ll = 0; ll < s->ip_num.v[np]; ll++) {
+        int j = s->ip_j.v[base + ll], nj = s->ip_nj.v[base + ll];
+        double xj[3];
+        site_pos(s, j, nj, xj);
+        double dx = xi[0] - xj[0], dy = xi[1] - xj[1], dz = xi[2] - xj[2];
+        double rsq = dx * dx + dy * dy + dz * dz;
+        if (s->pair_style == 1 && rsq < s->cutsq[1][1]) {
+          double r2inv = 1.0 / rsq, r6inv = r2inv * r2inv * r2inv;
+          e += 0.5 * r6inv * (s->lj3[1][1] * r6inv - s->lj4[1][1]);
+          add_vir(vir, 0.5 * w, dx, dy, dz, r6inv * (s->lj1[1][1] * r6inv - s->lj2[1][1]) * r2inv);
+        } else if (s->pair_style == 2 && rsq < s->cutforcesq) {
+          const double *M = s->spa_inter[s->etype[j]] + NPE * nj;
+          double rhoj = 0.0;
+          for (int kk = 0; kk < NPE; kk++) rhoj += M[kk] * s->erho[NPE * j + kk];
+          const double *cf = rho_coef(s, rhoj, &p);
+          double fpj = spl_deriv(cf, p);
+          double r = sqrt(rsq);
+          const double *cr = r_coef(s, s->rhor_spline, r, &p);
+          const double *z = r_coef(s, s->z2r_spline, r, &p);
+          double phi = spl_value(z, p) / r;
+          double phip = spl_deriv(z, p) / r - phi / r;
+          e += 0.5 * phi;
+          add_vir(vir, 0.5 * w, dx, dy, dz, -((fpi + fpj) * spl_deriv(cr, p) + phip) / r);
+        }
+      }
+      out[1] += w * e;
+    }
+  }
+  double mvv2e = s->ftm2v == 1.0 ? 1.0 : 1.0364269e-4; /* update.cpp:90,110 */
+  for (int i = 0; i < s->nlocal; i++) {
+    double m = s->amass[s->type[i]];
+    const double *v = s->v + 3 * i;
+    out[2] += 0.5 * m * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) * mvv2e;
+    double t6[6] = {v[0] * v[0], v[1] * v[1], v[2] * v[2], v[0] * v[1], v[0] * v[2], v[1] * v[2]};
+    for (int k = 0; k < 6; k++) out[10 + k] += m * t6[k] * mvv2e;
+  }
+  for (int i = 0; i < s->enlocal; i++) {
+    double m = s->emass[s->etype[i]] / NPE;
+    for (int q = 0; q < NPE; q++) {
+      const double *v = s->nodev + 24 * i + 3 * q;
+      out[3] += 0.5 * m * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) * mvv2e;
+      double t6[6] = {v[0] * v[0], v[1] * v[1], v[2] * v[2], v[0] * v[1], v[0] * v[2], v[1] * v[2]};
+      for (int k = 0; k < 6; k++) out[10 + k] += m * t6[k] * mvv2e;
+    }
+  }
+  out[16] = (s->boxhi[0] - s->boxlo[0]) * (s->boxhi[1] - s->boxlo[1]) * (s->boxhi[2] - s->boxlo[2]);
   return 0;
 }
 

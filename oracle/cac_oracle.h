@@ -47,6 +47,8 @@ int orc_atom_list(orc_sys *s);   /* Neighbor::build */
 int orc_elem_lists(orc_sys *s);  /* setup_cut + ebuild + nbuild */
 int orc_atom_forces(orc_sys *s); /* Pair::compute */
 int orc_elem_forces(orc_sys *s); /* Pair::ecompute */
+/* energies, virial and kinetic tensors at the current state (17 values) */
+int orc_thermo(orc_sys *s, double *out);
 int orc_run(orc_sys *s, int nsteps); /* Verlet::run loop with atom forces */
 
 /* sizes: 0 nlocal, 1 nghost, 2 atom list entries, 3 elem nlocal, 4 elem nghost,

@@ -170,6 +170,14 @@ class Oracle:
         self._ok(self._L.orc_elem_forces(self.h))
         return self.elements()["nodef"]
 
+    def thermo(self) -> Dict[str, object]:
+        """Energies, virial and kinetic tensors at the current state (orc_thermo)."""
+        out = np.zeros(17)
+        self._ok(self._L.orc_thermo(self.h, _d(out)))
+        return {"pe_atoms": out[0], "pe_elements": out[1], "ke_atoms": out[2],
+                "ke_nodes": out[3], "virial": out[4:10].copy(), "kinetic_tensor": out[10:16].copy(),
+                "volume": out[16], "etotal": out[0] + out[1] + out[2] + out[3]}
+
     def run(self, n: int):
         self._ok(self._L.orc_run(self.h, n))
 
