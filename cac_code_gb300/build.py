@@ -34,6 +34,7 @@ UNITS = [
     ("k_force_fma.cu", ["-fmad=true"]),
     ("k_mixed.cu", ["-fmad=true"]),
     ("k_thermo.cu", ["-fmad=true"]),
+    ("k_noalloc.cu", ["-fmad=true"]),
 ]
 
 

@@ -29,7 +29,7 @@ from . import build as _build
 
 FP64_EXACT, FP64, MIXED = 0, 1, 2
 _STATUS = {0: "ok", -1: "invalid", -2: "state", -3: "cuda", -4: "overflow", -5: "io",
-           -6: "nomem", -7: "timeout"}
+           -6: "nomem", -7: "timeout", -8: "scratch"}
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int)
@@ -44,7 +44,7 @@ EXPORTED = [
     "cacg_fix_nve_final_integrate", "cacg_run", "cacg_get_counts", "cacg_get_atoms",
     "cacg_get_elements", "cacg_get_atom_list", "cacg_get_elem_list", "cacg_get_ip_list",
     "cacg_get_cut", "cacg_set_timing", "cacg_get_timing", "cacg_measure_fp64_peak",
-    "cacg_put_atoms", "cacg_put_nodes", "cacg_compute_thermo",
+    "cacg_put_atoms", "cacg_put_nodes", "cacg_compute_thermo", "cacg_kinetic_noalloc",
 ]
 
 
@@ -83,6 +83,9 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
     lib.cacg_set_timing.argtypes = [ctypes.c_void_p, ctypes.c_int]
     lib.cacg_pair_compute.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
     lib.cacg_get_cut.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp]
+    lib.cacg_kinetic_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                         ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                         ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]
     _LIB = lib
     return lib
 

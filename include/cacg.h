@@ -31,6 +31,7 @@ typedef struct cacg_context *cacg_handle;
 #define CACG_EIO (-5)        /* file could not be read */
 #define CACG_ENOMEM (-6)     /* device allocation failed */
 #define CACG_ETIMEOUT (-7)   /* a bounded device wait ran out */
+#define CACG_ESCRATCH (-8)   /* request larger than a fixed scratch array */
 
 /* precision modes (cacg_set_precision) */
 #define CACG_FP64_EXACT 0    /* reference operation order, no contraction: bit-identical */
@@ -118,6 +119,26 @@ int cacg_get_cut(cacg_handle h, int what, double *value);
    [16] box volume.  Energies in the unit style's energy unit.  Returns the
    number filled (n <= 17). */
 int cacg_compute_thermo(cacg_handle h, double *out, int n);
+
+/* ---- kinetic sums without device allocation (no counterpart in the
+   reference) ----
+   For callers that may not allocate device memory when they call: a driver
+   reporting thermo from its per-step output hook, where cudaMalloc/cudaFree
+   would synchronise the device, or one whose device memory is reserved by
+   another framework's allocator.  v[n][3], type[n / per_item] (1-based, or
+   element types for nodes) and mass[type] are the caller's device arrays;
+   out[7] (device) receives mvv2e * (sum 1/2 m v^2, sum m vx vx, m vy vy,
+   m vz vz, m vx vy, m vx vz, m vy vz) with m = mass[type[i / per_item]] *
+   scale, launched on `stream` (a cudaStream_t; NULL = default stream).
+   Partial sums live in a fixed 448 KiB device array: n above
+   CACG_NOALLOC_MAX_ITEMS returns CACG_ESCRATCH.  Nothing has to be zeroed
+   first.  Calls share that array per device, so calls that can overlap
+   race: serialise them.  The first call on a device resolves the array's
+   address (make it, n = 0 is enough, before any stream capture).  Returns
+   CACG_OK once both kernels are queued. */
+#define CACG_NOALLOC_MAX_ITEMS (8192 * 256)
+int cacg_kinetic_noalloc(const double *v, const int *type, const double *mass, int n,
+                         int per_item, double scale, double mvv2e, double *out, void *stream);
 
 /* ---- measurement ---- */
 /* Phase timing of the last cacg_run from CUDA events on the handle's stream
