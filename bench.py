@@ -1,6 +1,9 @@
 #!/usr/bin/env python
 """Benchmark: site-steps/s of the CAC step on the C2 workload (EAM Cu, 1,000,000
-atoms + 20,000 elements, FP64) on one GB300 per rank.
+atoms + 20,000 elements) on one GB300 per rank.  The headline mode is mixed
+precision (FP32 pair terms, FP64 accumulation and integration); the plain FP64
+and bit-exact FP64 modes are timed beside it on the same system, with their
+force difference.
 
 A step is one full Verlet step of the reference's loop (verlet.cpp:163-218):
 NVE half-kick and drift of atoms and nodes, rebuild decision (every 10 steps,
@@ -41,7 +44,9 @@ def parse():
     p.add_argument("--steps", type=int, default=50)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--mode", default="fp64", choices=["fp64", "exact", "mixed"])
+    p.add_argument("--mode", default="mixed", choices=["fp64", "exact", "mixed"])
+    p.add_argument("--drift-steps", type=int, default=1000,
+                   help="NVE steps of the energy-drift run after the timed region (0: skip)")
     p.add_argument("--size", default="full", choices=["full", "medium", "small"],
                    help="full C2; medium = 360,000-atom slab (profiling, > L2); small = 8,000 atoms")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -169,10 +174,16 @@ def cpu_leg(cores, steps, warm, eam):
 
 # ----------------------------------------------------------------------------- arms
 
-def algorithmic_bytes_force_atoms(natoms, mean_neigh):
-    """EAM force pass over the atom list (bytes per launch): x_i 24 + list 4n +
-    fp_i 8 + f_i 24."""
-    return natoms * (24 + 4 * mean_neigh + 8 + 24)
+def algorithmic_bytes_force_atoms(natoms, mean_short):
+    """FP64 EAM force pass over the atom short list (bytes per launch): x_i 24 +
+    count 4 + list 4n + fp_i 8 + f_i 24."""
+    return natoms * (24 + 4 + 4 * mean_short + 8 + 24)
+
+
+def algorithmic_bytes_rho_mixed(natoms, mean_neigh, mean_short):
+    """Mixed EAM density pass (bytes per launch): double-single x_i 32 + count 4 +
+    full list 4n + short-list count 4 and entries 4n_s written + rho 8 + F' 8."""
+    return natoms * (32 + 4 + 4 * mean_neigh + 4 + 4 * mean_short + 8 + 8)
 
 
 def run_ours(a, ws, rank, local):
@@ -230,12 +241,23 @@ def run_ours(a, ws, rank, local):
     ms_max = allmax(ws, dev_ms)
     value = ws * sites * a.steps / (ms_max * 1e-3)
 
-    # dominant kernel: EAM force pass over the atom list (phase 3), one launch per step
+    # dominant kernel, one launch per step: the FP64 modes' EAM force pass
+    # over the atom list (phase 3); the mixed mode's EAM density pass (phase 2),
+    # which also writes the force pass's short list
     mean_neigh = c0["atom_entries"] / max(c0["nlocal"], 1)
+    mean_short = c1["short_entries"] / max(c1["nlocal"], 1)
     phase = {"integrate+comm": tm[1], "atom_rho": tm[2], "atom_force": tm[3],
              "element": tm[4], "final": tm[5]}
-    k_ms = tm[3] / a.steps
-    abytes = algorithmic_bytes_force_atoms(c0["nlocal"], mean_neigh)
+    if a.mode == "mixed":
+        kname = "mixed k_eam_rho_atoms (EAM density pass over the atom list, emits the short list)"
+        k_ms = tm[2] / a.steps
+        abytes = algorithmic_bytes_rho_mixed(c0["nlocal"], mean_neigh, mean_short)
+        tkey = "mixed_k_eam_rho_atoms_bytes_per_atom"
+    else:
+        kname = "k_eam_force_atoms (EAM force pass over the atom list)"
+        k_ms = tm[3] / a.steps
+        abytes = algorithmic_bytes_force_atoms(c0["nlocal"], mean_short)
+        tkey = "k_eam_force_atoms_bytes_per_atom"
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     peak, peak_src = 6790.0, "fallback 6.8 TB/s"
     if os.path.exists(peaks_path):
@@ -250,7 +272,7 @@ def run_ours(a, ws, rank, local):
     if os.path.exists(tpath):
         try:
             tj = json.load(open(tpath))
-            per_atom = tj.get("k_eam_force_atoms_bytes_per_atom")
+            per_atom = tj.get(tkey)
             if per_atom:
                 traffic = per_atom * c0["nlocal"]
         except Exception:
@@ -296,34 +318,51 @@ def run_ours(a, ws, rank, local):
                "d2h_bytes_per_step": int(hx.nbytes + hv.nbytes + hf.nbytes),
                "steps": e_steps}
 
-    # the other precision modes on the same system: timing and force error
-    # against the FP64 forces of the same configuration
+    # energy drift of the headline mode: FP64 energies before and after an NVE
+    # run (the potential is not smoothed at the cutoff: phi(rc) = -0.0189 eV,
+    # so pairs crossing it make the total jump by that much)
+    drift = None
+    if a.drift_steps > 0:
+        s.set_timing(False)
+        t_a = s.thermo()
+        s.run(a.drift_steps)
+        t_b = s.thermo()
+        drift = {"steps": a.drift_steps, "mode": a.mode,
+                 "e_start_ev": t_a["etotal"], "e_end_ev": t_b["etotal"],
+                 "ev_per_site": (t_b["etotal"] - t_a["etotal"]) / sites,
+                 "ke_start_ev": t_a["ke_atoms"] + t_a["ke_nodes"]}
+
+    # the other precision modes on the same system: timing, and every mode's
+    # force difference from the bit-exact FP64 forces of one configuration
     modes = {}
+    force_error = None
     if not a.no_modes and ws == 1:
         def forces():
             s.pair_compute()
             s.pair_ecompute()
             return s.atoms()["f"].copy(), s.elements()["nodef"].copy()
-        others = [(n_, c_) for n_, c_ in (("exact", cacg.FP64_EXACT), ("fp64", cacg.FP64),
-                                          ("mixed", cacg.MIXED)) if c_ != mode]
-        # forces of every mode at one configuration first, then the timed runs
-        s.set_precision(mode)
-        f_ref, nf_ref = forces()
-        errs = {}
-        for name, mcode in others:
-            s.set_precision(mcode)
-            f_m, nf_m = forces()
-            err = {}
-            for key, (fa, fb) in {"atoms": (f_m, f_ref), "nodes": (nf_m, nf_ref)}.items():
-                fa = fa.reshape(-1, 3)
-                fb = fb.reshape(-1, 3)
-                if fb.size:
-                    d = np.linalg.norm(fa - fb, axis=1)
-                    n_ = np.linalg.norm(fb, axis=1)
-                    err[key] = {"rms_rel": float(np.sqrt((d ** 2).mean() / (n_ ** 2).mean())),
+
+        def rel_err(fa, fb):
+            out = {}
+            for key, (x, y) in {"atoms": (fa[0], fb[0]), "nodes": (fa[1], fb[1])}.items():
+                x = x.reshape(-1, 3)
+                y = y.reshape(-1, 3)
+                if y.size:
+                    d = np.linalg.norm(x - y, axis=1)
+                    n_ = np.linalg.norm(y, axis=1)
+                    out[key] = {"rms_rel": float(np.sqrt((d ** 2).mean() / (n_ ** 2).mean())),
                                 "max_rel": float(d.max() / n_.max())}
-            errs[name] = err
-        for name, mcode in others:
+            return out
+        codes = {"exact": cacg.FP64_EXACT, "fp64": cacg.FP64, "mixed": cacg.MIXED}
+        fs = {}
+        for name, mcode in codes.items():
+            s.set_precision(mcode)
+            fs[name] = forces()
+        errs = {name: rel_err(fs[name], fs["exact"]) for name in codes}
+        force_error = {"vs": "bit-exact FP64 forces at the same configuration", **errs[a.mode]}
+        for name, mcode in codes.items():
+            if name == a.mode:
+                continue
             s.set_precision(mcode)
             s.set_timing(True)
             s.run(2)
@@ -332,7 +371,7 @@ def run_ours(a, ws, rank, local):
             modes[name] = {"value": sites * a.steps / (tmm[0] * 1e-3),
                            "ms_per_step": tmm[0] / a.steps,
                            "phase_ms_per_step": [round(v / a.steps, 4) for v in tmm[1:6]],
-                           "force_err_vs_" + a.mode: errs[name]}
+                           "force_err_vs_exact": errs[name]}
         s.set_precision(mode)
 
     if rank == 0:
@@ -345,7 +384,7 @@ def run_ours(a, ws, rank, local):
                 "workload": {"small": "C2 sample: EAM Cu 8,000 atoms + 160 elements",
                              "medium": "C2 medium: EAM Cu 360,000 atoms + 7,200 elements",
                              "full": "C2: EAM Cu CAC slab, 1,000,000 atoms + 20,000 elements "
-                                     "(10 sites/edge), FP64"}[a.size],
+                                     "(11 sites/edge, 8 Gauss points each)"}[a.size],
                 "mode": a.mode, "atoms": c0["nlocal"], "ghost_atoms": c0["nghost"],
                 "elements": c0["enlocal"], "ghost_elements": c0["enghost"],
                 "gauss_points": cfg["gauss_per_element"] * c0["enlocal"],
@@ -361,17 +400,22 @@ def run_ours(a, ws, rank, local):
                 "wall_s": round(wall, 3)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "k_eam_force_atoms (EAM force pass over the atom list)",
+                         "kernel": kname,
                          "algorithmic_bytes_per_launch": abytes, "kernel_ms": k_ms,
                          "peak_source": peak_src,
                          "fp64_peak_flops_measured": fp64_peak,
-                         "note": "FP64 pair math is ALU-bound on GB300; see fp64_peak"},
+                         "note": "FP64 pair math is ALU-bound on GB300 (see fp64_peak); the "
+                                 "mixed passes are bound by the latency of neighbor gathers"},
             "cpu_baseline": cpu,
             "e2e": e2e,
             "clocks": clk,
             "gpu_launches": launches,
             "other_modes": modes,
+            "energy_drift": drift,
+            "force_error": force_error,
         }
+        if "fp64" in modes:
+            line["speedup_vs_plain_fp64"] = value / modes["fp64"]["value"]
         print(json.dumps(line), flush=True)
     s.close()
 

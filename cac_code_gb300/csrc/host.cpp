@@ -2220,9 +2220,9 @@ int cacg_run(cacg_handle h, int nsteps) {
 
 int cacg_get_counts(cacg_handle h, long long *c, int n) {
   API_BEGIN
-  long long v[15] = {h->nlocal, h->nghost, 0, h->enlocal, h->enghost, 0, h->nrows, 0,
+  long long v[16] = {h->nlocal, h->nghost, 0, h->enlocal, h->enghost, 0, h->nrows, 0,
                      h->nrebuild, (long long) h->stencil.size(), h->ntimestep, h->nsites,
-                     h->launches, h->nneed, h->nforce};
+                     h->launches, h->nneed, h->nforce, 0};
   if (h->list_built && h->nlocal) {
     std::vector<int> num(h->nlocal);
     check(cudaMemcpyAsync(num.data(), h->d_num.p, sizeof(int) * h->nlocal, cudaMemcpyDeviceToHost, h->stream), "num");
@@ -2241,7 +2241,13 @@ int cacg_get_counts(cacg_handle h, long long *c, int n) {
     h->sync();
     for (int x : num) v[7] += x;
   }
-  for (int i = 0; i < n && i < 15; i++) c[i] = v[i];
+  if (h->list_built && h->nlocal && h->d_snum.p && h->d_snum.cap >= (size_t) h->nlocal) {
+    std::vector<int> num(h->nlocal);
+    check(cudaMemcpyAsync(num.data(), h->d_snum.p, sizeof(int) * h->nlocal, cudaMemcpyDeviceToHost, h->stream), "snum");
+    h->sync();
+    for (int x : num) v[15] += x;
+  }
+  for (int i = 0; i < n && i < 16; i++) c[i] = v[i];
   API_END
 }
 

@@ -94,7 +94,8 @@ int cacg_put_nodes(cacg_handle h, const double *nodex, const double *nodev); /* 
    5 element-list entries 6 integration-point rows 7 ip-list entries
    8 rebuilds so far 9 stencil bins 10 step number 11 interpolated sites
    12 kernel launches issued 13 sites referenced by the lists
-   14 integration points of nonzero weight */
+   14 integration points of nonzero weight 15 atom short-list entries of the
+   last force evaluation */
 int cacg_get_counts(cacg_handle h, long long *counts, int n);
 /* Atom::x/v/f (atom.h:40); all != 0 includes ghosts for x and tag */
 int cacg_get_atoms(cacg_handle h, int all, double *x, double *v, double *f, int *tag);
