@@ -35,6 +35,8 @@ UNITS = [
     ("k_mixed.cu", ["-fmad=true"]),
     ("k_thermo.cu", ["-fmad=true"]),
     ("k_noalloc.cu", ["-fmad=true"]),
+    ("k_gemm.cu", ["-fmad=true"]),
+    ("mlp.cu", ["-fmad=true"]),
 ]
 
 

@@ -34,6 +34,7 @@ _STATUS = {0: "ok", -1: "invalid", -2: "state", -3: "cuda", -4: "overflow", -5: 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int)
 _lp = ctypes.POINTER(ctypes.c_longlong)
+_fp = ctypes.POINTER(ctypes.c_float)
 
 EXPORTED = [
     "cacg_create", "cacg_destroy", "cacg_error", "cacg_version", "cacg_command", "cacg_file",
@@ -45,6 +46,10 @@ EXPORTED = [
     "cacg_get_elements", "cacg_get_atom_list", "cacg_get_elem_list", "cacg_get_ip_list",
     "cacg_get_cut", "cacg_set_timing", "cacg_get_timing", "cacg_measure_fp64_peak",
     "cacg_put_atoms", "cacg_put_nodes", "cacg_compute_thermo", "cacg_kinetic_noalloc",
+    "cacg_mlp_create", "cacg_mlp_destroy", "cacg_mlp_error", "cacg_mlp_sizes",
+    "cacg_mlp_get_params", "cacg_mlp_set_params", "cacg_mlp_set_normalization",
+    "cacg_mlp_get_normalization", "cacg_mlp_loss_grad", "cacg_mlp_train", "cacg_mlp_predict",
+    "cacg_gemm_bf16_tn",
 ]
 
 
@@ -86,6 +91,21 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
     lib.cacg_kinetic_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                          ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                          ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]
+    vp, i, d, f = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_float
+    lib.cacg_mlp_create.argtypes = [ctypes.POINTER(vp), i, i, ctypes.c_ulonglong]
+    lib.cacg_mlp_destroy.argtypes = [vp]
+    lib.cacg_mlp_error.restype = ctypes.c_char_p
+    lib.cacg_mlp_error.argtypes = [vp]
+    lib.cacg_mlp_sizes.argtypes = [vp, _lp, i]
+    lib.cacg_mlp_get_params.argtypes = [vp, i, _fp]
+    lib.cacg_mlp_set_params.argtypes = [vp, i, _fp]
+    lib.cacg_mlp_set_normalization.argtypes = [vp, _fp, _fp, _fp, _fp, d]
+    lib.cacg_mlp_get_normalization.argtypes = [vp, _fp, _fp, _fp, _fp, _dp]
+    lib.cacg_mlp_loss_grad.argtypes = [vp, i, _fp, _fp, i, _dp, _fp]
+    lib.cacg_mlp_train.argtypes = [vp, _fp, _fp, ctypes.c_longlong, i, i, f, ctypes.c_ulonglong,
+                                   _dp]
+    lib.cacg_mlp_predict.argtypes = [vp, _fp, ctypes.c_longlong, _fp, _fp]
+    lib.cacg_gemm_bf16_tn.argtypes = [vp, i, vp, i, vp, i, i, i, i, vp, vp]
     _LIB = lib
     return lib
 
@@ -96,6 +116,94 @@ def _d(a):
 
 def _i(a):
     return a.ctypes.data_as(_ip) if a is not None else None
+
+
+def _f(a):
+    return a.ctypes.data_as(_fp) if a is not None else None
+
+
+class Mlp:
+    """The nodal-force surrogate ensemble (cacg_mlp_*): host arrays in and out."""
+
+    def __init__(self, device: int = 0, members: int = 4, seed: int = 1):
+        self._L = load()
+        self.h = ctypes.c_void_p()
+        rc = self._L.cacg_mlp_create(ctypes.byref(self.h), device, members, seed)
+        if rc != 0:
+            raise CacgError(rc, "cacg_mlp_create failed (no CUDA device visible?)")
+        sz = np.zeros(6, dtype=np.int64)
+        self._ok(self._L.cacg_mlp_sizes(self.h, sz.ctypes.data_as(_lp), 6))
+        self.members, self.nparam, self.nin, self.nout, self.hidden = (int(v) for v in sz[:5])
+
+    def _ok(self, rc: int):
+        if rc != 0:
+            raise CacgError(rc, self._L.cacg_mlp_error(self.h).decode())
+
+    def close(self):
+        if self.h:
+            self._L.cacg_mlp_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self, member: int) -> np.ndarray:
+        p = np.zeros(self.nparam, dtype=np.float32)
+        self._ok(self._L.cacg_mlp_get_params(self.h, member, _f(p)))
+        return p
+
+    def set_params(self, member: int, p: np.ndarray):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        self._ok(self._L.cacg_mlp_set_params(self.h, member, _f(p)))
+
+    def set_normalization(self, in_mean, in_std, out_mean, out_std, force_scale: float):
+        a = [np.ascontiguousarray(v, dtype=np.float32) for v in (in_mean, in_std, out_mean, out_std)]
+        self._ok(self._L.cacg_mlp_set_normalization(self.h, *(_f(v) for v in a), float(force_scale)))
+
+    def fit_normalization(self, x: np.ndarray, t: np.ndarray):
+        """Standardise inputs and outputs on a training set; force scale = rms
+        per-element nodal-force norm."""
+        sd = x.std(axis=0)
+        osd = t.std(axis=0)
+        fs = float(np.sqrt((t.astype(np.float64) ** 2).sum(axis=1).mean() / 8.0))
+        self.set_normalization(x.mean(axis=0), np.where(sd > 0, sd, 1.0), t.mean(axis=0),
+                               np.where(osd > 0, osd, 1.0), max(fs, 1e-30))
+
+    def normalization(self):
+        im, isd = np.zeros(self.nin, np.float32), np.zeros(self.nin, np.float32)
+        om, osd = np.zeros(self.nout, np.float32), np.zeros(self.nout, np.float32)
+        fs = np.zeros(1)
+        self._ok(self._L.cacg_mlp_get_normalization(self.h, _f(im), _f(isd), _f(om), _f(osd),
+                                                     _d(fs)))
+        return im, isd, om, osd, float(fs[0])
+
+    def loss_grad(self, member: int, x: np.ndarray, t: np.ndarray):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        loss = np.zeros(1)
+        g = np.zeros(self.nparam, dtype=np.float32)
+        self._ok(self._L.cacg_mlp_loss_grad(self.h, member, _f(x), _f(t), x.shape[0], _d(loss), _f(g)))
+        return float(loss[0]), g
+
+    def train(self, x: np.ndarray, t: np.ndarray, epochs: int, batch: int = 1024,
+              lr: float = 1e-3, seed: int = 7) -> float:
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        loss = np.zeros(1)
+        self._ok(self._L.cacg_mlp_train(self.h, _f(x), _f(t), x.shape[0], epochs, batch, lr, seed,
+                                        _d(loss)))
+        return float(loss[0])
+
+    def predict(self, x: np.ndarray):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        n = x.shape[0]
+        mean = np.zeros((n, self.nout), dtype=np.float32)
+        spread = np.zeros(n, dtype=np.float32)
+        self._ok(self._L.cacg_mlp_predict(self.h, _f(x), n, _f(mean), _f(spread)))
+        return mean, spread
 
 
 class System:

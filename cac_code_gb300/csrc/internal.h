@@ -293,6 +293,16 @@ void kinetic(const double *v, const int *type, const double *mass, int n, int pe
              double scale, double *part, cudaStream_t s);
 }  // namespace thermo
 
+// ---- tensor-core GEMM (k_gemm.cu) and the surrogate MLP (mlp.cu) ----
+namespace gemm {
+// C = A B^T, bf16 operands (K-major), fp32 accumulation; kind: 0 store C,
+// 1 C = acc + bias, 2 Z = acc + bias and H = silu(Z), 3 H = acc * silu'(Z),
+// 4 H = silu(acc + bias)
+void gemm_tn(const void *A, int lda, const void *B, int ldb, int M, int N, int K, int kind,
+             const float *bias, float *c, int ldc, void *h, int ldh, int *err, cudaStream_t s);
+}  // namespace gemm
+constexpr int MLP_IN = 32, MLP_HIDDEN = 256, MLP_OUT = 24;
+
 // ---- integration and reductions (k_nve.cu) ----
 void launch_nve_atoms_initial(double4 *x, double *v, const double *f, const int *type,
                               const double *mass, int n, double dtv, double dtf,

@@ -141,6 +141,48 @@ int cacg_compute_thermo(cacg_handle h, double *out, int n);
 int cacg_kinetic_noalloc(const double *v, const int *type, const double *mass, int n,
                          int per_item, double scale, double mvv2e, double *out, void *stream);
 
+/* ---- nodal-force surrogate (no counterpart in the reference, which
+   evaluates every element by integration-point quadrature) ----
+   An ensemble of MLPs 32 -> 256 -> 256 -> 256 -> 24 (SiLU) maps an element's
+   features (24 nodal displacements about their mean, relative to the ideal
+   lattice, then 8 nodal densities) to its 24 nodal forces.  Forward and
+   backward passes run on the tensor cores (BF16 operands, FP32 accumulation);
+   weights are FP32 masters trained with Adam.  Parameters per member, in
+   order: W1[256][32] b1[256] W2[256][256] b2[256] W3[256][256] b3[256]
+   W4[24][256] b4[24].  Arrays are host arrays. */
+typedef struct cacg_mlp_t *cacg_mlp;
+int cacg_mlp_create(cacg_mlp *m, int device, int members, unsigned long long seed);
+int cacg_mlp_destroy(cacg_mlp m);
+const char *cacg_mlp_error(cacg_mlp m);
+/* sizes: 0 members 1 parameters per member 2 inputs 3 outputs 4 hidden width
+   5 optimizer steps taken */
+int cacg_mlp_sizes(cacg_mlp m, long long *sizes, int n);
+int cacg_mlp_get_params(cacg_mlp m, int member, float *params);
+int cacg_mlp_set_params(cacg_mlp m, int member, const float *params);
+/* inputs are standardised as (x - in_mean) / in_std; outputs are
+   out_mean + out_std * y; force_scale (rms nodal-force magnitude) is the unit
+   of the ensemble-spread tolerance */
+int cacg_mlp_set_normalization(cacg_mlp m, const float *in_mean, const float *in_std,
+                               const float *out_mean, const float *out_std, double force_scale);
+int cacg_mlp_get_normalization(cacg_mlp m, float *in_mean, float *in_std, float *out_mean,
+                               float *out_std, double *force_scale);
+/* mean-squared error of member's normalised outputs on n samples x[n][32],
+   t[n][24] and its gradient with respect to every parameter (no update) */
+int cacg_mlp_loss_grad(cacg_mlp m, int member, const float *x, const float *t, int n,
+                       double *loss, float *grad);
+/* Adam over shuffled whole batches (batch a multiple of 128) for every member;
+   *loss = mean normalised loss of the last epoch */
+int cacg_mlp_train(cacg_mlp m, const float *x, const float *t, long long n, int epochs, int batch,
+                   float lr, unsigned long long seed, double *loss);
+/* ensemble mean[n][24] (force units) and spread[n] (largest per-output
+   standard deviation across members, force units) */
+int cacg_mlp_predict(cacg_mlp m, const float *x, long long n, float *mean, float *spread);
+/* C[m][n] = A[m][k] B[n][k]^T on device arrays (bf16 A, B; fp32 C), k a
+   multiple of 64, lda/ldb multiples of 8; *err (device int) is set if a
+   bounded wait in the kernel ran out */
+int cacg_gemm_bf16_tn(const void *a, int lda, const void *b, int ldb, float *c, int ldc, int m,
+                      int n, int k, int *err, void *stream);
+
 /* ---- measurement ---- */
 /* Phase timing of the last cacg_run from CUDA events on the handle's stream
    (recorded only after cacg_set_timing(h, 1)): ms[0] total, [1] integrate +
