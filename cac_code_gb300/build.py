@@ -37,6 +37,7 @@ UNITS = [
     ("k_noalloc.cu", ["-fmad=true"]),
     ("k_gemm.cu", ["-fmad=true"]),
     ("mlp.cu", ["-fmad=true"]),
+    ("k_surrogate.cu", ["-fmad=true"]),
 ]
 
 

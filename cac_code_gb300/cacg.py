@@ -49,7 +49,8 @@ EXPORTED = [
     "cacg_mlp_create", "cacg_mlp_destroy", "cacg_mlp_error", "cacg_mlp_sizes",
     "cacg_mlp_get_params", "cacg_mlp_set_params", "cacg_mlp_set_normalization",
     "cacg_mlp_get_normalization", "cacg_mlp_loss_grad", "cacg_mlp_train", "cacg_mlp_predict",
-    "cacg_gemm_bf16_tn",
+    "cacg_gemm_bf16_tn", "cacg_surrogate_reference", "cacg_surrogate_samples",
+    "cacg_surrogate_attach",
 ]
 
 
@@ -106,6 +107,9 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
                                    _dp]
     lib.cacg_mlp_predict.argtypes = [vp, _fp, ctypes.c_longlong, _fp, _fp]
     lib.cacg_gemm_bf16_tn.argtypes = [vp, i, vp, i, vp, i, i, i, i, vp, vp]
+    lib.cacg_surrogate_reference.argtypes = [vp, _dp]
+    lib.cacg_surrogate_samples.argtypes = [vp, _fp, _fp, i]
+    lib.cacg_surrogate_attach.argtypes = [vp, vp, d, d]
     _LIB = lib
     return lib
 
@@ -320,11 +324,12 @@ class System:
 
     # ---- state out ----
     def counts(self) -> Dict[str, int]:
-        c = np.zeros(16, dtype=np.int64)
-        self._ok(self._L.cacg_get_counts(self.h, c.ctypes.data_as(_lp), 16))
+        c = np.zeros(19, dtype=np.int64)
+        self._ok(self._L.cacg_get_counts(self.h, c.ctypes.data_as(_lp), 19))
         keys = ["nlocal", "nghost", "atom_entries", "enlocal", "enghost", "elem_entries",
                 "ip_rows", "ip_entries", "rebuilds", "nstencil", "step", "sites", "launches",
-                "sites_needed", "force_rows", "short_entries"]
+                "sites_needed", "force_rows", "short_entries", "surrogate_elements",
+                "surrogate_evaluated", "surrogate_accepted"]
         return dict(zip(keys, (int(v) for v in c)))
 
     def atoms(self, all_: bool = False) -> Dict[str, np.ndarray]:
@@ -380,6 +385,21 @@ class System:
         return {"pe_atoms": out[0], "pe_elements": out[1], "ke_atoms": out[2],
                 "ke_nodes": out[3], "virial": out[4:10].copy(), "kinetic_tensor": out[10:16].copy(),
                 "volume": out[16], "etotal": out[0] + out[1] + out[2] + out[3]}
+
+    def surrogate_reference(self, nodex0=None):
+        a = None if nodex0 is None else np.ascontiguousarray(nodex0, dtype=np.float64)
+        self._ok(self._L.cacg_surrogate_reference(self.h, _d(a)))
+
+    def surrogate_samples(self):
+        n = self.counts()["enlocal"]
+        x = np.zeros((n, 32), dtype=np.float32)
+        t = np.zeros((n, 24), dtype=np.float32)
+        self._ok(self._L.cacg_surrogate_samples(self.h, _f(x), _f(t), n))
+        return x, t
+
+    def surrogate_attach(self, mlp: Optional["Mlp"], tol: float = 1e-4, dist: float = 11.0):
+        self._ok(self._L.cacg_surrogate_attach(self.h, mlp.h if mlp is not None else None,
+                                               float(tol), float(dist)))
 
     def set_timing(self, enable: bool = True):
         self._ok(self._L.cacg_set_timing(self.h, 1 if enable else 0))

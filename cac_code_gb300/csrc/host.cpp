@@ -202,6 +202,17 @@ struct cacg_context {
   DBuf<float> d_u, d_shape_f, d_ljf, d_site_rho;
   DBuf<double> d_cutsq64, d_stage, d_part, d_lj5;
   std::vector<double> h_lj5;
+  // nodal-force surrogate (elements far from the atoms)
+  cacg_mlp_t *sur = nullptr;
+  double sur_tol = 1e-4, sur_dist = 0.0;
+  DBuf<double> d_nodex0;
+  bool have_x0 = false;
+  DBuf<int> d_far, d_far_rows, d_static_rows;
+  int nfar = 0, nfar_rows = 0, nstatic_rows = 0;
+  DBuf<unsigned char> d_skip;
+  DBuf<unsigned short> d_sfeat;  // bf16 features [nfar][64]
+  DBuf<float> d_smean, d_sspread, d_sraw;
+  DBuf<unsigned long long> d_scount;  // evaluated, accepted element-steps
   DBuf<double> d_v, d_f, d_xhold, d_rho, d_fp, d_mass;
   DBuf<int> d_type, d_tag, d_root, d_send;
   DBuf<int> d_abin, d_bcount, d_bstart, d_bmem, d_stencil;
@@ -339,6 +350,10 @@ struct cacg_context {
   void nve_initial();
   void nve_final();
   void compute_thermo(double *out);
+  void surrogate_reference(const double *nodex0);
+  void surrogate_samples(float *x, float *t);
+  void surrogate_attach(cacg_mlp_t *m, double tol, double dist);
+  void surrogate_predict(const EamTables &e);
   int decide();
   void rebuild();
   void run(int n);
@@ -368,6 +383,16 @@ cacg_context::~cacg_context() {
   d_stage.release();
   d_part.release();
   d_lj5.release();
+  d_nodex0.release();
+  d_far.release();
+  d_far_rows.release();
+  d_static_rows.release();
+  d_skip.release();
+  d_sfeat.release();
+  d_smean.release();
+  d_sspread.release();
+  d_sraw.release();
+  d_scount.release();
   DBuf<double> *bd[] = {&d_v, &d_f, &d_xhold, &d_rho, &d_fp, &d_mass, &d_ex, &d_nodex, &d_nodev,
                         &d_nodef, &d_nodexhold, &d_erho, &d_emass, &d_diag, &d_fip, &d_site_fp,
                         &d_spa_int, &d_weight, &d_spa_inter, &d_spa_csub, &d_spa_isub, &d_frho,
@@ -1673,9 +1698,24 @@ void cacg_context::pair_ecompute_mixed() {
   const double csq = pair_style == 1 ? ljtab.cutsq[1 * (MAXT + 1) + 1] : cutforcesq;
   d_sipnum.ensure(std::max(nrows, 1), s);
   d_sipent.ensure((size_t) maxip * rowstride, s);
-  fp64_fma::filter_rows(d_nodex.p, d_etype.p, d_row_elem.p, d_row_jj.p, nrows, d_ipnum.p, d_ipent.p,
-                        rowstride, d_site_h.p, t, cut_pass(csq), 1, d_sipnum.p, d_sipent.p, s);
+  const bool use_sur = sur && nfar > 0;
+  if (use_sur)  // node rows of every element, force rows of the elements near the atoms
+    fp64_fma::filter_rows(d_nodex.p, d_etype.p, d_row_elem.p, d_row_jj.p, nstatic_rows, d_ipnum.p,
+                          d_ipent.p, rowstride, d_site_h.p, t, cut_pass(csq), 1, d_sipnum.p,
+                          d_sipent.p, s, d_static_rows.p, nullptr);
+  else
+    fp64_fma::filter_rows(d_nodex.p, d_etype.p, d_row_elem.p, d_row_jj.p, nrows, d_ipnum.p, d_ipent.p,
+                          rowstride, d_site_h.p, t, cut_pass(csq), 1, d_sipnum.p, d_sipent.p, s);
   launches += 2;
+  // the surrogate's verdict for the far elements, then the short lists of the
+  // force rows of those it declined
+  auto far_rows = [&]() {
+    surrogate_predict(eamtab());
+    fp64_fma::filter_rows(d_nodex.p, d_etype.p, d_row_elem.p, d_row_jj.p, nfar_rows, d_ipnum.p,
+                          d_ipent.p, rowstride, d_site_h.p, t, cut_pass(csq), 1, d_sipnum.p,
+                          d_sipent.p, s, d_far_rows.p, d_skip.p);
+    launches++;
+  };
   launches++;
   const float eps = 1.0e-4f;
   mixed::MixedElems m{};
@@ -1699,6 +1739,7 @@ void cacg_context::pair_ecompute_mixed() {
   m.nforce = nforce;
   m.node_hl = d_node_hl.p;
   m.spa_int_hl = d_spa_int_hl.p;
+  if (use_sur) m.skip = d_skip.p;
   if (pair_style == 1) {
     int a = 1 * (MAXT + 1) + 1;
     m.cutsq = ljtab.cutsq[a];
@@ -1706,6 +1747,7 @@ void cacg_context::pair_ecompute_mixed() {
     m.band_lo = m.cutsq_f * (1.0f - eps);
     m.band_hi = m.cutsq_f * (1.0f + eps);
     EamTables e{};
+    if (use_sur) far_rows();
     mixed::ip_pass(m, 0, nullptr, e, (float) ljtab.lj1[a], (float) ljtab.lj2[a], d_fip.p, s);
     launches++;
   } else {
@@ -1722,11 +1764,178 @@ void cacg_context::pair_ecompute_mixed() {
                            d_site_rho.p, s);
     m.erho = d_erho.p;
     m.site_rho = d_site_rho.p;
+    if (use_sur) far_rows();
     mixed::ip_pass(m, 2, d_ftab.p, e, 0.f, 0.f, d_fip.p, s);
     launches += 4;
   }
   fp64_fma::gather_nodef(d_fip.p, d_etype.p, d_row_first.p, enlocal, t, d_nodef.p, s);
   launches++;
+  if (use_sur) {
+    surrogate::write_forces(d_smean.p, d_far.p, nfar, d_skip.p, d_nodef.p, s);
+    launches++;
+  }
+}
+
+// ------------------------------------------------------------------ surrogate
+
+void cacg_context::surrogate_reference(const double *nodex0) {
+  if (!inited || enlocal == 0) fail(CACG_ESTATE, "no elements on the device yet");
+  d_nodex0.ensure((size_t) 24 * enlocal, stream);
+  if (nodex0)
+    check(cudaMemcpyAsync(d_nodex0.p, nodex0, sizeof(double) * 24 * enlocal, cudaMemcpyHostToDevice, stream), "nodex0");
+  else
+    check(cudaMemcpyAsync(d_nodex0.p, d_nodex.p, sizeof(double) * 24 * enlocal, cudaMemcpyDeviceToDevice, stream), "nodex0");
+  have_x0 = true;
+}
+
+// features (raw) and plain-quadrature nodal forces of every local element at
+// the current state, in the handle's precision mode, the surrogate detached
+void cacg_context::surrogate_samples(float *x, float *t) {
+  if (!elists_built) fail(CACG_ESTATE, "samples before the node neighbor list is built");
+  if (!have_x0) surrogate_reference(nullptr);
+  cacg_mlp_t *keep = sur;
+  sur = nullptr;
+  try {
+    forward_comm();  // ghosts follow nodes put since the last step
+    pair_ecompute();
+  } catch (...) {
+    sur = keep;
+    throw;
+  }
+  sur = keep;
+  cudaStream_t s = stream;
+  d_sraw.ensure((size_t) enlocal * (MLP_IN + MLP_OUT), s);
+  surrogate::raw_features(d_nodex.p, d_nodex0.p, pair_style == 2 ? d_erho.p : nullptr, enlocal,
+                          d_sraw.p, s);
+  surrogate::to_float(d_nodef.p, (long long) enlocal * MLP_OUT, d_sraw.p + (size_t) enlocal * MLP_IN, s);
+  check(cudaMemcpyAsync(x, d_sraw.p, sizeof(float) * enlocal * MLP_IN, cudaMemcpyDeviceToHost, s), "x");
+  check(cudaMemcpyAsync(t, d_sraw.p + (size_t) enlocal * MLP_IN, sizeof(float) * enlocal * MLP_OUT,
+                        cudaMemcpyDeviceToHost, s), "t");
+  sync();
+}
+
+// Elements whose whole extent (centre +- the largest centre-node distance)
+// lies farther than `dist` from every local atom use the surrogate; the rows
+// lists of both kinds are fixed here.
+void cacg_context::surrogate_attach(cacg_mlp_t *m, double tol, double dist) {
+  sur = nullptr;
+  nfar = nfar_rows = nstatic_rows = 0;
+  if (!m) return;
+  if (mode != CACG_MIXED) fail(CACG_EINVAL, "the surrogate runs in the mixed-precision element pass");
+  if (!elists_built || !setup_done) fail(CACG_ESTATE, "attach the surrogate after the lists are built");
+  if (!(tol >= 0) || !(dist >= 0)) fail(CACG_EINVAL, "bad surrogate tolerance or distance");
+  if (!have_x0) surrogate_reference(nullptr);
+  cudaStream_t s = stream;
+  std::vector<double> nx((size_t) 24 * enlocal), ax;
+  check(cudaMemcpyAsync(nx.data(), d_nodex.p, sizeof(double) * nx.size(), cudaMemcpyDeviceToHost, s), "nodex");
+  std::vector<double4> x4(nlocal);
+  if (nlocal)
+    check(cudaMemcpyAsync(x4.data(), d_x.p, sizeof(double4) * nlocal, cudaMemcpyDeviceToHost, s), "x");
+  sync();
+  std::vector<double> cx(3 * enlocal), rad(enlocal);
+  double rmax = 0.0;
+  for (int e = 0; e < enlocal; e++) {
+    double c[3] = {0, 0, 0};
+    for (int k = 0; k < NPE; k++)
+      for (int d = 0; d < 3; d++) c[d] += nx[24 * e + 3 * k + d] / NPE;
+    double r2 = 0.0;
+    for (int k = 0; k < NPE; k++) {
+      double q = 0.0;
+      for (int d = 0; d < 3; d++) q += (nx[24 * e + 3 * k + d] - c[d]) * (nx[24 * e + 3 * k + d] - c[d]);
+      r2 = std::max(r2, q);
+    }
+    for (int d = 0; d < 3; d++) cx[3 * e + d] = c[d];
+    rad[e] = std::sqrt(r2);
+    rmax = std::max(rmax, rad[e]);
+  }
+  // atoms binned in cubes of side >= dist + rmax
+  const double side = std::max(dist + rmax, 1e-6);
+  int nb[3];
+  for (int d = 0; d < 3; d++) nb[d] = std::max(1, std::min(1024, (int) std::floor(prd[d] / side)));
+  auto cell = [&](double v, int d) {
+    int c = (int) std::floor((v - lo[d]) / prd[d] * nb[d]);
+    return std::min(std::max(c, 0), nb[d] - 1);
+  };
+  std::vector<std::vector<int>> bins((size_t) nb[0] * nb[1] * nb[2]);
+  for (int i = 0; i < nlocal; i++)
+    bins[((size_t) cell(x4[i].x, 0) * nb[1] + cell(x4[i].y, 1)) * nb[2] + cell(x4[i].z, 2)].push_back(i);
+  std::vector<int> far, is_far(enlocal, 0);
+  for (int e = 0; e < enlocal; e++) {
+    const double lim = dist + rad[e];
+    const double *c = &cx[3 * e];
+    int cc[3] = {cell(c[0], 0), cell(c[1], 1), cell(c[2], 2)};
+    bool near_ = false;
+    for (int dx = -1; dx <= 1 && !near_; dx++)
+      for (int dy = -1; dy <= 1 && !near_; dy++)
+        for (int dz = -1; dz <= 1 && !near_; dz++) {
+          int q[3] = {cc[0] + dx, cc[1] + dy, cc[2] + dz};
+          bool outside = false;
+          for (int d = 0; d < 3; d++)
+            if (q[d] < 0 || q[d] >= nb[d]) {
+              if (periodic[d]) q[d] = (q[d] + nb[d]) % nb[d];
+              else outside = true;
+            }
+          if (outside) continue;
+          for (int i : bins[((size_t) q[0] * nb[1] + q[1]) * nb[2] + q[2]]) {
+            double dd[3] = {x4[i].x - c[0], x4[i].y - c[1], x4[i].z - c[2]};
+            double r2 = 0.0;
+            for (int d = 0; d < 3; d++) {
+              if (periodic[d]) dd[d] -= prd[d] * std::nearbyint(dd[d] / prd[d]);
+              r2 += dd[d] * dd[d];
+            }
+            if (r2 < lim * lim) {
+              near_ = true;
+              break;
+            }
+          }
+        }
+    if (!near_) {
+      far.push_back(e);
+      is_far[e] = 1;
+    }
+  }
+  // rows: node rows of every element plus force rows of the near elements
+  // (static), force rows of the far elements (filtered per step)
+  std::vector<int> st, fr;
+  for (int e = 0; e < enlocal; e++) {
+    const int ty = h_etype[e];
+    for (int jj = 0; jj < numint[ty]; jj++) {
+      const int r = h_row_first[e] + jj;
+      bool node = false;
+      for (int q = 0; q < NPE; q++) node = node || node_list[ty * NPE + q] == jj;
+      const bool force = weight[ty][jj] != 0.0;
+      if (node || (force && !is_far[e])) st.push_back(r);
+      if (force && is_far[e]) fr.push_back(r);
+    }
+  }
+  nfar = (int) far.size();
+  nfar_rows = (int) fr.size();
+  nstatic_rows = (int) st.size();
+  upload(d_far, far.empty() ? std::vector<int>{0} : far, s);
+  upload(d_far_rows, fr.empty() ? std::vector<int>{0} : fr, s);
+  upload(d_static_rows, st.empty() ? std::vector<int>{0} : st, s);
+  d_skip.ensure(std::max(enlocal, 1), s);
+  check(cudaMemsetAsync(d_skip.p, 0, std::max(enlocal, 1), s), "skip");
+  d_scount.ensure(2, s);
+  check(cudaMemsetAsync(d_scount.p, 0, 2 * sizeof(unsigned long long), s), "scount");
+  d_sfeat.ensure((size_t) 64 * std::max(nfar, 1), s);
+  d_smean.ensure((size_t) MLP_OUT * std::max(nfar, 1), s);
+  d_sspread.ensure(std::max(nfar, 1), s);
+  sur_tol = tol;
+  sur_dist = dist;
+  sur = m;
+  sync();
+}
+
+void cacg_context::surrogate_predict(const EamTables &) {
+  mlp::Net *net = mlp::net_of(sur);
+  cudaStream_t s = stream;
+  surrogate::features(d_nodex.p, d_nodex0.p, pair_style == 2 ? d_erho.p : nullptr, d_far.p, nfar,
+                      mlp::norm_device(net), d_sfeat.p, s);
+  mlp::predict(net, d_sfeat.p, nfar, d_smean.p, d_sspread.p, s);
+  surrogate::accept(d_sspread.p, d_far.p, nfar, (float) (sur_tol * mlp::force_scale(net)), d_skip.p,
+                    d_scount.p, s);
+  launches += 3 + 1 + 3 * mlp::members(net);
 }
 
 void cacg_context::pair_ecompute() {
@@ -2220,9 +2429,16 @@ int cacg_run(cacg_handle h, int nsteps) {
 
 int cacg_get_counts(cacg_handle h, long long *c, int n) {
   API_BEGIN
-  long long v[16] = {h->nlocal, h->nghost, 0, h->enlocal, h->enghost, 0, h->nrows, 0,
+  long long v[19] = {h->nlocal, h->nghost, 0, h->enlocal, h->enghost, 0, h->nrows, 0,
                      h->nrebuild, (long long) h->stencil.size(), h->ntimestep, h->nsites,
-                     h->launches, h->nneed, h->nforce, 0};
+                     h->launches, h->nneed, h->nforce, 0, h->sur ? h->nfar : 0, 0, 0};
+  if (h->sur && h->d_scount.p) {
+    unsigned long long c2[2] = {0, 0};
+    check(cudaMemcpyAsync(c2, h->d_scount.p, sizeof(c2), cudaMemcpyDeviceToHost, h->stream), "scount");
+    h->sync();
+    v[17] = (long long) c2[0];
+    v[18] = (long long) c2[1];
+  }
   if (h->list_built && h->nlocal) {
     std::vector<int> num(h->nlocal);
     check(cudaMemcpyAsync(num.data(), h->d_num.p, sizeof(int) * h->nlocal, cudaMemcpyDeviceToHost, h->stream), "num");
@@ -2247,7 +2463,7 @@ int cacg_get_counts(cacg_handle h, long long *c, int n) {
     h->sync();
     for (int x : num) v[15] += x;
   }
-  for (int i = 0; i < n && i < 16; i++) c[i] = v[i];
+  for (int i = 0; i < n && i < 19; i++) c[i] = v[i];
   API_END
 }
 
@@ -2364,6 +2580,27 @@ int cacg_compute_thermo(cacg_handle h, double *out, int n) {
   double v[17];
   h->compute_thermo(v);
   for (int i = 0; i < n && i < 17; i++) out[i] = v[i];
+  API_END
+}
+
+int cacg_surrogate_reference(cacg_handle h, const double *nodex0) {
+  API_BEGIN
+  h->surrogate_reference(nodex0);
+  h->sync();
+  API_END
+}
+
+int cacg_surrogate_samples(cacg_handle h, float *x, float *t, int n) {
+  API_BEGIN
+  if (!x || !t) fail(CACG_EINVAL, "null output array");
+  if (n != h->enlocal) fail(CACG_EINVAL, "n must equal the number of local elements (%d)", h->enlocal);
+  h->surrogate_samples(x, t);
+  API_END
+}
+
+int cacg_surrogate_attach(cacg_handle h, cacg_mlp m, double tol, double dist) {
+  API_BEGIN
+  h->surrogate_attach(m, tol, dist);
   API_END
 }
 

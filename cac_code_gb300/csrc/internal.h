@@ -9,6 +9,8 @@
 #include <string>
 #include <vector>
 
+struct cacg_mlp_t;
+
 namespace cacg {
 
 constexpr int NPE = 8;    // nodes per 3-d element (element.cpp:41)
@@ -224,7 +226,8 @@ void filter_atoms(const float4 *xh, const int *num, const int *list, int stride,
 void filter_rows(const double *nodex, const int *etype, const int *row_elem, const int *row_jj,
                  int nrows, const int *ipnum, const int *ipent, int rowstride,
                  const float4 *site_h, ElemTables t, float cut_pass, int only_needed, int *snum,
-                 int *sent, cudaStream_t s);
+                 int *sent, cudaStream_t s, const int *row_list = nullptr,
+                 const unsigned char *skip = nullptr);
 }  // namespace fp64_fma
 
 // ---- mixed precision (k_mixed.cu): FP32 pair terms, FP64 accumulation ----
@@ -252,6 +255,7 @@ struct MixedElems {
   double cutsq;
   const float2 *node_hl;     // [nall][24] double-single node coordinates
   const float2 *spa_int_hl;  // double-single integration-point shape functions
+  const unsigned char *skip = nullptr;  // elements whose forces come from the surrogate
 };
 void split_hilo(const double4 *x, float4 *xh, float4 *xl, int n, cudaStream_t s);
 void sites_ds(const double *nodex, const int *etype, const int *site_base, const int *inter_num,
@@ -300,8 +304,34 @@ namespace gemm {
 // 4 H = silu(acc + bias)
 void gemm_tn(const void *A, int lda, const void *B, int ldb, int M, int N, int K, int kind,
              const float *bias, float *c, int ldc, void *h, int ldh, int *err, cudaStream_t s);
+// all members and layers of the surrogate in one launch (k_mlp_ensemble)
+void mlp_ensemble(const void *xf, int n, const void *w1s, const void *w2s, const void *w3s,
+                  const void *w4s, const float *bias, int members, const float *norm, float *mean,
+                  float *spread, int *err, cudaStream_t s);
 }  // namespace gemm
 constexpr int MLP_IN = 32, MLP_HIDDEN = 256, MLP_OUT = 24;
+namespace mlp {
+struct Net;
+Net *net_of(cacg_mlp_t *m);
+const float *norm_device(const Net *n);  // in_mean[32], in_inv_std[32], out_mean[24], out_std[24]
+double force_scale(const Net *n);
+int members(const Net *n);
+// ensemble prediction on normalised bf16 features [count][64] on the device
+void predict(Net *n, const void *xf, long long count, float *mean, float *spread, cudaStream_t s);
+// throws when a bounded wait inside a GEMM ran out (reads a device flag)
+void check_error(Net *n, cudaStream_t s);
+}  // namespace mlp
+namespace surrogate {
+void features(const double *nodex, const double *nodex0, const double *erho, const int *elems,
+              int n, const float *norm, void *xf, cudaStream_t s);
+void raw_features(const double *nodex, const double *nodex0, const double *erho, int n, float *x,
+                  cudaStream_t s);
+void accept(const float *spread, const int *far, int nfar, float thr, unsigned char *skip,
+            unsigned long long *counters, cudaStream_t s);
+void write_forces(const float *mean, const int *far, int nfar, const unsigned char *skip,
+                  double *nodef, cudaStream_t s);
+void to_float(const double *src, long long n, float *dst, cudaStream_t s);
+}  // namespace surrogate
 
 // ---- integration and reductions (k_nve.cu) ----
 void launch_nve_atoms_initial(double4 *x, double *v, const double *f, const int *type,

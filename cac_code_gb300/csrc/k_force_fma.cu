@@ -382,10 +382,17 @@ k_filter_rows(const double *__restrict__ nodex, const int *__restrict__ etype,
               const int *__restrict__ row_elem, const int *__restrict__ row_jj, int nrows,
               const int *__restrict__ ipnum, const int *__restrict__ ipent, int rowstride,
               const float4 *__restrict__ site_h, ElemTables t, float cut_pass, int only_needed,
-              int *__restrict__ snum, int *__restrict__ sent) {
-  int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= nrows) return;
+              int *__restrict__ snum, int *__restrict__ sent, const int *__restrict__ row_list,
+              const unsigned char *__restrict__ skip) {
+  int it = blockIdx.x * blockDim.x + threadIdx.x;
+  if (it >= nrows) return;
+  const int r = row_list ? row_list[it] : it;
   const int e = row_elem[r], jj = row_jj[r], ty = etype[e];
+  // rows of nonzero weight of an element whose forces come from elsewhere
+  if (skip && skip[e] && t.weight[t.int_off[ty] + jj] != 0.0) {
+    snum[r] = 0;
+    return;
+  }
   if (only_needed && t.weight[t.int_off[ty] + jj] == 0.0) {
     bool node = false;
     for (int q = 0; q < NPE; q++) node = node || t.node_list[ty * NPE + q] == jj;
@@ -504,11 +511,11 @@ void filter_atoms(const float4 *xh, const int *num, const int *list, int stride,
 void filter_rows(const double *nodex, const int *etype, const int *row_elem, const int *row_jj,
                  int nrows, const int *ipnum, const int *ipent, int rowstride,
                  const float4 *site_h, ElemTables t, float cut_pass, int only_needed, int *snum,
-                 int *sent, cudaStream_t s) {
+                 int *sent, cudaStream_t s, const int *row_list, const unsigned char *skip) {
   if (nrows <= 0) return;
   k_filter_rows<<<nblk(nrows, 128), 128, 0, s>>>(nodex, etype, row_elem, row_jj, nrows, ipnum,
                                                 ipent, rowstride, site_h, t, cut_pass,
-                                                only_needed, snum, sent);
+                                                only_needed, snum, sent, row_list, skip);
   check(cudaGetLastError(), "filter_rows");
 }
 

@@ -121,7 +121,8 @@ __device__ __forceinline__ void tmem_ld16(unsigned taddr, float (&v)[16]) {
   for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
-__device__ __forceinline__ float sigmoidf_(float z) { return 1.f / (1.f + __expf(-z)); }
+__device__ __forceinline__ float sigmoidf_(float z) { return __fdividef(1.f, 1.f + __expf(-z)); }
+__device__ __forceinline__ float siluf_(float z) { return __fdividef(z, 1.f + __expf(-z)); }
 
 struct Epi {
   int kind;
@@ -247,38 +248,55 @@ k_gemm_tn(const __grid_constant__ CUtensorMap tma_a, const __grid_constant__ CUt
       tmem_ld16(tl + c, v);
       if (row >= M) continue;
       const int col = n0 + c;
+      const bool full = col + 16 <= N;
       if (ep.kind == 0 || ep.kind == 1) {
         float *dst = ep.c + (size_t) row * ep.ldc + col;
+        if (ep.kind == 1)
 #pragma unroll
-        for (int i = 0; i < 16; i++)
-          if (col + i < N) dst[i] = v[i] + (ep.kind == 1 ? ep.bias[col + i] : 0.f);
-      } else if (ep.kind == 2) {
-        float *z = ep.c + (size_t) row * ep.ldc + col;
-        __nv_bfloat16 *h = ep.h + (size_t) row * ep.ldh + col;
+          for (int i = 0; i < 16; i++) v[i] += col + i < N ? ep.bias[col + i] : 0.f;
+        if (full && (ep.ldc & 3) == 0 && (reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
 #pragma unroll
-        for (int i = 0; i < 16; i++)
-          if (col + i < N) {
-            float zz = v[i] + ep.bias[col + i];
-            z[i] = zz;
-            h[i] = __float2bfloat16(zz * sigmoidf_(zz));
-          }
-      } else if (ep.kind == 4) {
-        __nv_bfloat16 *h = ep.h + (size_t) row * ep.ldh + col;
+          for (int i = 0; i < 4; i++)
+            reinterpret_cast<float4 *>(dst)[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+        } else {
 #pragma unroll
-        for (int i = 0; i < 16; i++)
-          if (col + i < N) {
-            float zz = v[i] + ep.bias[col + i];
-            h[i] = __float2bfloat16(zz * sigmoidf_(zz));
-          }
+          for (int i = 0; i < 16; i++)
+            if (col + i < N) dst[i] = v[i];
+        }
+        continue;
+      }
+      // bf16 outputs: 16 values as two 16-byte stores where the row allows it
+      float hv[16];
+      if (ep.kind == 2 || ep.kind == 4) {
+        float *z = ep.c ? ep.c + (size_t) row * ep.ldc + col : nullptr;
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+          const float zz = v[i] + (col + i < N ? ep.bias[col + i] : 0.f);
+          if (ep.kind == 2 && col + i < N) z[i] = zz;
+          hv[i] = zz * sigmoidf_(zz);
+        }
       } else {
         const float *z = ep.c + (size_t) row * ep.ldc + col;
-        __nv_bfloat16 *h = ep.h + (size_t) row * ep.ldh + col;
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+          const float zz = col + i < N ? z[i] : 0.f, sg = sigmoidf_(zz);
+          hv[i] = v[i] * sg * (1.f + zz * (1.f - sg));
+        }
+      }
+      __nv_bfloat16 *h = ep.h + (size_t) row * ep.ldh + col;
+      if (full && (ep.ldh & 7) == 0 && (reinterpret_cast<uintptr_t>(h) & 15) == 0) {
+        unsigned w[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+          __nv_bfloat162 p2 = __floats2bfloat162_rn(hv[2 * i], hv[2 * i + 1]);
+          w[i] = *reinterpret_cast<unsigned *>(&p2);
+        }
+        reinterpret_cast<uint4 *>(h)[0] = make_uint4(w[0], w[1], w[2], w[3]);
+        reinterpret_cast<uint4 *>(h)[1] = make_uint4(w[4], w[5], w[6], w[7]);
+      } else {
 #pragma unroll
         for (int i = 0; i < 16; i++)
-          if (col + i < N) {
-            float zz = z[i], sg = sigmoidf_(zz);
-            h[i] = __float2bfloat16(v[i] * sg * (1.f + zz * (1.f - sg)));
-          }
+          if (col + i < N) h[i] = __float2bfloat16(hv[i]);
       }
     }
   }
@@ -288,6 +306,225 @@ k_gemm_tn(const __grid_constant__ CUtensorMap tma_a, const __grid_constant__ CUt
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"(TMEM_COLS)
+                 : "memory");
+  }
+}
+
+// ---------------------------------------------------------------- fused ensemble
+//
+// The whole surrogate ensemble for 128 elements per CTA in one launch:
+// for each member k and layer l the CTA runs D = A_l W_l^T on the tensor cores
+// (A_1 = the features tile sX, A_l = the previous layer's activations in sA),
+// reads D back from TMEM, applies bias + SiLU and writes the BF16 activations
+// into sA in the same 128-byte-swizzled K-major layout TMA would produce, so
+// the next layer's MMAs read them directly.  The 13 weight k-tiles of each
+// member (W1: 1, W2: 4, W3: 4, W4: 4) stream through four shared-memory
+// stages, loaded by TMA up to four tiles ahead of the MMAs.  Sixteen warps
+// share the epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (its rows)
+// and columns 64 (w / 4) .. + 63.  The last layer's
+// outputs are summed over the members in registers; the kernel writes the
+// denormalised ensemble mean and the spread (largest per-output standard
+// deviation across members).
+constexpr int ENS_NT = 512, ENS_STAGES = 4, ENS_H = 256, ENS_OUT = 24, ENS_BSTRIDE = 3 * 256 + 24;
+constexpr int ENS_MAX_MEMBERS = 4;  // shared memory: 16 + 64 + 4 x 32 KB + biases
+constexpr int ENS_X_BYTES = BM * BK * 2, ENS_A_BYTES = BM * ENS_H * 2, ENS_W_BYTES = ENS_H * BK * 2;
+
+struct EnsArgs {
+  const float *bias;  // [members][b1 256, b2 256, b3 256, b4 24]
+  const float *norm;  // out_mean at [64, 88), out_std at [88, 112)
+  float *mean, *spread;
+  int n, members;
+  int *err;
+};
+
+__device__ __forceinline__ void ens_issue(int g, const CUtensorMap *w1, const CUtensorMap *w2,
+                                          const CUtensorMap *w3, const CUtensorMap *w4,
+                                          unsigned char *sw, unsigned long long *full) {
+  const int k = g / 13, r = g % 13;
+  const int st = g % ENS_STAGES;
+  const unsigned fb = smem_u32(full + st), dst = smem_u32(sw + st * ENS_W_BYTES);
+  if (r == 0) {
+    mbar_expect_tx(fb, ENS_W_BYTES);
+    tma_load_2d(dst, w1, 0, k * ENS_H, fb);
+  } else if (r < 5) {
+    mbar_expect_tx(fb, ENS_W_BYTES);
+    tma_load_2d(dst, w2, (r - 1) * BK, k * ENS_H, fb);
+  } else if (r < 9) {
+    mbar_expect_tx(fb, ENS_W_BYTES);
+    tma_load_2d(dst, w3, (r - 5) * BK, k * ENS_H, fb);
+  } else {
+    mbar_expect_tx(fb, 32 * BK * 2);
+    tma_load_2d(dst, w4, (r - 9) * BK, k * ENS_OUT, fb);
+  }
+}
+
+// byte offset of (row, 16-byte chunk) in a 128-row, 64-column bf16 SW128 atom column
+__device__ __forceinline__ unsigned sw128_off(int row, int chunk) {
+  return (unsigned) ((row >> 3) * 1024 + (row & 7) * 128 + ((chunk ^ (row & 7)) << 4));
+}
+
+__global__ void __launch_bounds__(ENS_NT, 1)
+k_mlp_ensemble(const __grid_constant__ CUtensorMap tma_x, const __grid_constant__ CUtensorMap tma_w1,
+               const __grid_constant__ CUtensorMap tma_w2, const __grid_constant__ CUtensorMap tma_w3,
+               const __grid_constant__ CUtensorMap tma_w4, EnsArgs a) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char *base = reinterpret_cast<unsigned char *>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  unsigned char *sx = base;
+  unsigned char *sa = sx + ENS_X_BYTES;
+  unsigned char *sw = sa + ENS_A_BYTES;
+  float *sbias = reinterpret_cast<float *>(sw + ENS_STAGES * ENS_W_BYTES);
+  unsigned long long *bars =
+      reinterpret_cast<unsigned long long *>(sbias + a.members * ENS_BSTRIDE);  // full[3] empty[3] x done
+  unsigned *tmem_slot = reinterpret_cast<unsigned *>(bars + 2 * ENS_STAGES + 2);
+  unsigned long long *full = bars, *empty = bars + ENS_STAGES, *xbar = bars + 2 * ENS_STAGES,
+                     *done = bars + 2 * ENS_STAGES + 1;
+  __shared__ int s_fail;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int wg = warp >> 2, q = warp & 3, row = q * 32 + lane;
+  const int m0 = blockIdx.x * BM;
+  const int T = 13 * a.members;
+
+  for (int i = tid; i < a.members * ENS_BSTRIDE; i += ENS_NT) sbias[i] = a.bias[i];
+  if (tid == 0) {
+    s_fail = 0;
+    for (int i = 0; i < 2 * ENS_STAGES + 2; i++) mbar_init(smem_u32(bars + i), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(ENS_H)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const unsigned tmem = *tmem_slot;
+
+  int issued = 0;
+  if (tid == 0) {
+    mbar_expect_tx(smem_u32(xbar), ENS_X_BYTES);
+    tma_load_2d(smem_u32(sx), &tma_x, 0, m0, smem_u32(xbar));
+    for (; issued < ENS_STAGES && issued < T; issued++)
+      ens_issue(issued, &tma_w1, &tma_w2, &tma_w3, &tma_w4, sw, full);
+  }
+  float s1[ENS_OUT], s2[ENS_OUT];
+#pragma unroll
+  for (int c = 0; c < ENS_OUT; c++) s1[c] = s2[c] = 0.f;
+
+  int g = 0;        // next weight tile to consume
+  int nlayer = 0;   // layers completed (parity of `done`)
+  bool ok = true;
+  for (int k = 0; k < a.members && ok; k++) {
+    const float *bk = sbias + k * ENS_BSTRIDE;
+    for (int l = 1; l <= 4 && ok; l++) {
+      if (tid == 0) {
+        bool good = true;
+        if (g == 0) good = mbar_wait(smem_u32(xbar), 0);
+        const int nk = l == 1 ? 1 : 4;
+        const unsigned idesc = idesc_bf16(l == 4 ? 32 : ENS_H);
+        for (int kt = 0; kt < nk && good; kt++, g++) {
+          const int st = g % ENS_STAGES;
+          if (!mbar_wait(smem_u32(full + st), (g / ENS_STAGES) & 1)) {
+            good = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const unsigned a_addr = l == 1 ? smem_u32(sx) : smem_u32(sa + kt * (BM * BK * 2));
+          const unsigned b_addr = smem_u32(sw + st * ENS_W_BYTES);
+#pragma unroll
+          for (int kk = 0; kk < BK / 16; kk++)
+            mma_bf16(tmem, sw128_desc(a_addr + kk * 32), sw128_desc(b_addr + kk * 32), idesc,
+                     (kt | kk) != 0);
+          mma_commit(smem_u32(empty + st));
+          if (g >= 1 && issued < T) {  // refill the stage the previous tile used
+            const int pg = g - 1;
+            if (!mbar_wait(smem_u32(empty + pg % ENS_STAGES), (pg / ENS_STAGES) & 1)) {
+              good = false;
+              break;
+            }
+            ens_issue(issued++, &tma_w1, &tma_w2, &tma_w3, &tma_w4, sw, full);
+          }
+        }
+        mma_commit(smem_u32(done));
+        if (!good) {
+          atomicExch(a.err, 1);
+          s_fail = 1;
+        }
+      }
+      __syncwarp();
+      bool ready = false;
+      for (unsigned it = 0; it < WAIT_LIMIT; it++) {
+        if (mbar_try(smem_u32(done), nlayer & 1)) {
+          ready = true;
+          break;
+        }
+      }
+      nlayer++;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const unsigned tl = tmem + ((unsigned) (q * 32) << 16);
+      if (l < 4) {
+        const float *b = bk + (l - 1) * ENS_H;
+#pragma unroll 1
+        for (int c = wg * 64; c < wg * 64 + 64; c += 16) {
+          float v[16];
+          tmem_ld16(tl + c, v);
+          unsigned w[8];
+#pragma unroll
+          for (int i = 0; i < 8; i++) {
+            float z0 = v[2 * i] + b[c + 2 * i], z1 = v[2 * i + 1] + b[c + 2 * i + 1];
+            __nv_bfloat162 h2 = __floats2bfloat162_rn(siluf_(z0), siluf_(z1));
+            w[i] = *reinterpret_cast<unsigned *>(&h2);
+          }
+          const int ac = c >> 6, ch = (c & 63) >> 3;
+          unsigned char *dst = sa + ac * (BM * BK * 2);
+          *reinterpret_cast<uint4 *>(dst + sw128_off(row, ch)) = make_uint4(w[0], w[1], w[2], w[3]);
+          *reinterpret_cast<uint4 *>(dst + sw128_off(row, ch + 1)) = make_uint4(w[4], w[5], w[6], w[7]);
+        }
+      } else if (wg == 0) {
+        const float *b = bk + 3 * ENS_H;
+        float v0[16], v1[16];
+        tmem_ld16(tl, v0);
+        tmem_ld16(tl + 16, v1);
+#pragma unroll
+        for (int c = 0; c < ENS_OUT; c++) {
+          float y = (c < 16 ? v0[c] : v1[c - 16]) + b[c];
+          s1[c] += y;
+          s2[c] += y * y;
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      if (__syncthreads_or(!ready || *((volatile int *) &s_fail))) ok = false;
+    }
+  }
+  if (!ok && tid == 0) {
+    atomicExch(a.err, 2);
+    // let the weight copies already issued land before the CTA exits
+    for (int t = g; t < issued; t++) mbar_wait(smem_u32(full + t % ENS_STAGES), (t / ENS_STAGES) & 1);
+  }
+  if (ok && wg == 0 && m0 + row < a.n) {
+    const float inv = 1.f / a.members;
+    float smax = 0.f;
+    float *mo = a.mean + (size_t) (m0 + row) * ENS_OUT;
+#pragma unroll
+    for (int c = 0; c < ENS_OUT; c++) {
+      const float mu = s1[c] * inv, var = fmaxf(s2[c] * inv - mu * mu, 0.f);
+      const float sd = a.norm[88 + c];
+      mo[c] = mu * sd + a.norm[64 + c];
+      smax = fmaxf(smax, sqrtf(var) * sd);
+    }
+    a.spread[m0 + row] = smax;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ENS_H)
                  : "memory");
   }
 }
@@ -364,6 +601,33 @@ void gemm_tn(const void *A, int lda, const void *B, int ldb, int M, int N, int K
     case 128: launch<128, 4>(ta, tb, M, N, K, ep, err, s); break;
     default: launch<256, 3>(ta, tb, M, N, K, ep, err, s); break;
   }
+}
+
+// The fused ensemble on normalised bf16 features xf[n][64]; weights stacked
+// over the members: w1s[m*256][64], w2s/w3s[m*256][256], w4s[m*24][256];
+// bias[m][792] (b1, b2, b3, b4).
+void mlp_ensemble(const void *xf, int n, const void *w1s, const void *w2s, const void *w3s,
+                  const void *w4s, const float *bias, int members, const float *norm, float *mean,
+                  float *spread, int *err, cudaStream_t s) {
+  if (n <= 0) return;
+  if (members < 1 || members > ENS_MAX_MEMBERS)
+    throw CudaError{cudaErrorInvalidValue, "mlp_ensemble: 1..4 members"};
+  CUtensorMap tx = make_map(xf, n, 64, 64, BM);
+  CUtensorMap t1 = make_map(w1s, members * ENS_H, 64, 64, ENS_H);
+  CUtensorMap t2 = make_map(w2s, members * ENS_H, ENS_H, ENS_H, ENS_H);
+  CUtensorMap t3 = make_map(w3s, members * ENS_H, ENS_H, ENS_H, ENS_H);
+  CUtensorMap t4 = make_map(w4s, members * ENS_OUT, ENS_H, ENS_H, 32);
+  const size_t smem = 1024 + ENS_X_BYTES + ENS_A_BYTES + (size_t) ENS_STAGES * ENS_W_BYTES +
+                      sizeof(float) * members * ENS_BSTRIDE + (2 * ENS_STAGES + 2) * 8 + 16;
+  static size_t attr = 0;
+  if (smem > attr) {
+    check(cudaFuncSetAttribute(k_mlp_ensemble, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem),
+          "ensemble smem attribute");
+    attr = smem;
+  }
+  EnsArgs a{bias, norm, mean, spread, n, members, err};
+  k_mlp_ensemble<<<(n + BM - 1) / BM, ENS_NT, smem, s>>>(tx, t1, t2, t3, t4, a);
+  check(cudaGetLastError(), "k_mlp_ensemble");
 }
 
 }  // namespace gemm

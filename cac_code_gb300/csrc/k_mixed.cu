@@ -360,6 +360,7 @@ struct ElemArgs {
   float cutsq_f, band_lo, band_hi;
   double cutsq;
   const float2 *node_hl, *spa_int_hl;
+  const unsigned char *skip;
 };
 
 // integration-point position in double-single from the split nodes and the
@@ -404,6 +405,7 @@ k_ip(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr,
     } else {
       r = a.rows[it];  // rows of nonzero weight only; the others stay zero
       e = a.row_elem[r];
+      if (a.skip && a.skip[e]) continue;  // nodal forces from the surrogate
       ty = a.etype[e];
       jj = a.row_jj[r];
     }
@@ -582,7 +584,7 @@ void ip_pass(const MixedElems &m, int pass, const float4 *tab, const EamTables &
   ElemArgs a{m.nodex, m.erho, m.site_h, m.site_l, m.site_rho, m.etype, m.row_elem, m.row_jj,
              m.row_first, m.ipnum, m.ipent, m.nrows, m.rowstride, m.nlocal_e, m.spa_int,
              m.weight, m.int_off, m.node_list, m.rows, m.nforce, m.cutsq_f, m.band_lo,
-             m.band_hi, m.cutsq, m.node_hl, m.spa_int_hl};
+             m.band_hi, m.cutsq, m.node_hl, m.spa_int_hl, m.skip};
   if (pass == 0) {  // LJ forces
     int g = persistent_grid((const void *) k_ip<false, false>, 512, 0, m.nforce);
     k_ip<false, false><<<g, 512, 0, s>>>(a, tab, 0, 0.f, nullptr, 0, 0.0, lj1, lj2, out);

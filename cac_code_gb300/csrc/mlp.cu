@@ -77,20 +77,22 @@ __global__ void k_transpose(const bf16 *__restrict__ in, int rows, int cols, int
   }
 }
 
-// column sums of a bf16 [rows][ld] matrix into fp32 out[cols]
+// column sums of a bf16 [rows][ld] matrix, added into fp32 out[cols] (zeroed
+// by the caller): block (x, y) sums 256 rows of 32 columns
 __global__ void k_colsum(const bf16 *__restrict__ g, int rows, int cols, int ld,
                          float *__restrict__ out) {
   __shared__ float red[8][33];
-  int c = blockIdx.x * 32 + threadIdx.x;
+  const int c = blockIdx.x * 32 + threadIdx.x;
+  const int r0 = blockIdx.y * 256, r1 = min(rows, r0 + 256);
   float s = 0.f;
   if (c < cols)
-    for (int r = threadIdx.y; r < rows; r += blockDim.y) s += __bfloat162float(g[(long) r * ld + c]);
+    for (int r = r0 + threadIdx.y; r < r1; r += blockDim.y) s += __bfloat162float(g[(long) r * ld + c]);
   red[threadIdx.y][threadIdx.x] = s;
   __syncthreads();
   if (threadIdx.y == 0 && c < cols) {
     float t = 0.f;
     for (int k = 0; k < (int) blockDim.y; k++) t += red[k][threadIdx.x];
-    out[c] = t;
+    atomicAdd(out + c, t);
   }
 }
 
@@ -231,6 +233,12 @@ struct Net {
 
   void sync() { check(cudaStreamSynchronize(stream), "mlp sync"); }
 
+  void ensure_err(cudaStream_t s) {
+    if (errflag.p) return;
+    errflag.ensure(1, s);
+    check(cudaMemsetAsync(errflag.p, 0, sizeof(int), s), "errflag");
+  }
+
   void upload_norm() {
     d_norm.ensure(2 * NIN + 2 * NOUT, stream);
     check(cudaMemcpyAsync(d_norm.p, norm, sizeof(norm), cudaMemcpyHostToDevice, stream), "norm");
@@ -265,6 +273,7 @@ struct Net {
   // bf16 copies of member k's weights (forward and transposed)
   void refresh(int k) {
     Member &M = mem[k];
+    stacked = false;
     cudaStream_t s = stream;
     M.w1.ensure((size_t) NH * NINP, s);
     M.w2.ensure((size_t) NH * NH, s);
@@ -298,8 +307,7 @@ struct Net {
     tb.ensure(b * NOUT, s);
     db.ensure(NH, s);
     part.ensure(nblk(b * NGP, 256), s);
-    errflag.ensure(1, s);
-    check(cudaMemsetAsync(errflag.p, 0, sizeof(int), s), "errflag");
+    ensure_err(s);
     bcap = B;
   }
 
@@ -310,7 +318,8 @@ struct Net {
   }
 
   void colsum(const bf16 *g, int rows, int cols, int ld, float *out) {
-    k_colsum<<<nblk(cols, 32), dim3(32, 8), 0, stream>>>(g, rows, cols, ld, out);
+    check(cudaMemsetAsync(out, 0, sizeof(float) * cols, stream), "colsum zero");
+    k_colsum<<<dim3(nblk(cols, 32), nblk(rows, 256)), dim3(32, 8), 0, stream>>>(g, rows, cols, ld, out);
     check(cudaGetLastError(), "colsum");
   }
 
@@ -383,44 +392,55 @@ struct Net {
     refresh(k);
   }
 
-  // ensemble prediction on normalised bf16 features already on the device
-  void predict_device(const bf16 *xf, long long n, float *mean, float *spread) {
+  bool stacked = false;  // iw1/iw1b hold the current first layers
+
+  // ensemble prediction on normalised bf16 features already on the device:
+  // one fused launch over all members and layers (gemm::mlp_ensemble)
+  DBuf<bf16> iw2, iw3, iw4;
+  DBuf<float> ibias;
+  void predict_device(const bf16 *xf, long long n, float *mean, float *spread, cudaStream_t s) {
     if (n <= 0) return;
-    cudaStream_t s = stream;
-    if (n > icap) {
-      size_t b = (size_t) n;
-      ih1.ensure(b * NH * members, s);
-      ih2.ensure(b * NH, s);
-      ih3.ensure(b * NH, s);
-      iy.ensure(b * NOUT * members, s);
-      icap = n;
+    ensure_err(s);
+    if (!stacked) {
+      const int BS = 3 * NH + NOUT;
+      iw1.ensure((size_t) members * NH * NINP, s);
+      iw2.ensure((size_t) members * NH * NH, s);
+      iw3.ensure((size_t) members * NH * NH, s);
+      iw4.ensure((size_t) members * NOUT * NH, s);
+      ibias.ensure((size_t) members * BS, s);
+      for (int k = 0; k < members; k++) {
+        Member &M = mem[k];
+        check(cudaMemcpyAsync(iw1.p + (size_t) k * NH * NINP, M.w1.p, sizeof(bf16) * NH * NINP, cudaMemcpyDeviceToDevice, s), "w1s");
+        check(cudaMemcpyAsync(iw2.p + (size_t) k * NH * NH, M.w2.p, sizeof(bf16) * NH * NH, cudaMemcpyDeviceToDevice, s), "w2s");
+        check(cudaMemcpyAsync(iw3.p + (size_t) k * NH * NH, M.w3.p, sizeof(bf16) * NH * NH, cudaMemcpyDeviceToDevice, s), "w3s");
+        check(cudaMemcpyAsync(iw4.p + (size_t) k * NOUT * NH, M.w4.p, sizeof(bf16) * NOUT * NH, cudaMemcpyDeviceToDevice, s), "w4s");
+        float *b = ibias.p + (size_t) k * BS;
+        check(cudaMemcpyAsync(b, M.p.p + ob1, sizeof(float) * NH, cudaMemcpyDeviceToDevice, s), "b1s");
+        check(cudaMemcpyAsync(b + NH, M.p.p + ob2, sizeof(float) * NH, cudaMemcpyDeviceToDevice, s), "b2s");
+        check(cudaMemcpyAsync(b + 2 * NH, M.p.p + ob3, sizeof(float) * NH, cudaMemcpyDeviceToDevice, s), "b3s");
+        check(cudaMemcpyAsync(b + 3 * NH, M.p.p + ob4, sizeof(float) * NOUT, cudaMemcpyDeviceToDevice, s), "b4s");
+      }
+      stacked = true;
     }
-    errflag.ensure(1, s);
-    // layer 1 of all members at once: stacked W1 [members*256][64]
-    iw1.ensure((size_t) members * NH * NINP, s);
-    iw1b.ensure((size_t) members * NH, s);
-    for (int k = 0; k < members; k++) {
-      check(cudaMemcpyAsync(iw1.p + (size_t) k * NH * NINP, mem[k].w1.p, sizeof(bf16) * NH * NINP,
-                            cudaMemcpyDeviceToDevice, s), "w1 stack");
-      check(cudaMemcpyAsync(iw1b.p + (size_t) k * NH, mem[k].p.p + ob1, sizeof(float) * NH,
-                            cudaMemcpyDeviceToDevice, s), "b1 stack");
-    }
-    const int W = members * NH;
-    int *e = errflag.p;
-    gemm::gemm_tn(xf, NINP, iw1.p, NINP, (int) n, W, NINP, 4, iw1b.p, nullptr, 0, ih1.p, W, e, s);
-    for (int k = 0; k < members; k++) {
-      Member &M = mem[k];
-      gemm::gemm_tn(ih1.p + k * NH, W, M.w2.p, NH, (int) n, NH, NH, 4, M.p.p + ob2, nullptr, 0,
-                    ih2.p, NH, e, s);
-      gemm::gemm_tn(ih2.p, NH, M.w3.p, NH, (int) n, NH, NH, 4, M.p.p + ob3, nullptr, 0, ih3.p,
-                    NH, e, s);
-      gemm::gemm_tn(ih3.p, NH, M.w4.p, NH, (int) n, NOUT, NH, 1, M.p.p + ob4,
-                    iy.p + (size_t) k * n * NOUT, NOUT, nullptr, 0, e, s);
-    }
-    k_ensemble<<<nblk(n, 256), 256, 0, s>>>(iy.p, n, members, n * NOUT, d_norm.p, mean, spread);
-    check(cudaGetLastError(), "ensemble");
+    gemm::mlp_ensemble(xf, (int) n, iw1.p, iw2.p, iw3.p, iw4.p, ibias.p, members, d_norm.p, mean,
+                       spread, errflag.p, s);
   }
 };
+
+Net *net_of(cacg_mlp_t *m);
+const float *norm_device(const Net *n) { return n->d_norm.p; }
+double force_scale(const Net *n) { return n->force_scale; }
+int members(const Net *n) { return n->members; }
+void predict(Net *n, const void *xf, long long count, float *mean, float *spread, cudaStream_t s) {
+  n->ensure_err(s);
+  n->predict_device(static_cast<const bf16 *>(xf), count, mean, spread, s);
+}
+void check_error(Net *n, cudaStream_t s) {
+  int v = 0;
+  check(cudaMemcpyAsync(&v, n->errflag.p, sizeof(int), cudaMemcpyDeviceToHost, s), "errflag");
+  check(cudaStreamSynchronize(s), "errflag sync");
+  if (v) throw CudaError{cudaErrorLaunchTimeout, "tensor-core GEMM: a bounded wait ran out"};
+}
 
 void features_bf16(const float *x, long long n, const float *norm, bf16 *out, cudaStream_t s) {
   k_features<<<nblk(n * NINP, 256), 256, 0, s>>>(x, n, norm, out);
@@ -450,6 +470,12 @@ using cacg::mlp::bf16;
 struct cacg_mlp_t {
   Net net;
 };
+
+namespace cacg {
+namespace mlp {
+Net *net_of(cacg_mlp_t *m) { return m ? &m->net : nullptr; }
+}  // namespace mlp
+}  // namespace cacg
 
 namespace {
 
@@ -516,7 +542,7 @@ void upload_set(Net &N, const float *x, const float *t, long long n, cacg::DBuf<
 extern "C" {
 
 int cacg_mlp_create(cacg_mlp *out, int device, int members, unsigned long long seed) {
-  if (!out || members < 1 || members > 16) return CACG_EINVAL;
+  if (!out || members < 1 || members > 4) return CACG_EINVAL;
   *out = nullptr;
   cacg_mlp m = new (std::nothrow) cacg_mlp_t;
   if (!m) return CACG_ENOMEM;
@@ -560,7 +586,9 @@ int cacg_mlp_destroy(cacg_mlp m) {
   for (auto *b : {&N.x0, &N.h1, &N.h2, &N.h3, &N.g4, &N.g3, &N.g2, &N.g1, &N.x0t, &N.h1t, &N.h2t,
                   &N.h3t, &N.g1t, &N.g2t, &N.g3t, &N.g4t, &N.ix0, &N.ih1, &N.ih2, &N.ih3, &N.iw1})
     b->release();
-  for (auto *b : {&N.d_norm, &N.z1, &N.z2, &N.z3, &N.y, &N.tb, &N.db, &N.iy, &N.iw1b}) b->release();
+  for (auto *b : {&N.d_norm, &N.z1, &N.z2, &N.z3, &N.y, &N.tb, &N.db, &N.iy, &N.iw1b, &N.ibias})
+    b->release();
+  for (auto *b : {&N.iw2, &N.iw3, &N.iw4}) b->release();
   N.part.release();
   N.errflag.release();
   if (N.stream) cudaStreamDestroy(N.stream);
@@ -713,9 +741,8 @@ int cacg_mlp_predict(cacg_mlp m, const float *x, long long n, float *mean, float
   upload_set(N, x, nullptr, n, xf, tf);
   dm.ensure((size_t) n * MLP_OUT, N.stream);
   ds.ensure((size_t) n, N.stream);
-  N.errflag.ensure(1, N.stream);
-  cacg::check(cudaMemsetAsync(N.errflag.p, 0, sizeof(int), N.stream), "err");
-  N.predict_device(xf.p, n, dm.p, ds.p);
+  N.ensure_err(N.stream);
+  N.predict_device(xf.p, n, dm.p, ds.p, N.stream);
   N.check_err();
   if (mean)
     cacg::check(cudaMemcpyAsync(mean, dm.p, sizeof(float) * n * MLP_OUT, cudaMemcpyDeviceToHost, N.stream), "mean");

@@ -95,7 +95,8 @@ int cacg_put_nodes(cacg_handle h, const double *nodex, const double *nodev); /* 
    8 rebuilds so far 9 stencil bins 10 step number 11 interpolated sites
    12 kernel launches issued 13 sites referenced by the lists
    14 integration points of nonzero weight 15 atom short-list entries of the
-   last force evaluation */
+   last force evaluation 16 elements handed to the surrogate 17 surrogate
+   evaluations (element-steps) 18 of which accepted */
 int cacg_get_counts(cacg_handle h, long long *counts, int n);
 /* Atom::x/v/f (atom.h:40); all != 0 includes ghosts for x and tag */
 int cacg_get_atoms(cacg_handle h, int all, double *x, double *v, double *f, int *tag);
@@ -151,6 +152,7 @@ int cacg_kinetic_noalloc(const double *v, const int *type, const double *mass, i
    order: W1[256][32] b1[256] W2[256][256] b2[256] W3[256][256] b3[256]
    W4[24][256] b4[24].  Arrays are host arrays. */
 typedef struct cacg_mlp_t *cacg_mlp;
+/* members: 1..4 */
 int cacg_mlp_create(cacg_mlp *m, int device, int members, unsigned long long seed);
 int cacg_mlp_destroy(cacg_mlp m);
 const char *cacg_mlp_error(cacg_mlp m);
@@ -182,6 +184,19 @@ int cacg_mlp_predict(cacg_mlp m, const float *x, long long n, float *mean, float
    bounded wait in the kernel ran out */
 int cacg_gemm_bf16_tn(const void *a, int lda, const void *b, int ldb, float *c, int ldc, int m,
                       int n, int k, int *err, void *stream);
+
+/* Surrogate in the step (CACG_MIXED element pass).  Reference node
+   positions [enlocal][8][3] for the displacement features (NULL: the current
+   nodes); by default the nodes at the first surrogate call. */
+int cacg_surrogate_reference(cacg_handle h, const double *nodex0);
+/* Features x[n][32] and plain-quadrature nodal forces t[n][24] of every local
+   element at the current state (n = local elements), in the handle's
+   precision mode: the surrogate's training samples. */
+int cacg_surrogate_samples(cacg_handle h, float *x, float *t, int n);
+/* Use m for the elements lying farther than dist from every atom; an
+   element whose ensemble spread exceeds tol * force_scale falls back to the
+   quadrature that step.  m = NULL detaches. */
+int cacg_surrogate_attach(cacg_handle h, cacg_mlp m, double tol, double dist);
 
 /* ---- measurement ---- */
 /* Phase timing of the last cacg_run from CUDA events on the handle's stream

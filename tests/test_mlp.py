@@ -8,9 +8,10 @@ from oracle import mlp_oracle as MO
 
 
 def _data(n, seed):
+    # one fixed target function; the seed draws the inputs
+    w = np.random.default_rng(0).normal(size=(MO.NIN, MO.NOUT)) / np.sqrt(MO.NIN)
     rng = np.random.default_rng(seed)
     x = rng.normal(size=(n, MO.NIN)).astype(np.float32)
-    w = rng.normal(size=(MO.NIN, MO.NOUT)) / np.sqrt(MO.NIN)
     t = (np.tanh(x @ w) + 0.1 * np.sin(3 * x[:, :MO.NOUT])).astype(np.float32)
     return x, t
 
@@ -101,29 +102,37 @@ def test_device_loss_grad_matches_oracle(cacg_lib):
         net.close()
 
 
+def _oracle_ensemble(net, x, norm):
+    ys = []
+    for k in range(net.members):
+        xn, _ = MO.normalize(x, None, norm)
+        y, _ = MO.forward(net.params(k).astype(np.float64), xn)
+        ys.append(y * norm[3] + norm[2])
+    ys = np.array(ys)
+    return ys.mean(axis=0), ys.std(axis=0).max(axis=1)
+
+
 @pytest.mark.gpu
 def test_device_prediction_and_training(cacg_lib):
-    x, t = _data(8192, 5)
+    x, t = _data(32768, 5)
     xv, tv = _data(1024, 6)
     net = cacg_lib.Mlp(0, members=4, seed=3)
     try:
         net.fit_normalization(x, t)
         norm = net.normalization()[:4]
-        # prediction of the untrained ensemble against the oracle forward
-        mean, spread = net.predict(xv[:256])
-        ys = []
-        for k in range(4):
-            xn, _ = MO.normalize(xv[:256], None, norm)
-            y, _ = MO.forward(net.params(k).astype(np.float64), xn)
-            ys.append(y * norm[3] + norm[2])
-        ys = np.array(ys)
-        assert np.abs(mean - ys.mean(axis=0)).max() <= 2e-2 * np.abs(ys).max()
-        assert np.all(spread >= 0)
-        before = float(((mean - tv[:256]) ** 2).mean())
-        loss = net.train(x, t, epochs=40, batch=512, lr=2e-3)
+        # the fused ensemble kernel against the oracle forward, untrained
         mean, spread = net.predict(xv)
+        m_ref, s_ref = _oracle_ensemble(net, xv, norm)
+        assert np.abs(mean - m_ref).max() <= 2e-2 * np.abs(m_ref).max()
+        assert np.abs(spread - s_ref).max() <= 5e-2 * s_ref.max() + 1e-6
+        before = float(((mean - tv) ** 2).mean())
+        loss = net.train(x, t, epochs=10, batch=1024, lr=2e-3)
+        mean, spread = net.predict(xv)
+        # and trained
+        m_ref, s_ref = _oracle_ensemble(net, xv, norm)
+        assert np.abs(mean - m_ref).max() <= 2e-2 * np.abs(m_ref).max()
         after = float(((mean - tv) ** 2).mean())
-        assert loss < 0.05, loss
-        assert after < 0.1 * before, (before, after)
+        assert loss < 0.1, loss
+        assert after < 0.3 * before, (before, after)
     finally:
         net.close()
