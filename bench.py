@@ -45,6 +45,12 @@ def parse():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--mode", default="mixed", choices=["fp64", "exact", "mixed"])
+    p.add_argument("--no-surrogate", action="store_true",
+                   help="mixed mode without the nodal-force surrogate")
+    p.add_argument("--sur-tol", type=float, default=1e-4,
+                   help="ensemble-spread tolerance (fraction of the rms nodal force)")
+    p.add_argument("--sur-samples", type=int, default=262144)
+    p.add_argument("--sur-epochs", type=int, default=10)
     p.add_argument("--drift-steps", type=int, default=1000,
                    help="NVE steps of the energy-drift run after the timed region (0: skip)")
     p.add_argument("--size", default="full", choices=["full", "medium", "small"],
@@ -221,6 +227,34 @@ def run_ours(a, ws, rank, local):
     if m.nelements:
         s.neighbor_ebuild()
         s.neighbor_nbuild()
+    # the surrogate: samples from the plain FP64 quadrature on strained,
+    # thermally perturbed periodic element boxes, trained on the GPU, attached
+    # to the elements farther than 2 r_c from the atoms
+    sur, net = None, None
+    use_sur = a.mode == "mixed" and not a.no_surrogate and m.nelements > 0
+    if use_sur:
+        from cac_code_gb300 import surrogate as S
+        t0 = time.perf_counter()
+        xs, ts, info = S.generate(eam, a.sur_samples, seed=11, planes=8, ny=8, nz=8,
+                                  snapshots=4, device=local)
+        xv, tv, _ = S.generate(eam, 16384, seed=12, planes=8, ny=8, nz=8, snapshots=4,
+                               device=local)
+        t_gen = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        net, loss = S.train(xs, ts, members=4, epochs=a.sur_epochs, batch=2048, lr=2e-3,
+                            device=local)
+        t_train = time.perf_counter() - t0
+        pm, psp = net.predict(xv)
+        fs = net.normalization()[4]
+        sur = {"tol": a.sur_tol, "distance_A": 11.0, "members": 4,
+               "network": "32-256-256-256-24 SiLU, bf16 tensor cores, fp32 accumulation",
+               "samples": info, "generate_s": round(t_gen, 2), "train_s": round(t_train, 2),
+               "epochs": a.sur_epochs, "train_loss_normalised": loss,
+               "heldout_force_error": S.force_errors(pm, tv),
+               "heldout_spread_median_rel": float(np.median(psp) / fs),
+               "heldout_fraction_within_tol": float(np.mean(psp <= a.sur_tol * fs))}
+        s.surrogate_reference(m.nodex)
+        s.surrogate_attach(net, tol=a.sur_tol, dist=11.0)
     c0 = s.counts()
     s.run(max(a.warmup, 3))
     s.set_timing(True)
@@ -237,6 +271,12 @@ def run_ours(a, ws, rank, local):
     tm = s.timing()
     c1 = s.counts()
     launches = c1["launches"] - l0
+    if sur is not None:
+        ev = c1["surrogate_evaluated"] - c0["surrogate_evaluated"]
+        ac = c1["surrogate_accepted"] - c0["surrogate_accepted"]
+        sur["far_elements"] = c1["surrogate_elements"]
+        sur["elements"] = c1["enlocal"]
+        sur["accepted_fraction_timed"] = ac / ev if ev else 0.0
     dev_ms = float(tm[0])
     ms_max = allmax(ws, dev_ms)
     value = ws * sites * a.steps / (ms_max * 1e-3)
@@ -279,6 +319,83 @@ def run_ours(a, ws, rank, local):
             traffic = None
     fp64_peak = s.fp64_peak()
 
+    # every later measurement starts from the state right after the timed
+    # region (the synthetic configuration is far from equilibrium: left to run,
+    # it changes the neighbor counts the timings depend on)
+    st_a = s.atoms()
+    st_e = s.elements()
+    st = (st_a["x"].copy(), st_a["v"].copy(), st_e["nodex"].copy(), st_e["nodev"].copy())
+
+    def restore():
+        s.put_atoms(st[0], st[1])
+        s.put_nodes(st[2], st[3])
+        s.neighbor_build()
+        if m.nelements:
+            s.neighbor_ebuild()
+            s.neighbor_nbuild()
+
+    # the other precision modes on the same system: timing, and every mode's
+    # force difference from the bit-exact FP64 forces of one configuration
+    modes = {}
+    force_error = None
+    if not a.no_modes and ws == 1:
+        def forces():
+            s.pair_compute()
+            s.pair_ecompute()
+            return s.atoms()["f"].copy(), s.elements()["nodef"].copy()
+
+        def rel_err(fa, fb):
+            out = {}
+            for key, (x, y) in {"atoms": (fa[0], fb[0]), "nodes": (fa[1], fb[1])}.items():
+                x = x.reshape(-1, 3)
+                y = y.reshape(-1, 3)
+                if y.size:
+                    d = np.linalg.norm(x - y, axis=1)
+                    n_ = np.linalg.norm(y, axis=1)
+                    out[key] = {"rms_rel": float(np.sqrt((d ** 2).mean() / (n_ ** 2).mean())),
+                                "max_rel": float(d.max() / n_.max())}
+            return out
+        # (name, precision, surrogate tolerance or None)
+        variants = [("exact", cacg.FP64_EXACT, None), ("fp64", cacg.FP64, None),
+                    ("mixed", cacg.MIXED, None)]
+        head = a.mode
+        if use_sur:
+            head = "mixed+surrogate"
+            variants += [(head, cacg.MIXED, a.sur_tol),
+                         ("mixed+surrogate(tol=1e-2)", cacg.MIXED, 1e-2)]
+
+        def setv(mcode, tol):
+            s.set_precision(mcode)
+            if use_sur:
+                s.surrogate_attach(net if tol is not None else None, tol=tol or 0.0, dist=11.0)
+        fs = {}
+        restore()
+        for name, mcode, tol in variants:
+            setv(mcode, tol)
+            fs[name] = forces()
+        errs = {name: rel_err(fs[name], fs["exact"]) for name, _, _ in variants}
+        force_error = {"vs": "bit-exact FP64 forces at the same configuration", **errs[head]}
+        for name, mcode, tol in variants:
+            if name == head:
+                continue
+            setv(mcode, tol)
+            restore()
+            s.set_timing(True)
+            cs0 = s.counts()
+            s.run(2)
+            s.run(a.steps)
+            tmm = s.timing()
+            cs1 = s.counts()
+            modes[name] = {"value": sites * a.steps / (tmm[0] * 1e-3),
+                           "ms_per_step": tmm[0] / a.steps,
+                           "phase_ms_per_step": [round(v / a.steps, 4) for v in tmm[1:6]],
+                           "force_err_vs_exact": errs[name]}
+            if tol is not None:
+                ev = cs1["surrogate_evaluated"] - cs0["surrogate_evaluated"]
+                modes[name]["accepted_fraction"] = (
+                    (cs1["surrogate_accepted"] - cs0["surrogate_accepted"]) / ev if ev else 0.0)
+        setv(mode, a.sur_tol if use_sur else None)
+
     # e2e through the C ABI with host-resident state: push x,v (atoms + nodes)
     # from pinned host memory, one step, read x,v,f back, every step
     e2e = None
@@ -296,6 +413,7 @@ def run_ours(a, ws, rank, local):
                 import torch
                 return torch.empty(shape, dtype=torch.float64).pin_memory().numpy()
             return np.empty(shape, dtype=np.float64)
+        restore()
         hx, hv, hf = host((n, 3)), host((n, 3)), host((n, 3))
         hnx, hnv = host((ne, 8, 3)), host((ne, 8, 3))
         s.get_state_into(hx, hv, hf)
@@ -324,6 +442,7 @@ def run_ours(a, ws, rank, local):
     drift = None
     if a.drift_steps > 0:
         s.set_timing(False)
+        restore()
         t_a = s.thermo()
         s.run(a.drift_steps)
         t_b = s.thermo()
@@ -331,48 +450,6 @@ def run_ours(a, ws, rank, local):
                  "e_start_ev": t_a["etotal"], "e_end_ev": t_b["etotal"],
                  "ev_per_site": (t_b["etotal"] - t_a["etotal"]) / sites,
                  "ke_start_ev": t_a["ke_atoms"] + t_a["ke_nodes"]}
-
-    # the other precision modes on the same system: timing, and every mode's
-    # force difference from the bit-exact FP64 forces of one configuration
-    modes = {}
-    force_error = None
-    if not a.no_modes and ws == 1:
-        def forces():
-            s.pair_compute()
-            s.pair_ecompute()
-            return s.atoms()["f"].copy(), s.elements()["nodef"].copy()
-
-        def rel_err(fa, fb):
-            out = {}
-            for key, (x, y) in {"atoms": (fa[0], fb[0]), "nodes": (fa[1], fb[1])}.items():
-                x = x.reshape(-1, 3)
-                y = y.reshape(-1, 3)
-                if y.size:
-                    d = np.linalg.norm(x - y, axis=1)
-                    n_ = np.linalg.norm(y, axis=1)
-                    out[key] = {"rms_rel": float(np.sqrt((d ** 2).mean() / (n_ ** 2).mean())),
-                                "max_rel": float(d.max() / n_.max())}
-            return out
-        codes = {"exact": cacg.FP64_EXACT, "fp64": cacg.FP64, "mixed": cacg.MIXED}
-        fs = {}
-        for name, mcode in codes.items():
-            s.set_precision(mcode)
-            fs[name] = forces()
-        errs = {name: rel_err(fs[name], fs["exact"]) for name in codes}
-        force_error = {"vs": "bit-exact FP64 forces at the same configuration", **errs[a.mode]}
-        for name, mcode in codes.items():
-            if name == a.mode:
-                continue
-            s.set_precision(mcode)
-            s.set_timing(True)
-            s.run(2)
-            s.run(a.steps)
-            tmm = s.timing()
-            modes[name] = {"value": sites * a.steps / (tmm[0] * 1e-3),
-                           "ms_per_step": tmm[0] / a.steps,
-                           "phase_ms_per_step": [round(v / a.steps, 4) for v in tmm[1:6]],
-                           "force_err_vs_exact": errs[name]}
-        s.set_precision(mode)
 
     if rank == 0:
         line = {
@@ -385,7 +462,8 @@ def run_ours(a, ws, rank, local):
                              "medium": "C2 medium: EAM Cu 360,000 atoms + 7,200 elements",
                              "full": "C2: EAM Cu CAC slab, 1,000,000 atoms + 20,000 elements "
                                      "(11 sites/edge, 8 Gauss points each)"}[a.size],
-                "mode": a.mode, "atoms": c0["nlocal"], "ghost_atoms": c0["nghost"],
+                "mode": a.mode + ("+surrogate" if use_sur else ""),
+                "atoms": c0["nlocal"], "ghost_atoms": c0["nghost"],
                 "elements": c0["enlocal"], "ghost_elements": c0["enghost"],
                 "gauss_points": cfg["gauss_per_element"] * c0["enlocal"],
                 "integration_rows": c0["ip_rows"], "sites": sites,
@@ -413,11 +491,14 @@ def run_ours(a, ws, rank, local):
             "other_modes": modes,
             "energy_drift": drift,
             "force_error": force_error,
+            "surrogate": sur,
         }
         if "fp64" in modes:
             line["speedup_vs_plain_fp64"] = value / modes["fp64"]["value"]
         print(json.dumps(line), flush=True)
     s.close()
+    if net is not None:
+        net.close()
 
 
 def run_reference(a, ws, rank):
