@@ -80,6 +80,13 @@ def barrier(ws):
         dist.barrier()
 
 
+def aggregate(ws, sites_per_rank, steps, ms_local):
+    """Whole-job site-steps/s of independent replicas: every rank's sites over
+    the slowest rank's device time (ranks exchange only this scalar)."""
+    ms_max = allmax(ws, ms_local)
+    return ws * sites_per_rank * steps / (ms_max * 1e-3), ms_max
+
+
 def allmax(ws, v):
     if ws <= 1:
         return v
@@ -278,8 +285,7 @@ def run_ours(a, ws, rank, local):
         sur["elements"] = c1["enlocal"]
         sur["accepted_fraction_timed"] = ac / ev if ev else 0.0
     dev_ms = float(tm[0])
-    ms_max = allmax(ws, dev_ms)
-    value = ws * sites * a.steps / (ms_max * 1e-3)
+    value, ms_max = aggregate(ws, sites, a.steps, dev_ms)
 
     # dominant kernel, one launch per step: the FP64 modes' EAM force pass
     # over the atom list (phase 3); the mixed mode's EAM density pass (phase 2),
