@@ -38,6 +38,7 @@ UNITS = [
     ("k_gemm.cu", ["-fmad=true"]),
     ("mlp.cu", ["-fmad=true"]),
     ("k_surrogate.cu", ["-fmad=true"]),
+    ("k_analysis.cu", ["-fmad=false"]),
 ]
 
 

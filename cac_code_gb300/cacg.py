@@ -50,7 +50,8 @@ EXPORTED = [
     "cacg_mlp_get_params", "cacg_mlp_set_params", "cacg_mlp_set_normalization",
     "cacg_mlp_get_normalization", "cacg_mlp_loss_grad", "cacg_mlp_train", "cacg_mlp_predict",
     "cacg_gemm_bf16_tn", "cacg_surrogate_reference", "cacg_surrogate_samples",
-    "cacg_surrogate_attach",
+    "cacg_surrogate_attach", "cacg_compute_centro", "cacg_dump_xyz", "cacg_dump_elements",
+    "cacg_fix_post_force",
 ]
 
 
@@ -79,6 +80,7 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
     lib.cacg_version.restype = ctypes.c_char_p
     lib.cacg_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int]
     for name in ("cacg_destroy", "cacg_init", "cacg_setup", "cacg_neighbor_build",
+                 "cacg_fix_post_force",
                  "cacg_neighbor_ebuild", "cacg_neighbor_nbuild", "cacg_pair_ecompute",
                  "cacg_fix_nve_initial_integrate", "cacg_fix_nve_final_integrate"):
         getattr(lib, name).argtypes = [ctypes.c_void_p]
@@ -110,6 +112,9 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
     lib.cacg_surrogate_reference.argtypes = [vp, _dp]
     lib.cacg_surrogate_samples.argtypes = [vp, _fp, _fp, i]
     lib.cacg_surrogate_attach.argtypes = [vp, vp, d, d]
+    lib.cacg_compute_centro.argtypes = [vp, _dp, i]
+    lib.cacg_dump_xyz.argtypes = [vp, ctypes.c_char_p]
+    lib.cacg_dump_elements.argtypes = [vp, ctypes.c_char_p, i]
     _LIB = lib
     return lib
 
@@ -385,6 +390,22 @@ class System:
         return {"pe_atoms": out[0], "pe_elements": out[1], "ke_atoms": out[2],
                 "ke_nodes": out[3], "virial": out[4:10].copy(), "kinetic_tensor": out[10:16].copy(),
                 "volume": out[16], "etotal": out[0] + out[1] + out[2] + out[3]}
+
+    def fix_post_force(self):
+        self._ok(self._L.cacg_fix_post_force(self.h))
+
+    def centro(self) -> np.ndarray:
+        """Centro-symmetry of the local atoms (Output::centro_atom)."""
+        n = self.counts()["nlocal"]
+        out = np.zeros(n)
+        self._ok(self._L.cacg_compute_centro(self.h, _d(out), n))
+        return out
+
+    def dump_xyz(self, path: str):
+        self._ok(self._L.cacg_dump_xyz(self.h, path.encode()))
+
+    def dump_elements(self, path: str, append: bool = False):
+        self._ok(self._L.cacg_dump_elements(self.h, path.encode(), 1 if append else 0))
 
     def surrogate_reference(self, nodex0=None):
         a = None if nodex0 is None else np.ascontiguousarray(nodex0, dtype=np.float64)

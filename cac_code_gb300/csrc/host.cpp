@@ -202,6 +202,34 @@ struct cacg_context {
   DBuf<float> d_u, d_shape_f, d_ljf, d_site_rho;
   DBuf<double> d_cutsq64, d_stage, d_part, d_lj5;
   std::vector<double> h_lj5;
+  // regions, groups and post-force fixes (region_block.cpp, region_sphere.cpp,
+  // group.cpp, fix_setforce.cpp, fix_viscous.cpp)
+  struct Region {
+    std::string id;
+    int sphere = 0, interior = 1;
+    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0}, c[3] = {0, 0, 0}, r = 0;
+    bool match(double x, double y, double z) const {
+      int in;
+      if (sphere) {
+        double dx = x - c[0], dy = y - c[1], dz = z - c[2];
+        in = std::sqrt(dx * dx + dy * dy + dz * dz) <= r;
+      } else {
+        in = x >= lo[0] && x <= hi[0] && y >= lo[1] && y <= hi[1] && z >= lo[2] && z <= hi[2];
+      }
+      return !(in ^ interior);  // Region::match, region.cpp:96-99
+    }
+  };
+  struct PostFix {
+    int viscous = 0, bit = 1;
+    int set[3] = {0, 0, 0};
+    double val[3] = {0, 0, 0}, gamma = 0;
+  };
+  std::vector<Region> regions;
+  std::vector<std::string> groups{"all"};
+  std::vector<int> h_amask, h_emask;  // group bits of the local atoms / elements
+  std::vector<PostFix> post_fixes;
+  DBuf<int> d_amask, d_emask;
+  bool masks_dirty = true;
   // nodal-force surrogate (elements far from the atoms)
   cacg_mlp_t *sur = nullptr;
   double sur_tol = 1e-4, sur_dist = 0.0;
@@ -350,6 +378,14 @@ struct cacg_context {
   void nve_initial();
   void nve_final();
   void compute_thermo(double *out);
+  void compute_centro(double *out);
+  void region_cmd(const std::vector<std::string> &a);
+  void group_cmd(const std::vector<std::string> &a);
+  void fix_cmd(const std::vector<std::string> &a);
+  int group_bit(const std::string &name) const;
+  void post_force();
+  void dump_xyz(const char *path);
+  void dump_elements(const char *path, int append);
   void surrogate_reference(const double *nodex0);
   void surrogate_samples(float *x, float *t);
   void surrogate_attach(cacg_mlp_t *m, double tol, double dist);
@@ -384,6 +420,8 @@ cacg_context::~cacg_context() {
   d_part.release();
   d_lj5.release();
   d_nodex0.release();
+  d_amask.release();
+  d_emask.release();
   d_far.release();
   d_far_rows.release();
   d_static_rows.release();
@@ -554,18 +592,199 @@ void cacg_context::command(const std::string &raw) {
     }
     inited = false;
   } else if (c == "fix") {
-    if (a.size() < 3) fail(CACG_EINVAL, "Illegal fix command");
-    if (a[2] != "nve") fail(CACG_EINVAL, "Only fix nve is on this path");
-    if (a[1] != "all") fail(CACG_EINVAL, "fix nve applies to group all here");
-    fix_nve = true;
+    fix_cmd(a);
+  } else if (c == "region") {
+    region_cmd(a);
+  } else if (c == "group") {
+    group_cmd(a);
   } else if (c == "run") {
     if (a.size() < 1) fail(CACG_EINVAL, "Illegal run command");
     run(inumeric(a[0]));
-  } else if (c == "thermo" || c == "thermo_style" || c == "dump" || c == "velocity" ||
-             c == "region" || c == "group") {
+  } else if (c == "thermo" || c == "thermo_style" || c == "dump" || c == "velocity") {
     // output and setup commands outside this path are accepted and ignored
   } else {
     fail(CACG_EINVAL, "Unknown command: %s", raw.c_str());
+  }
+}
+
+// ------------------------------------------------------------------ regions, groups, fixes
+
+// region ID block xlo xhi ylo yhi zlo zhi [side in|out] [units box|lattice]
+// (region_block.cpp:15-67, INF = +-1e20, EDGE = the box face);
+// region ID sphere xc yc zc r (region_sphere.cpp:15-32)
+void cacg_context::region_cmd(const std::vector<std::string> &a) {
+  if (a.size() < 2) fail(CACG_EINVAL, "Illegal region command");
+  Region r;
+  r.id = a[0];
+  size_t iarg;
+  if (a[1] == "block") {
+    if (a.size() < 8) fail(CACG_EINVAL, "Illegal region block command");
+    for (int d = 0; d < 3; d++) {
+      for (int side = 0; side < 2; side++) {
+        const std::string &v = a[2 + 2 * d + side];
+        double &dst = side ? r.hi[d] : r.lo[d];
+        if (v == "INF" || v == "EDGE") {
+          if (!box_set) fail(CACG_EINVAL, "Cannot use region INF or EDGE when box does not exist");
+          if (v == "INF") dst = side ? 1.0e20 : -1.0e20;
+          else dst = side ? hi[d] : lo[d];
+        } else {
+          dst = numeric(v);
+        }
+      }
+    }
+    if (r.lo[0] > r.hi[0] || r.lo[1] > r.hi[1] || r.lo[2] > r.hi[2])
+      fail(CACG_EINVAL, "Illegal region block command");
+    iarg = 8;
+  } else if (a[1] == "sphere") {
+    if (a.size() < 6) fail(CACG_EINVAL, "Illegal region sphere command");
+    r.sphere = 1;
+    for (int d = 0; d < 3; d++) r.c[d] = numeric(a[2 + d]);
+    r.r = numeric(a[5]);
+    if (r.r < 0.0) fail(CACG_EINVAL, "Illegal region sphere command");
+    iarg = 6;
+  } else {
+    fail(CACG_EINVAL, "Unknown region style %s", a[1].c_str());
+  }
+  for (; iarg < a.size(); iarg += 2) {  // Region::options, region.cpp:55-84
+    if (iarg + 1 >= a.size()) fail(CACG_EINVAL, "Illegal region command");
+    if (a[iarg] == "units") {
+      if (a[iarg + 1] != "box" && a[iarg + 1] != "lattice") fail(CACG_EINVAL, "Illegal region command");
+    } else if (a[iarg] == "side") {
+      if (a[iarg + 1] == "in") r.interior = 1;
+      else if (a[iarg + 1] == "out") r.interior = 0;
+      else fail(CACG_EINVAL, "Illegal region command");
+    } else {
+      fail(CACG_EINVAL, "Illegal region command");
+    }
+  }
+  for (auto &q : regions)
+    if (q.id == r.id) fail(CACG_EINVAL, "Reuse of region ID");
+  regions.push_back(r);
+}
+
+int cacg_context::group_bit(const std::string &name) const {
+  for (size_t g = 0; g < groups.size(); g++)
+    if (groups[g] == name) return 1 << g;
+  return 0;
+}
+
+// group ID region RID | subtract G1 G2 ... | union G1 ... (group.cpp:80-200):
+// atoms by position, elements by centre, at the time of the command
+void cacg_context::group_cmd(const std::vector<std::string> &a) {
+  if (a.size() < 2) fail(CACG_EINVAL, "Illegal group command");
+  int bit = group_bit(a[0]);
+  if (!bit) {
+    if (groups.size() == 32) fail(CACG_EINVAL, "Too many groups");
+    groups.push_back(a[0]);
+    bit = 1 << (groups.size() - 1);
+  }
+  // current positions: the device copy once it exists
+  std::vector<double> ax(h_x), ex(h_ex);
+  if (inited) {
+    std::vector<double4> x4(std::max(nlocal, 1));
+    if (nlocal)
+      check(cudaMemcpyAsync(x4.data(), d_x.p, sizeof(double4) * nlocal, cudaMemcpyDeviceToHost, stream), "x");
+    ex.assign((size_t) 3 * enlocal, 0.0);
+    if (enlocal)
+      check(cudaMemcpyAsync(ex.data(), d_ex.p, sizeof(double) * 3 * enlocal, cudaMemcpyDeviceToHost, stream), "ex");
+    sync();
+    ax.assign((size_t) 3 * nlocal, 0.0);
+    for (int i = 0; i < nlocal; i++) {
+      ax[3 * i] = x4[i].x;
+      ax[3 * i + 1] = x4[i].y;
+      ax[3 * i + 2] = x4[i].z;
+    }
+  }
+  const int na = (int) (ax.size() / 3), ne = (int) (ex.size() / 3);
+  h_amask.resize(na, 1);
+  h_emask.resize(ne, 1);
+  if (a[1] == "region") {
+    if (a.size() != 3) fail(CACG_EINVAL, "Illegal group command");
+    const Region *r = nullptr;
+    for (auto &q : regions)
+      if (q.id == a[2]) r = &q;
+    if (!r) fail(CACG_EINVAL, "Group region ID does not exist");
+    for (int i = 0; i < na; i++)
+      if (r->match(ax[3 * i], ax[3 * i + 1], ax[3 * i + 2])) h_amask[i] |= bit;
+    for (int i = 0; i < ne; i++)
+      if (r->match(ex[3 * i], ex[3 * i + 1], ex[3 * i + 2])) h_emask[i] |= bit;
+  } else if (a[1] == "subtract" || a[1] == "union") {
+    if (a.size() < (a[1] == "subtract" ? 4u : 3u)) fail(CACG_EINVAL, "Illegal group command");
+    std::vector<int> bits;
+    for (size_t k = 2; k < a.size(); k++) {
+      int b = group_bit(a[k]);
+      if (!b) fail(CACG_EINVAL, "Group ID does not exist");
+      bits.push_back(b);
+    }
+    for (std::vector<int> *mk : {&h_amask, &h_emask}) {
+      for (int &m : *mk) {
+        if (a[1] == "union") {
+          for (int b : bits)
+            if (m & b) m |= bit;
+        } else {
+          if (m & bits[0]) m |= bit;
+          for (size_t k = 1; k < bits.size(); k++)
+            if (m & bits[k]) m &= ~bit;
+        }
+      }
+    }
+  } else {
+    fail(CACG_EINVAL, "Illegal group command");
+  }
+  masks_dirty = true;
+}
+
+// fix ID group nve | setforce fx fy fz (NULL keeps a component) | viscous gamma
+void cacg_context::fix_cmd(const std::vector<std::string> &a) {
+  if (a.size() < 3) fail(CACG_EINVAL, "Illegal fix command");
+  const int bit = group_bit(a[1]);
+  if (!bit) fail(CACG_EINVAL, "Could not find fix group ID");
+  if (a[2] == "nve") {
+    if (a[1] != "all") fail(CACG_EINVAL, "fix nve applies to group all here");
+    fix_nve = true;
+  } else if (a[2] == "setforce") {  // fix_setforce.cpp:18-60
+    if (a.size() < 6) fail(CACG_EINVAL, "Illegal fix setforce command");
+    PostFix f;
+    f.bit = bit;
+    for (int d = 0; d < 3; d++)
+      if (a[3 + d] != "NULL") {
+        f.set[d] = 1;
+        f.val[d] = numeric(a[3 + d]);
+      }
+    post_fixes.push_back(f);
+  } else if (a[2] == "viscous") {  // fix_viscous.cpp:14-30
+    if (a.size() < 4) fail(CACG_EINVAL, "Illegal fix viscous command");
+    PostFix f;
+    f.viscous = 1;
+    f.bit = bit;
+    f.gamma = numeric(a[3]);
+    post_fixes.push_back(f);
+  } else {
+    fail(CACG_EINVAL, "Fix style %s is not on this path", a[2].c_str());
+  }
+}
+
+// Modify::post_force (modify.cpp:663-669): each fix in order, atoms then nodes
+void cacg_context::post_force() {
+  if (post_fixes.empty()) return;
+  cudaStream_t s = stream;
+  if (masks_dirty) {
+    std::vector<int> am(h_amask), em(h_emask);
+    am.resize(std::max(nlocal, 1), 1);
+    em.resize(std::max(enlocal, 1), 1);
+    upload(d_amask, am, s);
+    upload(d_emask, em, s);
+    masks_dirty = false;
+  }
+  for (const PostFix &f : post_fixes) {
+    if (f.viscous) {
+      if (nlocal) launch_viscous(d_f.p, d_v.p, d_amask.p, nlocal, 1, f.bit, f.gamma, s);
+      if (enlocal) launch_viscous(d_nodef.p, d_nodev.p, d_emask.p, enlocal, NPE, f.bit, f.gamma, s);
+    } else {
+      if (nlocal) launch_setforce(d_f.p, d_amask.p, nlocal, 1, f.bit, f.set, f.val, s);
+      if (enlocal) launch_setforce(d_nodef.p, d_emask.p, enlocal, NPE, f.bit, f.set, f.val, s);
+    }
+    launches += (nlocal > 0) + (enlocal > 0);
   }
 }
 
@@ -633,7 +852,11 @@ void cacg_context::read_data(const std::string &path) {
   ntypes = nat;
   netypes = net;
   h_x.clear(); h_v.clear(); h_type.clear(); h_tag.clear();
+  h_amask.clear();
+  masks_dirty = true;
   h_ex.clear(); h_nodex.clear(); h_nodev.clear(); h_etype.clear(); h_etag.clear();
+  h_emask.clear();
+  masks_dirty = true;
   std::vector<int> eid_to_index;
   auto next_lines = [&](long long n, std::vector<std::string> &out) {
     out.clear();
@@ -1776,6 +1999,85 @@ void cacg_context::pair_ecompute_mixed() {
   }
 }
 
+// ------------------------------------------------------------------ analysis and output
+
+// Output::centro_atom (output.cpp:352-447) over the atom list, in chunks of
+// atoms so that the per-atom neighbor scratch stays bounded
+void cacg_context::compute_centro(double *out) {
+  if (!list_built) fail(CACG_ESTATE, "centro-symmetry before the atom neighbor list is built");
+  cudaStream_t s = stream;
+  DBuf<double> d_out, d_dsq;
+  DBuf<int> d_near;
+  const int chunk = std::max(1, std::min(nlocal, 65536));
+  d_out.ensure(std::max(nlocal, 1), s);
+  d_dsq.ensure((size_t) std::max(maxneigh, 1) * chunk, s);
+  d_near.ensure((size_t) std::max(maxneigh, 1) * chunk, s);
+  for (int i0 = 0; i0 < nlocal; i0 += chunk)
+    analysis::centro(d_x.p, d_num.p, d_list.p, stride, i0, std::min(chunk, nlocal - i0),
+                     cutneighmaxsq, d_dsq.p, d_near.p, chunk, d_out.p, s);
+  launches += (nlocal + chunk - 1) / chunk;
+  if (nlocal)
+    check(cudaMemcpyAsync(out, d_out.p, sizeof(double) * nlocal, cudaMemcpyDeviceToHost, s), "centro");
+  sync();
+  d_out.release();
+  d_dsq.release();
+  d_near.release();
+}
+
+// DumpXyz (dump_xyz.cpp:36-140 with Dump::count, dump.cpp:352-365): the atoms
+// with 1 < centro < 10, header "N\nXYZ\n", lines "Cu x y z centro" (%g)
+void cacg_context::dump_xyz(const char *path) {
+  std::vector<double> c(std::max(nlocal, 1));
+  compute_centro(c.data());
+  std::vector<double4> x4(std::max(nlocal, 1));
+  if (nlocal)
+    check(cudaMemcpyAsync(x4.data(), d_x.p, sizeof(double4) * nlocal, cudaMemcpyDeviceToHost, stream), "x");
+  sync();
+  FILE *fp = fopen(path, "w");
+  if (!fp) fail(CACG_EIO, "Cannot open dump file %s", path);
+  long long nd = 0;
+  for (int i = 0; i < nlocal; i++) nd += c[i] > 1 && c[i] < 10;
+  fprintf(fp, "%lld\nXYZ\n", nd);
+  for (int i = 0; i < nlocal; i++)
+    if (c[i] > 1 && c[i] < 10) fprintf(fp, "Cu %g %g %g %g\n", x4[i].x, x4[i].y, x4[i].z, c[i]);
+  fclose(fp);
+}
+
+// DumpElement (dump_element.cpp:69-128): a Tecplot FE-brick zone of the local
+// elements' nodes, one "x y z vx vy vz fx fy fz" (%g) line per node in
+// element order, then each element's 8 node numbers (1-based, consecutive:
+// the reference writes connectivity one element after another).  n counts
+// the nodes written (the reference's header takes the atom count of its
+// centro filter, dump.cpp:247, which does not describe the element zone).
+void cacg_context::dump_elements(const char *path, int append) {
+  if (!inited) fail(CACG_ESTATE, "no device state yet (cacg_init)");
+  const int n = enlocal;
+  std::vector<double> nx((size_t) 24 * n + 1), nv((size_t) 24 * n + 1), nf((size_t) 24 * n + 1);
+  if (n) {
+    check(cudaMemcpyAsync(nx.data(), d_nodex.p, sizeof(double) * 24 * n, cudaMemcpyDeviceToHost, stream), "nodex");
+    check(cudaMemcpyAsync(nv.data(), d_nodev.p, sizeof(double) * 24 * n, cudaMemcpyDeviceToHost, stream), "nodev");
+    check(cudaMemcpyAsync(nf.data(), d_nodef.p, sizeof(double) * 24 * n, cudaMemcpyDeviceToHost, stream), "nodef");
+  }
+  sync();
+  FILE *fp = fopen(path, append ? "a" : "w");
+  if (!fp) fail(CACG_EIO, "Cannot open dump file %s", path);
+  const long long nn = (long long) NPE * n;
+  fprintf(fp, "title=\"results for cac\"\n");
+  fprintf(fp, "variables=\"x\", \"y\", \"z\", \"vx\", \"vy\", \"vz\", \"fx\", \"fy\", \"fz\"\n");
+  fprintf(fp, "zone t=\"load step %lld\",", ntimestep);
+  fprintf(fp, " n=  %lld e =  %d", nn, n);
+  fprintf(fp, " datapacking=point, zonetype=febrick\n");
+  for (long long k = 0; k < nn; k++)
+    fprintf(fp, "%g %g %g %g %g %g %g %g %g\n", nx[3 * k], nx[3 * k + 1], nx[3 * k + 2], nv[3 * k],
+            nv[3 * k + 1], nv[3 * k + 2], nf[3 * k], nf[3 * k + 1], nf[3 * k + 2]);
+  for (int e = 0; e < n; e++) {
+    long long b = (long long) NPE * e;
+    fprintf(fp, "%lld %lld %lld %lld %lld %lld %lld %lld\n", b + 1, b + 2, b + 3, b + 4, b + 5,
+            b + 6, b + 7, b + 8);
+  }
+  fclose(fp);
+}
+
 // ------------------------------------------------------------------ surrogate
 
 void cacg_context::surrogate_reference(const double *nodex0) {
@@ -2171,6 +2473,7 @@ void cacg_context::run(int n) {
     pair_compute_pass(2);
     mark(b + 3);
     pair_ecompute();
+    post_force();  // verlet.cpp:206
     mark(b + 4);
     nve_final();
     mark(b + 5);
@@ -2580,6 +2883,35 @@ int cacg_compute_thermo(cacg_handle h, double *out, int n) {
   double v[17];
   h->compute_thermo(v);
   for (int i = 0; i < n && i < 17; i++) out[i] = v[i];
+  API_END
+}
+
+int cacg_fix_post_force(cacg_handle h) {
+  API_BEGIN
+  if (!h->inited) fail(CACG_ESTATE, "no device state yet (cacg_init)");
+  h->post_force();
+  API_END
+}
+
+int cacg_compute_centro(cacg_handle h, double *centro, int n) {
+  API_BEGIN
+  if (!centro) fail(CACG_EINVAL, "null output array");
+  if (n != h->nlocal) fail(CACG_EINVAL, "n must equal the number of local atoms (%d)", h->nlocal);
+  h->compute_centro(centro);
+  API_END
+}
+
+int cacg_dump_xyz(cacg_handle h, const char *path) {
+  API_BEGIN
+  if (!path) fail(CACG_EINVAL, "null path");
+  h->dump_xyz(path);
+  API_END
+}
+
+int cacg_dump_elements(cacg_handle h, const char *path, int append) {
+  API_BEGIN
+  if (!path) fail(CACG_EINVAL, "null path");
+  h->dump_elements(path, append);
   API_END
 }
 

@@ -297,6 +297,14 @@ void kinetic(const double *v, const int *type, const double *mass, int n, int pe
              double scale, double *part, cudaStream_t s);
 }  // namespace thermo
 
+// ---- analysis (k_analysis.cu, -fmad=false) ----
+namespace analysis {
+// centro-symmetry of atoms i0 .. i0+n-1; scratch dsq/near hold maxn x chunk
+// entries (column-major, chunk >= n)
+void centro(const double4 *x, const int *num, const int *list, int stride, int i0, int n,
+            double cutsq, double *dsq, int *near, int chunk, double *out, cudaStream_t s);
+}  // namespace analysis
+
 // ---- tensor-core GEMM (k_gemm.cu) and the surrogate MLP (mlp.cu) ----
 namespace gemm {
 // C = A B^T, bf16 operands (K-major), fp32 accumulation; kind: 0 store C,
@@ -342,6 +350,12 @@ void launch_nve_atoms_final(double *v, const double *f, const int *type, const d
 void launch_nve_nodes_initial(double *ex, double *nodex, double *nodev, const double *nodef,
                               const int *etype, const double *emass, int n, double dtv,
                               double dtf, cudaStream_t s);
+// fix setforce / fix viscous on the items (atoms, or elements x 8 nodes) whose
+// group mask has `bit` (fix_setforce.cpp:107-161, fix_viscous.cpp:73-123)
+void launch_setforce(double *f, const int *mask, int n, int per_item, int bit, const int *set,
+                     const double *val, cudaStream_t s);
+void launch_viscous(double *f, const double *v, const int *mask, int n, int per_item, int bit,
+                    double gamma, cudaStream_t s);
 void launch_nve_nodes_final(double *nodev, const double *nodef, const int *etype,
                             const double *emass, int n, double dtf, cudaStream_t s);
 void launch_check_distance(const double4 *x, const double *xhold, int n,

@@ -233,6 +233,39 @@ void launch_unpack4to3(const double4 *in, double *out, int n, cudaStream_t s) {
   check(cudaGetLastError(), "unpack4to3");
 }
 
+namespace {
+__global__ void k_setforce(double *__restrict__ f, const int *__restrict__ mask, int n, int per,
+                           int bit, int sx, int sy, int sz, double vx, double vy, double vz) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n * per || !(mask[i / per] & bit)) return;
+  if (sx) f[3 * (size_t) i] = vx;
+  if (sy) f[3 * (size_t) i + 1] = vy;
+  if (sz) f[3 * (size_t) i + 2] = vz;
+}
+
+__global__ void k_viscous(double *__restrict__ f, const double *__restrict__ v,
+                          const int *__restrict__ mask, int n, int per, int bit, double drag) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n * per || !(mask[i / per] & bit)) return;
+  for (int d = 0; d < 3; d++) f[3 * (size_t) i + d] -= drag * v[3 * (size_t) i + d];
+}
+}  // namespace
+
+void launch_setforce(double *f, const int *mask, int n, int per_item, int bit, const int *set,
+                     const double *val, cudaStream_t s) {
+  if (n <= 0) return;
+  k_setforce<<<nblk((long long) n * per_item, 256), 256, 0, s>>>(f, mask, n, per_item, bit, set[0], set[1],
+                                                              set[2], val[0], val[1], val[2]);
+  check(cudaGetLastError(), "setforce");
+}
+
+void launch_viscous(double *f, const double *v, const int *mask, int n, int per_item, int bit,
+                    double gamma, cudaStream_t s) {
+  if (n <= 0) return;
+  k_viscous<<<nblk((long long) n * per_item, 256), 256, 0, s>>>(f, v, mask, n, per_item, bit, gamma);
+  check(cudaGetLastError(), "viscous");
+}
+
 double fp64_fma_rate(cudaStream_t s) {
   int dev = 0;
   check(cudaGetDevice(&dev), "getdevice");

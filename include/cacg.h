@@ -142,6 +142,24 @@ int cacg_compute_thermo(cacg_handle h, double *out, int n);
 int cacg_kinetic_noalloc(const double *v, const int *type, const double *mass, int n,
                          int per_item, double scale, double mvv2e, double *out, void *stream);
 
+/* Modify::post_force (modify.cpp:663-669): the fix setforce / fix viscous
+   commands of the input, in order, on the current forces (cacg_run applies
+   them itself between the force passes and the final integration). */
+int cacg_fix_post_force(cacg_handle h);
+
+/* ---- analysis and output ----
+   Output::centro_atom (output.cpp:352-447): centro-symmetry of the n local
+   atoms (n = local atoms) over the atom neighbor list, bit-identical to the
+   reference; 0 for atoms with fewer than 12 neighbors in range. */
+int cacg_compute_centro(cacg_handle h, double *centro, int n);
+/* DumpXyz (dump_xyz.cpp): "N\nXYZ\n" then "Cu x y z centro" for the atoms
+   with 1 < centro < 10 (the reference's dump after Verlet::setup). */
+int cacg_dump_xyz(cacg_handle h, const char *path);
+/* DumpElement (dump_element.cpp:69-128): a Tecplot FE-brick zone (header,
+   one "x y z vx vy vz fx fy fz" line per node, 8 node numbers per element);
+   append != 0 adds a zone to an existing file. */
+int cacg_dump_elements(cacg_handle h, const char *path, int append);
+
 /* ---- nodal-force surrogate (no counterpart in the reference, which
    evaluates every element by integration-point quadrature) ----
    An ensemble of MLPs 32 -> 256 -> 256 -> 256 -> 24 (SiLU) maps an element's

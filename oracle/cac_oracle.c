@@ -127,6 +127,10 @@ struct orc_sys {
   double dr, drho, rdr, rdrho, cutforcesq, eam_mass;
   double *frho_spline, *rhor_spline, *z2r_spline; /* [(n+1)*7] */
   double *rho, *fp, *erho;
+  /* group masks and post-force fixes (fix_setforce.cpp, fix_viscous.cpp) */
+  int *amask, *emask;
+  int nfix;
+  struct { int viscous, bit, set[3]; double val[3], gamma; } fixes[16];
   /* run state */
   long long ntimestep;
   int ago, nrebuild;
@@ -156,6 +160,8 @@ orc_sys *orc_create(void) {
 
 void orc_destroy(orc_sys *s) {
   if (!s) return;
+  free(s->amask);
+  free(s->emask);
   free(s->x); free(s->v); free(s->f); free(s->type); free(s->tag); free(s->xhold);
   for (int t = 0; t <= MAXTYPES; t++) {
     free(s->intp[t]); free(s->weight[t]); free(s->spa_int[t]);
@@ -1591,6 +1597,106 @@ int orc_thermo(orc_sys *s, double *out) {
   return 0;
 }
 
+/* ---- centro-symmetry, Output::centro_atom (output.cpp:352-447) ----
+   The k smallest of n values land in the first k slots by the partial
+   quickselect of Numerical Recipes (select / select2, output.cpp:458-554):
+   median-of-three pivot at l+1, Hoare partition, narrow to the side holding
+   k.  The same steps are kept so that the same neighbors are chosen among
+   equal distances and the pair sums add in the same order. */
+
+static void nr_select(int k, int n, double *arr, int *iarr) {
+  /* 1-based positions, as the published routine states them */
+#define A(p) arr[(p) - 1]
+#define IA(p) iarr[(p) - 1]
+#define SWAP_AT(p, q)                                          \
+  {                                                            \
+    double t_ = A(p); A(p) = A(q); A(q) = t_;                  \
+    if (iarr) { int u_ = IA(p); IA(p) = IA(q); IA(q) = u_; }   \
+  }
+  int l = 1, ir = n;
+  for (;;) {
+    if (ir <= l + 1) {
+      if (ir == l + 1 && A(ir) < A(l)) SWAP_AT(l, ir);
+      return;
+    }
+    int mid = (l + ir) >> 1;
+    SWAP_AT(mid, l + 1);
+    if (A(l) > A(ir)) SWAP_AT(l, ir);
+    if (A(l + 1) > A(ir)) SWAP_AT(l + 1, ir);
+    if (A(l) > A(l + 1)) SWAP_AT(l, l + 1);
+    int i = l + 1, j = ir;
+    double piv = A(l + 1);
+    int ipiv = iarr ? IA(l + 1) : 0;
+    for (;;) {
+      do i++; while (A(i) < piv);
+      do j--; while (A(j) > piv);
+      if (j < i) break;
+      SWAP_AT(i, j);
+    }
+    A(l + 1) = A(j);
+    A(j) = piv;
+    if (iarr) {
+      IA(l + 1) = IA(j);
+      IA(j) = ipiv;
+    }
+    if (j >= k) ir = j - 1;
+    if (j <= k) l = i;
+  }
+#undef A
+#undef IA
+#undef SWAP_AT
+}
+
+/* centro[i] for the local atoms over the full atom list: the 12 nearest
+   neighbors within the list cutoff, the 66 pair vectors R_j + R_k - 2 R_i,
+   the sum of the 6 smallest |.|^2; 0 with fewer than 12 neighbors */
+int orc_centro(orc_sys *s, double *out) {
+  if (!s->have_list) return fail(s, "atom neighbor list not built");
+  const int nnn = 12, nhalf = nnn / 2, npairs = nnn * (nnn - 1) / 2;
+  double pairs[66];
+  int maxn = 1;
+  for (int i = 0; i < s->nlocal; i++) maxn = s->numneigh[i] > maxn ? s->numneigh[i] : maxn;
+  double *dsq = (double *) malloc(sizeof(double) * maxn);
+  int *near = (int *) malloc(sizeof(int) * maxn);
+  for (int i = 0; i < s->nlocal; i++) {
+    const double *xi = s->x + 3 * i;
+    const int *jl = s->neigh.v + s->firstneigh[i];
+    int n = 0;
+    for (int jj = 0; jj < s->numneigh[i]; jj++) {
+      int j = jl[jj];
+      double dx = xi[0] - s->x[3 * j], dy = xi[1] - s->x[3 * j + 1], dz = xi[2] - s->x[3 * j + 2];
+      double rsq = dx * dx + dy * dy + dz * dz;
+      if (rsq < s->cutneighmaxsq) {
+        dsq[n] = rsq;
+        near[n++] = j;
+      }
+    }
+    if (n < nnn) {
+      out[i] = 0.0;
+      continue;
+    }
+    nr_select(nnn, n, dsq, near);
+    int m = 0;
+    for (int a = 0; a < nnn; a++) {
+      const double *xa = s->x + 3 * near[a];
+      for (int b = a + 1; b < nnn; b++) {
+        const double *xb = s->x + 3 * near[b];
+        double dx = xa[0] + xb[0] - 2.0 * xi[0];
+        double dy = xa[1] + xb[1] - 2.0 * xi[1];
+        double dz = xa[2] + xb[2] - 2.0 * xi[2];
+        pairs[m++] = dx * dx + dy * dy + dz * dz;
+      }
+    }
+    nr_select(nhalf, npairs, pairs, NULL);
+    double v = 0.0;
+    for (int a = 0; a < nhalf; a++) v += pairs[a];
+    out[i] = v;
+  }
+  free(dsq);
+  free(near);
+  return 0;
+}
+
 /* FixNVE, fix_nve.cpp:54-157 */
 static void nve_initial(orc_sys *s) {
   double dtv = s->dt, dtf = 0.5 * s->dt * s->ftm2v;
@@ -1686,6 +1792,73 @@ static void pbc(orc_sys *s) {
 }
 
 /* Verlet::run order (verlet.cpp:163-218), with Pair::compute for atoms */
+/* group bits of the local atoms and elements (NULL: every item in "all" only) */
+int orc_set_masks(orc_sys *s, const int *amask, const int *emask) {
+  free(s->amask);
+  free(s->emask);
+  s->amask = (int *) malloc(sizeof(int) * (s->nlocal + 1));
+  s->emask = (int *) malloc(sizeof(int) * (s->enlocal + 1));
+  for (int i = 0; i < s->nlocal; i++) s->amask[i] = amask ? amask[i] : 1;
+  for (int i = 0; i < s->enlocal; i++) s->emask[i] = emask ? emask[i] : 1;
+  return 0;
+}
+
+/* FixSetForce (fix_setforce.cpp:18-60): set[d] != 0 assigns val[d] */
+int orc_add_setforce(orc_sys *s, int bit, const int *set, const double *val) {
+  if (s->nfix == 16) return fail(s, "too many fixes");
+  s->fixes[s->nfix].viscous = 0;
+  s->fixes[s->nfix].bit = bit;
+  for (int d = 0; d < 3; d++) {
+    s->fixes[s->nfix].set[d] = set[d];
+    s->fixes[s->nfix].val[d] = val[d];
+  }
+  s->nfix++;
+  return 0;
+}
+
+/* FixViscous (fix_viscous.cpp:14-30) */
+int orc_add_viscous(orc_sys *s, int bit, double gamma) {
+  if (s->nfix == 16) return fail(s, "too many fixes");
+  s->fixes[s->nfix].viscous = 1;
+  s->fixes[s->nfix].bit = bit;
+  s->fixes[s->nfix].gamma = gamma;
+  s->nfix++;
+  return 0;
+}
+
+/* Modify::post_force (modify.cpp:663-669): each fix on the atoms
+   (FixSetForce::post_force 107-134, FixViscous::post_force 73-95), then on
+   the element nodes (epost_force 136-161, 97-123) */
+int orc_post_force(orc_sys *s) {
+  for (int k = 0; k < s->nfix; k++) {
+    const int bit = s->fixes[k].bit;
+    for (int pass = 0; pass < 2; pass++) {
+      const int n = pass ? s->enlocal : s->nlocal, per = pass ? NPE : 1;
+      const int *mask = pass ? s->emask : s->amask;
+      double *f = pass ? s->nodef : s->f;
+      const double *v = pass ? s->nodev : s->v;
+      for (int i = 0; i < n; i++) {
+        int m = mask ? mask[i] : 1;
+        if (!(m & bit)) continue;
+        for (int q = 0; q < per; q++) {
+          double *fi = f + 3 * (per * i + q);
+          const double *vi = v + 3 * (per * i + q);
+          if (s->fixes[k].viscous) {
+            double drag = s->fixes[k].gamma;
+            fi[0] -= drag * vi[0];
+            fi[1] -= drag * vi[1];
+            fi[2] -= drag * vi[2];
+          } else {
+            for (int d = 0; d < 3; d++)
+              if (s->fixes[k].set[d]) fi[d] = s->fixes[k].val[d];
+          }
+        }
+      }
+    }
+  }
+  return 0;
+}
+
 int orc_run(orc_sys *s, int nsteps) {
   for (int step = 0; step < nsteps; step++) {
     s->ntimestep++;
@@ -1709,6 +1882,7 @@ int orc_run(orc_sys *s, int nsteps) {
       for (int i = 0; i < 24 * s->enlocal; i++) s->nodef[i] = 0.0;
     if (s->nlocal && orc_atom_forces(s)) return -1;
     if (s->enlocal && orc_elem_forces(s)) return -1;
+    orc_post_force(s); /* verlet.cpp:206 */
     nve_final(s);
   }
   return 0;

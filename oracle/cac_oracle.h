@@ -47,6 +47,13 @@ int orc_atom_list(orc_sys *s);   /* Neighbor::build */
 int orc_elem_lists(orc_sys *s);  /* setup_cut + ebuild + nbuild */
 int orc_atom_forces(orc_sys *s); /* Pair::compute */
 int orc_elem_forces(orc_sys *s); /* Pair::ecompute */
+/* group masks and the post-force fixes setforce / viscous */
+int orc_set_masks(orc_sys *s, const int *amask, const int *emask);
+int orc_add_setforce(orc_sys *s, int bit, const int *set, const double *val);
+int orc_add_viscous(orc_sys *s, int bit, double gamma);
+int orc_post_force(orc_sys *s);
+/* centro-symmetry of the local atoms over the atom list (Output::centro_atom) */
+int orc_centro(orc_sys *s, double *out);
 /* energies, virial and kinetic tensors at the current state (17 values) */
 int orc_thermo(orc_sys *s, double *out);
 int orc_run(orc_sys *s, int nsteps); /* Verlet::run loop with atom forces */

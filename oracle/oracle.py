@@ -10,7 +10,7 @@ import ctypes
 import os
 import subprocess
 import tempfile
-from typing import Dict, Optional
+from typing import Sequence, Dict, Optional
 
 import numpy as np
 
@@ -170,6 +170,27 @@ class Oracle:
         self._ok(self._L.orc_elem_forces(self.h))
         return self.elements()["nodef"]
 
+    def centro(self) -> np.ndarray:
+        """Centro-symmetry of the local atoms (orc_centro)."""
+        out = np.zeros(self.size(0))
+        self._ok(self._L.orc_centro(self.h, _d(out)))
+        return out
+
+    def set_masks(self, amask=None, emask=None):
+        a = None if amask is None else np.ascontiguousarray(amask, dtype=np.int32)
+        e = None if emask is None else np.ascontiguousarray(emask, dtype=np.int32)
+        self._ok(self._L.orc_set_masks(self.h, _i(a) if a is not None else None,
+                                       _i(e) if e is not None else None))
+
+    def add_setforce(self, bit: int, values):
+        """values: three floats or None (NULL keeps the component)."""
+        st = np.array([0 if v is None else 1 for v in values], dtype=np.int32)
+        vals = np.array([0.0 if v is None else float(v) for v in values])
+        self._ok(self._L.orc_add_setforce(self.h, bit, _i(st), _d(vals)))
+
+    def add_viscous(self, bit: int, gamma: float):
+        self._ok(self._L.orc_add_viscous(self.h, bit, ctypes.c_double(gamma)))
+
     def thermo(self) -> Dict[str, object]:
         """Energies, virial and kinetic tensors at the current state (orc_thermo)."""
         out = np.zeros(17)
@@ -208,7 +229,7 @@ class Oracle:
 def input_script(data_file: str, *, units: str, boundary: str, pair: str, skin: float,
                  lj=(1.0, 1.0, 2.5), eam_file: Optional[str] = None, every: int = 1,
                  delay: int = 0, check: bool = True, binsize: float = 0.0, nsplit: int = 2,
-                 dt: Optional[float] = None) -> str:
+                 dt: Optional[float] = None, extra: Sequence[str] = ()) -> str:
     """Reference input-script commands for one configuration (input.cpp:362-404)."""
     lines = [f"units {units}", f"boundary {boundary}"]
     if nsplit != 2:
@@ -226,6 +247,7 @@ def input_script(data_file: str, *, units: str, boundary: str, pair: str, skin: 
     if dt is not None:
         lines.append(f"timestep {dt!r}")
     lines.append("fix 1 all nve")
+    lines += list(extra)
     return "\n".join(lines) + "\n"
 
 

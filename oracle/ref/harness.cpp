@@ -51,6 +51,7 @@
 #include "modify.h"
 #include "neigh_list.h"
 #include "neighbor.h"
+#include "output.h"
 #include "node_neigh_list.h"
 #include "pair.h"
 #include "update.h"
@@ -407,7 +408,15 @@ struct Harness {
     }
     if (atom->nlocal) atom_forces();
     if (cac->element_flag) elem_forces();
+    if (cac->modify->n_post_force) cac->modify->post_force(0);  // verlet.cpp:206
     cac->modify->final_integrate();
+  }
+
+  // Output::centro_atom over the atom list (output.cpp:352-447)
+  void dump_centro() {
+    cac->output->centro_atom(cac->neighbor->lists[0]);
+    std::vector<double> c(cac->output->centro, cac->output->centro + cac->atom->nlocal);
+    write_f64("centro.f64", c);
   }
 };
 
@@ -465,6 +474,8 @@ int main(int argc, char **argv) {
     } else if (cmd == "atom_list") {
       h.atom_build();
       h.dump_atom_list();
+    } else if (cmd == "centro") {
+      h.dump_centro();
     } else if (cmd == "atom_forces") {
       h.atom_forces();
       h.dump_atom_forces("atom_f.f64");

@@ -43,6 +43,11 @@ CASES: Dict[str, dict] = {
                     every=2, delay=0, check=True, binsize=0.0, nsplit=2, dt=None,
                     cells=(4, 8, 8), nae=4, layers=2, nodes_as_ip=True, jitter=0.05,
                     temp=300.0, seed=14, steps=6),
+    # lj_cac with regions, groups and the post-force fixes setforce / viscous
+    "lj_cac_fixes": dict(kind="slab", units="lj", pair="lj/cut", skin=2.8, boundary="f p p",
+                         every=1, delay=0, check=False, binsize=0.0, nsplit=2, dt=None,
+                         cells=(4, 8, 8), nae=4, layers=2, nodes_as_ip=False, jitter=0.03,
+                         temp=0.1, seed=16, steps=6, fixes=True),
     # EAM atoms only, periodic, forced rebuild every step
     "eam_atoms": dict(kind="atoms", units="metal", pair="eam", skin=7.5, boundary="p p p",
                       every=1, delay=0, check=False, binsize=0.0, nsplit=2, dt=None,
@@ -72,6 +77,48 @@ def build_model(cfg: dict) -> L.Model:
     L.thermalize(m, cfg["temp"], KB[cfg["units"]], MVV2E[cfg["units"]], cfg["seed"] + 1000)
     L.remap_into_box(m)
     return m
+
+
+def _fix_bounds(m: L.Model):
+    lo, hi = float(m.boxlo[0]), float(m.boxhi[0])
+    return lo + 0.3 * (hi - lo), lo + 0.7 * (hi - lo)
+
+
+def fix_lines(cfg: dict, m: L.Model) -> list:
+    """Reference commands of a case's regions, groups and post-force fixes."""
+    if not cfg.get("fixes"):
+        return []
+    x1, x2 = _fix_bounds(m)
+    return [f"region lo block INF {x1!r} INF INF INF INF",
+            f"region hi block {x2!r} INF INF INF INF INF",
+            "group lo region lo",
+            "group hi region hi",
+            "group mid subtract all lo hi",
+            "fix 2 lo setforce 0.0 0.0 NULL",
+            "fix 3 hi viscous 0.5",
+            "fix 4 mid viscous 0.05"]
+
+
+def fix_setup(cfg: dict, m: L.Model):
+    """The same groups as masks (bit 1 all, 2 lo, 4 hi, 8 mid: region block
+    bounds inclusive, atoms by position, elements by centre) and the fixes in
+    order, for the oracle."""
+    if not cfg.get("fixes"):
+        return None, None, []
+    x1, x2 = _fix_bounds(m)
+
+    def masks(x):
+        mk = np.ones(len(x), dtype=np.int32)
+        lo = x[:, 0] <= x1
+        hi = x[:, 0] >= x2
+        mk[lo] |= 2
+        mk[hi] |= 4
+        mk[~lo & ~hi] |= 8
+        return mk
+    am = masks(m.atom_x)
+    em = masks(m.element_centres()) if m.nelements else np.zeros(0, np.int32)
+    return am, em, [("setforce", 2, (0.0, 0.0, None)), ("viscous", 4, 0.5),
+                    ("viscous", 8, 0.05)]
 
 
 def settings_kwargs(cfg: dict, eam_file: str = EAM_FILE) -> dict:

@@ -44,11 +44,12 @@ def run_case(name: str, cfg: dict) -> None:
     L.write_data(m, os.path.join(wd, "data.cac"), with_velocities=True)
     m.atom_v.astype(np.float64).tofile(os.path.join(wd, "v.bin"))
     kw = C.settings_kwargs(cfg)
-    script = O.input_script("data.cac", boundary=cfg["boundary"], **kw)
+    script = O.input_script("data.cac", boundary=cfg["boundary"], extra=C.fix_lines(cfg, m),
+                            **kw)
     cap = 8 * (m.natoms + 64)
     directives = [f"capacity {cap}", "velocities v.bin", "setup"]
     if m.natoms:
-        directives += ["atom_list", "atom_forces"]
+        directives += ["atom_list", "centro", "atom_forces"]
     if m.nelements:
         directives += ["elem_lists", "elem_forces"]
     directives += [f"step {cfg['steps']}", "state s1"]

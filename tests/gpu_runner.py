@@ -19,7 +19,7 @@ def configure(s, cfg, m, via_files=False, eam_file=C.EAM_FILE):
         data = os.path.join(wd, "data.cac")
         L.write_data(m, data, with_velocities=True)
         from oracle import oracle as O
-        script = O.input_script(data, boundary=cfg["boundary"], **kw)
+        script = O.input_script(data, boundary=cfg["boundary"], extra=C.fix_lines(cfg, m), **kw)
         path = os.path.join(wd, "in.cac")
         with open(path, "w") as f:
             f.write(script)
@@ -47,6 +47,8 @@ def configure(s, cfg, m, via_files=False, eam_file=C.EAM_FILE):
     if kw["dt"] is not None:
         s.command(f"timestep {kw['dt']!r}")
     s.command("fix 1 all nve")
+    for line in C.fix_lines(cfg, m):
+        s.command(line)
 
 
 def run_gpu(cfg, m, mode=cacg.FP64_EXACT, via_files=False, steps=None):
@@ -62,6 +64,7 @@ def run_gpu(cfg, m, mode=cacg.FP64_EXACT, via_files=False, steps=None):
             out["atom_numneigh"], out["atom_neigh"] = s.atom_list()
             a = s.atoms(all_=True)
             out["atom_tag_all"], out["atom_x_all"] = a["tag"], a["x"].reshape(-1)
+            out["centro"] = s.centro()
             s.pair_compute()
             out["atom_f"] = s.atoms()["f"].reshape(-1)
         if m.nelements:

@@ -16,12 +16,21 @@ def run_oracle(O, name):
     cfg, z = C.load_golden(name)
     m = C.model_from_arrays(z)
     o = O.Oracle(m, **C.settings_kwargs(cfg))
+    am, em, fixes = C.fix_setup(cfg, m)
+    if fixes:
+        o.set_masks(am, em)
+        for kind, bit, arg in fixes:
+            if kind == "setforce":
+                o.add_setforce(bit, arg)
+            else:
+                o.add_viscous(bit, arg)
     o.setup()
     out = {}
     if m.natoms:
         out["atom_numneigh"], out["atom_neigh"] = o.atom_list()
         a = o.atoms(all_=True)
         out["atom_tag_all"], out["atom_x_all"] = a["tag"], a["x"].reshape(-1)
+        out["centro"] = o.centro()
         out["atom_f"] = o.atom_forces().reshape(-1)
     if m.nelements:
         enum, eneigh, ipn, ipj, ipnj = o.elem_lists()
@@ -52,6 +61,6 @@ def test_oracle_matches_reference(oracle_lib, name):
 
 def test_rebuilds_happened():
     # the forced-rebuild cases exercise pbc + borders + all three builders
-    for name in ("lj_cac", "eam_atoms", "lj_cac_bigbins"):
+    for name in ("lj_cac", "eam_atoms", "lj_cac_bigbins", "lj_cac_fixes"):
         cfg, z = C.load_golden(name)
         assert int(z["ref_rebuilds"][0]) >= 1, name

@@ -11,6 +11,11 @@ import cases as C
 
 def _oracle(O, cfg, m, eam_file=C.EAM_FILE):
     o = O.Oracle(m, **C.settings_kwargs(cfg, eam_file))
+    am, em, fixes = C.fix_setup(cfg, m)
+    if fixes:
+        o.set_masks(am, em)
+        for kind, bit, arg in fixes:
+            (o.add_setforce if kind == "setforce" else o.add_viscous)(bit, arg)
     o.setup()
     if m.natoms:
         o.atom_list()
