@@ -51,7 +51,7 @@ EXPORTED = [
     "cacg_mlp_get_normalization", "cacg_mlp_loss_grad", "cacg_mlp_train", "cacg_mlp_predict",
     "cacg_gemm_bf16_tn", "cacg_surrogate_reference", "cacg_surrogate_samples",
     "cacg_surrogate_attach", "cacg_compute_centro", "cacg_dump_xyz", "cacg_dump_elements",
-    "cacg_fix_post_force",
+    "cacg_fix_post_force", "cacg_get_box",
 ]
 
 
@@ -113,6 +113,7 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
     lib.cacg_surrogate_samples.argtypes = [vp, _fp, _fp, i]
     lib.cacg_surrogate_attach.argtypes = [vp, vp, d, d]
     lib.cacg_compute_centro.argtypes = [vp, _dp, i]
+    lib.cacg_get_box.argtypes = [vp, _dp, _dp]
     lib.cacg_dump_xyz.argtypes = [vp, ctypes.c_char_p]
     lib.cacg_dump_elements.argtypes = [vp, ctypes.c_char_p, i]
     _LIB = lib
@@ -390,6 +391,11 @@ class System:
         return {"pe_atoms": out[0], "pe_elements": out[1], "ke_atoms": out[2],
                 "ke_nodes": out[3], "virial": out[4:10].copy(), "kinetic_tensor": out[10:16].copy(),
                 "volume": out[16], "etotal": out[0] + out[1] + out[2] + out[3]}
+
+    def box(self):
+        lo, hi = np.zeros(3), np.zeros(3)
+        self._ok(self._L.cacg_get_box(self.h, _d(lo), _d(hi)))
+        return lo, hi
 
     def fix_post_force(self):
         self._ok(self._L.cacg_fix_post_force(self.h))

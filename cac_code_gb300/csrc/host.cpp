@@ -167,6 +167,7 @@ struct cacg_context {
 
   // pair
   int pair_style = 0;  // 1 lj/cut, 2 eam
+  bool eam_setfl = false;  // eam/alloy: the tables come from a setfl file
   double cut_global = 0.0;
   double eps[MAXT + 1][MAXT + 1] = {}, sig[MAXT + 1][MAXT + 1] = {}, cutp[MAXT + 1][MAXT + 1] = {};
   int setflag[MAXT + 1][MAXT + 1] = {};
@@ -228,6 +229,11 @@ struct cacg_context {
   std::vector<std::string> groups{"all"};
   std::vector<int> h_amask, h_emask;  // group bits of the local atoms / elements
   std::vector<PostFix> post_fixes;
+  // fix deform: L(t) = L0 (1 + erate t) about the box centre, affine remap of
+  // atom and node positions at the end of every step
+  bool deform_on = false;
+  double erate[3] = {0, 0, 0}, dL0[3] = {0, 0, 0}, dc0[3] = {0, 0, 0};
+  long long deform_t0 = 0;
   DBuf<int> d_amask, d_emask;
   bool masks_dirty = true;
   // nodal-force surrogate (elements far from the atoms)
@@ -353,7 +359,7 @@ struct cacg_context {
   // ---- commands ----
   void command(const std::string &line);
   void read_data(const std::string &path);
-  void read_eam(const std::string &path);
+  void read_eam(const std::string &path, bool setfl = false, const std::string &element = "");
   void set_units(const std::string &style);
 
   // ---- path ----
@@ -384,6 +390,7 @@ struct cacg_context {
   void fix_cmd(const std::vector<std::string> &a);
   int group_bit(const std::string &name) const;
   void post_force();
+  void deform_step();
   void dump_xyz(const char *path);
   void dump_elements(const char *path, int append);
   void surrogate_reference(const double *nodex0);
@@ -547,9 +554,10 @@ void cacg_context::command(const std::string &raw) {
       if (a.size() != 2) fail(CACG_EINVAL, "Illegal pair_style command");
       pair_style = 1;
       cut_global = numeric(a[1]);
-    } else if (a[0] == "eam") {
+    } else if (a[0] == "eam" || a[0] == "eam/alloy") {
       if (a.size() != 1) fail(CACG_EINVAL, "Illegal pair_style command");
       pair_style = 2;
+      eam_setfl = a[0] == "eam/alloy";
     } else {
       fail(CACG_EINVAL, "Unknown pair style %s", a[0].c_str());
     }
@@ -575,6 +583,17 @@ void cacg_context::command(const std::string &raw) {
           count++;
         }
       if (count == 0) fail(CACG_EINVAL, "Incorrect args for pair coefficients");
+    } else if (eam_setfl) {
+      // pair_coeff * * file el1 ... elN: one element name per atom type
+      if (a.size() != 3 + (size_t) nt || a[0] != "*" || a[1] != "*")
+        fail(CACG_EINVAL, "Incorrect args for pair coefficients");
+      for (int t = 1; t < nt; t++)
+        if (a[3 + t] != a[3]) fail(CACG_EINVAL, "one species per system on this path");
+      read_eam(a[2], true, a[3]);
+      for (int i = 1; i <= nt; i++) {
+        setflag[i][i] = 1;
+        amass[i] = eam_mass;
+      }
     } else {
       if (a.size() != 3) fail(CACG_EINVAL, "Incorrect args for pair coefficients");
       bounds(a[0], nt, ilo, ihi);
@@ -752,6 +771,32 @@ void cacg_context::fix_cmd(const std::vector<std::string> &a) {
         f.val[d] = numeric(a[3 + d]);
       }
     post_fixes.push_back(f);
+  } else if (a[2] == "deform") {
+    // fix ID all deform 1 x|y|z erate R ... [remap x]: the reference has no
+    // box deformation; this follows the engineering strain-rate convention,
+    // L(t) = L0 (1 + R t) with the centre fixed, positions remapped affinely
+    if (a[1] != "all") fail(CACG_EINVAL, "fix deform applies to group all here");
+    if (a.size() < 7 || inumeric(a[3]) != 1) fail(CACG_EINVAL, "Illegal fix deform command");
+    if (!box_set) fail(CACG_EINVAL, "fix deform before the box is defined");
+    double er[3] = {0, 0, 0};
+    size_t k = 4;
+    while (k < a.size()) {
+      if (a[k] == "remap" && k + 1 < a.size() && a[k + 1] == "x") {
+        k += 2;
+        continue;
+      }
+      int d = a[k] == "x" ? 0 : a[k] == "y" ? 1 : a[k] == "z" ? 2 : -1;
+      if (d < 0 || k + 2 >= a.size() || a[k + 1] != "erate") fail(CACG_EINVAL, "Illegal fix deform command");
+      er[d] = numeric(a[k + 2]);
+      k += 3;
+    }
+    for (int d = 0; d < 3; d++) {
+      erate[d] = er[d];
+      dL0[d] = hi[d] - lo[d];
+      dc0[d] = 0.5 * (lo[d] + hi[d]);
+    }
+    deform_t0 = ntimestep;
+    deform_on = er[0] != 0.0 || er[1] != 0.0 || er[2] != 0.0;
   } else if (a[2] == "viscous") {  // fix_viscous.cpp:14-30
     if (a.size() < 4) fail(CACG_EINVAL, "Illegal fix viscous command");
     PostFix f;
@@ -786,6 +831,31 @@ void cacg_context::post_force() {
     }
     launches += (nlocal > 0) + (enlocal > 0);
   }
+}
+
+void cacg_context::deform_step() {
+  if (!deform_on) return;
+  cudaStream_t s = stream;
+  const double t = (double) (ntimestep - deform_t0) * dt;
+  for (int d = 0; d < 3; d++) {
+    if (erate[d] == 0.0) continue;
+    const double L = dL0[d] * (1.0 + erate[d] * t);
+    const double nlo = dc0[d] - 0.5 * L, olo = lo[d];
+    const double f = L / prd[d];
+    launch_affine(reinterpret_cast<double *>(d_x.p) + d, nlocal, 4, olo, nlo, f, s);
+    launch_affine(d_nodex.p + d, NPE * enlocal, 3, olo, nlo, f, s);
+    launch_affine(d_ex.p + d, enlocal, 3, olo, nlo, f, s);
+    launches += 3;
+    lo[d] = nlo;
+    hi[d] = dc0[d] + 0.5 * L;
+    prd[d] = L;
+  }
+  // ghost images are owners + pbc * prd: the shifts follow the new box, and
+  // the ghosts follow their remapped owners now (the next step would refresh
+  // them anyway; a force call between steps must not see the old images)
+  for (auto &w : swaps)
+    for (int d = 0; d < 3; d++) w.d[d] = (d == w.dim ? w.pbc : 0) * prd[d];
+  forward_comm();
 }
 
 // ------------------------------------------------------------------ read_data
@@ -992,22 +1062,59 @@ void cacg_context::read_data(const std::string &path) {
 }
 
 // PairEAM::read_file + file2array + array2spline (pair_eam.cpp:197-580)
-void cacg_context::read_eam(const std::string &path) {
+// The reference's funcfl variant (PairEAM::read_file, pair_eam.cpp:197-248):
+// comment, "Z mass", "Nrho drho Nr dr cut", F(rho), rho(r), r*phi(r).
+// With setfl (the eam/alloy format; the reference has no reader for it):
+// three comments, "N el1 ... elN", "Nrho drho Nr dr cut", then for each
+// element "Z mass a lattice", F(rho), rho(r), then the r*phi(r) tables of the
+// pairs (i >= j).  One species is on this path (the element kernels are
+// type-1 only), so a setfl file supplies `element`'s F and rho and the
+// element-element r*phi; the tables then take the funcfl path's regrid and
+// splines unchanged.
+void cacg_context::read_eam(const std::string &path, bool setfl, const std::string &element) {
   FILE *fp = fopen(path.c_str(), "r");
   if (!fp) fail(CACG_EIO, "Cannot open EAM potential file %s", path.c_str());
-  char buf[1024];
-  int tmp, nrho_f, nr_f;
-  double mass, drho_f, dr_f, cut;
-  if (!fgets(buf, sizeof(buf), fp) || !fgets(buf, sizeof(buf), fp)) {
-    fclose(fp);
-    fail(CACG_EIO, "EAM file truncated");
+  char buf[4096];
+  int tmp, nrho_f = 0, nr_f = 0;
+  double mass = 0, drho_f = 0, dr_f = 0, cut = 0;
+  auto line = [&]() {
+    if (!fgets(buf, sizeof(buf), fp)) {
+      fclose(fp);
+      fail(CACG_EIO, "EAM file truncated");
+    }
+  };
+  int nel = 1, iel = 0;
+  if (setfl) {
+    line();
+    line();
+    line();
+    line();
+    std::vector<std::string> w = split_words(buf);
+    if (w.empty()) {
+      fclose(fp);
+      fail(CACG_EIO, "Invalid setfl element line");
+    }
+    nel = atoi(w[0].c_str());
+    if (nel < 1 || (int) w.size() < nel + 1) {
+      fclose(fp);
+      fail(CACG_EIO, "Invalid setfl element line");
+    }
+    iel = -1;
+    for (int k = 0; k < nel; k++)
+      if (w[1 + k] == element) iel = k;
+    if (iel < 0) {
+      fclose(fp);
+      fail(CACG_EINVAL, "No matching element %s in setfl file", element.c_str());
+    }
+    line();
+    sscanf(buf, "%d %lg %d %lg %lg", &nrho_f, &drho_f, &nr_f, &dr_f, &cut);
+  } else {
+    line();
+    line();
+    sscanf(buf, "%d %lg", &tmp, &mass);
+    line();
+    sscanf(buf, "%d %lg %d %lg %lg", &nrho_f, &drho_f, &nr_f, &dr_f, &cut);
   }
-  sscanf(buf, "%d %lg", &tmp, &mass);
-  if (!fgets(buf, sizeof(buf), fp)) {
-    fclose(fp);
-    fail(CACG_EIO, "EAM file truncated");
-  }
-  sscanf(buf, "%d %lg %d %lg %lg", &nrho_f, &drho_f, &nr_f, &dr_f, &cut);
   if (nrho_f < 5 || nr_f < 5) {
     fclose(fp);
     fail(CACG_EINVAL, "EAM tables too short");
@@ -1025,7 +1132,32 @@ void cacg_context::read_eam(const std::string &path) {
     return true;
   };
   std::vector<double> F, R, Z;
-  bool ok = grab(nrho_f, F) && grab(nr_f, R) && grab(nr_f, Z);
+  bool ok = true;
+  if (setfl) {
+    std::vector<double> f2, r2;
+    for (int k = 0; k < nel && ok; k++) {
+      if (!fgets(buf, sizeof(buf), fp)) {
+        ok = false;
+        break;
+      }
+      double zz = 0, mk = 0;
+      sscanf(buf, "%lg %lg", &zz, &mk);
+      ok = grab(nrho_f, f2) && grab(nr_f, r2);
+      if (k == iel) {
+        mass = mk;
+        F = f2;
+        R = r2;
+      }
+    }
+    // pair tables in the order (i, j), i >= j
+    for (int i = 0; i < nel && ok; i++)
+      for (int j = 0; j <= i && ok; j++) {
+        ok = grab(nr_f, r2);
+        if (i == iel && j == iel) Z = r2;
+      }
+  } else {
+    ok = grab(nrho_f, F) && grab(nr_f, R) && grab(nr_f, Z);
+  }
   fclose(fp);
   if (!ok) fail(CACG_EIO, "EAM file truncated");
   eam_mass = mass;
@@ -2476,6 +2608,7 @@ void cacg_context::run(int n) {
     post_force();  // verlet.cpp:206
     mark(b + 4);
     nve_final();
+    deform_step();
     mark(b + 5);
   }
   check(cudaEventRecord(ev[1], stream), "ev");
@@ -2883,6 +3016,15 @@ int cacg_compute_thermo(cacg_handle h, double *out, int n) {
   double v[17];
   h->compute_thermo(v);
   for (int i = 0; i < n && i < 17; i++) out[i] = v[i];
+  API_END
+}
+
+int cacg_get_box(cacg_handle h, double *lo, double *hi) {
+  API_BEGIN
+  for (int d = 0; d < 3; d++) {
+    if (lo) lo[d] = h->lo[d];
+    if (hi) hi[d] = h->hi[d];
+  }
   API_END
 }
 

@@ -354,6 +354,8 @@ void launch_nve_nodes_initial(double *ex, double *nodex, double *nodev, const do
 // group mask has `bit` (fix_setforce.cpp:107-161, fix_viscous.cpp:73-123)
 void launch_setforce(double *f, const int *mask, int n, int per_item, int bit, const int *set,
                      const double *val, cudaStream_t s);
+// x[i * stride] = nlo + (x[i * stride] - olo) * f for i < n (fix deform remap)
+void launch_affine(double *x, int n, int stride, double olo, double nlo, double f, cudaStream_t s);
 void launch_viscous(double *f, const double *v, const int *mask, int n, int per_item, int bit,
                     double gamma, cudaStream_t s);
 void launch_nve_nodes_final(double *nodev, const double *nodef, const int *etype,

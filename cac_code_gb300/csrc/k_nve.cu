@@ -249,7 +249,18 @@ __global__ void k_viscous(double *__restrict__ f, const double *__restrict__ v,
   if (i >= n * per || !(mask[i / per] & bit)) return;
   for (int d = 0; d < 3; d++) f[3 * (size_t) i + d] -= drag * v[3 * (size_t) i + d];
 }
+__global__ void k_affine(double *__restrict__ x, int n, int stride, double olo, double nlo,
+                         double f) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[(size_t) i * stride] = nlo + (x[(size_t) i * stride] - olo) * f;
+}
 }  // namespace
+
+void launch_affine(double *x, int n, int stride, double olo, double nlo, double f, cudaStream_t s) {
+  if (n <= 0) return;
+  k_affine<<<nblk(n, 256), 256, 0, s>>>(x, n, stride, olo, nlo, f);
+  check(cudaGetLastError(), "affine");
+}
 
 void launch_setforce(double *f, const int *mask, int n, int per_item, int bit, const int *set,
                      const double *val, cudaStream_t s) {

@@ -335,6 +335,47 @@ class AnalyticEAM:
         return -self.A * np.sqrt(np.maximum(np.asarray(rho), 0.0))
 
 
+def write_eam_setfl(pot: AnalyticEAM, path: str, element: str = "Cu", nrho: int = 2000,
+                    drho: Optional[float] = None, nr: int = 2000,
+                    rho_max: Optional[float] = None, r_max: Optional[float] = None) -> None:
+    """Tabulate ``pot`` as a one-element setfl file (the eam/alloy format):
+    three comment lines, "1 el", "Nrho drho Nr dr cut", "Z mass a lattice",
+    F(rho), rho(r), r*phi(r) -- the same grids and values as
+    write_eam_funcfl with the same arguments."""
+    dr = (pot.cut if r_max is None else r_max) / (nr - 1)
+    if rho_max is None:
+        rho_max = 40.0
+    if drho is None:
+        drho = rho_max / (nrho - 1)
+    r = np.arange(nr) * dr
+    rho = np.arange(nrho) * drho
+
+    def block(vals):
+        return [" ".join(f"{v:.16e}" for v in vals[i:i + 5]) for i in range(0, len(vals), 5)]
+    lines = ["analytic EAM Cu: exp density, Morse pair, sqrt embedding (synthetic)",
+             "setfl layout, one element", "tables as in the funcfl file of the same grids",
+             f"1 {element}", f"{nrho} {drho:.16e} {nr} {dr:.16e} {pot.cut:.16e}",
+             f"29 {pot.mass:.6f} 3.615 fcc"]
+    lines += block(pot.embed(rho))
+    lines += block(pot.density(r))
+    lines += block(r * pot.pair(r))
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
+def funcfl_to_setfl(src: str, dst: str, element: str = "Cu", lattice: str = "3.615 fcc") -> None:
+    """Re-emit a funcfl-variant file as a one-element setfl file with the
+    very same number strings (F, rho, r*phi), so both parse to identical
+    tables on any host."""
+    with open(src) as f:
+        lines = f.read().splitlines()
+    z_mass = lines[1].split()
+    out = [lines[0], "setfl layout, one element", "converted from the funcfl file",
+           f"1 {element}", lines[2], f"{z_mass[0]} {z_mass[1]} {lattice}"] + lines[3:]
+    with open(dst, "w") as f:
+        f.write("\n".join(out) + "\n")
+
+
 def write_eam_funcfl(pot: AnalyticEAM, path: str, nrho: int = 2000, drho: Optional[float] = None,
                      nr: int = 2000, rho_max: Optional[float] = None,
                      r_max: Optional[float] = None) -> None:

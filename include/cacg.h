@@ -54,6 +54,10 @@ int cacg_file(cacg_handle h, const char *path);
 
 /* ---- direct state (ReadData::command sections, read_data.cpp:166-211) ---- */
 int cacg_set_box(cacg_handle h, const double *lo, const double *hi, const int *periodic);
+/* Domain::boxlo/boxhi now (they move under "fix ID all deform 1 x erate R":
+   L(t) = L0 (1 + R t) about the box centre, positions remapped affinely at the
+   end of each step; the reference has no box deformation) */
+int cacg_get_box(cacg_handle h, double *lo, double *hi);
 int cacg_set_masses(cacg_handle h, int ntypes, const double *mass);         /* Masses */
 int cacg_set_atoms(cacg_handle h, int n, const double *x, const double *v,
                    const int *type);                                          /* Atoms */

@@ -131,6 +131,10 @@ struct orc_sys {
   int *amask, *emask;
   int nfix;
   struct { int viscous, bit, set[3]; double val[3], gamma; } fixes[16];
+  /* box deformation (engineering strain rate about the centre) */
+  int deform;
+  double erate[3], dL0[3], dc0[3];
+  long long deform_t0;
   /* run state */
   long long ntimestep;
   int ago, nrebuild;
@@ -1859,6 +1863,46 @@ int orc_post_force(orc_sys *s) {
   return 0;
 }
 
+/* L(t) = L0 (1 + erate t) about the box centre from now on; positions of
+   atoms, nodes and element centres remapped affinely at the end of each step
+   (no reference counterpart) */
+int orc_get_box(orc_sys *s, double *lo, double *hi) {
+  for (int d = 0; d < 3; d++) {
+    lo[d] = s->boxlo[d];
+    hi[d] = s->boxhi[d];
+  }
+  return 0;
+}
+
+int orc_set_deform(orc_sys *s, const double *erate) {
+  s->deform = 0;
+  for (int d = 0; d < 3; d++) {
+    s->erate[d] = erate[d];
+    s->dL0[d] = s->boxhi[d] - s->boxlo[d];
+    s->dc0[d] = 0.5 * (s->boxlo[d] + s->boxhi[d]);
+    s->deform |= erate[d] != 0.0;
+  }
+  s->deform_t0 = s->ntimestep;
+  return 0;
+}
+
+static void deform_step(orc_sys *s) {
+  if (!s->deform) return;
+  double t = (double) (s->ntimestep - s->deform_t0) * s->dt;
+  for (int d = 0; d < 3; d++) {
+    if (s->erate[d] == 0.0) continue;
+    double L = s->dL0[d] * (1.0 + s->erate[d] * t);
+    double nlo = s->dc0[d] - 0.5 * L, olo = s->boxlo[d];
+    double f = L / s->prd[d];
+    for (int i = 0; i < s->nlocal; i++) s->x[3 * i + d] = nlo + (s->x[3 * i + d] - olo) * f;
+    for (int i = 0; i < NPE * s->enlocal; i++) s->nodex[3 * i + d] = nlo + (s->nodex[3 * i + d] - olo) * f;
+    for (int i = 0; i < s->enlocal; i++) s->ex[3 * i + d] = nlo + (s->ex[3 * i + d] - olo) * f;
+    s->boxlo[d] = nlo;
+    s->boxhi[d] = s->dc0[d] + 0.5 * L;
+    s->prd[d] = L;
+  }
+}
+
 int orc_run(orc_sys *s, int nsteps) {
   for (int step = 0; step < nsteps; step++) {
     s->ntimestep++;
@@ -1884,6 +1928,7 @@ int orc_run(orc_sys *s, int nsteps) {
     if (s->enlocal && orc_elem_forces(s)) return -1;
     orc_post_force(s); /* verlet.cpp:206 */
     nve_final(s);
+    deform_step(s);
   }
   return 0;
 }

@@ -52,6 +52,9 @@ int orc_set_masks(orc_sys *s, const int *amask, const int *emask);
 int orc_add_setforce(orc_sys *s, int bit, const int *set, const double *val);
 int orc_add_viscous(orc_sys *s, int bit, double gamma);
 int orc_post_force(orc_sys *s);
+/* box deformation at engineering strain rates erate[3] (per time unit) */
+int orc_set_deform(orc_sys *s, const double *erate);
+int orc_get_box(orc_sys *s, double *lo, double *hi);
 /* centro-symmetry of the local atoms over the atom list (Output::centro_atom) */
 int orc_centro(orc_sys *s, double *out);
 /* energies, virial and kinetic tensors at the current state (17 values) */

@@ -188,6 +188,15 @@ class Oracle:
         vals = np.array([0.0 if v is None else float(v) for v in values])
         self._ok(self._L.orc_add_setforce(self.h, bit, _i(st), _d(vals)))
 
+    def set_deform(self, erate):
+        e = np.ascontiguousarray(erate, dtype=np.float64)
+        self._ok(self._L.orc_set_deform(self.h, _d(e)))
+
+    def box(self):
+        lo, hi = np.zeros(3), np.zeros(3)
+        self._L.orc_get_box(self.h, _d(lo), _d(hi))
+        return lo, hi
+
     def add_viscous(self, bit: int, gamma: float):
         self._ok(self._L.orc_add_viscous(self.h, bit, ctypes.c_double(gamma)))
 

@@ -10,7 +10,7 @@ from cac_code_gb300 import cacg
 from cac_code_gb300 import lattice as L
 
 
-def configure(s, cfg, m, via_files=False, eam_file=C.EAM_FILE):
+def configure(s, cfg, m, via_files=False, eam_file=C.EAM_FILE, pair_lines=None):
     """Set up a System either through input commands + read_data (the drop-in
     path) or through direct array uploads."""
     kw = C.settings_kwargs(cfg, eam_file)
@@ -30,7 +30,10 @@ def configure(s, cfg, m, via_files=False, eam_file=C.EAM_FILE):
     s.command(f"units {kw['units']}")
     s.command(f"boundary {cfg['boundary']}")
     s.load_model(m)
-    if kw["pair"] == "lj/cut":
+    if pair_lines:
+        for line in pair_lines:
+            s.command(line)
+    elif kw["pair"] == "lj/cut":
         s.command(f"pair_style lj/cut {kw['lj'][2]!r}")
         s.command(f"pair_coeff 1 1 {kw['lj'][0]!r} {kw['lj'][1]!r}")
     else:
@@ -51,10 +54,10 @@ def configure(s, cfg, m, via_files=False, eam_file=C.EAM_FILE):
         s.command(line)
 
 
-def run_gpu(cfg, m, mode=cacg.FP64_EXACT, via_files=False, steps=None):
+def run_gpu(cfg, m, mode=cacg.FP64_EXACT, via_files=False, steps=None, pair_lines=None):
     s = cacg.System(0)
     try:
-        configure(s, cfg, m, via_files=via_files)
+        configure(s, cfg, m, via_files=via_files, pair_lines=pair_lines)
         s.set_precision(mode)
         s.init()
         s.setup()
