@@ -51,7 +51,7 @@ EXPORTED = [
     "cacg_mlp_get_normalization", "cacg_mlp_loss_grad", "cacg_mlp_train", "cacg_mlp_predict",
     "cacg_gemm_bf16_tn", "cacg_surrogate_reference", "cacg_surrogate_samples",
     "cacg_surrogate_attach", "cacg_compute_centro", "cacg_dump_xyz", "cacg_dump_elements",
-    "cacg_fix_post_force", "cacg_get_box",
+    "cacg_fix_post_force", "cacg_get_box", "cacg_set_graphs",
 ]
 
 
@@ -89,6 +89,7 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
     lib.cacg_run.argtypes = [ctypes.c_void_p, ctypes.c_int]
     lib.cacg_set_precision.argtypes = [ctypes.c_void_p, ctypes.c_int]
     lib.cacg_set_timing.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.cacg_set_graphs.argtypes = [ctypes.c_void_p, ctypes.c_int]
     lib.cacg_pair_compute.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
     lib.cacg_get_cut.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp]
     lib.cacg_kinetic_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -330,12 +331,12 @@ class System:
 
     # ---- state out ----
     def counts(self) -> Dict[str, int]:
-        c = np.zeros(19, dtype=np.int64)
-        self._ok(self._L.cacg_get_counts(self.h, c.ctypes.data_as(_lp), 19))
+        c = np.zeros(20, dtype=np.int64)
+        self._ok(self._L.cacg_get_counts(self.h, c.ctypes.data_as(_lp), 20))
         keys = ["nlocal", "nghost", "atom_entries", "enlocal", "enghost", "elem_entries",
                 "ip_rows", "ip_entries", "rebuilds", "nstencil", "step", "sites", "launches",
                 "sites_needed", "force_rows", "short_entries", "surrogate_elements",
-                "surrogate_evaluated", "surrogate_accepted"]
+                "surrogate_evaluated", "surrogate_accepted", "graph_steps"]
         return dict(zip(keys, (int(v) for v in c)))
 
     def atoms(self, all_: bool = False) -> Dict[str, np.ndarray]:
@@ -427,6 +428,9 @@ class System:
     def surrogate_attach(self, mlp: Optional["Mlp"], tol: float = 1e-4, dist: float = 11.0):
         self._ok(self._L.cacg_surrogate_attach(self.h, mlp.h if mlp is not None else None,
                                                float(tol), float(dist)))
+
+    def set_graphs(self, enable: bool = True):
+        self._ok(self._L.cacg_set_graphs(self.h, 1 if enable else 0))
 
     def set_timing(self, enable: bool = True):
         self._ok(self._L.cacg_set_timing(self.h, 1 if enable else 0))

@@ -283,15 +283,31 @@ struct cacg_context {
   cudaEvent_t ev[10] = {};
   double t_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   bool timing = false;
+  // CUDA graph of a step without a rebuild decision (captured once, replayed
+  // until a rebuild, a reallocation or a configuration change)
+  bool use_graphs = true, graph_ok = true, graph_valid = false;
+  cudaGraphExec_t gexec = nullptr;
+  unsigned long long graph_epoch = 0;
+  long long graph_launches = 0, graph_steps = 0;
+  int eager_since = 0;
+  void invalidate_graph() {
+    graph_valid = false;
+    eager_since = 0;
+  }
+  void plain_step();
+  bool capture_plain_step();
   std::vector<cudaEvent_t> pev;  // per-step phase events
+  std::vector<char> pev_used;  // marks recorded in the current run
   void mark(size_t k) {
     if (!timing) return;
     while (pev.size() <= k) {
       cudaEvent_t e;
       check(cudaEventCreate(&e), "event");
       pev.push_back(e);
+      pev_used.push_back(0);
     }
     check(cudaEventRecord(pev[k], stream), "event record");
+    pev_used[k] = 1;
   }
 
   ~cacg_context();
@@ -390,6 +406,7 @@ struct cacg_context {
   void fix_cmd(const std::vector<std::string> &a);
   int group_bit(const std::string &name) const;
   void post_force();
+  void upload_masks();
   void deform_step();
   void dump_xyz(const char *path);
   void dump_elements(const char *path, int append);
@@ -456,6 +473,7 @@ cacg_context::~cacg_context() {
   for (auto &e : ev)
     if (e) cudaEventDestroy(e);
   for (auto &e : pev) cudaEventDestroy(e);
+  if (gexec) cudaGraphExecDestroy(gexec);
   if (h_pin) cudaFreeHost(h_pin);
   if (stream) cudaStreamDestroy(stream);
 }
@@ -479,6 +497,7 @@ void cacg_context::set_units(const std::string &style) {
 }
 
 void cacg_context::command(const std::string &raw) {
+  invalidate_graph();  // any command may change what a captured step would do
   std::string line = raw;
   size_t hash = line.find('#');
   if (hash != std::string::npos) line = line.substr(0, hash);
@@ -810,17 +829,20 @@ void cacg_context::fix_cmd(const std::vector<std::string> &a) {
 }
 
 // Modify::post_force (modify.cpp:663-669): each fix in order, atoms then nodes
+void cacg_context::upload_masks() {
+  if (!masks_dirty || post_fixes.empty()) return;
+  std::vector<int> am(h_amask), em(h_emask);
+  am.resize(std::max(nlocal, 1), 1);
+  em.resize(std::max(enlocal, 1), 1);
+  upload(d_amask, am, stream);
+  upload(d_emask, em, stream);
+  masks_dirty = false;
+}
+
 void cacg_context::post_force() {
   if (post_fixes.empty()) return;
   cudaStream_t s = stream;
-  if (masks_dirty) {
-    std::vector<int> am(h_amask), em(h_emask);
-    am.resize(std::max(nlocal, 1), 1);
-    em.resize(std::max(enlocal, 1), 1);
-    upload(d_amask, am, s);
-    upload(d_emask, em, s);
-    masks_dirty = false;
-  }
+  upload_masks();
   for (const PostFix &f : post_fixes) {
     if (f.viscous) {
       if (nlocal) launch_viscous(d_f.p, d_v.p, d_amask.p, nlocal, 1, f.bit, f.gamma, s);
@@ -2252,6 +2274,7 @@ void cacg_context::surrogate_samples(float *x, float *t) {
 // lies farther than `dist` from every local atom use the surrogate; the rows
 // lists of both kinds are fixed here.
 void cacg_context::surrogate_attach(cacg_mlp_t *m, double tol, double dist) {
+  invalidate_graph();
   sur = nullptr;
   nfar = nfar_rows = nstatic_rows = 0;
   if (!m) return;
@@ -2554,6 +2577,7 @@ int cacg_context::decide() {
 
 void cacg_context::rebuild() {
   nrebuild++;
+  invalidate_graph();
   pbc();
   if (enlocal) element_size();
   setup_cut();
@@ -2569,6 +2593,7 @@ void cacg_context::rebuild() {
 
 void cacg_context::setup() {
   require_init();
+  invalidate_graph();
   comm_setup();
   setup_bins();
   borders();
@@ -2587,6 +2612,7 @@ void cacg_context::run(int n) {
   }
   if (!fix_nve) fail(CACG_ESTATE, "run without fix nve");
   for (int k = 0; k < 8; k++) t_ms[k] = 0.0;
+  std::fill(pev_used.begin(), pev_used.end(), 0);
   for (auto &e : ev)
     if (!e) check(cudaEventCreate(&e), "event");
   check(cudaEventRecord(ev[0], stream), "ev");
@@ -2594,6 +2620,39 @@ void cacg_context::run(int n) {
   for (int step = 0; step < n; step++) {
     size_t b = (size_t) step * P;
     ntimestep++;
+    // a step that reaches no rebuild decision (Neighbor::decide returns 0
+    // without checking) replays the captured graph of the previous such step
+    const bool plain = !(ago + 1 >= delay && (ago + 1) % every == 0);
+    if (plain && use_graphs && graph_ok && !deform_on) {
+      ago++;
+      if (graph_valid && graph_epoch == dbuf_epoch()) {
+        check(cudaGraphLaunch(gexec, stream), "graph launch");
+        launches += graph_launches;
+        graph_steps++;
+        continue;
+      }
+      if (eager_since >= 1 && capture_plain_step()) {
+        check(cudaGraphLaunch(gexec, stream), "graph launch");
+        launches += graph_launches;
+        graph_steps++;
+        continue;
+      }
+      mark(b);
+      nve_initial();
+      forward_comm();
+      mark(b + 1);
+      pair_compute_pass(1);
+      mark(b + 2);
+      pair_compute_pass(2);
+      mark(b + 3);
+      pair_ecompute();
+      post_force();
+      mark(b + 4);
+      nve_final();
+      mark(b + 5);
+      eager_since++;
+      continue;
+    }
     mark(b);
     nve_initial();
     int nflag = decide();
@@ -2621,11 +2680,59 @@ void cacg_context::run(int n) {
       size_t b = (size_t) step * P;
       for (size_t k = 0; k < P - 1; k++) {
         float d = 0;
+        if (b + k + 1 >= pev.size() || !pev_used[b + k] || !pev_used[b + k + 1]) continue;
         check(cudaEventElapsedTime(&d, pev[b + k], pev[b + k + 1]), "elapsed");
         t_ms[1 + k] += d;
       }
     }
   }
+}
+
+// The body of a step without a rebuild decision, captured into a CUDA graph.
+// Anything that would allocate or synchronise ends the capture with an error;
+// the step then runs eagerly and graphs stay off for this handle.
+bool cacg_context::capture_plain_step() {
+  cudaStream_t s = stream;
+  upload_masks();  // host-to-device copies stay outside the capture
+  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    graph_ok = false;
+    return false;
+  }
+  const long long l0 = launches;
+  const unsigned long long e0 = dbuf_epoch();
+  bool ok = true;
+  try {
+    nve_initial();
+    forward_comm();
+    pair_compute_pass(1);
+    pair_compute_pass(2);
+    pair_ecompute();
+    post_force();
+    nve_final();
+  } catch (...) {
+    ok = false;
+  }
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(s, &g);
+  if (e != cudaSuccess || !g || !ok || dbuf_epoch() != e0) ok = false;
+  cudaGraphExec_t ex = nullptr;
+  if (ok && cudaGraphInstantiate(&ex, g, 0) != cudaSuccess) ok = false;
+  if (g) cudaGraphDestroy(g);
+  cudaGetLastError();  // a failed capture leaves its error behind
+  if (!ok) {
+    if (ex) cudaGraphExecDestroy(ex);
+    graph_ok = false;
+    launches = l0;
+    return false;
+  }
+  if (gexec) cudaGraphExecDestroy(gexec);
+  gexec = ex;
+  graph_launches = launches - l0;
+  launches = l0;
+  graph_epoch = dbuf_epoch();
+  graph_valid = true;
+  return true;
 }
 
 // ------------------------------------------------------------------ ABI
@@ -2791,6 +2898,7 @@ int cacg_set_precision(cacg_handle h, int mode) {
   API_BEGIN
   if (mode != CACG_FP64_EXACT && mode != CACG_FP64 && mode != CACG_MIXED) fail(CACG_EINVAL, "unknown precision mode");
   h->mode = mode;
+  h->invalidate_graph();
   API_END
 }
 
@@ -2865,9 +2973,10 @@ int cacg_run(cacg_handle h, int nsteps) {
 
 int cacg_get_counts(cacg_handle h, long long *c, int n) {
   API_BEGIN
-  long long v[19] = {h->nlocal, h->nghost, 0, h->enlocal, h->enghost, 0, h->nrows, 0,
+  long long v[20] = {h->nlocal, h->nghost, 0, h->enlocal, h->enghost, 0, h->nrows, 0,
                      h->nrebuild, (long long) h->stencil.size(), h->ntimestep, h->nsites,
-                     h->launches, h->nneed, h->nforce, 0, h->sur ? h->nfar : 0, 0, 0};
+                     h->launches, h->nneed, h->nforce, 0, h->sur ? h->nfar : 0, 0, 0,
+                     h->graph_steps};
   if (h->sur && h->d_scount.p) {
     unsigned long long c2[2] = {0, 0};
     check(cudaMemcpyAsync(c2, h->d_scount.p, sizeof(c2), cudaMemcpyDeviceToHost, h->stream), "scount");
@@ -2899,7 +3008,7 @@ int cacg_get_counts(cacg_handle h, long long *c, int n) {
     h->sync();
     for (int x : num) v[15] += x;
   }
-  for (int i = 0; i < n && i < 19; i++) c[i] = v[i];
+  for (int i = 0; i < n && i < 20; i++) c[i] = v[i];
   API_END
 }
 
@@ -3025,6 +3134,14 @@ int cacg_get_box(cacg_handle h, double *lo, double *hi) {
     if (lo) lo[d] = h->lo[d];
     if (hi) hi[d] = h->hi[d];
   }
+  API_END
+}
+
+int cacg_set_graphs(cacg_handle h, int enable) {
+  API_BEGIN
+  h->use_graphs = enable != 0;
+  h->graph_ok = true;
+  h->invalidate_graph();
   API_END
 }
 

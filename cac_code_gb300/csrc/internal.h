@@ -26,6 +26,13 @@ inline void check(cudaError_t e, const char *where) {
   if (e != cudaSuccess) throw CudaError{e, where};
 }
 
+// Bumped whenever any device array is allocated or freed: a CUDA graph
+// captured under an older value may hold pointers that are gone.
+inline unsigned long long &dbuf_epoch() {
+  static unsigned long long e = 0;
+  return e;
+}
+
 // Growable device array.  Growth keeps contents when asked (ghost appends).
 template <class T>
 struct DBuf {
@@ -33,6 +40,7 @@ struct DBuf {
   size_t cap = 0;
   void ensure(size_t n, cudaStream_t s, bool keep = false) {
     if (n <= cap) return;
+    dbuf_epoch()++;
     size_t ncap = cap ? cap : 256;
     while (ncap < n) ncap = ncap + ncap / 2 + 256;
     T *q = nullptr;
@@ -46,7 +54,10 @@ struct DBuf {
     cap = ncap;
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      cudaFree(p);
+      dbuf_epoch()++;
+    }
     p = nullptr;
     cap = 0;
   }

@@ -100,7 +100,8 @@ int cacg_put_nodes(cacg_handle h, const double *nodex, const double *nodev); /* 
    12 kernel launches issued 13 sites referenced by the lists
    14 integration points of nonzero weight 15 atom short-list entries of the
    last force evaluation 16 elements handed to the surrogate 17 surrogate
-   evaluations (element-steps) 18 of which accepted */
+   evaluations (element-steps) 18 of which accepted 19 steps replayed from a
+   captured CUDA graph */
 int cacg_get_counts(cacg_handle h, long long *counts, int n);
 /* Atom::x/v/f (atom.h:40); all != 0 includes ghosts for x and tag */
 int cacg_get_atoms(cacg_handle h, int all, double *x, double *v, double *f, int *tag);
@@ -227,6 +228,11 @@ int cacg_surrogate_attach(cacg_handle h, cacg_mlp m, double tol, double dist);
    EAM density), [3] atom pass 2 (EAM force), [4] element forces and nodal
    gather, [5] final integrate; each summed over the steps of the run. */
 int cacg_set_timing(cacg_handle h, int enable);
+/* Steps that reach no rebuild decision (Neighbor::decide returns 0 without a
+   check) are captured once into a CUDA graph and replayed until a rebuild,
+   a reallocation or any command; on by default.  Phase timing covers the
+   steps run eagerly only. */
+int cacg_set_graphs(cacg_handle h, int enable);
 int cacg_get_timing(cacg_handle h, double *ms, int n);
 /* Device-time of a FP64 fused-multiply-add loop on this GPU, for the FP64 roof:
    returns achieved FP64 FLOP/s in *flops. */
