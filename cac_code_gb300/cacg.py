@@ -51,7 +51,7 @@ EXPORTED = [
     "cacg_mlp_get_normalization", "cacg_mlp_loss_grad", "cacg_mlp_train", "cacg_mlp_predict",
     "cacg_gemm_bf16_tn", "cacg_surrogate_reference", "cacg_surrogate_samples",
     "cacg_surrogate_attach", "cacg_compute_centro", "cacg_dump_xyz", "cacg_dump_elements",
-    "cacg_fix_post_force", "cacg_get_box", "cacg_set_graphs",
+    "cacg_fix_post_force", "cacg_get_box", "cacg_set_graphs", "cacg_set_group",
 ]
 
 
@@ -90,6 +90,7 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
     lib.cacg_set_precision.argtypes = [ctypes.c_void_p, ctypes.c_int]
     lib.cacg_set_timing.argtypes = [ctypes.c_void_p, ctypes.c_int]
     lib.cacg_set_graphs.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.cacg_set_group.argtypes = [ctypes.c_void_p, ctypes.c_char_p, _ip, _ip]
     lib.cacg_pair_compute.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
     lib.cacg_get_cut.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp]
     lib.cacg_kinetic_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -428,6 +429,11 @@ class System:
     def surrogate_attach(self, mlp: Optional["Mlp"], tol: float = 1e-4, dist: float = 11.0):
         self._ok(self._L.cacg_surrogate_attach(self.h, mlp.h if mlp is not None else None,
                                                float(tol), float(dist)))
+
+    def set_group(self, name: str, atom_in=None, elem_in=None):
+        a = None if atom_in is None else np.ascontiguousarray(atom_in, dtype=np.int32)
+        e = None if elem_in is None else np.ascontiguousarray(elem_in, dtype=np.int32)
+        self._ok(self._L.cacg_set_group(self.h, name.encode(), _i(a), _i(e)))
 
     def set_graphs(self, enable: bool = True):
         self._ok(self._L.cacg_set_graphs(self.h, 1 if enable else 0))

@@ -285,6 +285,8 @@ struct cacg_context {
   bool timing = false;
   // CUDA graph of a step without a rebuild decision (captured once, replayed
   // until a rebuild, a reallocation or a configuration change)
+  int mixed_block = 512;  // threads per block of the mixed persistent kernels ("tune block N")
+  bool ran = false;  // steps taken since init (positions may have left the box)
   bool use_graphs = true, graph_ok = true, graph_valid = false;
   cudaGraphExec_t gexec = nullptr;
   unsigned long long graph_epoch = 0;
@@ -407,6 +409,7 @@ struct cacg_context {
   int group_bit(const std::string &name) const;
   void post_force();
   void upload_masks();
+  void set_group(const std::string &name, const int *atom_in, const int *elem_in);
   void deform_step();
   void dump_xyz(const char *path);
   void dump_elements(const char *path, int append);
@@ -638,6 +641,12 @@ void cacg_context::command(const std::string &raw) {
   } else if (c == "run") {
     if (a.size() < 1) fail(CACG_EINVAL, "Illegal run command");
     run(inumeric(a[0]));
+  } else if (c == "tune") {
+    // tune block 128|256|512: threads per block of the mixed-precision kernels
+    if (a.size() != 2 || a[0] != "block") fail(CACG_EINVAL, "Illegal tune command");
+    int b = inumeric(a[1]);
+    if (b != 128 && b != 256 && b != 512) fail(CACG_EINVAL, "tune block takes 128, 256 or 512");
+    mixed_block = b;
   } else if (c == "thermo" || c == "thermo_style" || c == "dump" || c == "velocity") {
     // output and setup commands outside this path are accepted and ignored
   } else {
@@ -829,6 +838,31 @@ void cacg_context::fix_cmd(const std::vector<std::string> &a) {
 }
 
 // Modify::post_force (modify.cpp:663-669): each fix in order, atoms then nodes
+// group membership from flags per local atom / element (nonzero = member),
+// e.g. clamped slabs of many replicas at once
+void cacg_context::set_group(const std::string &name, const int *atom_in, const int *elem_in) {
+  int bit = group_bit(name);
+  if (!bit) {
+    if (groups.size() == 32) fail(CACG_EINVAL, "Too many groups");
+    groups.push_back(name);
+    bit = 1 << (groups.size() - 1);
+  }
+  const int na = inited ? nlocal : (int) (h_x.size() / 3);
+  const int ne = inited ? enlocal : (int) (h_ex.size() / 3);
+  h_amask.resize(na, 1);
+  h_emask.resize(ne, 1);
+  for (int i = 0; i < na; i++) {
+    if (atom_in && atom_in[i]) h_amask[i] |= bit;
+    else h_amask[i] &= ~bit;
+  }
+  for (int i = 0; i < ne; i++) {
+    if (elem_in && elem_in[i]) h_emask[i] |= bit;
+    else h_emask[i] &= ~bit;
+  }
+  masks_dirty = true;
+  invalidate_graph();
+}
+
 void cacg_context::upload_masks() {
   if (!masks_dirty || post_fixes.empty()) return;
   std::vector<int> am(h_amask), em(h_emask);
@@ -1559,6 +1593,7 @@ void cacg_context::setup_bins() {
 
 void cacg_context::init() {
   if (!box_set) fail(CACG_ESTATE, "Init before the box is defined (read_data or cacg_set_box)");
+  ran = false;
   if (pair_style == 0) fail(CACG_ESTATE, "No pair style defined");
   int nt = std::max(ntypes, 1);
   for (int i = 1; i <= nt; i++)
@@ -2015,6 +2050,7 @@ void cacg_context::pair_compute_mixed(int pass) {
   int nall = nlocal + nghost;
   const float eps = 1.0e-4f;
   mixed::MixedAtoms m{};
+  m.block = mixed_block;
   m.x = d_x.p;
   m.num = d_num.p;
   m.list = d_list.p;
@@ -2096,6 +2132,7 @@ void cacg_context::pair_ecompute_mixed() {
   launches++;
   const float eps = 1.0e-4f;
   mixed::MixedElems m{};
+  m.block = mixed_block;
   m.nodex = d_nodex.p;
   m.site_h = d_site_h.p;
   m.site_l = d_site_l.p;
@@ -2594,6 +2631,9 @@ void cacg_context::rebuild() {
 void cacg_context::setup() {
   require_init();
   invalidate_graph();
+  // Verlet::setup wraps positions first (domain->pbc before comm->setup): a
+  // set-up after steps finds atoms and elements back inside the periodic box
+  if (ran) pbc();
   comm_setup();
   setup_bins();
   borders();
@@ -2611,6 +2651,7 @@ void cacg_context::run(int n) {
     neighbor_nbuild();
   }
   if (!fix_nve) fail(CACG_ESTATE, "run without fix nve");
+  ran = ran || n > 0;
   for (int k = 0; k < 8; k++) t_ms[k] = 0.0;
   std::fill(pev_used.begin(), pev_used.end(), 0);
   for (auto &e : ev)
@@ -3134,6 +3175,13 @@ int cacg_get_box(cacg_handle h, double *lo, double *hi) {
     if (lo) lo[d] = h->lo[d];
     if (hi) hi[d] = h->hi[d];
   }
+  API_END
+}
+
+int cacg_set_group(cacg_handle h, const char *name, const int *atom_in, const int *elem_in) {
+  API_BEGIN
+  if (!name || !*name) fail(CACG_EINVAL, "null group name");
+  h->set_group(name, atom_in, elem_in);
   API_END
 }
 

@@ -251,6 +251,7 @@ struct MixedAtoms {
   float cutsq_f, band_lo, band_hi;  // FP32 test; [band_lo, band_hi] re-tested in FP64
   double cutsq;
   int *snum, *slist;  // EAM: short list written by the density pass, read by the force pass
+  int block = 512;    // threads per block of the persistent grids (autotuned)
 };
 struct MixedElems {
   const double *nodex, *erho;
@@ -267,6 +268,7 @@ struct MixedElems {
   const float2 *node_hl;     // [nall][24] double-single node coordinates
   const float2 *spa_int_hl;  // double-single integration-point shape functions
   const unsigned char *skip = nullptr;  // elements whose forces come from the surrogate
+  int block = 512;                      // threads per block of the persistent grids
 };
 void split_hilo(const double4 *x, float4 *xh, float4 *xl, int n, cudaStream_t s);
 void sites_ds(const double *nodex, const int *etype, const int *site_base, const int *inter_num,

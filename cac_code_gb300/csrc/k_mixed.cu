@@ -13,6 +13,8 @@
 //    band, so the set of interacting pairs is exactly the FP64 set;
 //  * per-site densities and forces are summed in FP32 over chunks of 8 pairs and
 //    the chunks in FP64; F'(rho) is evaluated from the FP64 table in FP64.
+#include <vector>
+
 #include "internal.h"
 
 namespace cacg {
@@ -487,13 +489,33 @@ k_ip(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr,
 
 inline int nblk(long long n, int t) { return (int) ((n + t - 1) / t); }
 
+// SM count x resident blocks, cached per (kernel, block size, shared memory)
 int persistent_grid(const void *kernel, int threads, size_t smem, long long work) {
-  int dev = 0, nsm = 0, occ = 0;
+  struct Key {
+    const void *k;
+    int t;
+    size_t m;
+    int dev, nsm, occ;
+  };
+  static thread_local std::vector<Key> cache;
+  int dev = 0;
   cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  if (smem > 48 * 1024)
-    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, smem);
+  int nsm = 0, occ = 0;
+  bool hit = false;
+  for (const Key &c : cache)
+    if (c.k == kernel && c.t == threads && c.m == smem && c.dev == dev) {
+      nsm = c.nsm;
+      occ = c.occ;
+      hit = true;
+      break;
+    }
+  if (!hit) {
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (smem > 48 * 1024)
+      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, smem);
+    cache.push_back(Key{kernel, threads, smem, dev, nsm, occ});
+  }
   if (occ < 1) occ = 1;
   long long need = (work + threads - 1) / threads;
   long long g = (long long) nsm * occ;
@@ -514,8 +536,8 @@ void eam_rho_atoms(const MixedAtoms &m, const float4 *rhor_val, const EamTables 
   AtomArgs a{m.x, m.xh, m.xl, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
              m.band_hi, m.cutsq, m.snum, m.slist};
   size_t smem = sizeof(float4) * (e.nr + 1);
-  int g = persistent_grid((const void *) k_eam_rho_atoms, 512, smem, m.nlocal);
-  k_eam_rho_atoms<<<g, 512, smem, s>>>(a, rhor_val, e.nr, (float) e.rdr, e.frho, e.nrho,
+  int g = persistent_grid((const void *) k_eam_rho_atoms, m.block, smem, m.nlocal);
+  k_eam_rho_atoms<<<g, m.block, smem, s>>>(a, rhor_val, e.nr, (float) e.rdr, e.frho, e.nrho,
                                        e.rdrho, rho, fp);
   check(cudaGetLastError(), "eam_rho_atoms_mixed");
 }
@@ -526,8 +548,8 @@ void eam_force_atoms(const MixedAtoms &m, const float4 *ftab, const EamTables &e
   AtomArgs a{m.x, m.xh, m.xl, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
              m.band_hi, m.cutsq, m.snum, m.slist};
   size_t smem = sizeof(float4) * 3 * (e.nr + 1);
-  int g = persistent_grid((const void *) k_eam_force_atoms, 512, smem, m.nlocal);
-  k_eam_force_atoms<<<g, 512, smem, s>>>(a, ftab, e.nr, (float) e.rdr, fp, f);
+  int g = persistent_grid((const void *) k_eam_force_atoms, m.block, smem, m.nlocal);
+  k_eam_force_atoms<<<g, m.block, smem, s>>>(a, ftab, e.nr, (float) e.rdr, fp, f);
   check(cudaGetLastError(), "eam_force_atoms_mixed");
 }
 
@@ -536,8 +558,8 @@ void lj_atoms(const MixedAtoms &m, const int *type, const float *lj1, const floa
   if (m.nlocal <= 0) return;
   AtomArgs a{m.x, m.xh, m.xl, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
              m.band_hi, m.cutsq, m.snum, m.slist};
-  int g = persistent_grid((const void *) k_lj_atoms, 512, 0, m.nlocal);
-  k_lj_atoms<<<g, 512, 0, s>>>(a, type, lj1, lj2, cutsq_t, cutsq64, f);
+  int g = persistent_grid((const void *) k_lj_atoms, m.block, 0, m.nlocal);
+  k_lj_atoms<<<g, m.block, 0, s>>>(a, type, lj1, lj2, cutsq_t, cutsq64, f);
   check(cudaGetLastError(), "lj_atoms_mixed");
 }
 
@@ -586,17 +608,17 @@ void ip_pass(const MixedElems &m, int pass, const float4 *tab, const EamTables &
              m.weight, m.int_off, m.node_list, m.rows, m.nforce, m.cutsq_f, m.band_lo,
              m.band_hi, m.cutsq, m.node_hl, m.spa_int_hl, m.skip};
   if (pass == 0) {  // LJ forces
-    int g = persistent_grid((const void *) k_ip<false, false>, 512, 0, m.nforce);
-    k_ip<false, false><<<g, 512, 0, s>>>(a, tab, 0, 0.f, nullptr, 0, 0.0, lj1, lj2, out);
+    int g = persistent_grid((const void *) k_ip<false, false>, m.block, 0, m.nforce);
+    k_ip<false, false><<<g, m.block, 0, s>>>(a, tab, 0, 0.f, nullptr, 0, 0.0, lj1, lj2, out);
   } else if (pass == 1) {  // EAM nodal densities
     size_t smem = sizeof(float4) * (e.nr + 1);
-    int g = persistent_grid((const void *) k_ip<true, true>, 512, smem, (long long) m.nlocal_e * NPE);
-    k_ip<true, true><<<g, 512, smem, s>>>(a, tab, e.nr, (float) e.rdr, e.frho, e.nrho, e.rdrho,
+    int g = persistent_grid((const void *) k_ip<true, true>, m.block, smem, (long long) m.nlocal_e * NPE);
+    k_ip<true, true><<<g, m.block, smem, s>>>(a, tab, e.nr, (float) e.rdr, e.frho, e.nrho, e.rdrho,
                                          0.f, 0.f, out);
   } else {  // EAM forces
     size_t smem = sizeof(float4) * 3 * (e.nr + 1);
-    int g = persistent_grid((const void *) k_ip<true, false>, 512, smem, m.nforce);
-    k_ip<true, false><<<g, 512, smem, s>>>(a, tab, e.nr, (float) e.rdr, e.frho, e.nrho, e.rdrho,
+    int g = persistent_grid((const void *) k_ip<true, false>, m.block, smem, m.nforce);
+    k_ip<true, false><<<g, m.block, smem, s>>>(a, tab, e.nr, (float) e.rdr, e.frho, e.nrho, e.rdrho,
                                           0.f, 0.f, out);
   }
   check(cudaGetLastError(), "ip_pass_mixed");

@@ -414,6 +414,21 @@ def write_eam_funcfl(pot: AnalyticEAM, path: str, nrho: int = 2000, drho: Option
         fh.write("\n".join(lines) + "\n")
 
 
+def wrap_elements(model: Model) -> None:
+    """Shift whole elements by periods so that every centre lies in the periodic
+    box (nodes move with their centre, as Domain::elepbc moves them)."""
+    if not model.nelements:
+        return
+    c = model.element_centres()
+    for d in range(3):
+        if not model.periodic[d]:
+            continue
+        lo, hi = float(model.boxlo[d]), float(model.boxhi[d])
+        prd = hi - lo
+        k = np.floor((c[:, d] - lo) / prd)
+        model.nodex[:, :, d] -= (k * prd)[:, None]
+
+
 def remap_into_box(model: Model) -> None:
     """Wrap atom positions and element centres into the periodic box.
 

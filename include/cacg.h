@@ -151,6 +151,11 @@ int cacg_kinetic_noalloc(const double *v, const int *type, const double *mass, i
    commands of the input, in order, on the current forces (cacg_run applies
    them itself between the force passes and the final integration). */
 int cacg_fix_post_force(cacg_handle h);
+/* Group membership from flags per local atom and element (nonzero = in the
+   group; NULL = none), for groups no region describes (the reference builds
+   groups with "group ID region ...", group.cpp:80-200, also accepted by
+   cacg_command). */
+int cacg_set_group(cacg_handle h, const char *name, const int *atom_in, const int *elem_in);
 
 /* ---- analysis and output ----
    Output::centro_atom (output.cpp:352-447): centro-symmetry of the n local
