@@ -287,6 +287,7 @@ struct cacg_context {
   // until a rebuild, a reallocation or a configuration change)
   int mixed_block = 512;  // threads per block of the mixed persistent kernels ("tune block N")
   bool ran = false;  // steps taken since init (positions may have left the box)
+  bool oob_zeroed = false;  // d_misc[9] (packed-range counter) initialised
   bool use_graphs = true, graph_ok = true, graph_valid = false;
   cudaGraphExec_t gexec = nullptr;
   unsigned long long graph_epoch = 0;
@@ -409,6 +410,7 @@ struct cacg_context {
   int group_bit(const std::string &name) const;
   void post_force();
   void upload_masks();
+  void check_packed_range();
   void set_group(const std::string &name, const int *atom_in, const int *elem_in);
   void deform_step();
   void dump_xyz(const char *path);
@@ -2056,14 +2058,28 @@ void cacg_context::pair_compute_mixed(int pass) {
   m.list = d_list.p;
   m.stride = stride;
   m.nlocal = nlocal;
+  // cell-relative packed coordinates: cells of a power-of-two size g cover
+  // the box, its ghost shell and a margin in 4096 x 1024 x 1024 cells
+  double l0[3], ext[3];
+  const double margin = std::max(cutghost[0], std::max(cutghost[1], cutghost[2])) + max_size + cutneighmax;
+  for (int d = 0; d < 3; d++) {
+    l0[d] = lo[d] - margin;
+    ext[d] = prd[d] + 2.0 * margin;
+  }
+  double g = 1.0 / 1024.0;
+  while (ext[0] / g > 4096.0 || ext[1] / g > 1024.0 || ext[2] / g > 1024.0) g *= 2.0;
   if (pass == 1) {
     d_xh.ensure(nall, s);
-    d_xl.ensure(nall, s);
-    mixed::split_hilo(d_x.p, d_xh.p, d_xl.p, nall, s);
+    d_misc.ensure(16, s);
+    if (!oob_zeroed) {
+      check(cudaMemsetAsync(d_misc.p + 9, 0, sizeof(int), s), "oob");
+      oob_zeroed = true;
+    }
+    mixed::pack_rel(d_x.p, nall, l0[0], l0[1], l0[2], g, d_xh.p, d_misc.p + 9, s);
     launches++;
   }
-  m.xh = d_xh.p;
-  m.xl = d_xl.p;
+  m.xq = d_xh.p;
+  m.qg = (float) g;
   d_snum.ensure(std::max(nlocal, 1), s);
   d_slist.ensure((size_t) maxneigh * stride, s);
   m.snum = d_snum.p;
@@ -2612,7 +2628,20 @@ int cacg_context::decide() {
   return 0;
 }
 
+// atoms that left the packed-coordinate range of the mixed atom passes
+void cacg_context::check_packed_range() {
+  if (mode != CACG_MIXED || !d_misc.p || !oob_zeroed) return;
+  check(cudaMemcpyAsync(h_pin + 9, d_misc.p + 9, sizeof(int), cudaMemcpyDeviceToHost, stream), "oob");
+  sync();
+  if (h_pin[9]) {
+    int n = h_pin[9];
+    check(cudaMemsetAsync(d_misc.p + 9, 0, sizeof(int), stream), "oob reset");
+    fail(CACG_EINVAL, "%d atoms outside the packed-coordinate range of the mixed passes", n);
+  }
+}
+
 void cacg_context::rebuild() {
+  check_packed_range();
   nrebuild++;
   invalidate_graph();
   pbc();
@@ -2713,6 +2742,7 @@ void cacg_context::run(int n) {
   }
   check(cudaEventRecord(ev[1], stream), "ev");
   check(cudaEventSynchronize(ev[1]), "ev sync");
+  check_packed_range();
   float ms = 0;
   cudaEventElapsedTime(&ms, ev[0], ev[1]);
   t_ms[0] = ms;

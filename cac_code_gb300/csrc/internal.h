@@ -245,7 +245,10 @@ void filter_rows(const double *nodex, const int *etype, const int *row_elem, con
 namespace mixed {
 struct MixedAtoms {
   const double4 *x;
-  const float4 *xh, *xl;  // double-single coordinates
+  // cell-relative coordinates: xyz = x - (L0 + g * cell) in FP32, w = the cell
+  // (12 + 10 + 10 bits); a pair vector is (q_i - q_j) + g * (cell_i - cell_j)
+  const float4 *xq;
+  float qg;
   const int *num, *list;
   int stride, nlocal;
   float cutsq_f, band_lo, band_hi;  // FP32 test; [band_lo, band_hi] re-tested in FP64
@@ -271,6 +274,10 @@ struct MixedElems {
   int block = 512;                      // threads per block of the persistent grids
 };
 void split_hilo(const double4 *x, float4 *xh, float4 *xl, int n, cudaStream_t s);
+// cell-relative packed coordinates for the atom passes; *oob counts atoms
+// outside the 4096 x 1024 x 1024-cell range
+void pack_rel(const double4 *x, int n, double l0x, double l0y, double l0z, double g,
+              float4 *xq, int *oob, cudaStream_t s);
 void sites_ds(const double *nodex, const int *etype, const int *site_base, const int *inter_num,
               const float2 *shape_hl, int nelem, float4 *site_h, float4 *site_l, cudaStream_t s);
 void site_rho(const double *erho, const int *etype, const int *site_base, const int *inter_num,

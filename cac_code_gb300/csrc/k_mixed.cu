@@ -65,6 +65,49 @@ __global__ void k_split_hilo(const double4 *__restrict__ x, float4 *__restrict__
   xl[i] = make_float4((float) (p.x - hx), (float) (p.y - hy), (float) (p.z - hz), 0.f);
 }
 
+__global__ void k_pack_rel(const double4 *__restrict__ x, int n, double l0x, double l0y,
+                           double l0z, double g, double ig, float4 *__restrict__ xq,
+                           int *__restrict__ oob) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double4 p = x[i];
+  const double u[3] = {p.x - l0x, p.y - l0y, p.z - l0z};
+  const int lim[3] = {4095, 1023, 1023};
+  int c[3];
+  float r[3];
+  bool bad = false;
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    int k = (int) floor(u[d] * ig);
+    if (k < 0 || k > lim[d]) {
+      bad = true;
+      k = k < 0 ? 0 : lim[d];
+    }
+    c[d] = k;
+    r[d] = (float) (u[d] - (double) k * g);
+  }
+  if (bad) atomicAdd(oob, 1);
+  const int w = c[0] | (c[1] << 12) | (c[2] << 22);
+  xq[i] = make_float4(r[0], r[1], r[2], __int_as_float(w));
+}
+
+__device__ __forceinline__ void cell_of(const float4 &q, int &cx, int &cy, int &cz) {
+  const int w = __float_as_int(q.w);
+  cx = w & 0xFFF;
+  cy = (w >> 12) & 0x3FF;
+  cz = (int) ((unsigned) w >> 22);
+}
+
+// pair vector from cell-relative coordinates: (q_i - q_j) + g * (cell_i - cell_j)
+__device__ __forceinline__ void rel_vec(const float4 &qi, int cx, int cy, int cz, const float4 &qj,
+                                        float g, float &dx, float &dy, float &dz) {
+  int jx, jy, jz;
+  cell_of(qj, jx, jy, jz);
+  dx = (qi.x - qj.x) + g * (float) (cx - jx);
+  dy = (qi.y - qj.y) + g * (float) (cy - jy);
+  dz = (qi.z - qj.z) + g * (float) (cz - jz);
+}
+
 __device__ __forceinline__ void pair_vec(const float4 &hi, const float4 &li, const float4 &hj,
                                          const float4 &lj, float &dx, float &dy, float &dz) {
   dx = (hi.x - hj.x) + (li.x - lj.x);
@@ -74,7 +117,8 @@ __device__ __forceinline__ void pair_vec(const float4 &hi, const float4 &li, con
 
 struct AtomArgs {
   const double4 *x;
-  const float4 *xh, *xl;
+  const float4 *xq;
+  float qg;
   const int *num, *list;
   int stride, nlocal;
   float cutsq_f, band_lo, band_hi;  // [band_lo, band_hi]: decide in FP64
@@ -90,15 +134,30 @@ k_eam_rho_atoms(AtomArgs a, const float4 *__restrict__ rhor_val, int nr, float r
   for (int m = threadIdx.x; m <= nr; m += blockDim.x) s_val[m] = rhor_val[m];
   __syncthreads();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.nlocal; i += gridDim.x * blockDim.x) {
-    const float4 hi = a.xh[i], li = a.xl[i];
+    const float4 qi = a.xq[i];
+    int cx, cy, cz;
+    cell_of(qi, cx, cy, cz);
     const int n = a.num[i];
     double acc = 0.0;
     float part = 0.f;
     int ns = 0, cnt = 0;
+    // the next entry's index and coordinates are fetched while this one is
+    // evaluated: two dependent gathers in flight per thread instead of one
+    int jn = 0;
+    float4 qn = qi;
+    if (n > 0) {
+      jn = __ldg(a.list + i);
+      qn = __ldg(a.xq + jn);
+    }
     for (int k = 0; k < n; k++) {
-      int j = __ldg(a.list + (size_t) k * a.stride + i);
+      const int j = jn;
+      const float4 qj = qn;
+      if (k + 1 < n) {
+        jn = __ldg(a.list + (size_t) (k + 1) * a.stride + i);
+        qn = __ldg(a.xq + jn);
+      }
       float dx, dy, dz;
-      pair_vec(hi, li, __ldg(a.xh + j), __ldg(a.xl + j), dx, dy, dz);
+      rel_vec(qi, cx, cy, cz, qj, a.qg, dx, dy, dz);
       float rsq = dx * dx + dy * dy + dz * dz;
       if (rsq > a.band_hi) continue;
       a.slist[(size_t) ns++ * a.stride + i] = j;
@@ -130,16 +189,33 @@ k_eam_force_atoms(AtomArgs a, const float4 *__restrict__ ftab, int nr, float rdr
   for (int m = threadIdx.x; m < 3 * (nr + 1); m += blockDim.x) s_tab[m] = ftab[m];
   __syncthreads();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.nlocal; i += gridDim.x * blockDim.x) {
-    const float4 hi = a.xh[i], li = a.xl[i];
+    const float4 qi = a.xq[i];
+    int cx, cy, cz;
+    cell_of(qi, cx, cy, cz);
     const float fpi = (float) fp[i];
     const int n = a.snum[i];
     double fx = 0.0, fy = 0.0, fz = 0.0;
     float px = 0.f, py = 0.f, pz = 0.f;
     int cnt = 0;
+    int jn = 0;
+    float4 qn = qi;
+    float fpn = 0.f;
+    if (n > 0) {
+      jn = __ldg(a.slist + i);
+      qn = __ldg(a.xq + jn);
+      fpn = (float) __ldg(fp + jn);
+    }
     for (int k = 0; k < n; k++) {
-      int j = __ldg(a.slist + (size_t) k * a.stride + i);
+      const int j = jn;
+      const float4 qj = qn;
+      const float fpj = fpn;
+      if (k + 1 < n) {  // next entry's gathers in flight during this one
+        jn = __ldg(a.slist + (size_t) (k + 1) * a.stride + i);
+        qn = __ldg(a.xq + jn);
+        fpn = (float) __ldg(fp + jn);
+      }
       float dx, dy, dz;
-      pair_vec(hi, li, __ldg(a.xh + j), __ldg(a.xl + j), dx, dy, dz);
+      rel_vec(qi, cx, cy, cz, qj, a.qg, dx, dy, dz);
       float rsq = dx * dx + dy * dy + dz * dz;
       bool in = rsq < a.cutsq_f;
       if (rsq >= a.band_lo && rsq <= a.band_hi) in = inside64(a.x[i], a.x[j], a.cutsq);
@@ -154,7 +230,7 @@ k_eam_force_atoms(AtomArgs a, const float4 *__restrict__ ftab, int nr, float rdr
         float z2 = ((t1.z * p + t1.w) * p + t2.x) * p + t2.y;
         float phi = z2 * recip;
         float phip = z2p * recip - phi * recip;
-        float psip = (fpi + (float) __ldg(fp + j)) * rhoip + phip;
+        float psip = (fpi + fpj) * rhoip + phip;
         float fpair = -psip * recip;
         px += dx * fpair;
         py += dy * fpair;
@@ -180,7 +256,9 @@ k_lj_atoms(AtomArgs a, const int *__restrict__ type, const float *__restrict__ l
            const float *__restrict__ lj2, const float *__restrict__ cutsq_t,
            const double *__restrict__ cutsq64, double *__restrict__ f) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.nlocal; i += gridDim.x * blockDim.x) {
-    const float4 hi = a.xh[i], li = a.xl[i];
+    const float4 qi = a.xq[i];
+    int cx, cy, cz;
+    cell_of(qi, cx, cy, cz);
     const int it = type[i];
     const int n = a.num[i];
     double fx = 0.0, fy = 0.0, fz = 0.0;
@@ -188,7 +266,7 @@ k_lj_atoms(AtomArgs a, const int *__restrict__ type, const float *__restrict__ l
     for (int k = 0; k < n; k++) {
       int j = __ldg(a.list + (size_t) k * a.stride + i);
       float dx, dy, dz;
-      pair_vec(hi, li, __ldg(a.xh + j), __ldg(a.xl + j), dx, dy, dz);
+      rel_vec(qi, cx, cy, cz, __ldg(a.xq + j), a.qg, dx, dy, dz);
       float rsq = dx * dx + dy * dy + dz * dz;
       int ij = it * (MAXT + 1) + type[j];
       float cs = cutsq_t[ij];
@@ -424,9 +502,21 @@ k_ip(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr,
     double acc = 0.0, fx = 0.0, fy = 0.0, fz = 0.0;
     float part = 0.f, px = 0.f, py = 0.f, pz = 0.f;
     const int n = a.ipnum[r];
+    int sn = 0;
+    float4 shn = ih, sln = il;
+    if (n > 0) {
+      sn = __ldg(a.ipent + r);
+      shn = __ldg(a.site_h + sn);
+      sln = __ldg(a.site_l + sn);
+    }
     for (int k = 0; k < n; k++) {
-      int sid = __ldg(a.ipent + (size_t) k * a.rowstride + r);
-      float4 sh = __ldg(a.site_h + sid), sl = __ldg(a.site_l + sid);
+      const int sid = sn;
+      const float4 sh = shn, sl = sln;
+      if (k + 1 < n) {  // next site's gathers in flight during this one
+        sn = __ldg(a.ipent + (size_t) (k + 1) * a.rowstride + r);
+        shn = __ldg(a.site_h + sn);
+        sln = __ldg(a.site_l + sn);
+      }
       float dx, dy, dz;
       pair_vec(ih, il, sh, sl, dx, dy, dz);
       float rsq = dx * dx + dy * dy + dz * dz;
@@ -524,6 +614,13 @@ int persistent_grid(const void *kernel, int threads, size_t smem, long long work
 
 }  // namespace
 
+void pack_rel(const double4 *x, int n, double l0x, double l0y, double l0z, double g,
+              float4 *xq, int *oob, cudaStream_t s) {
+  if (n <= 0) return;
+  k_pack_rel<<<nblk(n, 256), 256, 0, s>>>(x, n, l0x, l0y, l0z, g, 1.0 / g, xq, oob);
+  check(cudaGetLastError(), "pack_rel");
+}
+
 void split_hilo(const double4 *x, float4 *xh, float4 *xl, int n, cudaStream_t s) {
   if (n <= 0) return;
   k_split_hilo<<<nblk(n, 256), 256, 0, s>>>(x, xh, xl, n);
@@ -533,7 +630,7 @@ void split_hilo(const double4 *x, float4 *xh, float4 *xl, int n, cudaStream_t s)
 void eam_rho_atoms(const MixedAtoms &m, const float4 *rhor_val, const EamTables &e,
                    double *rho, double *fp, cudaStream_t s) {
   if (m.nlocal <= 0) return;
-  AtomArgs a{m.x, m.xh, m.xl, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
+  AtomArgs a{m.x, m.xq, m.qg, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
              m.band_hi, m.cutsq, m.snum, m.slist};
   size_t smem = sizeof(float4) * (e.nr + 1);
   int g = persistent_grid((const void *) k_eam_rho_atoms, m.block, smem, m.nlocal);
@@ -545,7 +642,7 @@ void eam_rho_atoms(const MixedAtoms &m, const float4 *rhor_val, const EamTables 
 void eam_force_atoms(const MixedAtoms &m, const float4 *ftab, const EamTables &e,
                      const double *fp, double *f, cudaStream_t s) {
   if (m.nlocal <= 0) return;
-  AtomArgs a{m.x, m.xh, m.xl, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
+  AtomArgs a{m.x, m.xq, m.qg, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
              m.band_hi, m.cutsq, m.snum, m.slist};
   size_t smem = sizeof(float4) * 3 * (e.nr + 1);
   int g = persistent_grid((const void *) k_eam_force_atoms, m.block, smem, m.nlocal);
@@ -556,7 +653,7 @@ void eam_force_atoms(const MixedAtoms &m, const float4 *ftab, const EamTables &e
 void lj_atoms(const MixedAtoms &m, const int *type, const float *lj1, const float *lj2,
               const float *cutsq_t, const double *cutsq64, double *f, cudaStream_t s) {
   if (m.nlocal <= 0) return;
-  AtomArgs a{m.x, m.xh, m.xl, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
+  AtomArgs a{m.x, m.xq, m.qg, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
              m.band_hi, m.cutsq, m.snum, m.slist};
   int g = persistent_grid((const void *) k_lj_atoms, m.block, 0, m.nlocal);
   k_lj_atoms<<<g, m.block, 0, s>>>(a, type, lj1, lj2, cutsq_t, cutsq64, f);
