@@ -286,6 +286,7 @@ struct cacg_context {
   // CUDA graph of a step without a rebuild decision (captured once, replayed
   // until a rebuild, a reallocation or a configuration change)
   int mixed_block = 512;  // threads per block of the mixed persistent kernels ("tune block N")
+  bool mixed_row_filter = true;  // short lists for the mixed element passes ("tune row_filter")
   bool ran = false;  // steps taken since init (positions may have left the box)
   bool oob_zeroed = false;  // d_misc[9] (packed-range counter) initialised
   bool use_graphs = true, graph_ok = true, graph_valid = false;
@@ -645,10 +646,18 @@ void cacg_context::command(const std::string &raw) {
     run(inumeric(a[0]));
   } else if (c == "tune") {
     // tune block 128|256|512: threads per block of the mixed-precision kernels
-    if (a.size() != 2 || a[0] != "block") fail(CACG_EINVAL, "Illegal tune command");
-    int b = inumeric(a[1]);
-    if (b != 128 && b != 256 && b != 512) fail(CACG_EINVAL, "tune block takes 128, 256 or 512");
-    mixed_block = b;
+    // tune row_filter yes|no: short lists for the mixed element passes
+    if (a.size() != 2) fail(CACG_EINVAL, "Illegal tune command");
+    if (a[0] == "block") {
+      int b = inumeric(a[1]);
+      if (b != 128 && b != 256 && b != 512) fail(CACG_EINVAL, "tune block takes 128, 256 or 512");
+      mixed_block = b;
+    } else if (a[0] == "row_filter") {
+      if (a[1] != "yes" && a[1] != "no") fail(CACG_EINVAL, "tune row_filter takes yes or no");
+      mixed_row_filter = a[1] == "yes";
+    } else {
+      fail(CACG_EINVAL, "Illegal tune command");
+    }
   } else if (c == "thermo" || c == "thermo_style" || c == "dump" || c == "velocity") {
     // output and setup commands outside this path are accepted and ignored
   } else {
@@ -2128,7 +2137,9 @@ void cacg_context::pair_ecompute_mixed() {
   d_sipnum.ensure(std::max(nrows, 1), s);
   d_sipent.ensure((size_t) maxip * rowstride, s);
   const bool use_sur = sur && nfar > 0;
-  if (use_sur)  // node rows of every element, force rows of the elements near the atoms
+  if (!mixed_row_filter) {
+    // no short lists: the passes test every list entry themselves
+  } else if (use_sur)  // node rows of every element, force rows of the elements near the atoms
     fp64_fma::filter_rows(d_nodex.p, d_etype.p, d_row_elem.p, d_row_jj.p, nstatic_rows, d_ipnum.p,
                           d_ipent.p, rowstride, d_site_h.p, t, cut_pass(csq), 1, d_sipnum.p,
                           d_sipent.p, s, d_static_rows.p, nullptr);
@@ -2140,6 +2151,7 @@ void cacg_context::pair_ecompute_mixed() {
   // force rows of those it declined
   auto far_rows = [&]() {
     surrogate_predict(eamtab());
+    if (!mixed_row_filter) return;
     fp64_fma::filter_rows(d_nodex.p, d_etype.p, d_row_elem.p, d_row_jj.p, nfar_rows, d_ipnum.p,
                           d_ipent.p, rowstride, d_site_h.p, t, cut_pass(csq), 1, d_sipnum.p,
                           d_sipent.p, s, d_far_rows.p, d_skip.p);
@@ -2156,8 +2168,8 @@ void cacg_context::pair_ecompute_mixed() {
   m.row_elem = d_row_elem.p;
   m.row_jj = d_row_jj.p;
   m.row_first = d_row_first.p;
-  m.ipnum = d_sipnum.p;
-  m.ipent = d_sipent.p;
+  m.ipnum = mixed_row_filter ? d_sipnum.p : d_ipnum.p;
+  m.ipent = mixed_row_filter ? d_sipent.p : d_ipent.p;
   m.nrows = nrows;
   m.rowstride = rowstride;
   m.nlocal_e = enlocal;
