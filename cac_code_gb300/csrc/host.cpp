@@ -287,6 +287,13 @@ struct cacg_context {
   // until a rebuild, a reallocation or a configuration change)
   int mixed_block = 512;  // threads per block of the mixed persistent kernels ("tune block N")
   bool mixed_row_filter = true;  // short lists for the mixed element passes ("tune row_filter")
+  // neighbor unions staged in shared memory ("tune union yes"): bit-identical
+  // to the direct passes; at C2 they run at 8 warps per SM and lose to the
+  // direct kernels' 32 (1.71 vs 0.77 ms for the density pass), so off by default
+  bool mixed_union = false;
+  long long list_builds = 0, union_of = -1;
+  DBuf<int> d_union_j, d_union_n;
+  DBuf<unsigned short> d_slot, d_sslot;
   bool ran = false;  // steps taken since init (positions may have left the box)
   bool oob_zeroed = false;  // d_misc[9] (packed-range counter) initialised
   bool use_graphs = true, graph_ok = true, graph_valid = false;
@@ -452,6 +459,10 @@ cacg_context::~cacg_context() {
   d_nodex0.release();
   d_amask.release();
   d_emask.release();
+  d_union_j.release();
+  d_union_n.release();
+  d_slot.release();
+  d_sslot.release();
   d_far.release();
   d_far_rows.release();
   d_static_rows.release();
@@ -652,6 +663,9 @@ void cacg_context::command(const std::string &raw) {
       int b = inumeric(a[1]);
       if (b != 128 && b != 256 && b != 512) fail(CACG_EINVAL, "tune block takes 128, 256 or 512");
       mixed_block = b;
+    } else if (a[0] == "union") {
+      if (a[1] != "yes" && a[1] != "no") fail(CACG_EINVAL, "tune union takes yes or no");
+      mixed_union = a[1] == "yes";
     } else if (a[0] == "row_filter") {
       if (a[1] != "yes" && a[1] != "no") fail(CACG_EINVAL, "tune row_filter takes yes or no");
       mixed_row_filter = a[1] == "yes";
@@ -1881,6 +1895,7 @@ void cacg_context::pbc() {
 // ------------------------------------------------------------------ lists
 
 void cacg_context::neighbor_build() {
+  list_builds++;
   cudaStream_t s = stream;
   int nall = nlocal + nghost;
   if (nlocal == 0) {
@@ -2108,14 +2123,32 @@ void cacg_context::pair_compute_mixed(int pass) {
   m.cutsq_f = (float) cutforcesq;
   m.band_lo = m.cutsq_f * (1.0f - eps);
   m.band_hi = m.cutsq_f * (1.0f + eps);
+  if (mixed_union && pass == 1 && union_of != list_builds) {
+    // the groups' neighbor unions, once per atom list build
+    const int ngroups = (nlocal + 31) / 32;
+    d_union_j.ensure((size_t) std::max(ngroups, 1) * mixed::union_max(), s);
+    d_union_n.ensure(std::max(ngroups, 1), s);
+    d_slot.ensure((size_t) maxneigh * stride, s);
+    d_sslot.ensure((size_t) maxneigh * stride, s);
+    mixed::union_build(d_num.p, d_list.p, stride, nlocal, d_union_j.p, d_union_n.p, d_slot.p, s);
+    launches++;
+    union_of = list_builds;
+  }
   if (pass == 1) {
     d_rho.ensure(nall, s);
     d_fp.ensure(nall, s);
-    mixed::eam_rho_atoms(m, d_rhor_val4.p, e, d_rho.p, d_fp.p, s);
+    if (mixed_union)
+      mixed::eam_rho_union(m, d_union_j.p, d_union_n.p, d_slot.p, d_sslot.p, d_rhor_val4.p, e,
+                           d_rho.p, d_fp.p, s);
+    else
+      mixed::eam_rho_atoms(m, d_rhor_val4.p, e, d_rho.p, d_fp.p, s);
     launch_copy_root(d_fp.p, 1, d_root.p, nlocal, nghost, s);
     launches += 2;
   } else {
-    mixed::eam_force_atoms(m, d_ftab.p, e, d_fp.p, d_f.p, s);
+    if (mixed_union)
+      mixed::eam_force_union(m, d_union_j.p, d_union_n.p, d_sslot.p, d_ftab.p, e, d_fp.p, d_f.p, s);
+    else
+      mixed::eam_force_atoms(m, d_ftab.p, e, d_fp.p, d_f.p, s);
     launches++;
   }
 }

@@ -289,6 +289,16 @@ void sites_ds_needed(const float2 *node_hl, const int *site_base, const int *nee
 void site_rho_needed(const double *erho, const int *site_base, const int *need,
                      const int *need_elem, int nneed, const float *shape, float *rho,
                      cudaStream_t s);
+// neighbor unions of 32-atom groups staged in shared memory (EAM atom passes)
+int union_max();
+void union_build(const int *num, const int *list, int stride, int nlocal, int *union_j,
+                 int *union_n, unsigned short *slot, cudaStream_t s);
+void eam_rho_union(const MixedAtoms &m, const int *union_j, const int *union_n,
+                   const unsigned short *slot, unsigned short *sslot, const float4 *rhor_val,
+                   const EamTables &e, double *rho, double *fp, cudaStream_t s);
+void eam_force_union(const MixedAtoms &m, const int *union_j, const int *union_n,
+                     const unsigned short *sslot, const float4 *ftab, const EamTables &e,
+                     const double *fp, double *f, cudaStream_t s);
 void eam_rho_atoms(const MixedAtoms &m, const float4 *rhor_val, const EamTables &e,
                    double *rho, double *fp, cudaStream_t s);
 void eam_force_atoms(const MixedAtoms &m, const float4 *ftab, const EamTables &e,

@@ -13,6 +13,7 @@
 //    band, so the set of interacting pairs is exactly the FP64 set;
 //  * per-site densities and forces are summed in FP32 over chunks of 8 pairs and
 //    the chunks in FP64; F'(rho) is evaluated from the FP64 table in FP64.
+#include <algorithm>
 #include <vector>
 
 #include "internal.h"
@@ -178,6 +179,234 @@ k_eam_rho_atoms(AtomArgs a, const float4 *__restrict__ rhor_val, int nr, float r
     acc += (double) part;
     rho[i] = acc;
     fp[i] = fprime64(acc, frho, nrho, rdrho);
+  }
+}
+
+// ---- neighbor unions staged in shared memory (EAM atom passes) ----
+//
+// The 32 atoms a warp owns (consecutive local indices) share most of their
+// neighbors.  At each list build the union of their list entries is
+// collected (at most UMAX distinct atoms; a larger union marks the group for
+// the direct path) and every list entry is re-expressed as a 16-bit slot
+// into it.  Each step a warp loads the union's packed coordinates (and, in
+// the force pass, F') once into shared memory and then walks its lists
+// exactly as the direct kernels do, reading neighbors from shared memory: the
+// arithmetic and its order are unchanged, the L2 gathers drop by the
+// neighbor overlap (about 7x for lattice-ordered atoms).
+constexpr int UGROUP = 32, UMAX = 640, UHASH = 2048, UWARPS = 8;
+
+// one block per group: hash the group's entries, number the distinct atoms,
+// write each entry's slot
+__global__ void __launch_bounds__(256)
+k_union_build(const int *__restrict__ num, const int *__restrict__ list, int stride, int nlocal,
+              int *__restrict__ union_j, int *__restrict__ union_n,
+              unsigned short *__restrict__ slot) {
+  __shared__ int keys[UHASH], vals[UHASH];
+  __shared__ int count, overflow;
+  const int g = blockIdx.x, i0 = g * UGROUP;
+  for (int h = threadIdx.x; h < UHASH; h += blockDim.x) keys[h] = -1;
+  if (threadIdx.x == 0) {
+    count = 0;
+    overflow = 0;
+  }
+  __syncthreads();
+  // insert: thread t takes entries t, t + 256, ... of the group (atom-major)
+  int maxn = 0;
+  for (int a = 0; a < UGROUP && i0 + a < nlocal; a++) maxn = max(maxn, num[i0 + a]);
+  const int total = UGROUP * maxn;
+  for (int e = threadIdx.x; e < total && !*((volatile int *) &overflow); e += blockDim.x) {
+    const int a = e % UGROUP, k = e / UGROUP, i = i0 + a;
+    if (i >= nlocal || k >= num[i]) continue;
+    const int j = list[(size_t) k * stride + i];
+    unsigned h = ((unsigned) j * 2654435761u) & (UHASH - 1);
+    for (int probe = 0; probe < UHASH; probe++) {
+      const int old = atomicCAS(&keys[h], -1, j);
+      if (old == -1) {
+        if (atomicAdd(&count, 1) >= UMAX) overflow = 1;
+        break;
+      }
+      if (old == j) break;
+      h = (h + 1) & (UHASH - 1);
+    }
+  }
+  __syncthreads();
+  if (overflow || count > UMAX) {
+    if (threadIdx.x == 0) union_n[g] = -1;
+    return;
+  }
+  if (threadIdx.x == 0) count = 0;
+  __syncthreads();
+  for (int h = threadIdx.x; h < UHASH; h += blockDim.x)
+    if (keys[h] != -1) {
+      const int sl = atomicAdd(&count, 1);
+      vals[h] = sl;
+      union_j[(size_t) g * UMAX + sl] = keys[h];
+    }
+  __syncthreads();
+  if (threadIdx.x == 0) union_n[g] = count;
+  for (int e = threadIdx.x; e < total; e += blockDim.x) {
+    const int a = e % UGROUP, k = e / UGROUP, i = i0 + a;
+    if (i >= nlocal || k >= num[i]) continue;
+    const int j = list[(size_t) k * stride + i];
+    unsigned h = ((unsigned) j * 2654435761u) & (UHASH - 1);
+    for (int probe = 0; probe < UHASH && keys[h] != j; probe++) h = (h + 1) & (UHASH - 1);
+    slot[(size_t) k * stride + i] = (unsigned short) vals[h];
+  }
+}
+
+struct UnionArgs {
+  const int *union_j, *union_n;
+  const unsigned short *slot;  // list entries as union slots
+  unsigned short *sslot;       // short list as union slots (staged groups)
+};
+
+__global__ void __launch_bounds__(UGROUP * UWARPS, 1)
+k_eam_rho_union(AtomArgs a, UnionArgs u, const float4 *__restrict__ rhor_val, int nr, float rdr,
+                const double *__restrict__ frho, int nrho, double rdrho,
+                double *__restrict__ rho, double *__restrict__ fp) {
+  extern __shared__ float4 sm[];
+  float4 *s_val = sm;                                  // nr + 1 knots
+  float4 *sx = sm + (nr + 1) + (threadIdx.x >> 5) * UMAX;  // this warp's union
+  for (int m = threadIdx.x; m <= nr; m += blockDim.x) s_val[m] = rhor_val[m];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int ngroups = (a.nlocal + UGROUP - 1) / UGROUP;
+  for (int g = blockIdx.x * UWARPS + (threadIdx.x >> 5); g < ngroups; g += gridDim.x * UWARPS) {
+    const int nu = u.union_n[g];
+    const int i = g * UGROUP + lane;
+    if (nu >= 0)
+      for (int s = lane; s < nu; s += 32) sx[s] = __ldg(a.xq + u.union_j[(size_t) g * UMAX + s]);
+    __syncwarp();
+    if (i < a.nlocal) {
+      const float4 qi = a.xq[i];
+      int cx, cy, cz;
+      cell_of(qi, cx, cy, cz);
+      const int n = a.num[i];
+      double acc = 0.0;
+      float part = 0.f;
+      int ns = 0, cnt = 0;
+      for (int k = 0; k < n; k++) {
+        int j, sl = 0;
+        float4 qj;
+        if (nu >= 0) {
+          sl = u.slot[(size_t) k * a.stride + i];
+          qj = sx[sl];
+          j = -1;
+        } else {
+          j = __ldg(a.list + (size_t) k * a.stride + i);
+          qj = __ldg(a.xq + j);
+        }
+        float dx, dy, dz;
+        rel_vec(qi, cx, cy, cz, qj, a.qg, dx, dy, dz);
+        float rsq = dx * dx + dy * dy + dz * dz;
+        if (rsq > a.band_hi) continue;
+        if (nu >= 0) u.sslot[(size_t) ns++ * a.stride + i] = (unsigned short) sl;
+        else a.slist[(size_t) ns++ * a.stride + i] = j;
+        bool in = rsq < a.cutsq_f;
+        if (rsq >= a.band_lo) {
+          if (j < 0) j = u.union_j[(size_t) g * UMAX + sl];
+          in = inside64(a.x[i], a.x[j], a.cutsq);
+        }
+        if (in) {
+          float p;
+          int m = findex(sqrtf(rsq), rdr, nr, p);
+          float4 c = s_val[m];
+          part += ((c.x * p + c.y) * p + c.z) * p + c.w;
+          if ((++cnt & (CHUNK - 1)) == 0) {
+            acc += (double) part;
+            part = 0.f;
+          }
+        }
+      }
+      a.snum[i] = ns;
+      acc += (double) part;
+      rho[i] = acc;
+      fp[i] = fprime64(acc, frho, nrho, rdrho);
+    }
+    __syncwarp();  // the union is overwritten by the warp's next group
+  }
+}
+
+__global__ void __launch_bounds__(UGROUP * UWARPS, 1)
+k_eam_force_union(AtomArgs a, UnionArgs u, const float4 *__restrict__ ftab, int nr, float rdr,
+                  const double *__restrict__ fp, double *__restrict__ f) {
+  extern __shared__ float4 sm[];
+  float4 *s_tab = sm;  // 3 float4 per knot
+  float4 *sx = sm + 3 * (nr + 1) + (threadIdx.x >> 5) * UMAX;
+  float *sfp = reinterpret_cast<float *>(sm + 3 * (nr + 1) + UWARPS * UMAX) + (threadIdx.x >> 5) * UMAX;
+  for (int m = threadIdx.x; m < 3 * (nr + 1); m += blockDim.x) s_tab[m] = ftab[m];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int ngroups = (a.nlocal + UGROUP - 1) / UGROUP;
+  for (int g = blockIdx.x * UWARPS + (threadIdx.x >> 5); g < ngroups; g += gridDim.x * UWARPS) {
+    const int nu = u.union_n[g];
+    const int i = g * UGROUP + lane;
+    if (nu >= 0)
+      for (int s = lane; s < nu; s += 32) {
+        const int j = u.union_j[(size_t) g * UMAX + s];
+        sx[s] = __ldg(a.xq + j);
+        sfp[s] = (float) __ldg(fp + j);
+      }
+    __syncwarp();
+    if (i < a.nlocal) {
+      const float4 qi = a.xq[i];
+      int cx, cy, cz;
+      cell_of(qi, cx, cy, cz);
+      const float fpi = (float) fp[i];
+      const int n = a.snum[i];
+      double fx = 0.0, fy = 0.0, fz = 0.0;
+      float px = 0.f, py = 0.f, pz = 0.f;
+      int cnt = 0;
+      for (int k = 0; k < n; k++) {
+        int j = -1, sl = 0;
+        float4 qj;
+        float fpj;
+        if (nu >= 0) {
+          sl = u.sslot[(size_t) k * a.stride + i];
+          qj = sx[sl];
+          fpj = sfp[sl];
+        } else {
+          j = __ldg(a.slist + (size_t) k * a.stride + i);
+          qj = __ldg(a.xq + j);
+          fpj = (float) __ldg(fp + j);
+        }
+        float dx, dy, dz;
+        rel_vec(qi, cx, cy, cz, qj, a.qg, dx, dy, dz);
+        float rsq = dx * dx + dy * dy + dz * dz;
+        bool in = rsq < a.cutsq_f;
+        if (rsq >= a.band_lo && rsq <= a.band_hi) {
+          if (j < 0) j = u.union_j[(size_t) g * UMAX + sl];
+          in = inside64(a.x[i], a.x[j], a.cutsq);
+        }
+        if (in) {
+          float recip = rsqrtf(rsq);
+          float r = rsq * recip;
+          float p;
+          int m = findex(r, rdr, nr, p);
+          float4 t0 = s_tab[3 * m], t1 = s_tab[3 * m + 1], t2 = s_tab[3 * m + 2];
+          float rhoip = (t0.x * p + t0.y) * p + t0.z;
+          float z2p = (t0.w * p + t1.x) * p + t1.y;
+          float z2 = ((t1.z * p + t1.w) * p + t2.x) * p + t2.y;
+          float phi = z2 * recip;
+          float phip = z2p * recip - phi * recip;
+          float psip = (fpi + fpj) * rhoip + phip;
+          float fpair = -psip * recip;
+          px += dx * fpair;
+          py += dy * fpair;
+          pz += dz * fpair;
+          if ((++cnt & (CHUNK - 1)) == 0) {
+            fx += (double) px;
+            fy += (double) py;
+            fz += (double) pz;
+            px = py = pz = 0.f;
+          }
+        }
+      }
+      f[3 * i] = fx + (double) px;
+      f[3 * i + 1] = fy + (double) py;
+      f[3 * i + 2] = fz + (double) pz;
+    }
+    __syncwarp();
   }
 }
 
@@ -637,6 +866,50 @@ void eam_rho_atoms(const MixedAtoms &m, const float4 *rhor_val, const EamTables 
   k_eam_rho_atoms<<<g, m.block, smem, s>>>(a, rhor_val, e.nr, (float) e.rdr, e.frho, e.nrho,
                                        e.rdrho, rho, fp);
   check(cudaGetLastError(), "eam_rho_atoms_mixed");
+}
+
+void union_build(const int *num, const int *list, int stride, int nlocal, int *union_j,
+                 int *union_n, unsigned short *slot, cudaStream_t s) {
+  if (nlocal <= 0) return;
+  k_union_build<<<(nlocal + UGROUP - 1) / UGROUP, 256, 0, s>>>(num, list, stride, nlocal, union_j,
+                                                             union_n, slot);
+  check(cudaGetLastError(), "union_build");
+}
+
+int union_max() { return UMAX; }
+
+static int union_grid(const void *k, size_t smem, int nlocal) {
+  int ngroups = (nlocal + UGROUP - 1) / UGROUP;
+  int need = (ngroups + UWARPS - 1) / UWARPS;
+  return std::min(need, persistent_grid(k, UGROUP * UWARPS, smem, (long long) need * UGROUP * UWARPS));
+}
+
+void eam_rho_union(const MixedAtoms &m, const int *union_j, const int *union_n,
+                   const unsigned short *slot, unsigned short *sslot, const float4 *rhor_val,
+                   const EamTables &e, double *rho, double *fp, cudaStream_t s) {
+  if (m.nlocal <= 0) return;
+  AtomArgs a{m.x, m.xq, m.qg, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
+             m.band_hi, m.cutsq, m.snum, m.slist};
+  UnionArgs u{union_j, union_n, slot, sslot};
+  size_t smem = sizeof(float4) * ((e.nr + 1) + (size_t) UWARPS * UMAX);
+  int g = union_grid((const void *) k_eam_rho_union, smem, m.nlocal);
+  k_eam_rho_union<<<g, UGROUP * UWARPS, smem, s>>>(a, u, rhor_val, e.nr, (float) e.rdr, e.frho,
+                                                  e.nrho, e.rdrho, rho, fp);
+  check(cudaGetLastError(), "eam_rho_union");
+}
+
+void eam_force_union(const MixedAtoms &m, const int *union_j, const int *union_n,
+                     const unsigned short *sslot, const float4 *ftab, const EamTables &e,
+                     const double *fp, double *f, cudaStream_t s) {
+  if (m.nlocal <= 0) return;
+  AtomArgs a{m.x, m.xq, m.qg, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
+             m.band_hi, m.cutsq, m.snum, m.slist};
+  UnionArgs u{union_j, union_n, nullptr, const_cast<unsigned short *>(sslot)};
+  size_t smem = sizeof(float4) * (3 * (size_t) (e.nr + 1) + (size_t) UWARPS * UMAX) +
+                sizeof(float) * (size_t) UWARPS * UMAX;
+  int g = union_grid((const void *) k_eam_force_union, smem, m.nlocal);
+  k_eam_force_union<<<g, UGROUP * UWARPS, smem, s>>>(a, u, ftab, e.nr, (float) e.rdr, fp, f);
+  check(cudaGetLastError(), "eam_force_union");
 }
 
 void eam_force_atoms(const MixedAtoms &m, const float4 *ftab, const EamTables &e,
