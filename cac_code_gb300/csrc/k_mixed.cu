@@ -127,7 +127,8 @@ struct AtomArgs {
   int *snum, *slist;  // short list written by the density pass, read by the force pass
 };
 
-__global__ void __launch_bounds__(512, 2)
+// 40 registers at three 512-thread blocks per SM (48 warps): more gathers in flight
+__global__ void __launch_bounds__(512, 3)
 k_eam_rho_atoms(AtomArgs a, const float4 *__restrict__ rhor_val, int nr, float rdr,
                 const double *__restrict__ frho, int nrho, double rdrho,
                 double *__restrict__ rho, double *__restrict__ fp) {
