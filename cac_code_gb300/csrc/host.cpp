@@ -196,11 +196,15 @@ struct cacg_context {
   // device arrays: atoms
   DBuf<double4> d_x;
   DBuf<float4> d_xh, d_site_h;  // float copies for the FP32 cutoff pre-tests
-  // mixed precision: low parts of the double-single coordinates, element node
-  // offsets, FP32 spline and shape tables
-  DBuf<float4> d_xl, d_rhor_val4, d_ftab, d_site_l;
-  DBuf<float2> d_shape_hl, d_node_hl, d_spa_int_hl;
-  DBuf<float> d_u, d_shape_f, d_ljf, d_site_rho;
+  // mixed precision: FP32 spline tables, double-single element nodes and
+  // integration-point shape functions, packed site positions and site F'(rho),
+  // the referenced sites of each lattice line, lattice sizes per type
+  DBuf<float4> d_xl, d_rhor_val4, d_ftab, d_fp4, d_site_q;
+  DBuf<float2> d_node_hl, d_spa_int_hl;
+  DBuf<float> d_u, d_ljf, d_site_fpf;
+  DBuf<unsigned long long> d_line_mask;
+  DBuf<int> d_nae;
+  int maxlines = 0, max_nax = 0, max_naz = 0;
   DBuf<double> d_cutsq64, d_stage, d_part, d_lj5;
   std::vector<double> h_lj5;
   // regions, groups and post-force fixes (region_block.cpp, region_sphere.cpp,
@@ -286,7 +290,6 @@ struct cacg_context {
   // CUDA graph of a step without a rebuild decision (captured once, replayed
   // until a rebuild, a reallocation or a configuration change)
   int mixed_block = 512;  // threads per block of the mixed persistent kernels ("tune block N")
-  bool mixed_row_filter = true;  // short lists for the mixed element passes ("tune row_filter")
   // neighbor unions staged in shared memory ("tune union yes"): bit-identical
   // to the direct passes; at C2 they run at 8 warps per SM and lose to the
   // direct kernels' 32 (1.71 vs 0.77 ms for the density pass), so off by default
@@ -419,6 +422,20 @@ struct cacg_context {
   void post_force();
   void upload_masks();
   void check_packed_range();
+  // cell-relative packed coordinates of the mixed passes: cells of a
+  // power-of-two size g cover the box, its ghost shell and a margin in
+  // 4096 x 1024 x 1024 cells from the corner l0
+  void pack_grid(double l0[3], double &g) const {
+    double ext[3];
+    const double margin =
+        std::max(cutghost[0], std::max(cutghost[1], cutghost[2])) + max_size + cutneighmax;
+    for (int d = 0; d < 3; d++) {
+      l0[d] = lo[d] - margin;
+      ext[d] = prd[d] + 2.0 * margin;
+    }
+    g = 1.0 / 1024.0;
+    while (ext[0] / g > 4096.0 || ext[1] / g > 1024.0 || ext[2] / g > 1024.0) g *= 2.0;
+  }
   void set_group(const std::string &name, const int *atom_in, const int *elem_in);
   void deform_step();
   void dump_xyz(const char *path);
@@ -445,12 +462,13 @@ cacg_context::~cacg_context() {
   d_rhor_val4.release();
   d_ftab.release();
   d_u.release();
-  d_shape_f.release();
-  d_site_l.release();
-  d_shape_hl.release();
+  d_fp4.release();
+  d_site_q.release();
   d_node_hl.release();
   d_spa_int_hl.release();
-  d_site_rho.release();
+  d_site_fpf.release();
+  d_line_mask.release();
+  d_nae.release();
   d_ljf.release();
   d_cutsq64.release();
   d_stage.release();
@@ -657,7 +675,7 @@ void cacg_context::command(const std::string &raw) {
     run(inumeric(a[0]));
   } else if (c == "tune") {
     // tune block 128|256|512: threads per block of the mixed-precision kernels
-    // tune row_filter yes|no: short lists for the mixed element passes
+    // tune union yes|no: neighbor unions staged in shared memory (EAM atom passes)
     if (a.size() != 2) fail(CACG_EINVAL, "Illegal tune command");
     if (a[0] == "block") {
       int b = inumeric(a[1]);
@@ -666,9 +684,6 @@ void cacg_context::command(const std::string &raw) {
     } else if (a[0] == "union") {
       if (a[1] != "yes" && a[1] != "no") fail(CACG_EINVAL, "tune union takes yes or no");
       mixed_union = a[1] == "yes";
-    } else if (a[0] == "row_filter") {
-      if (a[1] != "yes" && a[1] != "no") fail(CACG_EINVAL, "tune row_filter takes yes or no");
-      mixed_row_filter = a[1] == "yes";
     } else {
       fail(CACG_EINVAL, "Illegal tune command");
     }
@@ -1427,15 +1442,16 @@ void cacg_context::element_tables() {
   upload(d_node_list, node_list, s);
   upload(d_list_isub, list_isub, s);
   upload(d_sub_first, sub_first, s);
-  std::vector<float> shf((size_t) inter_num[1] * NPE);
-  std::vector<float2> shl((size_t) inter_num[1] * NPE);
-  for (size_t k = 0; k < shf.size(); k++) {
-    double v = spa_inter[(size_t) inter_off[1] * NPE + k];
-    shf[k] = (float) v;
-    shl[k] = make_float2((float) v, (float) (v - (double) (float) v));
+  // lattice sizes per type for the mixed site kernels
+  std::vector<int> nae3(3 * (MAXT + 1), 2);
+  maxlines = max_nax = max_naz = 0;
+  for (int t = 1; t <= netypes; t++) {
+    for (int d = 0; d < 3; d++) nae3[3 * t + d] = nae[t][d];
+    maxlines = std::max(maxlines, nae[t][0] * nae[t][1]);
+    max_nax = std::max(max_nax, nae[t][0]);
+    max_naz = std::max(max_naz, nae[t][2]);
   }
-  upload(d_shape_f, shf, s);
-  upload(d_shape_hl, shl, s);
+  upload(d_nae, nae3, s);
   std::vector<float2> sihl(spa_int.size());
   for (size_t k = 0; k < spa_int.size(); k++)
     sihl[k] = make_float2((float) spa_int[k], (float) (spa_int[k] - (double) (float) spa_int[k]));
@@ -1466,8 +1482,14 @@ void cacg_context::mixed_tables() {
       ft[3 * m + 1] = make_float4((float) z[1], (float) z[2], (float) z[3], (float) z[4]);
       ft[3 * m + 2] = make_float4((float) z[5], (float) z[6], 0.f, 0.f);
     }
+    std::vector<float4> f4(nrho + 1);
+    for (int m = 0; m <= nrho; m++) {
+      const double *c = &frho_sp[(size_t) m * 7];
+      f4[m] = make_float4((float) c[0], (float) c[1], (float) c[2], 0.f);
+    }
     upload(d_rhor_val4, val, stream);
     upload(d_ftab, ft, stream);
+    upload(d_fp4, f4, stream);
   }
 }
 
@@ -2015,6 +2037,11 @@ void cacg_context::neighbor_nbuild() {
   fp64_fma::need_compact(d_site_flag.p, d_site_pos.p, nsites, d_site_base.p, nall, d_need.p,
                          d_need_elem.p, s);
   launches += 4;
+  // the same per lattice line, for the mixed site kernels
+  d_line_mask.ensure((size_t) std::max(nall, 1) * std::max(maxlines, 1), s);
+  mixed::line_mask(d_site_flag.p, d_etype.p, d_site_base.p, d_nae.p, nall, maxlines, d_line_mask.p,
+                   s);
+  launches++;
   elists_built = true;
 }
 
@@ -2082,16 +2109,8 @@ void cacg_context::pair_compute_mixed(int pass) {
   m.list = d_list.p;
   m.stride = stride;
   m.nlocal = nlocal;
-  // cell-relative packed coordinates: cells of a power-of-two size g cover
-  // the box, its ghost shell and a margin in 4096 x 1024 x 1024 cells
-  double l0[3], ext[3];
-  const double margin = std::max(cutghost[0], std::max(cutghost[1], cutghost[2])) + max_size + cutneighmax;
-  for (int d = 0; d < 3; d++) {
-    l0[d] = lo[d] - margin;
-    ext[d] = prd[d] + 2.0 * margin;
-  }
-  double g = 1.0 / 1024.0;
-  while (ext[0] / g > 4096.0 || ext[1] / g > 1024.0 || ext[2] / g > 1024.0) g *= 2.0;
+  double l0[3], g;
+  pack_grid(l0, g);
   if (pass == 1) {
     d_xh.ensure(nall, s);
     d_misc.ensure(16, s);
@@ -2153,67 +2172,59 @@ void cacg_context::pair_compute_mixed(int pass) {
   }
 }
 
-// Mixed precision, elements: sites and integration points in double-single
-// FP32 (hi/lo float pairs), FP32 pair terms, FP64 sums and FP64 nodal gather
+// Mixed precision, elements: sites and integration points interpolated in
+// double-single FP32 (hi/lo float pairs) and packed cell-relative, FP32 pair
+// terms, FP64 sums and FP64 nodal gather
 void cacg_context::pair_ecompute_mixed() {
   cudaStream_t s = stream;
   int nall = enlocal + enghost;
   ElemTables t = etab();
-  d_site_h.ensure(std::max(nsites, 1), s);
-  d_site_l.ensure(std::max(nsites, 1), s);
+  double l0[3], g;
+  pack_grid(l0, g);
+  d_misc.ensure(16, s);
+  if (!oob_zeroed) {
+    check(cudaMemsetAsync(d_misc.p + 9, 0, sizeof(int), s), "oob");
+    oob_zeroed = true;
+  }
+  mixed::PackGrid pg{};
+  for (int d = 0; d < 3; d++) {
+    pg.l0h[d] = (float) l0[d];
+    pg.l0l[d] = (float) (l0[d] - (double) pg.l0h[d]);
+  }
+  pg.g = (float) g;
+  pg.ig = (float) (1.0 / g);
+  pg.oob = d_misc.p + 9;
+  d_site_q.ensure(std::max(nsites, 1), s);
   d_node_hl.ensure((size_t) 24 * nall, s);
   mixed::node_split(d_nodex.p, nall, d_node_hl.p, s);
-  mixed::sites_ds_needed(d_node_hl.p, d_site_base.p, d_need.p, d_need_elem.p, nneed, d_shape_hl.p,
-                         d_site_h.p, d_site_l.p, s);
-  // short lists of the rows this step (node rows and rows of nonzero weight)
-  const double csq = pair_style == 1 ? ljtab.cutsq[1 * (MAXT + 1) + 1] : cutforcesq;
-  d_sipnum.ensure(std::max(nrows, 1), s);
-  d_sipent.ensure((size_t) maxip * rowstride, s);
-  const bool use_sur = sur && nfar > 0;
-  if (!mixed_row_filter) {
-    // no short lists: the passes test every list entry themselves
-  } else if (use_sur)  // node rows of every element, force rows of the elements near the atoms
-    fp64_fma::filter_rows(d_nodex.p, d_etype.p, d_row_elem.p, d_row_jj.p, nstatic_rows, d_ipnum.p,
-                          d_ipent.p, rowstride, d_site_h.p, t, cut_pass(csq), 1, d_sipnum.p,
-                          d_sipent.p, s, d_static_rows.p, nullptr);
-  else
-    fp64_fma::filter_rows(d_nodex.p, d_etype.p, d_row_elem.p, d_row_jj.p, nrows, d_ipnum.p, d_ipent.p,
-                          rowstride, d_site_h.p, t, cut_pass(csq), 1, d_sipnum.p, d_sipent.p, s);
+  mixed::site_q(d_node_hl.p, d_etype.p, d_site_base.p, d_nae.p, max_nax, max_naz, d_line_mask.p,
+                maxlines, pg, nall, d_site_q.p, s);
   launches += 2;
-  // the surrogate's verdict for the far elements, then the short lists of the
-  // force rows of those it declined
-  auto far_rows = [&]() {
-    surrogate_predict(eamtab());
-    if (!mixed_row_filter) return;
-    fp64_fma::filter_rows(d_nodex.p, d_etype.p, d_row_elem.p, d_row_jj.p, nfar_rows, d_ipnum.p,
-                          d_ipent.p, rowstride, d_site_h.p, t, cut_pass(csq), 1, d_sipnum.p,
-                          d_sipent.p, s, d_far_rows.p, d_skip.p);
-    launches++;
-  };
-  launches++;
+  const bool use_sur = sur && nfar > 0;
   const float eps = 1.0e-4f;
   mixed::MixedElems m{};
   m.block = mixed_block;
-  m.nodex = d_nodex.p;
-  m.site_h = d_site_h.p;
-  m.site_l = d_site_l.p;
+  m.site_q = d_site_q.p;
   m.etype = d_etype.p;
   m.row_elem = d_row_elem.p;
   m.row_jj = d_row_jj.p;
   m.row_first = d_row_first.p;
-  m.ipnum = mixed_row_filter ? d_sipnum.p : d_ipnum.p;
-  m.ipent = mixed_row_filter ? d_sipent.p : d_ipent.p;
+  m.ipnum = d_ipnum.p;
+  m.ipent = d_ipent.p;
   m.nrows = nrows;
   m.rowstride = rowstride;
   m.nlocal_e = enlocal;
   m.spa_int = d_spa_int.p;
-  m.weight = d_weight.p;
   m.int_off = d_int_off.p;
   m.node_list = d_node_list.p;
   m.rows = d_force_rows.p;
   m.nforce = nforce;
   m.node_hl = d_node_hl.p;
   m.spa_int_hl = d_spa_int_hl.p;
+  m.site_base = d_site_base.p;
+  m.nae = d_nae.p;
+  m.nall_e = nall;
+  m.pg = pg;
   if (use_sur) m.skip = d_skip.p;
   if (pair_style == 1) {
     int a = 1 * (MAXT + 1) + 1;
@@ -2222,7 +2233,7 @@ void cacg_context::pair_ecompute_mixed() {
     m.band_lo = m.cutsq_f * (1.0f - eps);
     m.band_hi = m.cutsq_f * (1.0f + eps);
     EamTables e{};
-    if (use_sur) far_rows();
+    if (use_sur) surrogate_predict(eamtab());
     mixed::ip_pass(m, 0, nullptr, e, (float) ljtab.lj1[a], (float) ljtab.lj2[a], d_fip.p, s);
     launches++;
   } else {
@@ -2232,14 +2243,14 @@ void cacg_context::pair_ecompute_mixed() {
     m.band_lo = m.cutsq_f * (1.0f - eps);
     m.band_hi = m.cutsq_f * (1.0f + eps);
     d_erho.ensure((size_t) NPE * nall, s);
-    d_site_rho.ensure(std::max(nsites, 1), s);
+    d_site_fpf.ensure(std::max(nsites, 1), s);
     mixed::ip_pass(m, 1, d_rhor_val4.p, e, 0.f, 0.f, d_erho.p, s);
     launch_copy_root(d_erho.p, NPE, d_eroot.p, enlocal, enghost, s);
-    mixed::site_rho_needed(d_erho.p, d_site_base.p, d_need.p, d_need_elem.p, nneed, d_shape_f.p,
-                           d_site_rho.p, s);
+    mixed::site_fp(d_erho.p, d_etype.p, d_site_base.p, d_nae.p, d_line_mask.p, maxlines, d_fp4.p,
+                   nrho, rdrho, nall, d_site_fpf.p, s);
     m.erho = d_erho.p;
-    m.site_rho = d_site_rho.p;
-    if (use_sur) far_rows();
+    m.site_fp = d_site_fpf.p;
+    if (use_sur) surrogate_predict(e);
     mixed::ip_pass(m, 2, d_ftab.p, e, 0.f, 0.f, d_fip.p, s);
     launches += 4;
   }
@@ -2681,7 +2692,7 @@ void cacg_context::check_packed_range() {
   if (h_pin[9]) {
     int n = h_pin[9];
     check(cudaMemsetAsync(d_misc.p + 9, 0, sizeof(int), stream), "oob reset");
-    fail(CACG_EINVAL, "%d atoms outside the packed-coordinate range of the mixed passes", n);
+    fail(CACG_EINVAL, "%d atoms or element sites outside the packed-coordinate range of the mixed passes", n);
   }
 }
 

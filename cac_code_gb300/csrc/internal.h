@@ -256,13 +256,21 @@ struct MixedAtoms {
   int *snum, *slist;  // EAM: short list written by the density pass, read by the force pass
   int block = 512;    // threads per block of the persistent grids (autotuned)
 };
+// The packing grid of the cell-relative coordinates: cells of a power-of-two
+// size g from the corner l0 (split into double-single floats); *oob counts
+// positions outside the 4096 x 1024 x 1024-cell range.
+struct PackGrid {
+  float l0h[3], l0l[3];
+  float g, ig;
+  int *oob;
+};
 struct MixedElems {
-  const double *nodex, *erho;
-  const float4 *site_h, *site_l;  // double-single site positions of this step
-  const float *site_rho;          // FP32 site densities (EAM force pass)
+  const double *erho;
+  const float4 *site_q;  // packed site positions of this step (referenced sites)
+  const float *site_fp;  // FP32 F'(rho) at the referenced sites (EAM force pass)
   const int *etype, *row_elem, *row_jj, *row_first, *ipnum, *ipent;
   int nrows, rowstride, nlocal_e;
-  const double *spa_int, *weight;
+  const double *spa_int;
   const int *int_off, *node_list;
   const int *rows;  // rows of nonzero weight (force passes), count nforce
   int nforce;
@@ -271,24 +279,28 @@ struct MixedElems {
   const float2 *node_hl;     // [nall][24] double-single node coordinates
   const float2 *spa_int_hl;  // double-single integration-point shape functions
   const unsigned char *skip = nullptr;  // elements whose forces come from the surrogate
-  int block = 512;                      // threads per block of the persistent grids
+  const int *site_base, *nae;           // site offsets per element; lattice sizes per type
+  int nall_e;
+  PackGrid pg;
+  int block = 512;  // threads per block of the persistent grids
 };
-void split_hilo(const double4 *x, float4 *xh, float4 *xl, int n, cudaStream_t s);
 // cell-relative packed coordinates for the atom passes; *oob counts atoms
 // outside the 4096 x 1024 x 1024-cell range
 void pack_rel(const double4 *x, int n, double l0x, double l0y, double l0z, double g,
               float4 *xq, int *oob, cudaStream_t s);
-void sites_ds(const double *nodex, const int *etype, const int *site_base, const int *inter_num,
-              const float2 *shape_hl, int nelem, float4 *site_h, float4 *site_l, cudaStream_t s);
-void site_rho(const double *erho, const int *etype, const int *site_base, const int *inter_num,
-              const float *shape, int nelem, float *rho, cudaStream_t s);
 void node_split(const double *nodex, int n, float2 *hl, cudaStream_t s);
-void sites_ds_needed(const float2 *node_hl, const int *site_base, const int *need,
-                     const int *need_elem, int nneed, const float2 *shape_hl, float4 *site_h,
-                     float4 *site_l, cudaStream_t s);
-void site_rho_needed(const double *erho, const int *site_base, const int *need,
-                     const int *need_elem, int nneed, const float *shape, float *rho,
-                     cudaStream_t s);
+// per element and lattice line (ii, jj): bit kk set when site (ii, jj, kk) is
+// referenced by an integration-point list
+void line_mask(const int *flag, const int *etype, const int *site_base, const int *nae, int nelem,
+               int maxlines, unsigned long long *mask, cudaStream_t s);
+// packed positions of the referenced sites (double-single interpolation)
+void site_q(const float2 *node_hl, const int *etype, const int *site_base, const int *nae,
+            int max_nax, int max_naz, const unsigned long long *mask, int maxlines,
+            const PackGrid &pg, int nelem, float4 *q, cudaStream_t s);
+// FP32 F'(rho) at the referenced sites; fp4 holds F' coefficients c0..c2 per knot
+void site_fp(const double *erho, const int *etype, const int *site_base, const int *nae,
+             const unsigned long long *mask, int maxlines, const float4 *fp4, int nrho,
+             double rdrho, int nelem, float *fp, cudaStream_t s);
 // neighbor unions of 32-atom groups staged in shared memory (EAM atom passes)
 int union_max();
 void union_build(const int *num, const int *list, int stride, int nlocal, int *union_j,

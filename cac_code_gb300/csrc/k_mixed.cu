@@ -56,16 +56,6 @@ __device__ __forceinline__ bool inside64(const double4 &a, const double4 &b, dou
   return dx * dx + dy * dy + dz * dz < cutsq;
 }
 
-__global__ void k_split_hilo(const double4 *__restrict__ x, float4 *__restrict__ xh,
-                             float4 *__restrict__ xl, int n) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  double4 p = x[i];
-  float hx = (float) p.x, hy = (float) p.y, hz = (float) p.z;
-  xh[i] = make_float4(hx, hy, hz, 0.f);
-  xl[i] = make_float4((float) (p.x - hx), (float) (p.y - hy), (float) (p.z - hz), 0.f);
-}
-
 __global__ void k_pack_rel(const double4 *__restrict__ x, int n, double l0x, double l0y,
                            double l0z, double g, double ig, float4 *__restrict__ xq,
                            int *__restrict__ oob) {
@@ -107,13 +97,6 @@ __device__ __forceinline__ void rel_vec(const float4 &qi, int cx, int cy, int cz
   dx = (qi.x - qj.x) + g * (float) (cx - jx);
   dy = (qi.y - qj.y) + g * (float) (cy - jy);
   dz = (qi.z - qj.z) + g * (float) (cz - jz);
-}
-
-__device__ __forceinline__ void pair_vec(const float4 &hi, const float4 &li, const float4 &hj,
-                                         const float4 &lj, float &dx, float &dy, float &dz) {
-  dx = (hi.x - hj.x) + (li.x - lj.x);
-  dy = (hi.y - hj.y) + (li.y - lj.y);
-  dz = (hi.z - hj.z) + (li.z - lj.z);
 }
 
 struct AtomArgs {
@@ -525,145 +508,263 @@ k_lj_atoms(AtomArgs a, const int *__restrict__ type, const float *__restrict__ l
 
 // ---------------------------------------------------------------- elements
 //
-// Sites are computed once per step in double-single FP32 arithmetic (a value is
-// an unevaluated sum hi + lo of two floats; products and sums use error-free
-// transformations: TwoProduct via fma and Knuth's TwoSum), so a site carries
-// ~44 bits from the FP64 nodes without a single FP64 instruction per site.
+// Element sites are computed once per step in double-single FP32 arithmetic (a
+// value is an unevaluated sum hi + lo of two floats; products and sums use
+// error-free transformations: TwoProduct via fma and Knuth's TwoSum), so a site
+// carries ~44 bits from the FP64 nodes without a single FP64 instruction per
+// site, and is stored in the same cell-relative packed form as the atoms
+// (16 bytes a site).  The trilinear map of an element is evaluated as lerps:
+// along x per lattice column, along y per lattice line, and along z per site
+// (x(i,j,k) = U(i,j) + c_k D(i,j)), so a site costs three double-single
+// multiply-adds.
 
-__device__ __forceinline__ void ds_split(double x, float &h, float &l) {
-  h = (float) x;
-  l = (float) (x - (double) h);
+struct ds {
+  float h, l;
+};
+
+// fast TwoSum (|s| >= |e|)
+__device__ __forceinline__ ds ds_renorm(float s, float e) {
+  const float h = __fadd_rn(s, e);
+  return ds{h, __fsub_rn(e, __fsub_rn(h, s))};
 }
 
-// (ah, al) += (bh + bl) * (ch + cl), dropping bl*cl
-__device__ __forceinline__ void ds_acc_prod(float &ah, float &al, float bh, float bl, float ch,
-                                            float cl) {
-  float p = __fmul_rn(bh, ch);
-  float e = __fmaf_rn(bh, ch, -p);
-  e = __fmaf_rn(bh, cl, e);
-  e = __fmaf_rn(bl, ch, e);
-  float s = __fadd_rn(ah, p);
-  float v = __fsub_rn(s, ah);
-  float err = __fadd_rn(__fsub_rn(ah, __fsub_rn(s, v)), __fsub_rn(p, v));
-  al = __fadd_rn(al, __fadd_rn(e, err));
-  ah = s;
+__device__ __forceinline__ ds ds_add(ds a, ds b) {
+  const float s = __fadd_rn(a.h, b.h);
+  const float v = __fsub_rn(s, a.h);
+  float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, v)), __fsub_rn(b.h, v));
+  e = __fadd_rn(e, __fadd_rn(a.l, b.l));
+  return ds_renorm(s, e);
 }
 
-__device__ __forceinline__ void ds_norm(float &h, float &l) {
-  float s = __fadd_rn(h, l);
-  l = __fsub_rn(l, __fsub_rn(s, h));
-  h = s;
+__device__ __forceinline__ ds ds_sub(ds a, ds b) { return ds_add(a, ds{-b.h, -b.l}); }
+
+// x + a * d, dropping a.l * d.l
+__device__ __forceinline__ ds ds_madd(ds a, ds d, ds x) {
+  const float p = __fmul_rn(a.h, d.h);
+  float pe = __fmaf_rn(a.h, d.h, -p);
+  pe = __fmaf_rn(a.h, d.l, pe);
+  pe = __fmaf_rn(a.l, d.h, pe);
+  return ds_add(x, ds{p, pe});
 }
 
-// one block per element: nodes split into double-single once, then every site
-// of the element interpolated in double-single; also writes the per-site
-// element index used by the density interpolation
-__global__ void k_sites_ds(const double *__restrict__ nodex, const int *__restrict__ etype,
-                           const int *__restrict__ site_base, const int *__restrict__ inter_num,
-                           const float2 *__restrict__ shape_hl, float4 *__restrict__ site_h,
-                           float4 *__restrict__ site_l) {
-  __shared__ float nh[24], nl[24];
-  const int e = blockIdx.x;
-  if (threadIdx.x < 24) ds_split(nodex[24 * (size_t) e + threadIdx.x], nh[threadIdx.x], nl[threadIdx.x]);
-  __syncthreads();
-  const int nint = inter_num[etype[e]];
-  const int base = site_base[e];
-  for (int nj = threadIdx.x; nj < nint; nj += blockDim.x) {
-    const float2 *S = shape_hl + (size_t) nj * NPE;
-    float xh = 0.f, xl = 0.f, yh = 0.f, yl = 0.f, zh = 0.f, zl = 0.f;
-#pragma unroll
-    for (int k = 0; k < NPE; k++) {
-      float2 w = S[k];
-      ds_acc_prod(xh, xl, w.x, w.y, nh[3 * k], nl[3 * k]);
-      ds_acc_prod(yh, yl, w.x, w.y, nh[3 * k + 1], nl[3 * k + 1]);
-      ds_acc_prod(zh, zl, w.x, w.y, nh[3 * k + 2], nl[3 * k + 2]);
-    }
-    ds_norm(xh, xl);
-    ds_norm(yh, yl);
-    ds_norm(zh, zl);
-    site_h[base + nj] = make_float4(xh, yh, zh, 0.f);
-    site_l[base + nj] = make_float4(xl, yl, zl, 0.f);
-  }
+__device__ __forceinline__ ds ds_lerp(ds x, ds y, ds a) { return ds_madd(a, ds_sub(y, x), x); }
+
+// k / d as a double-single: the correctly rounded quotient and its remainder,
+// which one fma gives exactly
+__device__ __forceinline__ ds ds_frac(int k, int d) {
+  if (d <= 0) return ds{0.f, 0.f};
+  const float fk = (float) k, fd = (float) d;
+  const float q = __fdiv_rn(fk, fd);
+  const float r = __fmaf_rn(-q, fd, fk);
+  return ds{q, __fdiv_rn(r, fd)};
 }
 
 // node coordinates as double-single pairs, once per element and step
 __global__ void k_node_split(const double *__restrict__ nodex, int n, float2 *__restrict__ hl) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * 24) return;
-  float h, l;
-  ds_split(nodex[t], h, l);
-  hl[t] = make_float2(h, l);
+  const double x = nodex[t];
+  const float h = (float) x;
+  hl[t] = make_float2(h, (float) (x - (double) h));
 }
 
-// double-single positions of the needed sites only (one thread per site)
-__global__ void k_sites_ds_needed(const float2 *__restrict__ node_hl,
-                                  const int *__restrict__ site_base, const int *__restrict__ need,
-                                  const int *__restrict__ need_elem, int nneed,
-                                  const float2 *__restrict__ shape_hl,
-                                  float4 *__restrict__ site_h, float4 *__restrict__ site_l) {
-  int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= nneed) return;
-  const int sid = need[q], j = need_elem[q];
-  const int nj = sid - site_base[j];
-  const float2 *S = shape_hl + (size_t) nj * NPE;
-  const float2 *nx = node_hl + 24 * (size_t) j;
-  float xh = 0.f, xl = 0.f, yh = 0.f, yl = 0.f, zh = 0.f, zl = 0.f;
-#pragma unroll
-  for (int k = 0; k < NPE; k++) {
-    float2 w = S[k];
-    float2 a = __ldg(nx + 3 * k), b = __ldg(nx + 3 * k + 1), c = __ldg(nx + 3 * k + 2);
-    ds_acc_prod(xh, xl, w.x, w.y, a.x, a.y);
-    ds_acc_prod(yh, yl, w.x, w.y, b.x, b.y);
-    ds_acc_prod(zh, zl, w.x, w.y, c.x, c.y);
+__device__ __forceinline__ ds node_ds(const float2 *nx, int k, int d) {
+  const float2 v = nx[3 * k + d];
+  return ds{v.x, v.y};
+}
+
+// Packing of a double-single offset u = x - l0 into (cell, rel): the cell
+// index floor(u.h / g) is exact (g a power of two), u.h - k g is exact
+// (Sterbenz), so rel = (u.h - k g) + u.l is rounded once.
+__device__ __forceinline__ float rel_of(ds u, float g, float ig, int lim, int &k, bool &bad) {
+  k = (int) floorf(__fmul_rn(u.h, ig));
+  if (k < 0 || k > lim) {
+    bad = true;
+    k = k < 0 ? 0 : lim;
   }
-  ds_norm(xh, xl);
-  ds_norm(yh, yl);
-  ds_norm(zh, zl);
-  site_h[sid] = make_float4(xh, yh, zh, 0.f);
-  site_l[sid] = make_float4(xl, yl, zl, 0.f);
+  return __fadd_rn(__fsub_rn(u.h, __fmul_rn((float) k, g)), u.l);
 }
 
-__global__ void k_site_rho_needed(const double *__restrict__ erho,
-                                  const int *__restrict__ site_base, const int *__restrict__ need,
-                                  const int *__restrict__ need_elem, int nneed,
-                                  const float *__restrict__ shape, float *__restrict__ site_rho) {
-  int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= nneed) return;
-  const int sid = need[q], j = need_elem[q];
-  const float *S = shape + (size_t) (sid - site_base[j]) * NPE;
-  const double *er = erho + NPE * (size_t) j;
-  float r = 0.f;
+__device__ __forceinline__ float4 pack_u(ds ux, ds uy, ds uz, const PackGrid &pg) {
+  int cx, cy, cz;
+  bool bad = false;
+  const float rx = rel_of(ux, pg.g, pg.ig, 4095, cx, bad);
+  const float ry = rel_of(uy, pg.g, pg.ig, 1023, cy, bad);
+  const float rz = rel_of(uz, pg.g, pg.ig, 1023, cz, bad);
+  if (bad && pg.oob) atomicAdd(pg.oob, 1);
+  return make_float4(rx, ry, rz, __int_as_float(cx | (cy << 12) | (cz << 22)));
+}
+
+// the x-lerps of one lattice column ii: E0..E3 of the y/z edges (-,-), (+,-), (-,+), (+,+)
+__device__ __forceinline__ void column_ds(const float2 *nx, ds a, int d, ds (&E)[4]) {
+  E[0] = ds_lerp(node_ds(nx, 0, d), node_ds(nx, 1, d), a);
+  E[1] = ds_lerp(node_ds(nx, 3, d), node_ds(nx, 2, d), a);
+  E[2] = ds_lerp(node_ds(nx, 4, d), node_ds(nx, 5, d), a);
+  E[3] = ds_lerp(node_ds(nx, 7, d), node_ds(nx, 6, d), a);
+}
+
+// site (ii, jj, kk) of an element in double-single, by the same lerps as the
+// site kernel (the guard-band path of the integration-point passes)
+__device__ __forceinline__ void site_ds(const float2 *nx, int ii, int jj, int kk, int nax, int nay,
+                                        int naz, ds (&x)[3]) {
+  const ds a = ds_frac(ii, nax - 1), b = ds_frac(jj, nay - 1), c = ds_frac(kk, naz - 1);
 #pragma unroll
-  for (int k = 0; k < NPE; k++) r += S[k] * (float) er[k];
-  site_rho[sid] = r;
+  for (int d = 0; d < 3; d++) {
+    ds E[4];
+    column_ds(nx, a, d, E);
+    const ds B = ds_lerp(E[0], E[1], b), T = ds_lerp(E[2], E[3], b);
+    x[d] = ds_madd(c, ds_sub(T, B), B);
+  }
 }
 
-// density at every site, rho_s = sum_k N_k erho_k (FP32; pair_eam.cpp:1060-1065)
-__global__ void k_site_rho(const double *__restrict__ erho, const int *__restrict__ etype,
-                           const int *__restrict__ site_base, const int *__restrict__ inter_num,
-                           const float *__restrict__ shape, float *__restrict__ site_rho) {
-  __shared__ float er[NPE];
+// Lines (ii, jj) of an element whose sites any integration-point list
+// references: bit kk of the mask (sites kk >= 64 are always computed).
+__global__ void k_line_mask(const int *__restrict__ flag, const int *__restrict__ etype,
+                            const int *__restrict__ site_base, const int *__restrict__ nae,
+                            int nelem, int maxlines, unsigned long long *__restrict__ mask) {
+  const long long t = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long) nelem * maxlines) return;
+  const int e = (int) (t / maxlines), L = (int) (t % maxlines);
+  const int ty = etype[e];
+  const int nlines = nae[3 * ty] * nae[3 * ty + 1], naz = nae[3 * ty + 2];
+  unsigned long long m = 0;
+  if (L < nlines) {
+    const int *f = flag + site_base[e] + (size_t) L * naz;
+    for (int kk = 0; kk < naz && kk < 64; kk++)
+      if (f[kk]) m |= 1ull << kk;
+  }
+  mask[t] = m;
+}
+
+// Site positions of this step, packed; one block per element.  The element's
+// lines are taken LCH at a time: their start U = x(i,j,0) - l0 and step
+// D = x(i,j,nz-1) - x(i,j,0) go to shared memory, then the block's threads run
+// over the lines' sites in storage order, so the stores coalesce.
+constexpr int LCH = 128;
+
+__global__ void __launch_bounds__(LCH)
+k_site_q(const float2 *__restrict__ node_hl, const int *__restrict__ etype,
+         const int *__restrict__ site_base, const int *__restrict__ nae,
+         const unsigned long long *__restrict__ line_mask, int maxlines, PackGrid pg,
+         float4 *__restrict__ site_q) {
+  extern __shared__ ds s_mem[];
+  __shared__ float2 s_nx[24];
+  __shared__ unsigned long long s_mask[LCH];
   const int e = blockIdx.x;
-  if (threadIdx.x < NPE) er[threadIdx.x] = (float) erho[NPE * (size_t) e + threadIdx.x];
+  const int ty = etype[e];
+  const int nax = nae[3 * ty], nay = nae[3 * ty + 1], naz = nae[3 * ty + 2];
+  ds *s_E = s_mem;                 // [nax][3][4]
+  ds *s_U = s_E + 12 * nax;        // [LCH][3]
+  ds *s_D = s_U + 3 * LCH;         // [LCH][3]
+  ds *s_c = s_D + 3 * LCH;         // [naz]
+  if (threadIdx.x < 24) s_nx[threadIdx.x] = node_hl[24 * (size_t) e + threadIdx.x];
+  for (int k = threadIdx.x; k < naz; k += blockDim.x) s_c[k] = ds_frac(k, naz - 1);
   __syncthreads();
-  const int nint = inter_num[etype[e]];
-  const int base = site_base[e];
-  for (int nj = threadIdx.x; nj < nint; nj += blockDim.x) {
-    const float *S = shape + (size_t) nj * NPE;
-    float r = 0.f;
+  for (int q = threadIdx.x; q < 3 * nax; q += blockDim.x) {
+    const int ii = q / 3, d = q % 3;
+    ds E[4];
+    column_ds(s_nx, ds_frac(ii, nax - 1), d, E);
 #pragma unroll
-    for (int k = 0; k < NPE; k++) r += S[k] * er[k];
-    site_rho[base + nj] = r;
+    for (int w = 0; w < 4; w++) s_E[(ii * 3 + d) * 4 + w] = E[w];
+  }
+  const ds l0[3] = {{pg.l0h[0], pg.l0l[0]}, {pg.l0h[1], pg.l0l[1]}, {pg.l0h[2], pg.l0l[2]}};
+  const int nlines = nax * nay, base = site_base[e];
+  const unsigned long long *lm = line_mask + (size_t) e * maxlines;
+  for (int L0 = 0; L0 < nlines; L0 += LCH) {
+    const int nl = min(LCH, nlines - L0);
+    __syncthreads();  // s_E ready; the previous chunk's lines consumed
+    if (threadIdx.x < nl) {
+      const int L = L0 + threadIdx.x;
+      const unsigned long long mk = lm[L];
+      s_mask[threadIdx.x] = mk;
+      if (mk || naz > 64) {
+        const int ii = L / nay, jj = L % nay;
+        const ds b = ds_frac(jj, nay - 1);
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          const ds *E = s_E + (ii * 3 + d) * 4;
+          const ds B = ds_lerp(E[0], E[1], b), T = ds_lerp(E[2], E[3], b);
+          s_U[threadIdx.x * 3 + d] = ds_sub(B, l0[d]);
+          s_D[threadIdx.x * 3 + d] = ds_sub(T, B);
+        }
+      }
+    }
+    __syncthreads();
+    const int nsite = nl * naz;
+    for (int t = threadIdx.x; t < nsite; t += blockDim.x) {
+      const int l = t / naz, kk = t - l * naz;
+      if (kk < 64 && !((s_mask[l] >> kk) & 1ull)) continue;
+      const ds c = s_c[kk];
+      const ds *U = s_U + 3 * l, *D = s_D + 3 * l;
+      site_q[base + (size_t) L0 * naz + t] =
+          pack_u(ds_madd(c, D[0], U[0]), ds_madd(c, D[1], U[1]), ds_madd(c, D[2], U[2]), pg);
+    }
+  }
+}
+
+__device__ __forceinline__ float fprime32(float rho, const float4 *__restrict__ fp4, int nrho,
+                                          float rdrho) {
+  float p = rho * rdrho + 1.0f;
+  int m = (int) p;
+  m = m < nrho - 1 ? m : nrho - 1;
+  m = 1 > m ? 1 : m;
+  p -= (float) m;
+  p = fminf(p, 1.0f);
+  const float4 c = __ldg(fp4 + m);
+  return (c.x * p + c.y) * p + c.z;
+}
+
+// F'(rho) at the referenced sites, rho = sum_k N_k erho_k (pair_eam.cpp:1060-1065)
+// by the same lerps in FP32; one block per element, lines LCH at a time.
+__global__ void __launch_bounds__(LCH)
+k_site_fp(const double *__restrict__ erho, const int *__restrict__ etype,
+          const int *__restrict__ site_base, const int *__restrict__ nae,
+          const unsigned long long *__restrict__ line_mask, int maxlines,
+          const float4 *__restrict__ fp4, int nrho, float rdrho, float *__restrict__ site_fp) {
+  __shared__ float s_er[NPE];
+  __shared__ float s_U[LCH], s_D[LCH];
+  __shared__ unsigned long long s_mask[LCH];
+  const int e = blockIdx.x;
+  const int ty = etype[e];
+  const int nax = nae[3 * ty], nay = nae[3 * ty + 1], naz = nae[3 * ty + 2];
+  if (threadIdx.x < NPE) s_er[threadIdx.x] = (float) erho[NPE * (size_t) e + threadIdx.x];
+  const int nlines = nax * nay, base = site_base[e];
+  const unsigned long long *lm = line_mask + (size_t) e * maxlines;
+  const float rz = naz > 1 ? 1.0f / (float) (naz - 1) : 0.f;
+  for (int L0 = 0; L0 < nlines; L0 += LCH) {
+    const int nl = min(LCH, nlines - L0);
+    __syncthreads();
+    if (threadIdx.x < nl) {
+      const int L = L0 + threadIdx.x;
+      const unsigned long long mk = lm[L];
+      s_mask[threadIdx.x] = mk;
+      const int ii = L / nay, jj = L % nay;
+      const float a = nax > 1 ? (float) ii / (float) (nax - 1) : 0.f;
+      const float b = nay > 1 ? (float) jj / (float) (nay - 1) : 0.f;
+      const float e0 = s_er[0] + a * (s_er[1] - s_er[0]), e1 = s_er[3] + a * (s_er[2] - s_er[3]);
+      const float e2 = s_er[4] + a * (s_er[5] - s_er[4]), e3 = s_er[7] + a * (s_er[6] - s_er[7]);
+      const float B = e0 + b * (e1 - e0), T = e2 + b * (e3 - e2);
+      s_U[threadIdx.x] = B;
+      s_D[threadIdx.x] = T - B;
+    }
+    __syncthreads();
+    const int nsite = nl * naz;
+    for (int t = threadIdx.x; t < nsite; t += blockDim.x) {
+      const int l = t / naz, kk = t - l * naz;
+      if (kk < 64 && !((s_mask[l] >> kk) & 1ull)) continue;
+      const float rho = s_U[l] + ((float) kk * rz) * s_D[l];
+      site_fp[base + (size_t) L0 * naz + t] = fprime32(rho, fp4, nrho, rdrho);
+    }
   }
 }
 
 struct ElemArgs {
-  const double *nodex, *erho;
-  const float4 *site_h, *site_l;
-  const float *site_rho;
+  const double *erho;
+  const float4 *site_q;  // packed site positions of this step
+  const float *site_fp;  // F'(rho) at the sites (EAM force pass)
   const int *etype, *row_elem, *row_jj, *row_first, *ipnum, *ipent;
   int nrows, rowstride, nlocal_e;
-  const double *spa_int, *weight;
+  const double *spa_int;
   const int *int_off, *node_list;
   const int *rows;
   int nforce;
@@ -671,30 +772,55 @@ struct ElemArgs {
   double cutsq;
   const float2 *node_hl, *spa_int_hl;
   const unsigned char *skip;
+  const int *site_base, *nae;
+  int nall_e;
+  PackGrid pg;
 };
 
 // integration-point position in double-single from the split nodes and the
 // split integration-point shape functions
 __device__ __forceinline__ void ip_ds(const float2 *__restrict__ N, const float2 *__restrict__ nx,
-                                      float4 &h, float4 &l) {
-  float xh = 0.f, xl = 0.f, yh = 0.f, yl = 0.f, zh = 0.f, zl = 0.f;
+                                      ds (&x)[3]) {
 #pragma unroll
-  for (int k = 0; k < NPE; k++) {
-    float2 w = N[k];
-    float2 a = nx[3 * k], b = nx[3 * k + 1], c = nx[3 * k + 2];
-    ds_acc_prod(xh, xl, w.x, w.y, a.x, a.y);
-    ds_acc_prod(yh, yl, w.x, w.y, b.x, b.y);
-    ds_acc_prod(zh, zl, w.x, w.y, c.x, c.y);
+  for (int d = 0; d < 3; d++) {
+    float h = 0.f, l = 0.f;
+#pragma unroll
+    for (int k = 0; k < NPE; k++) {
+      const float2 w = N[k], c = nx[3 * k + d];
+      // (h, l) += (w.x + w.y) * (c.x + c.y), dropping w.y * c.y
+      const float p = __fmul_rn(w.x, c.x);
+      float e = __fmaf_rn(w.x, c.x, -p);
+      e = __fmaf_rn(w.x, c.y, e);
+      e = __fmaf_rn(w.y, c.x, e);
+      const float s = __fadd_rn(h, p);
+      const float v = __fsub_rn(s, h);
+      const float err = __fadd_rn(__fsub_rn(h, __fsub_rn(s, v)), __fsub_rn(p, v));
+      l = __fadd_rn(l, __fadd_rn(e, err));
+      h = s;
+    }
+    x[d] = ds_renorm(h, l);
   }
-  ds_norm(xh, xl);
-  ds_norm(yh, yl);
-  ds_norm(zh, zl);
-  h = make_float4(xh, yh, zh, 0.f);
-  l = make_float4(xl, yl, zl, 0.f);
+}
+
+// the site's double-single position, from its owning element (guard band only)
+__device__ __noinline__ void site_ds_of(const ElemArgs &a, int sid, ds (&x)[3]) {
+  int lo = 0, hi = a.nall_e;  // site_base[lo] <= sid < site_base[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(a.site_base + mid) <= sid) lo = mid;
+    else hi = mid;
+  }
+  const int ty = a.etype[lo];
+  const int nax = a.nae[3 * ty], nay = a.nae[3 * ty + 1], naz = a.nae[3 * ty + 2];
+  const int nj = sid - a.site_base[lo];
+  const int kk = nj % naz, L = nj / naz;
+  site_ds(a.node_hl + 24 * (size_t) lo, L / nay, L % nay, kk, nax, nay, naz, x);
 }
 
 // One thread per integration point.  DENSITY: node rows -> erho (EAM);
-// otherwise rows of nonzero weight -> forces (LJ or EAM).
+// otherwise rows of nonzero weight -> forces (LJ or EAM).  Every entry of the
+// row's list is tested: a 16-byte gather of the packed site, the FP32 cutoff
+// test, and in the guard band the FP64 test on the double-single positions.
 template <bool EAM, bool DENSITY>
 __global__ void __launch_bounds__(512, 2)
 k_ip(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr,
@@ -704,6 +830,9 @@ k_ip(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr,
   const int ntab = EAM ? (DENSITY ? (nr + 1) : 3 * (nr + 1)) : 0;
   for (int m = threadIdx.x; m < ntab; m += blockDim.x) s_tab[m] = tab[m];
   __syncthreads();
+  const float g = a.pg.g;
+  const ds l0[3] = {{a.pg.l0h[0], a.pg.l0l[0]}, {a.pg.l0h[1], a.pg.l0l[1]},
+                    {a.pg.l0h[2], a.pg.l0l[2]}};
   const int nitems = DENSITY ? a.nlocal_e * NPE : a.nforce;
   for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < nitems; it += gridDim.x * blockDim.x) {
     int r, e, ty, jj;
@@ -720,8 +849,12 @@ k_ip(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr,
       jj = a.row_jj[r];
     }
     const double *N64 = a.spa_int + ((size_t) a.int_off[ty] + jj) * NPE;
-    float4 ih, il;
-    ip_ds(a.spa_int_hl + ((size_t) a.int_off[ty] + jj) * NPE, a.node_hl + 24 * (size_t) e, ih, il);
+    ds ix[3];
+    ip_ds(a.spa_int_hl + ((size_t) a.int_off[ty] + jj) * NPE, a.node_hl + 24 * (size_t) e, ix);
+    const float4 qi =
+        pack_u(ds_sub(ix[0], l0[0]), ds_sub(ix[1], l0[1]), ds_sub(ix[2], l0[2]), a.pg);
+    int cx, cy, cz;
+    cell_of(qi, cx, cy, cz);
     double fpi = 0.0;
     if (EAM && !DENSITY) {
       double rhoi = 0.0;
@@ -733,28 +866,32 @@ k_ip(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr,
     float part = 0.f, px = 0.f, py = 0.f, pz = 0.f;
     const int n = a.ipnum[r];
     int sn = 0;
-    float4 shn = ih, sln = il;
+    float4 qn = qi;
+    float fpn = 0.f;
     if (n > 0) {
       sn = __ldg(a.ipent + r);
-      shn = __ldg(a.site_h + sn);
-      sln = __ldg(a.site_l + sn);
+      qn = __ldg(a.site_q + sn);
+      if (EAM && !DENSITY) fpn = __ldg(a.site_fp + sn);
     }
     for (int k = 0; k < n; k++) {
       const int sid = sn;
-      const float4 sh = shn, sl = sln;
+      const float4 qj = qn;
+      const float fpj = fpn;
       if (k + 1 < n) {  // next site's gathers in flight during this one
         sn = __ldg(a.ipent + (size_t) (k + 1) * a.rowstride + r);
-        shn = __ldg(a.site_h + sn);
-        sln = __ldg(a.site_l + sn);
+        qn = __ldg(a.site_q + sn);
+        if (EAM && !DENSITY) fpn = __ldg(a.site_fp + sn);
       }
       float dx, dy, dz;
-      pair_vec(ih, il, sh, sl, dx, dy, dz);
+      rel_vec(qi, cx, cy, cz, qj, g, dx, dy, dz);
       float rsq = dx * dx + dy * dy + dz * dz;
       bool in = rsq < a.cutsq_f;
       if (rsq >= a.band_lo && rsq <= a.band_hi) {
-        double ddx = ((double) ih.x + il.x) - ((double) sh.x + sl.x);
-        double ddy = ((double) ih.y + il.y) - ((double) sh.y + sl.y);
-        double ddz = ((double) ih.z + il.z) - ((double) sh.z + sl.z);
+        ds sx[3];
+        site_ds_of(a, sid, sx);
+        double ddx = ((double) ix[0].h + ix[0].l) - ((double) sx[0].h + sx[0].l);
+        double ddy = ((double) ix[1].h + ix[1].l) - ((double) sx[1].h + sx[1].l);
+        double ddz = ((double) ix[2].h + ix[2].l) - ((double) sx[2].h + sx[2].l);
         in = ddx * ddx + ddy * ddy + ddz * ddz < a.cutsq;
       }
       if (in) {
@@ -767,7 +904,6 @@ k_ip(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr,
             float4 c = s_tab[m];
             part += ((c.x * p + c.y) * p + c.z) * p + c.w;
           } else {
-            float fpj = (float) fprime64((double) __ldg(a.site_rho + sid), frho, nrho, rdrho);
             float4 t0 = s_tab[3 * m], t1 = s_tab[3 * m + 1], t2 = s_tab[3 * m + 2];
             float rhoip = (t0.x * p + t0.y) * p + t0.z;
             float z2p = (t0.w * p + t1.x) * p + t1.y;
@@ -851,12 +987,6 @@ void pack_rel(const double4 *x, int n, double l0x, double l0y, double l0z, doubl
   check(cudaGetLastError(), "pack_rel");
 }
 
-void split_hilo(const double4 *x, float4 *xh, float4 *xl, int n, cudaStream_t s) {
-  if (n <= 0) return;
-  k_split_hilo<<<nblk(n, 256), 256, 0, s>>>(x, xh, xl, n);
-  check(cudaGetLastError(), "split_hilo");
-}
-
 void eam_rho_atoms(const MixedAtoms &m, const float4 *rhor_val, const EamTables &e,
                    double *rho, double *fp, cudaStream_t s) {
   if (m.nlocal <= 0) return;
@@ -934,50 +1064,44 @@ void lj_atoms(const MixedAtoms &m, const int *type, const float *lj1, const floa
   check(cudaGetLastError(), "lj_atoms_mixed");
 }
 
-void sites_ds(const double *nodex, const int *etype, const int *site_base, const int *inter_num,
-              const float2 *shape_hl, int nelem, float4 *site_h, float4 *site_l, cudaStream_t s) {
-  if (nelem <= 0) return;
-  k_sites_ds<<<nelem, 128, 0, s>>>(nodex, etype, site_base, inter_num, shape_hl, site_h, site_l);
-  check(cudaGetLastError(), "sites_ds");
-}
-
 void node_split(const double *nodex, int n, float2 *hl, cudaStream_t s) {
   if (n <= 0) return;
   k_node_split<<<nblk((long long) n * 24, 256), 256, 0, s>>>(nodex, n, hl);
   check(cudaGetLastError(), "node_split");
 }
 
-void sites_ds_needed(const float2 *node_hl, const int *site_base, const int *need,
-                     const int *need_elem, int nneed, const float2 *shape_hl, float4 *site_h,
-                     float4 *site_l, cudaStream_t s) {
-  if (nneed <= 0) return;
-  k_sites_ds_needed<<<nblk(nneed, 128), 128, 0, s>>>(node_hl, site_base, need, need_elem, nneed,
-                                                    shape_hl, site_h, site_l);
-  check(cudaGetLastError(), "sites_ds_needed");
-}
-
-void site_rho_needed(const double *erho, const int *site_base, const int *need,
-                     const int *need_elem, int nneed, const float *shape, float *rho,
-                     cudaStream_t s) {
-  if (nneed <= 0) return;
-  k_site_rho_needed<<<nblk(nneed, 128), 128, 0, s>>>(erho, site_base, need, need_elem, nneed,
-                                                    shape, rho);
-  check(cudaGetLastError(), "site_rho_needed");
-}
-
-void site_rho(const double *erho, const int *etype, const int *site_base, const int *inter_num,
-              const float *shape, int nelem, float *rho, cudaStream_t s) {
+void line_mask(const int *flag, const int *etype, const int *site_base, const int *nae, int nelem,
+               int maxlines, unsigned long long *mask, cudaStream_t s) {
   if (nelem <= 0) return;
-  k_site_rho<<<nelem, 128, 0, s>>>(erho, etype, site_base, inter_num, shape, rho);
-  check(cudaGetLastError(), "site_rho");
+  k_line_mask<<<nblk((long long) nelem * maxlines, 256), 256, 0, s>>>(flag, etype, site_base, nae,
+                                                                    nelem, maxlines, mask);
+  check(cudaGetLastError(), "line_mask");
+}
+
+void site_q(const float2 *node_hl, const int *etype, const int *site_base, const int *nae,
+            int max_nax, int max_naz, const unsigned long long *mask, int maxlines,
+            const PackGrid &pg, int nelem, float4 *q, cudaStream_t s) {
+  if (nelem <= 0) return;
+  const size_t smem = sizeof(ds) * (12 * (size_t) max_nax + 6 * LCH + max_naz);
+  k_site_q<<<nelem, LCH, smem, s>>>(node_hl, etype, site_base, nae, mask, maxlines, pg, q);
+  check(cudaGetLastError(), "site_q");
+}
+
+void site_fp(const double *erho, const int *etype, const int *site_base, const int *nae,
+             const unsigned long long *mask, int maxlines, const float4 *fp4, int nrho,
+             double rdrho, int nelem, float *fp, cudaStream_t s) {
+  if (nelem <= 0) return;
+  k_site_fp<<<nelem, LCH, 0, s>>>(erho, etype, site_base, nae, mask, maxlines, fp4, nrho,
+                                  (float) rdrho, fp);
+  check(cudaGetLastError(), "site_fp");
 }
 
 void ip_pass(const MixedElems &m, int pass, const float4 *tab, const EamTables &e, float lj1,
              float lj2, double *out, cudaStream_t s) {
-  ElemArgs a{m.nodex, m.erho, m.site_h, m.site_l, m.site_rho, m.etype, m.row_elem, m.row_jj,
-             m.row_first, m.ipnum, m.ipent, m.nrows, m.rowstride, m.nlocal_e, m.spa_int,
-             m.weight, m.int_off, m.node_list, m.rows, m.nforce, m.cutsq_f, m.band_lo,
-             m.band_hi, m.cutsq, m.node_hl, m.spa_int_hl, m.skip};
+  ElemArgs a{m.erho, m.site_q, m.site_fp, m.etype, m.row_elem, m.row_jj, m.row_first, m.ipnum,
+             m.ipent, m.nrows, m.rowstride, m.nlocal_e, m.spa_int, m.int_off, m.node_list,
+             m.rows, m.nforce, m.cutsq_f, m.band_lo, m.band_hi, m.cutsq, m.node_hl,
+             m.spa_int_hl, m.skip, m.site_base, m.nae, m.nall_e, m.pg};
   if (pass == 0) {  // LJ forces
     int g = persistent_grid((const void *) k_ip<false, false>, m.block, 0, m.nforce);
     k_ip<false, false><<<g, m.block, 0, s>>>(a, tab, 0, 0.f, nullptr, 0, 0.0, lj1, lj2, out);
