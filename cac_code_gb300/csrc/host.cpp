@@ -204,6 +204,12 @@ struct cacg_context {
   DBuf<float> d_u, d_ljf, d_site_fpf;
   DBuf<unsigned long long> d_line_mask;
   DBuf<int> d_nae;
+  // mixed precision, per row: packed and double-single integration points,
+  // F'(rho) of the force rows; the integration-point lists row-major
+  DBuf<float4> d_ip_q, d_ip_h, d_ip_l;
+  DBuf<float> d_row_fpf;
+  DBuf<int> d_row_start, d_ent;
+  int mixed_ip_group = 8;  // lanes per integration point ("tune ip_group N")
   int maxlines = 0, max_nax = 0, max_naz = 0;
   DBuf<double> d_cutsq64, d_stage, d_part, d_lj5;
   std::vector<double> h_lj5;
@@ -469,6 +475,12 @@ cacg_context::~cacg_context() {
   d_site_fpf.release();
   d_line_mask.release();
   d_nae.release();
+  d_ip_q.release();
+  d_ip_h.release();
+  d_ip_l.release();
+  d_row_fpf.release();
+  d_row_start.release();
+  d_ent.release();
   d_ljf.release();
   d_cutsq64.release();
   d_stage.release();
@@ -676,11 +688,16 @@ void cacg_context::command(const std::string &raw) {
   } else if (c == "tune") {
     // tune block 128|256|512: threads per block of the mixed-precision kernels
     // tune union yes|no: neighbor unions staged in shared memory (EAM atom passes)
+    // tune ip_group 4|8|16: lanes per integration point in the mixed element passes
     if (a.size() != 2) fail(CACG_EINVAL, "Illegal tune command");
     if (a[0] == "block") {
       int b = inumeric(a[1]);
       if (b != 128 && b != 256 && b != 512) fail(CACG_EINVAL, "tune block takes 128, 256 or 512");
       mixed_block = b;
+    } else if (a[0] == "ip_group") {
+      int gsz = inumeric(a[1]);
+      if (gsz != 4 && gsz != 8 && gsz != 16) fail(CACG_EINVAL, "tune ip_group takes 4, 8 or 16");
+      mixed_ip_group = gsz;
     } else if (a[0] == "union") {
       if (a[1] != "yes" && a[1] != "no") fail(CACG_EINVAL, "tune union takes yes or no");
       mixed_union = a[1] == "yes";
@@ -2030,8 +2047,15 @@ void cacg_context::neighbor_nbuild() {
   fp64_fma::mark_sites(d_ipnum.p, d_ipent.p, nrows, rowstride, d_site_flag.p, s);
   scan_exclusive(d_site_flag.p, d_site_pos.p, nsites, d_misc.p + 7, d_scan, s);
   check(cudaMemcpyAsync(h_pin + 7, d_misc.p + 7, sizeof(int), cudaMemcpyDeviceToHost, s), "nneed");
+  // the lists row-major for the mixed passes: row_start[nrows] = all entries
+  d_row_start.ensure((size_t) nrows + 1, s);
+  scan_exclusive(d_ipnum.p, d_row_start.p, nrows, d_row_start.p + nrows, d_scan, s);
+  check(cudaMemcpyAsync(h_pin + 10, d_row_start.p + nrows, sizeof(int), cudaMemcpyDeviceToHost, s),
+        "entries");
   sync();
   nneed = h_pin[7];
+  d_ent.ensure(std::max(h_pin[10], 1), s);
+  mixed::ip_csr(d_ipnum.p, d_ipent.p, nrows, rowstride, d_row_start.p, d_ent.p, s);
   d_need.ensure(std::max(nneed, 1), s);
   d_need_elem.ensure(std::max(nneed, 1), s);
   fp64_fma::need_compact(d_site_flag.p, d_site_pos.p, nsites, d_site_base.p, nall, d_need.p,
@@ -2199,28 +2223,31 @@ void cacg_context::pair_ecompute_mixed() {
   mixed::node_split(d_nodex.p, nall, d_node_hl.p, s);
   mixed::site_q(d_node_hl.p, d_etype.p, d_site_base.p, d_nae.p, max_nax, max_naz, d_line_mask.p,
                 maxlines, pg, nall, d_site_q.p, s);
-  launches += 2;
+  d_ip_q.ensure(std::max(nrows, 1), s);
+  d_ip_h.ensure(std::max(nrows, 1), s);
+  d_ip_l.ensure(std::max(nrows, 1), s);
+  mixed::row_q(d_row_elem.p, d_row_jj.p, d_etype.p, d_int_off.p, d_spa_int_hl.p, d_node_hl.p, nrows,
+               pg, d_ip_q.p, d_ip_h.p, d_ip_l.p, s);
+  launches += 3;
   const bool use_sur = sur && nfar > 0;
   const float eps = 1.0e-4f;
   mixed::MixedElems m{};
   m.block = mixed_block;
+  m.group = mixed_ip_group;
   m.site_q = d_site_q.p;
+  m.ip_q = d_ip_q.p;
+  m.ip_h = d_ip_h.p;
+  m.ip_l = d_ip_l.p;
   m.etype = d_etype.p;
   m.row_elem = d_row_elem.p;
-  m.row_jj = d_row_jj.p;
   m.row_first = d_row_first.p;
-  m.ipnum = d_ipnum.p;
-  m.ipent = d_ipent.p;
-  m.nrows = nrows;
-  m.rowstride = rowstride;
-  m.nlocal_e = enlocal;
-  m.spa_int = d_spa_int.p;
-  m.int_off = d_int_off.p;
   m.node_list = d_node_list.p;
+  m.row_start = d_row_start.p;
+  m.ent = d_ent.p;
+  m.nlocal_e = enlocal;
   m.rows = d_force_rows.p;
   m.nforce = nforce;
   m.node_hl = d_node_hl.p;
-  m.spa_int_hl = d_spa_int_hl.p;
   m.site_base = d_site_base.p;
   m.nae = d_nae.p;
   m.nall_e = nall;
@@ -2248,11 +2275,14 @@ void cacg_context::pair_ecompute_mixed() {
     launch_copy_root(d_erho.p, NPE, d_eroot.p, enlocal, enghost, s);
     mixed::site_fp(d_erho.p, d_etype.p, d_site_base.p, d_nae.p, d_line_mask.p, maxlines, d_fp4.p,
                    nrho, rdrho, nall, d_site_fpf.p, s);
-    m.erho = d_erho.p;
+    d_row_fpf.ensure(std::max(nrows, 1), s);
+    mixed::row_fp(d_force_rows.p, nforce, d_row_elem.p, d_row_jj.p, d_etype.p, d_int_off.p,
+                  d_spa_int.p, d_erho.p, e, d_row_fpf.p, s);
     m.site_fp = d_site_fpf.p;
+    m.row_fp = d_row_fpf.p;
     if (use_sur) surrogate_predict(e);
     mixed::ip_pass(m, 2, d_ftab.p, e, 0.f, 0.f, d_fip.p, s);
-    launches += 4;
+    launches += 5;
   }
   fp64_fma::gather_nodef(d_fip.p, d_etype.p, d_row_first.p, enlocal, t, d_nodef.p, s);
   launches++;

@@ -265,24 +265,25 @@ struct PackGrid {
   int *oob;
 };
 struct MixedElems {
-  const double *erho;
-  const float4 *site_q;  // packed site positions of this step (referenced sites)
-  const float *site_fp;  // FP32 F'(rho) at the referenced sites (EAM force pass)
-  const int *etype, *row_elem, *row_jj, *row_first, *ipnum, *ipent;
-  int nrows, rowstride, nlocal_e;
-  const double *spa_int;
-  const int *int_off, *node_list;
+  const float4 *site_q;       // packed site positions of this step (referenced sites)
+  const float *site_fp;       // FP32 F'(rho) at the referenced sites (EAM force pass)
+  const float4 *ip_q;         // packed integration-point positions, per row
+  const float4 *ip_h, *ip_l;  // their double-single positions
+  const float *row_fp;        // FP32 F'(rho) at the rows of nonzero weight (EAM force pass)
+  const int *etype, *row_elem, *row_first, *node_list;
+  const int *row_start, *ent;  // integration-point lists, row-major
+  int nlocal_e;
   const int *rows;  // rows of nonzero weight (force passes), count nforce
   int nforce;
   float cutsq_f, band_lo, band_hi;
   double cutsq;
-  const float2 *node_hl;     // [nall][24] double-single node coordinates
-  const float2 *spa_int_hl;  // double-single integration-point shape functions
+  const float2 *node_hl;                // [nall][24] double-single node coordinates
   const unsigned char *skip = nullptr;  // elements whose forces come from the surrogate
   const int *site_base, *nae;           // site offsets per element; lattice sizes per type
   int nall_e;
   PackGrid pg;
   int block = 512;  // threads per block of the persistent grids
+  int group = 8;    // lanes per integration point (4, 8 or 16)
 };
 // cell-relative packed coordinates for the atom passes; *oob counts atoms
 // outside the 4096 x 1024 x 1024-cell range
@@ -317,6 +318,17 @@ void eam_force_atoms(const MixedAtoms &m, const float4 *ftab, const EamTables &e
                      const double *fp, double *f, cudaStream_t s);
 void lj_atoms(const MixedAtoms &m, const int *type, const float *lj1, const float *lj2,
               const float *cutsq_t, const double *cutsq64, double *f, cudaStream_t s);
+// every row's integration point: packed, and its double-single position
+void row_q(const int *row_elem, const int *row_jj, const int *etype, const int *int_off,
+           const float2 *spa_int_hl, const float2 *node_hl, int nrows, const PackGrid &pg,
+           float4 *ip_q, float4 *ip_h, float4 *ip_l, cudaStream_t s);
+// FP32 F'(rho) at the rows of nonzero weight, rho in FP64 from the nodal densities
+void row_fp(const int *rows, int nforce, const int *row_elem, const int *row_jj,
+            const int *etype, const int *int_off, const double *spa_int, const double *erho,
+            const EamTables &e, float *fp, cudaStream_t s);
+// row-major copy of the integration-point lists (row_start: exclusive scan of ipnum)
+void ip_csr(const int *ipnum, const int *ipent, int nrows, int rowstride, const int *row_start,
+            int *ent, cudaStream_t s);
 // pass 0: LJ forces -> out[3*rows]; 1: EAM nodal densities -> out[8*nlocal_e];
 // 2: EAM forces -> out[3*rows]
 void ip_pass(const MixedElems &m, int pass, const float4 *tab, const EamTables &e, float lj1,

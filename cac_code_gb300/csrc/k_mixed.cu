@@ -759,18 +759,19 @@ k_site_fp(const double *__restrict__ erho, const int *__restrict__ etype,
 }
 
 struct ElemArgs {
-  const double *erho;
   const float4 *site_q;  // packed site positions of this step
   const float *site_fp;  // F'(rho) at the sites (EAM force pass)
-  const int *etype, *row_elem, *row_jj, *row_first, *ipnum, *ipent;
-  int nrows, rowstride, nlocal_e;
-  const double *spa_int;
-  const int *int_off, *node_list;
+  const float4 *ip_q;    // packed integration-point positions of this step
+  const float4 *ip_h, *ip_l;  // their double-single positions (guard band)
+  const float *row_fp;        // F'(rho) at the rows of nonzero weight (EAM force pass)
+  const int *etype, *row_elem, *row_first, *node_list;
+  const int *row_start, *ent;  // integration-point lists, row-major
+  int nlocal_e;
   const int *rows;
   int nforce;
   float cutsq_f, band_lo, band_hi;
   double cutsq;
-  const float2 *node_hl, *spa_int_hl;
+  const float2 *node_hl;
   const unsigned char *skip;
   const int *site_base, *nae;
   int nall_e;
@@ -802,6 +803,50 @@ __device__ __forceinline__ void ip_ds(const float2 *__restrict__ N, const float2
   }
 }
 
+// Every row's integration point, once per step: packed, and in double-single
+// for the guard-band tests
+__global__ void k_row_q(const int *__restrict__ row_elem, const int *__restrict__ row_jj,
+                        const int *__restrict__ etype, const int *__restrict__ int_off,
+                        const float2 *__restrict__ spa_int_hl, const float2 *__restrict__ node_hl,
+                        int nrows, PackGrid pg, float4 *__restrict__ ip_q,
+                        float4 *__restrict__ ip_h, float4 *__restrict__ ip_l) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  const int e = row_elem[r], ty = etype[e];
+  ds x[3];
+  ip_ds(spa_int_hl + ((size_t) int_off[ty] + row_jj[r]) * NPE, node_hl + 24 * (size_t) e, x);
+  const ds l0[3] = {{pg.l0h[0], pg.l0l[0]}, {pg.l0h[1], pg.l0l[1]}, {pg.l0h[2], pg.l0l[2]}};
+  ip_q[r] = pack_u(ds_sub(x[0], l0[0]), ds_sub(x[1], l0[1]), ds_sub(x[2], l0[2]), pg);
+  ip_h[r] = make_float4(x[0].h, x[1].h, x[2].h, 0.f);
+  ip_l[r] = make_float4(x[0].l, x[1].l, x[2].l, 0.f);
+}
+
+// F'(rho_i) at the rows of nonzero weight, rho_i = sum_k N_k erho_k in FP64
+// (pair_eam.cpp:1090-1100)
+__global__ void k_row_fp(const int *__restrict__ rows, int nforce, const int *__restrict__ row_elem,
+                         const int *__restrict__ row_jj, const int *__restrict__ etype,
+                         const int *__restrict__ int_off, const double *__restrict__ spa_int,
+                         const double *__restrict__ erho, const double *__restrict__ frho, int nrho,
+                         double rdrho, float *__restrict__ row_fp) {
+  const int it = blockIdx.x * blockDim.x + threadIdx.x;
+  if (it >= nforce) return;
+  const int r = rows[it], e = row_elem[r], ty = etype[e];
+  const double *N = spa_int + ((size_t) int_off[ty] + row_jj[r]) * NPE;
+  double rho = 0.0;
+#pragma unroll
+  for (int k = 0; k < NPE; k++) rho += N[k] * erho[NPE * (size_t) e + k];
+  row_fp[r] = (float) fprime64(rho, frho, nrho, rdrho);
+}
+
+// row-major copy of the column-major integration-point lists
+__global__ void k_ip_csr(const int *__restrict__ ipnum, const int *__restrict__ ipent, int nrows,
+                         int rowstride, const int *__restrict__ row_start, int *__restrict__ ent) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  const int n = ipnum[r], s0 = row_start[r];
+  for (int k = 0; k < n; k++) ent[s0 + k] = __ldg(ipent + (size_t) k * rowstride + r);
+}
+
 // the site's double-single position, from its owning element (guard band only)
 __device__ __noinline__ void site_ds_of(const ElemArgs &a, int sid, ds (&x)[3]) {
   int lo = 0, hi = a.nall_e;  // site_base[lo] <= sid < site_base[hi]
@@ -817,128 +862,144 @@ __device__ __noinline__ void site_ds_of(const ElemArgs &a, int sid, ds (&x)[3]) 
   site_ds(a.node_hl + 24 * (size_t) lo, L / nay, L % nay, kk, nax, nay, naz, x);
 }
 
-// One thread per integration point.  DENSITY: node rows -> erho (EAM);
-// otherwise rows of nonzero weight -> forces (LJ or EAM).  Every entry of the
-// row's list is tested: a 16-byte gather of the packed site, the FP32 cutoff
-// test, and in the guard band the FP64 test on the double-single positions.
-template <bool EAM, bool DENSITY>
+__device__ __noinline__ bool inside_band(const ElemArgs &a, int r, int sid) {
+  ds sx[3];
+  site_ds_of(a, sid, sx);
+  const float4 h = __ldg(a.ip_h + r), l = __ldg(a.ip_l + r);
+  const double dx = ((double) h.x + l.x) - ((double) sx[0].h + sx[0].l);
+  const double dy = ((double) h.y + l.y) - ((double) sx[1].h + sx[1].l);
+  const double dz = ((double) h.z + l.z) - ((double) sx[2].h + sx[2].l);
+  return dx * dx + dy * dy + dz * dz < a.cutsq;
+}
+
+// G lanes per integration point, each taking every G-th entry of the row's
+// list; the lanes' sums meet by shuffles.  DENSITY: node rows -> erho (EAM);
+// otherwise rows of nonzero weight -> forces (LJ or EAM).  Every entry is
+// tested: a 16-byte gather of the packed site, the FP32 cutoff test, and in
+// the guard band the FP64 test on the double-single positions.
+template <bool EAM, bool DENSITY, int G>
 __global__ void __launch_bounds__(512, 2)
-k_ip(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr,
-     const double *__restrict__ frho, int nrho, double rdrho, float lj1, float lj2,
-     double *__restrict__ out) {
+k_ipg(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr, float lj1, float lj2,
+      double *__restrict__ out) {
   extern __shared__ float4 s_tab[];
   const int ntab = EAM ? (DENSITY ? (nr + 1) : 3 * (nr + 1)) : 0;
   for (int m = threadIdx.x; m < ntab; m += blockDim.x) s_tab[m] = tab[m];
   __syncthreads();
   const float g = a.pg.g;
-  const ds l0[3] = {{a.pg.l0h[0], a.pg.l0l[0]}, {a.pg.l0h[1], a.pg.l0l[1]},
-                    {a.pg.l0h[2], a.pg.l0l[2]}};
+  constexpr int GPW = 32 / G;  // groups per warp
+  const int lane = threadIdx.x & (G - 1), gsub = (threadIdx.x & 31) / G;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int nitems = DENSITY ? a.nlocal_e * NPE : a.nforce;
-  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < nitems; it += gridDim.x * blockDim.x) {
-    int r, e, ty, jj;
-    if (DENSITY) {
-      e = it / NPE;
-      ty = a.etype[e];
-      jj = a.node_list[ty * NPE + it % NPE];
-      r = a.row_first[e] + jj;
-    } else {
-      r = a.rows[it];  // rows of nonzero weight only; the others stay zero
-      e = a.row_elem[r];
-      if (a.skip && a.skip[e]) continue;  // nodal forces from the surrogate
-      ty = a.etype[e];
-      jj = a.row_jj[r];
+  // warp-uniform trip count: every lane reaches the shuffles
+  for (int wb = warp * GPW; wb < nitems; wb += nwarps * GPW) {
+    const int it = wb + gsub;
+    int r = 0, e = 0, n = 0;
+    bool live = it < nitems;
+    if (live) {
+      if (DENSITY) {
+        e = it / NPE;
+        r = a.row_first[e] + a.node_list[a.etype[e] * NPE + it % NPE];
+      } else {
+        r = a.rows[it];  // rows of nonzero weight only; the others stay zero
+        e = a.row_elem[r];
+        if (a.skip && a.skip[e]) live = false;  // nodal forces from the surrogate
+      }
     }
-    const double *N64 = a.spa_int + ((size_t) a.int_off[ty] + jj) * NPE;
-    ds ix[3];
-    ip_ds(a.spa_int_hl + ((size_t) a.int_off[ty] + jj) * NPE, a.node_hl + 24 * (size_t) e, ix);
-    const float4 qi =
-        pack_u(ds_sub(ix[0], l0[0]), ds_sub(ix[1], l0[1]), ds_sub(ix[2], l0[2]), a.pg);
+    int s0 = 0;
+    float4 qi = make_float4(0.f, 0.f, 0.f, 0.f);
+    float fpi = 0.f;
+    if (live) {
+      s0 = a.row_start[r];
+      n = a.row_start[r + 1] - s0;
+      qi = __ldg(a.ip_q + r);
+      if (EAM && !DENSITY) fpi = __ldg(a.row_fp + r);
+    }
     int cx, cy, cz;
     cell_of(qi, cx, cy, cz);
-    double fpi = 0.0;
-    if (EAM && !DENSITY) {
-      double rhoi = 0.0;
-#pragma unroll
-      for (int k = 0; k < NPE; k++) rhoi += N64[k] * a.erho[NPE * (size_t) e + k];
-      fpi = fprime64(rhoi, frho, nrho, rdrho);
-    }
     double acc = 0.0, fx = 0.0, fy = 0.0, fz = 0.0;
     float part = 0.f, px = 0.f, py = 0.f, pz = 0.f;
-    const int n = a.ipnum[r];
-    int sn = 0;
+    int sn = 0, cnt = 0;
     float4 qn = qi;
     float fpn = 0.f;
-    if (n > 0) {
-      sn = __ldg(a.ipent + r);
+    if (lane < n) {
+      sn = __ldg(a.ent + s0 + lane);
       qn = __ldg(a.site_q + sn);
       if (EAM && !DENSITY) fpn = __ldg(a.site_fp + sn);
     }
-    for (int k = 0; k < n; k++) {
+    for (int k = lane; k < n; k += G) {
       const int sid = sn;
       const float4 qj = qn;
       const float fpj = fpn;
-      if (k + 1 < n) {  // next site's gathers in flight during this one
-        sn = __ldg(a.ipent + (size_t) (k + 1) * a.rowstride + r);
+      if (k + G < n) {  // next entry's gathers in flight during this one
+        sn = __ldg(a.ent + s0 + k + G);
         qn = __ldg(a.site_q + sn);
         if (EAM && !DENSITY) fpn = __ldg(a.site_fp + sn);
       }
       float dx, dy, dz;
       rel_vec(qi, cx, cy, cz, qj, g, dx, dy, dz);
-      float rsq = dx * dx + dy * dy + dz * dz;
+      const float rsq = dx * dx + dy * dy + dz * dz;
       bool in = rsq < a.cutsq_f;
-      if (rsq >= a.band_lo && rsq <= a.band_hi) {
-        ds sx[3];
-        site_ds_of(a, sid, sx);
-        double ddx = ((double) ix[0].h + ix[0].l) - ((double) sx[0].h + sx[0].l);
-        double ddy = ((double) ix[1].h + ix[1].l) - ((double) sx[1].h + sx[1].l);
-        double ddz = ((double) ix[2].h + ix[2].l) - ((double) sx[2].h + sx[2].l);
-        in = ddx * ddx + ddy * ddy + ddz * ddz < a.cutsq;
-      }
+      if (rsq >= a.band_lo && rsq <= a.band_hi) in = inside_band(a, r, sid);
       if (in) {
         if (EAM) {
-          float recip = rsqrtf(rsq);
-          float rr = rsq * recip;
+          const float recip = rsqrtf(rsq);
+          const float rr = rsq * recip;
           float p;
-          int m = findex(rr, rdr, nr, p);
+          const int m = findex(rr, rdr, nr, p);
           if (DENSITY) {
-            float4 c = s_tab[m];
+            const float4 c = s_tab[m];
             part += ((c.x * p + c.y) * p + c.z) * p + c.w;
           } else {
-            float4 t0 = s_tab[3 * m], t1 = s_tab[3 * m + 1], t2 = s_tab[3 * m + 2];
-            float rhoip = (t0.x * p + t0.y) * p + t0.z;
-            float z2p = (t0.w * p + t1.x) * p + t1.y;
-            float z2 = ((t1.z * p + t1.w) * p + t2.x) * p + t2.y;
-            float phi = z2 * recip;
-            float phip = z2p * recip - phi * recip;
-            float psip = ((float) fpi + fpj) * rhoip + phip;
-            float fpair = -psip * recip;
+            const float4 t0 = s_tab[3 * m], t1 = s_tab[3 * m + 1], t2 = s_tab[3 * m + 2];
+            const float rhoip = (t0.x * p + t0.y) * p + t0.z;
+            const float z2p = (t0.w * p + t1.x) * p + t1.y;
+            const float z2 = ((t1.z * p + t1.w) * p + t2.x) * p + t2.y;
+            const float phi = z2 * recip;
+            const float phip = z2p * recip - phi * recip;
+            const float psip = (fpi + fpj) * rhoip + phip;
+            const float fpair = -psip * recip;
             px += dx * fpair;
             py += dy * fpair;
             pz += dz * fpair;
           }
         } else {
-          float r2inv = __frcp_rn(rsq);
-          float r6inv = r2inv * r2inv * r2inv;
-          float fpair = r6inv * (lj1 * r6inv - lj2) * r2inv;
+          const float r2inv = __frcp_rn(rsq);
+          const float r6inv = r2inv * r2inv * r2inv;
+          const float fpair = r6inv * (lj1 * r6inv - lj2) * r2inv;
           px += dx * fpair;
           py += dy * fpair;
           pz += dz * fpair;
         }
-      }
-      if ((k & (CHUNK - 1)) == CHUNK - 1) {
-        acc += (double) part;
-        fx += (double) px;
-        fy += (double) py;
-        fz += (double) pz;
-        part = px = py = pz = 0.f;
+        if ((++cnt & (CHUNK - 1)) == 0) {
+          acc += (double) part;
+          fx += (double) px;
+          fy += (double) py;
+          fz += (double) pz;
+          part = px = py = pz = 0.f;
+        }
       }
     }
     if (DENSITY) {
-      out[NPE * (size_t) e + it % NPE] = acc + (double) part;
+      acc += (double) part;
+#pragma unroll
+      for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (live && lane == 0) out[NPE * (size_t) e + it % NPE] = acc;
     } else {
-      out[3 * r] = fx + (double) px;
-      out[3 * r + 1] = fy + (double) py;
-      out[3 * r + 2] = fz + (double) pz;
+      fx += (double) px;
+      fy += (double) py;
+      fz += (double) pz;
+#pragma unroll
+      for (int o = G / 2; o > 0; o >>= 1) {
+        fx += __shfl_xor_sync(0xffffffffu, fx, o);
+        fy += __shfl_xor_sync(0xffffffffu, fy, o);
+        fz += __shfl_xor_sync(0xffffffffu, fz, o);
+      }
+      if (live && lane == 0) {
+        out[3 * r] = fx;
+        out[3 * r + 1] = fy;
+        out[3 * r + 2] = fz;
+      }
     }
   }
 }
@@ -1096,26 +1157,60 @@ void site_fp(const double *erho, const int *etype, const int *site_base, const i
   check(cudaGetLastError(), "site_fp");
 }
 
+void row_q(const int *row_elem, const int *row_jj, const int *etype, const int *int_off,
+           const float2 *spa_int_hl, const float2 *node_hl, int nrows, const PackGrid &pg,
+           float4 *ip_q, float4 *ip_h, float4 *ip_l, cudaStream_t s) {
+  if (nrows <= 0) return;
+  k_row_q<<<nblk(nrows, 128), 128, 0, s>>>(row_elem, row_jj, etype, int_off, spa_int_hl, node_hl,
+                                          nrows, pg, ip_q, ip_h, ip_l);
+  check(cudaGetLastError(), "row_q");
+}
+
+void row_fp(const int *rows, int nforce, const int *row_elem, const int *row_jj,
+            const int *etype, const int *int_off, const double *spa_int, const double *erho,
+            const EamTables &e, float *fp, cudaStream_t s) {
+  if (nforce <= 0) return;
+  k_row_fp<<<nblk(nforce, 128), 128, 0, s>>>(rows, nforce, row_elem, row_jj, etype, int_off,
+                                            spa_int, erho, e.frho, e.nrho, e.rdrho, fp);
+  check(cudaGetLastError(), "row_fp");
+}
+
+void ip_csr(const int *ipnum, const int *ipent, int nrows, int rowstride, const int *row_start,
+            int *ent, cudaStream_t s) {
+  if (nrows <= 0) return;
+  k_ip_csr<<<nblk(nrows, 128), 128, 0, s>>>(ipnum, ipent, nrows, rowstride, row_start, ent);
+  check(cudaGetLastError(), "ip_csr");
+}
+
+template <bool EAM, bool DENSITY, int G>
+static void launch_ipg(const ElemArgs &a, long long items, int block, const float4 *tab,
+                       const EamTables &e, float lj1, float lj2, double *out, cudaStream_t s) {
+  const size_t smem = EAM ? sizeof(float4) * (DENSITY ? 1 : 3) * (e.nr + 1) : 0;
+  const int g = persistent_grid((const void *) k_ipg<EAM, DENSITY, G>, block, smem, items * G);
+  k_ipg<EAM, DENSITY, G><<<g, block, smem, s>>>(a, tab, e.nr, (float) e.rdr, lj1, lj2, out);
+}
+
+template <bool EAM, bool DENSITY>
+static void launch_ip(const ElemArgs &a, long long items, int block, int group,
+                      const float4 *tab, const EamTables &e, float lj1, float lj2, double *out,
+                      cudaStream_t s) {
+  if (group == 4) launch_ipg<EAM, DENSITY, 4>(a, items, block, tab, e, lj1, lj2, out, s);
+  else if (group == 16) launch_ipg<EAM, DENSITY, 16>(a, items, block, tab, e, lj1, lj2, out, s);
+  else launch_ipg<EAM, DENSITY, 8>(a, items, block, tab, e, lj1, lj2, out, s);
+}
+
 void ip_pass(const MixedElems &m, int pass, const float4 *tab, const EamTables &e, float lj1,
              float lj2, double *out, cudaStream_t s) {
-  ElemArgs a{m.erho, m.site_q, m.site_fp, m.etype, m.row_elem, m.row_jj, m.row_first, m.ipnum,
-             m.ipent, m.nrows, m.rowstride, m.nlocal_e, m.spa_int, m.int_off, m.node_list,
-             m.rows, m.nforce, m.cutsq_f, m.band_lo, m.band_hi, m.cutsq, m.node_hl,
-             m.spa_int_hl, m.skip, m.site_base, m.nae, m.nall_e, m.pg};
-  if (pass == 0) {  // LJ forces
-    int g = persistent_grid((const void *) k_ip<false, false>, m.block, 0, m.nforce);
-    k_ip<false, false><<<g, m.block, 0, s>>>(a, tab, 0, 0.f, nullptr, 0, 0.0, lj1, lj2, out);
-  } else if (pass == 1) {  // EAM nodal densities
-    size_t smem = sizeof(float4) * (e.nr + 1);
-    int g = persistent_grid((const void *) k_ip<true, true>, m.block, smem, (long long) m.nlocal_e * NPE);
-    k_ip<true, true><<<g, m.block, smem, s>>>(a, tab, e.nr, (float) e.rdr, e.frho, e.nrho, e.rdrho,
-                                         0.f, 0.f, out);
-  } else {  // EAM forces
-    size_t smem = sizeof(float4) * 3 * (e.nr + 1);
-    int g = persistent_grid((const void *) k_ip<true, false>, m.block, smem, m.nforce);
-    k_ip<true, false><<<g, m.block, smem, s>>>(a, tab, e.nr, (float) e.rdr, e.frho, e.nrho, e.rdrho,
-                                          0.f, 0.f, out);
-  }
+  ElemArgs a{m.site_q, m.site_fp, m.ip_q, m.ip_h, m.ip_l, m.row_fp, m.etype, m.row_elem,
+             m.row_first, m.node_list, m.row_start, m.ent, m.nlocal_e, m.rows, m.nforce,
+             m.cutsq_f, m.band_lo, m.band_hi, m.cutsq, m.node_hl, m.skip, m.site_base, m.nae,
+             m.nall_e, m.pg};
+  if (pass == 0)  // LJ forces
+    launch_ip<false, false>(a, m.nforce, m.block, m.group, tab, e, lj1, lj2, out, s);
+  else if (pass == 1)  // EAM nodal densities
+    launch_ip<true, true>(a, (long long) m.nlocal_e * NPE, m.block, m.group, tab, e, 0.f, 0.f, out, s);
+  else  // EAM forces
+    launch_ip<true, false>(a, m.nforce, m.block, m.group, tab, e, 0.f, 0.f, out, s);
   check(cudaGetLastError(), "ip_pass_mixed");
 }
 
