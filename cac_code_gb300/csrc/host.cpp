@@ -201,7 +201,7 @@ struct cacg_context {
   // the referenced sites of each lattice line, lattice sizes per type
   DBuf<float4> d_xl, d_rhor_val4, d_ftab, d_fp4, d_site_q;
   DBuf<float2> d_node_hl, d_spa_int_hl;
-  DBuf<float> d_u, d_ljf, d_site_fpf;
+  DBuf<float> d_u, d_ljf, d_site_fpf, d_fpf;
   DBuf<unsigned long long> d_line_mask;
   DBuf<int> d_nae;
   // mixed precision, per row: packed and double-single integration points,
@@ -473,6 +473,7 @@ cacg_context::~cacg_context() {
   d_node_hl.release();
   d_spa_int_hl.release();
   d_site_fpf.release();
+  d_fpf.release();
   d_line_mask.release();
   d_nae.release();
   d_ip_q.release();
@@ -2179,19 +2180,20 @@ void cacg_context::pair_compute_mixed(int pass) {
   }
   if (pass == 1) {
     d_rho.ensure(nall, s);
-    d_fp.ensure(nall, s);
+    d_fpf.ensure(nall, s);
     if (mixed_union)
       mixed::eam_rho_union(m, d_union_j.p, d_union_n.p, d_slot.p, d_sslot.p, d_rhor_val4.p, e,
-                           d_rho.p, d_fp.p, s);
+                           d_fp4.p, d_rho.p, d_fpf.p, s);
     else
-      mixed::eam_rho_atoms(m, d_rhor_val4.p, e, d_rho.p, d_fp.p, s);
-    launch_copy_root(d_fp.p, 1, d_root.p, nlocal, nghost, s);
+      mixed::eam_rho_atoms(m, d_rhor_val4.p, e, d_fp4.p, d_rho.p, d_fpf.p, s);
+    launch_copy_root(d_fpf.p, 1, d_root.p, nlocal, nghost, s);
     launches += 2;
   } else {
     if (mixed_union)
-      mixed::eam_force_union(m, d_union_j.p, d_union_n.p, d_sslot.p, d_ftab.p, e, d_fp.p, d_f.p, s);
+      mixed::eam_force_union(m, d_union_j.p, d_union_n.p, d_sslot.p, d_ftab.p, e, d_fpf.p, d_f.p,
+                             s);
     else
-      mixed::eam_force_atoms(m, d_ftab.p, e, d_fp.p, d_f.p, s);
+      mixed::eam_force_atoms(m, d_ftab.p, e, d_fpf.p, d_f.p, s);
     launches++;
   }
 }

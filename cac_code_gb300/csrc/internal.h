@@ -120,6 +120,7 @@ void launch_forward_atoms(double4 *x, const int *sendlist, int n, int first, dou
                           double dy, double dz, cudaStream_t s);
 void launch_forward_elems(double *nodex, const int *sendlist, int n, int first, double dx,
                           double dy, double dz, cudaStream_t s);
+void launch_copy_root(float *a, int width, const int *root, int gfirst, int gn, cudaStream_t s);
 void launch_copy_root(double *a, int width, const int *root, int gfirst, int gn,
                       cudaStream_t s);
 void launch_pbc_atoms(double4 *x, int n, const double *lo, const double *hi,
@@ -308,14 +309,16 @@ void union_build(const int *num, const int *list, int stride, int nlocal, int *u
                  int *union_n, unsigned short *slot, cudaStream_t s);
 void eam_rho_union(const MixedAtoms &m, const int *union_j, const int *union_n,
                    const unsigned short *slot, unsigned short *sslot, const float4 *rhor_val,
-                   const EamTables &e, double *rho, double *fp, cudaStream_t s);
+                   const EamTables &e, const float4 *fp4, double *rho, float *fp,
+                   cudaStream_t s);
 void eam_force_union(const MixedAtoms &m, const int *union_j, const int *union_n,
                      const unsigned short *sslot, const float4 *ftab, const EamTables &e,
-                     const double *fp, double *f, cudaStream_t s);
+                     const float *fp, double *f, cudaStream_t s);
+// fp: FP32 F'(rho) from the FP32 coefficient table fp4 (c0..c2 per knot)
 void eam_rho_atoms(const MixedAtoms &m, const float4 *rhor_val, const EamTables &e,
-                   double *rho, double *fp, cudaStream_t s);
+                   const float4 *fp4, double *rho, float *fp, cudaStream_t s);
 void eam_force_atoms(const MixedAtoms &m, const float4 *ftab, const EamTables &e,
-                     const double *fp, double *f, cudaStream_t s);
+                     const float *fp, double *f, cudaStream_t s);
 void lj_atoms(const MixedAtoms &m, const int *type, const float *lj1, const float *lj2,
               const float *cutsq_t, const double *cutsq64, double *f, cudaStream_t s);
 // every row's integration point: packed, and its double-single position

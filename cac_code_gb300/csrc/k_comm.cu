@@ -198,8 +198,9 @@ __global__ void k_forward_elems(double *__restrict__ nodex, const int *__restric
   nodex[24 * (first + m) + r] = nodex[24 * send[m] + r] + d;
 }
 
-__global__ void k_copy_root(double *__restrict__ a, int width, const int *__restrict__ root,
-                            int gfirst, int gn) {
+template <class T>
+__global__ void k_copy_root(T *__restrict__ a, int width, const int *__restrict__ root, int gfirst,
+                            int gn) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= gn * width) return;
   int g = gfirst + t / width, c = t % width;
@@ -402,7 +403,13 @@ void launch_forward_elems(double *nodex, const int *sendlist, int n, int first, 
 void launch_copy_root(double *a, int width, const int *root, int gfirst, int gn,
                       cudaStream_t s) {
   if (gn <= 0) return;
-  k_copy_root<<<nblk((long long) gn * width, 256), 256, 0, s>>>(a, width, root, gfirst, gn);
+  k_copy_root<double><<<nblk((long long) gn * width, 256), 256, 0, s>>>(a, width, root, gfirst, gn);
+  check(cudaGetLastError(), "copy_root");
+}
+
+void launch_copy_root(float *a, int width, const int *root, int gfirst, int gn, cudaStream_t s) {
+  if (gn <= 0) return;
+  k_copy_root<float><<<nblk((long long) gn * width, 256), 256, 0, s>>>(a, width, root, gfirst, gn);
   check(cudaGetLastError(), "copy_root");
 }
 

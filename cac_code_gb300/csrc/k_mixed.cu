@@ -50,6 +50,45 @@ __device__ __forceinline__ double fprime64(double rho, const double *__restrict_
   return (c[0] * p + c[1]) * p + c[2];
 }
 
+__device__ __forceinline__ float fprime32(float rho, const float4 *__restrict__ fp4, int nrho,
+                                          float rdrho) {
+  float p = rho * rdrho + 1.0f;
+  int m = (int) p;
+  m = m < nrho - 1 ? m : nrho - 1;
+  m = 1 > m ? 1 : m;
+  p -= (float) m;
+  p = fminf(p, 1.0f);
+  const float4 c = __ldg(fp4 + m);
+  return (c.x * p + c.y) * p + c.z;
+}
+
+// FP32 double-single accumulator: the FP32 chunk sums are added by Knuth's
+// TwoSum, without FP64 instructions (the FP64 pipe issues a warp instruction
+// at a small fraction of the FP32 rate on this GPU, and it was the limit of
+// the atom force pass when the chunks were added in FP64)
+struct dsacc {
+  float h = 0.f, l = 0.f;
+  __device__ __forceinline__ void add(float v) {
+    const float s = __fadd_rn(h, v);
+    const float b = __fsub_rn(s, h);
+    l = __fadd_rn(l, __fadd_rn(__fsub_rn(h, __fsub_rn(s, b)), __fsub_rn(v, b)));
+    h = s;
+  }
+  __device__ __forceinline__ double value() const { return (double) h + (double) l; }
+};
+
+// sum of a double-single over each aligned group of G lanes (xor shuffles)
+template <int G>
+__device__ __forceinline__ void group_sum(dsacc &a) {
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) {
+    const float h = __shfl_xor_sync(0xffffffffu, a.h, o);
+    const float l = __shfl_xor_sync(0xffffffffu, a.l, o);
+    a.add(h);
+    a.l = __fadd_rn(a.l, l);
+  }
+}
+
 // exact FP64 cutoff decision for pairs whose FP32 rsq falls in the guard band
 __device__ __forceinline__ bool inside64(const double4 &a, const double4 &b, double cutsq) {
   double dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
@@ -113,8 +152,8 @@ struct AtomArgs {
 // 40 registers at three 512-thread blocks per SM (48 warps): more gathers in flight
 __global__ void __launch_bounds__(512, 3)
 k_eam_rho_atoms(AtomArgs a, const float4 *__restrict__ rhor_val, int nr, float rdr,
-                const double *__restrict__ frho, int nrho, double rdrho,
-                double *__restrict__ rho, double *__restrict__ fp) {
+                const float4 *__restrict__ fp4, int nrho, float rdrho,
+                double *__restrict__ rho, float *__restrict__ fp) {
   extern __shared__ float4 s_val[];
   for (int m = threadIdx.x; m <= nr; m += blockDim.x) s_val[m] = rhor_val[m];
   __syncthreads();
@@ -123,7 +162,7 @@ k_eam_rho_atoms(AtomArgs a, const float4 *__restrict__ rhor_val, int nr, float r
     int cx, cy, cz;
     cell_of(qi, cx, cy, cz);
     const int n = a.num[i];
-    double acc = 0.0;
+    dsacc acc;
     float part = 0.f;
     int ns = 0, cnt = 0;
     // the next entry's index and coordinates are fetched while this one is
@@ -154,15 +193,15 @@ k_eam_rho_atoms(AtomArgs a, const float4 *__restrict__ rhor_val, int nr, float r
         float4 c = s_val[m];
         part += ((c.x * p + c.y) * p + c.z) * p + c.w;
         if ((++cnt & (CHUNK - 1)) == 0) {
-          acc += (double) part;
+          acc.add(part);
           part = 0.f;
         }
       }
     }
     a.snum[i] = ns;
-    acc += (double) part;
-    rho[i] = acc;
-    fp[i] = fprime64(acc, frho, nrho, rdrho);
+    acc.add(part);
+    rho[i] = acc.value();
+    fp[i] = fprime32(__fadd_rn(acc.h, acc.l), fp4, nrho, rdrho);
   }
 }
 
@@ -246,8 +285,8 @@ struct UnionArgs {
 
 __global__ void __launch_bounds__(UGROUP * UWARPS, 1)
 k_eam_rho_union(AtomArgs a, UnionArgs u, const float4 *__restrict__ rhor_val, int nr, float rdr,
-                const double *__restrict__ frho, int nrho, double rdrho,
-                double *__restrict__ rho, double *__restrict__ fp) {
+                const float4 *__restrict__ fp4, int nrho, float rdrho,
+                double *__restrict__ rho, float *__restrict__ fp) {
   extern __shared__ float4 sm[];
   float4 *s_val = sm;                                  // nr + 1 knots
   float4 *sx = sm + (nr + 1) + (threadIdx.x >> 5) * UMAX;  // this warp's union
@@ -266,7 +305,7 @@ k_eam_rho_union(AtomArgs a, UnionArgs u, const float4 *__restrict__ rhor_val, in
       int cx, cy, cz;
       cell_of(qi, cx, cy, cz);
       const int n = a.num[i];
-      double acc = 0.0;
+      dsacc acc;
       float part = 0.f;
       int ns = 0, cnt = 0;
       for (int k = 0; k < n; k++) {
@@ -297,15 +336,15 @@ k_eam_rho_union(AtomArgs a, UnionArgs u, const float4 *__restrict__ rhor_val, in
           float4 c = s_val[m];
           part += ((c.x * p + c.y) * p + c.z) * p + c.w;
           if ((++cnt & (CHUNK - 1)) == 0) {
-            acc += (double) part;
+            acc.add(part);
             part = 0.f;
           }
         }
       }
       a.snum[i] = ns;
-      acc += (double) part;
-      rho[i] = acc;
-      fp[i] = fprime64(acc, frho, nrho, rdrho);
+      acc.add(part);
+      rho[i] = acc.value();
+      fp[i] = fprime32(__fadd_rn(acc.h, acc.l), fp4, nrho, rdrho);
     }
     __syncwarp();  // the union is overwritten by the warp's next group
   }
@@ -313,7 +352,7 @@ k_eam_rho_union(AtomArgs a, UnionArgs u, const float4 *__restrict__ rhor_val, in
 
 __global__ void __launch_bounds__(UGROUP * UWARPS, 1)
 k_eam_force_union(AtomArgs a, UnionArgs u, const float4 *__restrict__ ftab, int nr, float rdr,
-                  const double *__restrict__ fp, double *__restrict__ f) {
+                  const float *__restrict__ fp, double *__restrict__ f) {
   extern __shared__ float4 sm[];
   float4 *s_tab = sm;  // 3 float4 per knot
   float4 *sx = sm + 3 * (nr + 1) + (threadIdx.x >> 5) * UMAX;
@@ -329,16 +368,16 @@ k_eam_force_union(AtomArgs a, UnionArgs u, const float4 *__restrict__ ftab, int 
       for (int s = lane; s < nu; s += 32) {
         const int j = u.union_j[(size_t) g * UMAX + s];
         sx[s] = __ldg(a.xq + j);
-        sfp[s] = (float) __ldg(fp + j);
+        sfp[s] = __ldg(fp + j);
       }
     __syncwarp();
     if (i < a.nlocal) {
       const float4 qi = a.xq[i];
       int cx, cy, cz;
       cell_of(qi, cx, cy, cz);
-      const float fpi = (float) fp[i];
+      const float fpi = fp[i];
       const int n = a.snum[i];
-      double fx = 0.0, fy = 0.0, fz = 0.0;
+      dsacc fx, fy, fz;
       float px = 0.f, py = 0.f, pz = 0.f;
       int cnt = 0;
       for (int k = 0; k < n; k++) {
@@ -352,7 +391,7 @@ k_eam_force_union(AtomArgs a, UnionArgs u, const float4 *__restrict__ ftab, int 
         } else {
           j = __ldg(a.slist + (size_t) k * a.stride + i);
           qj = __ldg(a.xq + j);
-          fpj = (float) __ldg(fp + j);
+          fpj = __ldg(fp + j);
         }
         float dx, dy, dz;
         rel_vec(qi, cx, cy, cz, qj, a.qg, dx, dy, dz);
@@ -379,16 +418,19 @@ k_eam_force_union(AtomArgs a, UnionArgs u, const float4 *__restrict__ ftab, int 
           py += dy * fpair;
           pz += dz * fpair;
           if ((++cnt & (CHUNK - 1)) == 0) {
-            fx += (double) px;
-            fy += (double) py;
-            fz += (double) pz;
+            fx.add(px);
+            fy.add(py);
+            fz.add(pz);
             px = py = pz = 0.f;
           }
         }
       }
-      f[3 * i] = fx + (double) px;
-      f[3 * i + 1] = fy + (double) py;
-      f[3 * i + 2] = fz + (double) pz;
+      fx.add(px);
+      f[3 * i] = fx.value();
+      fy.add(py);
+      f[3 * i + 1] = fy.value();
+      fz.add(pz);
+      f[3 * i + 2] = fz.value();
     }
     __syncwarp();
   }
@@ -397,7 +439,7 @@ k_eam_force_union(AtomArgs a, UnionArgs u, const float4 *__restrict__ ftab, int 
 // force table per knot: rho'(r) c0..c2 (x,y,z of f0), r*phi c0..c6 (w of f0, f1, f2.xy)
 __global__ void __launch_bounds__(512, 2)
 k_eam_force_atoms(AtomArgs a, const float4 *__restrict__ ftab, int nr, float rdr,
-                  const double *__restrict__ fp, double *__restrict__ f) {
+                  const float *__restrict__ fp, double *__restrict__ f) {
   extern __shared__ float4 s_tab[];  // 3 float4 per knot
   for (int m = threadIdx.x; m < 3 * (nr + 1); m += blockDim.x) s_tab[m] = ftab[m];
   __syncthreads();
@@ -405,9 +447,9 @@ k_eam_force_atoms(AtomArgs a, const float4 *__restrict__ ftab, int nr, float rdr
     const float4 qi = a.xq[i];
     int cx, cy, cz;
     cell_of(qi, cx, cy, cz);
-    const float fpi = (float) fp[i];
+    const float fpi = fp[i];
     const int n = a.snum[i];
-    double fx = 0.0, fy = 0.0, fz = 0.0;
+    dsacc fx, fy, fz;
     float px = 0.f, py = 0.f, pz = 0.f;
     int cnt = 0;
     int jn = 0;
@@ -416,7 +458,7 @@ k_eam_force_atoms(AtomArgs a, const float4 *__restrict__ ftab, int nr, float rdr
     if (n > 0) {
       jn = __ldg(a.slist + i);
       qn = __ldg(a.xq + jn);
-      fpn = (float) __ldg(fp + jn);
+      fpn = __ldg(fp + jn);
     }
     for (int k = 0; k < n; k++) {
       const int j = jn;
@@ -425,7 +467,7 @@ k_eam_force_atoms(AtomArgs a, const float4 *__restrict__ ftab, int nr, float rdr
       if (k + 1 < n) {  // next entry's gathers in flight during this one
         jn = __ldg(a.slist + (size_t) (k + 1) * a.stride + i);
         qn = __ldg(a.xq + jn);
-        fpn = (float) __ldg(fp + jn);
+        fpn = __ldg(fp + jn);
       }
       float dx, dy, dz;
       rel_vec(qi, cx, cy, cz, qj, a.qg, dx, dy, dz);
@@ -449,16 +491,19 @@ k_eam_force_atoms(AtomArgs a, const float4 *__restrict__ ftab, int nr, float rdr
         py += dy * fpair;
         pz += dz * fpair;
         if ((++cnt & (CHUNK - 1)) == 0) {
-          fx += (double) px;
-          fy += (double) py;
-          fz += (double) pz;
+          fx.add(px);
+          fy.add(py);
+          fz.add(pz);
           px = py = pz = 0.f;
         }
       }
     }
-    f[3 * i] = fx + (double) px;
-    f[3 * i + 1] = fy + (double) py;
-    f[3 * i + 2] = fz + (double) pz;
+    fx.add(px);
+    f[3 * i] = fx.value();
+    fy.add(py);
+    f[3 * i + 1] = fy.value();
+    fz.add(pz);
+    f[3 * i + 2] = fz.value();
   }
 }
 
@@ -474,7 +519,7 @@ k_lj_atoms(AtomArgs a, const int *__restrict__ type, const float *__restrict__ l
     cell_of(qi, cx, cy, cz);
     const int it = type[i];
     const int n = a.num[i];
-    double fx = 0.0, fy = 0.0, fz = 0.0;
+    dsacc fx, fy, fz;
     float px = 0.f, py = 0.f, pz = 0.f;
     for (int k = 0; k < n; k++) {
       int j = __ldg(a.list + (size_t) k * a.stride + i);
@@ -494,15 +539,18 @@ k_lj_atoms(AtomArgs a, const int *__restrict__ type, const float *__restrict__ l
         pz += dz * fpair;
       }
       if ((k & (CHUNK - 1)) == CHUNK - 1) {
-        fx += (double) px;
-        fy += (double) py;
-        fz += (double) pz;
+        fx.add(px);
+        fy.add(py);
+        fz.add(pz);
         px = py = pz = 0.f;
       }
     }
-    f[3 * i] = fx + (double) px;
-    f[3 * i + 1] = fy + (double) py;
-    f[3 * i + 2] = fz + (double) pz;
+    fx.add(px);
+    f[3 * i] = fx.value();
+    fy.add(py);
+    f[3 * i + 1] = fy.value();
+    fz.add(pz);
+    f[3 * i + 2] = fz.value();
   }
 }
 
@@ -700,18 +748,6 @@ k_site_q(const float2 *__restrict__ node_hl, const int *__restrict__ etype,
           pack_u(ds_madd(c, D[0], U[0]), ds_madd(c, D[1], U[1]), ds_madd(c, D[2], U[2]), pg);
     }
   }
-}
-
-__device__ __forceinline__ float fprime32(float rho, const float4 *__restrict__ fp4, int nrho,
-                                          float rdrho) {
-  float p = rho * rdrho + 1.0f;
-  int m = (int) p;
-  m = m < nrho - 1 ? m : nrho - 1;
-  m = 1 > m ? 1 : m;
-  p -= (float) m;
-  p = fminf(p, 1.0f);
-  const float4 c = __ldg(fp4 + m);
-  return (c.x * p + c.y) * p + c.z;
 }
 
 // F'(rho) at the referenced sites, rho = sum_k N_k erho_k (pair_eam.cpp:1060-1065)
@@ -917,7 +953,7 @@ k_ipg(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr, float lj1, 
     }
     int cx, cy, cz;
     cell_of(qi, cx, cy, cz);
-    double acc = 0.0, fx = 0.0, fy = 0.0, fz = 0.0;
+    dsacc acc, fx, fy, fz;
     float part = 0.f, px = 0.f, py = 0.f, pz = 0.f;
     int sn = 0, cnt = 0;
     float4 qn = qi;
@@ -972,33 +1008,29 @@ k_ipg(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr, float lj1, 
           pz += dz * fpair;
         }
         if ((++cnt & (CHUNK - 1)) == 0) {
-          acc += (double) part;
-          fx += (double) px;
-          fy += (double) py;
-          fz += (double) pz;
+          acc.add(part);
+          fx.add(px);
+          fy.add(py);
+          fz.add(pz);
           part = px = py = pz = 0.f;
         }
       }
     }
     if (DENSITY) {
-      acc += (double) part;
-#pragma unroll
-      for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-      if (live && lane == 0) out[NPE * (size_t) e + it % NPE] = acc;
+      acc.add(part);
+      group_sum<G>(acc);
+      if (live && lane == 0) out[NPE * (size_t) e + it % NPE] = acc.value();
     } else {
-      fx += (double) px;
-      fy += (double) py;
-      fz += (double) pz;
-#pragma unroll
-      for (int o = G / 2; o > 0; o >>= 1) {
-        fx += __shfl_xor_sync(0xffffffffu, fx, o);
-        fy += __shfl_xor_sync(0xffffffffu, fy, o);
-        fz += __shfl_xor_sync(0xffffffffu, fz, o);
-      }
+      fx.add(px);
+      fy.add(py);
+      fz.add(pz);
+      group_sum<G>(fx);
+      group_sum<G>(fy);
+      group_sum<G>(fz);
       if (live && lane == 0) {
-        out[3 * r] = fx;
-        out[3 * r + 1] = fy;
-        out[3 * r + 2] = fz;
+        out[3 * r] = fx.value();
+        out[3 * r + 1] = fy.value();
+        out[3 * r + 2] = fz.value();
       }
     }
   }
@@ -1049,14 +1081,14 @@ void pack_rel(const double4 *x, int n, double l0x, double l0y, double l0z, doubl
 }
 
 void eam_rho_atoms(const MixedAtoms &m, const float4 *rhor_val, const EamTables &e,
-                   double *rho, double *fp, cudaStream_t s) {
+                   const float4 *fp4, double *rho, float *fp, cudaStream_t s) {
   if (m.nlocal <= 0) return;
   AtomArgs a{m.x, m.xq, m.qg, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
              m.band_hi, m.cutsq, m.snum, m.slist};
   size_t smem = sizeof(float4) * (e.nr + 1);
   int g = persistent_grid((const void *) k_eam_rho_atoms, m.block, smem, m.nlocal);
-  k_eam_rho_atoms<<<g, m.block, smem, s>>>(a, rhor_val, e.nr, (float) e.rdr, e.frho, e.nrho,
-                                       e.rdrho, rho, fp);
+  k_eam_rho_atoms<<<g, m.block, smem, s>>>(a, rhor_val, e.nr, (float) e.rdr, fp4, e.nrho,
+                                           (float) e.rdrho, rho, fp);
   check(cudaGetLastError(), "eam_rho_atoms_mixed");
 }
 
@@ -1078,21 +1110,22 @@ static int union_grid(const void *k, size_t smem, int nlocal) {
 
 void eam_rho_union(const MixedAtoms &m, const int *union_j, const int *union_n,
                    const unsigned short *slot, unsigned short *sslot, const float4 *rhor_val,
-                   const EamTables &e, double *rho, double *fp, cudaStream_t s) {
+                   const EamTables &e, const float4 *fp4, double *rho, float *fp,
+                   cudaStream_t s) {
   if (m.nlocal <= 0) return;
   AtomArgs a{m.x, m.xq, m.qg, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
              m.band_hi, m.cutsq, m.snum, m.slist};
   UnionArgs u{union_j, union_n, slot, sslot};
   size_t smem = sizeof(float4) * ((e.nr + 1) + (size_t) UWARPS * UMAX);
   int g = union_grid((const void *) k_eam_rho_union, smem, m.nlocal);
-  k_eam_rho_union<<<g, UGROUP * UWARPS, smem, s>>>(a, u, rhor_val, e.nr, (float) e.rdr, e.frho,
-                                                  e.nrho, e.rdrho, rho, fp);
+  k_eam_rho_union<<<g, UGROUP * UWARPS, smem, s>>>(a, u, rhor_val, e.nr, (float) e.rdr, fp4,
+                                                  e.nrho, (float) e.rdrho, rho, fp);
   check(cudaGetLastError(), "eam_rho_union");
 }
 
 void eam_force_union(const MixedAtoms &m, const int *union_j, const int *union_n,
                      const unsigned short *sslot, const float4 *ftab, const EamTables &e,
-                     const double *fp, double *f, cudaStream_t s) {
+                     const float *fp, double *f, cudaStream_t s) {
   if (m.nlocal <= 0) return;
   AtomArgs a{m.x, m.xq, m.qg, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
              m.band_hi, m.cutsq, m.snum, m.slist};
@@ -1105,7 +1138,7 @@ void eam_force_union(const MixedAtoms &m, const int *union_j, const int *union_n
 }
 
 void eam_force_atoms(const MixedAtoms &m, const float4 *ftab, const EamTables &e,
-                     const double *fp, double *f, cudaStream_t s) {
+                     const float *fp, double *f, cudaStream_t s) {
   if (m.nlocal <= 0) return;
   AtomArgs a{m.x, m.xq, m.qg, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
              m.band_hi, m.cutsq, m.snum, m.slist};
