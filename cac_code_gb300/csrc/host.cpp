@@ -301,6 +301,10 @@ struct cacg_context {
   // direct kernels' 32 (1.71 vs 0.77 ms for the density pass), so off by default
   bool mixed_union = false;
   long long list_builds = 0, union_of = -1;
+  // the atom lists reordered for the mixed EAM passes (in-range entries
+  // first), once per list build
+  long long part_of = -1;
+  DBuf<int> d_mlist;
   DBuf<int> d_union_j, d_union_n;
   DBuf<unsigned short> d_slot, d_sslot;
   bool ran = false;  // steps taken since init (positions may have left the box)
@@ -491,6 +495,7 @@ cacg_context::~cacg_context() {
   d_amask.release();
   d_emask.release();
   d_union_j.release();
+  d_mlist.release();
   d_union_n.release();
   d_slot.release();
   d_sslot.release();
@@ -2177,6 +2182,16 @@ void cacg_context::pair_compute_mixed(int pass) {
     mixed::union_build(d_num.p, d_list.p, stride, nlocal, d_union_j.p, d_union_n.p, d_slot.p, s);
     launches++;
     union_of = list_builds;
+  }
+  if (!mixed_union) {
+    if (pass == 1 && part_of != list_builds) {
+      d_mlist.ensure((size_t) maxneigh * stride, s);
+      mixed::list_partition(d_xh.p, m.qg, d_num.p, d_list.p, stride, nlocal, m.band_hi, d_mlist.p,
+                            s);
+      launches++;
+      part_of = list_builds;
+    }
+    m.list = d_mlist.p;
   }
   if (pass == 1) {
     d_rho.ensure(nall, s);

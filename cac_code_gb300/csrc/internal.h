@@ -303,6 +303,9 @@ void site_q(const float2 *node_hl, const int *etype, const int *site_base, const
 void site_fp(const double *erho, const int *etype, const int *site_base, const int *nae,
              const unsigned long long *mask, int maxlines, const float4 *fp4, int nrho,
              double rdrho, int nelem, float *fp, cudaStream_t s);
+// each atom's list reordered: entries within cut_rsq (packed positions) first
+void list_partition(const float4 *xq, float g, const int *num, const int *list, int stride,
+                    int nlocal, float cut_rsq, int *out, cudaStream_t s);
 // neighbor unions of 32-atom groups staged in shared memory (EAM atom passes)
 int union_max();
 void union_build(const int *num, const int *list, int stride, int nlocal, int *union_j,

@@ -121,21 +121,29 @@ __global__ void k_pack_rel(const double4 *__restrict__ x, int n, double l0x, dou
   xq[i] = make_float4(r[0], r[1], r[2], __int_as_float(w));
 }
 
-__device__ __forceinline__ void cell_of(const float4 &q, int &cx, int &cy, int &cz) {
+// The cell fields as floats without a conversion instruction: a field k below
+// 2^23 OR-ed into the bits of 2^23 reads as the float 2^23 + k, so the
+// difference of two such floats is the exact integer difference of the
+// fields.  The y field is left in place (bits 12-21), its difference scaled
+// by 2^-12; the z field (bits 22-31) is shifted down.
+constexpr int MAGIC = 0x4B000000;  // the bits of 2^23
+
+__device__ __forceinline__ void cell_of(const float4 &q, float &cx, float &cy, float &cz) {
   const int w = __float_as_int(q.w);
-  cx = w & 0xFFF;
-  cy = (w >> 12) & 0x3FF;
-  cz = (int) ((unsigned) w >> 22);
+  cx = __int_as_float((w & 0xFFF) | MAGIC);
+  cy = __int_as_float((w & 0x3FF000) | MAGIC);
+  cz = __int_as_float((int) ((unsigned) w >> 22) | MAGIC);
 }
 
 // pair vector from cell-relative coordinates: (q_i - q_j) + g * (cell_i - cell_j)
-__device__ __forceinline__ void rel_vec(const float4 &qi, int cx, int cy, int cz, const float4 &qj,
-                                        float g, float &dx, float &dy, float &dz) {
-  int jx, jy, jz;
+__device__ __forceinline__ void rel_vec(const float4 &qi, float cx, float cy, float cz,
+                                        const float4 &qj, float g, float &dx, float &dy,
+                                        float &dz) {
+  float jx, jy, jz;
   cell_of(qj, jx, jy, jz);
-  dx = (qi.x - qj.x) + g * (float) (cx - jx);
-  dy = (qi.y - qj.y) + g * (float) (cy - jy);
-  dz = (qi.z - qj.z) + g * (float) (cz - jz);
+  dx = (qi.x - qj.x) + g * (cx - jx);
+  dy = (qi.y - qj.y) + (g * (1.0f / 4096.0f)) * (cy - jy);
+  dz = (qi.z - qj.z) + g * (cz - jz);
 }
 
 struct AtomArgs {
@@ -159,7 +167,7 @@ k_eam_rho_atoms(AtomArgs a, const float4 *__restrict__ rhor_val, int nr, float r
   __syncthreads();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.nlocal; i += gridDim.x * blockDim.x) {
     const float4 qi = a.xq[i];
-    int cx, cy, cz;
+    float cx, cy, cz;
     cell_of(qi, cx, cy, cz);
     const int n = a.num[i];
     dsacc acc;
@@ -203,6 +211,31 @@ k_eam_rho_atoms(AtomArgs a, const float4 *__restrict__ rhor_val, int nr, float r
     rho[i] = acc.value();
     fp[i] = fprime32(__fadd_rn(acc.h, acc.l), fp4, nrho, rdrho);
   }
+}
+
+// The list of each atom reordered at each build: the entries within the
+// cutoff first (at the positions of the build), the rest after, each part in
+// list order.  Atoms move little between builds, so in the density pass the
+// lanes of a warp meet the in-range entries together and then the
+// out-of-range ones together, instead of diverging on every entry.
+__global__ void k_list_partition(const float4 *__restrict__ xq, float g, const int *__restrict__ num,
+                                 const int *__restrict__ list, int stride, int nlocal,
+                                 float cut_rsq, int *__restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nlocal) return;
+  const float4 qi = xq[i];
+  float cx, cy, cz;
+  cell_of(qi, cx, cy, cz);
+  const int n = num[i];
+  int m = 0;
+  for (int pass = 0; pass < 2; pass++)
+    for (int k = 0; k < n; k++) {
+      const int j = __ldg(list + (size_t) k * stride + i);
+      float dx, dy, dz;
+      rel_vec(qi, cx, cy, cz, __ldg(xq + j), g, dx, dy, dz);
+      const bool near = dx * dx + dy * dy + dz * dz <= cut_rsq;
+      if (near == (pass == 0)) out[(size_t) m++ * stride + i] = j;
+    }
 }
 
 // ---- neighbor unions staged in shared memory (EAM atom passes) ----
@@ -302,7 +335,7 @@ k_eam_rho_union(AtomArgs a, UnionArgs u, const float4 *__restrict__ rhor_val, in
     __syncwarp();
     if (i < a.nlocal) {
       const float4 qi = a.xq[i];
-      int cx, cy, cz;
+      float cx, cy, cz;
       cell_of(qi, cx, cy, cz);
       const int n = a.num[i];
       dsacc acc;
@@ -373,7 +406,7 @@ k_eam_force_union(AtomArgs a, UnionArgs u, const float4 *__restrict__ ftab, int 
     __syncwarp();
     if (i < a.nlocal) {
       const float4 qi = a.xq[i];
-      int cx, cy, cz;
+      float cx, cy, cz;
       cell_of(qi, cx, cy, cz);
       const float fpi = fp[i];
       const int n = a.snum[i];
@@ -445,7 +478,7 @@ k_eam_force_atoms(AtomArgs a, const float4 *__restrict__ ftab, int nr, float rdr
   __syncthreads();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.nlocal; i += gridDim.x * blockDim.x) {
     const float4 qi = a.xq[i];
-    int cx, cy, cz;
+    float cx, cy, cz;
     cell_of(qi, cx, cy, cz);
     const float fpi = fp[i];
     const int n = a.snum[i];
@@ -515,7 +548,7 @@ k_lj_atoms(AtomArgs a, const int *__restrict__ type, const float *__restrict__ l
            const double *__restrict__ cutsq64, double *__restrict__ f) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.nlocal; i += gridDim.x * blockDim.x) {
     const float4 qi = a.xq[i];
-    int cx, cy, cz;
+    float cx, cy, cz;
     cell_of(qi, cx, cy, cz);
     const int it = type[i];
     const int n = a.num[i];
@@ -951,7 +984,7 @@ k_ipg(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr, float lj1, 
       qi = __ldg(a.ip_q + r);
       if (EAM && !DENSITY) fpi = __ldg(a.row_fp + r);
     }
-    int cx, cy, cz;
+    float cx, cy, cz;
     cell_of(qi, cx, cy, cz);
     dsacc acc, fx, fy, fz;
     float part = 0.f, px = 0.f, py = 0.f, pz = 0.f;
@@ -1090,6 +1123,14 @@ void eam_rho_atoms(const MixedAtoms &m, const float4 *rhor_val, const EamTables 
   k_eam_rho_atoms<<<g, m.block, smem, s>>>(a, rhor_val, e.nr, (float) e.rdr, fp4, e.nrho,
                                            (float) e.rdrho, rho, fp);
   check(cudaGetLastError(), "eam_rho_atoms_mixed");
+}
+
+void list_partition(const float4 *xq, float g, const int *num, const int *list, int stride,
+                    int nlocal, float cut_rsq, int *out, cudaStream_t s) {
+  if (nlocal <= 0) return;
+  k_list_partition<<<nblk(nlocal, 128), 128, 0, s>>>(xq, g, num, list, stride, nlocal, cut_rsq,
+                                                    out);
+  check(cudaGetLastError(), "list_partition");
 }
 
 void union_build(const int *num, const int *list, int stride, int nlocal, int *union_j,
