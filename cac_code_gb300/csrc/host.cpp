@@ -2148,7 +2148,7 @@ void cacg_context::pair_compute_mixed(int pass) {
       check(cudaMemsetAsync(d_misc.p + 9, 0, sizeof(int), s), "oob");
       oob_zeroed = true;
     }
-    mixed::pack_rel(d_x.p, nall, l0[0], l0[1], l0[2], g, d_xh.p, d_misc.p + 9, s);
+    mixed::pack_rel(d_x.p, nall, mixed::make_pack_grid(l0, g, d_misc.p + 9), d_xh.p, s);
     launches++;
   }
   m.xq = d_xh.p;
@@ -2227,14 +2227,7 @@ void cacg_context::pair_ecompute_mixed() {
     check(cudaMemsetAsync(d_misc.p + 9, 0, sizeof(int), s), "oob");
     oob_zeroed = true;
   }
-  mixed::PackGrid pg{};
-  for (int d = 0; d < 3; d++) {
-    pg.l0h[d] = (float) l0[d];
-    pg.l0l[d] = (float) (l0[d] - (double) pg.l0h[d]);
-  }
-  pg.g = (float) g;
-  pg.ig = (float) (1.0 / g);
-  pg.oob = d_misc.p + 9;
+  const mixed::PackGrid pg = mixed::make_pack_grid(l0, g, d_misc.p + 9);
   d_site_q.ensure(std::max(nsites, 1), s);
   d_node_hl.ensure((size_t) 24 * nall, s);
   mixed::node_split(d_nodex.p, nall, d_node_hl.p, s);

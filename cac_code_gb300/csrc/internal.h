@@ -288,8 +288,8 @@ struct MixedElems {
 };
 // cell-relative packed coordinates for the atom passes; *oob counts atoms
 // outside the 4096 x 1024 x 1024-cell range
-void pack_rel(const double4 *x, int n, double l0x, double l0y, double l0z, double g,
-              float4 *xq, int *oob, cudaStream_t s);
+PackGrid make_pack_grid(const double l0[3], double g, int *oob);
+void pack_rel(const double4 *x, int n, const PackGrid &pg, float4 *xq, cudaStream_t s);
 void node_split(const double *nodex, int n, float2 *hl, cudaStream_t s);
 // per element and lattice line (ii, jj): bit kk set when site (ii, jj, kk) is
 // referenced by an integration-point list

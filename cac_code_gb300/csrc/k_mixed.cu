@@ -95,32 +95,6 @@ __device__ __forceinline__ bool inside64(const double4 &a, const double4 &b, dou
   return dx * dx + dy * dy + dz * dz < cutsq;
 }
 
-__global__ void k_pack_rel(const double4 *__restrict__ x, int n, double l0x, double l0y,
-                           double l0z, double g, double ig, float4 *__restrict__ xq,
-                           int *__restrict__ oob) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double4 p = x[i];
-  const double u[3] = {p.x - l0x, p.y - l0y, p.z - l0z};
-  const int lim[3] = {4095, 1023, 1023};
-  int c[3];
-  float r[3];
-  bool bad = false;
-#pragma unroll
-  for (int d = 0; d < 3; d++) {
-    int k = (int) floor(u[d] * ig);
-    if (k < 0 || k > lim[d]) {
-      bad = true;
-      k = k < 0 ? 0 : lim[d];
-    }
-    c[d] = k;
-    r[d] = (float) (u[d] - (double) k * g);
-  }
-  if (bad) atomicAdd(oob, 1);
-  const int w = c[0] | (c[1] << 12) | (c[2] << 22);
-  xq[i] = make_float4(r[0], r[1], r[2], __int_as_float(w));
-}
-
 // The cell fields as floats without a conversion instruction: a field k below
 // 2^23 OR-ed into the bits of 2^23 reads as the float 2^23 + k, so the
 // difference of two such floats is the exact integer difference of the
@@ -640,13 +614,28 @@ __device__ __forceinline__ ds ds_frac(int k, int d) {
   return ds{q, __fdiv_rn(r, fd)};
 }
 
+// A double as a double-single by integer operations on its bits, without an
+// FP64 instruction: hi keeps the sign, the exponent and the top 23 stored
+// mantissa bits (a truncation, exact in FP32), lo the remaining 29 bits
+// scaled by 2^(e-1075) (rounded once).  Zero and values below 2^-74 give 0.
+__device__ __forceinline__ ds ds_of_double(double x) {
+  const unsigned bh = (unsigned) __double2hiint(x), bl = (unsigned) __double2loint(x);
+  const int ex = (int) ((bh >> 20) & 0x7FF);
+  if (ex < 949) return ds{0.f, 0.f};
+  const unsigned sign = bh & 0x80000000u;
+  const float h = __uint_as_float(sign | ((unsigned) (ex - 896) << 23) | ((bh & 0xFFFFFu) << 3) |
+                                  (bl >> 29));
+  const float scale = __uint_as_float((unsigned) (ex - 948) << 23);  // 2^(ex - 1075)
+  const float l = __fmul_rn(__uint2float_rn(bl & 0x1FFFFFFFu), scale);
+  return ds{h, sign ? -l : l};
+}
+
 // node coordinates as double-single pairs, once per element and step
 __global__ void k_node_split(const double *__restrict__ nodex, int n, float2 *__restrict__ hl) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * 24) return;
-  const double x = nodex[t];
-  const float h = (float) x;
-  hl[t] = make_float2(h, (float) (x - (double) h));
+  const ds v = ds_of_double(nodex[t]);
+  hl[t] = make_float2(v.h, v.l);
 }
 
 __device__ __forceinline__ ds node_ds(const float2 *nx, int k, int d) {
@@ -674,6 +663,16 @@ __device__ __forceinline__ float4 pack_u(ds ux, ds uy, ds uz, const PackGrid &pg
   const float rz = rel_of(uz, pg.g, pg.ig, 1023, cz, bad);
   if (bad && pg.oob) atomicAdd(pg.oob, 1);
   return make_float4(rx, ry, rz, __int_as_float(cx | (cy << 12) | (cz << 22)));
+}
+
+__global__ void k_pack_rel(const double4 *__restrict__ x, int n, PackGrid pg,
+                           float4 *__restrict__ xq) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double4 p = x[i];
+  xq[i] = pack_u(ds_sub(ds_of_double(p.x), ds{pg.l0h[0], pg.l0l[0]}),
+                 ds_sub(ds_of_double(p.y), ds{pg.l0h[1], pg.l0l[1]}),
+                 ds_sub(ds_of_double(p.z), ds{pg.l0h[2], pg.l0l[2]}), pg);
 }
 
 // the x-lerps of one lattice column ii: E0..E3 of the y/z edges (-,-), (+,-), (-,+), (+,+)
@@ -771,14 +770,22 @@ k_site_q(const float2 *__restrict__ node_hl, const int *__restrict__ etype,
       }
     }
     __syncthreads();
-    const int nsite = nl * naz;
-    for (int t = threadIdx.x; t < nsite; t += blockDim.x) {
-      const int l = t / naz, kk = t - l * naz;
-      if (kk < 64 && !((s_mask[l] >> kk) & 1ull)) continue;
-      const ds c = s_c[kk];
-      const ds *U = s_U + 3 * l, *D = s_D + 3 * l;
-      site_q[base + (size_t) L0 * naz + t] =
-          pack_u(ds_madd(c, D[0], U[0]), ds_madd(c, D[1], U[1]), ds_madd(c, D[2], U[2]), pg);
+    // site t = l * naz + kk of the chunk; (l, kk) stepped by LCH without a division
+    const int nsite = nl * naz, dl = LCH / naz, dk = LCH - dl * naz;
+    int l = threadIdx.x / naz, kk = threadIdx.x - l * naz;
+    for (int t = threadIdx.x; t < nsite; t += LCH) {
+      if (kk >= 64 || ((s_mask[l] >> kk) & 1ull)) {
+        const ds c = s_c[kk];
+        const ds *U = s_U + 3 * l, *D = s_D + 3 * l;
+        site_q[base + (size_t) L0 * naz + t] =
+            pack_u(ds_madd(c, D[0], U[0]), ds_madd(c, D[1], U[1]), ds_madd(c, D[2], U[2]), pg);
+      }
+      l += dl;
+      kk += dk;
+      if (kk >= naz) {
+        kk -= naz;
+        l++;
+      }
     }
   }
 }
@@ -817,12 +824,19 @@ k_site_fp(const double *__restrict__ erho, const int *__restrict__ etype,
       s_D[threadIdx.x] = T - B;
     }
     __syncthreads();
-    const int nsite = nl * naz;
-    for (int t = threadIdx.x; t < nsite; t += blockDim.x) {
-      const int l = t / naz, kk = t - l * naz;
-      if (kk < 64 && !((s_mask[l] >> kk) & 1ull)) continue;
-      const float rho = s_U[l] + ((float) kk * rz) * s_D[l];
-      site_fp[base + (size_t) L0 * naz + t] = fprime32(rho, fp4, nrho, rdrho);
+    const int nsite = nl * naz, dl = LCH / naz, dk = LCH - dl * naz;
+    int l = threadIdx.x / naz, kk = threadIdx.x - l * naz;
+    for (int t = threadIdx.x; t < nsite; t += LCH) {
+      if (kk >= 64 || ((s_mask[l] >> kk) & 1ull)) {
+        const float rho = s_U[l] + ((float) kk * rz) * s_D[l];
+        site_fp[base + (size_t) L0 * naz + t] = fprime32(rho, fp4, nrho, rdrho);
+      }
+      l += dl;
+      kk += dk;
+      if (kk >= naz) {
+        kk -= naz;
+        l++;
+      }
     }
   }
 }
@@ -1106,10 +1120,21 @@ int persistent_grid(const void *kernel, int threads, size_t smem, long long work
 
 }  // namespace
 
-void pack_rel(const double4 *x, int n, double l0x, double l0y, double l0z, double g,
-              float4 *xq, int *oob, cudaStream_t s) {
+PackGrid make_pack_grid(const double l0[3], double g, int *oob) {
+  PackGrid pg{};
+  for (int d = 0; d < 3; d++) {
+    pg.l0h[d] = (float) l0[d];
+    pg.l0l[d] = (float) (l0[d] - (double) pg.l0h[d]);
+  }
+  pg.g = (float) g;
+  pg.ig = (float) (1.0 / g);
+  pg.oob = oob;
+  return pg;
+}
+
+void pack_rel(const double4 *x, int n, const PackGrid &pg, float4 *xq, cudaStream_t s) {
   if (n <= 0) return;
-  k_pack_rel<<<nblk(n, 256), 256, 0, s>>>(x, n, l0x, l0y, l0z, g, 1.0 / g, xq, oob);
+  k_pack_rel<<<nblk(n, 256), 256, 0, s>>>(x, n, pg, xq);
   check(cudaGetLastError(), "pack_rel");
 }
 
