@@ -304,7 +304,12 @@ struct cacg_context {
   // the atom lists reordered for the mixed EAM passes (in-range entries
   // first), once per list build
   long long part_of = -1;
-  DBuf<int> d_mlist;
+  DBuf<int> d_mlist, d_nnear;
+  // packed coordinates at the reorder and their grid: the density pass skips
+  // the far part of each list while no atom has moved 0.495 A since then
+  DBuf<float4> d_xq_ref;
+  bool mixed_cull = true;  // "tune cull yes|no"
+  double ref_l0[3] = {0, 0, 0}, ref_g = 0;
   DBuf<int> d_union_j, d_union_n;
   DBuf<unsigned short> d_slot, d_sslot;
   bool ran = false;  // steps taken since init (positions may have left the box)
@@ -496,6 +501,8 @@ cacg_context::~cacg_context() {
   d_emask.release();
   d_union_j.release();
   d_mlist.release();
+  d_nnear.release();
+  d_xq_ref.release();
   d_union_n.release();
   d_slot.release();
   d_sslot.release();
@@ -695,6 +702,8 @@ void cacg_context::command(const std::string &raw) {
     // tune block 128|256|512: threads per block of the mixed-precision kernels
     // tune union yes|no: neighbor unions staged in shared memory (EAM atom passes)
     // tune ip_group 4|8|16: lanes per integration point in the mixed element passes
+    // tune cull yes|no: the mixed EAM density pass skips list entries that no
+    //   displacement since the list reorder can bring within the cutoff
     if (a.size() != 2) fail(CACG_EINVAL, "Illegal tune command");
     if (a[0] == "block") {
       int b = inumeric(a[1]);
@@ -704,6 +713,9 @@ void cacg_context::command(const std::string &raw) {
       int gsz = inumeric(a[1]);
       if (gsz != 4 && gsz != 8 && gsz != 16) fail(CACG_EINVAL, "tune ip_group takes 4, 8 or 16");
       mixed_ip_group = gsz;
+    } else if (a[0] == "cull") {
+      if (a[1] != "yes" && a[1] != "no") fail(CACG_EINVAL, "tune cull takes yes or no");
+      mixed_cull = a[1] == "yes";
     } else if (a[0] == "union") {
       if (a[1] != "yes" && a[1] != "no") fail(CACG_EINVAL, "tune union takes yes or no");
       mixed_union = a[1] == "yes";
@@ -2148,7 +2160,17 @@ void cacg_context::pair_compute_mixed(int pass) {
       check(cudaMemsetAsync(d_misc.p + 9, 0, sizeof(int), s), "oob");
       oob_zeroed = true;
     }
-    mixed::pack_rel(d_x.p, nall, mixed::make_pack_grid(l0, g, d_misc.p + 9), d_xh.p, s);
+    // the displacement since the list reorder (slot 11, float bits), measured
+    // against the reorder's packed coordinates when the lists and the grid are
+    // unchanged, else set huge so that the lists are reordered in this pass;
+    // slot 12: reordered in this pass
+    const bool same = part_of == list_builds && ref_g == g && ref_l0[0] == l0[0] &&
+                      ref_l0[1] == l0[1] && ref_l0[2] == l0[2];
+    check(cudaMemsetAsync(d_misc.p + 11, same ? 0 : 0x7F, sizeof(int), s), "dmax");
+    check(cudaMemsetAsync(d_misc.p + 12, 0, sizeof(int), s), "reordered");
+    mixed::pack_rel(d_x.p, nall, mixed::make_pack_grid(l0, g, d_misc.p + 9), d_xh.p,
+                    same ? d_xq_ref.p : nullptr, nlocal,
+                    reinterpret_cast<unsigned *>(d_misc.p + 11), s);
     launches++;
   }
   m.xq = d_xh.p;
@@ -2184,14 +2206,21 @@ void cacg_context::pair_compute_mixed(int pass) {
     union_of = list_builds;
   }
   if (!mixed_union) {
-    if (pass == 1 && part_of != list_builds) {
+    if (pass == 1) {
       d_mlist.ensure((size_t) maxneigh * stride, s);
-      mixed::list_partition(d_xh.p, m.qg, d_num.p, d_list.p, stride, nlocal, m.band_hi, d_mlist.p,
-                            s);
+      d_nnear.ensure(std::max(nlocal, 1), s);
+      d_xq_ref.ensure(std::max(nlocal, 1), s);
+      mixed::list_partition(d_xh.p, m.qg, d_num.p, d_list.p, stride, nlocal, m.band_hi,
+                            (float) std::sqrt(cutforcesq), d_mlist.p, d_nnear.p, d_xq_ref.p,
+                            reinterpret_cast<unsigned *>(d_misc.p + 11), s);
+      for (int d = 0; d < 3; d++) ref_l0[d] = l0[d];
+      ref_g = g;
       launches++;
       part_of = list_builds;
     }
     m.list = d_mlist.p;
+    m.nnear = mixed_cull ? d_nnear.p : nullptr;
+    m.dmax2 = reinterpret_cast<const unsigned *>(d_misc.p + 11);
   }
   if (pass == 1) {
     d_rho.ensure(nall, s);

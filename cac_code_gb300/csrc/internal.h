@@ -255,6 +255,11 @@ struct MixedAtoms {
   float cutsq_f, band_lo, band_hi;  // FP32 test; [band_lo, band_hi] re-tested in FP64
   double cutsq;
   int *snum, *slist;  // EAM: short list written by the density pass, read by the force pass
+  // EAM density pass over a reordered list: nnear[i] entries lie within the
+  // cutoff + 1 A at the reorder; dmax2 = the largest squared displacement
+  // since (float bits); null: every entry is scanned
+  const int *nnear = nullptr;
+  const unsigned *dmax2 = nullptr;
   int block = 512;    // threads per block of the persistent grids (autotuned)
 };
 // The packing grid of the cell-relative coordinates: cells of a power-of-two
@@ -289,7 +294,10 @@ struct MixedElems {
 // cell-relative packed coordinates for the atom passes; *oob counts atoms
 // outside the 4096 x 1024 x 1024-cell range
 PackGrid make_pack_grid(const double l0[3], double g, int *oob);
-void pack_rel(const double4 *x, int n, const PackGrid &pg, float4 *xq, cudaStream_t s);
+// with ref (packed coordinates of the list reorder, same grid): the largest
+// squared displacement of the first nref atoms is max-folded into *dmax2
+void pack_rel(const double4 *x, int n, const PackGrid &pg, float4 *xq, const float4 *ref, int nref,
+              unsigned *dmax2, cudaStream_t s);
 void node_split(const double *nodex, int n, float2 *hl, cudaStream_t s);
 // per element and lattice line (ii, jj): bit kk set when site (ii, jj, kk) is
 // referenced by an integration-point list
@@ -303,9 +311,13 @@ void site_q(const float2 *node_hl, const int *etype, const int *site_base, const
 void site_fp(const double *erho, const int *etype, const int *site_base, const int *nae,
              const unsigned long long *mask, int maxlines, const float4 *fp4, int nrho,
              double rdrho, int nelem, float *fp, cudaStream_t s);
-// each atom's list reordered: entries within cut_rsq (packed positions) first
+// each atom's list reordered (entries within cut_rsq at the packed positions,
+// then those within cutoff + 1 A, counted together in nnear, then the rest)
+// when the displacement since the last reorder (dmax2[0], against ref) no
+// longer allows culling; it then sets ref to the positions and dmax2[1] = 1
 void list_partition(const float4 *xq, float g, const int *num, const int *list, int stride,
-                    int nlocal, float cut_rsq, int *out, cudaStream_t s);
+                    int nlocal, float cut_rsq, float cutoff, int *out, int *nnear, float4 *ref,
+                    unsigned *dmax2, cudaStream_t s);
 // neighbor unions of 32-atom groups staged in shared memory (EAM atom passes)
 int union_max();
 void union_build(const int *num, const int *list, int stride, int nlocal, int *union_j,

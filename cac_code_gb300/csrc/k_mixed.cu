@@ -129,7 +129,25 @@ struct AtomArgs {
   float cutsq_f, band_lo, band_hi;  // [band_lo, band_hi]: decide in FP64
   double cutsq;
   int *snum, *slist;  // short list written by the density pass, read by the force pass
+  // displacement culling of the density pass (null: every entry is scanned):
+  // nnear[i] leading entries of the reordered list lie within r_c + CULL_DELTA
+  // at the reorder; the rest may be skipped while twice the largest
+  // displacement since then (dmax2: its square, float bits) stays below
+  // CULL_DELTA - CULL_MARGIN
+  const int *nnear;
+  const unsigned *dmax2;  // [0]: squared displacement bits; [1]: reordered in this step
 };
+
+constexpr float CULL_DELTA = 1.0f, CULL_MARGIN = 0.01f;
+
+__device__ __forceinline__ bool moved_little(const unsigned *dmax2) {
+  return 2.0f * sqrtf(__uint_as_float(dmax2[0])) + CULL_MARGIN <= CULL_DELTA;
+}
+
+__device__ __forceinline__ bool cull_ok(const unsigned *dmax2) {
+  return dmax2[1] != 0u || moved_little(dmax2);
+}
+
 
 // 40 registers at three 512-thread blocks per SM (48 warps): more gathers in flight
 __global__ void __launch_bounds__(512, 3)
@@ -139,11 +157,12 @@ k_eam_rho_atoms(AtomArgs a, const float4 *__restrict__ rhor_val, int nr, float r
   extern __shared__ float4 s_val[];
   for (int m = threadIdx.x; m <= nr; m += blockDim.x) s_val[m] = rhor_val[m];
   __syncthreads();
+  const bool cull = a.nnear && cull_ok(a.dmax2);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.nlocal; i += gridDim.x * blockDim.x) {
     const float4 qi = a.xq[i];
     float cx, cy, cz;
     cell_of(qi, cx, cy, cz);
-    const int n = a.num[i];
+    const int n = cull ? a.nnear[i] : a.num[i];
     dsacc acc;
     float part = 0.f;
     int ns = 0, cnt = 0;
@@ -187,29 +206,42 @@ k_eam_rho_atoms(AtomArgs a, const float4 *__restrict__ rhor_val, int nr, float r
   }
 }
 
-// The list of each atom reordered at each build: the entries within the
-// cutoff first (at the positions of the build), the rest after, each part in
-// list order.  Atoms move little between builds, so in the density pass the
-// lanes of a warp meet the in-range entries together and then the
-// out-of-range ones together, instead of diverging on every entry.
+// The list of each atom reordered, in three parts, each in list order: the
+// entries within the cutoff (at the positions of the reorder), those within
+// r_c + CULL_DELTA, the rest; nnear[i] counts the first two parts.  Atoms move
+// little, so in the density pass the lanes of a warp meet the in-range entries
+// together and the out-of-range ones together, and the third part is skipped
+// while no atom has moved (CULL_DELTA - CULL_MARGIN) / 2 since the reorder.
+// Launched every step: it returns at once while that holds, else it reorders
+// from the current positions, keeps them as the new reference and flags the
+// step (dmax2[1]) so that the density pass culls against the new order.
 __global__ void k_list_partition(const float4 *__restrict__ xq, float g, const int *__restrict__ num,
                                  const int *__restrict__ list, int stride, int nlocal,
-                                 float cut_rsq, int *__restrict__ out) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nlocal) return;
-  const float4 qi = xq[i];
-  float cx, cy, cz;
-  cell_of(qi, cx, cy, cz);
-  const int n = num[i];
-  int m = 0;
-  for (int pass = 0; pass < 2; pass++)
-    for (int k = 0; k < n; k++) {
-      const int j = __ldg(list + (size_t) k * stride + i);
-      float dx, dy, dz;
-      rel_vec(qi, cx, cy, cz, __ldg(xq + j), g, dx, dy, dz);
-      const bool near = dx * dx + dy * dy + dz * dz <= cut_rsq;
-      if (near == (pass == 0)) out[(size_t) m++ * stride + i] = j;
+                                 float cut_rsq, float near_rsq, int *__restrict__ out,
+                                 int *__restrict__ nnear, float4 *__restrict__ ref,
+                                 unsigned *__restrict__ dmax2) {
+  // (the gate reads only dmax2[0], which no block of this kernel writes)
+  if (moved_little(dmax2)) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0) dmax2[1] = 1u;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nlocal; i += gridDim.x * blockDim.x) {
+    const float4 qi = xq[i];
+    ref[i] = qi;
+    float cx, cy, cz;
+    cell_of(qi, cx, cy, cz);
+    const int n = num[i];
+    int m = 0;
+    for (int part = 0; part < 3; part++) {
+      if (part == 2) nnear[i] = m;
+      for (int k = 0; k < n; k++) {
+        const int j = __ldg(list + (size_t) k * stride + i);
+        float dx, dy, dz;
+        rel_vec(qi, cx, cy, cz, __ldg(xq + j), g, dx, dy, dz);
+        const float rsq = dx * dx + dy * dy + dz * dz;
+        const int p = rsq <= cut_rsq ? 0 : (rsq <= near_rsq ? 1 : 2);
+        if (p == part) out[(size_t) m++ * stride + i] = j;
+      }
     }
+  }
 }
 
 // ---- neighbor unions staged in shared memory (EAM atom passes) ----
@@ -665,14 +697,30 @@ __device__ __forceinline__ float4 pack_u(ds ux, ds uy, ds uz, const PackGrid &pg
   return make_float4(rx, ry, rz, __int_as_float(cx | (cy << 12) | (cz << 22)));
 }
 
+// packed coordinates; with a reference (the packed coordinates of the list
+// reorder, same grid) the largest squared displacement of the first nref
+// atoms is folded into *dmax2 (float bits, atomic max)
 __global__ void k_pack_rel(const double4 *__restrict__ x, int n, PackGrid pg,
-                           float4 *__restrict__ xq) {
+                           float4 *__restrict__ xq, const float4 *__restrict__ ref, int nref,
+                           unsigned *__restrict__ dmax2) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double4 p = x[i];
-  xq[i] = pack_u(ds_sub(ds_of_double(p.x), ds{pg.l0h[0], pg.l0l[0]}),
-                 ds_sub(ds_of_double(p.y), ds{pg.l0h[1], pg.l0l[1]}),
-                 ds_sub(ds_of_double(p.z), ds{pg.l0h[2], pg.l0l[2]}), pg);
+  const float4 q = pack_u(ds_sub(ds_of_double(p.x), ds{pg.l0h[0], pg.l0l[0]}),
+                          ds_sub(ds_of_double(p.y), ds{pg.l0h[1], pg.l0l[1]}),
+                          ds_sub(ds_of_double(p.z), ds{pg.l0h[2], pg.l0l[2]}), pg);
+  xq[i] = q;
+  if (ref) {
+    float d2 = 0.f;
+    if (i < nref) {
+      float cx, cy, cz, dx, dy, dz;
+      cell_of(q, cx, cy, cz);
+      rel_vec(q, cx, cy, cz, ref[i], pg.g, dx, dy, dz);
+      d2 = dx * dx + dy * dy + dz * dz;
+    }
+    const unsigned m = __reduce_max_sync(__activemask(), __float_as_uint(d2));
+    if ((threadIdx.x & 31) == __ffs(__activemask()) - 1) atomicMax(dmax2, m);
+  }
 }
 
 // the x-lerps of one lattice column ii: E0..E3 of the y/z edges (-,-), (+,-), (-,+), (+,+)
@@ -1132,9 +1180,10 @@ PackGrid make_pack_grid(const double l0[3], double g, int *oob) {
   return pg;
 }
 
-void pack_rel(const double4 *x, int n, const PackGrid &pg, float4 *xq, cudaStream_t s) {
+void pack_rel(const double4 *x, int n, const PackGrid &pg, float4 *xq, const float4 *ref, int nref,
+              unsigned *dmax2, cudaStream_t s) {
   if (n <= 0) return;
-  k_pack_rel<<<nblk(n, 256), 256, 0, s>>>(x, n, pg, xq);
+  k_pack_rel<<<nblk(n, 256), 256, 0, s>>>(x, n, pg, xq, ref, nref, dmax2);
   check(cudaGetLastError(), "pack_rel");
 }
 
@@ -1142,7 +1191,7 @@ void eam_rho_atoms(const MixedAtoms &m, const float4 *rhor_val, const EamTables 
                    const float4 *fp4, double *rho, float *fp, cudaStream_t s) {
   if (m.nlocal <= 0) return;
   AtomArgs a{m.x, m.xq, m.qg, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
-             m.band_hi, m.cutsq, m.snum, m.slist};
+             m.band_hi, m.cutsq, m.snum, m.slist, m.nnear, m.dmax2};
   size_t smem = sizeof(float4) * (e.nr + 1);
   int g = persistent_grid((const void *) k_eam_rho_atoms, m.block, smem, m.nlocal);
   k_eam_rho_atoms<<<g, m.block, smem, s>>>(a, rhor_val, e.nr, (float) e.rdr, fp4, e.nrho,
@@ -1151,10 +1200,13 @@ void eam_rho_atoms(const MixedAtoms &m, const float4 *rhor_val, const EamTables 
 }
 
 void list_partition(const float4 *xq, float g, const int *num, const int *list, int stride,
-                    int nlocal, float cut_rsq, int *out, cudaStream_t s) {
+                    int nlocal, float cut_rsq, float cutoff, int *out, int *nnear, float4 *ref,
+                    unsigned *dmax2, cudaStream_t s) {
   if (nlocal <= 0) return;
-  k_list_partition<<<nblk(nlocal, 128), 128, 0, s>>>(xq, g, num, list, stride, nlocal, cut_rsq,
-                                                    out);
+  const float rn = cutoff + CULL_DELTA;
+  const int grid = persistent_grid((const void *) k_list_partition, 256, 0, nlocal);
+  k_list_partition<<<grid, 256, 0, s>>>(xq, g, num, list, stride, nlocal, cut_rsq, rn * rn, out,
+                                        nnear, ref, dmax2);
   check(cudaGetLastError(), "list_partition");
 }
 
@@ -1180,7 +1232,7 @@ void eam_rho_union(const MixedAtoms &m, const int *union_j, const int *union_n,
                    cudaStream_t s) {
   if (m.nlocal <= 0) return;
   AtomArgs a{m.x, m.xq, m.qg, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
-             m.band_hi, m.cutsq, m.snum, m.slist};
+             m.band_hi, m.cutsq, m.snum, m.slist, nullptr, nullptr};
   UnionArgs u{union_j, union_n, slot, sslot};
   size_t smem = sizeof(float4) * ((e.nr + 1) + (size_t) UWARPS * UMAX);
   int g = union_grid((const void *) k_eam_rho_union, smem, m.nlocal);
@@ -1194,7 +1246,7 @@ void eam_force_union(const MixedAtoms &m, const int *union_j, const int *union_n
                      const float *fp, double *f, cudaStream_t s) {
   if (m.nlocal <= 0) return;
   AtomArgs a{m.x, m.xq, m.qg, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
-             m.band_hi, m.cutsq, m.snum, m.slist};
+             m.band_hi, m.cutsq, m.snum, m.slist, nullptr, nullptr};
   UnionArgs u{union_j, union_n, nullptr, const_cast<unsigned short *>(sslot)};
   size_t smem = sizeof(float4) * (3 * (size_t) (e.nr + 1) + (size_t) UWARPS * UMAX) +
                 sizeof(float) * (size_t) UWARPS * UMAX;
@@ -1207,7 +1259,7 @@ void eam_force_atoms(const MixedAtoms &m, const float4 *ftab, const EamTables &e
                      const float *fp, double *f, cudaStream_t s) {
   if (m.nlocal <= 0) return;
   AtomArgs a{m.x, m.xq, m.qg, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
-             m.band_hi, m.cutsq, m.snum, m.slist};
+             m.band_hi, m.cutsq, m.snum, m.slist, nullptr, nullptr};
   size_t smem = sizeof(float4) * 3 * (e.nr + 1);
   int g = persistent_grid((const void *) k_eam_force_atoms, m.block, smem, m.nlocal);
   k_eam_force_atoms<<<g, m.block, smem, s>>>(a, ftab, e.nr, (float) e.rdr, fp, f);
@@ -1218,7 +1270,7 @@ void lj_atoms(const MixedAtoms &m, const int *type, const float *lj1, const floa
               const float *cutsq_t, const double *cutsq64, double *f, cudaStream_t s) {
   if (m.nlocal <= 0) return;
   AtomArgs a{m.x, m.xq, m.qg, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
-             m.band_hi, m.cutsq, m.snum, m.slist};
+             m.band_hi, m.cutsq, m.snum, m.slist, nullptr, nullptr};
   int g = persistent_grid((const void *) k_lj_atoms, m.block, 0, m.nlocal);
   k_lj_atoms<<<g, m.block, 0, s>>>(a, type, lj1, lj2, cutsq_t, cutsq64, f);
   check(cudaGetLastError(), "lj_atoms_mixed");
