@@ -202,8 +202,11 @@ struct cacg_context {
   DBuf<float4> d_xl, d_rhor_val4, d_ftab, d_fp4, d_site_q;
   DBuf<float2> d_node_hl, d_spa_int_hl;
   DBuf<float> d_u, d_ljf, d_site_fpf, d_fpf;
-  DBuf<unsigned long long> d_line_mask;
+  DBuf<unsigned long long> d_line_mask, d_line_mask_f;  // all rows; rows of nonzero weight
   DBuf<int> d_nae;
+  DBuf<float2> d_frac, d_fipf;  // lattice fractions; double-single row forces
+  DBuf<float> d_wn;             // weight x shape function per type row and node (FP32)
+  int fstride = 1;
   // mixed precision, per row: packed and double-single integration points,
   // F'(rho) of the force rows; the integration-point lists row-major
   DBuf<float4> d_ip_q, d_ip_h, d_ip_l;
@@ -484,7 +487,11 @@ cacg_context::~cacg_context() {
   d_site_fpf.release();
   d_fpf.release();
   d_line_mask.release();
+  d_line_mask_f.release();
   d_nae.release();
+  d_frac.release();
+  d_fipf.release();
+  d_wn.release();
   d_ip_q.release();
   d_ip_h.release();
   d_ip_l.release();
@@ -1487,6 +1494,24 @@ void cacg_context::element_tables() {
     max_naz = std::max(max_naz, nae[t][2]);
   }
   upload(d_nae, nae3, s);
+  // the fractions k / (n - 1) of each lattice axis as double-single floats
+  fstride = 1;
+  for (int t = 1; t <= netypes; t++)
+    for (int d = 0; d < 3; d++) fstride = std::max(fstride, nae[t][d]);
+  std::vector<float2> frac((size_t) (MAXT + 1) * 3 * fstride, make_float2(0.f, 0.f));
+  for (int t = 1; t <= netypes; t++)
+    for (int d = 0; d < 3; d++)
+      for (int k = 0; k < nae[t][d]; k++) {
+        const double v = nae[t][d] > 1 ? (double) k / (double) (nae[t][d] - 1) : 0.0;
+        const float h = (float) v;
+        frac[(size_t) (t * 3 + d) * fstride + k] = make_float2(h, (float) (v - (double) h));
+      }
+  upload(d_frac, frac, s);
+  // weight x shape function of every row and node, FP32 (the mixed nodal gather)
+  std::vector<float> wn(spa_int.size());
+  for (size_t r = 0; r < w_all.size(); r++)
+    for (int q = 0; q < NPE; q++) wn[r * NPE + q] = (float) (w_all[r] * spa_int[r * NPE + q]);
+  upload(d_wn, wn, s);
   std::vector<float2> sihl(spa_int.size());
   for (size_t k = 0; k < spa_int.size(); k++)
     sihl[k] = make_float2((float) spa_int[k], (float) (spa_int[k] - (double) (float) spa_int[k]));
@@ -2058,6 +2083,8 @@ void cacg_context::neighbor_nbuild() {
   }
   d_fip.ensure(3 * (size_t) std::max(nrows, 1), s);
   check(cudaMemsetAsync(d_fip.p, 0, sizeof(double) * 3 * std::max(nrows, 1), s), "fip");
+  d_fipf.ensure(3 * (size_t) std::max(nrows, 1), s);
+  check(cudaMemsetAsync(d_fipf.p, 0, sizeof(float2) * 3 * std::max(nrows, 1), s), "fipf");
   // the sites any list references: the per-step site kernels compute only these
   d_site_flag.ensure(std::max(nsites, 1), s);
   d_site_pos.ensure(std::max(nsites, 1), s);
@@ -2084,6 +2111,15 @@ void cacg_context::neighbor_nbuild() {
   mixed::line_mask(d_site_flag.p, d_etype.p, d_site_base.p, d_nae.p, nall, maxlines, d_line_mask.p,
                    s);
   launches++;
+  // the sites that the rows of nonzero weight reference: the mixed F'(rho)
+  // kernel computes only these (d_site_pos, the positions of the compaction
+  // above, is free again once that has run)
+  check(cudaMemsetAsync(d_site_pos.p, 0, sizeof(int) * std::max(nsites, 1), s), "flag_f");
+  mixed::mark_rows(d_force_rows.p, nforce, d_row_start.p, d_ent.p, d_site_pos.p, s);
+  d_line_mask_f.ensure((size_t) std::max(nall, 1) * std::max(maxlines, 1), s);
+  mixed::line_mask(d_site_pos.p, d_etype.p, d_site_base.p, d_nae.p, nall, maxlines,
+                   d_line_mask_f.p, s);
+  launches += 3;
   elists_built = true;
 }
 
@@ -2260,7 +2296,8 @@ void cacg_context::pair_ecompute_mixed() {
   d_site_q.ensure(std::max(nsites, 1), s);
   d_node_hl.ensure((size_t) 24 * nall, s);
   mixed::node_split(d_nodex.p, nall, d_node_hl.p, s);
-  mixed::site_q(d_node_hl.p, d_etype.p, d_site_base.p, d_nae.p, max_nax, max_naz, d_line_mask.p,
+  const mixed::Lattice lat{d_nae.p, d_frac.p, fstride};
+  mixed::site_q(d_node_hl.p, d_etype.p, d_site_base.p, lat, max_nax, max_naz, d_line_mask.p,
                 maxlines, pg, nall, d_site_q.p, s);
   d_ip_q.ensure(std::max(nrows, 1), s);
   d_ip_h.ensure(std::max(nrows, 1), s);
@@ -2288,7 +2325,7 @@ void cacg_context::pair_ecompute_mixed() {
   m.nforce = nforce;
   m.node_hl = d_node_hl.p;
   m.site_base = d_site_base.p;
-  m.nae = d_nae.p;
+  m.lat = lat;
   m.nall_e = nall;
   m.pg = pg;
   if (use_sur) m.skip = d_skip.p;
@@ -2300,7 +2337,8 @@ void cacg_context::pair_ecompute_mixed() {
     m.band_hi = m.cutsq_f * (1.0f + eps);
     EamTables e{};
     if (use_sur) surrogate_predict(eamtab());
-    mixed::ip_pass(m, 0, nullptr, e, (float) ljtab.lj1[a], (float) ljtab.lj2[a], d_fip.p, s);
+    mixed::ip_pass(m, 0, nullptr, e, (float) ljtab.lj1[a], (float) ljtab.lj2[a], nullptr,
+                   d_fipf.p, s);
     launches++;
   } else {
     EamTables e = eamtab();
@@ -2310,9 +2348,9 @@ void cacg_context::pair_ecompute_mixed() {
     m.band_hi = m.cutsq_f * (1.0f + eps);
     d_erho.ensure((size_t) NPE * nall, s);
     d_site_fpf.ensure(std::max(nsites, 1), s);
-    mixed::ip_pass(m, 1, d_rhor_val4.p, e, 0.f, 0.f, d_erho.p, s);
+    mixed::ip_pass(m, 1, d_rhor_val4.p, e, 0.f, 0.f, d_erho.p, nullptr, s);
     launch_copy_root(d_erho.p, NPE, d_eroot.p, enlocal, enghost, s);
-    mixed::site_fp(d_erho.p, d_etype.p, d_site_base.p, d_nae.p, d_line_mask.p, maxlines, d_fp4.p,
+    mixed::site_fp(d_erho.p, d_etype.p, d_site_base.p, lat, d_line_mask_f.p, maxlines, d_fp4.p,
                    nrho, rdrho, nall, d_site_fpf.p, s);
     d_row_fpf.ensure(std::max(nrows, 1), s);
     mixed::row_fp(d_force_rows.p, nforce, d_row_elem.p, d_row_jj.p, d_etype.p, d_int_off.p,
@@ -2320,10 +2358,11 @@ void cacg_context::pair_ecompute_mixed() {
     m.site_fp = d_site_fpf.p;
     m.row_fp = d_row_fpf.p;
     if (use_sur) surrogate_predict(e);
-    mixed::ip_pass(m, 2, d_ftab.p, e, 0.f, 0.f, d_fip.p, s);
+    mixed::ip_pass(m, 2, d_ftab.p, e, 0.f, 0.f, nullptr, d_fipf.p, s);
     launches += 5;
   }
-  fp64_fma::gather_nodef(d_fip.p, d_etype.p, d_row_first.p, enlocal, t, d_nodef.p, s);
+  mixed::gather_nodef(d_fipf.p, d_etype.p, d_row_first.p, d_numint.p, d_int_off.p, d_wn.p, enlocal,
+                      d_nodef.p, s);
   launches++;
   if (use_sur) {
     surrogate::write_forces(d_smean.p, d_far.p, nfar, d_skip.p, d_nodef.p, s);

@@ -270,6 +270,13 @@ struct PackGrid {
   float g, ig;
   int *oob;
 };
+// lattice sizes per type ([3 * type + axis]) and the fractions k / (n - 1)
+// per type and axis as double-single floats ([(3 * type + axis) * fstride + k])
+struct Lattice {
+  const int *nae;
+  const float2 *frac;
+  int fstride;
+};
 struct MixedElems {
   const float4 *site_q;       // packed site positions of this step (referenced sites)
   const float *site_fp;       // FP32 F'(rho) at the referenced sites (EAM force pass)
@@ -285,7 +292,8 @@ struct MixedElems {
   double cutsq;
   const float2 *node_hl;                // [nall][24] double-single node coordinates
   const unsigned char *skip = nullptr;  // elements whose forces come from the surrogate
-  const int *site_base, *nae;           // site offsets per element; lattice sizes per type
+  const int *site_base;                 // site offsets per element
+  Lattice lat;
   int nall_e;
   PackGrid pg;
   int block = 512;  // threads per block of the persistent grids
@@ -301,14 +309,17 @@ void pack_rel(const double4 *x, int n, const PackGrid &pg, float4 *xq, const flo
 void node_split(const double *nodex, int n, float2 *hl, cudaStream_t s);
 // per element and lattice line (ii, jj): bit kk set when site (ii, jj, kk) is
 // referenced by an integration-point list
+// flag the sites referenced by the listed rows
+void mark_rows(const int *rows, int nlisted, const int *row_start, const int *ent, int *flag,
+               cudaStream_t s);
 void line_mask(const int *flag, const int *etype, const int *site_base, const int *nae, int nelem,
                int maxlines, unsigned long long *mask, cudaStream_t s);
 // packed positions of the referenced sites (double-single interpolation)
-void site_q(const float2 *node_hl, const int *etype, const int *site_base, const int *nae,
+void site_q(const float2 *node_hl, const int *etype, const int *site_base, const Lattice &lat,
             int max_nax, int max_naz, const unsigned long long *mask, int maxlines,
             const PackGrid &pg, int nelem, float4 *q, cudaStream_t s);
 // FP32 F'(rho) at the referenced sites; fp4 holds F' coefficients c0..c2 per knot
-void site_fp(const double *erho, const int *etype, const int *site_base, const int *nae,
+void site_fp(const double *erho, const int *etype, const int *site_base, const Lattice &lat,
              const unsigned long long *mask, int maxlines, const float4 *fp4, int nrho,
              double rdrho, int nelem, float *fp, cudaStream_t s);
 // each atom's list reordered (entries within cut_rsq at the packed positions,
@@ -347,10 +358,15 @@ void row_fp(const int *rows, int nforce, const int *row_elem, const int *row_jj,
 // row-major copy of the integration-point lists (row_start: exclusive scan of ipnum)
 void ip_csr(const int *ipnum, const int *ipent, int nrows, int rowstride, const int *row_start,
             int *ent, cudaStream_t s);
-// pass 0: LJ forces -> out[3*rows]; 1: EAM nodal densities -> out[8*nlocal_e];
-// 2: EAM forces -> out[3*rows]
+// pass 0: LJ forces -> outf[3*rows]; 1: EAM nodal densities -> out[8*nlocal_e]
+// (FP64); 2: EAM forces -> outf[3*rows] (double-single floats)
 void ip_pass(const MixedElems &m, int pass, const float4 *tab, const EamTables &e, float lj1,
-             float lj2, double *out, cudaStream_t s);
+             float lj2, double *out, float2 *outf, cudaStream_t s);
+// nodal forces from the double-single row forces; wn = weight x shape function
+// (FP32) per type row and node
+void gather_nodef(const float2 *fipf, const int *etype, const int *row_first, const int *numint,
+                  const int *int_off, const float *wn, int nlocal_e, double *nodef,
+                  cudaStream_t s);
 }  // namespace mixed
 
 // ---- energy, virial, kinetic energy (k_thermo.cu); 7 partial sums per block ----

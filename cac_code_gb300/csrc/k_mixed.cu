@@ -636,14 +636,10 @@ __device__ __forceinline__ ds ds_madd(ds a, ds d, ds x) {
 
 __device__ __forceinline__ ds ds_lerp(ds x, ds y, ds a) { return ds_madd(a, ds_sub(y, x), x); }
 
-// k / d as a double-single: the correctly rounded quotient and its remainder,
-// which one fma gives exactly
-__device__ __forceinline__ ds ds_frac(int k, int d) {
-  if (d <= 0) return ds{0.f, 0.f};
-  const float fk = (float) k, fd = (float) d;
-  const float q = __fdiv_rn(fk, fd);
-  const float r = __fmaf_rn(-q, fd, fk);
-  return ds{q, __fdiv_rn(r, fd)};
+// the lattice fraction k / (n - 1) along an axis of a type, as a double-single
+__device__ __forceinline__ ds frac_of(const Lattice &lat, int ty, int axis, int k) {
+  const float2 v = __ldg(lat.frac + (size_t) (ty * 3 + axis) * lat.fstride + k);
+  return ds{v.x, v.y};
 }
 
 // A double as a double-single by integer operations on its bits, without an
@@ -733,9 +729,9 @@ __device__ __forceinline__ void column_ds(const float2 *nx, ds a, int d, ds (&E)
 
 // site (ii, jj, kk) of an element in double-single, by the same lerps as the
 // site kernel (the guard-band path of the integration-point passes)
-__device__ __forceinline__ void site_ds(const float2 *nx, int ii, int jj, int kk, int nax, int nay,
-                                        int naz, ds (&x)[3]) {
-  const ds a = ds_frac(ii, nax - 1), b = ds_frac(jj, nay - 1), c = ds_frac(kk, naz - 1);
+__device__ __forceinline__ void site_ds(const float2 *nx, const Lattice &lat, int ty, int ii, int jj,
+                                        int kk, ds (&x)[3]) {
+  const ds a = frac_of(lat, ty, 0, ii), b = frac_of(lat, ty, 1, jj), c = frac_of(lat, ty, 2, kk);
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     ds E[4];
@@ -764,6 +760,15 @@ __global__ void k_line_mask(const int *__restrict__ flag, const int *__restrict_
   mask[t] = m;
 }
 
+// flag the sites referenced by the listed rows (row-major lists)
+__global__ void k_mark_rows(const int *__restrict__ rows, int nlisted, const int *__restrict__ row_start,
+                            const int *__restrict__ ent, int *__restrict__ flag) {
+  const int it = blockIdx.x * blockDim.x + threadIdx.x;
+  if (it >= nlisted) return;
+  const int r = rows[it];
+  for (int k = row_start[r]; k < row_start[r + 1]; k++) flag[ent[k]] = 1;
+}
+
 // Site positions of this step, packed; one block per element.  The element's
 // lines are taken LCH at a time: their start U = x(i,j,0) - l0 and step
 // D = x(i,j,nz-1) - x(i,j,0) go to shared memory, then the block's threads run
@@ -772,9 +777,10 @@ constexpr int LCH = 128;
 
 __global__ void __launch_bounds__(LCH)
 k_site_q(const float2 *__restrict__ node_hl, const int *__restrict__ etype,
-         const int *__restrict__ site_base, const int *__restrict__ nae,
+         const int *__restrict__ site_base, Lattice lat,
          const unsigned long long *__restrict__ line_mask, int maxlines, PackGrid pg,
          float4 *__restrict__ site_q) {
+  const int *nae = lat.nae;
   extern __shared__ ds s_mem[];
   __shared__ float2 s_nx[24];
   __shared__ unsigned long long s_mask[LCH];
@@ -786,12 +792,12 @@ k_site_q(const float2 *__restrict__ node_hl, const int *__restrict__ etype,
   ds *s_D = s_U + 3 * LCH;         // [LCH][3]
   ds *s_c = s_D + 3 * LCH;         // [naz]
   if (threadIdx.x < 24) s_nx[threadIdx.x] = node_hl[24 * (size_t) e + threadIdx.x];
-  for (int k = threadIdx.x; k < naz; k += blockDim.x) s_c[k] = ds_frac(k, naz - 1);
+  for (int k = threadIdx.x; k < naz; k += blockDim.x) s_c[k] = frac_of(lat, ty, 2, k);
   __syncthreads();
   for (int q = threadIdx.x; q < 3 * nax; q += blockDim.x) {
     const int ii = q / 3, d = q % 3;
     ds E[4];
-    column_ds(s_nx, ds_frac(ii, nax - 1), d, E);
+    column_ds(s_nx, frac_of(lat, ty, 0, ii), d, E);
 #pragma unroll
     for (int w = 0; w < 4; w++) s_E[(ii * 3 + d) * 4 + w] = E[w];
   }
@@ -807,7 +813,7 @@ k_site_q(const float2 *__restrict__ node_hl, const int *__restrict__ etype,
       s_mask[threadIdx.x] = mk;
       if (mk || naz > 64) {
         const int ii = L / nay, jj = L % nay;
-        const ds b = ds_frac(jj, nay - 1);
+        const ds b = frac_of(lat, ty, 1, jj);
 #pragma unroll
         for (int d = 0; d < 3; d++) {
           const ds *E = s_E + (ii * 3 + d) * 4;
@@ -842,9 +848,10 @@ k_site_q(const float2 *__restrict__ node_hl, const int *__restrict__ etype,
 // by the same lerps in FP32; one block per element, lines LCH at a time.
 __global__ void __launch_bounds__(LCH)
 k_site_fp(const double *__restrict__ erho, const int *__restrict__ etype,
-          const int *__restrict__ site_base, const int *__restrict__ nae,
+          const int *__restrict__ site_base, Lattice lat,
           const unsigned long long *__restrict__ line_mask, int maxlines,
           const float4 *__restrict__ fp4, int nrho, float rdrho, float *__restrict__ site_fp) {
+  const int *nae = lat.nae;
   __shared__ float s_er[NPE];
   __shared__ float s_U[LCH], s_D[LCH];
   __shared__ unsigned long long s_mask[LCH];
@@ -854,7 +861,6 @@ k_site_fp(const double *__restrict__ erho, const int *__restrict__ etype,
   if (threadIdx.x < NPE) s_er[threadIdx.x] = (float) erho[NPE * (size_t) e + threadIdx.x];
   const int nlines = nax * nay, base = site_base[e];
   const unsigned long long *lm = line_mask + (size_t) e * maxlines;
-  const float rz = naz > 1 ? 1.0f / (float) (naz - 1) : 0.f;
   for (int L0 = 0; L0 < nlines; L0 += LCH) {
     const int nl = min(LCH, nlines - L0);
     __syncthreads();
@@ -863,8 +869,7 @@ k_site_fp(const double *__restrict__ erho, const int *__restrict__ etype,
       const unsigned long long mk = lm[L];
       s_mask[threadIdx.x] = mk;
       const int ii = L / nay, jj = L % nay;
-      const float a = nax > 1 ? (float) ii / (float) (nax - 1) : 0.f;
-      const float b = nay > 1 ? (float) jj / (float) (nay - 1) : 0.f;
+      const float a = frac_of(lat, ty, 0, ii).h, b = frac_of(lat, ty, 1, jj).h;
       const float e0 = s_er[0] + a * (s_er[1] - s_er[0]), e1 = s_er[3] + a * (s_er[2] - s_er[3]);
       const float e2 = s_er[4] + a * (s_er[5] - s_er[4]), e3 = s_er[7] + a * (s_er[6] - s_er[7]);
       const float B = e0 + b * (e1 - e0), T = e2 + b * (e3 - e2);
@@ -876,7 +881,7 @@ k_site_fp(const double *__restrict__ erho, const int *__restrict__ etype,
     int l = threadIdx.x / naz, kk = threadIdx.x - l * naz;
     for (int t = threadIdx.x; t < nsite; t += LCH) {
       if (kk >= 64 || ((s_mask[l] >> kk) & 1ull)) {
-        const float rho = s_U[l] + ((float) kk * rz) * s_D[l];
+        const float rho = s_U[l] + frac_of(lat, ty, 2, kk).h * s_D[l];
         site_fp[base + (size_t) L0 * naz + t] = fprime32(rho, fp4, nrho, rdrho);
       }
       l += dl;
@@ -904,7 +909,8 @@ struct ElemArgs {
   double cutsq;
   const float2 *node_hl;
   const unsigned char *skip;
-  const int *site_base, *nae;
+  const int *site_base;
+  Lattice lat;
   int nall_e;
   PackGrid pg;
 };
@@ -987,10 +993,10 @@ __device__ __noinline__ void site_ds_of(const ElemArgs &a, int sid, ds (&x)[3]) 
     else hi = mid;
   }
   const int ty = a.etype[lo];
-  const int nax = a.nae[3 * ty], nay = a.nae[3 * ty + 1], naz = a.nae[3 * ty + 2];
+  const int nay = a.lat.nae[3 * ty + 1], naz = a.lat.nae[3 * ty + 2];
   const int nj = sid - a.site_base[lo];
   const int kk = nj % naz, L = nj / naz;
-  site_ds(a.node_hl + 24 * (size_t) lo, L / nay, L % nay, kk, nax, nay, naz, x);
+  site_ds(a.node_hl + 24 * (size_t) lo, a.lat, ty, L / nay, L % nay, kk, x);
 }
 
 __device__ __noinline__ bool inside_band(const ElemArgs &a, int r, int sid) {
@@ -1011,7 +1017,7 @@ __device__ __noinline__ bool inside_band(const ElemArgs &a, int r, int sid) {
 template <bool EAM, bool DENSITY, int G>
 __global__ void __launch_bounds__(512, 2)
 k_ipg(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr, float lj1, float lj2,
-      double *__restrict__ out) {
+      double *__restrict__ out, float2 *__restrict__ outf) {
   extern __shared__ float4 s_tab[];
   const int ntab = EAM ? (DENSITY ? (nr + 1) : 3 * (nr + 1)) : 0;
   for (int m = threadIdx.x; m < ntab; m += blockDim.x) s_tab[m] = tab[m];
@@ -1122,13 +1128,36 @@ k_ipg(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr, float lj1, 
       group_sum<G>(fx);
       group_sum<G>(fy);
       group_sum<G>(fz);
-      if (live && lane == 0) {
-        out[3 * r] = fx.value();
-        out[3 * r + 1] = fy.value();
-        out[3 * r + 2] = fz.value();
+      if (live && lane == 0) {  // double-single: the nodal gather reads it without FP64
+        outf[3 * r] = make_float2(fx.h, fx.l);
+        outf[3 * r + 1] = make_float2(fy.h, fy.l);
+        outf[3 * r + 2] = make_float2(fz.h, fz.l);
       }
     }
   }
+}
+
+// Nodal forces f_q = sum_r w_r N_q(r) f_r (the FP64 gather's formula) from the
+// double-single row forces, with the products w_r N_q(r) as FP32 and the sum
+// as a double-single: no FP64 instruction but the final conversion
+__global__ void k_gather_nodef_ds(const float2 *__restrict__ fipf, const int *__restrict__ etype,
+                                  const int *__restrict__ row_first, const int *__restrict__ numint,
+                                  const int *__restrict__ int_off, const float *__restrict__ wn,
+                                  int nlocal_e, double *__restrict__ nodef) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= nlocal_e * 24) return;
+  const int e = tid / 24, rem = tid % 24, q = rem / 3, c = rem % 3;
+  const int ty = etype[e], nint = numint[ty], r0 = row_first[e];
+  const float *w = wn + (size_t) int_off[ty] * NPE;
+  dsacc acc;
+  for (int jj = 0; jj < nint; jj++) {
+    const float wq = __ldg(w + jj * NPE + q);
+    if (wq == 0.f) continue;  // rows of zero weight carry no force
+    const float2 f = fipf[3 * (r0 + jj) + c];
+    acc.add(__fmul_rn(wq, f.x));
+    acc.add(__fmul_rn(wq, f.y));
+  }
+  nodef[tid] = acc.value();
 }
 
 inline int nblk(long long n, int t) { return (int) ((n + t - 1) / t); }
@@ -1282,6 +1311,13 @@ void node_split(const double *nodex, int n, float2 *hl, cudaStream_t s) {
   check(cudaGetLastError(), "node_split");
 }
 
+void mark_rows(const int *rows, int nlisted, const int *row_start, const int *ent, int *flag,
+               cudaStream_t s) {
+  if (nlisted <= 0) return;
+  k_mark_rows<<<nblk(nlisted, 128), 128, 0, s>>>(rows, nlisted, row_start, ent, flag);
+  check(cudaGetLastError(), "mark_rows");
+}
+
 void line_mask(const int *flag, const int *etype, const int *site_base, const int *nae, int nelem,
                int maxlines, unsigned long long *mask, cudaStream_t s) {
   if (nelem <= 0) return;
@@ -1290,20 +1326,20 @@ void line_mask(const int *flag, const int *etype, const int *site_base, const in
   check(cudaGetLastError(), "line_mask");
 }
 
-void site_q(const float2 *node_hl, const int *etype, const int *site_base, const int *nae,
+void site_q(const float2 *node_hl, const int *etype, const int *site_base, const Lattice &lat,
             int max_nax, int max_naz, const unsigned long long *mask, int maxlines,
             const PackGrid &pg, int nelem, float4 *q, cudaStream_t s) {
   if (nelem <= 0) return;
   const size_t smem = sizeof(ds) * (12 * (size_t) max_nax + 6 * LCH + max_naz);
-  k_site_q<<<nelem, LCH, smem, s>>>(node_hl, etype, site_base, nae, mask, maxlines, pg, q);
+  k_site_q<<<nelem, LCH, smem, s>>>(node_hl, etype, site_base, lat, mask, maxlines, pg, q);
   check(cudaGetLastError(), "site_q");
 }
 
-void site_fp(const double *erho, const int *etype, const int *site_base, const int *nae,
+void site_fp(const double *erho, const int *etype, const int *site_base, const Lattice &lat,
              const unsigned long long *mask, int maxlines, const float4 *fp4, int nrho,
              double rdrho, int nelem, float *fp, cudaStream_t s) {
   if (nelem <= 0) return;
-  k_site_fp<<<nelem, LCH, 0, s>>>(erho, etype, site_base, nae, mask, maxlines, fp4, nrho,
+  k_site_fp<<<nelem, LCH, 0, s>>>(erho, etype, site_base, lat, mask, maxlines, fp4, nrho,
                                   (float) rdrho, fp);
   check(cudaGetLastError(), "site_fp");
 }
@@ -1335,34 +1371,46 @@ void ip_csr(const int *ipnum, const int *ipent, int nrows, int rowstride, const 
 
 template <bool EAM, bool DENSITY, int G>
 static void launch_ipg(const ElemArgs &a, long long items, int block, const float4 *tab,
-                       const EamTables &e, float lj1, float lj2, double *out, cudaStream_t s) {
+                       const EamTables &e, float lj1, float lj2, double *out, float2 *outf,
+                       cudaStream_t s) {
   const size_t smem = EAM ? sizeof(float4) * (DENSITY ? 1 : 3) * (e.nr + 1) : 0;
   const int g = persistent_grid((const void *) k_ipg<EAM, DENSITY, G>, block, smem, items * G);
-  k_ipg<EAM, DENSITY, G><<<g, block, smem, s>>>(a, tab, e.nr, (float) e.rdr, lj1, lj2, out);
+  k_ipg<EAM, DENSITY, G><<<g, block, smem, s>>>(a, tab, e.nr, (float) e.rdr, lj1, lj2, out, outf);
 }
 
 template <bool EAM, bool DENSITY>
 static void launch_ip(const ElemArgs &a, long long items, int block, int group,
                       const float4 *tab, const EamTables &e, float lj1, float lj2, double *out,
-                      cudaStream_t s) {
-  if (group == 4) launch_ipg<EAM, DENSITY, 4>(a, items, block, tab, e, lj1, lj2, out, s);
-  else if (group == 16) launch_ipg<EAM, DENSITY, 16>(a, items, block, tab, e, lj1, lj2, out, s);
-  else launch_ipg<EAM, DENSITY, 8>(a, items, block, tab, e, lj1, lj2, out, s);
+                      float2 *outf, cudaStream_t s) {
+  if (group == 4) launch_ipg<EAM, DENSITY, 4>(a, items, block, tab, e, lj1, lj2, out, outf, s);
+  else if (group == 16)
+    launch_ipg<EAM, DENSITY, 16>(a, items, block, tab, e, lj1, lj2, out, outf, s);
+  else launch_ipg<EAM, DENSITY, 8>(a, items, block, tab, e, lj1, lj2, out, outf, s);
 }
 
 void ip_pass(const MixedElems &m, int pass, const float4 *tab, const EamTables &e, float lj1,
-             float lj2, double *out, cudaStream_t s) {
+             float lj2, double *out, float2 *outf, cudaStream_t s) {
   ElemArgs a{m.site_q, m.site_fp, m.ip_q, m.ip_h, m.ip_l, m.row_fp, m.etype, m.row_elem,
              m.row_first, m.node_list, m.row_start, m.ent, m.nlocal_e, m.rows, m.nforce,
-             m.cutsq_f, m.band_lo, m.band_hi, m.cutsq, m.node_hl, m.skip, m.site_base, m.nae,
+             m.cutsq_f, m.band_lo, m.band_hi, m.cutsq, m.node_hl, m.skip, m.site_base, m.lat,
              m.nall_e, m.pg};
   if (pass == 0)  // LJ forces
-    launch_ip<false, false>(a, m.nforce, m.block, m.group, tab, e, lj1, lj2, out, s);
+    launch_ip<false, false>(a, m.nforce, m.block, m.group, tab, e, lj1, lj2, out, outf, s);
   else if (pass == 1)  // EAM nodal densities
-    launch_ip<true, true>(a, (long long) m.nlocal_e * NPE, m.block, m.group, tab, e, 0.f, 0.f, out, s);
+    launch_ip<true, true>(a, (long long) m.nlocal_e * NPE, m.block, m.group, tab, e, 0.f, 0.f, out,
+                          outf, s);
   else  // EAM forces
-    launch_ip<true, false>(a, m.nforce, m.block, m.group, tab, e, 0.f, 0.f, out, s);
+    launch_ip<true, false>(a, m.nforce, m.block, m.group, tab, e, 0.f, 0.f, out, outf, s);
   check(cudaGetLastError(), "ip_pass_mixed");
+}
+
+void gather_nodef(const float2 *fipf, const int *etype, const int *row_first, const int *numint,
+                  const int *int_off, const float *wn, int nlocal_e, double *nodef,
+                  cudaStream_t s) {
+  if (nlocal_e <= 0) return;
+  k_gather_nodef_ds<<<nblk((long long) nlocal_e * 24, 128), 128, 0, s>>>(
+      fipf, etype, row_first, numint, int_off, wn, nlocal_e, nodef);
+  check(cudaGetLastError(), "gather_nodef_ds");
 }
 
 }  // namespace mixed
