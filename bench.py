@@ -195,10 +195,12 @@ def algorithmic_bytes_force_atoms(natoms, mean_short):
     return natoms * (24 + 4 + 4 * mean_short + 8 + 24)
 
 
-def algorithmic_bytes_rho_mixed(natoms, mean_neigh, mean_short):
-    """Mixed EAM density pass (bytes per launch): double-single x_i 32 + count 4 +
-    full list 4n + short-list count 4 and entries 4n_s written + rho 8 + F' 8."""
-    return natoms * (32 + 4 + 4 * mean_neigh + 4 + 4 * mean_short + 8 + 8)
+def algorithmic_bytes_rho_mixed(natoms, mean_scan, mean_short):
+    """Mixed EAM density pass (bytes per launch): packed x_i 16 + count 4 + the
+    scanned list entries 4 n (the near part of each reordered list while
+    displacement culling holds) + short-list count 4 and entries 4 n_s written +
+    rho 8 + F' 4 (FP32)."""
+    return natoms * (16 + 4 + 4 * mean_scan + 4 + 4 * mean_short + 8 + 4)
 
 
 def run_ours(a, ws, rank, local):
@@ -304,10 +306,12 @@ def run_ours(a, ws, rank, local):
     mean_short = c1["short_entries"] / max(c1["nlocal"], 1)
     phase = {"integrate+comm": tm[1], "atom_rho": tm[2], "atom_force": tm[3],
              "element": tm[4], "final": tm[5]}
+    mean_scan = mean_neigh
     if a.mode == "mixed":
         kname = "mixed k_eam_rho_atoms (EAM density pass over the atom list, emits the short list)"
         k_ms = tm[2] / a.steps
-        abytes = algorithmic_bytes_rho_mixed(c0["nlocal"], mean_neigh, mean_short)
+        mean_scan = c1["density_scan_entries"] / max(c1["nlocal"], 1)
+        abytes = algorithmic_bytes_rho_mixed(c0["nlocal"], mean_scan, mean_short)
         tkey = "mixed_k_eam_rho_atoms_bytes_per_atom"
     else:
         kname = "k_eam_force_atoms (EAM force pass over the atom list)"
@@ -501,6 +505,8 @@ def run_ours(a, ws, rank, local):
                 "integration_rows": c0["ip_rows"], "sites": sites,
                 "interpolated_sites": c0["sites"], "sites_referenced": c0["sites_needed"],
                 "atom_list_mean": round(mean_neigh, 2),
+                "density_pass_scan_mean": round(mean_scan, 2),
+                "short_list_mean": round(mean_short, 2),
                 "ip_list_mean": round(c0["ip_entries"] / max(c0["ip_rows"], 1), 2),
                 "rebuild": "every 10 steps if any displacement > skin/2 (check yes)",
                 "rebuilds_in_timed_region": c1["rebuilds"] - c0["rebuilds"],
@@ -518,7 +524,9 @@ def run_ours(a, ws, rank, local):
                          "peak_source": peak_src,
                          "fp64_peak_flops_measured": fp64_peak,
                          "note": "FP64 pair math is ALU-bound on GB300 (see fp64_peak); the "
-                                 "mixed passes are bound by the latency of neighbor gathers"},
+                                 "mixed passes run no FP64 in their pair loops and are bound "
+                                 "by instruction issue and the latency of neighbor gathers "
+                                 "(L2 hits)"},
             "cpu_baseline": cpu,
             "e2e": e2e,
             "clocks": clk,

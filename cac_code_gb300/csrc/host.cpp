@@ -3208,10 +3208,10 @@ int cacg_run(cacg_handle h, int nsteps) {
 
 int cacg_get_counts(cacg_handle h, long long *c, int n) {
   API_BEGIN
-  long long v[20] = {h->nlocal, h->nghost, 0, h->enlocal, h->enghost, 0, h->nrows, 0,
+  long long v[21] = {h->nlocal, h->nghost, 0, h->enlocal, h->enghost, 0, h->nrows, 0,
                      h->nrebuild, (long long) h->stencil.size(), h->ntimestep, h->nsites,
                      h->launches, h->nneed, h->nforce, 0, h->sur ? h->nfar : 0, 0, 0,
-                     h->graph_steps};
+                     h->graph_steps, 0};
   if (h->sur && h->d_scount.p) {
     unsigned long long c2[2] = {0, 0};
     check(cudaMemcpyAsync(c2, h->d_scount.p, sizeof(c2), cudaMemcpyDeviceToHost, h->stream), "scount");
@@ -3243,7 +3243,25 @@ int cacg_get_counts(cacg_handle h, long long *c, int n) {
     h->sync();
     for (int x : num) v[15] += x;
   }
-  for (int i = 0; i < n && i < 20; i++) c[i] = v[i];
+  // entries the last mixed density pass scanned: the near parts of the
+  // reordered lists when the displacement since the reorder allowed culling
+  // (the device test of k_eam_rho_atoms, repeated here), else every entry
+  v[20] = v[2];
+  if (h->mode == CACG_MIXED && h->pair_style == 2 && !h->mixed_union && h->mixed_cull &&
+      h->part_of == h->list_builds && h->nlocal && h->d_nnear.p && h->d_misc.p) {
+    unsigned dm[2] = {0, 0};
+    check(cudaMemcpyAsync(dm, h->d_misc.p + 11, sizeof(dm), cudaMemcpyDeviceToHost, h->stream), "dmax");
+    std::vector<int> nn(h->nlocal);
+    check(cudaMemcpyAsync(nn.data(), h->d_nnear.p, sizeof(int) * h->nlocal, cudaMemcpyDeviceToHost, h->stream), "nnear");
+    h->sync();
+    float d2;
+    std::memcpy(&d2, &dm[0], sizeof(float));
+    if (dm[1] != 0u || 2.0f * std::sqrt(d2) + mixed::CULL_MARGIN <= mixed::CULL_DELTA) {
+      v[20] = 0;
+      for (int x : nn) v[20] += x;
+    }
+  }
+  for (int i = 0; i < n && i < 21; i++) c[i] = v[i];
   API_END
 }
 

@@ -262,6 +262,11 @@ struct MixedAtoms {
   const unsigned *dmax2 = nullptr;
   int block = 512;    // threads per block of the persistent grids (autotuned)
 };
+// Displacement culling of the mixed EAM density pass: list entries beyond
+// r_c + CULL_DELTA at the last reorder are skipped while twice the largest
+// displacement since then, plus CULL_MARGIN, stays within CULL_DELTA (A).
+constexpr float CULL_DELTA = 1.0f, CULL_MARGIN = 0.01f;
+
 // The packing grid of the cell-relative coordinates: cells of a power-of-two
 // size g from the corner l0 (split into double-single floats); *oob counts
 // positions outside the 4096 x 1024 x 1024-cell range.

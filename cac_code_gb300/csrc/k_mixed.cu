@@ -138,8 +138,6 @@ struct AtomArgs {
   const unsigned *dmax2;  // [0]: squared displacement bits; [1]: reordered in this step
 };
 
-constexpr float CULL_DELTA = 1.0f, CULL_MARGIN = 0.01f;
-
 __device__ __forceinline__ bool moved_little(const unsigned *dmax2) {
   return 2.0f * sqrtf(__uint_as_float(dmax2[0])) + CULL_MARGIN <= CULL_DELTA;
 }
