@@ -227,18 +227,26 @@ __global__ void k_list_partition(const float4 *__restrict__ xq, float g, const i
     float cx, cy, cz;
     cell_of(qi, cx, cy, cz);
     const int n = num[i];
-    int m = 0;
-    for (int part = 0; part < 3; part++) {
-      if (part == 2) nnear[i] = m;
+    // two sweeps: count the parts, then place every entry at its part's cursor
+    int c0 = 0, c1 = 0;
+    for (int sweep = 0; sweep < 2; sweep++) {
+      int m0 = 0, m1 = c0, m2 = c0 + c1;
       for (int k = 0; k < n; k++) {
         const int j = __ldg(list + (size_t) k * stride + i);
         float dx, dy, dz;
         rel_vec(qi, cx, cy, cz, __ldg(xq + j), g, dx, dy, dz);
         const float rsq = dx * dx + dy * dy + dz * dz;
         const int p = rsq <= cut_rsq ? 0 : (rsq <= near_rsq ? 1 : 2);
-        if (p == part) out[(size_t) m++ * stride + i] = j;
+        if (sweep == 0) {
+          c0 += p == 0;
+          c1 += p == 1;
+        } else {
+          const int at = p == 0 ? m0++ : (p == 1 ? m1++ : m2++);
+          out[(size_t) at * stride + i] = j;
+        }
       }
     }
+    nnear[i] = c0 + c1;
   }
 }
 
@@ -767,94 +775,127 @@ __global__ void k_mark_rows(const int *__restrict__ rows, int nlisted, const int
   for (int k = row_start[r]; k < row_start[r + 1]; k++) flag[ent[k]] = 1;
 }
 
-// Site positions of this step, packed; one block per element.  The element's
-// lines are taken LCH at a time: their start U = x(i,j,0) - l0 and step
-// D = x(i,j,nz-1) - x(i,j,0) go to shared memory, then the block's threads run
-// over the lines' sites in storage order, so the stores coalesce.
+// Site positions of this step, packed; one block per element.  Per lattice
+// column ii the x-lerps give P = E0 - l0, Q = E1 - E0, R = E2 - E0 and
+// S = (E3 - E2) - (E1 - E0), so that a line (ii, jj) starts at U = P + b Q and
+// steps D = R + b S (b = jj / (ny - 1)), and its site kk is U + c D.  The
+// element's lines are taken LCH at a time: each thread prepares one line and
+// lists the line's referenced sites in shared memory (a block prefix sum of
+// the masks' popcounts), then the block's threads run over that compact list.
 constexpr int LCH = 128;
+
+// exclusive prefix sum over the block (LCH threads); returns the block total
+__device__ __forceinline__ int block_scan(int v, int &excl, int *s_warp) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_warp[w] = x;
+  __syncthreads();
+  int before = 0, total = 0;
+#pragma unroll
+  for (int k = 0; k < LCH / 32; k++) {
+    const int t = s_warp[k];
+    if (k < w) before += t;
+    total += t;
+  }
+  excl = before + x - v;
+  __syncthreads();  // s_warp may be reused
+  return total;
+}
 
 __global__ void __launch_bounds__(LCH)
 k_site_q(const float2 *__restrict__ node_hl, const int *__restrict__ etype,
          const int *__restrict__ site_base, Lattice lat,
          const unsigned long long *__restrict__ line_mask, int maxlines, PackGrid pg,
          float4 *__restrict__ site_q) {
-  const int *nae = lat.nae;
   extern __shared__ ds s_mem[];
   __shared__ float2 s_nx[24];
-  __shared__ unsigned long long s_mask[LCH];
+  __shared__ int s_warp[LCH / 32];
+  __shared__ unsigned short s_list[LCH * 64];  // (line in chunk) << 6 | kk
   const int e = blockIdx.x;
   const int ty = etype[e];
+  const int *nae = lat.nae;
   const int nax = nae[3 * ty], nay = nae[3 * ty + 1], naz = nae[3 * ty + 2];
-  ds *s_E = s_mem;                 // [nax][3][4]
-  ds *s_U = s_E + 12 * nax;        // [LCH][3]
-  ds *s_D = s_U + 3 * LCH;         // [LCH][3]
-  ds *s_c = s_D + 3 * LCH;         // [naz]
+  ds *s_col = s_mem;          // [nax][3][4]: P, Q, R, S
+  ds *s_U = s_col + 12 * nax;  // [LCH][3]
+  ds *s_D = s_U + 3 * LCH;     // [LCH][3]
+  ds *s_c = s_D + 3 * LCH;     // [naz]
   if (threadIdx.x < 24) s_nx[threadIdx.x] = node_hl[24 * (size_t) e + threadIdx.x];
   for (int k = threadIdx.x; k < naz; k += blockDim.x) s_c[k] = frac_of(lat, ty, 2, k);
   __syncthreads();
+  const ds l0[3] = {{pg.l0h[0], pg.l0l[0]}, {pg.l0h[1], pg.l0l[1]}, {pg.l0h[2], pg.l0l[2]}};
   for (int q = threadIdx.x; q < 3 * nax; q += blockDim.x) {
     const int ii = q / 3, d = q % 3;
     ds E[4];
     column_ds(s_nx, frac_of(lat, ty, 0, ii), d, E);
-#pragma unroll
-    for (int w = 0; w < 4; w++) s_E[(ii * 3 + d) * 4 + w] = E[w];
+    ds *o = s_col + (ii * 3 + d) * 4;
+    const ds q1 = ds_sub(E[1], E[0]);
+    o[0] = ds_sub(E[0], l0[d]);
+    o[1] = q1;
+    o[2] = ds_sub(E[2], E[0]);
+    o[3] = ds_sub(ds_sub(E[3], E[2]), q1);
   }
-  const ds l0[3] = {{pg.l0h[0], pg.l0l[0]}, {pg.l0h[1], pg.l0l[1]}, {pg.l0h[2], pg.l0l[2]}};
   const int nlines = nax * nay, base = site_base[e];
   const unsigned long long *lm = line_mask + (size_t) e * maxlines;
   for (int L0 = 0; L0 < nlines; L0 += LCH) {
     const int nl = min(LCH, nlines - L0);
-    __syncthreads();  // s_E ready; the previous chunk's lines consumed
+    __syncthreads();  // columns ready; the previous chunk consumed
+    unsigned long long mk = 0;
     if (threadIdx.x < nl) {
       const int L = L0 + threadIdx.x;
-      const unsigned long long mk = lm[L];
-      s_mask[threadIdx.x] = mk;
+      mk = lm[L];
       if (mk || naz > 64) {
-        const int ii = L / nay, jj = L % nay;
+        const int ii = L / nay, jj = L - ii * nay;
         const ds b = frac_of(lat, ty, 1, jj);
 #pragma unroll
         for (int d = 0; d < 3; d++) {
-          const ds *E = s_E + (ii * 3 + d) * 4;
-          const ds B = ds_lerp(E[0], E[1], b), T = ds_lerp(E[2], E[3], b);
-          s_U[threadIdx.x * 3 + d] = ds_sub(B, l0[d]);
-          s_D[threadIdx.x * 3 + d] = ds_sub(T, B);
+          const ds *c = s_col + (ii * 3 + d) * 4;
+          s_U[threadIdx.x * 3 + d] = ds_madd(b, c[1], c[0]);
+          s_D[threadIdx.x * 3 + d] = ds_madd(b, c[3], c[2]);
         }
       }
     }
+    int at;
+    const int total = block_scan(__popcll(mk), at, s_warp);
+    for (unsigned long long m = mk; m; m &= m - 1)
+      s_list[at++] = (unsigned short) ((threadIdx.x << 6) | (__ffsll((long long) m) - 1));
     __syncthreads();
-    // site t = l * naz + kk of the chunk; (l, kk) stepped by LCH without a division
-    const int nsite = nl * naz, dl = LCH / naz, dk = LCH - dl * naz;
-    int l = threadIdx.x / naz, kk = threadIdx.x - l * naz;
-    for (int t = threadIdx.x; t < nsite; t += LCH) {
-      if (kk >= 64 || ((s_mask[l] >> kk) & 1ull)) {
+    for (int t = threadIdx.x; t < total; t += LCH) {
+      const int v = s_list[t], l = v >> 6, kk = v & 63;
+      const ds c = s_c[kk];
+      const ds *U = s_U + 3 * l, *D = s_D + 3 * l;
+      site_q[base + (size_t) (L0 + l) * naz + kk] =
+          pack_u(ds_madd(c, D[0], U[0]), ds_madd(c, D[1], U[1]), ds_madd(c, D[2], U[2]), pg);
+    }
+    if (naz > 64 && threadIdx.x < nl)  // sites beyond the mask's 64 bits: every one
+      for (int kk = 64; kk < naz; kk++) {
         const ds c = s_c[kk];
-        const ds *U = s_U + 3 * l, *D = s_D + 3 * l;
-        site_q[base + (size_t) L0 * naz + t] =
+        const ds *U = s_U + 3 * threadIdx.x, *D = s_D + 3 * threadIdx.x;
+        site_q[base + (size_t) (L0 + threadIdx.x) * naz + kk] =
             pack_u(ds_madd(c, D[0], U[0]), ds_madd(c, D[1], U[1]), ds_madd(c, D[2], U[2]), pg);
       }
-      l += dl;
-      kk += dk;
-      if (kk >= naz) {
-        kk -= naz;
-        l++;
-      }
-    }
   }
 }
 
 // F'(rho) at the referenced sites, rho = sum_k N_k erho_k (pair_eam.cpp:1060-1065)
-// by the same lerps in FP32; one block per element, lines LCH at a time.
+// by the same lerps in FP32; one block per element, lines LCH at a time, the
+// referenced sites listed in shared memory as in k_site_q.
 __global__ void __launch_bounds__(LCH)
 k_site_fp(const double *__restrict__ erho, const int *__restrict__ etype,
           const int *__restrict__ site_base, Lattice lat,
           const unsigned long long *__restrict__ line_mask, int maxlines,
           const float4 *__restrict__ fp4, int nrho, float rdrho, float *__restrict__ site_fp) {
-  const int *nae = lat.nae;
   __shared__ float s_er[NPE];
   __shared__ float s_U[LCH], s_D[LCH];
-  __shared__ unsigned long long s_mask[LCH];
+  __shared__ int s_warp[LCH / 32];
+  __shared__ unsigned short s_list[LCH * 64];
   const int e = blockIdx.x;
   const int ty = etype[e];
+  const int *nae = lat.nae;
   const int nax = nae[3 * ty], nay = nae[3 * ty + 1], naz = nae[3 * ty + 2];
   if (threadIdx.x < NPE) s_er[threadIdx.x] = (float) erho[NPE * (size_t) e + threadIdx.x];
   const int nlines = nax * nay, base = site_base[e];
@@ -862,11 +903,11 @@ k_site_fp(const double *__restrict__ erho, const int *__restrict__ etype,
   for (int L0 = 0; L0 < nlines; L0 += LCH) {
     const int nl = min(LCH, nlines - L0);
     __syncthreads();
+    unsigned long long mk = 0;
     if (threadIdx.x < nl) {
       const int L = L0 + threadIdx.x;
-      const unsigned long long mk = lm[L];
-      s_mask[threadIdx.x] = mk;
-      const int ii = L / nay, jj = L % nay;
+      mk = lm[L];
+      const int ii = L / nay, jj = L - ii * nay;
       const float a = frac_of(lat, ty, 0, ii).h, b = frac_of(lat, ty, 1, jj).h;
       const float e0 = s_er[0] + a * (s_er[1] - s_er[0]), e1 = s_er[3] + a * (s_er[2] - s_er[3]);
       const float e2 = s_er[4] + a * (s_er[5] - s_er[4]), e3 = s_er[7] + a * (s_er[6] - s_er[7]);
@@ -874,21 +915,21 @@ k_site_fp(const double *__restrict__ erho, const int *__restrict__ etype,
       s_U[threadIdx.x] = B;
       s_D[threadIdx.x] = T - B;
     }
+    int at;
+    const int total = block_scan(__popcll(mk), at, s_warp);
+    for (unsigned long long m = mk; m; m &= m - 1)
+      s_list[at++] = (unsigned short) ((threadIdx.x << 6) | (__ffsll((long long) m) - 1));
     __syncthreads();
-    const int nsite = nl * naz, dl = LCH / naz, dk = LCH - dl * naz;
-    int l = threadIdx.x / naz, kk = threadIdx.x - l * naz;
-    for (int t = threadIdx.x; t < nsite; t += LCH) {
-      if (kk >= 64 || ((s_mask[l] >> kk) & 1ull)) {
-        const float rho = s_U[l] + frac_of(lat, ty, 2, kk).h * s_D[l];
-        site_fp[base + (size_t) L0 * naz + t] = fprime32(rho, fp4, nrho, rdrho);
-      }
-      l += dl;
-      kk += dk;
-      if (kk >= naz) {
-        kk -= naz;
-        l++;
-      }
+    for (int t = threadIdx.x; t < total; t += LCH) {
+      const int v = s_list[t], l = v >> 6, kk = v & 63;
+      const float rho = s_U[l] + frac_of(lat, ty, 2, kk).h * s_D[l];
+      site_fp[base + (size_t) (L0 + l) * naz + kk] = fprime32(rho, fp4, nrho, rdrho);
     }
+    if (naz > 64 && threadIdx.x < nl)
+      for (int kk = 64; kk < naz; kk++) {
+        const float rho = s_U[threadIdx.x] + frac_of(lat, ty, 2, kk).h * s_D[threadIdx.x];
+        site_fp[base + (size_t) (L0 + threadIdx.x) * naz + kk] = fprime32(rho, fp4, nrho, rdrho);
+      }
   }
 }
 
