@@ -1,18 +1,20 @@
-// Mixed-precision pair kernels (sm_103a): FP32 pair terms, FP64 accumulation.
+// Mixed-precision pair kernels (sm_103a): FP32 pair terms, no FP64 instruction in
+// any pair loop.
 //
 // Same formulas as the FP64 kernels (PairLJCut::compute/ecompute,
 // pair_lj_cut.cpp:227-442; PairEAM::compute/ecompute, pair_eam.cpp:584-1141),
-// evaluated in FP32 where the spec allows it:
-//  * atom coordinates are double-single pairs (hi = float(x), lo = float(x-hi)),
-//    so a pair vector (hi_i-hi_j)+(lo_i-lo_j) is good to ~1e-6 A at any box size;
-//  * element sites and integration points are interpolated once per step in
-//    double-single FP32 arithmetic (k_sites_ds), stored as hi/lo float pairs;
+// evaluated in FP32 within a 1e-4 relative force tolerance:
+//  * positions are packed cell-relative: xyz = the offset from a cell of
+//    power-of-two size g in FP32, w = the cell; a pair vector
+//    (q_i - q_j) + g (cell_i - cell_j) is exact up to one FP32 rounding at any
+//    box size.  Atoms are packed from their FP64 positions, element sites and
+//    integration points from double-single interpolation of the nodes;
 //  * r, 1/r and the rho(r), r*phi(r) splines are FP32, the spline coefficients
 //    FP32 in shared memory, loaded once by each resident block (persistent grid);
 //  * the cutoff test is made in FP32 and re-made in FP64 inside a thin guard
-//    band, so the set of interacting pairs is exactly the FP64 set;
-//  * per-site densities and forces are summed in FP32 over chunks of 8 pairs and
-//    the chunks in FP64; F'(rho) is evaluated from the FP64 table in FP64.
+//    band, so the set of interacting pairs is the FP64 set;
+//  * densities and forces are summed in FP32 over chunks of 8 pairs and the
+//    chunks as FP32 double-single pairs; F'(rho) of atoms and sites is FP32.
 #include <algorithm>
 #include <vector>
 

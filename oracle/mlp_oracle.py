@@ -1,6 +1,6 @@
 """CPU restatement of the surrogate MLP (numpy), for tests only.
 
-This is test infrastructure: the checker for the device MLP in
+This is test infrastructure: the oracle for the device MLP in
 cac_code_gb300/csrc/mlp.cu and k_gemm.cu, never a product path.  The
 reference has no surrogate (it evaluates every element by integration-point
 quadrature), so the network has no reference file to cite; this module

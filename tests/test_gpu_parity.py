@@ -4,7 +4,7 @@
   trajectories bit-identical to the reference's golden outputs and to the CPU
   restatement run on the same host.
 * FP64 (fused multiply-add): lists identical; forces within 1e-12 of the force
-  scale (max |f| of the reference) -- the spec FP64 tolerance.
+  scale (max |f| of the reference) -- the FP64 tolerance of the path.
 """
 import numpy as np
 import pytest

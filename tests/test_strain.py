@@ -1,7 +1,7 @@
 """Uniaxial strain ramp (fix deform, x erate): the box grows as
 L(t) = L0 (1 + R t) about its centre with affine remaps of the positions.
 The reference has no box deformation, so the oracle's restatement is the
-checker (parity unpinned against the reference itself)."""
+reference here (parity unpinned against the reference itself)."""
 import numpy as np
 import pytest
 
