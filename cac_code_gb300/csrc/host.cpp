@@ -150,6 +150,7 @@ struct cacg_context {
   // atoms (host staging until init)
   int ntypes = 0;
   double amass[MAXT + 1] = {};
+  double up_mass[MAXT + 1] = {}, up_emass[MAXT + 1] = {};  // the masses on the device
   std::vector<double> h_x, h_v;
   std::vector<int> h_type, h_tag;
   int nlocal = 0, nghost = 0;
@@ -440,6 +441,7 @@ struct cacg_context {
   void post_force();
   void upload_masks();
   void check_packed_range();
+  void nve_scales(TypeScale &a, TypeScale &e) const;
   // cell-relative packed coordinates of the mixed passes: cells of a
   // power-of-two size g cover the box, its ghost shell and a margin in
   // 4096 x 1024 x 1024 cells from the corner l0
@@ -1795,6 +1797,10 @@ void cacg_context::init() {
   }
   upload(d_mass, massv, s);
   upload(d_emass, emassv, s);
+  for (int t = 0; t <= MAXT; t++) {
+    up_mass[t] = massv[t];
+    up_emass[t] = emassv[t];
+  }
   nghost = 0;
   int ne = std::max(enlocal, 1);
   d_ex.ensure(3 * (size_t) ne, s);
@@ -2760,17 +2766,30 @@ void cacg_context::compute_thermo(double *out) {
 
 // ------------------------------------------------------------------ integrate
 
+// FixNVE's dtfm = dtf / mass per atom type, and dtf / (M_e / 8) per element
+// type (fix_nve.cpp:54-157), formed on the host: the same IEEE quotients
+void cacg_context::nve_scales(TypeScale &a, TypeScale &e) const {
+  const double dtf = 0.5 * dt * ftm2v;
+  const double inv_npe = 1 / (double) NPE;
+  for (int t = 0; t <= MAXT; t++) {
+    a.v[t] = up_mass[t] != 0.0 ? dtf / up_mass[t] : 0.0;
+    e.v[t] = up_emass[t] != 0.0 ? dtf / (inv_npe * up_emass[t]) : 0.0;
+  }
+}
+
 void cacg_context::nve_initial() {
-  double dtf = 0.5 * dt * ftm2v;
-  launch_nve_atoms_initial(d_x.p, d_v.p, d_f.p, d_type.p, d_mass.p, nlocal, dt, dtf, stream);
-  launch_nve_nodes_initial(d_ex.p, d_nodex.p, d_nodev.p, d_nodef.p, d_etype.p, d_emass.p, enlocal, dt, dtf, stream);
+  TypeScale a, e;
+  nve_scales(a, e);
+  launch_nve_atoms_initial(d_x.p, d_v.p, d_f.p, d_type.p, a, nlocal, dt, stream);
+  launch_nve_nodes_initial(d_ex.p, d_nodex.p, d_nodev.p, d_nodef.p, d_etype.p, e, enlocal, dt, stream);
   launches += 2;
 }
 
 void cacg_context::nve_final() {
-  double dtf = 0.5 * dt * ftm2v;
-  launch_nve_atoms_final(d_v.p, d_f.p, d_type.p, d_mass.p, nlocal, dtf, stream);
-  launch_nve_nodes_final(d_nodev.p, d_nodef.p, d_etype.p, d_emass.p, enlocal, dtf, stream);
+  TypeScale a, e;
+  nve_scales(a, e);
+  launch_nve_atoms_final(d_v.p, d_f.p, d_type.p, a, nlocal, stream);
+  launch_nve_nodes_final(d_nodev.p, d_nodef.p, d_etype.p, e, enlocal, stream);
   launches += 2;
 }
 

@@ -703,27 +703,37 @@ __device__ __forceinline__ float4 pack_u(ds ux, ds uy, ds uz, const PackGrid &pg
 
 // packed coordinates; with a reference (the packed coordinates of the list
 // reorder, same grid) the largest squared displacement of the first nref
-// atoms is folded into *dmax2 (float bits, atomic max)
-__global__ void k_pack_rel(const double4 *__restrict__ x, int n, PackGrid pg,
-                           float4 *__restrict__ xq, const float4 *__restrict__ ref, int nref,
-                           unsigned *__restrict__ dmax2) {
+// atoms is folded into *dmax2 (float bits, one atomic max per block)
+constexpr int PACK_BLOCK = 256;
+
+__global__ void __launch_bounds__(PACK_BLOCK)
+k_pack_rel(const double4 *__restrict__ x, int n, PackGrid pg, float4 *__restrict__ xq,
+           const float4 *__restrict__ ref, int nref, unsigned *__restrict__ dmax2) {
+  __shared__ unsigned s_max[PACK_BLOCK / 32];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double4 p = x[i];
-  const float4 q = pack_u(ds_sub(ds_of_double(p.x), ds{pg.l0h[0], pg.l0l[0]}),
-                          ds_sub(ds_of_double(p.y), ds{pg.l0h[1], pg.l0l[1]}),
-                          ds_sub(ds_of_double(p.z), ds{pg.l0h[2], pg.l0l[2]}), pg);
-  xq[i] = q;
-  if (ref) {
-    float d2 = 0.f;
-    if (i < nref) {
+  unsigned m = 0u;
+  if (i < n) {
+    const double4 p = x[i];
+    const float4 q = pack_u(ds_sub(ds_of_double(p.x), ds{pg.l0h[0], pg.l0l[0]}),
+                            ds_sub(ds_of_double(p.y), ds{pg.l0h[1], pg.l0l[1]}),
+                            ds_sub(ds_of_double(p.z), ds{pg.l0h[2], pg.l0l[2]}), pg);
+    xq[i] = q;
+    if (ref && i < nref) {
       float cx, cy, cz, dx, dy, dz;
       cell_of(q, cx, cy, cz);
       rel_vec(q, cx, cy, cz, ref[i], pg.g, dx, dy, dz);
-      d2 = dx * dx + dy * dy + dz * dz;
+      m = __float_as_uint(dx * dx + dy * dy + dz * dz);
     }
-    const unsigned m = __reduce_max_sync(__activemask(), __float_as_uint(d2));
-    if ((threadIdx.x & 31) == __ffs(__activemask()) - 1) atomicMax(dmax2, m);
+  }
+  if (ref) {  // the same for every thread of the grid
+    m = __reduce_max_sync(0xffffffffu, m);
+    if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      m = threadIdx.x < PACK_BLOCK / 32 ? s_max[threadIdx.x] : 0u;
+      m = __reduce_max_sync(0xffffffffu, m);
+      if (threadIdx.x == 0 && m) atomicMax(dmax2, m);
+    }
   }
 }
 
@@ -1253,7 +1263,7 @@ PackGrid make_pack_grid(const double l0[3], double g, int *oob) {
 void pack_rel(const double4 *x, int n, const PackGrid &pg, float4 *xq, const float4 *ref, int nref,
               unsigned *dmax2, cudaStream_t s) {
   if (n <= 0) return;
-  k_pack_rel<<<nblk(n, 256), 256, 0, s>>>(x, n, pg, xq, ref, nref, dmax2);
+  k_pack_rel<<<nblk(n, PACK_BLOCK), PACK_BLOCK, 0, s>>>(x, n, pg, xq, ref, nref, dmax2);
   check(cudaGetLastError(), "pack_rel");
 }
 

@@ -12,11 +12,10 @@ inline int nblk(long long n, int t) { return (int) ((n + t - 1) / t); }
 // FixNVE::initial_integrate, fix_nve.cpp:54-98 (per-type mass branch)
 __global__ void k_nve_atoms_initial(double4 *__restrict__ x, double *__restrict__ v,
                                     const double *__restrict__ f, const int *__restrict__ type,
-                                    const double *__restrict__ mass, int n, double dtv,
-                                    double dtf) {
+                                    TypeScale dtfm_t, int n, double dtv) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double dtfm = dtf / mass[type[i]];
+  double dtfm = dtfm_t.v[type[i]];
   double vx = v[3 * i] + dtfm * f[3 * i];
   double vy = v[3 * i + 1] + dtfm * f[3 * i + 1];
   double vz = v[3 * i + 2] + dtfm * f[3 * i + 2];
@@ -32,11 +31,10 @@ __global__ void k_nve_atoms_initial(double4 *__restrict__ x, double *__restrict_
 
 // FixNVE::final_integrate, fix_nve.cpp:181-212
 __global__ void k_nve_atoms_final(double *__restrict__ v, const double *__restrict__ f,
-                                  const int *__restrict__ type, const double *__restrict__ mass,
-                                  int n, double dtf) {
+                                  const int *__restrict__ type, TypeScale dtfm_t, int n) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double dtfm = dtf / mass[type[i]];
+  double dtfm = dtfm_t.v[type[i]];
   v[3 * i] = v[3 * i] + dtfm * f[3 * i];
   v[3 * i + 1] = v[3 * i + 1] + dtfm * f[3 * i + 1];
   v[3 * i + 2] = v[3 * i + 2] + dtfm * f[3 * i + 2];
@@ -47,13 +45,11 @@ __global__ void k_nve_atoms_final(double *__restrict__ v, const double *__restri
 __global__ void k_nve_nodes_initial(double *__restrict__ ex, double *__restrict__ nodex,
                                     double *__restrict__ nodev,
                                     const double *__restrict__ nodef,
-                                    const int *__restrict__ etype,
-                                    const double *__restrict__ emass, int n, double dtv,
-                                    double dtf) {
+                                    const int *__restrict__ etype, TypeScale dtfm_t, int n,
+                                    double dtv) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const double inv_npe = 1 / (double) NPE;
-  double dtfm = dtf / (inv_npe * emass[etype[i]]);
+  double dtfm = dtfm_t.v[etype[i]];
   double c[3] = {0.0, 0.0, 0.0};
   for (int q = 0; q < NPE; q++) {
     for (int d = 0; d < 3; d++) {
@@ -70,13 +66,11 @@ __global__ void k_nve_nodes_initial(double *__restrict__ ex, double *__restrict_
 
 // FixNVE::efinal_integrate, fix_nve.cpp:216-242
 __global__ void k_nve_nodes_final(double *__restrict__ nodev, const double *__restrict__ nodef,
-                                  const int *__restrict__ etype,
-                                  const double *__restrict__ emass, int n, double dtf) {
+                                  const int *__restrict__ etype, TypeScale dtfm_t, int n) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * 24) return;
   int i = t / 24;
-  const double inv_npe = 1 / (double) NPE;
-  double dtfm = dtf / (inv_npe * emass[etype[i]]);
+  double dtfm = dtfm_t.v[etype[i]];
   nodev[t] = nodev[t] + dtfm * nodef[t];
 }
 
@@ -167,34 +161,31 @@ __global__ void k_fma_loop(double *out, int iters) {
 }  // namespace
 
 void launch_nve_atoms_initial(double4 *x, double *v, const double *f, const int *type,
-                              const double *mass, int n, double dtv, double dtf,
-                              cudaStream_t s) {
+                              const TypeScale &dtfm, int n, double dtv, cudaStream_t s) {
   if (n <= 0) return;
-  k_nve_atoms_initial<<<nblk(n, 256), 256, 0, s>>>(x, v, f, type, mass, n, dtv, dtf);
+  k_nve_atoms_initial<<<nblk(n, 256), 256, 0, s>>>(x, v, f, type, dtfm, n, dtv);
   check(cudaGetLastError(), "nve_atoms_initial");
 }
 
-void launch_nve_atoms_final(double *v, const double *f, const int *type, const double *mass,
-                            int n, double dtf, cudaStream_t s) {
+void launch_nve_atoms_final(double *v, const double *f, const int *type, const TypeScale &dtfm,
+                            int n, cudaStream_t s) {
   if (n <= 0) return;
-  k_nve_atoms_final<<<nblk(n, 256), 256, 0, s>>>(v, f, type, mass, n, dtf);
+  k_nve_atoms_final<<<nblk(n, 256), 256, 0, s>>>(v, f, type, dtfm, n);
   check(cudaGetLastError(), "nve_atoms_final");
 }
 
 void launch_nve_nodes_initial(double *ex, double *nodex, double *nodev, const double *nodef,
-                              const int *etype, const double *emass, int n, double dtv,
-                              double dtf, cudaStream_t s) {
+                              const int *etype, const TypeScale &dtfm, int n, double dtv,
+                              cudaStream_t s) {
   if (n <= 0) return;
-  k_nve_nodes_initial<<<nblk(n, 128), 128, 0, s>>>(ex, nodex, nodev, nodef, etype, emass, n,
-                                                    dtv, dtf);
+  k_nve_nodes_initial<<<nblk(n, 128), 128, 0, s>>>(ex, nodex, nodev, nodef, etype, dtfm, n, dtv);
   check(cudaGetLastError(), "nve_nodes_initial");
 }
 
 void launch_nve_nodes_final(double *nodev, const double *nodef, const int *etype,
-                            const double *emass, int n, double dtf, cudaStream_t s) {
+                            const TypeScale &dtfm, int n, cudaStream_t s) {
   if (n <= 0) return;
-  k_nve_nodes_final<<<nblk((long long) n * 24, 256), 256, 0, s>>>(nodev, nodef, etype, emass,
-                                                                   n, dtf);
+  k_nve_nodes_final<<<nblk((long long) n * 24, 256), 256, 0, s>>>(nodev, nodef, etype, dtfm, n);
   check(cudaGetLastError(), "nve_nodes_final");
 }
 
