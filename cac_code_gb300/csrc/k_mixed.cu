@@ -166,21 +166,22 @@ k_eam_rho_atoms(AtomArgs a, const float4 *__restrict__ rhor_val, int nr, float r
     dsacc acc;
     float part = 0.f;
     int ns = 0, cnt = 0;
-    // the next entry's index and coordinates are fetched while this one is
-    // evaluated: two dependent gathers in flight per thread instead of one
-    int jn = 0;
+    // software pipeline: the list index two entries ahead and the coordinates
+    // one entry ahead are in flight while this entry is evaluated, so the
+    // gather never waits on a list load issued in the same iteration
+    int jn = 0, jnn = 0;
     float4 qn = qi;
     if (n > 0) {
       jn = __ldg(a.list + i);
       qn = __ldg(a.xq + jn);
     }
+    if (n > 1) jnn = __ldg(a.list + (size_t) a.stride + i);
     for (int k = 0; k < n; k++) {
       const int j = jn;
       const float4 qj = qn;
-      if (k + 1 < n) {
-        jn = __ldg(a.list + (size_t) (k + 1) * a.stride + i);
-        qn = __ldg(a.xq + jn);
-      }
+      jn = jnn;
+      if (k + 2 < n) jnn = __ldg(a.list + (size_t) (k + 2) * a.stride + i);
+      if (k + 1 < n) qn = __ldg(a.xq + jn);
       float dx, dy, dz;
       rel_vec(qi, cx, cy, cz, qj, a.qg, dx, dy, dz);
       float rsq = dx * dx + dy * dy + dz * dz;
