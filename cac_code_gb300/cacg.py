@@ -332,12 +332,13 @@ class System:
 
     # ---- state out ----
     def counts(self) -> Dict[str, int]:
-        c = np.zeros(21, dtype=np.int64)
-        self._ok(self._L.cacg_get_counts(self.h, c.ctypes.data_as(_lp), 21))
+        c = np.zeros(23, dtype=np.int64)
+        self._ok(self._L.cacg_get_counts(self.h, c.ctypes.data_as(_lp), 23))
         keys = ["nlocal", "nghost", "atom_entries", "enlocal", "enghost", "elem_entries",
                 "ip_rows", "ip_entries", "rebuilds", "nstencil", "step", "sites", "launches",
                 "sites_needed", "force_rows", "short_entries", "surrogate_elements",
-                "surrogate_evaluated", "surrogate_accepted", "graph_steps", "density_scan_entries"]
+                "surrogate_evaluated", "surrogate_accepted", "graph_steps", "density_scan_entries",
+                "ip_scan_entries", "ip_reorders"]
         return dict(zip(keys, (int(v) for v in c)))
 
     def atoms(self, all_: bool = False) -> Dict[str, np.ndarray]:

@@ -213,6 +213,16 @@ struct cacg_context {
   DBuf<float4> d_ip_q, d_ip_h, d_ip_l;
   DBuf<float> d_row_fpf;
   DBuf<int> d_row_start, d_ent;
+  // displacement culling of the integration-point lists: rows' near entries
+  // first, their count, the nodes at the reorder, near-site masks, the line
+  // code of every site, force-row flags; reordered once per element list build
+  // and whenever a node has moved 0.495 A since
+  DBuf<int> d_ent_near, d_nnear_row, d_site_code;
+  DBuf<float2> d_node_ref;
+  DBuf<unsigned long long> d_line_mask_n, d_line_mask_nf;
+  DBuf<unsigned char> d_row_isforce;
+  long long elist_builds = 0, epart_of = -1;
+  bool ereorders_zeroed = false;  // the reorder counter (d_misc slot 15)
   int mixed_ip_group = 8;  // lanes per integration point ("tune ip_group N")
   int maxlines = 0, max_nax = 0, max_naz = 0;
   DBuf<double> d_cutsq64, d_stage, d_part, d_lj5;
@@ -500,6 +510,13 @@ cacg_context::~cacg_context() {
   d_row_fpf.release();
   d_row_start.release();
   d_ent.release();
+  d_ent_near.release();
+  d_nnear_row.release();
+  d_site_code.release();
+  d_node_ref.release();
+  d_line_mask_n.release();
+  d_line_mask_nf.release();
+  d_row_isforce.release();
   d_ljf.release();
   d_cutsq64.release();
   d_stage.release();
@@ -1843,6 +1860,9 @@ void cacg_context::init() {
       if (weight[h_etype[re[r]]][rj[r]] != 0.0) fr.push_back(r);
     nforce = (int) fr.size();
     upload(d_force_rows, fr, s);
+    std::vector<unsigned char> isf(std::max(nrows, 1), 0);
+    for (int r : fr) isf[r] = 1;
+    upload(d_row_isforce, isf, s);
     element_size();
   } else {
     nrows = 0;
@@ -2126,6 +2146,12 @@ void cacg_context::neighbor_nbuild() {
   mixed::line_mask(d_site_pos.p, d_etype.p, d_site_base.p, d_nae.p, nall, maxlines,
                    d_line_mask_f.p, s);
   launches += 3;
+  if (max_naz <= 64) {  // the line code of every site (mixed list culling)
+    d_site_code.ensure(std::max(nsites, 1), s);
+    mixed::site_code(d_etype.p, d_site_base.p, d_nae.p, maxlines, nall, d_site_code.p, s);
+    launches++;
+  }
+  elist_builds++;
   elists_built = true;
 }
 
@@ -2301,16 +2327,50 @@ void cacg_context::pair_ecompute_mixed() {
   const mixed::PackGrid pg = mixed::make_pack_grid(l0, g, d_misc.p + 9);
   d_site_q.ensure(std::max(nsites, 1), s);
   d_node_hl.ensure((size_t) 24 * nall, s);
-  mixed::node_split(d_nodex.p, nall, d_node_hl.p, s);
+  // displacement culling of the integration-point lists: slot 13 holds the
+  // largest squared node displacement since the last reorder (set huge after
+  // an element list build, so that this pass reorders), slot 14 flags a
+  // reorder in this pass
+  // (the lists are kept reordered even with "tune cull no", so that culling
+  // changes no bit: it only stops each row before its far entries)
+  const bool reorder_e = max_naz <= 64 && nrows > 0;
+  const bool cull_e = reorder_e && mixed_cull;
+  const long long nmask = (long long) std::max(nall, 1) * std::max(maxlines, 1);
+  unsigned *eflags = reinterpret_cast<unsigned *>(d_misc.p + 13);
+  const bool same_e = reorder_e && epart_of == elist_builds;
+  if (reorder_e) {
+    d_ent_near.ensure(std::max((size_t) 1, d_ent.cap), s);
+    d_nnear_row.ensure(std::max(nrows, 1), s);
+    d_node_ref.ensure((size_t) 24 * nall, s);
+    d_line_mask_n.ensure(nmask, s);
+    d_line_mask_nf.ensure(nmask, s);
+  }
+  if (!ereorders_zeroed) {
+    check(cudaMemsetAsync(d_misc.p + 15, 0, sizeof(int), s), "ereorders");
+    ereorders_zeroed = true;
+  }
+  check(cudaMemsetAsync(d_misc.p + 13, same_e ? 0 : 0x7F, sizeof(int), s), "edmax");
+  check(cudaMemsetAsync(d_misc.p + 14, 0, sizeof(int), s), "ereordered");
+  mixed::node_split(d_nodex.p, nall, d_node_hl.p, same_e ? d_node_ref.p : nullptr, eflags, s);
   const mixed::Lattice lat{d_nae.p, d_frac.p, fstride};
   mixed::site_q(d_node_hl.p, d_etype.p, d_site_base.p, lat, max_nax, max_naz, d_line_mask.p,
-                maxlines, pg, nall, d_site_q.p, s);
+                cull_e ? d_line_mask_n.p : nullptr, eflags, maxlines, pg, nall, d_site_q.p, s);
   d_ip_q.ensure(std::max(nrows, 1), s);
   d_ip_h.ensure(std::max(nrows, 1), s);
   d_ip_l.ensure(std::max(nrows, 1), s);
   mixed::row_q(d_row_elem.p, d_row_jj.p, d_etype.p, d_int_off.p, d_spa_int_hl.p, d_node_hl.p, nrows,
                pg, d_ip_q.p, d_ip_h.p, d_ip_l.p, s);
   launches += 3;
+  const double csq_e = pair_style == 1 ? ljtab.cutsq[1 * (MAXT + 1) + 1] : cutforcesq;
+  if (reorder_e) {
+    mixed::ip_reorder(d_row_start.p, d_ent.p, nrows, d_ip_q.p, d_site_q.p, pg.g,
+                      (float) std::sqrt(csq_e), d_ent_near.p, d_nnear_row.p, d_node_hl.p, nall,
+                      d_node_ref.p, eflags, s);
+    mixed::near_masks(d_row_start.p, d_ent_near.p, d_nnear_row.p, nrows, d_row_isforce.p,
+                      d_site_code.p, d_line_mask_n.p, d_line_mask_nf.p, nmask, eflags, s);
+    launches += 3;
+    epart_of = elist_builds;
+  }
   const bool use_sur = sur && nfar > 0;
   const float eps = 1.0e-4f;
   mixed::MixedElems m{};
@@ -2325,7 +2385,9 @@ void cacg_context::pair_ecompute_mixed() {
   m.row_first = d_row_first.p;
   m.node_list = d_node_list.p;
   m.row_start = d_row_start.p;
-  m.ent = d_ent.p;
+  m.ent = reorder_e ? d_ent_near.p : d_ent.p;
+  m.nnear_row = cull_e ? d_nnear_row.p : nullptr;
+  m.eflags = eflags;
   m.nlocal_e = enlocal;
   m.rows = d_force_rows.p;
   m.nforce = nforce;
@@ -2356,8 +2418,9 @@ void cacg_context::pair_ecompute_mixed() {
     d_site_fpf.ensure(std::max(nsites, 1), s);
     mixed::ip_pass(m, 1, d_rhor_val4.p, e, 0.f, 0.f, d_erho.p, nullptr, s);
     launch_copy_root(d_erho.p, NPE, d_eroot.p, enlocal, enghost, s);
-    mixed::site_fp(d_erho.p, d_etype.p, d_site_base.p, lat, d_line_mask_f.p, maxlines, d_fp4.p,
-                   nrho, rdrho, nall, d_site_fpf.p, s);
+    mixed::site_fp(d_erho.p, d_etype.p, d_site_base.p, lat, d_line_mask_f.p,
+                   cull_e ? d_line_mask_nf.p : nullptr, eflags, maxlines, d_fp4.p, nrho, rdrho,
+                   nall, d_site_fpf.p, s);
     d_row_fpf.ensure(std::max(nrows, 1), s);
     mixed::row_fp(d_force_rows.p, nforce, d_row_elem.p, d_row_jj.p, d_etype.p, d_int_off.p,
                   d_spa_int.p, d_erho.p, e, d_row_fpf.p, s);
@@ -3227,10 +3290,10 @@ int cacg_run(cacg_handle h, int nsteps) {
 
 int cacg_get_counts(cacg_handle h, long long *c, int n) {
   API_BEGIN
-  long long v[21] = {h->nlocal, h->nghost, 0, h->enlocal, h->enghost, 0, h->nrows, 0,
+  long long v[23] = {h->nlocal, h->nghost, 0, h->enlocal, h->enghost, 0, h->nrows, 0,
                      h->nrebuild, (long long) h->stencil.size(), h->ntimestep, h->nsites,
                      h->launches, h->nneed, h->nforce, 0, h->sur ? h->nfar : 0, 0, 0,
-                     h->graph_steps, 0};
+                     h->graph_steps, 0, 0, 0};
   if (h->sur && h->d_scount.p) {
     unsigned long long c2[2] = {0, 0};
     check(cudaMemcpyAsync(c2, h->d_scount.p, sizeof(c2), cudaMemcpyDeviceToHost, h->stream), "scount");
@@ -3280,7 +3343,26 @@ int cacg_get_counts(cacg_handle h, long long *c, int n) {
       for (int x : nn) v[20] += x;
     }
   }
-  for (int i = 0; i < n && i < 21; i++) c[i] = v[i];
+  // integration-point entries the last mixed passes scanned (near parts while
+  // the node displacement allowed culling) and the list reorders so far
+  v[21] = v[7];
+  if (h->mode == CACG_MIXED && h->epart_of == h->elist_builds && h->nrows && h->d_nnear_row.p &&
+      h->d_misc.p) {
+    unsigned dm[3] = {0, 0, 0};
+    check(cudaMemcpyAsync(dm, h->d_misc.p + 13, sizeof(dm), cudaMemcpyDeviceToHost, h->stream), "edmax");
+    h->sync();
+    v[22] = dm[2];
+    float d2;
+    std::memcpy(&d2, &dm[0], sizeof(float));
+    if (h->mixed_cull && (dm[1] != 0u || 2.0f * std::sqrt(d2) + mixed::CULL_MARGIN <= mixed::CULL_DELTA)) {
+      std::vector<int> nn(h->nrows);
+      check(cudaMemcpyAsync(nn.data(), h->d_nnear_row.p, sizeof(int) * h->nrows, cudaMemcpyDeviceToHost, h->stream), "nnear_row");
+      h->sync();
+      v[21] = 0;
+      for (int x : nn) v[21] += x;
+    }
+  }
+  for (int i = 0; i < n && i < 23; i++) c[i] = v[i];
   API_END
 }
 

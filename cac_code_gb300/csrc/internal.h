@@ -290,6 +290,10 @@ struct MixedElems {
   const float *row_fp;        // FP32 F'(rho) at the rows of nonzero weight (EAM force pass)
   const int *etype, *row_elem, *row_first, *node_list;
   const int *row_start, *ent;  // integration-point lists, row-major
+  // displacement culling: ent holds each row's near entries first, nnear_row
+  // counts them; eflags = [node displacement^2 bits, reordered this step]
+  const int *nnear_row = nullptr;
+  const unsigned *eflags = nullptr;
   int nlocal_e;
   const int *rows;  // rows of nonzero weight (force passes), count nforce
   int nforce;
@@ -311,7 +315,9 @@ PackGrid make_pack_grid(const double l0[3], double g, int *oob);
 // squared displacement of the first nref atoms is max-folded into *dmax2
 void pack_rel(const double4 *x, int n, const PackGrid &pg, float4 *xq, const float4 *ref, int nref,
               unsigned *dmax2, cudaStream_t s);
-void node_split(const double *nodex, int n, float2 *hl, cudaStream_t s);
+// with ref: the largest squared node displacement against ref -> *dmax2 (atomic max)
+void node_split(const double *nodex, int n, float2 *hl, const float2 *ref, unsigned *dmax2,
+                cudaStream_t s);
 // per element and lattice line (ii, jj): bit kk set when site (ii, jj, kk) is
 // referenced by an integration-point list
 // flag the sites referenced by the listed rows
@@ -320,13 +326,31 @@ void mark_rows(const int *rows, int nlisted, const int *row_start, const int *en
 void line_mask(const int *flag, const int *etype, const int *site_base, const int *nae, int nelem,
                int maxlines, unsigned long long *mask, cudaStream_t s);
 // packed positions of the referenced sites (double-single interpolation)
+// mask_near (with eflags): the sites of near entries, used while culling holds
 void site_q(const float2 *node_hl, const int *etype, const int *site_base, const Lattice &lat,
-            int max_nax, int max_naz, const unsigned long long *mask, int maxlines,
+            int max_nax, int max_naz, const unsigned long long *mask,
+            const unsigned long long *mask_near, const unsigned *eflags, int maxlines,
             const PackGrid &pg, int nelem, float4 *q, cudaStream_t s);
 // FP32 F'(rho) at the referenced sites; fp4 holds F' coefficients c0..c2 per knot
 void site_fp(const double *erho, const int *etype, const int *site_base, const Lattice &lat,
-             const unsigned long long *mask, int maxlines, const float4 *fp4, int nrho,
-             double rdrho, int nelem, float *fp, cudaStream_t s);
+             const unsigned long long *mask, const unsigned long long *mask_near,
+             const unsigned *eflags, int maxlines, const float4 *fp4, int nrho, double rdrho,
+             int nelem, float *fp, cudaStream_t s);
+// displacement culling of the integration-point lists: reorder (gated on the
+// node displacement in eflags[0]) into ent_near / nnear_row and keep the
+// nodes as the reference (eflags[1] = 1, eflags[2] counts reorders); rebuild
+// the near-site masks after a reorder
+void ip_reorder(const int *row_start, const int *ent, int nrows, const float4 *ip_q,
+                const float4 *site_q, float g, float cutoff, int *ent_near, int *nnear_row,
+                const float2 *node_hl, int nall_e, float2 *node_ref, unsigned *eflags,
+                cudaStream_t s);
+void near_masks(const int *row_start, const int *ent_near, const int *nnear_row, int nrows,
+                const unsigned char *isforce, const int *site_code, unsigned long long *mask,
+                unsigned long long *mask_f, long long nmask, const unsigned *eflags,
+                cudaStream_t s);
+// per site: (element * maxlines + line) << 6 | kk (lattice lines of <= 64 sites)
+void site_code(const int *etype, const int *site_base, const int *nae, int maxlines, int nelem,
+               int *code, cudaStream_t s);
 // each atom's list reordered (entries within cut_rsq at the packed positions,
 // then those within cutoff + 1 A, counted together in nnear, then the rest)
 // when the displacement since the last reorder (dmax2[0], against ref) no

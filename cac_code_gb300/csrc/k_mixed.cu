@@ -668,11 +668,40 @@ __device__ __forceinline__ ds ds_of_double(double x) {
 }
 
 // node coordinates as double-single pairs, once per element and step
-__global__ void k_node_split(const double *__restrict__ nodex, int n, float2 *__restrict__ hl) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n * 24) return;
-  const ds v = ds_of_double(nodex[t]);
-  hl[t] = make_float2(v.h, v.l);
+// with a reference (the split nodes of the last integration-point list
+// reorder) the largest squared node displacement since then is folded into
+// *dmax2 (float bits, one atomic max per block): every site and integration
+// point is a convex combination of its element's nodes, so none moved more
+constexpr int SPLIT_BLOCK = 256;
+
+__global__ void __launch_bounds__(SPLIT_BLOCK)
+k_node_split(const double *__restrict__ nodex, int n, float2 *__restrict__ hl,
+             const float2 *__restrict__ ref, unsigned *__restrict__ dmax2) {
+  __shared__ unsigned s_max[SPLIT_BLOCK / 32];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;  // one node (3 coordinates)
+  float d2 = 0.f;
+  if (t < n * NPE) {
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      const ds v = ds_of_double(nodex[3 * (size_t) t + d]);
+      hl[3 * (size_t) t + d] = make_float2(v.h, v.l);
+      if (ref) {
+        const float2 r = ref[3 * (size_t) t + d];
+        const float dd = __fsub_rn(v.h, r.x) + __fsub_rn(v.l, r.y);
+        d2 += dd * dd;
+      }
+    }
+  }
+  if (ref) {  // the same for every thread of the grid
+    unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(d2));
+    if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      m = threadIdx.x < SPLIT_BLOCK / 32 ? s_max[threadIdx.x] : 0u;
+      m = __reduce_max_sync(0xffffffffu, m);
+      if (threadIdx.x == 0 && m) atomicMax(dmax2, m);
+    }
+  }
 }
 
 __device__ __forceinline__ ds node_ds(const float2 *nx, int k, int d) {
@@ -823,8 +852,9 @@ __device__ __forceinline__ int block_scan(int v, int &excl, int *s_warp) {
 __global__ void __launch_bounds__(LCH)
 k_site_q(const float2 *__restrict__ node_hl, const int *__restrict__ etype,
          const int *__restrict__ site_base, Lattice lat,
-         const unsigned long long *__restrict__ line_mask, int maxlines, PackGrid pg,
-         float4 *__restrict__ site_q) {
+         const unsigned long long *__restrict__ line_mask,
+         const unsigned long long *__restrict__ line_mask_near, const unsigned *__restrict__ eflags,
+         int maxlines, PackGrid pg, float4 *__restrict__ site_q) {
   extern __shared__ ds s_mem[];
   __shared__ float2 s_nx[24];
   __shared__ int s_warp[LCH / 32];
@@ -853,7 +883,9 @@ k_site_q(const float2 *__restrict__ node_hl, const int *__restrict__ etype,
     o[3] = ds_sub(ds_sub(E[3], E[2]), q1);
   }
   const int nlines = nax * nay, base = site_base[e];
-  const unsigned long long *lm = line_mask + (size_t) e * maxlines;
+  // while culling holds only the sites of the rows' near entries are needed
+  const unsigned long long *lm =
+      (line_mask_near && cull_ok(eflags) ? line_mask_near : line_mask) + (size_t) e * maxlines;
   for (int L0 = 0; L0 < nlines; L0 += LCH) {
     const int nl = min(LCH, nlines - L0);
     __syncthreads();  // columns ready; the previous chunk consumed
@@ -900,8 +932,10 @@ k_site_q(const float2 *__restrict__ node_hl, const int *__restrict__ etype,
 __global__ void __launch_bounds__(LCH)
 k_site_fp(const double *__restrict__ erho, const int *__restrict__ etype,
           const int *__restrict__ site_base, Lattice lat,
-          const unsigned long long *__restrict__ line_mask, int maxlines,
-          const float4 *__restrict__ fp4, int nrho, float rdrho, float *__restrict__ site_fp) {
+          const unsigned long long *__restrict__ line_mask,
+          const unsigned long long *__restrict__ line_mask_near, const unsigned *__restrict__ eflags,
+          int maxlines, const float4 *__restrict__ fp4, int nrho, float rdrho,
+          float *__restrict__ site_fp) {
   __shared__ float s_er[NPE];
   __shared__ float s_U[LCH], s_D[LCH];
   __shared__ int s_warp[LCH / 32];
@@ -912,7 +946,9 @@ k_site_fp(const double *__restrict__ erho, const int *__restrict__ etype,
   const int nax = nae[3 * ty], nay = nae[3 * ty + 1], naz = nae[3 * ty + 2];
   if (threadIdx.x < NPE) s_er[threadIdx.x] = (float) erho[NPE * (size_t) e + threadIdx.x];
   const int nlines = nax * nay, base = site_base[e];
-  const unsigned long long *lm = line_mask + (size_t) e * maxlines;
+  // while culling holds only the sites of the rows' near entries are needed
+  const unsigned long long *lm =
+      (line_mask_near && cull_ok(eflags) ? line_mask_near : line_mask) + (size_t) e * maxlines;
   for (int L0 = 0; L0 < nlines; L0 += LCH) {
     const int nl = min(LCH, nlines - L0);
     __syncthreads();
@@ -953,7 +989,9 @@ struct ElemArgs {
   const float4 *ip_h, *ip_l;  // their double-single positions (guard band)
   const float *row_fp;        // F'(rho) at the rows of nonzero weight (EAM force pass)
   const int *etype, *row_elem, *row_first, *node_list;
-  const int *row_start, *ent;  // integration-point lists, row-major
+  const int *row_start, *ent;  // integration-point lists, row-major (near entries first)
+  const int *nnear_row;        // near entries per row (null: no culling)
+  const unsigned *eflags;      // [0] node displacement^2 since the reorder, [1] reordered now
   int nlocal_e;
   const int *rows;
   int nforce;
@@ -1036,6 +1074,94 @@ __global__ void k_ip_csr(const int *__restrict__ ipnum, const int *__restrict__ 
   for (int k = 0; k < n; k++) ent[s0 + k] = __ldg(ipent + (size_t) k * rowstride + r);
 }
 
+// Displacement culling of the integration-point lists (as for the atoms): each
+// row's entries reordered, those within r_c + CULL_DELTA at the reorder first
+// (nnear_row), the rest after; the node positions of the reorder kept as the
+// reference.  Launched every step, it returns at once while no node has moved
+// (CULL_DELTA - CULL_MARGIN) / 2 since the last reorder; else it reorders from
+// this step's packed positions (all referenced sites are computed in such a
+// step) and flags the step (eflags[1]).
+__global__ void k_ip_reorder(const int *__restrict__ row_start, const int *__restrict__ ent,
+                             int nrows, const float4 *__restrict__ ip_q,
+                             const float4 *__restrict__ site_q, float g, float near_rsq,
+                             int *__restrict__ ent_near, int *__restrict__ nnear_row,
+                             const float2 *__restrict__ node_hl, long long nvals,
+                             float2 *__restrict__ node_ref, unsigned *__restrict__ eflags) {
+  if (moved_little(eflags)) return;  // reads eflags[0] only, which no block writes
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    eflags[1] = 1u;
+    eflags[2] += 1u;  // reorders so far
+  }
+  const int stride = gridDim.x * blockDim.x;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += stride) {
+    const float4 qi = ip_q[r];
+    float cx, cy, cz;
+    cell_of(qi, cx, cy, cz);
+    const int s0 = row_start[r], n = row_start[r + 1] - s0;
+    int c = 0;
+    for (int sweep = 0; sweep < 2; sweep++) {
+      int m0 = 0, m1 = c;
+      for (int k = 0; k < n; k++) {
+        const int sid = __ldg(ent + s0 + k);
+        float dx, dy, dz;
+        rel_vec(qi, cx, cy, cz, __ldg(site_q + sid), g, dx, dy, dz);
+        const bool near = dx * dx + dy * dy + dz * dz <= near_rsq;
+        if (sweep == 0) c += near;
+        else ent_near[s0 + (near ? m0++ : m1++)] = sid;
+      }
+    }
+    nnear_row[r] = c;
+  }
+  for (long long t = blockIdx.x * blockDim.x + threadIdx.x; t < nvals; t += stride)
+    node_ref[t] = node_hl[t];
+}
+
+// the near-entry site masks after a reorder in this step (eflags[1]): cleared,
+// then every near entry ORs its site's bit into its line (all rows; rows of
+// nonzero weight also into the force mask)
+__global__ void k_near_masks_clear(unsigned long long *__restrict__ mask,
+                                   unsigned long long *__restrict__ mask_f, long long n,
+                                   const unsigned *__restrict__ eflags) {
+  if (eflags[1] == 0u) return;
+  for (long long t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    mask[t] = 0ull;
+    mask_f[t] = 0ull;
+  }
+}
+
+__global__ void k_near_masks_or(const int *__restrict__ row_start, const int *__restrict__ ent_near,
+                                const int *__restrict__ nnear_row, int nrows,
+                                const unsigned char *__restrict__ isforce,
+                                const int *__restrict__ site_code,
+                                unsigned long long *__restrict__ mask,
+                                unsigned long long *__restrict__ mask_f,
+                                const unsigned *__restrict__ eflags) {
+  if (eflags[1] == 0u) return;
+  const int stride = gridDim.x * blockDim.x;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += stride) {
+    const int s0 = row_start[r], n = nnear_row[r];
+    const bool f = isforce[r] != 0;
+    for (int k = 0; k < n; k++) {
+      const int code = __ldg(site_code + __ldg(ent_near + s0 + k));
+      const unsigned long long bit = 1ull << (code & 63);
+      atomicOr(mask + (code >> 6), bit);
+      if (f) atomicOr(mask_f + (code >> 6), bit);
+    }
+  }
+}
+
+// per site: its line (element * maxlines + line) << 6 | kk, for the masks above
+__global__ void k_site_code(const int *__restrict__ etype, const int *__restrict__ site_base,
+                            const int *__restrict__ nae, int maxlines, int *__restrict__ code) {
+  const int e = blockIdx.x, ty = etype[e];
+  const int naz = nae[3 * ty + 2], nint = nae[3 * ty] * nae[3 * ty + 1] * naz;
+  const int base = site_base[e];
+  for (int t = threadIdx.x; t < nint; t += blockDim.x) {
+    const int L = t / naz, kk = t - L * naz;
+    code[base + t] = (int) ((((long long) e * maxlines + L) << 6) | kk);
+  }
+}
+
 // the site's double-single position, from its owning element (guard band only)
 __device__ __noinline__ void site_ds_of(const ElemArgs &a, int sid, ds (&x)[3]) {
   int lo = 0, hi = a.nall_e;  // site_base[lo] <= sid < site_base[hi]
@@ -1080,6 +1206,7 @@ k_ipg(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr, float lj1, 
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int nitems = DENSITY ? a.nlocal_e * NPE : a.nforce;
+  const bool cull = a.nnear_row && cull_ok(a.eflags);
   // warp-uniform trip count: every lane reaches the shuffles
   for (int wb = warp * GPW; wb < nitems; wb += nwarps * GPW) {
     const int it = wb + gsub;
@@ -1100,7 +1227,7 @@ k_ipg(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr, float lj1, 
     float fpi = 0.f;
     if (live) {
       s0 = a.row_start[r];
-      n = a.row_start[r + 1] - s0;
+      n = cull ? a.nnear_row[r] : a.row_start[r + 1] - s0;
       qi = __ldg(a.ip_q + r);
       if (EAM && !DENSITY) fpi = __ldg(a.row_fp + r);
     }
@@ -1357,9 +1484,11 @@ void lj_atoms(const MixedAtoms &m, const int *type, const float *lj1, const floa
   check(cudaGetLastError(), "lj_atoms_mixed");
 }
 
-void node_split(const double *nodex, int n, float2 *hl, cudaStream_t s) {
+void node_split(const double *nodex, int n, float2 *hl, const float2 *ref, unsigned *dmax2,
+                cudaStream_t s) {
   if (n <= 0) return;
-  k_node_split<<<nblk((long long) n * 24, 256), 256, 0, s>>>(nodex, n, hl);
+  k_node_split<<<nblk((long long) n * NPE, SPLIT_BLOCK), SPLIT_BLOCK, 0, s>>>(nodex, n, hl, ref,
+                                                                           dmax2);
   check(cudaGetLastError(), "node_split");
 }
 
@@ -1379,21 +1508,56 @@ void line_mask(const int *flag, const int *etype, const int *site_base, const in
 }
 
 void site_q(const float2 *node_hl, const int *etype, const int *site_base, const Lattice &lat,
-            int max_nax, int max_naz, const unsigned long long *mask, int maxlines,
+            int max_nax, int max_naz, const unsigned long long *mask,
+            const unsigned long long *mask_near, const unsigned *eflags, int maxlines,
             const PackGrid &pg, int nelem, float4 *q, cudaStream_t s) {
   if (nelem <= 0) return;
   const size_t smem = sizeof(ds) * (12 * (size_t) max_nax + 6 * LCH + max_naz);
-  k_site_q<<<nelem, LCH, smem, s>>>(node_hl, etype, site_base, lat, mask, maxlines, pg, q);
+  k_site_q<<<nelem, LCH, smem, s>>>(node_hl, etype, site_base, lat, mask, mask_near, eflags,
+                                    maxlines, pg, q);
   check(cudaGetLastError(), "site_q");
 }
 
 void site_fp(const double *erho, const int *etype, const int *site_base, const Lattice &lat,
-             const unsigned long long *mask, int maxlines, const float4 *fp4, int nrho,
-             double rdrho, int nelem, float *fp, cudaStream_t s) {
+             const unsigned long long *mask, const unsigned long long *mask_near,
+             const unsigned *eflags, int maxlines, const float4 *fp4, int nrho, double rdrho,
+             int nelem, float *fp, cudaStream_t s) {
   if (nelem <= 0) return;
-  k_site_fp<<<nelem, LCH, 0, s>>>(erho, etype, site_base, lat, mask, maxlines, fp4, nrho,
-                                  (float) rdrho, fp);
+  k_site_fp<<<nelem, LCH, 0, s>>>(erho, etype, site_base, lat, mask, mask_near, eflags, maxlines,
+                                  fp4, nrho, (float) rdrho, fp);
   check(cudaGetLastError(), "site_fp");
+}
+
+void ip_reorder(const int *row_start, const int *ent, int nrows, const float4 *ip_q,
+                const float4 *site_q, float g, float cutoff, int *ent_near, int *nnear_row,
+                const float2 *node_hl, int nall_e, float2 *node_ref, unsigned *eflags,
+                cudaStream_t s) {
+  if (nrows <= 0) return;
+  const float rn = cutoff + CULL_DELTA;
+  const int grid = persistent_grid((const void *) k_ip_reorder, 256, 0, nrows);
+  k_ip_reorder<<<grid, 256, 0, s>>>(row_start, ent, nrows, ip_q, site_q, g, rn * rn, ent_near,
+                                    nnear_row, node_hl, (long long) nall_e * 24, node_ref, eflags);
+  check(cudaGetLastError(), "ip_reorder");
+}
+
+void near_masks(const int *row_start, const int *ent_near, const int *nnear_row, int nrows,
+                const unsigned char *isforce, const int *site_code, unsigned long long *mask,
+                unsigned long long *mask_f, long long nmask, const unsigned *eflags,
+                cudaStream_t s) {
+  if (nrows <= 0 || nmask <= 0) return;
+  const int g1 = persistent_grid((const void *) k_near_masks_clear, 256, 0, nmask);
+  k_near_masks_clear<<<g1, 256, 0, s>>>(mask, mask_f, nmask, eflags);
+  const int g2 = persistent_grid((const void *) k_near_masks_or, 256, 0, nrows);
+  k_near_masks_or<<<g2, 256, 0, s>>>(row_start, ent_near, nnear_row, nrows, isforce, site_code,
+                                     mask, mask_f, eflags);
+  check(cudaGetLastError(), "near_masks");
+}
+
+void site_code(const int *etype, const int *site_base, const int *nae, int maxlines, int nelem,
+               int *code, cudaStream_t s) {
+  if (nelem <= 0) return;
+  k_site_code<<<nelem, 128, 0, s>>>(etype, site_base, nae, maxlines, code);
+  check(cudaGetLastError(), "site_code");
 }
 
 void row_q(const int *row_elem, const int *row_jj, const int *etype, const int *int_off,
@@ -1443,7 +1607,8 @@ static void launch_ip(const ElemArgs &a, long long items, int block, int group,
 void ip_pass(const MixedElems &m, int pass, const float4 *tab, const EamTables &e, float lj1,
              float lj2, double *out, float2 *outf, cudaStream_t s) {
   ElemArgs a{m.site_q, m.site_fp, m.ip_q, m.ip_h, m.ip_l, m.row_fp, m.etype, m.row_elem,
-             m.row_first, m.node_list, m.row_start, m.ent, m.nlocal_e, m.rows, m.nforce,
+             m.row_first, m.node_list, m.row_start, m.ent, m.nnear_row, m.eflags, m.nlocal_e,
+             m.rows, m.nforce,
              m.cutsq_f, m.band_lo, m.band_hi, m.cutsq, m.node_hl, m.skip, m.site_base, m.lat,
              m.nall_e, m.pg};
   if (pass == 0)  // LJ forces

@@ -102,7 +102,9 @@ int cacg_put_nodes(cacg_handle h, const double *nodex, const double *nodev); /* 
    last force evaluation 16 elements handed to the surrogate 17 surrogate
    evaluations (element-steps) 18 of which accepted 19 steps replayed from a
    captured CUDA graph 20 atom-list entries the last mixed EAM density pass
-   scanned (fewer than 2 while displacement culling holds) */
+   scanned (fewer than 2 while displacement culling holds) 21 integration-point
+   list entries the last mixed element passes scanned per pass (fewer than 7
+   while culling holds) 22 reorders of the mixed integration-point lists so far */
 int cacg_get_counts(cacg_handle h, long long *counts, int n);
 /* Atom::x/v/f (atom.h:40); all != 0 includes ghosts for x and tag */
 int cacg_get_atoms(cacg_handle h, int all, double *x, double *v, double *f, int *tag);

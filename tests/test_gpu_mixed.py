@@ -62,25 +62,31 @@ def _run_cull(cacg, cfg, m, cull, steps):
             s.neighbor_nbuild()
             s.pair_ecompute()
         s.run(steps)
-        return s.atoms(), s.counts()
+        return s.atoms(), s.elements(), s.counts()
     finally:
         s.close()
 
 
+@pytest.mark.parametrize("case", ["eam_atoms", "eam_cac"])
 @pytest.mark.parametrize("vscale", [1.0, 5.0, 40.0])
-def test_displacement_culling_is_bit_identical(cacg_lib, vscale):
-    """The density pass skips list entries beyond r_c + 1 A at the list reorder
-    while no atom has moved 0.495 A since: the skipped entries are provably out
-    of range, so the trajectory equals the unculled one bit for bit, with
-    thermal motion (culling engaged throughout), faster atoms (lists reordered
-    again on the device between builds) and atoms fast enough to force
-    rebuilds."""
-    cfg, z = C.load_golden("eam_atoms")
+def test_displacement_culling_is_bit_identical(cacg_lib, case, vscale):
+    """The density pass skips atom-list entries beyond r_c + 1 A at the list
+    reorder, and both integration-point passes skip such entries of their rows
+    (their sites are not even computed), while no atom (node) has moved 0.495 A
+    since: the skipped entries are provably out of range, so the trajectory
+    equals the unculled one bit for bit, with thermal motion (culling engaged
+    throughout), faster motion (lists reordered again on the device between
+    builds) and motion fast enough to force rebuilds."""
+    cfg, z = C.load_golden(case)
     cfg = dict(cfg, every=10, check=True)
     m = C.model_from_arrays(z)
     m.atom_v = m.atom_v * vscale
-    a0, c0 = _run_cull(cacg_lib, cfg, m, "no", 40)
-    a1, c1 = _run_cull(cacg_lib, cfg, m, "yes", 40)
+    if m.nelements:
+        m.nodev = m.nodev * vscale
+    a0, e0, c0 = _run_cull(cacg_lib, cfg, m, "no", 40)
+    a1, e1, c1 = _run_cull(cacg_lib, cfg, m, "yes", 40)
     assert c0["rebuilds"] == c1["rebuilds"]
     for k in ("x", "v", "f"):
         assert np.array_equal(a0[k], a1[k]), k
+    for k in ("nodex", "nodev", "nodef"):
+        assert np.array_equal(e0[k], e1[k]), k
