@@ -1552,14 +1552,13 @@ void cacg_context::mixed_tables() {
     upload(d_ljf, lf, stream);
     upload(d_cutsq64, c64, stream);
   } else if (pair_style == 2) {
-    std::vector<float4> val(nr + 1), ft(3 * (size_t) (nr + 1));
+    std::vector<float4> val(nr + 1), ft(mixed::FTAB_W * (size_t) (nr + 1));
     for (int m = 0; m <= nr; m++) {
       const double *c = &rhor_sp[(size_t) m * 7];
       const double *z = &z2r_sp[(size_t) m * 7];
       val[m] = make_float4((float) c[3], (float) c[4], (float) c[5], (float) c[6]);
-      ft[3 * m] = make_float4((float) c[0], (float) c[1], (float) c[2], (float) z[0]);
-      ft[3 * m + 1] = make_float4((float) z[1], (float) z[2], (float) z[3], (float) z[4]);
-      ft[3 * m + 2] = make_float4((float) z[5], (float) z[6], 0.f, 0.f);
+      ft[2 * m] = make_float4((float) c[0], (float) c[1], (float) c[2], (float) z[3]);
+      ft[2 * m + 1] = make_float4((float) z[4], (float) z[5], (float) z[6], 0.f);
     }
     std::vector<float4> f4(nrho + 1);
     for (int m = 0; m <= nrho; m++) {

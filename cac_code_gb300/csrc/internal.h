@@ -266,6 +266,9 @@ struct MixedAtoms {
 // r_c + CULL_DELTA at the last reorder are skipped while twice the largest
 // displacement since then, plus CULL_MARGIN, stays within CULL_DELTA (A).
 constexpr float CULL_DELTA = 1.0f, CULL_MARGIN = 0.01f;
+// float4 per knot of the FP32 EAM force table: (rho c0, c1, c2, r*phi c3),
+// (r*phi c4, c5, c6, 0)
+constexpr int FTAB_W = 2;
 
 // The packing grid of the cell-relative coordinates: cells of a power-of-two
 // size g from the corner l0 (split into double-single floats); *oob counts

@@ -40,6 +40,18 @@ __device__ __forceinline__ int findex(float r, float rdr, int nr, float &p) {
   return m;
 }
 
+// The force spline per knot, 2 float4 (FTAB_W): rho'(r) c0..c2 | r*phi c3,
+// then r*phi c4..c6.  The derivative of r*phi comes from its value
+// coefficients, as array2spline forms it (c0 = 3 c3 / dr, c1 = 2 c4 / dr,
+// c2 = c5 / dr, pair_eam.cpp:565-571): one 16-byte shared load less per pair.
+__device__ __forceinline__ void force_spline(const float4 *__restrict__ tab, int m, float p,
+                                             float rdr, float &rhoip, float &z2, float &z2p) {
+  const float4 t0 = tab[FTAB_W * m], t1 = tab[FTAB_W * m + 1];
+  rhoip = (t0.x * p + t0.y) * p + t0.z;
+  z2 = ((t0.w * p + t1.x) * p + t1.y) * p + t1.z;
+  z2p = ((3.0f * t0.w * p + 2.0f * t1.x) * p + t1.y) * rdr;
+}
+
 __device__ __forceinline__ double fprime64(double rho, const double *__restrict__ frho,
                                            int nrho, double rdrho) {
   double p = rho * rdrho + 1.0;
@@ -403,9 +415,9 @@ k_eam_force_union(AtomArgs a, UnionArgs u, const float4 *__restrict__ ftab, int 
                   const float *__restrict__ fp, double *__restrict__ f) {
   extern __shared__ float4 sm[];
   float4 *s_tab = sm;  // 3 float4 per knot
-  float4 *sx = sm + 3 * (nr + 1) + (threadIdx.x >> 5) * UMAX;
-  float *sfp = reinterpret_cast<float *>(sm + 3 * (nr + 1) + UWARPS * UMAX) + (threadIdx.x >> 5) * UMAX;
-  for (int m = threadIdx.x; m < 3 * (nr + 1); m += blockDim.x) s_tab[m] = ftab[m];
+  float4 *sx = sm + FTAB_W * (nr + 1) + (threadIdx.x >> 5) * UMAX;
+  float *sfp = reinterpret_cast<float *>(sm + FTAB_W * (nr + 1) + UWARPS * UMAX) + (threadIdx.x >> 5) * UMAX;
+  for (int m = threadIdx.x; m < FTAB_W * (nr + 1); m += blockDim.x) s_tab[m] = ftab[m];
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int ngroups = (a.nlocal + UGROUP - 1) / UGROUP;
@@ -454,10 +466,8 @@ k_eam_force_union(AtomArgs a, UnionArgs u, const float4 *__restrict__ ftab, int 
           float r = rsq * recip;
           float p;
           int m = findex(r, rdr, nr, p);
-          float4 t0 = s_tab[3 * m], t1 = s_tab[3 * m + 1], t2 = s_tab[3 * m + 2];
-          float rhoip = (t0.x * p + t0.y) * p + t0.z;
-          float z2p = (t0.w * p + t1.x) * p + t1.y;
-          float z2 = ((t1.z * p + t1.w) * p + t2.x) * p + t2.y;
+          float rhoip, z2, z2p;
+          force_spline(s_tab, m, p, rdr, rhoip, z2, z2p);
           float phi = z2 * recip;
           float phip = z2p * recip - phi * recip;
           float psip = (fpi + fpj) * rhoip + phip;
@@ -484,12 +494,12 @@ k_eam_force_union(AtomArgs a, UnionArgs u, const float4 *__restrict__ ftab, int 
   }
 }
 
-// force table per knot: rho'(r) c0..c2 (x,y,z of f0), r*phi c0..c6 (w of f0, f1, f2.xy)
+// force table per knot: FTAB_W float4 (force_spline)
 __global__ void __launch_bounds__(512, 2)
 k_eam_force_atoms(AtomArgs a, const float4 *__restrict__ ftab, int nr, float rdr,
                   const float *__restrict__ fp, double *__restrict__ f) {
   extern __shared__ float4 s_tab[];  // 3 float4 per knot
-  for (int m = threadIdx.x; m < 3 * (nr + 1); m += blockDim.x) s_tab[m] = ftab[m];
+  for (int m = threadIdx.x; m < FTAB_W * (nr + 1); m += blockDim.x) s_tab[m] = ftab[m];
   __syncthreads();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.nlocal; i += gridDim.x * blockDim.x) {
     const float4 qi = a.xq[i];
@@ -527,10 +537,8 @@ k_eam_force_atoms(AtomArgs a, const float4 *__restrict__ ftab, int nr, float rdr
         float r = rsq * recip;
         float p;
         int m = findex(r, rdr, nr, p);
-        float4 t0 = s_tab[3 * m], t1 = s_tab[3 * m + 1], t2 = s_tab[3 * m + 2];
-        float rhoip = (t0.x * p + t0.y) * p + t0.z;
-        float z2p = (t0.w * p + t1.x) * p + t1.y;
-        float z2 = ((t1.z * p + t1.w) * p + t2.x) * p + t2.y;
+        float rhoip, z2, z2p;
+        force_spline(s_tab, m, p, rdr, rhoip, z2, z2p);
         float phi = z2 * recip;
         float phip = z2p * recip - phi * recip;
         float psip = (fpi + fpj) * rhoip + phip;
@@ -1197,7 +1205,7 @@ __global__ void __launch_bounds__(512, 2)
 k_ipg(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr, float lj1, float lj2,
       double *__restrict__ out, float2 *__restrict__ outf) {
   extern __shared__ float4 s_tab[];
-  const int ntab = EAM ? (DENSITY ? (nr + 1) : 3 * (nr + 1)) : 0;
+  const int ntab = EAM ? (DENSITY ? (nr + 1) : FTAB_W * (nr + 1)) : 0;
   for (int m = threadIdx.x; m < ntab; m += blockDim.x) s_tab[m] = tab[m];
   __syncthreads();
   const float g = a.pg.g;
@@ -1267,10 +1275,8 @@ k_ipg(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr, float lj1, 
             const float4 c = s_tab[m];
             part += ((c.x * p + c.y) * p + c.z) * p + c.w;
           } else {
-            const float4 t0 = s_tab[3 * m], t1 = s_tab[3 * m + 1], t2 = s_tab[3 * m + 2];
-            const float rhoip = (t0.x * p + t0.y) * p + t0.z;
-            const float z2p = (t0.w * p + t1.x) * p + t1.y;
-            const float z2 = ((t1.z * p + t1.w) * p + t2.x) * p + t2.y;
+            float rhoip, z2, z2p;
+            force_spline(s_tab, m, p, rdr, rhoip, z2, z2p);
             const float phi = z2 * recip;
             const float phip = z2p * recip - phi * recip;
             const float psip = (fpi + fpj) * rhoip + phip;
@@ -1456,7 +1462,7 @@ void eam_force_union(const MixedAtoms &m, const int *union_j, const int *union_n
   AtomArgs a{m.x, m.xq, m.qg, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
              m.band_hi, m.cutsq, m.snum, m.slist, nullptr, nullptr};
   UnionArgs u{union_j, union_n, nullptr, const_cast<unsigned short *>(sslot)};
-  size_t smem = sizeof(float4) * (3 * (size_t) (e.nr + 1) + (size_t) UWARPS * UMAX) +
+  size_t smem = sizeof(float4) * (FTAB_W * (size_t) (e.nr + 1) + (size_t) UWARPS * UMAX) +
                 sizeof(float) * (size_t) UWARPS * UMAX;
   int g = union_grid((const void *) k_eam_force_union, smem, m.nlocal);
   k_eam_force_union<<<g, UGROUP * UWARPS, smem, s>>>(a, u, ftab, e.nr, (float) e.rdr, fp, f);
@@ -1468,7 +1474,7 @@ void eam_force_atoms(const MixedAtoms &m, const float4 *ftab, const EamTables &e
   if (m.nlocal <= 0) return;
   AtomArgs a{m.x, m.xq, m.qg, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
              m.band_hi, m.cutsq, m.snum, m.slist, nullptr, nullptr};
-  size_t smem = sizeof(float4) * 3 * (e.nr + 1);
+  size_t smem = sizeof(float4) * FTAB_W * (e.nr + 1);
   int g = persistent_grid((const void *) k_eam_force_atoms, m.block, smem, m.nlocal);
   k_eam_force_atoms<<<g, m.block, smem, s>>>(a, ftab, e.nr, (float) e.rdr, fp, f);
   check(cudaGetLastError(), "eam_force_atoms_mixed");
@@ -1589,7 +1595,7 @@ template <bool EAM, bool DENSITY, int G>
 static void launch_ipg(const ElemArgs &a, long long items, int block, const float4 *tab,
                        const EamTables &e, float lj1, float lj2, double *out, float2 *outf,
                        cudaStream_t s) {
-  const size_t smem = EAM ? sizeof(float4) * (DENSITY ? 1 : 3) * (e.nr + 1) : 0;
+  const size_t smem = EAM ? sizeof(float4) * (DENSITY ? 1 : FTAB_W) * (e.nr + 1) : 0;
   const int g = persistent_grid((const void *) k_ipg<EAM, DENSITY, G>, block, smem, items * G);
   k_ipg<EAM, DENSITY, G><<<g, block, smem, s>>>(a, tab, e.nr, (float) e.rdr, lj1, lj2, out, outf);
 }
