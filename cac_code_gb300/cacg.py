@@ -456,8 +456,14 @@ class System:
         self._ok(self._L.cacg_put_nodes(self.h, _d(nodex), _d(nodev)))
 
     def get_state_into(self, x, v, f):
-        """Read owned-atom x, v, f into caller-provided float64 [nlocal][3] buffers."""
+        """Read owned-atom x, v, f into caller-provided float64 [nlocal][3] buffers
+        (any of them None: not read)."""
         self._ok(self._L.cacg_get_atoms(self.h, 0, _d(x), _d(v), _d(f), None))
+
+    def get_nodes_into(self, nodex, nodev):
+        """Read owned-element node x, v into caller-provided float64
+        [enlocal][8][3] buffers (either None: not read)."""
+        self._ok(self._L.cacg_get_elements(self.h, 0, None, _d(nodex), _d(nodev), None, None))
 
     def fp64_peak(self) -> float:
         v = ctypes.c_double()
