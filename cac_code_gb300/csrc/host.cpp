@@ -217,7 +217,8 @@ struct cacg_context {
   // first, their count, the nodes at the reorder, near-site masks, the line
   // code of every site, force-row flags; reordered once per element list build
   // and whenever a node has moved 0.495 A since
-  DBuf<int> d_ent_near, d_nnear_row, d_site_code;
+  DBuf<int> d_ent_near, d_site_code;
+  DBuf<int4> d_nnear_row;
   DBuf<float2> d_node_ref;
   DBuf<unsigned long long> d_line_mask_n, d_line_mask_nf;
   DBuf<unsigned char> d_row_isforce;
@@ -318,7 +319,8 @@ struct cacg_context {
   // the atom lists reordered for the mixed EAM passes (in-range entries
   // first), once per list build
   long long part_of = -1;
-  DBuf<int> d_mlist, d_nnear;
+  DBuf<int> d_mlist;
+  DBuf<int4> d_nnear;
   // packed coordinates at the reorder and their grid: the density pass skips
   // the far part of each list while no atom has moved 0.495 A since then
   DBuf<float4> d_xq_ref;
@@ -3332,14 +3334,15 @@ int cacg_get_counts(cacg_handle h, long long *c, int n) {
       h->part_of == h->list_builds && h->nlocal && h->d_nnear.p && h->d_misc.p) {
     unsigned dm[2] = {0, 0};
     check(cudaMemcpyAsync(dm, h->d_misc.p + 11, sizeof(dm), cudaMemcpyDeviceToHost, h->stream), "dmax");
-    std::vector<int> nn(h->nlocal);
-    check(cudaMemcpyAsync(nn.data(), h->d_nnear.p, sizeof(int) * h->nlocal, cudaMemcpyDeviceToHost, h->stream), "nnear");
+    std::vector<int4> nn(h->nlocal);
+    check(cudaMemcpyAsync(nn.data(), h->d_nnear.p, sizeof(int4) * h->nlocal, cudaMemcpyDeviceToHost, h->stream), "nnear");
     h->sync();
     float d2;
     std::memcpy(&d2, &dm[0], sizeof(float));
-    if (dm[1] != 0u || 2.0f * std::sqrt(d2) + mixed::CULL_MARGIN <= mixed::CULL_DELTA) {
+    const int level = mixed::cull_level_host(d2, dm[1]);
+    if (level < 4) {
       v[20] = 0;
-      for (int x : nn) v[20] += x;
+      for (const int4 &x : nn) v[20] += level == 1 ? x.x : level == 2 ? x.y : x.z;
     }
   }
   // integration-point entries the last mixed passes scanned (near parts while
@@ -3353,12 +3356,13 @@ int cacg_get_counts(cacg_handle h, long long *c, int n) {
     v[22] = dm[2];
     float d2;
     std::memcpy(&d2, &dm[0], sizeof(float));
-    if (h->mixed_cull && (dm[1] != 0u || 2.0f * std::sqrt(d2) + mixed::CULL_MARGIN <= mixed::CULL_DELTA)) {
-      std::vector<int> nn(h->nrows);
-      check(cudaMemcpyAsync(nn.data(), h->d_nnear_row.p, sizeof(int) * h->nrows, cudaMemcpyDeviceToHost, h->stream), "nnear_row");
+    const int level = mixed::cull_level_host(d2, dm[1]);
+    if (h->mixed_cull && level < 4) {
+      std::vector<int4> nn(h->nrows);
+      check(cudaMemcpyAsync(nn.data(), h->d_nnear_row.p, sizeof(int4) * h->nrows, cudaMemcpyDeviceToHost, h->stream), "nnear_row");
       h->sync();
       v[21] = 0;
-      for (int x : nn) v[21] += x;
+      for (const int4 &x : nn) v[21] += level == 1 ? x.x : level == 2 ? x.y : x.z;
     }
   }
   for (int i = 0; i < n && i < 23; i++) c[i] = v[i];

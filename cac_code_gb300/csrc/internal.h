@@ -258,14 +258,23 @@ struct MixedAtoms {
   // EAM density pass over a reordered list: nnear[i] entries lie within the
   // cutoff + 1 A at the reorder; dmax2 = the largest squared displacement
   // since (float bits); null: every entry is scanned
-  const int *nnear = nullptr;
+  const int4 *nnear = nullptr;
   const unsigned *dmax2 = nullptr;
   int block = 512;    // threads per block of the persistent grids (autotuned)
 };
-// Displacement culling of the mixed EAM density pass: list entries beyond
-// r_c + CULL_DELTA at the last reorder are skipped while twice the largest
-// displacement since then, plus CULL_MARGIN, stays within CULL_DELTA (A).
-constexpr float CULL_DELTA = 1.0f, CULL_MARGIN = 0.01f;
+// Displacement culling of the mixed passes: list entries beyond r_c + d at
+// the last reorder are skipped while twice the largest displacement since
+// then, plus CULL_MARGIN, stays within d, for the levels d = CULL_D1, CULL_D2,
+// CULL_DELTA (A); beyond CULL_DELTA the lists are reordered.
+constexpr float CULL_D1 = 0.25f, CULL_D2 = 0.5f, CULL_DELTA = 1.0f, CULL_MARGIN = 0.01f;
+
+// the culling level the device kernels choose (1..3; 4: no culling), from
+// the squared displacement and the reordered-this-step flag
+inline int cull_level_host(float d2, unsigned reordered) {
+  if (reordered) return 1;
+  const float d = 2.0f * __builtin_sqrtf(d2) + CULL_MARGIN;
+  return d <= CULL_D1 ? 1 : d <= CULL_D2 ? 2 : d <= CULL_DELTA ? 3 : 4;
+}
 // float4 per knot of the FP32 EAM force table: (rho c0, c1, c2, r*phi c3),
 // (r*phi c4, c5, c6, 0)
 constexpr int FTAB_W = 2;
@@ -295,7 +304,7 @@ struct MixedElems {
   const int *row_start, *ent;  // integration-point lists, row-major
   // displacement culling: ent holds each row's near entries first, nnear_row
   // counts them; eflags = [node displacement^2 bits, reordered this step]
-  const int *nnear_row = nullptr;
+  const int4 *nnear_row = nullptr;
   const unsigned *eflags = nullptr;
   int nlocal_e;
   const int *rows;  // rows of nonzero weight (force passes), count nforce
@@ -344,10 +353,10 @@ void site_fp(const double *erho, const int *etype, const int *site_base, const L
 // nodes as the reference (eflags[1] = 1, eflags[2] counts reorders); rebuild
 // the near-site masks after a reorder
 void ip_reorder(const int *row_start, const int *ent, int nrows, const float4 *ip_q,
-                const float4 *site_q, float g, float cutoff, int *ent_near, int *nnear_row,
+                const float4 *site_q, float g, float cutoff, int *ent_near, int4 *nnear_row,
                 const float2 *node_hl, int nall_e, float2 *node_ref, unsigned *eflags,
                 cudaStream_t s);
-void near_masks(const int *row_start, const int *ent_near, const int *nnear_row, int nrows,
+void near_masks(const int *row_start, const int *ent_near, const int4 *nnear_row, int nrows,
                 const unsigned char *isforce, const int *site_code, unsigned long long *mask,
                 unsigned long long *mask_f, long long nmask, const unsigned *eflags,
                 cudaStream_t s);
@@ -359,7 +368,7 @@ void site_code(const int *etype, const int *site_base, const int *nae, int maxli
 // when the displacement since the last reorder (dmax2[0], against ref) no
 // longer allows culling; it then sets ref to the positions and dmax2[1] = 1
 void list_partition(const float4 *xq, float g, const int *num, const int *list, int stride,
-                    int nlocal, float cut_rsq, float cutoff, int *out, int *nnear, float4 *ref,
+                    int nlocal, float cut_rsq, float cutoff, int *out, int4 *nnear, float4 *ref,
                     unsigned *dmax2, cudaStream_t s);
 // neighbor unions of 32-atom groups staged in shared memory (EAM atom passes)
 int union_max();

@@ -144,11 +144,11 @@ struct AtomArgs {
   double cutsq;
   int *snum, *slist;  // short list written by the density pass, read by the force pass
   // displacement culling of the density pass (null: every entry is scanned):
-  // nnear[i] leading entries of the reordered list lie within r_c + CULL_DELTA
-  // at the reorder; the rest may be skipped while twice the largest
-  // displacement since then (dmax2: its square, float bits) stays below
-  // CULL_DELTA - CULL_MARGIN
-  const int *nnear;
+  // nnear[i].x/.y/.z leading entries of the reordered list lay within
+  // r_c + CULL_D1/D2/DELTA at the reorder; the entries beyond the level that
+  // twice the largest displacement since then (dmax2: its square, float bits)
+  // plus CULL_MARGIN reaches are skipped
+  const int4 *nnear;
   const unsigned *dmax2;  // [0]: squared displacement bits; [1]: reordered in this step
 };
 
@@ -160,6 +160,41 @@ __device__ __forceinline__ bool cull_ok(const unsigned *dmax2) {
   return dmax2[1] != 0u || moved_little(dmax2);
 }
 
+// the culling level of this step: 1..3 (nnear .x/.y/.z), 4 = no culling
+__device__ __forceinline__ int cull_level(const unsigned *dmax2) {
+  if (dmax2[1] != 0u) return 1;  // reordered from this step's positions
+  const float d = 2.0f * sqrtf(__uint_as_float(dmax2[0])) + CULL_MARGIN;
+  return d <= CULL_D1 ? 1 : d <= CULL_D2 ? 2 : d <= CULL_DELTA ? 3 : 4;
+}
+
+__device__ __forceinline__ int culled_count(int level, const int4 &nn, int nfull) {
+  return level == 1 ? nn.x : level == 2 ? nn.y : level == 3 ? nn.z : nfull;
+}
+
+// the part of an entry at squared distance rsq: 0 within the cutoff, 1..3
+// within r_c + CULL_D1/D2/DELTA, 4 beyond
+__device__ __forceinline__ int cull_part(float rsq, const float4 &lim) {
+  return rsq <= lim.x ? 0 : rsq <= lim.y ? 1 : rsq <= lim.z ? 2 : rsq <= lim.w ? 3 : 4;
+}
+
+// Reorder of one list in two sweeps (count the parts, then place each entry at
+// its part's cursor), each part in list order.  get(k) -> (entry, rsq).
+template <class Get, class Put>
+__device__ __forceinline__ int4 reorder_parts(int n, const float4 &lim, Get get, Put put) {
+  int c[4] = {0, 0, 0, 0};
+  for (int k = 0; k < n; k++) {
+    const int p = cull_part(get(k).y, lim);
+    if (p < 4) c[p]++;
+  }
+  int m[5] = {0, c[0], c[0] + c[1], c[0] + c[1] + c[2], c[0] + c[1] + c[2] + c[3]};
+  const int4 nn = make_int4(m[2], m[3], m[4], n);
+  for (int k = 0; k < n; k++) {
+    const float2 e = get(k);
+    put(m[cull_part(e.y, lim)]++, __float_as_int(e.x));
+  }
+  return nn;
+}
+
 
 // 40 registers at three 512-thread blocks per SM (48 warps): more gathers in flight
 __global__ void __launch_bounds__(512, 3)
@@ -169,12 +204,12 @@ k_eam_rho_atoms(AtomArgs a, const float4 *__restrict__ rhor_val, int nr, float r
   extern __shared__ float4 s_val[];
   for (int m = threadIdx.x; m <= nr; m += blockDim.x) s_val[m] = rhor_val[m];
   __syncthreads();
-  const bool cull = a.nnear && cull_ok(a.dmax2);
+  const int level = a.nnear ? cull_level(a.dmax2) : 4;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.nlocal; i += gridDim.x * blockDim.x) {
     const float4 qi = a.xq[i];
     float cx, cy, cz;
     cell_of(qi, cx, cy, cz);
-    const int n = cull ? a.nnear[i] : a.num[i];
+    const int n = level < 4 ? culled_count(level, a.nnear[i], 0) : a.num[i];
     dsacc acc;
     float part = 0.f;
     int ns = 0, cnt = 0;
@@ -219,20 +254,20 @@ k_eam_rho_atoms(AtomArgs a, const float4 *__restrict__ rhor_val, int nr, float r
   }
 }
 
-// The list of each atom reordered, in three parts, each in list order: the
-// entries within the cutoff (at the positions of the reorder), those within
-// r_c + CULL_DELTA, the rest; nnear[i] counts the first two parts.  Atoms move
+// The list of each atom reordered in five parts, each in list order: the
+// entries within the cutoff (at the positions of the reorder), within
+// r_c + CULL_D1, r_c + CULL_D2, r_c + CULL_DELTA, and the rest; nnear[i]
+// counts the entries through the second, third and fourth parts.  Atoms move
 // little, so in the density pass the lanes of a warp meet the in-range entries
-// together and the out-of-range ones together, and the third part is skipped
-// while no atom has moved (CULL_DELTA - CULL_MARGIN) / 2 since the reorder.
-// Launched every step: it returns at once while that holds, else it reorders
-// from the current positions, keeps them as the new reference and flags the
-// step (dmax2[1]) so that the density pass culls against the new order.
+// together and the out-of-range ones together, and the farther parts are
+// skipped while no atom has moved far enough to reach them.  Launched every
+// step: it returns at once while no atom has moved (CULL_DELTA - CULL_MARGIN)
+// / 2 since the last reorder, else it reorders from the current positions,
+// keeps them as the new reference and flags the step (dmax2[1]).
 __global__ void k_list_partition(const float4 *__restrict__ xq, float g, const int *__restrict__ num,
-                                 const int *__restrict__ list, int stride, int nlocal,
-                                 float cut_rsq, float near_rsq, int *__restrict__ out,
-                                 int *__restrict__ nnear, float4 *__restrict__ ref,
-                                 unsigned *__restrict__ dmax2) {
+                                 const int *__restrict__ list, int stride, int nlocal, float4 lim,
+                                 int *__restrict__ out, int4 *__restrict__ nnear,
+                                 float4 *__restrict__ ref, unsigned *__restrict__ dmax2) {
   // (the gate reads only dmax2[0], which no block of this kernel writes)
   if (moved_little(dmax2)) return;
   if (blockIdx.x == 0 && threadIdx.x == 0) dmax2[1] = 1u;
@@ -241,27 +276,14 @@ __global__ void k_list_partition(const float4 *__restrict__ xq, float g, const i
     ref[i] = qi;
     float cx, cy, cz;
     cell_of(qi, cx, cy, cz);
-    const int n = num[i];
-    // two sweeps: count the parts, then place every entry at its part's cursor
-    int c0 = 0, c1 = 0;
-    for (int sweep = 0; sweep < 2; sweep++) {
-      int m0 = 0, m1 = c0, m2 = c0 + c1;
-      for (int k = 0; k < n; k++) {
-        const int j = __ldg(list + (size_t) k * stride + i);
-        float dx, dy, dz;
-        rel_vec(qi, cx, cy, cz, __ldg(xq + j), g, dx, dy, dz);
-        const float rsq = dx * dx + dy * dy + dz * dz;
-        const int p = rsq <= cut_rsq ? 0 : (rsq <= near_rsq ? 1 : 2);
-        if (sweep == 0) {
-          c0 += p == 0;
-          c1 += p == 1;
-        } else {
-          const int at = p == 0 ? m0++ : (p == 1 ? m1++ : m2++);
-          out[(size_t) at * stride + i] = j;
-        }
-      }
-    }
-    nnear[i] = c0 + c1;
+    auto get = [&](int k) {
+      const int j = __ldg(list + (size_t) k * stride + i);
+      float dx, dy, dz;
+      rel_vec(qi, cx, cy, cz, __ldg(xq + j), g, dx, dy, dz);
+      return make_float2(__int_as_float(j), dx * dx + dy * dy + dz * dz);
+    };
+    auto put = [&](int at, int j) { out[(size_t) at * stride + i] = j; };
+    nnear[i] = reorder_parts(num[i], lim, get, put);
   }
 }
 
@@ -998,7 +1020,7 @@ struct ElemArgs {
   const float *row_fp;        // F'(rho) at the rows of nonzero weight (EAM force pass)
   const int *etype, *row_elem, *row_first, *node_list;
   const int *row_start, *ent;  // integration-point lists, row-major (near entries first)
-  const int *nnear_row;        // near entries per row (null: no culling)
+  const int4 *nnear_row;       // culled entry counts per row (null: no culling)
   const unsigned *eflags;      // [0] node displacement^2 since the reorder, [1] reordered now
   int nlocal_e;
   const int *rows;
@@ -1091,8 +1113,8 @@ __global__ void k_ip_csr(const int *__restrict__ ipnum, const int *__restrict__ 
 // step) and flags the step (eflags[1]).
 __global__ void k_ip_reorder(const int *__restrict__ row_start, const int *__restrict__ ent,
                              int nrows, const float4 *__restrict__ ip_q,
-                             const float4 *__restrict__ site_q, float g, float near_rsq,
-                             int *__restrict__ ent_near, int *__restrict__ nnear_row,
+                             const float4 *__restrict__ site_q, float g, float4 lim,
+                             int *__restrict__ ent_near, int4 *__restrict__ nnear_row,
                              const float2 *__restrict__ node_hl, long long nvals,
                              float2 *__restrict__ node_ref, unsigned *__restrict__ eflags) {
   if (moved_little(eflags)) return;  // reads eflags[0] only, which no block writes
@@ -1105,20 +1127,15 @@ __global__ void k_ip_reorder(const int *__restrict__ row_start, const int *__res
     const float4 qi = ip_q[r];
     float cx, cy, cz;
     cell_of(qi, cx, cy, cz);
-    const int s0 = row_start[r], n = row_start[r + 1] - s0;
-    int c = 0;
-    for (int sweep = 0; sweep < 2; sweep++) {
-      int m0 = 0, m1 = c;
-      for (int k = 0; k < n; k++) {
-        const int sid = __ldg(ent + s0 + k);
-        float dx, dy, dz;
-        rel_vec(qi, cx, cy, cz, __ldg(site_q + sid), g, dx, dy, dz);
-        const bool near = dx * dx + dy * dy + dz * dz <= near_rsq;
-        if (sweep == 0) c += near;
-        else ent_near[s0 + (near ? m0++ : m1++)] = sid;
-      }
-    }
-    nnear_row[r] = c;
+    const int s0 = row_start[r];
+    auto get = [&](int k) {
+      const int sid = __ldg(ent + s0 + k);
+      float dx, dy, dz;
+      rel_vec(qi, cx, cy, cz, __ldg(site_q + sid), g, dx, dy, dz);
+      return make_float2(__int_as_float(sid), dx * dx + dy * dy + dz * dz);
+    };
+    auto put = [&](int at, int sid) { ent_near[s0 + at] = sid; };
+    nnear_row[r] = reorder_parts(row_start[r + 1] - s0, lim, get, put);
   }
   for (long long t = blockIdx.x * blockDim.x + threadIdx.x; t < nvals; t += stride)
     node_ref[t] = node_hl[t];
@@ -1138,7 +1155,7 @@ __global__ void k_near_masks_clear(unsigned long long *__restrict__ mask,
 }
 
 __global__ void k_near_masks_or(const int *__restrict__ row_start, const int *__restrict__ ent_near,
-                                const int *__restrict__ nnear_row, int nrows,
+                                const int4 *__restrict__ nnear_row, int nrows,
                                 const unsigned char *__restrict__ isforce,
                                 const int *__restrict__ site_code,
                                 unsigned long long *__restrict__ mask,
@@ -1147,7 +1164,7 @@ __global__ void k_near_masks_or(const int *__restrict__ row_start, const int *__
   if (eflags[1] == 0u) return;
   const int stride = gridDim.x * blockDim.x;
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += stride) {
-    const int s0 = row_start[r], n = nnear_row[r];
+    const int s0 = row_start[r], n = nnear_row[r].z;  // every entry of the culled parts
     const bool f = isforce[r] != 0;
     for (int k = 0; k < n; k++) {
       const int code = __ldg(site_code + __ldg(ent_near + s0 + k));
@@ -1214,7 +1231,7 @@ k_ipg(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr, float lj1, 
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int nitems = DENSITY ? a.nlocal_e * NPE : a.nforce;
-  const bool cull = a.nnear_row && cull_ok(a.eflags);
+  const int level = a.nnear_row ? cull_level(a.eflags) : 4;
   // warp-uniform trip count: every lane reaches the shuffles
   for (int wb = warp * GPW; wb < nitems; wb += nwarps * GPW) {
     const int it = wb + gsub;
@@ -1235,7 +1252,7 @@ k_ipg(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr, float lj1, 
     float fpi = 0.f;
     if (live) {
       s0 = a.row_start[r];
-      n = cull ? a.nnear_row[r] : a.row_start[r + 1] - s0;
+      n = level < 4 ? culled_count(level, a.nnear_row[r], 0) : a.row_start[r + 1] - s0;
       qi = __ldg(a.ip_q + r);
       if (EAM && !DENSITY) fpi = __ldg(a.row_fp + r);
     }
@@ -1413,14 +1430,18 @@ void eam_rho_atoms(const MixedAtoms &m, const float4 *rhor_val, const EamTables 
   check(cudaGetLastError(), "eam_rho_atoms_mixed");
 }
 
+static float4 part_limits(float cut_rsq, float cutoff) {
+  const float r1 = cutoff + CULL_D1, r2 = cutoff + CULL_D2, r3 = cutoff + CULL_DELTA;
+  return make_float4(cut_rsq, r1 * r1, r2 * r2, r3 * r3);
+}
+
 void list_partition(const float4 *xq, float g, const int *num, const int *list, int stride,
-                    int nlocal, float cut_rsq, float cutoff, int *out, int *nnear, float4 *ref,
+                    int nlocal, float cut_rsq, float cutoff, int *out, int4 *nnear, float4 *ref,
                     unsigned *dmax2, cudaStream_t s) {
   if (nlocal <= 0) return;
-  const float rn = cutoff + CULL_DELTA;
   const int grid = persistent_grid((const void *) k_list_partition, 256, 0, nlocal);
-  k_list_partition<<<grid, 256, 0, s>>>(xq, g, num, list, stride, nlocal, cut_rsq, rn * rn, out,
-                                        nnear, ref, dmax2);
+  k_list_partition<<<grid, 256, 0, s>>>(xq, g, num, list, stride, nlocal,
+                                        part_limits(cut_rsq, cutoff), out, nnear, ref, dmax2);
   check(cudaGetLastError(), "list_partition");
 }
 
@@ -1535,18 +1556,18 @@ void site_fp(const double *erho, const int *etype, const int *site_base, const L
 }
 
 void ip_reorder(const int *row_start, const int *ent, int nrows, const float4 *ip_q,
-                const float4 *site_q, float g, float cutoff, int *ent_near, int *nnear_row,
+                const float4 *site_q, float g, float cutoff, int *ent_near, int4 *nnear_row,
                 const float2 *node_hl, int nall_e, float2 *node_ref, unsigned *eflags,
                 cudaStream_t s) {
   if (nrows <= 0) return;
-  const float rn = cutoff + CULL_DELTA;
   const int grid = persistent_grid((const void *) k_ip_reorder, 256, 0, nrows);
-  k_ip_reorder<<<grid, 256, 0, s>>>(row_start, ent, nrows, ip_q, site_q, g, rn * rn, ent_near,
-                                    nnear_row, node_hl, (long long) nall_e * 24, node_ref, eflags);
+  k_ip_reorder<<<grid, 256, 0, s>>>(row_start, ent, nrows, ip_q, site_q, g,
+                                    part_limits(cutoff * cutoff, cutoff), ent_near, nnear_row,
+                                    node_hl, (long long) nall_e * 24, node_ref, eflags);
   check(cudaGetLastError(), "ip_reorder");
 }
 
-void near_masks(const int *row_start, const int *ent_near, const int *nnear_row, int nrows,
+void near_masks(const int *row_start, const int *ent_near, const int4 *nnear_row, int nrows,
                 const unsigned char *isforce, const int *site_code, unsigned long long *mask,
                 unsigned long long *mask_f, long long nmask, const unsigned *eflags,
                 cudaStream_t s) {
