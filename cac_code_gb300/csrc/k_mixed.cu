@@ -177,24 +177,46 @@ __device__ __forceinline__ int cull_part(float rsq, const float4 &lim) {
   return rsq <= lim.x ? 0 : rsq <= lim.y ? 1 : rsq <= lim.z ? 2 : rsq <= lim.w ? 3 : 4;
 }
 
-// Reorder of one list in two sweeps (count the parts, then place each entry at
-// its part's cursor), each part in list order.  get(k) -> (entry, rsq).
-template <class Get, class Put>
-__device__ __forceinline__ int4 reorder_parts(int n, const float4 &lim, Get get, Put put) {
+// Reorder of one list in two sweeps, each part in list order: the first sweep
+// classifies every entry (index(k) -> entry, rsq(entry) -> squared distance)
+// and counts the parts, keeping the 4-bit part codes in thread-local memory;
+// the second re-reads the entries and places each at its part's cursor.  Lists
+// longer than REORDER_CAP classify again in the second sweep.
+constexpr int REORDER_CAP = 256;
+
+template <class Index, class Rsq, class Put>
+__device__ __forceinline__ int4 reorder_parts(int n, const float4 &lim, Index index, Rsq rsq,
+                                              Put put) {
+  unsigned codes[REORDER_CAP / 8];
+  const bool keep = n <= REORDER_CAP;
   int c[4] = {0, 0, 0, 0};
+  unsigned word = 0u;
   for (int k = 0; k < n; k++) {
-    const int p = cull_part(get(k).y, lim);
+    const int p = cull_part(rsq(index(k)), lim);
     if (p < 4) c[p]++;
+    if (keep) {
+      word |= (unsigned) p << (4 * (k & 7));
+      if ((k & 7) == 7 || k == n - 1) {
+        codes[k >> 3] = word;
+        word = 0u;
+      }
+    }
   }
   int m[5] = {0, c[0], c[0] + c[1], c[0] + c[1] + c[2], c[0] + c[1] + c[2] + c[3]};
   const int4 nn = make_int4(m[2], m[3], m[4], n);
   for (int k = 0; k < n; k++) {
-    const float2 e = get(k);
-    put(m[cull_part(e.y, lim)]++, __float_as_int(e.x));
+    const int e = index(k);
+    int p;
+    if (keep) {
+      if ((k & 7) == 0) word = codes[k >> 3];
+      p = (int) ((word >> (4 * (k & 7))) & 15u);
+    } else {
+      p = cull_part(rsq(e), lim);
+    }
+    put(m[p]++, e);
   }
   return nn;
 }
-
 
 // 40 registers at three 512-thread blocks per SM (48 warps): more gathers in flight
 __global__ void __launch_bounds__(512, 3)
@@ -276,14 +298,14 @@ __global__ void k_list_partition(const float4 *__restrict__ xq, float g, const i
     ref[i] = qi;
     float cx, cy, cz;
     cell_of(qi, cx, cy, cz);
-    auto get = [&](int k) {
-      const int j = __ldg(list + (size_t) k * stride + i);
+    auto index = [&](int k) { return __ldg(list + (size_t) k * stride + i); };
+    auto rsq = [&](int j) {
       float dx, dy, dz;
       rel_vec(qi, cx, cy, cz, __ldg(xq + j), g, dx, dy, dz);
-      return make_float2(__int_as_float(j), dx * dx + dy * dy + dz * dz);
+      return dx * dx + dy * dy + dz * dz;
     };
     auto put = [&](int at, int j) { out[(size_t) at * stride + i] = j; };
-    nnear[i] = reorder_parts(num[i], lim, get, put);
+    nnear[i] = reorder_parts(num[i], lim, index, rsq, put);
   }
 }
 
@@ -1128,14 +1150,14 @@ __global__ void k_ip_reorder(const int *__restrict__ row_start, const int *__res
     float cx, cy, cz;
     cell_of(qi, cx, cy, cz);
     const int s0 = row_start[r];
-    auto get = [&](int k) {
-      const int sid = __ldg(ent + s0 + k);
+    auto index = [&](int k) { return __ldg(ent + s0 + k); };
+    auto rsq = [&](int sid) {
       float dx, dy, dz;
       rel_vec(qi, cx, cy, cz, __ldg(site_q + sid), g, dx, dy, dz);
-      return make_float2(__int_as_float(sid), dx * dx + dy * dy + dz * dz);
+      return dx * dx + dy * dy + dz * dz;
     };
     auto put = [&](int at, int sid) { ent_near[s0 + at] = sid; };
-    nnear_row[r] = reorder_parts(row_start[r + 1] - s0, lim, get, put);
+    nnear_row[r] = reorder_parts(row_start[r + 1] - s0, lim, index, rsq, put);
   }
   for (long long t = blockIdx.x * blockDim.x + threadIdx.x; t < nvals; t += stride)
     node_ref[t] = node_hl[t];
