@@ -1983,6 +1983,24 @@ void cacg_context::borders() {
 // CommBrick::forward_comm / eforward_comm: ghost positions from their sources,
 // swap by swap (comm_brick.cpp:1017-1112)
 void cacg_context::forward_comm() {
+  if (!swaps.empty() && swaps.size() <= (size_t) MAX_SWAPS) {
+    SwapChain ca{}, ce{};
+    ca.n = ce.n = (int) swaps.size();
+    for (size_t k = 0; k < swaps.size(); k++) {
+      ca.first[k] = swaps[k].firstrecv;
+      ce.first[k] = swaps[k].efirstrecv;
+      for (int d = 0; d < 3; d++) ca.d[k][d] = ce.d[k][d] = swaps[k].d[d];
+    }
+    if (nlocal && nghost) {
+      launch_forward_atoms_all(d_x.p, d_send.p, nlocal, nghost, ca, stream);
+      launches++;
+    }
+    if (enlocal && enghost) {
+      launch_forward_elems_all(d_nodex.p, d_esend.p, enlocal, enghost, ce, stream);
+      launches++;
+    }
+    return;
+  }
   for (auto &w : swaps) {
     if (nlocal && w.nsend) {
       launch_forward_atoms(d_x.p, d_send.p + w.send_off, w.nsend, w.firstrecv, w.d[0], w.d[1], w.d[2], stream);

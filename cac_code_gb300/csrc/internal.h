@@ -116,6 +116,18 @@ void launch_border_scatter_elems(double *ex, double *nodex, int *etype, int *eta
                                  int *sendlist, const int *flags, const int *pos, int nfirst,
                                  int nlast, int n0, double dx, double dy, double dz,
                                  cudaStream_t s);
+// the swaps of a forward communication: first ghost index and shift of each
+constexpr int MAX_SWAPS = 8;
+struct SwapChain {
+  int n;
+  int first[MAX_SWAPS];
+  double d[MAX_SWAPS][3];
+};
+// every swap in one launch, each ghost value computed as swap by swap
+void launch_forward_atoms_all(double4 *x, const int *send, int nlocal, int nghost,
+                              const SwapChain &c, cudaStream_t s);
+void launch_forward_elems_all(double *nodex, const int *send, int nlocal, int nghost,
+                              const SwapChain &c, cudaStream_t s);
 void launch_forward_atoms(double4 *x, const int *sendlist, int n, int first, double dx,
                           double dy, double dz, cudaStream_t s);
 void launch_forward_elems(double *nodex, const int *sendlist, int n, int first, double dx,

@@ -198,6 +198,52 @@ __global__ void k_forward_elems(double *__restrict__ nodex, const int *__restric
   nodex[24 * (first + m) + r] = nodex[24 * send[m] + r] + d;
 }
 
+// All swaps of a forward communication in one launch: each ghost follows its
+// chain of sources back to the owned item (ghost g was sent from
+// send[g - nfirst], an owned item or an earlier swap's ghost) and applies the
+// swaps' shifts in the order the swaps ran, so every ghost value is the same
+// sum of the same doubles as swap-by-swap communication.
+__device__ __forceinline__ int swap_of(const SwapChain &c, int g) {
+  int w = 0;
+  for (int k = 1; k < c.n; k++)
+    if (g >= c.first[k]) w = k;
+  return w;
+}
+
+__global__ void k_forward_atoms_all(double4 *__restrict__ x, const int *__restrict__ send,
+                                    int nlocal, int nghost, SwapChain c) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nghost) return;
+  int chain[MAX_SWAPS], depth = 0, src = nlocal + t;
+  while (src >= nlocal && depth < MAX_SWAPS) {
+    chain[depth++] = swap_of(c, src);
+    src = send[src - nlocal];
+  }
+  double4 p = x[src];
+  for (int k = depth - 1; k >= 0; k--) {
+    const int w = chain[k];
+    p.x = p.x + c.d[w][0];
+    p.y = p.y + c.d[w][1];
+    p.z = p.z + c.d[w][2];
+  }
+  x[nlocal + t] = p;
+}
+
+__global__ void k_forward_elems_all(double *__restrict__ nodex, const int *__restrict__ send,
+                                    int nlocal, int nghost, SwapChain c) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nghost * 24) return;
+  const int m = t / 24, r = t % 24, dim = r % 3;
+  int chain[MAX_SWAPS], depth = 0, src = nlocal + m;
+  while (src >= nlocal && depth < MAX_SWAPS) {
+    chain[depth++] = swap_of(c, src);
+    src = send[src - nlocal];
+  }
+  double v = nodex[24 * (size_t) src + r];
+  for (int k = depth - 1; k >= 0; k--) v = v + c.d[chain[k]][dim];
+  nodex[24 * (size_t) (nlocal + m) + r] = v;
+}
+
 template <class T>
 __global__ void k_copy_root(T *__restrict__ a, int width, const int *__restrict__ root, int gfirst,
                             int gn) {
@@ -390,6 +436,21 @@ void launch_forward_atoms(double4 *x, const int *sendlist, int n, int first, dou
   if (n <= 0) return;
   k_forward_atoms<<<nblk(n, 256), 256, 0, s>>>(x, sendlist, n, first, dx, dy, dz);
   check(cudaGetLastError(), "forward_atoms");
+}
+
+void launch_forward_atoms_all(double4 *x, const int *send, int nlocal, int nghost,
+                              const SwapChain &c, cudaStream_t s) {
+  if (nghost <= 0) return;
+  k_forward_atoms_all<<<nblk(nghost, 256), 256, 0, s>>>(x, send, nlocal, nghost, c);
+  check(cudaGetLastError(), "forward_atoms_all");
+}
+
+void launch_forward_elems_all(double *nodex, const int *send, int nlocal, int nghost,
+                              const SwapChain &c, cudaStream_t s) {
+  if (nghost <= 0) return;
+  k_forward_elems_all<<<nblk((long long) nghost * 24, 256), 256, 0, s>>>(nodex, send, nlocal,
+                                                                         nghost, c);
+  check(cudaGetLastError(), "forward_elems_all");
 }
 
 void launch_forward_elems(double *nodex, const int *sendlist, int n, int first, double dx,
