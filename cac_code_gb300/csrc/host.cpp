@@ -200,9 +200,10 @@ struct cacg_context {
   // mixed precision: FP32 spline tables, double-single element nodes and
   // integration-point shape functions, packed site positions and site F'(rho),
   // the referenced sites of each lattice line, lattice sizes per type
-  DBuf<float4> d_xl, d_rhor_val4, d_ftab, d_fp4, d_site_q;
+  DBuf<float4> d_xl, d_rhor_val4, d_ftab, d_fp4, d_line_pos;
   DBuf<float2> d_node_hl, d_spa_int_hl;
-  DBuf<float> d_u, d_ljf, d_site_fpf, d_fpf;
+  DBuf<float> d_u, d_ljf, d_fpf;
+  DBuf<float2> d_line_rho;
   DBuf<unsigned long long> d_line_mask, d_line_mask_f;  // all rows; rows of nonzero weight
   DBuf<int> d_nae;
   DBuf<float2> d_frac, d_fipf;  // lattice fractions; double-single row forces
@@ -217,7 +218,8 @@ struct cacg_context {
   // first, their count, the nodes at the reorder, near-site masks, the line
   // code of every site, force-row flags; reordered once per element list build
   // and whenever a node has moved 0.495 A since
-  DBuf<int> d_ent_near, d_site_code;
+  DBuf<int> d_ent_near;
+  bool codes_ok = false;  // the lists fit the line codes of the mixed element passes
   DBuf<int4> d_nnear_row;
   DBuf<float2> d_node_ref;
   DBuf<unsigned long long> d_line_mask_n, d_line_mask_nf;
@@ -495,10 +497,10 @@ cacg_context::~cacg_context() {
   d_ftab.release();
   d_u.release();
   d_fp4.release();
-  d_site_q.release();
+  d_line_pos.release();
+  d_line_rho.release();
   d_node_hl.release();
   d_spa_int_hl.release();
-  d_site_fpf.release();
   d_fpf.release();
   d_line_mask.release();
   d_line_mask_f.release();
@@ -514,7 +516,6 @@ cacg_context::~cacg_context() {
   d_ent.release();
   d_ent_near.release();
   d_nnear_row.release();
-  d_site_code.release();
   d_node_ref.release();
   d_line_mask_n.release();
   d_line_mask_nf.release();
@@ -2151,24 +2152,18 @@ void cacg_context::neighbor_nbuild() {
   fp64_fma::need_compact(d_site_flag.p, d_site_pos.p, nsites, d_site_base.p, nall, d_need.p,
                          d_need_elem.p, s);
   launches += 4;
-  // the same per lattice line, for the mixed site kernels
-  d_line_mask.ensure((size_t) std::max(nall, 1) * std::max(maxlines, 1), s);
-  mixed::line_mask(d_site_flag.p, d_etype.p, d_site_base.p, d_nae.p, nall, maxlines, d_line_mask.p,
-                   s);
-  launches++;
-  // the sites that the rows of nonzero weight reference: the mixed F'(rho)
-  // kernel computes only these (d_site_pos, the positions of the compaction
-  // above, is free again once that has run)
-  check(cudaMemsetAsync(d_site_pos.p, 0, sizeof(int) * std::max(nsites, 1), s), "flag_f");
-  mixed::mark_rows(d_force_rows.p, nforce, d_row_start.p, d_ent.p, d_site_pos.p, s);
-  d_line_mask_f.ensure((size_t) std::max(nall, 1) * std::max(maxlines, 1), s);
-  mixed::line_mask(d_site_pos.p, d_etype.p, d_site_base.p, d_nae.p, nall, maxlines,
-                   d_line_mask_f.p, s);
-  launches += 3;
-  if (max_naz <= 64) {  // the line code of every site (mixed list culling)
-    d_site_code.ensure(std::max(nsites, 1), s);
-    mixed::site_code(d_etype.p, d_site_base.p, d_nae.p, maxlines, nall, d_site_code.p, s);
-    launches++;
+  // for the mixed passes: the row-major lists as line codes
+  // (element * maxlines + line) << 6 | kk, and the lines every row's entries
+  // (every force row's) reference, a bit per site
+  codes_ok = max_naz <= 64 && (long long) nall * std::max(maxlines, 1) < (1LL << 25);
+  if (codes_ok) {
+    const long long nmask = (long long) std::max(nall, 1) * std::max(maxlines, 1);
+    mixed::ent_codes(d_ent.p, h_pin[10], d_site_base.p, nall, d_etype.p, d_nae.p, maxlines, s);
+    d_line_mask.ensure(nmask, s);
+    d_line_mask_f.ensure(nmask, s);
+    mixed::line_masks(d_row_start.p, d_ent.p, nullptr, nrows, d_row_isforce.p, d_line_mask.p,
+                      d_line_mask_f.p, nmask, nullptr, s);
+    launches += 3;
   }
   elist_builds++;
   elists_built = true;
@@ -2335,7 +2330,9 @@ void cacg_context::pair_compute_mixed(int pass) {
 void cacg_context::pair_ecompute_mixed() {
   cudaStream_t s = stream;
   int nall = enlocal + enghost;
-  ElemTables t = etab();
+  if (!codes_ok)
+    fail(CACG_EINVAL, "mixed element passes: at most 64 sites per lattice line and 2^25 lattice "
+                      "lines (element list build)");
   double l0[3], g;
   pack_grid(l0, g);
   d_misc.ensure(16, s);
@@ -2344,26 +2341,22 @@ void cacg_context::pair_ecompute_mixed() {
     oob_zeroed = true;
   }
   const mixed::PackGrid pg = mixed::make_pack_grid(l0, g, d_misc.p + 9);
-  d_site_q.ensure(std::max(nsites, 1), s);
+  const long long nmask = (long long) std::max(nall, 1) * std::max(maxlines, 1);
   d_node_hl.ensure((size_t) 24 * nall, s);
+  d_line_pos.ensure(3 * (size_t) nmask, s);
   // displacement culling of the integration-point lists: slot 13 holds the
   // largest squared node displacement since the last reorder (set huge after
   // an element list build, so that this pass reorders), slot 14 flags a
-  // reorder in this pass
-  // (the lists are kept reordered even with "tune cull no", so that culling
-  // changes no bit: it only stops each row before its far entries)
-  const bool reorder_e = max_naz <= 64 && nrows > 0;
-  const bool cull_e = reorder_e && mixed_cull;
-  const long long nmask = (long long) std::max(nall, 1) * std::max(maxlines, 1);
+  // reorder in this pass.  The lists are kept reordered even with "tune cull
+  // no", so that culling changes no bit: it only stops each row early.
+  const bool cull_e = mixed_cull;
   unsigned *eflags = reinterpret_cast<unsigned *>(d_misc.p + 13);
-  const bool same_e = reorder_e && epart_of == elist_builds;
-  if (reorder_e) {
-    d_ent_near.ensure(std::max((size_t) 1, d_ent.cap), s);
-    d_nnear_row.ensure(std::max(nrows, 1), s);
-    d_node_ref.ensure((size_t) 24 * nall, s);
-    d_line_mask_n.ensure(nmask, s);
-    d_line_mask_nf.ensure(nmask, s);
-  }
+  const bool same_e = epart_of == elist_builds;
+  d_ent_near.ensure(std::max((size_t) 1, d_ent.cap), s);
+  d_nnear_row.ensure(std::max(nrows, 1), s);
+  d_node_ref.ensure((size_t) 24 * nall, s);
+  d_line_mask_n.ensure(nmask, s);
+  d_line_mask_nf.ensure(nmask, s);
   if (!ereorders_zeroed) {
     check(cudaMemsetAsync(d_misc.p + 15, 0, sizeof(int), s), "ereorders");
     ereorders_zeroed = true;
@@ -2372,30 +2365,29 @@ void cacg_context::pair_ecompute_mixed() {
   check(cudaMemsetAsync(d_misc.p + 14, 0, sizeof(int), s), "ereordered");
   mixed::node_split(d_nodex.p, nall, d_node_hl.p, same_e ? d_node_ref.p : nullptr, eflags, s);
   const mixed::Lattice lat{d_nae.p, d_frac.p, fstride};
-  mixed::site_q(d_node_hl.p, d_etype.p, d_site_base.p, lat, max_nax, max_naz, d_line_mask.p,
-                cull_e ? d_line_mask_n.p : nullptr, eflags, maxlines, pg, nall, d_site_q.p, s);
+  // the lattice lines that the scanned entries reference (all referenced
+  // lines in a step that reorders)
+  mixed::lines(d_node_hl.p, d_etype.p, lat, max_nax, d_line_mask.p,
+               cull_e ? d_line_mask_n.p : nullptr, eflags, maxlines, pg, nall, d_line_pos.p, s);
   d_ip_q.ensure(std::max(nrows, 1), s);
   d_ip_h.ensure(std::max(nrows, 1), s);
   d_ip_l.ensure(std::max(nrows, 1), s);
   mixed::row_q(d_row_elem.p, d_row_jj.p, d_etype.p, d_int_off.p, d_spa_int_hl.p, d_node_hl.p, nrows,
                pg, d_ip_q.p, d_ip_h.p, d_ip_l.p, s);
-  launches += 3;
   const double csq_e = pair_style == 1 ? ljtab.cutsq[1 * (MAXT + 1) + 1] : cutforcesq;
-  if (reorder_e) {
-    mixed::ip_reorder(d_row_start.p, d_ent.p, nrows, d_ip_q.p, d_site_q.p, pg.g,
-                      (float) std::sqrt(csq_e), d_ent_near.p, d_nnear_row.p, d_node_hl.p, nall,
-                      d_node_ref.p, eflags, s);
-    mixed::near_masks(d_row_start.p, d_ent_near.p, d_nnear_row.p, nrows, d_row_isforce.p,
-                      d_site_code.p, d_line_mask_n.p, d_line_mask_nf.p, nmask, eflags, s);
-    launches += 3;
-    epart_of = elist_builds;
-  }
+  mixed::ip_reorder(d_row_start.p, d_ent.p, nrows, d_ip_q.p, d_line_pos.p, lat, pg,
+                    (float) std::sqrt(csq_e), d_ent_near.p, d_nnear_row.p, d_node_hl.p, nall,
+                    d_node_ref.p, eflags, s);
+  mixed::line_masks(d_row_start.p, d_ent_near.p, d_nnear_row.p, nrows, d_row_isforce.p,
+                    d_line_mask_n.p, d_line_mask_nf.p, nmask, eflags, s);
+  launches += 6;
+  epart_of = elist_builds;
   const bool use_sur = sur && nfar > 0;
   const float eps = 1.0e-4f;
   mixed::MixedElems m{};
   m.block = mixed_block;
   m.group = mixed_ip_group;
-  m.site_q = d_site_q.p;
+  m.line_pos = d_line_pos.p;
   m.ip_q = d_ip_q.p;
   m.ip_h = d_ip_h.p;
   m.ip_l = d_ip_l.p;
@@ -2404,16 +2396,13 @@ void cacg_context::pair_ecompute_mixed() {
   m.row_first = d_row_first.p;
   m.node_list = d_node_list.p;
   m.row_start = d_row_start.p;
-  m.ent = reorder_e ? d_ent_near.p : d_ent.p;
+  m.ent = d_ent_near.p;
   m.nnear_row = cull_e ? d_nnear_row.p : nullptr;
   m.eflags = eflags;
   m.nlocal_e = enlocal;
   m.rows = d_force_rows.p;
   m.nforce = nforce;
-  m.node_hl = d_node_hl.p;
-  m.site_base = d_site_base.p;
   m.lat = lat;
-  m.nall_e = nall;
   m.pg = pg;
   if (use_sur) m.skip = d_skip.p;
   if (pair_style == 1) {
@@ -2434,16 +2423,18 @@ void cacg_context::pair_ecompute_mixed() {
     m.band_lo = m.cutsq_f * (1.0f - eps);
     m.band_hi = m.cutsq_f * (1.0f + eps);
     d_erho.ensure((size_t) NPE * nall, s);
-    d_site_fpf.ensure(std::max(nsites, 1), s);
+    d_line_rho.ensure(nmask, s);
     mixed::ip_pass(m, 1, d_rhor_val4.p, e, 0.f, 0.f, d_erho.p, nullptr, s);
     launch_copy_root(d_erho.p, NPE, d_eroot.p, enlocal, enghost, s);
-    mixed::site_fp(d_erho.p, d_etype.p, d_site_base.p, lat, d_line_mask_f.p,
-                   cull_e ? d_line_mask_nf.p : nullptr, eflags, maxlines, d_fp4.p, nrho, rdrho,
-                   nall, d_site_fpf.p, s);
+    mixed::line_rho(d_erho.p, d_etype.p, lat, d_line_mask_f.p, cull_e ? d_line_mask_nf.p : nullptr,
+                    eflags, maxlines, nall, d_line_rho.p, s);
     d_row_fpf.ensure(std::max(nrows, 1), s);
     mixed::row_fp(d_force_rows.p, nforce, d_row_elem.p, d_row_jj.p, d_etype.p, d_int_off.p,
                   d_spa_int.p, d_erho.p, e, d_row_fpf.p, s);
-    m.site_fp = d_site_fpf.p;
+    m.line_rho = d_line_rho.p;
+    m.fp4 = d_fp4.p;
+    m.nrho = nrho;
+    m.rdrho = (float) rdrho;
     m.row_fp = d_row_fpf.p;
     if (use_sur) surrogate_predict(e);
     mixed::ip_pass(m, 2, d_ftab.p, e, 0.f, 0.f, nullptr, d_fipf.p, s);

@@ -307,27 +307,27 @@ struct Lattice {
   int fstride;
 };
 struct MixedElems {
-  const float4 *site_q;       // packed site positions of this step (referenced sites)
-  const float *site_fp;       // FP32 F'(rho) at the referenced sites (EAM force pass)
+  const float4 *line_pos;  // lattice lines of this step: U, D double-single (3 float4)
+  const float2 *line_rho;  // nodal-density lines of this step (EAM force pass)
+  const float4 *fp4;       // FP32 F' spline, c0..c2 per knot
+  int nrho = 0;
+  float rdrho = 0.f;
   const float4 *ip_q;         // packed integration-point positions, per row
   const float4 *ip_h, *ip_l;  // their double-single positions
   const float *row_fp;        // FP32 F'(rho) at the rows of nonzero weight (EAM force pass)
   const int *etype, *row_elem, *row_first, *node_list;
-  const int *row_start, *ent;  // integration-point lists, row-major
-  // displacement culling: ent holds each row's near entries first, nnear_row
-  // counts them; eflags = [node displacement^2 bits, reordered this step]
-  const int4 *nnear_row = nullptr;
-  const unsigned *eflags = nullptr;
+  // integration-point lists, row-major: line codes (element * maxlines + line)
+  // << 6 | kk, each row's culling parts in order
+  const int *row_start, *ent;
+  const int4 *nnear_row = nullptr;  // culled entry counts per row (null: no culling)
+  const unsigned *eflags = nullptr;  // [node displacement^2 bits, reordered this step]
   int nlocal_e;
   const int *rows;  // rows of nonzero weight (force passes), count nforce
   int nforce;
   float cutsq_f, band_lo, band_hi;
   double cutsq;
-  const float2 *node_hl;                // [nall][24] double-single node coordinates
   const unsigned char *skip = nullptr;  // elements whose forces come from the surrogate
-  const int *site_base;                 // site offsets per element
   Lattice lat;
-  int nall_e;
   PackGrid pg;
   int block = 512;  // threads per block of the persistent grids
   int group = 8;    // lanes per integration point (4, 8 or 16)
@@ -342,43 +342,34 @@ void pack_rel(const double4 *x, int n, const PackGrid &pg, float4 *xq, const flo
 // with ref: the largest squared node displacement against ref -> *dmax2 (atomic max)
 void node_split(const double *nodex, int n, float2 *hl, const float2 *ref, unsigned *dmax2,
                 cudaStream_t s);
-// per element and lattice line (ii, jj): bit kk set when site (ii, jj, kk) is
-// referenced by an integration-point list
-// flag the sites referenced by the listed rows
-void mark_rows(const int *rows, int nlisted, const int *row_start, const int *ent, int *flag,
-               cudaStream_t s);
-void line_mask(const int *flag, const int *etype, const int *site_base, const int *nae, int nelem,
-               int maxlines, unsigned long long *mask, cudaStream_t s);
-// packed positions of the referenced sites (double-single interpolation)
-// mask_near (with eflags): the sites of near entries, used while culling holds
-void site_q(const float2 *node_hl, const int *etype, const int *site_base, const Lattice &lat,
-            int max_nax, int max_naz, const unsigned long long *mask,
-            const unsigned long long *mask_near, const unsigned *eflags, int maxlines,
-            const PackGrid &pg, int nelem, float4 *q, cudaStream_t s);
-// FP32 F'(rho) at the referenced sites; fp4 holds F' coefficients c0..c2 per knot
-void site_fp(const double *erho, const int *etype, const int *site_base, const Lattice &lat,
-             const unsigned long long *mask, const unsigned long long *mask_near,
-             const unsigned *eflags, int maxlines, const float4 *fp4, int nrho, double rdrho,
-             int nelem, float *fp, cudaStream_t s);
+// Lattice lines: U, D (double-single, relative to l0) of every line that
+// mask (mask_near while culling holds) marks; FP32 nodal-density lines
+void lines(const float2 *node_hl, const int *etype, const Lattice &lat, int max_nax,
+           const unsigned long long *mask, const unsigned long long *mask_near,
+           const unsigned *eflags, int maxlines, const PackGrid &pg, int nelem, float4 *line_pos,
+           cudaStream_t s);
+void line_rho(const double *erho, const int *etype, const Lattice &lat,
+              const unsigned long long *mask, const unsigned long long *mask_near,
+              const unsigned *eflags, int maxlines, int nelem, float2 *out, cudaStream_t s);
+// the integration-point lists' site ids turned into line codes in place
+void ent_codes(int *ent, long long n, const int *site_base, int nall_e, const int *etype,
+               const int *nae, int maxlines, cudaStream_t s);
+// line masks (bit kk per line) of the rows' entries (all rows; force rows);
+// with nnear_row, of the culled parts; with gate, only after a reorder
+void line_masks(const int *row_start, const int *ent, const int4 *nnear_row, int nrows,
+                const unsigned char *isforce, unsigned long long *mask,
+                unsigned long long *mask_f, long long nmask, const unsigned *gate,
+                cudaStream_t s);
 // displacement culling of the integration-point lists: reorder (gated on the
 // node displacement in eflags[0]) into ent_near / nnear_row and keep the
-// nodes as the reference (eflags[1] = 1, eflags[2] counts reorders); rebuild
-// the near-site masks after a reorder
+// nodes as the reference (eflags[1] = 1, eflags[2] counts reorders)
 void ip_reorder(const int *row_start, const int *ent, int nrows, const float4 *ip_q,
-                const float4 *site_q, float g, float cutoff, int *ent_near, int4 *nnear_row,
-                const float2 *node_hl, int nall_e, float2 *node_ref, unsigned *eflags,
-                cudaStream_t s);
-void near_masks(const int *row_start, const int *ent_near, const int4 *nnear_row, int nrows,
-                const unsigned char *isforce, const int *site_code, unsigned long long *mask,
-                unsigned long long *mask_f, long long nmask, const unsigned *eflags,
-                cudaStream_t s);
-// per site: (element * maxlines + line) << 6 | kk (lattice lines of <= 64 sites)
-void site_code(const int *etype, const int *site_base, const int *nae, int maxlines, int nelem,
-               int *code, cudaStream_t s);
-// each atom's list reordered (entries within cut_rsq at the packed positions,
-// then those within cutoff + 1 A, counted together in nnear, then the rest)
-// when the displacement since the last reorder (dmax2[0], against ref) no
-// longer allows culling; it then sets ref to the positions and dmax2[1] = 1
+                const float4 *line_pos, const Lattice &lat, const PackGrid &pg, float cutoff,
+                int *ent_near, int4 *nnear_row, const float2 *node_hl, int nall_e,
+                float2 *node_ref, unsigned *eflags, cudaStream_t s);
+// each atom's list reordered in its culling parts when the displacement since
+// the last reorder (dmax2[0], against ref) no longer allows culling; it then
+// sets ref to the positions and dmax2[1] = 1
 void list_partition(const float4 *xq, float g, const int *num, const int *list, int stride,
                     int nlocal, float cut_rsq, float cutoff, int *out, int4 *nnear, float4 *ref,
                     unsigned *dmax2, cudaStream_t s);

@@ -827,100 +827,38 @@ __device__ __forceinline__ void column_ds(const float2 *nx, ds a, int d, ds (&E)
   E[3] = ds_lerp(node_ds(nx, 7, d), node_ds(nx, 6, d), a);
 }
 
-// site (ii, jj, kk) of an element in double-single, by the same lerps as the
-// site kernel (the guard-band path of the integration-point passes)
-__device__ __forceinline__ void site_ds(const float2 *nx, const Lattice &lat, int ty, int ii, int jj,
-                                        int kk, ds (&x)[3]) {
-  const ds a = frac_of(lat, ty, 0, ii), b = frac_of(lat, ty, 1, jj), c = frac_of(lat, ty, 2, kk);
-#pragma unroll
-  for (int d = 0; d < 3; d++) {
-    ds E[4];
-    column_ds(nx, a, d, E);
-    const ds B = ds_lerp(E[0], E[1], b), T = ds_lerp(E[2], E[3], b);
-    x[d] = ds_madd(c, ds_sub(T, B), B);
-  }
-}
-
-// Lines (ii, jj) of an element whose sites any integration-point list
-// references: bit kk of the mask (sites kk >= 64 are always computed).
-__global__ void k_line_mask(const int *__restrict__ flag, const int *__restrict__ etype,
-                            const int *__restrict__ site_base, const int *__restrict__ nae,
-                            int nelem, int maxlines, unsigned long long *__restrict__ mask) {
-  const long long t = (long long) blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long) nelem * maxlines) return;
-  const int e = (int) (t / maxlines), L = (int) (t % maxlines);
-  const int ty = etype[e];
-  const int nlines = nae[3 * ty] * nae[3 * ty + 1], naz = nae[3 * ty + 2];
-  unsigned long long m = 0;
-  if (L < nlines) {
-    const int *f = flag + site_base[e] + (size_t) L * naz;
-    for (int kk = 0; kk < naz && kk < 64; kk++)
-      if (f[kk]) m |= 1ull << kk;
-  }
-  mask[t] = m;
-}
-
-// flag the sites referenced by the listed rows (row-major lists)
-__global__ void k_mark_rows(const int *__restrict__ rows, int nlisted, const int *__restrict__ row_start,
-                            const int *__restrict__ ent, int *__restrict__ flag) {
-  const int it = blockIdx.x * blockDim.x + threadIdx.x;
-  if (it >= nlisted) return;
-  const int r = rows[it];
-  for (int k = row_start[r]; k < row_start[r + 1]; k++) flag[ent[k]] = 1;
-}
-
-// Site positions of this step, packed; one block per element.  Per lattice
-// column ii the x-lerps give P = E0 - l0, Q = E1 - E0, R = E2 - E0 and
-// S = (E3 - E2) - (E1 - E0), so that a line (ii, jj) starts at U = P + b Q and
-// steps D = R + b S (b = jj / (ny - 1)), and its site kk is U + c D.  The
-// element's lines are taken LCH at a time: each thread prepares one line and
-// lists the line's referenced sites in shared memory (a block prefix sum of
-// the masks' popcounts), then the block's threads run over that compact list.
+// Lattice lines of this step: per element, per lattice column ii the x-lerps
+// give P = E0 - l0, Q = E1 - E0, R = E2 - E0 and S = (E3 - E2) - (E1 - E0),
+// so that a line (ii, jj) starts at U = P + b Q and steps D = R + b S
+// (b = jj / (ny - 1)); its site kk is U + c D (c = kk / (nz - 1)), all in
+// double-single.  One block per element writes U and D of every line that a
+// scanned list entry references (48 bytes a line); the integration-point
+// passes evaluate the sites from them.
 constexpr int LCH = 128;
 
-// exclusive prefix sum over the block (LCH threads); returns the block total
-__device__ __forceinline__ int block_scan(int v, int &excl, int *s_warp) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  int x = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) s_warp[w] = x;
-  __syncthreads();
-  int before = 0, total = 0;
-#pragma unroll
-  for (int k = 0; k < LCH / 32; k++) {
-    const int t = s_warp[k];
-    if (k < w) before += t;
-    total += t;
-  }
-  excl = before + x - v;
-  __syncthreads();  // s_warp may be reused
-  return total;
+// line data: U.x, U.y | U.z, D.x | D.y, D.z as double-single pairs
+__device__ __forceinline__ void line_site(const float4 *__restrict__ lp, int code, ds c,
+                                          ds (&x)[3]) {
+  const float4 a = __ldg(lp + 3 * (size_t) (code >> 6));
+  const float4 b = __ldg(lp + 3 * (size_t) (code >> 6) + 1);
+  const float4 d = __ldg(lp + 3 * (size_t) (code >> 6) + 2);
+  x[0] = ds_madd(c, ds{b.z, b.w}, ds{a.x, a.y});
+  x[1] = ds_madd(c, ds{d.x, d.y}, ds{a.z, a.w});
+  x[2] = ds_madd(c, ds{d.z, d.w}, ds{b.x, b.y});
 }
 
 __global__ void __launch_bounds__(LCH)
-k_site_q(const float2 *__restrict__ node_hl, const int *__restrict__ etype,
-         const int *__restrict__ site_base, Lattice lat,
-         const unsigned long long *__restrict__ line_mask,
-         const unsigned long long *__restrict__ line_mask_near, const unsigned *__restrict__ eflags,
-         int maxlines, PackGrid pg, float4 *__restrict__ site_q) {
-  extern __shared__ ds s_mem[];
+k_lines(const float2 *__restrict__ node_hl, const int *__restrict__ etype, Lattice lat,
+        const unsigned long long *__restrict__ line_mask,
+        const unsigned long long *__restrict__ line_mask_near, const unsigned *__restrict__ eflags,
+        int maxlines, PackGrid pg, float4 *__restrict__ line_pos) {
+  extern __shared__ ds s_col[];  // [nax][3][4]: P, Q, R, S
   __shared__ float2 s_nx[24];
-  __shared__ int s_warp[LCH / 32];
-  __shared__ unsigned short s_list[LCH * 64];  // (line in chunk) << 6 | kk
   const int e = blockIdx.x;
   const int ty = etype[e];
   const int *nae = lat.nae;
-  const int nax = nae[3 * ty], nay = nae[3 * ty + 1], naz = nae[3 * ty + 2];
-  ds *s_col = s_mem;          // [nax][3][4]: P, Q, R, S
-  ds *s_U = s_col + 12 * nax;  // [LCH][3]
-  ds *s_D = s_U + 3 * LCH;     // [LCH][3]
-  ds *s_c = s_D + 3 * LCH;     // [naz]
+  const int nax = nae[3 * ty], nay = nae[3 * ty + 1];
   if (threadIdx.x < 24) s_nx[threadIdx.x] = node_hl[24 * (size_t) e + threadIdx.x];
-  for (int k = threadIdx.x; k < naz; k += blockDim.x) s_c[k] = frac_of(lat, ty, 2, k);
   __syncthreads();
   const ds l0[3] = {{pg.l0h[0], pg.l0l[0]}, {pg.l0h[1], pg.l0l[1]}, {pg.l0h[2], pg.l0l[2]}};
   for (int q = threadIdx.x; q < 3 * nax; q += blockDim.x) {
@@ -934,114 +872,121 @@ k_site_q(const float2 *__restrict__ node_hl, const int *__restrict__ etype,
     o[2] = ds_sub(E[2], E[0]);
     o[3] = ds_sub(ds_sub(E[3], E[2]), q1);
   }
-  const int nlines = nax * nay, base = site_base[e];
-  // while culling holds only the sites of the rows' near entries are needed
+  __syncthreads();
+  // while culling holds only the lines of the rows' near entries are needed
   const unsigned long long *lm =
       (line_mask_near && cull_ok(eflags) ? line_mask_near : line_mask) + (size_t) e * maxlines;
-  for (int L0 = 0; L0 < nlines; L0 += LCH) {
-    const int nl = min(LCH, nlines - L0);
-    __syncthreads();  // columns ready; the previous chunk consumed
-    unsigned long long mk = 0;
-    if (threadIdx.x < nl) {
-      const int L = L0 + threadIdx.x;
-      mk = lm[L];
-      if (mk || naz > 64) {
-        const int ii = L / nay, jj = L - ii * nay;
-        const ds b = frac_of(lat, ty, 1, jj);
+  float4 *out = line_pos + 3 * (size_t) e * maxlines;
+  for (int L = threadIdx.x; L < nax * nay; L += blockDim.x) {
+    if (lm[L] == 0ull) continue;
+    const int ii = L / nay, jj = L - ii * nay;
+    const ds b = frac_of(lat, ty, 1, jj);
+    ds U[3], D[3];
 #pragma unroll
-        for (int d = 0; d < 3; d++) {
-          const ds *c = s_col + (ii * 3 + d) * 4;
-          s_U[threadIdx.x * 3 + d] = ds_madd(b, c[1], c[0]);
-          s_D[threadIdx.x * 3 + d] = ds_madd(b, c[3], c[2]);
-        }
-      }
+    for (int d = 0; d < 3; d++) {
+      const ds *c = s_col + (ii * 3 + d) * 4;
+      U[d] = ds_madd(b, c[1], c[0]);
+      D[d] = ds_madd(b, c[3], c[2]);
     }
-    int at;
-    const int total = block_scan(__popcll(mk), at, s_warp);
-    for (unsigned long long m = mk; m; m &= m - 1)
-      s_list[at++] = (unsigned short) ((threadIdx.x << 6) | (__ffsll((long long) m) - 1));
-    __syncthreads();
-    for (int t = threadIdx.x; t < total; t += LCH) {
-      const int v = s_list[t], l = v >> 6, kk = v & 63;
-      const ds c = s_c[kk];
-      const ds *U = s_U + 3 * l, *D = s_D + 3 * l;
-      site_q[base + (size_t) (L0 + l) * naz + kk] =
-          pack_u(ds_madd(c, D[0], U[0]), ds_madd(c, D[1], U[1]), ds_madd(c, D[2], U[2]), pg);
-    }
-    if (naz > 64 && threadIdx.x < nl)  // sites beyond the mask's 64 bits: every one
-      for (int kk = 64; kk < naz; kk++) {
-        const ds c = s_c[kk];
-        const ds *U = s_U + 3 * threadIdx.x, *D = s_D + 3 * threadIdx.x;
-        site_q[base + (size_t) (L0 + threadIdx.x) * naz + kk] =
-            pack_u(ds_madd(c, D[0], U[0]), ds_madd(c, D[1], U[1]), ds_madd(c, D[2], U[2]), pg);
-      }
+    out[3 * L] = make_float4(U[0].h, U[0].l, U[1].h, U[1].l);
+    out[3 * L + 1] = make_float4(U[2].h, U[2].l, D[0].h, D[0].l);
+    out[3 * L + 2] = make_float4(D[1].h, D[1].l, D[2].h, D[2].l);
   }
 }
 
-// F'(rho) at the referenced sites, rho = sum_k N_k erho_k (pair_eam.cpp:1060-1065)
-// by the same lerps in FP32; one block per element, lines LCH at a time, the
-// referenced sites listed in shared memory as in k_site_q.
+// Nodal-density lines, FP32: rho at site kk of line (ii, jj) is B + c (T - B)
+// with B, T the bilinear values of the nodal densities on the z = -1 and z = +1
+// faces (pair_eam.cpp:1060-1065: rho_s = sum_k N_k erho_k).  One block per
+// element, the lines that a scanned force-row entry references.
 __global__ void __launch_bounds__(LCH)
-k_site_fp(const double *__restrict__ erho, const int *__restrict__ etype,
-          const int *__restrict__ site_base, Lattice lat,
-          const unsigned long long *__restrict__ line_mask,
-          const unsigned long long *__restrict__ line_mask_near, const unsigned *__restrict__ eflags,
-          int maxlines, const float4 *__restrict__ fp4, int nrho, float rdrho,
-          float *__restrict__ site_fp) {
+k_line_rho(const double *__restrict__ erho, const int *__restrict__ etype, Lattice lat,
+           const unsigned long long *__restrict__ line_mask,
+           const unsigned long long *__restrict__ line_mask_near,
+           const unsigned *__restrict__ eflags, int maxlines, float2 *__restrict__ line_rho) {
   __shared__ float s_er[NPE];
-  __shared__ float s_U[LCH], s_D[LCH];
-  __shared__ int s_warp[LCH / 32];
-  __shared__ unsigned short s_list[LCH * 64];
   const int e = blockIdx.x;
   const int ty = etype[e];
-  const int *nae = lat.nae;
-  const int nax = nae[3 * ty], nay = nae[3 * ty + 1], naz = nae[3 * ty + 2];
+  const int nax = lat.nae[3 * ty], nay = lat.nae[3 * ty + 1];
   if (threadIdx.x < NPE) s_er[threadIdx.x] = (float) erho[NPE * (size_t) e + threadIdx.x];
-  const int nlines = nax * nay, base = site_base[e];
-  // while culling holds only the sites of the rows' near entries are needed
+  __syncthreads();
   const unsigned long long *lm =
       (line_mask_near && cull_ok(eflags) ? line_mask_near : line_mask) + (size_t) e * maxlines;
-  for (int L0 = 0; L0 < nlines; L0 += LCH) {
-    const int nl = min(LCH, nlines - L0);
-    __syncthreads();
-    unsigned long long mk = 0;
-    if (threadIdx.x < nl) {
-      const int L = L0 + threadIdx.x;
-      mk = lm[L];
-      const int ii = L / nay, jj = L - ii * nay;
-      const float a = frac_of(lat, ty, 0, ii).h, b = frac_of(lat, ty, 1, jj).h;
-      const float e0 = s_er[0] + a * (s_er[1] - s_er[0]), e1 = s_er[3] + a * (s_er[2] - s_er[3]);
-      const float e2 = s_er[4] + a * (s_er[5] - s_er[4]), e3 = s_er[7] + a * (s_er[6] - s_er[7]);
-      const float B = e0 + b * (e1 - e0), T = e2 + b * (e3 - e2);
-      s_U[threadIdx.x] = B;
-      s_D[threadIdx.x] = T - B;
+  float2 *out = line_rho + (size_t) e * maxlines;
+  for (int L = threadIdx.x; L < nax * nay; L += blockDim.x) {
+    if (lm[L] == 0ull) continue;
+    const int ii = L / nay, jj = L - ii * nay;
+    const float a = frac_of(lat, ty, 0, ii).h, b = frac_of(lat, ty, 1, jj).h;
+    const float e0 = s_er[0] + a * (s_er[1] - s_er[0]), e1 = s_er[3] + a * (s_er[2] - s_er[3]);
+    const float e2 = s_er[4] + a * (s_er[5] - s_er[4]), e3 = s_er[7] + a * (s_er[6] - s_er[7]);
+    const float B = e0 + b * (e1 - e0), T = e2 + b * (e3 - e2);
+    out[L] = make_float2(B, T - B);
+  }
+}
+
+// Line masks from the entry codes: bit kk of mask[line] for every entry of
+// every row (mask) and of the rows of nonzero weight (mask_f); with `gate`,
+// only after a reorder in this step, from the rows' culled parts.
+__global__ void k_masks_clear(unsigned long long *__restrict__ mask,
+                              unsigned long long *__restrict__ mask_f, long long n,
+                              const unsigned *__restrict__ gate) {
+  if (gate && gate[1] == 0u) return;
+  for (long long t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    mask[t] = 0ull;
+    mask_f[t] = 0ull;
+  }
+}
+
+__global__ void k_masks_or(const int *__restrict__ row_start, const int *__restrict__ ent,
+                           const int4 *__restrict__ nnear_row, int nrows,
+                           const unsigned char *__restrict__ isforce,
+                           unsigned long long *__restrict__ mask,
+                           unsigned long long *__restrict__ mask_f,
+                           const unsigned *__restrict__ gate) {
+  if (gate && gate[1] == 0u) return;
+  const int stride = gridDim.x * blockDim.x;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += stride) {
+    const int s0 = row_start[r];
+    const int n = nnear_row ? nnear_row[r].z : row_start[r + 1] - s0;  // every culled part
+    const bool f = isforce[r] != 0;
+    for (int k = 0; k < n; k++) {
+      const int code = __ldg(ent + s0 + k);
+      const unsigned long long bit = 1ull << (code & 63);
+      atomicOr(mask + (code >> 6), bit);
+      if (f) atomicOr(mask_f + (code >> 6), bit);
     }
-    int at;
-    const int total = block_scan(__popcll(mk), at, s_warp);
-    for (unsigned long long m = mk; m; m &= m - 1)
-      s_list[at++] = (unsigned short) ((threadIdx.x << 6) | (__ffsll((long long) m) - 1));
-    __syncthreads();
-    for (int t = threadIdx.x; t < total; t += LCH) {
-      const int v = s_list[t], l = v >> 6, kk = v & 63;
-      const float rho = s_U[l] + frac_of(lat, ty, 2, kk).h * s_D[l];
-      site_fp[base + (size_t) (L0 + l) * naz + kk] = fprime32(rho, fp4, nrho, rdrho);
+  }
+}
+
+// the integration-point lists' site ids turned into line codes
+// (element * maxlines + line) << 6 | kk
+__global__ void k_ent_codes(int *__restrict__ ent, long long n, const int *__restrict__ site_base,
+                            int nall_e, const int *__restrict__ etype, const int *__restrict__ nae,
+                            int maxlines) {
+  for (long long t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int sid = ent[t];
+    int lo = 0, hi = nall_e;  // site_base[lo] <= sid < site_base[hi]
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (site_base[mid] <= sid) lo = mid;
+      else hi = mid;
     }
-    if (naz > 64 && threadIdx.x < nl)
-      for (int kk = 64; kk < naz; kk++) {
-        const float rho = s_U[threadIdx.x] + frac_of(lat, ty, 2, kk).h * s_D[threadIdx.x];
-        site_fp[base + (size_t) (L0 + threadIdx.x) * naz + kk] = fprime32(rho, fp4, nrho, rdrho);
-      }
+    const int naz = nae[3 * etype[lo] + 2], nj = sid - site_base[lo];
+    const int L = nj / naz, kk = nj - L * naz;
+    ent[t] = (int) ((((long long) lo * maxlines + L) << 6) | kk);
   }
 }
 
 struct ElemArgs {
-  const float4 *site_q;  // packed site positions of this step
-  const float *site_fp;  // F'(rho) at the sites (EAM force pass)
+  const float4 *line_pos;  // lattice lines of this step (k_lines)
+  const float2 *line_rho;  // nodal-density lines (EAM force pass)
+  const float4 *fp4;       // FP32 F' spline, c0..c2 per knot
+  int nrho;
+  float rdrho;
   const float4 *ip_q;    // packed integration-point positions of this step
   const float4 *ip_h, *ip_l;  // their double-single positions (guard band)
   const float *row_fp;        // F'(rho) at the rows of nonzero weight (EAM force pass)
   const int *etype, *row_elem, *row_first, *node_list;
-  const int *row_start, *ent;  // integration-point lists, row-major (near entries first)
+  const int *row_start, *ent;  // integration-point lists, row-major line codes (near first)
   const int4 *nnear_row;       // culled entry counts per row (null: no culling)
   const unsigned *eflags;      // [0] node displacement^2 since the reorder, [1] reordered now
   int nlocal_e;
@@ -1049,11 +994,8 @@ struct ElemArgs {
   int nforce;
   float cutsq_f, band_lo, band_hi;
   double cutsq;
-  const float2 *node_hl;
   const unsigned char *skip;
-  const int *site_base;
   Lattice lat;
-  int nall_e;
   PackGrid pg;
 };
 
@@ -1135,8 +1077,8 @@ __global__ void k_ip_csr(const int *__restrict__ ipnum, const int *__restrict__ 
 // step) and flags the step (eflags[1]).
 __global__ void k_ip_reorder(const int *__restrict__ row_start, const int *__restrict__ ent,
                              int nrows, const float4 *__restrict__ ip_q,
-                             const float4 *__restrict__ site_q, float g, float4 lim,
-                             int *__restrict__ ent_near, int4 *__restrict__ nnear_row,
+                             const float4 *__restrict__ line_pos, Lattice lat, PackGrid pg,
+                             float4 lim, int *__restrict__ ent_near, int4 *__restrict__ nnear_row,
                              const float2 *__restrict__ node_hl, long long nvals,
                              float2 *__restrict__ node_ref, unsigned *__restrict__ eflags) {
   if (moved_little(eflags)) return;  // reads eflags[0] only, which no block writes
@@ -1151,86 +1093,30 @@ __global__ void k_ip_reorder(const int *__restrict__ row_start, const int *__res
     cell_of(qi, cx, cy, cz);
     const int s0 = row_start[r];
     auto index = [&](int k) { return __ldg(ent + s0 + k); };
-    auto rsq = [&](int sid) {
+    auto rsq = [&](int code) {
+      ds x[3];
+      line_site(line_pos, code, frac_of(lat, 1, 2, code & 63), x);
       float dx, dy, dz;
-      rel_vec(qi, cx, cy, cz, __ldg(site_q + sid), g, dx, dy, dz);
+      rel_vec(qi, cx, cy, cz, pack_u(x[0], x[1], x[2], pg), pg.g, dx, dy, dz);
       return dx * dx + dy * dy + dz * dz;
     };
-    auto put = [&](int at, int sid) { ent_near[s0 + at] = sid; };
+    auto put = [&](int at, int code) { ent_near[s0 + at] = code; };
     nnear_row[r] = reorder_parts(row_start[r + 1] - s0, lim, index, rsq, put);
   }
   for (long long t = blockIdx.x * blockDim.x + threadIdx.x; t < nvals; t += stride)
     node_ref[t] = node_hl[t];
 }
 
-// the near-entry site masks after a reorder in this step (eflags[1]): cleared,
-// then every near entry ORs its site's bit into its line (all rows; rows of
-// nonzero weight also into the force mask)
-__global__ void k_near_masks_clear(unsigned long long *__restrict__ mask,
-                                   unsigned long long *__restrict__ mask_f, long long n,
-                                   const unsigned *__restrict__ eflags) {
-  if (eflags[1] == 0u) return;
-  for (long long t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-    mask[t] = 0ull;
-    mask_f[t] = 0ull;
-  }
-}
-
-__global__ void k_near_masks_or(const int *__restrict__ row_start, const int *__restrict__ ent_near,
-                                const int4 *__restrict__ nnear_row, int nrows,
-                                const unsigned char *__restrict__ isforce,
-                                const int *__restrict__ site_code,
-                                unsigned long long *__restrict__ mask,
-                                unsigned long long *__restrict__ mask_f,
-                                const unsigned *__restrict__ eflags) {
-  if (eflags[1] == 0u) return;
-  const int stride = gridDim.x * blockDim.x;
-  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += stride) {
-    const int s0 = row_start[r], n = nnear_row[r].z;  // every entry of the culled parts
-    const bool f = isforce[r] != 0;
-    for (int k = 0; k < n; k++) {
-      const int code = __ldg(site_code + __ldg(ent_near + s0 + k));
-      const unsigned long long bit = 1ull << (code & 63);
-      atomicOr(mask + (code >> 6), bit);
-      if (f) atomicOr(mask_f + (code >> 6), bit);
-    }
-  }
-}
-
-// per site: its line (element * maxlines + line) << 6 | kk, for the masks above
-__global__ void k_site_code(const int *__restrict__ etype, const int *__restrict__ site_base,
-                            const int *__restrict__ nae, int maxlines, int *__restrict__ code) {
-  const int e = blockIdx.x, ty = etype[e];
-  const int naz = nae[3 * ty + 2], nint = nae[3 * ty] * nae[3 * ty + 1] * naz;
-  const int base = site_base[e];
-  for (int t = threadIdx.x; t < nint; t += blockDim.x) {
-    const int L = t / naz, kk = t - L * naz;
-    code[base + t] = (int) ((((long long) e * maxlines + L) << 6) | kk);
-  }
-}
-
-// the site's double-single position, from its owning element (guard band only)
-__device__ __noinline__ void site_ds_of(const ElemArgs &a, int sid, ds (&x)[3]) {
-  int lo = 0, hi = a.nall_e;  // site_base[lo] <= sid < site_base[hi]
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (__ldg(a.site_base + mid) <= sid) lo = mid;
-    else hi = mid;
-  }
-  const int ty = a.etype[lo];
-  const int nay = a.lat.nae[3 * ty + 1], naz = a.lat.nae[3 * ty + 2];
-  const int nj = sid - a.site_base[lo];
-  const int kk = nj % naz, L = nj / naz;
-  site_ds(a.node_hl + 24 * (size_t) lo, a.lat, ty, L / nay, L % nay, kk, x);
-}
-
-__device__ __noinline__ bool inside_band(const ElemArgs &a, int r, int sid) {
-  ds sx[3];
-  site_ds_of(a, sid, sx);
+// FP64 cutoff test of a guard-band pair from the double-single positions: the
+// integration point's (ip_h + ip_l) and the site's (line data, relative to l0)
+__device__ __noinline__ bool inside_band(const ElemArgs &a, int r, const ds (&x)[3]) {
   const float4 h = __ldg(a.ip_h + r), l = __ldg(a.ip_l + r);
-  const double dx = ((double) h.x + l.x) - ((double) sx[0].h + sx[0].l);
-  const double dy = ((double) h.y + l.y) - ((double) sx[1].h + sx[1].l);
-  const double dz = ((double) h.z + l.z) - ((double) sx[2].h + sx[2].l);
+  const double lx = (double) a.pg.l0h[0] + a.pg.l0l[0];
+  const double ly = (double) a.pg.l0h[1] + a.pg.l0l[1];
+  const double lz = (double) a.pg.l0h[2] + a.pg.l0l[2];
+  const double dx = (((double) h.x + l.x) - lx) - ((double) x[0].h + x[0].l);
+  const double dy = (((double) h.y + l.y) - ly) - ((double) x[1].h + x[1].l);
+  const double dz = (((double) h.z + l.z) - lz) - ((double) x[2].h + x[2].l);
   return dx * dx + dy * dy + dz * dz < a.cutsq;
 }
 
@@ -1282,28 +1168,21 @@ k_ipg(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr, float lj1, 
     cell_of(qi, cx, cy, cz);
     dsacc acc, fx, fy, fz;
     float part = 0.f, px = 0.f, py = 0.f, pz = 0.f;
-    int sn = 0, cnt = 0;
-    float4 qn = qi;
-    float fpn = 0.f;
-    if (lane < n) {
-      sn = __ldg(a.ent + s0 + lane);
-      qn = __ldg(a.site_q + sn);
-      if (EAM && !DENSITY) fpn = __ldg(a.site_fp + sn);
-    }
+    int cn = 0, cnt = 0;
+    if (lane < n) cn = __ldg(a.ent + s0 + lane);
     for (int k = lane; k < n; k += G) {
-      const int sid = sn;
-      const float4 qj = qn;
-      const float fpj = fpn;
-      if (k + G < n) {  // next entry's gathers in flight during this one
-        sn = __ldg(a.ent + s0 + k + G);
-        qn = __ldg(a.site_q + sn);
-        if (EAM && !DENSITY) fpn = __ldg(a.site_fp + sn);
-      }
+      const int code = cn;
+      if (k + G < n) cn = __ldg(a.ent + s0 + k + G);  // the next entry's code in flight
+      // the site from its lattice line: (line data, kk) -> double-single -> packed
+      const ds c = frac_of(a.lat, 1, 2, code & 63);
+      ds x[3];
+      line_site(a.line_pos, code, c, x);
+      const float4 qj = pack_u(x[0], x[1], x[2], a.pg);
       float dx, dy, dz;
       rel_vec(qi, cx, cy, cz, qj, g, dx, dy, dz);
       const float rsq = dx * dx + dy * dy + dz * dz;
       bool in = rsq < a.cutsq_f;
-      if (rsq >= a.band_lo && rsq <= a.band_hi) in = inside_band(a, r, sid);
+      if (rsq >= a.band_lo && rsq <= a.band_hi) in = inside_band(a, r, x);
       if (in) {
         if (EAM) {
           const float recip = rsqrtf(rsq);
@@ -1314,6 +1193,9 @@ k_ipg(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr, float lj1, 
             const float4 c = s_tab[m];
             part += ((c.x * p + c.y) * p + c.z) * p + c.w;
           } else {
+            // the site's density from its nodal-density line, then F'
+            const float2 lr = __ldg(a.line_rho + (code >> 6));
+            const float fpj = fprime32(lr.x + c.h * lr.y, a.fp4, a.nrho, a.rdrho);
             float rhoip, z2, z2p;
             force_spline(s_tab, m, p, rdr, rhoip, z2, z2p);
             const float phi = z2 * recip;
@@ -1541,72 +1423,55 @@ void node_split(const double *nodex, int n, float2 *hl, const float2 *ref, unsig
   check(cudaGetLastError(), "node_split");
 }
 
-void mark_rows(const int *rows, int nlisted, const int *row_start, const int *ent, int *flag,
-               cudaStream_t s) {
-  if (nlisted <= 0) return;
-  k_mark_rows<<<nblk(nlisted, 128), 128, 0, s>>>(rows, nlisted, row_start, ent, flag);
-  check(cudaGetLastError(), "mark_rows");
+void lines(const float2 *node_hl, const int *etype, const Lattice &lat, int max_nax,
+           const unsigned long long *mask, const unsigned long long *mask_near,
+           const unsigned *eflags, int maxlines, const PackGrid &pg, int nelem, float4 *line_pos,
+           cudaStream_t s) {
+  if (nelem <= 0) return;
+  const size_t smem = sizeof(ds) * 12 * (size_t) max_nax;
+  k_lines<<<nelem, LCH, smem, s>>>(node_hl, etype, lat, mask, mask_near, eflags, maxlines, pg,
+                                   line_pos);
+  check(cudaGetLastError(), "lines");
 }
 
-void line_mask(const int *flag, const int *etype, const int *site_base, const int *nae, int nelem,
-               int maxlines, unsigned long long *mask, cudaStream_t s) {
+void line_rho(const double *erho, const int *etype, const Lattice &lat,
+              const unsigned long long *mask, const unsigned long long *mask_near,
+              const unsigned *eflags, int maxlines, int nelem, float2 *out, cudaStream_t s) {
   if (nelem <= 0) return;
-  k_line_mask<<<nblk((long long) nelem * maxlines, 256), 256, 0, s>>>(flag, etype, site_base, nae,
-                                                                    nelem, maxlines, mask);
-  check(cudaGetLastError(), "line_mask");
+  k_line_rho<<<nelem, LCH, 0, s>>>(erho, etype, lat, mask, mask_near, eflags, maxlines, out);
+  check(cudaGetLastError(), "line_rho");
 }
 
-void site_q(const float2 *node_hl, const int *etype, const int *site_base, const Lattice &lat,
-            int max_nax, int max_naz, const unsigned long long *mask,
-            const unsigned long long *mask_near, const unsigned *eflags, int maxlines,
-            const PackGrid &pg, int nelem, float4 *q, cudaStream_t s) {
-  if (nelem <= 0) return;
-  const size_t smem = sizeof(ds) * (12 * (size_t) max_nax + 6 * LCH + max_naz);
-  k_site_q<<<nelem, LCH, smem, s>>>(node_hl, etype, site_base, lat, mask, mask_near, eflags,
-                                    maxlines, pg, q);
-  check(cudaGetLastError(), "site_q");
+void ent_codes(int *ent, long long n, const int *site_base, int nall_e, const int *etype,
+               const int *nae, int maxlines, cudaStream_t s) {
+  if (n <= 0) return;
+  const int grid = persistent_grid((const void *) k_ent_codes, 256, 0, n);
+  k_ent_codes<<<grid, 256, 0, s>>>(ent, n, site_base, nall_e, etype, nae, maxlines);
+  check(cudaGetLastError(), "ent_codes");
 }
 
-void site_fp(const double *erho, const int *etype, const int *site_base, const Lattice &lat,
-             const unsigned long long *mask, const unsigned long long *mask_near,
-             const unsigned *eflags, int maxlines, const float4 *fp4, int nrho, double rdrho,
-             int nelem, float *fp, cudaStream_t s) {
-  if (nelem <= 0) return;
-  k_site_fp<<<nelem, LCH, 0, s>>>(erho, etype, site_base, lat, mask, mask_near, eflags, maxlines,
-                                  fp4, nrho, (float) rdrho, fp);
-  check(cudaGetLastError(), "site_fp");
+void line_masks(const int *row_start, const int *ent, const int4 *nnear_row, int nrows,
+                const unsigned char *isforce, unsigned long long *mask,
+                unsigned long long *mask_f, long long nmask, const unsigned *gate,
+                cudaStream_t s) {
+  if (nrows <= 0 || nmask <= 0) return;
+  const int g1 = persistent_grid((const void *) k_masks_clear, 256, 0, nmask);
+  k_masks_clear<<<g1, 256, 0, s>>>(mask, mask_f, nmask, gate);
+  const int g2 = persistent_grid((const void *) k_masks_or, 256, 0, nrows);
+  k_masks_or<<<g2, 256, 0, s>>>(row_start, ent, nnear_row, nrows, isforce, mask, mask_f, gate);
+  check(cudaGetLastError(), "line_masks");
 }
 
 void ip_reorder(const int *row_start, const int *ent, int nrows, const float4 *ip_q,
-                const float4 *site_q, float g, float cutoff, int *ent_near, int4 *nnear_row,
-                const float2 *node_hl, int nall_e, float2 *node_ref, unsigned *eflags,
-                cudaStream_t s) {
+                const float4 *line_pos, const Lattice &lat, const PackGrid &pg, float cutoff,
+                int *ent_near, int4 *nnear_row, const float2 *node_hl, int nall_e,
+                float2 *node_ref, unsigned *eflags, cudaStream_t s) {
   if (nrows <= 0) return;
   const int grid = persistent_grid((const void *) k_ip_reorder, 256, 0, nrows);
-  k_ip_reorder<<<grid, 256, 0, s>>>(row_start, ent, nrows, ip_q, site_q, g,
+  k_ip_reorder<<<grid, 256, 0, s>>>(row_start, ent, nrows, ip_q, line_pos, lat, pg,
                                     part_limits(cutoff * cutoff, cutoff), ent_near, nnear_row,
                                     node_hl, (long long) nall_e * 24, node_ref, eflags);
   check(cudaGetLastError(), "ip_reorder");
-}
-
-void near_masks(const int *row_start, const int *ent_near, const int4 *nnear_row, int nrows,
-                const unsigned char *isforce, const int *site_code, unsigned long long *mask,
-                unsigned long long *mask_f, long long nmask, const unsigned *eflags,
-                cudaStream_t s) {
-  if (nrows <= 0 || nmask <= 0) return;
-  const int g1 = persistent_grid((const void *) k_near_masks_clear, 256, 0, nmask);
-  k_near_masks_clear<<<g1, 256, 0, s>>>(mask, mask_f, nmask, eflags);
-  const int g2 = persistent_grid((const void *) k_near_masks_or, 256, 0, nrows);
-  k_near_masks_or<<<g2, 256, 0, s>>>(row_start, ent_near, nnear_row, nrows, isforce, site_code,
-                                     mask, mask_f, eflags);
-  check(cudaGetLastError(), "near_masks");
-}
-
-void site_code(const int *etype, const int *site_base, const int *nae, int maxlines, int nelem,
-               int *code, cudaStream_t s) {
-  if (nelem <= 0) return;
-  k_site_code<<<nelem, 128, 0, s>>>(etype, site_base, nae, maxlines, code);
-  check(cudaGetLastError(), "site_code");
 }
 
 void row_q(const int *row_elem, const int *row_jj, const int *etype, const int *int_off,
@@ -1655,11 +1520,10 @@ static void launch_ip(const ElemArgs &a, long long items, int block, int group,
 
 void ip_pass(const MixedElems &m, int pass, const float4 *tab, const EamTables &e, float lj1,
              float lj2, double *out, float2 *outf, cudaStream_t s) {
-  ElemArgs a{m.site_q, m.site_fp, m.ip_q, m.ip_h, m.ip_l, m.row_fp, m.etype, m.row_elem,
-             m.row_first, m.node_list, m.row_start, m.ent, m.nnear_row, m.eflags, m.nlocal_e,
-             m.rows, m.nforce,
-             m.cutsq_f, m.band_lo, m.band_hi, m.cutsq, m.node_hl, m.skip, m.site_base, m.lat,
-             m.nall_e, m.pg};
+  ElemArgs a{m.line_pos, m.line_rho, m.fp4, m.nrho, m.rdrho, m.ip_q, m.ip_h, m.ip_l,
+             m.row_fp, m.etype, m.row_elem, m.row_first, m.node_list, m.row_start, m.ent,
+             m.nnear_row, m.eflags, m.nlocal_e, m.rows, m.nforce, m.cutsq_f, m.band_lo,
+             m.band_hi, m.cutsq, m.skip, m.lat, m.pg};
   if (pass == 0)  // LJ forces
     launch_ip<false, false>(a, m.nforce, m.block, m.group, tab, e, lj1, lj2, out, outf, s);
   else if (pass == 1)  // EAM nodal densities
