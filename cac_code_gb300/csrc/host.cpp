@@ -226,7 +226,9 @@ struct cacg_context {
   DBuf<unsigned char> d_row_isforce;
   long long elist_builds = 0, epart_of = -1;
   bool ereorders_zeroed = false;  // the reorder counter (d_misc slot 15)
-  int mixed_ip_group = 8;  // lanes per integration point ("tune ip_group N")
+  // lanes per integration point ("tune ip_group N"; 0: from the row count, so
+  // that rows x lanes reach the GPU's resident threads)
+  int mixed_ip_group = 0;
   int maxlines = 0, max_nax = 0, max_naz = 0;
   DBuf<double> d_cutsq64, d_stage, d_part, d_lj5;
   std::vector<double> h_lj5;
@@ -730,7 +732,8 @@ void cacg_context::command(const std::string &raw) {
   } else if (c == "tune") {
     // tune block 128|256|512: threads per block of the mixed-precision kernels
     // tune union yes|no: neighbor unions staged in shared memory (EAM atom passes)
-    // tune ip_group 4|8|16: lanes per integration point in the mixed element passes
+    // tune ip_group 0|4|8|16: lanes per integration point in the mixed element
+    //   passes (0: chosen from the row count)
     // tune cull yes|no: the mixed EAM density pass skips list entries that no
     //   displacement since the list reorder can bring within the cutoff
     if (a.size() != 2) fail(CACG_EINVAL, "Illegal tune command");
@@ -740,7 +743,8 @@ void cacg_context::command(const std::string &raw) {
       mixed_block = b;
     } else if (a[0] == "ip_group") {
       int gsz = inumeric(a[1]);
-      if (gsz != 4 && gsz != 8 && gsz != 16) fail(CACG_EINVAL, "tune ip_group takes 4, 8 or 16");
+      if (gsz != 0 && gsz != 4 && gsz != 8 && gsz != 16)
+        fail(CACG_EINVAL, "tune ip_group takes 0, 4, 8 or 16");
       mixed_ip_group = gsz;
     } else if (a[0] == "cull") {
       if (a[1] != "yes" && a[1] != "no") fail(CACG_EINVAL, "tune cull takes yes or no");
@@ -2386,7 +2390,15 @@ void cacg_context::pair_ecompute_mixed() {
   const float eps = 1.0e-4f;
   mixed::MixedElems m{};
   m.block = mixed_block;
-  m.group = mixed_ip_group;
+  if (mixed_ip_group) {
+    m.group = mixed_ip_group;
+  } else {
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const long long want = (long long) nsm * 2048;
+    m.group = (long long) nforce * 4 >= want ? 4 : (long long) nforce * 8 >= want ? 8 : 16;
+  }
   m.line_pos = d_line_pos.p;
   m.ip_q = d_ip_q.p;
   m.ip_h = d_ip_h.p;
