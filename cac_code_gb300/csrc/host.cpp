@@ -220,6 +220,7 @@ struct cacg_context {
   // and whenever a node has moved 0.495 A since
   DBuf<int> d_ent_near;
   bool codes_ok = false;  // the lists fit the line codes of the mixed element passes
+  int code_kb = 6;        // bits of kk in a line code
   DBuf<int4> d_nnear_row;
   DBuf<float2> d_node_ref;
   DBuf<unsigned long long> d_line_mask_n, d_line_mask_nf;
@@ -2159,13 +2160,17 @@ void cacg_context::neighbor_nbuild() {
   // for the mixed passes: the row-major lists as line codes
   // (element * maxlines + line) << 6 | kk, and the lines every row's entries
   // (every force row's) reference, a bit per site
-  codes_ok = max_naz <= 64 && (long long) nall * std::max(maxlines, 1) < (1LL << 25);
+  code_kb = 1;
+  while ((1 << code_kb) < max_naz) code_kb++;
+  codes_ok = max_naz <= 64 && (long long) nall * std::max(maxlines, 1) < (1LL << (31 - code_kb));
   if (codes_ok) {
     const long long nmask = (long long) std::max(nall, 1) * std::max(maxlines, 1);
-    mixed::ent_codes(d_ent.p, h_pin[10], d_site_base.p, nall, d_etype.p, d_nae.p, maxlines, s);
+    mixed::Lattice lat{d_nae.p, d_frac.p, fstride, code_kb};
+    mixed::ent_codes(d_ent.p, h_pin[10], d_site_base.p, nall, d_etype.p, d_nae.p, maxlines, code_kb,
+                     s);
     d_line_mask.ensure(nmask, s);
     d_line_mask_f.ensure(nmask, s);
-    mixed::line_masks(d_row_start.p, d_ent.p, nullptr, nrows, d_row_isforce.p, d_line_mask.p,
+    mixed::line_masks(d_row_start.p, d_ent.p, nullptr, nrows, lat, d_row_isforce.p, d_line_mask.p,
                       d_line_mask_f.p, nmask, nullptr, s);
     launches += 3;
   }
@@ -2335,8 +2340,8 @@ void cacg_context::pair_ecompute_mixed() {
   cudaStream_t s = stream;
   int nall = enlocal + enghost;
   if (!codes_ok)
-    fail(CACG_EINVAL, "mixed element passes: at most 64 sites per lattice line and 2^25 lattice "
-                      "lines (element list build)");
+    fail(CACG_EINVAL, "mixed element passes: at most 64 sites per lattice line and 2^(31 - bits of "
+                      "the sites per line) lattice lines (element list build)");
   double l0[3], g;
   pack_grid(l0, g);
   d_misc.ensure(16, s);
@@ -2368,7 +2373,7 @@ void cacg_context::pair_ecompute_mixed() {
   check(cudaMemsetAsync(d_misc.p + 13, same_e ? 0 : 0x7F, sizeof(int), s), "edmax");
   check(cudaMemsetAsync(d_misc.p + 14, 0, sizeof(int), s), "ereordered");
   mixed::node_split(d_nodex.p, nall, d_node_hl.p, same_e ? d_node_ref.p : nullptr, eflags, s);
-  const mixed::Lattice lat{d_nae.p, d_frac.p, fstride};
+  const mixed::Lattice lat{d_nae.p, d_frac.p, fstride, code_kb};
   // the lattice lines that the scanned entries reference (all referenced
   // lines in a step that reorders)
   mixed::lines(d_node_hl.p, d_etype.p, lat, max_nax, d_line_mask.p,
@@ -2382,7 +2387,7 @@ void cacg_context::pair_ecompute_mixed() {
   mixed::ip_reorder(d_row_start.p, d_ent.p, nrows, d_ip_q.p, d_line_pos.p, lat, pg,
                     (float) std::sqrt(csq_e), d_ent_near.p, d_nnear_row.p, d_node_hl.p, nall,
                     d_node_ref.p, eflags, s);
-  mixed::line_masks(d_row_start.p, d_ent_near.p, d_nnear_row.p, nrows, d_row_isforce.p,
+  mixed::line_masks(d_row_start.p, d_ent_near.p, d_nnear_row.p, nrows, lat, d_row_isforce.p,
                     d_line_mask_n.p, d_line_mask_nf.p, nmask, eflags, s);
   launches += 6;
   epart_of = elist_builds;

@@ -305,6 +305,7 @@ struct Lattice {
   const int *nae;
   const float2 *frac;
   int fstride;
+  int kb = 6;  // bits of the site index kk in a list entry's line code
 };
 struct MixedElems {
   const float4 *line_pos;  // lattice lines of this step: U, D double-single (3 float4)
@@ -317,7 +318,7 @@ struct MixedElems {
   const float *row_fp;        // FP32 F'(rho) at the rows of nonzero weight (EAM force pass)
   const int *etype, *row_elem, *row_first, *node_list;
   // integration-point lists, row-major: line codes (element * maxlines + line)
-  // << 6 | kk, each row's culling parts in order
+  // << lat.kb | kk, each row's culling parts in order
   const int *row_start, *ent;
   const int4 *nnear_row = nullptr;  // culled entry counts per row (null: no culling)
   const unsigned *eflags = nullptr;  // [node displacement^2 bits, reordered this step]
@@ -353,11 +354,11 @@ void line_rho(const double *erho, const int *etype, const Lattice &lat,
               const unsigned *eflags, int maxlines, int nelem, float2 *out, cudaStream_t s);
 // the integration-point lists' site ids turned into line codes in place
 void ent_codes(int *ent, long long n, const int *site_base, int nall_e, const int *etype,
-               const int *nae, int maxlines, cudaStream_t s);
+               const int *nae, int maxlines, int kb, cudaStream_t s);
 // line masks (bit kk per line) of the rows' entries (all rows; force rows);
 // with nnear_row, of the culled parts; with gate, only after a reorder
 void line_masks(const int *row_start, const int *ent, const int4 *nnear_row, int nrows,
-                const unsigned char *isforce, unsigned long long *mask,
+                const Lattice &lat, const unsigned char *isforce, unsigned long long *mask,
                 unsigned long long *mask_f, long long nmask, const unsigned *gate,
                 cudaStream_t s);
 // displacement culling of the integration-point lists: reorder (gated on the

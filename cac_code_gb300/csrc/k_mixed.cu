@@ -837,11 +837,17 @@ __device__ __forceinline__ void column_ds(const float2 *nx, ds a, int d, ds (&E)
 constexpr int LCH = 128;
 
 // line data: U.x, U.y | U.z, D.x | D.y, D.z as double-single pairs
-__device__ __forceinline__ void line_site(const float4 *__restrict__ lp, int code, ds c,
+// list entries are line codes: line << lat.kb | kk
+__device__ __forceinline__ int code_line(const Lattice &lat, int code) { return code >> lat.kb; }
+__device__ __forceinline__ int code_kk(const Lattice &lat, int code) {
+  return code & ((1 << lat.kb) - 1);
+}
+
+__device__ __forceinline__ void line_site(const float4 *__restrict__ lp, int line, ds c,
                                           ds (&x)[3]) {
-  const float4 a = __ldg(lp + 3 * (size_t) (code >> 6));
-  const float4 b = __ldg(lp + 3 * (size_t) (code >> 6) + 1);
-  const float4 d = __ldg(lp + 3 * (size_t) (code >> 6) + 2);
+  const float4 a = __ldg(lp + 3 * (size_t) line);
+  const float4 b = __ldg(lp + 3 * (size_t) line + 1);
+  const float4 d = __ldg(lp + 3 * (size_t) line + 2);
   x[0] = ds_madd(c, ds{b.z, b.w}, ds{a.x, a.y});
   x[1] = ds_madd(c, ds{d.x, d.y}, ds{a.z, a.w});
   x[2] = ds_madd(c, ds{d.z, d.w}, ds{b.x, b.y});
@@ -937,7 +943,7 @@ __global__ void k_masks_clear(unsigned long long *__restrict__ mask,
 }
 
 __global__ void k_masks_or(const int *__restrict__ row_start, const int *__restrict__ ent,
-                           const int4 *__restrict__ nnear_row, int nrows,
+                           const int4 *__restrict__ nnear_row, int nrows, Lattice lat,
                            const unsigned char *__restrict__ isforce,
                            unsigned long long *__restrict__ mask,
                            unsigned long long *__restrict__ mask_f,
@@ -950,9 +956,9 @@ __global__ void k_masks_or(const int *__restrict__ row_start, const int *__restr
     const bool f = isforce[r] != 0;
     for (int k = 0; k < n; k++) {
       const int code = __ldg(ent + s0 + k);
-      const unsigned long long bit = 1ull << (code & 63);
-      atomicOr(mask + (code >> 6), bit);
-      if (f) atomicOr(mask_f + (code >> 6), bit);
+      const unsigned long long bit = 1ull << code_kk(lat, code);
+      atomicOr(mask + code_line(lat, code), bit);
+      if (f) atomicOr(mask_f + code_line(lat, code), bit);
     }
   }
 }
@@ -961,7 +967,7 @@ __global__ void k_masks_or(const int *__restrict__ row_start, const int *__restr
 // (element * maxlines + line) << 6 | kk
 __global__ void k_ent_codes(int *__restrict__ ent, long long n, const int *__restrict__ site_base,
                             int nall_e, const int *__restrict__ etype, const int *__restrict__ nae,
-                            int maxlines) {
+                            int maxlines, int kb) {
   for (long long t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     const int sid = ent[t];
     int lo = 0, hi = nall_e;  // site_base[lo] <= sid < site_base[hi]
@@ -972,7 +978,7 @@ __global__ void k_ent_codes(int *__restrict__ ent, long long n, const int *__res
     }
     const int naz = nae[3 * etype[lo] + 2], nj = sid - site_base[lo];
     const int L = nj / naz, kk = nj - L * naz;
-    ent[t] = (int) ((((long long) lo * maxlines + L) << 6) | kk);
+    ent[t] = (int) ((((long long) lo * maxlines + L) << kb) | kk);
   }
 }
 
@@ -1095,7 +1101,7 @@ __global__ void k_ip_reorder(const int *__restrict__ row_start, const int *__res
     auto index = [&](int k) { return __ldg(ent + s0 + k); };
     auto rsq = [&](int code) {
       ds x[3];
-      line_site(line_pos, code, frac_of(lat, 1, 2, code & 63), x);
+      line_site(line_pos, code_line(lat, code), frac_of(lat, 1, 2, code_kk(lat, code)), x);
       float dx, dy, dz;
       rel_vec(qi, cx, cy, cz, pack_u(x[0], x[1], x[2], pg), pg.g, dx, dy, dz);
       return dx * dx + dy * dy + dz * dz;
@@ -1174,9 +1180,9 @@ k_ipg(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr, float lj1, 
       const int code = cn;
       if (k + G < n) cn = __ldg(a.ent + s0 + k + G);  // the next entry's code in flight
       // the site from its lattice line: (line data, kk) -> double-single -> packed
-      const ds c = frac_of(a.lat, 1, 2, code & 63);
+      const ds c = frac_of(a.lat, 1, 2, code_kk(a.lat, code));
       ds x[3];
-      line_site(a.line_pos, code, c, x);
+      line_site(a.line_pos, code_line(a.lat, code), c, x);
       const float4 qj = pack_u(x[0], x[1], x[2], a.pg);
       float dx, dy, dz;
       rel_vec(qi, cx, cy, cz, qj, g, dx, dy, dz);
@@ -1194,7 +1200,7 @@ k_ipg(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr, float lj1, 
             part += ((c.x * p + c.y) * p + c.z) * p + c.w;
           } else {
             // the site's density from its nodal-density line, then F'
-            const float2 lr = __ldg(a.line_rho + (code >> 6));
+            const float2 lr = __ldg(a.line_rho + code_line(a.lat, code));
             const float fpj = fprime32(lr.x + c.h * lr.y, a.fp4, a.nrho, a.rdrho);
             float rhoip, z2, z2p;
             force_spline(s_tab, m, p, rdr, rhoip, z2, z2p);
@@ -1443,22 +1449,23 @@ void line_rho(const double *erho, const int *etype, const Lattice &lat,
 }
 
 void ent_codes(int *ent, long long n, const int *site_base, int nall_e, const int *etype,
-               const int *nae, int maxlines, cudaStream_t s) {
+               const int *nae, int maxlines, int kb, cudaStream_t s) {
   if (n <= 0) return;
   const int grid = persistent_grid((const void *) k_ent_codes, 256, 0, n);
-  k_ent_codes<<<grid, 256, 0, s>>>(ent, n, site_base, nall_e, etype, nae, maxlines);
+  k_ent_codes<<<grid, 256, 0, s>>>(ent, n, site_base, nall_e, etype, nae, maxlines, kb);
   check(cudaGetLastError(), "ent_codes");
 }
 
 void line_masks(const int *row_start, const int *ent, const int4 *nnear_row, int nrows,
-                const unsigned char *isforce, unsigned long long *mask,
+                const Lattice &lat, const unsigned char *isforce, unsigned long long *mask,
                 unsigned long long *mask_f, long long nmask, const unsigned *gate,
                 cudaStream_t s) {
   if (nrows <= 0 || nmask <= 0) return;
   const int g1 = persistent_grid((const void *) k_masks_clear, 256, 0, nmask);
   k_masks_clear<<<g1, 256, 0, s>>>(mask, mask_f, nmask, gate);
   const int g2 = persistent_grid((const void *) k_masks_or, 256, 0, nrows);
-  k_masks_or<<<g2, 256, 0, s>>>(row_start, ent, nnear_row, nrows, isforce, mask, mask_f, gate);
+  k_masks_or<<<g2, 256, 0, s>>>(row_start, ent, nnear_row, nrows, lat, isforce, mask, mask_f,
+                                gate);
   check(cudaGetLastError(), "line_masks");
 }
 
