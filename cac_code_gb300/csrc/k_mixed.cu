@@ -538,8 +538,12 @@ k_eam_force_union(AtomArgs a, UnionArgs u, const float4 *__restrict__ ftab, int 
   }
 }
 
-// force table per knot: FTAB_W float4 (force_spline)
-__global__ void __launch_bounds__(512, 2)
+// force table per knot: FTAB_W float4 (force_spline).  For large systems one
+// 1024-thread block per SM: the 64 KB table is held once per SM, which leaves
+// the unified L1/shared memory's rest to the neighbor gathers (smaller systems
+// keep the tuned block size, for more blocks than SMs).
+constexpr int FORCE_BLOCK = 1024;
+__global__ void __launch_bounds__(FORCE_BLOCK, 1)
 k_eam_force_atoms(AtomArgs a, const float4 *__restrict__ ftab, int nr, float rdr,
                   const float *__restrict__ fp, double *__restrict__ f) {
   extern __shared__ float4 s_tab[];  // 3 float4 per knot
@@ -1406,8 +1410,12 @@ void eam_force_atoms(const MixedAtoms &m, const float4 *ftab, const EamTables &e
   AtomArgs a{m.x, m.xq, m.qg, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
              m.band_hi, m.cutsq, m.snum, m.slist, nullptr, nullptr};
   size_t smem = sizeof(float4) * FTAB_W * (e.nr + 1);
-  int g = persistent_grid((const void *) k_eam_force_atoms, m.block, smem, m.nlocal);
-  k_eam_force_atoms<<<g, m.block, smem, s>>>(a, ftab, e.nr, (float) e.rdr, fp, f);
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int block = m.nlocal >= 4LL * nsm * FORCE_BLOCK ? FORCE_BLOCK : m.block;
+  int g = persistent_grid((const void *) k_eam_force_atoms, block, smem, m.nlocal);
+  k_eam_force_atoms<<<g, block, smem, s>>>(a, ftab, e.nr, (float) e.rdr, fp, f);
   check(cudaGetLastError(), "eam_force_atoms_mixed");
 }
 
