@@ -1132,9 +1132,10 @@ __device__ __noinline__ bool inside_band(const ElemArgs &a, int r, const ds (&x)
 
 // G lanes per integration point, each taking every G-th entry of the row's
 // list; the lanes' sums meet by shuffles.  DENSITY: node rows -> erho (EAM);
-// otherwise rows of nonzero weight -> forces (LJ or EAM).  Every entry is
-// tested: a 16-byte gather of the packed site, the FP32 cutoff test, and in
-// the guard band the FP64 test on the double-single positions.
+// otherwise rows of nonzero weight -> forces (LJ or EAM).  Every scanned entry
+// is a line code: the site is formed from its lattice line (double-single,
+// then packed), tested in FP32, and in the guard band in FP64 on the
+// double-single positions.
 template <bool EAM, bool DENSITY, int G>
 __global__ void __launch_bounds__(512, 2)
 k_ipg(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr, float lj1, float lj2,
