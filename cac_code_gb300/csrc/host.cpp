@@ -271,8 +271,8 @@ struct cacg_context {
   double sur_tol = 1e-4, sur_dist = 0.0;
   DBuf<double> d_nodex0;
   bool have_x0 = false;
-  DBuf<int> d_far, d_far_rows, d_static_rows;
-  int nfar = 0, nfar_rows = 0, nstatic_rows = 0;
+  DBuf<int> d_far;
+  int nfar = 0;
   DBuf<unsigned char> d_skip;
   DBuf<unsigned short> d_sfeat;  // bf16 features [nfar][64]
   DBuf<float> d_smean, d_sspread, d_sraw;
@@ -539,8 +539,6 @@ cacg_context::~cacg_context() {
   d_slot.release();
   d_sslot.release();
   d_far.release();
-  d_far_rows.release();
-  d_static_rows.release();
   d_skip.release();
   d_sfeat.release();
   d_smean.release();
@@ -2589,7 +2587,7 @@ void cacg_context::surrogate_samples(float *x, float *t) {
 void cacg_context::surrogate_attach(cacg_mlp_t *m, double tol, double dist) {
   invalidate_graph();
   sur = nullptr;
-  nfar = nfar_rows = nstatic_rows = 0;
+  nfar = 0;
   if (!m) return;
   if (mode != CACG_MIXED) fail(CACG_EINVAL, "the surrogate runs in the mixed-precision element pass");
   if (!elists_built || !setup_done) fail(CACG_ESTATE, "attach the surrogate after the lists are built");
@@ -2629,7 +2627,7 @@ void cacg_context::surrogate_attach(cacg_mlp_t *m, double tol, double dist) {
   std::vector<std::vector<int>> bins((size_t) nb[0] * nb[1] * nb[2]);
   for (int i = 0; i < nlocal; i++)
     bins[((size_t) cell(x4[i].x, 0) * nb[1] + cell(x4[i].y, 1)) * nb[2] + cell(x4[i].z, 2)].push_back(i);
-  std::vector<int> far, is_far(enlocal, 0);
+  std::vector<int> far;
   for (int e = 0; e < enlocal; e++) {
     const double lim = dist + rad[e];
     const double *c = &cx[3 * e];
@@ -2661,29 +2659,10 @@ void cacg_context::surrogate_attach(cacg_mlp_t *m, double tol, double dist) {
         }
     if (!near_) {
       far.push_back(e);
-      is_far[e] = 1;
-    }
-  }
-  // rows: node rows of every element plus force rows of the near elements
-  // (static), force rows of the far elements (filtered per step)
-  std::vector<int> st, fr;
-  for (int e = 0; e < enlocal; e++) {
-    const int ty = h_etype[e];
-    for (int jj = 0; jj < numint[ty]; jj++) {
-      const int r = h_row_first[e] + jj;
-      bool node = false;
-      for (int q = 0; q < NPE; q++) node = node || node_list[ty * NPE + q] == jj;
-      const bool force = weight[ty][jj] != 0.0;
-      if (node || (force && !is_far[e])) st.push_back(r);
-      if (force && is_far[e]) fr.push_back(r);
     }
   }
   nfar = (int) far.size();
-  nfar_rows = (int) fr.size();
-  nstatic_rows = (int) st.size();
   upload(d_far, far.empty() ? std::vector<int>{0} : far, s);
-  upload(d_far_rows, fr.empty() ? std::vector<int>{0} : fr, s);
-  upload(d_static_rows, st.empty() ? std::vector<int>{0} : st, s);
   d_skip.ensure(std::max(enlocal, 1), s);
   check(cudaMemsetAsync(d_skip.p, 0, std::max(enlocal, 1), s), "skip");
   d_scount.ensure(2, s);
