@@ -316,6 +316,13 @@ struct cacg_context {
   // CUDA graph of a step without a rebuild decision (captured once, replayed
   // until a rebuild, a reallocation or a configuration change)
   int mixed_block = 512;  // threads per block of the mixed persistent kernels ("tune block N")
+  // a mixed step as two chains on two streams ("tune streams yes|no"): atoms
+  // and element sites do not interact, so the atom chain (initial
+  // integration, ghost update, density and force passes) and the element
+  // chain meet only before the fixes and the final integration
+  bool two_streams = true;
+  cudaStream_t astream = nullptr;  // the atom chain's stream (higher priority)
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   // neighbor unions staged in shared memory ("tune union yes"): bit-identical
   // to the direct passes; at C2 they run at 8 warps per SM and lose to the
   // direct kernels' 32 (1.71 vs 0.77 ms for the density pass), so off by default
@@ -437,7 +444,7 @@ struct cacg_context {
   void comm_setup();
   void setup_bins();
   void borders();
-  void forward_comm();
+  void forward_comm(int which = 3);  // 1 atoms, 2 elements, 3 both
   void pbc();
   void neighbor_build();
   void neighbor_ebuild();
@@ -447,7 +454,7 @@ struct cacg_context {
   void pair_compute_mixed(int pass);
   void pair_ecompute_mixed();
   void pair_ecompute();
-  void nve_initial();
+  void nve_initial(int which = 3);
   void nve_final();
   void compute_thermo(double *out);
   void compute_centro(double *out);
@@ -484,6 +491,12 @@ struct cacg_context {
   int decide();
   void rebuild();
   void run(int n);
+  void force_passes(long long b);  // b: phase-mark base of the step, < 0 for none
+  bool fork_ok() const {
+    return two_streams && mode == CACG_MIXED && !timing && nlocal > 0 && enlocal > 0;
+  }
+  template <class A, class E>
+  void forked(A atoms, E elems);
   void setup();
   void require_init() {
     if (!inited) init();
@@ -565,6 +578,9 @@ cacg_context::~cacg_context() {
   for (auto &e : pev) cudaEventDestroy(e);
   if (gexec) cudaGraphExecDestroy(gexec);
   if (h_pin) cudaFreeHost(h_pin);
+  if (fork_ev) cudaEventDestroy(fork_ev);
+  if (join_ev) cudaEventDestroy(join_ev);
+  if (astream) cudaStreamDestroy(astream);
   if (stream) cudaStreamDestroy(stream);
 }
 
@@ -735,6 +751,7 @@ void cacg_context::command(const std::string &raw) {
     //   passes (0: chosen from the row count)
     // tune cull yes|no: the mixed EAM density pass skips list entries that no
     //   displacement since the list reorder can bring within the cutoff
+    // tune streams yes|no: a mixed step's atom and element chains on two streams
     if (a.size() != 2) fail(CACG_EINVAL, "Illegal tune command");
     if (a[0] == "block") {
       int b = inumeric(a[1]);
@@ -751,6 +768,10 @@ void cacg_context::command(const std::string &raw) {
     } else if (a[0] == "union") {
       if (a[1] != "yes" && a[1] != "no") fail(CACG_EINVAL, "tune union takes yes or no");
       mixed_union = a[1] == "yes";
+    } else if (a[0] == "streams") {
+      if (a[1] != "yes" && a[1] != "no") fail(CACG_EINVAL, "tune streams takes yes or no");
+      two_streams = a[1] == "yes";
+      invalidate_graph();
     } else {
       fail(CACG_EINVAL, "Illegal tune command");
     }
@@ -1986,7 +2007,7 @@ void cacg_context::borders() {
 
 // CommBrick::forward_comm / eforward_comm: ghost positions from their sources,
 // swap by swap (comm_brick.cpp:1017-1112)
-void cacg_context::forward_comm() {
+void cacg_context::forward_comm(int which) {
   if (!swaps.empty() && swaps.size() <= (size_t) MAX_SWAPS) {
     SwapChain ca{}, ce{};
     ca.n = ce.n = (int) swaps.size();
@@ -1995,22 +2016,22 @@ void cacg_context::forward_comm() {
       ce.first[k] = swaps[k].efirstrecv;
       for (int d = 0; d < 3; d++) ca.d[k][d] = ce.d[k][d] = swaps[k].d[d];
     }
-    if (nlocal && nghost) {
+    if ((which & 1) && nlocal && nghost) {
       launch_forward_atoms_all(d_x.p, d_send.p, nlocal, nghost, ca, stream);
       launches++;
     }
-    if (enlocal && enghost) {
+    if ((which & 2) && enlocal && enghost) {
       launch_forward_elems_all(d_nodex.p, d_esend.p, enlocal, enghost, ce, stream);
       launches++;
     }
     return;
   }
   for (auto &w : swaps) {
-    if (nlocal && w.nsend) {
+    if ((which & 1) && nlocal && w.nsend) {
       launch_forward_atoms(d_x.p, d_send.p + w.send_off, w.nsend, w.firstrecv, w.d[0], w.d[1], w.d[2], stream);
       launches++;
     }
-    if (enlocal && w.ensend) {
+    if ((which & 2) && enlocal && w.ensend) {
       launch_forward_elems(d_nodex.p, d_esend.p + w.esend_off, w.ensend, w.efirstrecv, w.d[0], w.d[1], w.d[2], stream);
       launches++;
     }
@@ -2846,12 +2867,17 @@ void cacg_context::nve_scales(TypeScale &a, TypeScale &e) const {
   }
 }
 
-void cacg_context::nve_initial() {
+void cacg_context::nve_initial(int which) {
   TypeScale a, e;
   nve_scales(a, e);
-  launch_nve_atoms_initial(d_x.p, d_v.p, d_f.p, d_type.p, a, nlocal, dt, stream);
-  launch_nve_nodes_initial(d_ex.p, d_nodex.p, d_nodev.p, d_nodef.p, d_etype.p, e, enlocal, dt, stream);
-  launches += 2;
+  if (which & 1) {
+    launch_nve_atoms_initial(d_x.p, d_v.p, d_f.p, d_type.p, a, nlocal, dt, stream);
+    launches++;
+  }
+  if (which & 2) {
+    launch_nve_nodes_initial(d_ex.p, d_nodex.p, d_nodev.p, d_nodef.p, d_etype.p, e, enlocal, dt, stream);
+    launches++;
+  }
 }
 
 void cacg_context::nve_final() {
@@ -2960,14 +2986,25 @@ void cacg_context::run(int n) {
         continue;
       }
       mark(b);
-      nve_initial();
-      forward_comm();
-      mark(b + 1);
-      pair_compute_pass(1);
-      mark(b + 2);
-      pair_compute_pass(2);
-      mark(b + 3);
-      pair_ecompute();
+      if (fork_ok()) {
+        forked(
+            [&] {
+              nve_initial(1);
+              forward_comm(1);
+              pair_compute_pass(1);
+              pair_compute_pass(2);
+            },
+            [&] {
+              nve_initial(2);
+              forward_comm(2);
+              pair_ecompute();
+            });
+      } else {
+        nve_initial();
+        forward_comm();
+        mark(b + 1);
+        force_passes((long long) b);
+      }
       post_force();
       mark(b + 4);
       nve_final();
@@ -2981,20 +3018,25 @@ void cacg_context::run(int n) {
     if (nflag == 0) forward_comm();
     else rebuild();
     mark(b + 1);
-    pair_compute_pass(1);
-    mark(b + 2);
-    pair_compute_pass(2);
-    mark(b + 3);
-    pair_ecompute();
+    force_passes((long long) b);
     post_force();  // verlet.cpp:206
     mark(b + 4);
     nve_final();
     deform_step();
     mark(b + 5);
   }
+  // the packed-range counter is read back behind the last step, so that one
+  // synchronisation serves both
+  const bool oob_read = mode == CACG_MIXED && d_misc.p && oob_zeroed;
+  if (oob_read)
+    check(cudaMemcpyAsync(h_pin + 9, d_misc.p + 9, sizeof(int), cudaMemcpyDeviceToHost, stream), "oob");
   check(cudaEventRecord(ev[1], stream), "ev");
   check(cudaEventSynchronize(ev[1]), "ev sync");
-  check_packed_range();
+  if (oob_read && h_pin[9]) {
+    const int nout = h_pin[9];
+    check(cudaMemsetAsync(d_misc.p + 9, 0, sizeof(int), stream), "oob reset");
+    fail(CACG_EINVAL, "%d atoms or element sites outside the packed-coordinate range of the mixed passes", nout);
+  }
   float ms = 0;
   cudaEventElapsedTime(&ms, ev[0], ev[1]);
   t_ms[0] = ms;
@@ -3009,6 +3051,63 @@ void cacg_context::run(int n) {
       }
     }
   }
+}
+
+// The atom chain and the element chain of a mixed step, from this point on the
+// handle's stream: the atom chain on a second stream of higher priority (it is
+// the longer one), the element chain on the handle's stream, which waits for
+// the atom chain before its next operation.  Both streams take part in a
+// graph capture of the handle's stream.
+template <class A, class E>
+void cacg_context::forked(A atoms, E elems) {
+  if (!astream) {
+    int least = 0, greatest = 0;
+    check(cudaDeviceGetStreamPriorityRange(&least, &greatest), "stream priorities");
+    check(cudaStreamCreateWithPriority(&astream, cudaStreamNonBlocking, greatest), "atom stream");
+  }
+  if (!fork_ev) check(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming), "fork event");
+  if (!join_ev) check(cudaEventCreateWithFlags(&join_ev, cudaEventDisableTiming), "join event");
+  check(cudaEventRecord(fork_ev, stream), "fork");
+  check(cudaStreamWaitEvent(astream, fork_ev, 0), "fork wait");
+  const cudaStream_t main_stream = stream;
+  stream = astream;
+  try {
+    atoms();
+  } catch (...) {
+    stream = main_stream;
+    cudaEventRecord(join_ev, astream);
+    cudaStreamWaitEvent(stream, join_ev, 0);
+    throw;
+  }
+  stream = main_stream;
+  check(cudaEventRecord(join_ev, astream), "join");
+  try {
+    elems();
+  } catch (...) {
+    cudaStreamWaitEvent(stream, join_ev, 0);
+    throw;
+  }
+  check(cudaStreamWaitEvent(stream, join_ev, 0), "join wait");
+}
+
+// Pair::compute for atoms (density, then force pass) and Pair::ecompute for
+// elements: in order on the handle's stream, marking the phases (b + 2,
+// b + 3; b < 0: no marks), or as two chains (forked) when that is on.
+void cacg_context::force_passes(long long b) {
+  if (fork_ok()) {
+    forked(
+        [&] {
+          pair_compute_pass(1);
+          pair_compute_pass(2);
+        },
+        [&] { pair_ecompute(); });
+    return;
+  }
+  pair_compute_pass(1);
+  if (b >= 0) mark((size_t) b + 2);
+  pair_compute_pass(2);
+  if (b >= 0) mark((size_t) b + 3);
+  pair_ecompute();
 }
 
 // The body of a step without a rebuild decision, captured into a CUDA graph.
@@ -3026,11 +3125,24 @@ bool cacg_context::capture_plain_step() {
   const unsigned long long e0 = dbuf_epoch();
   bool ok = true;
   try {
-    nve_initial();
-    forward_comm();
-    pair_compute_pass(1);
-    pair_compute_pass(2);
-    pair_ecompute();
+    if (fork_ok()) {
+      forked(
+          [&] {
+            nve_initial(1);
+            forward_comm(1);
+            pair_compute_pass(1);
+            pair_compute_pass(2);
+          },
+          [&] {
+            nve_initial(2);
+            forward_comm(2);
+            pair_ecompute();
+          });
+    } else {
+      nve_initial();
+      forward_comm();
+      force_passes(-1);
+    }
     post_force();
     nve_final();
   } catch (...) {

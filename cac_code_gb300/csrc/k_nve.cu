@@ -9,59 +9,62 @@ namespace {
 
 inline int nblk(long long n, int t) { return (int) ((n + t - 1) / t); }
 
-// FixNVE::initial_integrate, fix_nve.cpp:54-98 (per-type mass branch)
+// FixNVE::initial_integrate, fix_nve.cpp:54-98 (per-type mass branch).  One
+// thread per component, so the v and f loads of a warp are 256 contiguous
+// bytes; x is the padded double4 array.
 __global__ void k_nve_atoms_initial(double4 *__restrict__ x, double *__restrict__ v,
                                     const double *__restrict__ f, const int *__restrict__ type,
                                     TypeScale dtfm_t, int n, double dtv) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  double dtfm = dtfm_t.v[type[i]];
-  double vx = v[3 * i] + dtfm * f[3 * i];
-  double vy = v[3 * i + 1] + dtfm * f[3 * i + 1];
-  double vz = v[3 * i + 2] + dtfm * f[3 * i + 2];
-  v[3 * i] = vx;
-  v[3 * i + 1] = vy;
-  v[3 * i + 2] = vz;
-  double4 p = x[i];
-  p.x = p.x + dtv * vx;
-  p.y = p.y + dtv * vy;
-  p.z = p.z + dtv * vz;
-  x[i] = p;
+  const long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+  if (t >= 3LL * n) return;
+  const long long i = t / 3;
+  const int d = (int) (t - 3 * i);
+  const double vv = v[t] + dtfm_t.v[type[i]] * f[t];
+  v[t] = vv;
+  double *xp = reinterpret_cast<double *>(x) + 4 * i + d;
+  *xp = *xp + dtv * vv;
 }
 
-// FixNVE::final_integrate, fix_nve.cpp:181-212
+// FixNVE::final_integrate, fix_nve.cpp:181-212 (one thread per component)
 __global__ void k_nve_atoms_final(double *__restrict__ v, const double *__restrict__ f,
                                   const int *__restrict__ type, TypeScale dtfm_t, int n) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  double dtfm = dtfm_t.v[type[i]];
-  v[3 * i] = v[3 * i] + dtfm * f[3 * i];
-  v[3 * i + 1] = v[3 * i + 1] + dtfm * f[3 * i + 1];
-  v[3 * i + 2] = v[3 * i + 2] + dtfm * f[3 * i + 2];
+  const long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+  if (t >= 3LL * n) return;
+  v[t] = v[t] + dtfm_t.v[type[t / 3]] * f[t];
 }
 
 // FixNVE::einitial_integrate, fix_nve.cpp:100-157: nodal mass M_e/8, then the
-// centre is recomputed as the mean of the nodes
+// centre is recomputed as the mean of the nodes.  Eight threads per element,
+// one per node (its three components contiguous, so a warp's loads cover four
+// elements' 768 bytes); the centre sums the nodes in node order through
+// shuffles within the eight lanes, as the reference's loop adds them.
+static_assert(NPE == 8, "eight nodes per element");
 __global__ void k_nve_nodes_initial(double *__restrict__ ex, double *__restrict__ nodex,
                                     double *__restrict__ nodev,
                                     const double *__restrict__ nodef,
                                     const int *__restrict__ etype, TypeScale dtfm_t, int n,
                                     double dtv) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  double dtfm = dtfm_t.v[etype[i]];
-  double c[3] = {0.0, 0.0, 0.0};
-  for (int q = 0; q < NPE; q++) {
+  const long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+  const long long i = t >> 3;
+  const int q = (int) (t & 7);
+  const bool live = i < n;
+  double xn[3] = {0.0, 0.0, 0.0};
+  if (live) {
+    const double dtfm = dtfm_t.v[etype[i]];
     for (int d = 0; d < 3; d++) {
-      size_t k = 24 * (size_t) i + 3 * q + d;
-      double vv = nodev[k] + dtfm * nodef[k];
+      const size_t k = 24 * (size_t) i + 3 * q + d;
+      const double vv = nodev[k] + dtfm * nodef[k];
       nodev[k] = vv;
-      nodex[k] = nodex[k] + dtv * vv;
+      xn[d] = nodex[k] + dtv * vv;
+      nodex[k] = xn[d];
     }
   }
-  for (int q = 0; q < NPE; q++)
-    for (int d = 0; d < 3; d++) c[d] += nodex[24 * (size_t) i + 3 * q + d];
-  for (int d = 0; d < 3; d++) ex[3 * i + d] = c[d] / NPE;
+  // every lane of the warp takes part in the shuffles (the grid is whole warps)
+  for (int d = 0; d < 3; d++) {
+    double c = 0.0;
+    for (int r = 0; r < NPE; r++) c += __shfl_sync(0xffffffffu, xn[d], r, NPE);
+    if (live && q == 0) ex[3 * i + d] = c / NPE;
+  }
 }
 
 // FixNVE::efinal_integrate, fix_nve.cpp:216-242
@@ -163,14 +166,14 @@ __global__ void k_fma_loop(double *out, int iters) {
 void launch_nve_atoms_initial(double4 *x, double *v, const double *f, const int *type,
                               const TypeScale &dtfm, int n, double dtv, cudaStream_t s) {
   if (n <= 0) return;
-  k_nve_atoms_initial<<<nblk(n, 256), 256, 0, s>>>(x, v, f, type, dtfm, n, dtv);
+  k_nve_atoms_initial<<<nblk(3LL * n, 256), 256, 0, s>>>(x, v, f, type, dtfm, n, dtv);
   check(cudaGetLastError(), "nve_atoms_initial");
 }
 
 void launch_nve_atoms_final(double *v, const double *f, const int *type, const TypeScale &dtfm,
                             int n, cudaStream_t s) {
   if (n <= 0) return;
-  k_nve_atoms_final<<<nblk(n, 256), 256, 0, s>>>(v, f, type, dtfm, n);
+  k_nve_atoms_final<<<nblk(3LL * n, 256), 256, 0, s>>>(v, f, type, dtfm, n);
   check(cudaGetLastError(), "nve_atoms_final");
 }
 
@@ -178,7 +181,7 @@ void launch_nve_nodes_initial(double *ex, double *nodex, double *nodev, const do
                               const int *etype, const TypeScale &dtfm, int n, double dtv,
                               cudaStream_t s) {
   if (n <= 0) return;
-  k_nve_nodes_initial<<<nblk(n, 128), 128, 0, s>>>(ex, nodex, nodev, nodef, etype, dtfm, n, dtv);
+  k_nve_nodes_initial<<<nblk((long long) n * NPE, 256), 256, 0, s>>>(ex, nodex, nodev, nodef, etype, dtfm, n, dtv);
   check(cudaGetLastError(), "nve_nodes_initial");
 }
 
