@@ -443,10 +443,12 @@ class System:
         self._ok(self._L.cacg_set_timing(self.h, 1 if enable else 0))
 
     def timing(self) -> np.ndarray:
-        """[total, integrate+comm/rebuild, atom pass 1, atom pass 2, element, final]"""
+        """[total, integrate+comm/rebuild, atom pass 1, atom pass 2, element, final,
+        EAM atom density kernel alone] in ms (all but the total: eager steps with
+        timing on)"""
         ms = np.zeros(8)
         self._ok(self._L.cacg_get_timing(self.h, _d(ms), 8))
-        return ms[:6]
+        return ms[:7]
 
     def put_atoms(self, x, v):
         """Push host-owned owned-atom x, v (float64 [nlocal][3], C order)."""

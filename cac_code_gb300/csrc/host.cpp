@@ -351,9 +351,25 @@ struct cacg_context {
     graph_valid = false;
     eager_since = 0;
   }
-  void plain_step();
   bool capture_plain_step();
   std::vector<cudaEvent_t> pev;  // per-step phase events
+  // with timing on: events around the EAM atom density kernel of each step
+  std::vector<cudaEvent_t> kev;
+  std::vector<char> kev_used;
+  size_t cur_step = 0;
+  bool capturing = false;
+  void kmark(int k) {
+    if (!timing || capturing) return;
+    const size_t at = 2 * cur_step + k;
+    while (kev.size() <= at) {
+      cudaEvent_t e;
+      check(cudaEventCreate(&e), "event");
+      kev.push_back(e);
+      kev_used.push_back(0);
+    }
+    check(cudaEventRecord(kev[at], stream), "event record");
+    kev_used[at] = 1;
+  }
   std::vector<char> pev_used;  // marks recorded in the current run
   void mark(size_t k) {
     if (!timing) return;
@@ -576,6 +592,7 @@ cacg_context::~cacg_context() {
   for (auto &e : ev)
     if (e) cudaEventDestroy(e);
   for (auto &e : pev) cudaEventDestroy(e);
+  for (auto &e : kev) cudaEventDestroy(e);
   if (gexec) cudaGraphExecDestroy(gexec);
   if (h_pin) cudaFreeHost(h_pin);
   if (fork_ev) cudaEventDestroy(fork_ev);
@@ -2237,8 +2254,10 @@ void cacg_context::pair_compute_pass(int pass) {
   if (pass == 1) {
     d_rho.ensure(nall, s);
     d_fp.ensure(nall, s);
+    kmark(0);
     if (exact) fp64_exact::eam_rho_atoms(d_x.p, num, lst, stride, nlocal, e, d_rho.p, d_fp.p, s);
     else fp64_fma::eam_rho_atoms(d_x.p, d_xh.p, num, lst, stride, nlocal, e, cp, d_rho.p, d_fp.p, s);
+    kmark(1);
     // forward_comm_pair: ghost fp = owner fp (comm_brick.cpp:941-971)
     launch_copy_root(d_fp.p, 1, d_root.p, nlocal, nghost, s);
     launches += 2;
@@ -2338,8 +2357,11 @@ void cacg_context::pair_compute_mixed(int pass) {
     if (mixed_union)
       mixed::eam_rho_union(m, d_union_j.p, d_union_n.p, d_slot.p, d_sslot.p, d_rhor_val4.p, e,
                            d_fp4.p, d_rho.p, d_fpf.p, s);
-    else
+    else {
+      kmark(0);
       mixed::eam_rho_atoms(m, d_rhor_val4.p, e, d_fp4.p, d_rho.p, d_fpf.p, s);
+      kmark(1);
+    }
     launch_copy_root(d_fpf.p, 1, d_root.p, nlocal, nghost, s);
     launches += 2;
   } else {
@@ -2871,11 +2893,12 @@ void cacg_context::nve_initial(int which) {
   TypeScale a, e;
   nve_scales(a, e);
   if (which & 1) {
-    launch_nve_atoms_initial(d_x.p, d_v.p, d_f.p, d_type.p, a, nlocal, dt, stream);
+    launch_nve_atoms_initial(d_x.p, d_v.p, d_f.p, d_type.p, a, nlocal, dt, fast(), stream);
     launches++;
   }
   if (which & 2) {
-    launch_nve_nodes_initial(d_ex.p, d_nodex.p, d_nodev.p, d_nodef.p, d_etype.p, e, enlocal, dt, stream);
+    launch_nve_nodes_initial(d_ex.p, d_nodex.p, d_nodev.p, d_nodef.p, d_etype.p, e, enlocal, dt, fast(),
+                             stream);
     launches++;
   }
 }
@@ -2883,8 +2906,8 @@ void cacg_context::nve_initial(int which) {
 void cacg_context::nve_final() {
   TypeScale a, e;
   nve_scales(a, e);
-  launch_nve_atoms_final(d_v.p, d_f.p, d_type.p, a, nlocal, stream);
-  launch_nve_nodes_final(d_nodev.p, d_nodef.p, d_etype.p, e, enlocal, stream);
+  launch_nve_atoms_final(d_v.p, d_f.p, d_type.p, a, nlocal, fast(), stream);
+  launch_nve_nodes_final(d_nodev.p, d_nodef.p, d_etype.p, e, enlocal, fast(), stream);
   launches += 2;
 }
 
@@ -2965,8 +2988,11 @@ void cacg_context::run(int n) {
     if (!e) check(cudaEventCreate(&e), "event");
   check(cudaEventRecord(ev[0], stream), "ev");
   const size_t P = 6;  // phase marks per step
+  std::fill(kev_used.begin(), kev_used.end(), 0);
+  cur_step = 0;
   for (int step = 0; step < n; step++) {
     size_t b = (size_t) step * P;
+    cur_step = (size_t) step;
     ntimestep++;
     // a step that reaches no rebuild decision (Neighbor::decide returns 0
     // without checking) replays the captured graph of the previous such step
@@ -3049,8 +3075,16 @@ void cacg_context::run(int n) {
         check(cudaEventElapsedTime(&d, pev[b + k], pev[b + k + 1]), "elapsed");
         t_ms[1 + k] += d;
       }
+      // [6]: the EAM atom density kernel alone
+      const size_t kb = 2 * (size_t) step;
+      float d = 0;
+      if (kb + 1 < kev.size() && kev_used[kb] && kev_used[kb + 1]) {
+        check(cudaEventElapsedTime(&d, kev[kb], kev[kb + 1]), "elapsed");
+        t_ms[6] += d;
+      }
     }
   }
+  cur_step = 0;
 }
 
 // The atom chain and the element chain of a mixed step, from this point on the
@@ -3124,6 +3158,7 @@ bool cacg_context::capture_plain_step() {
   const long long l0 = launches;
   const unsigned long long e0 = dbuf_epoch();
   bool ok = true;
+  capturing = true;
   try {
     if (fork_ok()) {
       forked(
@@ -3148,6 +3183,7 @@ bool cacg_context::capture_plain_step() {
   } catch (...) {
     ok = false;
   }
+  capturing = false;
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaStreamEndCapture(s, &g);
   if (e != cudaSuccess || !g || !ok || dbuf_epoch() != e0) ok = false;

@@ -480,13 +480,16 @@ void to_float(const double *src, long long n, float *dst, cudaStream_t s);
 struct TypeScale {
   double v[MAXT + 1];
 };
+// fused: one FMA per update (FP64 FMA and mixed modes); else the exact mode's
+// multiply-then-add
 void launch_nve_atoms_initial(double4 *x, double *v, const double *f, const int *type,
-                              const TypeScale &dtfm, int n, double dtv, cudaStream_t s);
+                              const TypeScale &dtfm, int n, double dtv, bool fused,
+                              cudaStream_t s);
 void launch_nve_atoms_final(double *v, const double *f, const int *type, const TypeScale &dtfm,
-                            int n, cudaStream_t s);
+                            int n, bool fused, cudaStream_t s);
 void launch_nve_nodes_initial(double *ex, double *nodex, double *nodev, const double *nodef,
                               const int *etype, const TypeScale &dtfm, int n, double dtv,
-                              cudaStream_t s);
+                              bool fused, cudaStream_t s);
 // fix setforce / fix viscous on the items (atoms, or elements x 8 nodes) whose
 // group mask has `bit` (fix_setforce.cpp:107-161, fix_viscous.cpp:73-123)
 void launch_setforce(double *f, const int *mask, int n, int per_item, int bit, const int *set,
@@ -496,7 +499,7 @@ void launch_affine(double *x, int n, int stride, double olo, double nlo, double 
 void launch_viscous(double *f, const double *v, const int *mask, int n, int per_item, int bit,
                     double gamma, cudaStream_t s);
 void launch_nve_nodes_final(double *nodev, const double *nodef, const int *etype,
-                            const TypeScale &dtfm, int n, cudaStream_t s);
+                            const TypeScale &dtfm, int n, bool fused, cudaStream_t s);
 void launch_check_distance(const double4 *x, const double *xhold, int n,
                            const double *nodex, const double *nodexhold, int ne,
                            double triggersq, int *flag, cudaStream_t s);

@@ -1119,15 +1119,20 @@ __global__ void k_ip_reorder(const int *__restrict__ row_start, const int *__res
 
 // FP64 cutoff test of a guard-band pair from the double-single positions: the
 // integration point's (ip_h + ip_l) and the site's (line data, relative to l0)
-__device__ __noinline__ bool inside_band(const ElemArgs &a, int r, const ds (&x)[3]) {
-  const float4 h = __ldg(a.ip_h + r), l = __ldg(a.ip_l + r);
-  const double lx = (double) a.pg.l0h[0] + a.pg.l0l[0];
-  const double ly = (double) a.pg.l0h[1] + a.pg.l0l[1];
-  const double lz = (double) a.pg.l0h[2] + a.pg.l0l[2];
-  const double dx = (((double) h.x + l.x) - lx) - ((double) x[0].h + x[0].l);
-  const double dy = (((double) h.y + l.y) - ly) - ((double) x[1].h + x[1].l);
-  const double dz = (((double) h.z + l.z) - lz) - ((double) x[2].h + x[2].l);
-  return dx * dx + dy * dy + dz * dz < a.cutsq;
+// (arguments by value: a reference to the kernel's arrays would put them in
+// local memory on every iteration of the caller's loop)
+__device__ __noinline__ bool inside_band(const float4 *__restrict__ ip_h,
+                                         const float4 *__restrict__ ip_l, PackGrid pg,
+                                         double cutsq, int r, float x0h, float x0l, float x1h,
+                                         float x1l, float x2h, float x2l) {
+  const float4 h = __ldg(ip_h + r), l = __ldg(ip_l + r);
+  const double lx = (double) pg.l0h[0] + pg.l0l[0];
+  const double ly = (double) pg.l0h[1] + pg.l0l[1];
+  const double lz = (double) pg.l0h[2] + pg.l0l[2];
+  const double dx = (((double) h.x + l.x) - lx) - ((double) x0h + x0l);
+  const double dy = (((double) h.y + l.y) - ly) - ((double) x1h + x1l);
+  const double dz = (((double) h.z + l.z) - lz) - ((double) x2h + x2l);
+  return dx * dx + dy * dy + dz * dz < cutsq;
 }
 
 // G lanes per integration point, each taking every G-th entry of the row's
@@ -1193,7 +1198,9 @@ k_ipg(ElemArgs a, const float4 *__restrict__ tab, int nr, float rdr, float lj1, 
       rel_vec(qi, cx, cy, cz, qj, g, dx, dy, dz);
       const float rsq = dx * dx + dy * dy + dz * dz;
       bool in = rsq < a.cutsq_f;
-      if (rsq >= a.band_lo && rsq <= a.band_hi) in = inside_band(a, r, x);
+      if (rsq >= a.band_lo && rsq <= a.band_hi)
+        in = inside_band(a.ip_h, a.ip_l, a.pg, a.cutsq, r, x[0].h, x[0].l, x[1].h, x[1].l,
+                         x[2].h, x[2].l);
       if (in) {
         if (EAM) {
           const float recip = rsqrtf(rsq);

@@ -1,6 +1,7 @@
 // Velocity-Verlet for atoms and element nodes, rebuild check and element-size
-// reduction (sm_103a).  Compiled without contraction so the updates are the
-// reference's own multiply-then-add sequences (FixNVE, fix_nve.cpp:54-242).
+// reduction (sm_103a).  Compiled without contraction so the exact mode's
+// updates are the reference's own multiply-then-add sequences (FixNVE,
+// fix_nve.cpp:54-242); the other modes fuse them explicitly.
 #include "internal.h"
 
 namespace cacg {
@@ -9,9 +10,28 @@ namespace {
 
 inline int nblk(long long n, int t) { return (int) ((n + t - 1) / t); }
 
+// dt/(2m) of a type: a select over constant indices, so that the table stays
+// in the parameter space (a runtime index into a by-value parameter array
+// would copy it to each thread's local memory)
+__device__ __forceinline__ double type_scale(const TypeScale &t, int ty) {
+  double d = t.v[0];
+#pragma unroll
+  for (int k = 1; k <= MAXT; k++) d = ty == k ? t.v[k] : d;
+  return d;
+}
+
+// a + b * c: the reference's multiply-then-add, or one fused multiply-add in
+// the FP64 (FMA) and mixed modes (FP64 instructions are scarce on this GPU:
+// the integrators are bound by their FP64 issue, not by HBM)
+template <bool FUSED>
+__device__ __forceinline__ double madd(double a, double b, double c) {
+  return FUSED ? fma(b, c, a) : a + b * c;
+}
+
 // FixNVE::initial_integrate, fix_nve.cpp:54-98 (per-type mass branch).  One
 // thread per component, so the v and f loads of a warp are 256 contiguous
 // bytes; x is the padded double4 array.
+template <bool FUSED>
 __global__ void k_nve_atoms_initial(double4 *__restrict__ x, double *__restrict__ v,
                                     const double *__restrict__ f, const int *__restrict__ type,
                                     TypeScale dtfm_t, int n, double dtv) {
@@ -19,62 +39,69 @@ __global__ void k_nve_atoms_initial(double4 *__restrict__ x, double *__restrict_
   if (t >= 3LL * n) return;
   const long long i = t / 3;
   const int d = (int) (t - 3 * i);
-  const double vv = v[t] + dtfm_t.v[type[i]] * f[t];
+  const double vv = madd<FUSED>(v[t], type_scale(dtfm_t, type[i]), f[t]);
   v[t] = vv;
   double *xp = reinterpret_cast<double *>(x) + 4 * i + d;
-  *xp = *xp + dtv * vv;
+  *xp = madd<FUSED>(*xp, dtv, vv);
 }
 
 // FixNVE::final_integrate, fix_nve.cpp:181-212 (one thread per component)
+template <bool FUSED>
 __global__ void k_nve_atoms_final(double *__restrict__ v, const double *__restrict__ f,
                                   const int *__restrict__ type, TypeScale dtfm_t, int n) {
   const long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x;
   if (t >= 3LL * n) return;
-  v[t] = v[t] + dtfm_t.v[type[t / 3]] * f[t];
+  v[t] = madd<FUSED>(v[t], type_scale(dtfm_t, type[t / 3]), f[t]);
 }
 
 // FixNVE::einitial_integrate, fix_nve.cpp:100-157: nodal mass M_e/8, then the
-// centre is recomputed as the mean of the nodes.  Eight threads per element,
-// one per node (its three components contiguous, so a warp's loads cover four
-// elements' 768 bytes); the centre sums the nodes in node order through
-// shuffles within the eight lanes, as the reference's loop adds them.
+// centre is recomputed as the mean of the nodes.  One thread per node for the
+// update (its three components contiguous, so a warp's loads cover four
+// elements' 768 bytes); the new positions of the block's 32 elements are
+// staged in shared memory and one warp sums each element's nodes in node
+// order, as the reference's loop adds them (one summing thread per element
+// keeps the FP64 additions at 24 per element).
 static_assert(NPE == 8, "eight nodes per element");
-__global__ void k_nve_nodes_initial(double *__restrict__ ex, double *__restrict__ nodex,
-                                    double *__restrict__ nodev,
-                                    const double *__restrict__ nodef,
-                                    const int *__restrict__ etype, TypeScale dtfm_t, int n,
-                                    double dtv) {
-  const long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+constexpr int NODE_BLOCK = 256, NODE_ELEMS = NODE_BLOCK / NPE;
+template <bool FUSED>
+__global__ void __launch_bounds__(NODE_BLOCK)
+k_nve_nodes_initial(double *__restrict__ ex, double *__restrict__ nodex,
+                    double *__restrict__ nodev, const double *__restrict__ nodef,
+                    const int *__restrict__ etype, TypeScale dtfm_t, int n, double dtv) {
+  __shared__ double sx[NODE_ELEMS][3 * NPE + 1];
+  const long long t = blockIdx.x * (long long) NODE_BLOCK + threadIdx.x;
   const long long i = t >> 3;
-  const int q = (int) (t & 7);
-  const bool live = i < n;
-  double xn[3] = {0.0, 0.0, 0.0};
-  if (live) {
-    const double dtfm = dtfm_t.v[etype[i]];
+  const int q = (int) (t & 7), le = threadIdx.x >> 3;
+  if (i < n) {
+    const double dtfm = type_scale(dtfm_t, etype[i]);
     for (int d = 0; d < 3; d++) {
       const size_t k = 24 * (size_t) i + 3 * q + d;
-      const double vv = nodev[k] + dtfm * nodef[k];
+      const double vv = madd<FUSED>(nodev[k], dtfm, nodef[k]);
       nodev[k] = vv;
-      xn[d] = nodex[k] + dtv * vv;
-      nodex[k] = xn[d];
+      const double xn = madd<FUSED>(nodex[k], dtv, vv);
+      nodex[k] = xn;
+      sx[le][3 * q + d] = xn;
     }
   }
-  // every lane of the warp takes part in the shuffles (the grid is whole warps)
-  for (int d = 0; d < 3; d++) {
-    double c = 0.0;
-    for (int r = 0; r < NPE; r++) c += __shfl_sync(0xffffffffu, xn[d], r, NPE);
-    if (live && q == 0) ex[3 * i + d] = c / NPE;
+  __syncthreads();
+  const long long e = blockIdx.x * (long long) NODE_ELEMS + threadIdx.x;
+  if (threadIdx.x < NODE_ELEMS && e < n) {
+    for (int d = 0; d < 3; d++) {
+      double c = 0.0;
+      for (int r = 0; r < NPE; r++) c += sx[threadIdx.x][3 * r + d];
+      ex[3 * e + d] = c / NPE;
+    }
   }
 }
 
 // FixNVE::efinal_integrate, fix_nve.cpp:216-242
+template <bool FUSED>
 __global__ void k_nve_nodes_final(double *__restrict__ nodev, const double *__restrict__ nodef,
                                   const int *__restrict__ etype, TypeScale dtfm_t, int n) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * 24) return;
   int i = t / 24;
-  double dtfm = dtfm_t.v[etype[i]];
-  nodev[t] = nodev[t] + dtfm * nodef[t];
+  nodev[t] = madd<FUSED>(nodev[t], type_scale(dtfm_t, etype[i]), nodef[t]);
 }
 
 // Neighbor::check_distance, neighbor.cpp:1176-1217
@@ -164,31 +191,37 @@ __global__ void k_fma_loop(double *out, int iters) {
 }  // namespace
 
 void launch_nve_atoms_initial(double4 *x, double *v, const double *f, const int *type,
-                              const TypeScale &dtfm, int n, double dtv, cudaStream_t s) {
+                              const TypeScale &dtfm, int n, double dtv, bool fused,
+                              cudaStream_t s) {
   if (n <= 0) return;
-  k_nve_atoms_initial<<<nblk(3LL * n, 256), 256, 0, s>>>(x, v, f, type, dtfm, n, dtv);
+  auto k = fused ? k_nve_atoms_initial<true> : k_nve_atoms_initial<false>;
+  k<<<nblk(3LL * n, 256), 256, 0, s>>>(x, v, f, type, dtfm, n, dtv);
   check(cudaGetLastError(), "nve_atoms_initial");
 }
 
 void launch_nve_atoms_final(double *v, const double *f, const int *type, const TypeScale &dtfm,
-                            int n, cudaStream_t s) {
+                            int n, bool fused, cudaStream_t s) {
   if (n <= 0) return;
-  k_nve_atoms_final<<<nblk(3LL * n, 256), 256, 0, s>>>(v, f, type, dtfm, n);
+  auto k = fused ? k_nve_atoms_final<true> : k_nve_atoms_final<false>;
+  k<<<nblk(3LL * n, 256), 256, 0, s>>>(v, f, type, dtfm, n);
   check(cudaGetLastError(), "nve_atoms_final");
 }
 
 void launch_nve_nodes_initial(double *ex, double *nodex, double *nodev, const double *nodef,
                               const int *etype, const TypeScale &dtfm, int n, double dtv,
-                              cudaStream_t s) {
+                              bool fused, cudaStream_t s) {
   if (n <= 0) return;
-  k_nve_nodes_initial<<<nblk((long long) n * NPE, 256), 256, 0, s>>>(ex, nodex, nodev, nodef, etype, dtfm, n, dtv);
+  auto k = fused ? k_nve_nodes_initial<true> : k_nve_nodes_initial<false>;
+  k<<<nblk((long long) n * NPE, NODE_BLOCK), NODE_BLOCK, 0, s>>>(ex, nodex, nodev, nodef, etype,
+                                                                  dtfm, n, dtv);
   check(cudaGetLastError(), "nve_nodes_initial");
 }
 
 void launch_nve_nodes_final(double *nodev, const double *nodef, const int *etype,
-                            const TypeScale &dtfm, int n, cudaStream_t s) {
+                            const TypeScale &dtfm, int n, bool fused, cudaStream_t s) {
   if (n <= 0) return;
-  k_nve_nodes_final<<<nblk((long long) n * 24, 256), 256, 0, s>>>(nodev, nodef, etype, dtfm, n);
+  auto k = fused ? k_nve_nodes_final<true> : k_nve_nodes_final<false>;
+  k<<<nblk((long long) n * 24, 256), 256, 0, s>>>(nodev, nodef, etype, dtfm, n);
   check(cudaGetLastError(), "nve_nodes_final");
 }
 

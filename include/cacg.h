@@ -241,6 +241,10 @@ int cacg_set_timing(cacg_handle h, int enable);
    a reallocation or any command; on by default.  Phase timing covers the
    steps run eagerly only. */
 int cacg_set_graphs(cacg_handle h, int enable);
+/* Milliseconds of the last cacg_run: [0] all steps (device events), and with
+   timing on, summed over the eagerly run steps: [1] integration + ghost update
+   or rebuild, [2] atom pass 1, [3] atom pass 2, [4] element passes and fixes,
+   [5] final integration, [6] the EAM atom density kernel alone.  n <= 8. */
 int cacg_get_timing(cacg_handle h, double *ms, int n);
 /* Device-time of a FP64 fused-multiply-add loop on this GPU, for the FP64 roof:
    returns achieved FP64 FLOP/s in *flops. */
