@@ -835,7 +835,7 @@ __device__ __forceinline__ void column_ds(const float2 *nx, ds a, int d, ds (&E)
 // give P = E0 - l0, Q = E1 - E0, R = E2 - E0 and S = (E3 - E2) - (E1 - E0),
 // so that a line (ii, jj) starts at U = P + b Q and steps D = R + b S
 // (b = jj / (ny - 1)); its site kk is U + c D (c = kk / (nz - 1)), all in
-// double-single.  One block per element writes U and D of every line that a
+// double-single.  One warp per element writes U and D of every line that a
 // scanned list entry references (48 bytes a line); the integration-point
 // passes evaluate the sites from them.
 constexpr int LCH = 128;
@@ -861,17 +861,22 @@ __global__ void __launch_bounds__(LCH)
 k_lines(const float2 *__restrict__ node_hl, const int *__restrict__ etype, Lattice lat,
         const unsigned long long *__restrict__ line_mask,
         const unsigned long long *__restrict__ line_mask_near, const unsigned *__restrict__ eflags,
-        int maxlines, PackGrid pg, float4 *__restrict__ line_pos) {
-  extern __shared__ ds s_col[];  // [nax][3][4]: P, Q, R, S
-  __shared__ float2 s_nx[24];
-  const int e = blockIdx.x;
+        int maxlines, PackGrid pg, int nelem, int max_nax, float4 *__restrict__ line_pos) {
+  // one warp per element: [nax][3][4] P, Q, R, S of the warp's element
+  extern __shared__ ds s_cols[];
+  __shared__ float2 s_nodes[LCH / 32][24];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int e = blockIdx.x * (LCH / 32) + w;
+  if (e >= nelem) return;
+  ds *s_col = s_cols + (size_t) w * 12 * max_nax;
+  float2 *s_nx = s_nodes[w];
   const int ty = etype[e];
   const int *nae = lat.nae;
   const int nax = nae[3 * ty], nay = nae[3 * ty + 1];
-  if (threadIdx.x < 24) s_nx[threadIdx.x] = node_hl[24 * (size_t) e + threadIdx.x];
-  __syncthreads();
+  if (lane < 24) s_nx[lane] = node_hl[24 * (size_t) e + lane];
+  __syncwarp();
   const ds l0[3] = {{pg.l0h[0], pg.l0l[0]}, {pg.l0h[1], pg.l0l[1]}, {pg.l0h[2], pg.l0l[2]}};
-  for (int q = threadIdx.x; q < 3 * nax; q += blockDim.x) {
+  for (int q = lane; q < 3 * nax; q += 32) {
     const int ii = q / 3, d = q % 3;
     ds E[4];
     column_ds(s_nx, frac_of(lat, ty, 0, ii), d, E);
@@ -882,12 +887,12 @@ k_lines(const float2 *__restrict__ node_hl, const int *__restrict__ etype, Latti
     o[2] = ds_sub(E[2], E[0]);
     o[3] = ds_sub(ds_sub(E[3], E[2]), q1);
   }
-  __syncthreads();
+  __syncwarp();
   // while culling holds only the lines of the rows' near entries are needed
   const unsigned long long *lm =
       (line_mask_near && cull_ok(eflags) ? line_mask_near : line_mask) + (size_t) e * maxlines;
   float4 *out = line_pos + 3 * (size_t) e * maxlines;
-  for (int L = threadIdx.x; L < nax * nay; L += blockDim.x) {
+  for (int L = lane; L < nax * nay; L += 32) {
     if (lm[L] == 0ull) continue;
     const int ii = L / nay, jj = L - ii * nay;
     const ds b = frac_of(lat, ty, 1, jj);
@@ -906,23 +911,28 @@ k_lines(const float2 *__restrict__ node_hl, const int *__restrict__ etype, Latti
 
 // Nodal-density lines, FP32: rho at site kk of line (ii, jj) is B + c (T - B)
 // with B, T the bilinear values of the nodal densities on the z = -1 and z = +1
-// faces (pair_eam.cpp:1060-1065: rho_s = sum_k N_k erho_k).  One block per
+// faces (pair_eam.cpp:1060-1065: rho_s = sum_k N_k erho_k).  One warp per
 // element, the lines that a scanned force-row entry references.
 __global__ void __launch_bounds__(LCH)
 k_line_rho(const double *__restrict__ erho, const int *__restrict__ etype, Lattice lat,
            const unsigned long long *__restrict__ line_mask,
            const unsigned long long *__restrict__ line_mask_near,
-           const unsigned *__restrict__ eflags, int maxlines, float2 *__restrict__ line_rho) {
-  __shared__ float s_er[NPE];
-  const int e = blockIdx.x;
+           const unsigned *__restrict__ eflags, int maxlines, int nelem,
+           float2 *__restrict__ line_rho) {
+  // one warp per element
+  __shared__ float s_erho[LCH / 32][NPE];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int e = blockIdx.x * (LCH / 32) + w;
+  if (e >= nelem) return;
+  float *s_er = s_erho[w];
   const int ty = etype[e];
   const int nax = lat.nae[3 * ty], nay = lat.nae[3 * ty + 1];
-  if (threadIdx.x < NPE) s_er[threadIdx.x] = (float) erho[NPE * (size_t) e + threadIdx.x];
-  __syncthreads();
+  if (lane < NPE) s_er[lane] = (float) erho[NPE * (size_t) e + lane];
+  __syncwarp();
   const unsigned long long *lm =
       (line_mask_near && cull_ok(eflags) ? line_mask_near : line_mask) + (size_t) e * maxlines;
   float2 *out = line_rho + (size_t) e * maxlines;
-  for (int L = threadIdx.x; L < nax * nay; L += blockDim.x) {
+  for (int L = lane; L < nax * nay; L += 32) {
     if (lm[L] == 0ull) continue;
     const int ii = L / nay, jj = L - ii * nay;
     const float a = frac_of(lat, ty, 0, ii).h, b = frac_of(lat, ty, 1, jj).h;
@@ -1450,9 +1460,10 @@ void lines(const float2 *node_hl, const int *etype, const Lattice &lat, int max_
            const unsigned *eflags, int maxlines, const PackGrid &pg, int nelem, float4 *line_pos,
            cudaStream_t s) {
   if (nelem <= 0) return;
-  const size_t smem = sizeof(ds) * 12 * (size_t) max_nax;
-  k_lines<<<nelem, LCH, smem, s>>>(node_hl, etype, lat, mask, mask_near, eflags, maxlines, pg,
-                                   line_pos);
+  const size_t smem = sizeof(ds) * 12 * (size_t) max_nax * (LCH / 32);
+  const int grid = (nelem + LCH / 32 - 1) / (LCH / 32);
+  k_lines<<<grid, LCH, smem, s>>>(node_hl, etype, lat, mask, mask_near, eflags, maxlines, pg,
+                                  nelem, max_nax, line_pos);
   check(cudaGetLastError(), "lines");
 }
 
@@ -1460,7 +1471,8 @@ void line_rho(const double *erho, const int *etype, const Lattice &lat,
               const unsigned long long *mask, const unsigned long long *mask_near,
               const unsigned *eflags, int maxlines, int nelem, float2 *out, cudaStream_t s) {
   if (nelem <= 0) return;
-  k_line_rho<<<nelem, LCH, 0, s>>>(erho, etype, lat, mask, mask_near, eflags, maxlines, out);
+  const int grid = (nelem + LCH / 32 - 1) / (LCH / 32);
+  k_line_rho<<<grid, LCH, 0, s>>>(erho, etype, lat, mask, mask_near, eflags, maxlines, nelem, out);
   check(cudaGetLastError(), "line_rho");
 }
 
