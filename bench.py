@@ -422,9 +422,9 @@ def run_ours(a, ws, rank, local):
                     (cs1["surrogate_accepted"] - cs0["surrogate_accepted"]) / ev if ev else 0.0)
         setv(mode, a.sur_tol if use_sur else None)
 
-    # e2e through the C ABI with host-resident state: push x,v (atoms + nodes)
-    # from pinned host memory, one step, read the new x,v (atoms + nodes) back,
-    # every step
+    # e2e through the C ABI with host-resident state: x,v (atoms + nodes) in
+    # from pinned host memory, one step, the new x,v (atoms + nodes) back out,
+    # every step (cacg_run_host)
     e2e = None
     if not a.no_e2e:
         try:
@@ -452,20 +452,17 @@ def run_ours(a, ws, rank, local):
         barrier(ws)
         t0 = time.perf_counter()
         for _ in range(e_steps):
-            s.put_atoms(hx, hv)
-            s.put_nodes(hnx, hnv)
-            s.run(1)
-            s.get_state_into(hx, hv, None)
-            s.get_nodes_into(hnx, hnv)
+            s.run_host(1, hx, hv, hnx, hnv)
         e_wall = time.perf_counter() - t0
         e_wall = allmax(ws, e_wall)
         e2e = {"value": ws * sites * e_steps / e_wall, "unit": UNIT,
                "h2d_bytes_per_step": int(hx.nbytes + hv.nbytes + hnx.nbytes + hnv.nbytes),
                "d2h_bytes_per_step": int(hx.nbytes + hv.nbytes + hnx.nbytes + hnv.nbytes),
                "steps": e_steps,
-               "note": "state round trip per step: x, v of atoms and nodes in and out through "
-                       "the C ABI (pinned host buffers; host<->device copies measured at "
-                       "~200 GB/s on this box)"}
+               "note": "state round trip per step: x, v of atoms and nodes in and out of "
+                       "pinned host buffers through cacg_run_host, one call per step (copies "
+                       "overlap the step where the data allow; host<->device copies run at "
+                       "~200 GB/s each way on this box)"}
 
     # energy drift of the headline mode: FP64 energies before and after an NVE
     # run (the potential is not smoothed at the cutoff: phi(rc) = -0.0189 eV,

@@ -52,6 +52,7 @@ EXPORTED = [
     "cacg_gemm_bf16_tn", "cacg_surrogate_reference", "cacg_surrogate_samples",
     "cacg_surrogate_attach", "cacg_compute_centro", "cacg_dump_xyz", "cacg_dump_elements",
     "cacg_fix_post_force", "cacg_get_box", "cacg_set_graphs", "cacg_set_group",
+    "cacg_run_host",
 ]
 
 
@@ -87,6 +88,7 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
     lib.cacg_command.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
     lib.cacg_file.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
     lib.cacg_run.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.cacg_run_host.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _dp, _dp]
     lib.cacg_set_precision.argtypes = [ctypes.c_void_p, ctypes.c_int]
     lib.cacg_set_timing.argtypes = [ctypes.c_void_p, ctypes.c_int]
     lib.cacg_set_graphs.argtypes = [ctypes.c_void_p, ctypes.c_int]
@@ -329,6 +331,18 @@ class System:
 
     def run(self, n: int):
         self._ok(self._L.cacg_run(self.h, n))
+
+    def run_host(self, n: int, x, v, nodex, nodev):
+        """Advance host-resident state n steps: x, v (float64 [nlocal][3]) and
+        nodex, nodev (float64 [enlocal][8][3]), C order, updated in place."""
+        for a, tail in ((x, (3,)), (v, (3,)), (nodex, (8, 3)), (nodev, (8, 3))):
+            if (a.dtype != np.float64 or a.shape[1:] != tail or not a.flags["C_CONTIGUOUS"]
+                    or not a.flags["WRITEABLE"]):
+                raise ValueError("run_host wants writeable float64 C-ordered arrays "
+                                 "[nlocal][3] and [enlocal][8][3]")
+        if x.shape != v.shape or nodex.shape != nodev.shape:
+            raise ValueError("run_host: x, v (and nodex, nodev) differ in shape")
+        self._ok(self._L.cacg_run_host(self.h, n, _d(x), _d(v), _d(nodex), _d(nodev)))
 
     # ---- state out ----
     def counts(self) -> Dict[str, int]:

@@ -323,6 +323,11 @@ struct cacg_context {
   bool two_streams = true;
   cudaStream_t astream = nullptr;  // the atom chain's stream (higher priority)
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  // host-resident stepping (run_host): copy-in and copy-out streams and the
+  // events that order the copies against the step's two chains
+  cudaStream_t cin = nullptr, cout_s = nullptr;
+  cudaEvent_t ev_ain = nullptr, ev_nin = nullptr, ev_xout = nullptr, ev_nxout = nullptr,
+              ev_nvout = nullptr, ev_end = nullptr;
   // neighbor unions staged in shared memory ("tune union yes"): bit-identical
   // to the direct passes; at C2 they run at 8 warps per SM and lose to the
   // direct kernels' 32 (1.71 vs 0.77 ms for the density pass), so off by default
@@ -471,7 +476,7 @@ struct cacg_context {
   void pair_ecompute_mixed();
   void pair_ecompute();
   void nve_initial(int which = 3);
-  void nve_final();
+  void nve_final(int which = 3);
   void compute_thermo(double *out);
   void compute_centro(double *out);
   void region_cmd(const std::vector<std::string> &a);
@@ -508,11 +513,12 @@ struct cacg_context {
   void rebuild();
   void run(int n);
   void force_passes(long long b);  // b: phase-mark base of the step, < 0 for none
+  void run_host(int n, double *x, double *v, double *nodex, double *nodev);
   bool fork_ok() const {
     return two_streams && mode == CACG_MIXED && !timing && nlocal > 0 && enlocal > 0;
   }
   template <class A, class E>
-  void forked(A atoms, E elems);
+  void forked(A atoms, E elems, bool elems_first = false);
   void setup();
   void require_init() {
     if (!inited) init();
@@ -596,6 +602,10 @@ cacg_context::~cacg_context() {
   if (gexec) cudaGraphExecDestroy(gexec);
   if (h_pin) cudaFreeHost(h_pin);
   if (fork_ev) cudaEventDestroy(fork_ev);
+  for (cudaEvent_t e : {ev_ain, ev_nin, ev_xout, ev_nxout, ev_nvout, ev_end})
+    if (e) cudaEventDestroy(e);
+  if (cin) cudaStreamDestroy(cin);
+  if (cout_s) cudaStreamDestroy(cout_s);
   if (join_ev) cudaEventDestroy(join_ev);
   if (astream) cudaStreamDestroy(astream);
   if (stream) cudaStreamDestroy(stream);
@@ -2903,12 +2913,17 @@ void cacg_context::nve_initial(int which) {
   }
 }
 
-void cacg_context::nve_final() {
+void cacg_context::nve_final(int which) {
   TypeScale a, e;
   nve_scales(a, e);
-  launch_nve_atoms_final(d_v.p, d_f.p, d_type.p, a, nlocal, fast(), stream);
-  launch_nve_nodes_final(d_nodev.p, d_nodef.p, d_etype.p, e, enlocal, fast(), stream);
-  launches += 2;
+  if (which & 1) {
+    launch_nve_atoms_final(d_v.p, d_f.p, d_type.p, a, nlocal, fast(), stream);
+    launches++;
+  }
+  if (which & 2) {
+    launch_nve_nodes_final(d_nodev.p, d_nodef.p, d_etype.p, e, enlocal, fast(), stream);
+    launches++;
+  }
 }
 
 // Neighbor::decide (neighbor.cpp:1150-1163); ago counts steps since setup and
@@ -3093,7 +3108,7 @@ void cacg_context::run(int n) {
 // the atom chain before its next operation.  Both streams take part in a
 // graph capture of the handle's stream.
 template <class A, class E>
-void cacg_context::forked(A atoms, E elems) {
+void cacg_context::forked(A atoms, E elems, bool elems_first) {
   if (!astream) {
     int least = 0, greatest = 0;
     check(cudaDeviceGetStreamPriorityRange(&least, &greatest), "stream priorities");
@@ -3104,22 +3119,37 @@ void cacg_context::forked(A atoms, E elems) {
   check(cudaEventRecord(fork_ev, stream), "fork");
   check(cudaStreamWaitEvent(astream, fork_ev, 0), "fork wait");
   const cudaStream_t main_stream = stream;
-  stream = astream;
-  try {
-    atoms();
-  } catch (...) {
+  auto atom_chain = [&] {
+    stream = astream;
+    try {
+      atoms();
+    } catch (...) {
+      stream = main_stream;
+      cudaEventRecord(join_ev, astream);
+      cudaStreamWaitEvent(stream, join_ev, 0);
+      throw;
+    }
     stream = main_stream;
-    cudaEventRecord(join_ev, astream);
-    cudaStreamWaitEvent(stream, join_ev, 0);
-    throw;
-  }
-  stream = main_stream;
-  check(cudaEventRecord(join_ev, astream), "join");
-  try {
-    elems();
-  } catch (...) {
-    cudaStreamWaitEvent(stream, join_ev, 0);
-    throw;
+    check(cudaEventRecord(join_ev, astream), "join");
+  };
+  // the chain enqueued first is the one whose kernels the device can start first
+  if (elems_first) {
+    try {
+      elems();
+    } catch (...) {
+      cudaEventRecord(join_ev, astream);
+      cudaStreamWaitEvent(stream, join_ev, 0);
+      throw;
+    }
+    atom_chain();
+  } else {
+    atom_chain();
+    try {
+      elems();
+    } catch (...) {
+      cudaStreamWaitEvent(stream, join_ev, 0);
+      throw;
+    }
   }
   check(cudaStreamWaitEvent(stream, join_ev, 0), "join wait");
 }
@@ -3142,6 +3172,140 @@ void cacg_context::force_passes(long long b) {
   pair_compute_pass(2);
   if (b >= 0) mark((size_t) b + 3);
   pair_ecompute();
+}
+
+// Host-resident state advanced by n steps: x, v of the owned atoms and nodex,
+// nodev of the owned elements are copied in from the caller's buffers, the
+// steps run, and the new state is copied back before the call returns.  When
+// the last step is a plain mixed step (no rebuild decision, two chains), its
+// copies overlap the computation: the element inputs are copied first and the
+// element chain runs on them while the atom inputs are still in flight (at C2
+// it finishes within that window, and the atom chain then has the GPU to
+// itself); positions go out as soon as that step's initial integration
+// has moved them (nothing later in a plain step writes owned positions), node
+// velocities after the element chain's final integration when no fix acts on
+// the forces, atom velocities after the atoms' final integration.  Otherwise
+// the copies and the steps run in order.
+// Results are those of the same steps run on device-resident state.
+void cacg_context::run_host(int n, double *x, double *v, double *nodex, double *nodev) {
+  if (n < 1) fail(CACG_EINVAL, "run_host: at least one step");
+  require_init();
+  if ((nlocal && (!x || !v)) || (enlocal && (!nodex || !nodev)))
+    fail(CACG_EINVAL, "run_host: null state buffer");
+  if (!fix_nve) fail(CACG_ESTATE, "run without fix nve");
+  d_stage.ensure(3 * (size_t) std::max(nlocal, 1), stream);
+  const long long ago_last = (long long) ago + n - 1;
+  const bool last_plain = !(ago_last + 1 >= delay && (ago_last + 1) % every == 0);
+  const bool overlap = fork_ok() && setup_done && list_built && elists_built && !deform_on &&
+                       last_plain;
+  const size_t xb = sizeof(double) * 3 * (size_t) nlocal, nb = sizeof(double) * 24 * (size_t) enlocal;
+  if (!overlap) {
+    cudaStream_t s = stream;
+    if (nlocal) {
+      check(cudaMemcpyAsync(d_stage.p, x, xb, cudaMemcpyHostToDevice, s), "x in");
+      launch_pack3to4(d_stage.p, d_x.p, nlocal, s);
+      check(cudaMemcpyAsync(d_v.p, v, xb, cudaMemcpyHostToDevice, s), "v in");
+    }
+    if (enlocal) {
+      check(cudaMemcpyAsync(d_nodex.p, nodex, nb, cudaMemcpyHostToDevice, s), "nodex in");
+      check(cudaMemcpyAsync(d_nodev.p, nodev, nb, cudaMemcpyHostToDevice, s), "nodev in");
+    }
+    run(n);
+    if (nlocal) {
+      launch_unpack4to3(d_x.p, d_stage.p, nlocal, s);
+      check(cudaMemcpyAsync(x, d_stage.p, xb, cudaMemcpyDeviceToHost, s), "x out");
+      check(cudaMemcpyAsync(v, d_v.p, xb, cudaMemcpyDeviceToHost, s), "v out");
+    }
+    if (enlocal) {
+      check(cudaMemcpyAsync(nodex, d_nodex.p, nb, cudaMemcpyDeviceToHost, s), "nodex out");
+      check(cudaMemcpyAsync(nodev, d_nodev.p, nb, cudaMemcpyDeviceToHost, s), "nodev out");
+    }
+    sync();
+    return;
+  }
+  if (!cin) check(cudaStreamCreateWithFlags(&cin, cudaStreamNonBlocking), "copy-in stream");
+  if (!cout_s) check(cudaStreamCreateWithFlags(&cout_s, cudaStreamNonBlocking), "copy-out stream");
+  for (cudaEvent_t *e : {&ev_ain, &ev_nin, &ev_xout, &ev_nxout, &ev_nvout, &ev_end})
+    if (!*e) check(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "copy event");
+  // inputs: the element state first, so that the element chain runs while the
+  // atom state (six times larger) is still in flight
+  check(cudaMemcpyAsync(d_nodex.p, nodex, nb, cudaMemcpyHostToDevice, cin), "nodex in");
+  check(cudaMemcpyAsync(d_nodev.p, nodev, nb, cudaMemcpyHostToDevice, cin), "nodev in");
+  check(cudaEventRecord(ev_nin, cin), "nodes in");
+  check(cudaMemcpyAsync(d_stage.p, x, xb, cudaMemcpyHostToDevice, cin), "x in");
+  check(cudaMemcpyAsync(d_v.p, v, xb, cudaMemcpyHostToDevice, cin), "v in");
+  check(cudaEventRecord(ev_ain, cin), "atoms in");
+  bool pending = true;
+  if (n > 1) {
+    check(cudaStreamWaitEvent(stream, ev_nin, 0), "wait nodes in");
+    check(cudaStreamWaitEvent(stream, ev_ain, 0), "wait atoms in");
+    launch_pack3to4(d_stage.p, d_x.p, nlocal, stream);
+    launches++;
+    pending = false;
+    run(n - 1);
+  }
+  // the last step (the plain branch of run, with the copies hooked in)
+  const bool early_nodes = post_fixes.empty();
+  ran = true;
+  ntimestep++;
+  ago++;
+  forked(
+      [&] {
+        if (pending) {
+          check(cudaStreamWaitEvent(stream, ev_ain, 0), "wait atoms in");
+          launch_pack3to4(d_stage.p, d_x.p, nlocal, stream);
+          launches++;
+        }
+        nve_initial(1);
+        check(cudaEventRecord(ev_xout, stream), "x final");
+        forward_comm(1);
+        pair_compute_pass(1);
+        pair_compute_pass(2);
+      },
+      [&] {
+        if (pending) check(cudaStreamWaitEvent(stream, ev_nin, 0), "wait nodes in");
+        nve_initial(2);
+        check(cudaEventRecord(ev_nxout, stream), "nodex final");
+        forward_comm(2);
+        pair_ecompute();
+        if (early_nodes) {  // no fix acts between the force passes and the integration
+          nve_final(2);
+          check(cudaEventRecord(ev_nvout, stream), "nodev final");
+        }
+      },
+      true);
+  if (early_nodes) {
+    nve_final(1);
+  } else {
+    post_force();
+    nve_final();
+  }
+  eager_since++;
+  check(cudaEventRecord(ev_end, stream), "step end");
+  // outputs
+  check(cudaStreamWaitEvent(cout_s, ev_xout, 0), "wait x final");
+  launch_unpack4to3(d_x.p, d_stage.p, nlocal, cout_s);
+  check(cudaMemcpyAsync(x, d_stage.p, xb, cudaMemcpyDeviceToHost, cout_s), "x out");
+  check(cudaStreamWaitEvent(cout_s, ev_nxout, 0), "wait nodex final");
+  check(cudaMemcpyAsync(nodex, d_nodex.p, nb, cudaMemcpyDeviceToHost, cout_s), "nodex out");
+  if (early_nodes) {
+    check(cudaStreamWaitEvent(cout_s, ev_nvout, 0), "wait nodev final");
+    check(cudaMemcpyAsync(nodev, d_nodev.p, nb, cudaMemcpyDeviceToHost, cout_s), "nodev out");
+  }
+  check(cudaStreamWaitEvent(cout_s, ev_end, 0), "wait step end");
+  check(cudaMemcpyAsync(v, d_v.p, xb, cudaMemcpyDeviceToHost, cout_s), "v out");
+  if (!early_nodes)
+    check(cudaMemcpyAsync(nodev, d_nodev.p, nb, cudaMemcpyDeviceToHost, cout_s), "nodev out");
+  const bool oob_read = d_misc.p && oob_zeroed;
+  if (oob_read)
+    check(cudaMemcpyAsync(h_pin + 9, d_misc.p + 9, sizeof(int), cudaMemcpyDeviceToHost, cout_s), "oob");
+  check(cudaStreamSynchronize(cout_s), "copy out");
+  // the handle's stream saw every chain joined before ev_end; nothing is left on it
+  if (oob_read && h_pin[9]) {
+    const int nout = h_pin[9];
+    check(cudaMemsetAsync(d_misc.p + 9, 0, sizeof(int), stream), "oob reset");
+    fail(CACG_EINVAL, "%d atoms or element sites outside the packed-coordinate range of the mixed passes", nout);
+  }
 }
 
 // The body of a step without a rebuild decision, captured into a CUDA graph.
@@ -3439,6 +3603,12 @@ int cacg_fix_nve_final_integrate(cacg_handle h) {
 int cacg_run(cacg_handle h, int nsteps) {
   API_BEGIN
   h->run(nsteps);
+  API_END
+}
+
+int cacg_run_host(cacg_handle h, int nsteps, double *x, double *v, double *nodex, double *nodev) {
+  API_BEGIN
+  h->run_host(nsteps, x, v, nodex, nodev);
   API_END
 }
 

@@ -92,6 +92,14 @@ int cacg_run(cacg_handle h, int nsteps);
    atom.h:40, element.h:25, in host memory and push them every step) ---- */
 int cacg_put_atoms(cacg_handle h, const double *x, const double *v);      /* [nlocal][3] */
 int cacg_put_nodes(cacg_handle h, const double *nodex, const double *nodev); /* [n][8][3] */
+/* Verlet::run (verlet.cpp:149-219) on host-resident state: x, v [nlocal][3] and
+   nodex, nodev [enlocal][8][3] are copied in, nsteps steps run, and the new
+   state is copied back into the same buffers before the call returns (pinned
+   buffers give the full link bandwidth).  In mixed precision the last step's
+   copies overlap its computation (element state in first, positions out once
+   the step's initial integration is done); the results equal cacg_put_atoms +
+   cacg_put_nodes + cacg_run + cacg_get_atoms + cacg_get_elements. */
+int cacg_run_host(cacg_handle h, int nsteps, double *x, double *v, double *nodex, double *nodev);
 
 /* ---- state out ---- */
 /* counts: 0 nlocal 1 nghost 2 atom-list entries 3 elem nlocal 4 elem nghost

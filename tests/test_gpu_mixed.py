@@ -113,3 +113,54 @@ def test_two_stream_step_is_bit_identical(cacg_lib, graphs):
         assert np.array_equal(a0[k], a1[k]), k
     for k in ("nodex", "nodev", "nodef"):
         assert np.array_equal(e0[k], e1[k]), k
+
+
+def _prepared(cacg, cfg, m, precision):
+    from gpu_runner import configure
+    s = cacg.System(0)
+    configure(s, cfg, m)
+    s.set_precision(precision)
+    s.init()
+    s.setup()
+    s.neighbor_build()
+    s.pair_compute()
+    s.neighbor_ebuild()
+    s.neighbor_nbuild()
+    s.pair_ecompute()
+    return s
+
+
+@pytest.mark.parametrize("precision", ["MIXED", "FP64"])
+def test_run_host_matches_device_resident_run(cacg_lib, precision):
+    """cacg_run_host (state copied in from host buffers, stepped, copied back,
+    with the last step's copies overlapping its computation in mixed precision)
+    gives the device-resident trajectory bit for bit: one step per call across
+    rebuild decisions, then several steps per call."""
+    cfg, z = C.load_golden("eam_cac")
+    cfg = dict(cfg, every=10, check=True)
+    m = C.model_from_arrays(z)
+    m.atom_v = m.atom_v * 5.0
+    m.nodev = m.nodev * 5.0
+    prec = getattr(cacg_lib, precision)
+    a = _prepared(cacg_lib, cfg, m, prec)
+    b = _prepared(cacg_lib, cfg, m, prec)
+    try:
+        x0 = a.atoms()
+        e0 = a.elements()
+        hx = np.ascontiguousarray(x0["x"], dtype=np.float64)
+        hv = np.ascontiguousarray(x0["v"], dtype=np.float64)
+        hnx = np.ascontiguousarray(e0["nodex"], dtype=np.float64)
+        hnv = np.ascontiguousarray(e0["nodev"], dtype=np.float64)
+        for _ in range(23):
+            a.run_host(1, hx, hv, hnx, hnv)
+        a.run_host(7, hx, hv, hnx, hnv)
+        b.run(30)
+        xb, eb = b.atoms(), b.elements()
+        assert np.array_equal(hx, xb["x"])
+        assert np.array_equal(hv, xb["v"])
+        assert np.array_equal(hnx, eb["nodex"])
+        assert np.array_equal(hnv, eb["nodev"])
+        assert a.counts()["rebuilds"] == b.counts()["rebuilds"]
+    finally:
+        a.close()
+        b.close()
