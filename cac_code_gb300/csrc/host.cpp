@@ -3177,15 +3177,17 @@ void cacg_context::force_passes(long long b) {
 // Host-resident state advanced by n steps: x, v of the owned atoms and nodex,
 // nodev of the owned elements are copied in from the caller's buffers, the
 // steps run, and the new state is copied back before the call returns.  When
-// the last step is a plain mixed step (no rebuild decision, two chains), its
-// copies overlap the computation: the element inputs are copied first and the
-// element chain runs on them while the atom inputs are still in flight (at C2
-// it finishes within that window, and the atom chain then has the GPU to
-// itself); positions go out as soon as that step's initial integration
-// has moved them (nothing later in a plain step writes owned positions), node
-// velocities after the element chain's final integration when no fix acts on
-// the forces, atom velocities after the atoms' final integration.  Otherwise
-// the copies and the steps run in order.
+// the last step is a mixed step (two chains), its copies overlap the
+// computation.  In a step without a rebuild decision the element inputs are
+// copied first and the element chain runs on them while the atom inputs are
+// still in flight (at C2 it finishes within that window, and the atom chain
+// then has the GPU to itself); positions go out as soon as the step's initial
+// integration has moved them (nothing later in such a step writes owned
+// positions), node velocities after the element chain's final integration
+// when no fix acts on the forces, atom velocities last.  A step with a
+// rebuild decision waits for all its inputs (the decision reads the new
+// positions on the host) and sends positions out after the decision, while
+// its force passes run.  Otherwise the copies and the steps run in order.
 // Results are those of the same steps run on device-resident state.
 void cacg_context::run_host(int n, double *x, double *v, double *nodex, double *nodev) {
   if (n < 1) fail(CACG_EINVAL, "run_host: at least one step");
@@ -3196,8 +3198,7 @@ void cacg_context::run_host(int n, double *x, double *v, double *nodex, double *
   d_stage.ensure(3 * (size_t) std::max(nlocal, 1), stream);
   const long long ago_last = (long long) ago + n - 1;
   const bool last_plain = !(ago_last + 1 >= delay && (ago_last + 1) % every == 0);
-  const bool overlap = fork_ok() && setup_done && list_built && elists_built && !deform_on &&
-                       last_plain;
+  const bool overlap = fork_ok() && setup_done && list_built && elists_built && !deform_on;
   const size_t xb = sizeof(double) * 3 * (size_t) nlocal, nb = sizeof(double) * 24 * (size_t) enlocal;
   if (!overlap) {
     cudaStream_t s = stream;
@@ -3244,43 +3245,64 @@ void cacg_context::run_host(int n, double *x, double *v, double *nodex, double *
     pending = false;
     run(n - 1);
   }
-  // the last step (the plain branch of run, with the copies hooked in)
-  const bool early_nodes = post_fixes.empty();
+  // the last step: run's plain branch or its rebuild-decision branch, with the
+  // copies hooked in
+  const bool early_nodes = last_plain && post_fixes.empty();
   ran = true;
   ntimestep++;
-  ago++;
-  forked(
-      [&] {
-        if (pending) {
-          check(cudaStreamWaitEvent(stream, ev_ain, 0), "wait atoms in");
-          launch_pack3to4(d_stage.p, d_x.p, nlocal, stream);
-          launches++;
-        }
-        nve_initial(1);
-        check(cudaEventRecord(ev_xout, stream), "x final");
-        forward_comm(1);
-        pair_compute_pass(1);
-        pair_compute_pass(2);
-      },
-      [&] {
-        if (pending) check(cudaStreamWaitEvent(stream, ev_nin, 0), "wait nodes in");
-        nve_initial(2);
-        check(cudaEventRecord(ev_nxout, stream), "nodex final");
-        forward_comm(2);
-        pair_ecompute();
-        if (early_nodes) {  // no fix acts between the force passes and the integration
-          nve_final(2);
-          check(cudaEventRecord(ev_nvout, stream), "nodev final");
-        }
-      },
-      true);
-  if (early_nodes) {
-    nve_final(1);
-  } else {
+  if (!last_plain) {
+    // Neighbor::decide reads this step's integrated positions on the host, so
+    // the step waits for all its inputs; positions go out after the decision
+    // (a rebuild wraps them into the box first)
+    if (pending) {
+      check(cudaStreamWaitEvent(stream, ev_nin, 0), "wait nodes in");
+      check(cudaStreamWaitEvent(stream, ev_ain, 0), "wait atoms in");
+      launch_pack3to4(d_stage.p, d_x.p, nlocal, stream);
+      launches++;
+    }
+    nve_initial();
+    if (decide() == 0) forward_comm();
+    else rebuild();
+    check(cudaEventRecord(ev_xout, stream), "x final");
+    check(cudaEventRecord(ev_nxout, stream), "nodex final");
+    force_passes(-1);
     post_force();
     nve_final();
+  } else {
+    ago++;
+    forked(
+        [&] {
+          if (pending) {
+            check(cudaStreamWaitEvent(stream, ev_ain, 0), "wait atoms in");
+            launch_pack3to4(d_stage.p, d_x.p, nlocal, stream);
+            launches++;
+          }
+          nve_initial(1);
+          check(cudaEventRecord(ev_xout, stream), "x final");
+          forward_comm(1);
+          pair_compute_pass(1);
+          pair_compute_pass(2);
+        },
+        [&] {
+          if (pending) check(cudaStreamWaitEvent(stream, ev_nin, 0), "wait nodes in");
+          nve_initial(2);
+          check(cudaEventRecord(ev_nxout, stream), "nodex final");
+          forward_comm(2);
+          pair_ecompute();
+          if (early_nodes) {  // no fix acts between the force passes and the integration
+            nve_final(2);
+            check(cudaEventRecord(ev_nvout, stream), "nodev final");
+          }
+        },
+        true);
+    if (early_nodes) {
+      nve_final(1);
+    } else {
+      post_force();
+      nve_final();
+    }
+    eager_since++;
   }
-  eager_since++;
   check(cudaEventRecord(ev_end, stream), "step end");
   // outputs
   check(cudaStreamWaitEvent(cout_s, ev_xout, 0), "wait x final");
