@@ -448,7 +448,11 @@ def run_ours(a, ws, rank, local):
         hnx[...] = el["nodex"]
         hnv[...] = el["nodev"]
         s.set_timing(False)
-        e_steps = max(5, min(a.steps, 20))
+        e_steps = max(10, min(a.steps, 50))
+        # untimed warm-up through the same call (the first steps after the
+        # restore re-partition the lists)
+        for _ in range(max(a.warmup, 3)):
+            s.run_host(1, hx, hv, hnx, hnv)
         barrier(ws)
         t0 = time.perf_counter()
         for _ in range(e_steps):
@@ -458,7 +462,7 @@ def run_ours(a, ws, rank, local):
         e2e = {"value": ws * sites * e_steps / e_wall, "unit": UNIT,
                "h2d_bytes_per_step": int(hx.nbytes + hv.nbytes + hnx.nbytes + hnv.nbytes),
                "d2h_bytes_per_step": int(hx.nbytes + hv.nbytes + hnx.nbytes + hnv.nbytes),
-               "steps": e_steps,
+               "steps": e_steps, "warmup": max(a.warmup, 3),
                "note": "state round trip per step: x, v of atoms and nodes in and out of "
                        "pinned host buffers through cacg_run_host, one call per step (copies "
                        "overlap the step where the data allow; host<->device copies run at "
