@@ -327,7 +327,14 @@ struct cacg_context {
   // events that order the copies against the step's two chains
   cudaStream_t cin = nullptr, cout_s = nullptr;
   cudaEvent_t ev_ain = nullptr, ev_nin = nullptr, ev_xout = nullptr, ev_nxout = nullptr,
-              ev_nvout = nullptr, ev_end = nullptr;
+              ev_nvout = nullptr, ev_end = nullptr, ev_hstart = nullptr, ev_hdone = nullptr;
+  // graph of a whole single-step run_host call on pinned buffers
+  cudaGraphExec_t hexec = nullptr;
+  bool hgraph_valid = false, hgraph_ok = true;
+  unsigned long long hgraph_epoch = 0;
+  long long hgraph_launches = 0;
+  const void *hgraph_bufs[4] = {nullptr, nullptr, nullptr, nullptr};
+  const void *hlast_bufs[4] = {nullptr, nullptr, nullptr, nullptr};  // the previous call's
   // neighbor unions staged in shared memory ("tune union yes"): bit-identical
   // to the direct passes; at C2 they run at 8 warps per SM and lose to the
   // direct kernels' 32 (1.71 vs 0.77 ms for the density pass), so off by default
@@ -354,6 +361,7 @@ struct cacg_context {
   int eager_since = 0;
   void invalidate_graph() {
     graph_valid = false;
+    hgraph_valid = false;
     eager_since = 0;
   }
   bool capture_plain_step();
@@ -602,7 +610,8 @@ cacg_context::~cacg_context() {
   if (gexec) cudaGraphExecDestroy(gexec);
   if (h_pin) cudaFreeHost(h_pin);
   if (fork_ev) cudaEventDestroy(fork_ev);
-  for (cudaEvent_t e : {ev_ain, ev_nin, ev_xout, ev_nxout, ev_nvout, ev_end})
+  if (hexec) cudaGraphExecDestroy(hexec);
+  for (cudaEvent_t e : {ev_ain, ev_nin, ev_xout, ev_nxout, ev_nvout, ev_end, ev_hstart, ev_hdone})
     if (e) cudaEventDestroy(e);
   if (cin) cudaStreamDestroy(cin);
   if (cout_s) cudaStreamDestroy(cout_s);
@@ -3226,108 +3235,204 @@ void cacg_context::run_host(int n, double *x, double *v, double *nodex, double *
   }
   if (!cin) check(cudaStreamCreateWithFlags(&cin, cudaStreamNonBlocking), "copy-in stream");
   if (!cout_s) check(cudaStreamCreateWithFlags(&cout_s, cudaStreamNonBlocking), "copy-out stream");
-  for (cudaEvent_t *e : {&ev_ain, &ev_nin, &ev_xout, &ev_nxout, &ev_nvout, &ev_end})
+  for (cudaEvent_t *e : {&ev_ain, &ev_nin, &ev_xout, &ev_nxout, &ev_nvout, &ev_end, &ev_hstart,
+                         &ev_hdone})
     if (!*e) check(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "copy event");
-  // inputs: the element state first, so that the element chain runs while the
-  // atom state (six times larger) is still in flight
-  check(cudaMemcpyAsync(d_nodex.p, nodex, nb, cudaMemcpyHostToDevice, cin), "nodex in");
-  check(cudaMemcpyAsync(d_nodev.p, nodev, nb, cudaMemcpyHostToDevice, cin), "nodev in");
-  check(cudaEventRecord(ev_nin, cin), "nodes in");
-  check(cudaMemcpyAsync(d_stage.p, x, xb, cudaMemcpyHostToDevice, cin), "x in");
-  check(cudaMemcpyAsync(d_v.p, v, xb, cudaMemcpyHostToDevice, cin), "v in");
-  check(cudaEventRecord(ev_ain, cin), "atoms in");
+  const bool early_nodes = last_plain && post_fixes.empty();
+  const bool oob_read = d_misc.p && oob_zeroed;
+  // inputs, the last step with the copies hooked in, outputs; the copy
+  // streams fork from the handle's stream and join it again, so the whole
+  // call can be captured as one graph
+  auto body = [&](bool pending) {
+    check(cudaEventRecord(ev_hstart, stream), "host step start");
+    check(cudaStreamWaitEvent(cin, ev_hstart, 0), "copy-in fork");
+    check(cudaStreamWaitEvent(cout_s, ev_hstart, 0), "copy-out fork");
+    if (pending) {
+      // the element state first, so that the element chain runs while the
+      // atom state (six times larger) is still in flight
+      check(cudaMemcpyAsync(d_nodex.p, nodex, nb, cudaMemcpyHostToDevice, cin), "nodex in");
+      check(cudaMemcpyAsync(d_nodev.p, nodev, nb, cudaMemcpyHostToDevice, cin), "nodev in");
+      check(cudaEventRecord(ev_nin, cin), "nodes in");
+      check(cudaMemcpyAsync(d_stage.p, x, xb, cudaMemcpyHostToDevice, cin), "x in");
+      check(cudaMemcpyAsync(d_v.p, v, xb, cudaMemcpyHostToDevice, cin), "v in");
+      check(cudaEventRecord(ev_ain, cin), "atoms in");
+    } else {
+      check(cudaEventRecord(ev_ain, cin), "no inputs");
+      check(cudaEventRecord(ev_nin, cin), "no inputs");
+    }
+    ran = true;
+    ntimestep++;
+    if (!last_plain) {
+      // Neighbor::decide reads this step's integrated positions on the host,
+      // so the step waits for all its inputs; positions go out after the
+      // decision (a rebuild wraps them into the box first)
+      check(cudaStreamWaitEvent(stream, ev_nin, 0), "wait nodes in");
+      check(cudaStreamWaitEvent(stream, ev_ain, 0), "wait atoms in");
+      if (pending) {
+        launch_pack3to4(d_stage.p, d_x.p, nlocal, stream);
+        launches++;
+      }
+      nve_initial();
+      if (decide() == 0) forward_comm();
+      else rebuild();
+      check(cudaEventRecord(ev_xout, stream), "x final");
+      check(cudaEventRecord(ev_nxout, stream), "nodex final");
+      force_passes(-1);
+      post_force();
+      nve_final();
+    } else {
+      ago++;
+      forked(
+          [&] {
+            check(cudaStreamWaitEvent(stream, ev_ain, 0), "wait atoms in");
+            if (pending) {
+              launch_pack3to4(d_stage.p, d_x.p, nlocal, stream);
+              launches++;
+            }
+            nve_initial(1);
+            check(cudaEventRecord(ev_xout, stream), "x final");
+            forward_comm(1);
+            pair_compute_pass(1);
+            pair_compute_pass(2);
+          },
+          [&] {
+            check(cudaStreamWaitEvent(stream, ev_nin, 0), "wait nodes in");
+            nve_initial(2);
+            check(cudaEventRecord(ev_nxout, stream), "nodex final");
+            forward_comm(2);
+            pair_ecompute();
+            if (early_nodes) {  // no fix acts between the force passes and the integration
+              nve_final(2);
+              check(cudaEventRecord(ev_nvout, stream), "nodev final");
+            }
+          },
+          true);
+      if (early_nodes) {
+        nve_final(1);
+      } else {
+        post_force();
+        nve_final();
+      }
+      eager_since++;
+    }
+    check(cudaEventRecord(ev_end, stream), "step end");
+    // outputs
+    check(cudaStreamWaitEvent(cout_s, ev_xout, 0), "wait x final");
+    launch_unpack4to3(d_x.p, d_stage.p, nlocal, cout_s);
+    check(cudaMemcpyAsync(x, d_stage.p, xb, cudaMemcpyDeviceToHost, cout_s), "x out");
+    check(cudaStreamWaitEvent(cout_s, ev_nxout, 0), "wait nodex final");
+    check(cudaMemcpyAsync(nodex, d_nodex.p, nb, cudaMemcpyDeviceToHost, cout_s), "nodex out");
+    if (early_nodes) {
+      check(cudaStreamWaitEvent(cout_s, ev_nvout, 0), "wait nodev final");
+      check(cudaMemcpyAsync(nodev, d_nodev.p, nb, cudaMemcpyDeviceToHost, cout_s), "nodev out");
+    }
+    check(cudaStreamWaitEvent(cout_s, ev_end, 0), "wait step end");
+    check(cudaMemcpyAsync(v, d_v.p, xb, cudaMemcpyDeviceToHost, cout_s), "v out");
+    if (!early_nodes)
+      check(cudaMemcpyAsync(nodev, d_nodev.p, nb, cudaMemcpyDeviceToHost, cout_s), "nodev out");
+    if (oob_read)
+      check(cudaMemcpyAsync(h_pin + 9, d_misc.p + 9, sizeof(int), cudaMemcpyDeviceToHost, cout_s),
+            "oob");
+    check(cudaEventRecord(ev_hdone, cout_s), "copies out");
+    check(cudaStreamWaitEvent(stream, ev_hdone, 0), "copy-out join");
+  };
+  auto finish = [&] {
+    check(cudaStreamSynchronize(stream), "host step");
+    if (oob_read && h_pin[9]) {
+      const int nout = h_pin[9];
+      check(cudaMemsetAsync(d_misc.p + 9, 0, sizeof(int), stream), "oob reset");
+      fail(CACG_EINVAL, "%d atoms or element sites outside the packed-coordinate range of the mixed passes", nout);
+    }
+  };
+  // A single plain step on pinned buffers replays a graph of the whole call
+  // (copies, both chains, copies back), captured after an eager step on the
+  // same buffers and dropped like the step graph (rebuild, command,
+  // reallocation); other buffers run eagerly until they too are reused.
+  auto pinned = [](const void *p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    return at.type == cudaMemoryTypeHost;
+  };
+  const void *bufs[4] = {x, v, nodex, nodev};
+  const bool same_bufs = std::equal(bufs, bufs + 4, hlast_bufs);
+  std::copy(bufs, bufs + 4, hlast_bufs);
+  const bool graphable = n == 1 && last_plain && use_graphs && hgraph_ok && pinned(x) &&
+                         pinned(v) && pinned(nodex) && pinned(nodev);
+  if (graphable && hgraph_valid && hgraph_epoch == dbuf_epoch() &&
+      std::equal(bufs, bufs + 4, hgraph_bufs)) {
+    ran = true;
+    ntimestep++;
+    ago++;
+    eager_since++;
+    launches += hgraph_launches;
+    check(cudaGraphLaunch(hexec, stream), "host step graph");
+    graph_steps++;
+    finish();
+    return;
+  }
+  if (graphable && eager_since >= 1 && same_bufs) {  // buffers reused: worth a capture
+    const long long l0 = launches, ts0 = ntimestep;
+    const int ago0 = ago, es0 = eager_since;
+    const unsigned long long e0 = dbuf_epoch();
+    bool ok = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+      capturing = true;
+      try {
+        body(true);
+      } catch (...) {
+        ok = false;
+      }
+      capturing = false;
+      cudaGraph_t g = nullptr;
+      if (cudaStreamEndCapture(stream, &g) != cudaSuccess || !g || dbuf_epoch() != e0) ok = false;
+      cudaGraphExec_t ex = nullptr;
+      if (ok && cudaGraphInstantiate(&ex, g, 0) != cudaSuccess) ok = false;
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();  // a failed capture leaves its error behind
+      if (ok) {
+        if (hexec) cudaGraphExecDestroy(hexec);
+        hexec = ex;
+        hgraph_launches = launches - l0;
+        hgraph_epoch = e0;
+        std::copy(bufs, bufs + 4, hgraph_bufs);
+        hgraph_valid = true;
+        check(cudaGraphLaunch(hexec, stream), "host step graph");
+        graph_steps++;
+        finish();
+        return;
+      }
+      if (ex) cudaGraphExecDestroy(ex);
+    } else {
+      cudaGetLastError();
+    }
+    // the capture failed: the step runs eagerly, and graphs of this call stay off
+    hgraph_ok = false;
+    launches = l0;
+    ntimestep = ts0;
+    ago = ago0;
+    eager_since = es0;
+  }
   bool pending = true;
   if (n > 1) {
-    check(cudaStreamWaitEvent(stream, ev_nin, 0), "wait nodes in");
-    check(cudaStreamWaitEvent(stream, ev_ain, 0), "wait atoms in");
+    // the inputs, then the steps before the last one, in order
+    check(cudaEventRecord(ev_hstart, stream), "host steps start");
+    check(cudaStreamWaitEvent(cin, ev_hstart, 0), "copy-in fork");
+    check(cudaMemcpyAsync(d_nodex.p, nodex, nb, cudaMemcpyHostToDevice, cin), "nodex in");
+    check(cudaMemcpyAsync(d_nodev.p, nodev, nb, cudaMemcpyHostToDevice, cin), "nodev in");
+    check(cudaMemcpyAsync(d_stage.p, x, xb, cudaMemcpyHostToDevice, cin), "x in");
+    check(cudaMemcpyAsync(d_v.p, v, xb, cudaMemcpyHostToDevice, cin), "v in");
+    check(cudaEventRecord(ev_ain, cin), "inputs in");
+    check(cudaStreamWaitEvent(stream, ev_ain, 0), "wait inputs");
     launch_pack3to4(d_stage.p, d_x.p, nlocal, stream);
     launches++;
     pending = false;
     run(n - 1);
   }
-  // the last step: run's plain branch or its rebuild-decision branch, with the
-  // copies hooked in
-  const bool early_nodes = last_plain && post_fixes.empty();
-  ran = true;
-  ntimestep++;
-  if (!last_plain) {
-    // Neighbor::decide reads this step's integrated positions on the host, so
-    // the step waits for all its inputs; positions go out after the decision
-    // (a rebuild wraps them into the box first)
-    if (pending) {
-      check(cudaStreamWaitEvent(stream, ev_nin, 0), "wait nodes in");
-      check(cudaStreamWaitEvent(stream, ev_ain, 0), "wait atoms in");
-      launch_pack3to4(d_stage.p, d_x.p, nlocal, stream);
-      launches++;
-    }
-    nve_initial();
-    if (decide() == 0) forward_comm();
-    else rebuild();
-    check(cudaEventRecord(ev_xout, stream), "x final");
-    check(cudaEventRecord(ev_nxout, stream), "nodex final");
-    force_passes(-1);
-    post_force();
-    nve_final();
-  } else {
-    ago++;
-    forked(
-        [&] {
-          if (pending) {
-            check(cudaStreamWaitEvent(stream, ev_ain, 0), "wait atoms in");
-            launch_pack3to4(d_stage.p, d_x.p, nlocal, stream);
-            launches++;
-          }
-          nve_initial(1);
-          check(cudaEventRecord(ev_xout, stream), "x final");
-          forward_comm(1);
-          pair_compute_pass(1);
-          pair_compute_pass(2);
-        },
-        [&] {
-          if (pending) check(cudaStreamWaitEvent(stream, ev_nin, 0), "wait nodes in");
-          nve_initial(2);
-          check(cudaEventRecord(ev_nxout, stream), "nodex final");
-          forward_comm(2);
-          pair_ecompute();
-          if (early_nodes) {  // no fix acts between the force passes and the integration
-            nve_final(2);
-            check(cudaEventRecord(ev_nvout, stream), "nodev final");
-          }
-        },
-        true);
-    if (early_nodes) {
-      nve_final(1);
-    } else {
-      post_force();
-      nve_final();
-    }
-    eager_since++;
-  }
-  check(cudaEventRecord(ev_end, stream), "step end");
-  // outputs
-  check(cudaStreamWaitEvent(cout_s, ev_xout, 0), "wait x final");
-  launch_unpack4to3(d_x.p, d_stage.p, nlocal, cout_s);
-  check(cudaMemcpyAsync(x, d_stage.p, xb, cudaMemcpyDeviceToHost, cout_s), "x out");
-  check(cudaStreamWaitEvent(cout_s, ev_nxout, 0), "wait nodex final");
-  check(cudaMemcpyAsync(nodex, d_nodex.p, nb, cudaMemcpyDeviceToHost, cout_s), "nodex out");
-  if (early_nodes) {
-    check(cudaStreamWaitEvent(cout_s, ev_nvout, 0), "wait nodev final");
-    check(cudaMemcpyAsync(nodev, d_nodev.p, nb, cudaMemcpyDeviceToHost, cout_s), "nodev out");
-  }
-  check(cudaStreamWaitEvent(cout_s, ev_end, 0), "wait step end");
-  check(cudaMemcpyAsync(v, d_v.p, xb, cudaMemcpyDeviceToHost, cout_s), "v out");
-  if (!early_nodes)
-    check(cudaMemcpyAsync(nodev, d_nodev.p, nb, cudaMemcpyDeviceToHost, cout_s), "nodev out");
-  const bool oob_read = d_misc.p && oob_zeroed;
-  if (oob_read)
-    check(cudaMemcpyAsync(h_pin + 9, d_misc.p + 9, sizeof(int), cudaMemcpyDeviceToHost, cout_s), "oob");
-  check(cudaStreamSynchronize(cout_s), "copy out");
-  // the handle's stream saw every chain joined before ev_end; nothing is left on it
-  if (oob_read && h_pin[9]) {
-    const int nout = h_pin[9];
-    check(cudaMemsetAsync(d_misc.p + 9, 0, sizeof(int), stream), "oob reset");
-    fail(CACG_EINVAL, "%d atoms or element sites outside the packed-coordinate range of the mixed passes", nout);
-  }
+  body(pending);
+  finish();
 }
 
 // The body of a step without a rebuild decision, captured into a CUDA graph.
@@ -3850,6 +3955,7 @@ int cacg_set_graphs(cacg_handle h, int enable) {
   API_BEGIN
   h->use_graphs = enable != 0;
   h->graph_ok = true;
+  h->hgraph_ok = true;
   h->invalidate_graph();
   API_END
 }

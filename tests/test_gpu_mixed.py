@@ -130,11 +130,22 @@ def _prepared(cacg, cfg, m, precision):
     return s
 
 
-@pytest.mark.parametrize("precision", ["MIXED", "FP64"])
-def test_run_host_matches_device_resident_run(cacg_lib, precision):
+def _host_array(a, pinned):
+    if not pinned:
+        return np.ascontiguousarray(a, dtype=np.float64)
+    import torch
+    h = torch.empty(a.shape, dtype=torch.float64).pin_memory().numpy()
+    h[...] = a
+    return h
+
+
+@pytest.mark.parametrize("precision,pinned", [("MIXED", False), ("MIXED", True),
+                                              ("FP64", False)])
+def test_run_host_matches_device_resident_run(cacg_lib, precision, pinned):
     """cacg_run_host (state copied in from host buffers, stepped, copied back,
-    with the last step's copies overlapping its computation in mixed precision)
-    gives the device-resident trajectory bit for bit: one step per call across
+    with the last step's copies overlapping its computation in mixed precision,
+    and on reused pinned buffers the whole call replayed as one graph) gives
+    the device-resident trajectory bit for bit: one step per call across
     rebuild decisions, then several steps per call."""
     cfg, z = C.load_golden("eam_cac")
     cfg = dict(cfg, every=10, check=True)
@@ -147,12 +158,13 @@ def test_run_host_matches_device_resident_run(cacg_lib, precision):
     try:
         x0 = a.atoms()
         e0 = a.elements()
-        hx = np.ascontiguousarray(x0["x"], dtype=np.float64)
-        hv = np.ascontiguousarray(x0["v"], dtype=np.float64)
-        hnx = np.ascontiguousarray(e0["nodex"], dtype=np.float64)
-        hnv = np.ascontiguousarray(e0["nodev"], dtype=np.float64)
+        hx = _host_array(x0["x"], pinned)
+        hv = _host_array(x0["v"], pinned)
+        hnx = _host_array(e0["nodex"], pinned)
+        hnv = _host_array(e0["nodev"], pinned)
         for _ in range(23):
             a.run_host(1, hx, hv, hnx, hnv)
+        single_graph_steps = a.counts()["graph_steps"]
         a.run_host(7, hx, hv, hnx, hnv)
         b.run(30)
         xb, eb = b.atoms(), b.elements()
@@ -160,7 +172,10 @@ def test_run_host_matches_device_resident_run(cacg_lib, precision):
         assert np.array_equal(hv, xb["v"])
         assert np.array_equal(hnx, eb["nodex"])
         assert np.array_equal(hnv, eb["nodev"])
-        assert a.counts()["rebuilds"] == b.counts()["rebuilds"]
+        ca = a.counts()
+        assert ca["rebuilds"] == b.counts()["rebuilds"]
+        if pinned:  # single-step calls replayed the whole-call graph
+            assert single_graph_steps > 0
     finally:
         a.close()
         b.close()
