@@ -97,7 +97,9 @@ int cacg_put_nodes(cacg_handle h, const double *nodex, const double *nodev); /* 
    state is copied back into the same buffers before the call returns (pinned
    buffers give the full link bandwidth).  In mixed precision the last step's
    copies overlap its computation (element state in first, positions out once
-   the step's initial integration is done); the results equal cacg_put_atoms +
+   the step's initial integration is done), and a single-step call on pinned
+   buffers used in the previous call replays one captured graph of the whole
+   call (with cacg_set_graphs on); the results equal cacg_put_atoms +
    cacg_put_nodes + cacg_run + cacg_get_atoms + cacg_get_elements. */
 int cacg_run_host(cacg_handle h, int nsteps, double *x, double *v, double *nodex, double *nodev);
 
