@@ -3037,6 +3037,7 @@ void cacg_context::run(int n) {
       }
       mark(b);
       if (fork_ok()) {
+        const bool nodes_done = post_fixes.empty();
         forked(
             [&] {
               nve_initial(1);
@@ -3048,17 +3049,20 @@ void cacg_context::run(int n) {
               nve_initial(2);
               forward_comm(2);
               pair_ecompute();
+              if (nodes_done) nve_final(2);  // no fix acts on the forces in between
             });
+        post_force();
+        nve_final(nodes_done ? 1 : 3);
       } else {
         nve_initial();
         forward_comm();
         mark(b + 1);
         force_passes((long long) b);
+        post_force();
+        mark(b + 4);
+        nve_final();
+        mark(b + 5);
       }
-      post_force();
-      mark(b + 4);
-      nve_final();
-      mark(b + 5);
       eager_since++;
       continue;
     }
@@ -3452,6 +3456,7 @@ bool cacg_context::capture_plain_step() {
   capturing = true;
   try {
     if (fork_ok()) {
+      const bool nodes_done = post_fixes.empty();
       forked(
           [&] {
             nve_initial(1);
@@ -3463,14 +3468,17 @@ bool cacg_context::capture_plain_step() {
             nve_initial(2);
             forward_comm(2);
             pair_ecompute();
+            if (nodes_done) nve_final(2);  // no fix acts on the forces in between
           });
+      post_force();
+      nve_final(nodes_done ? 1 : 3);
     } else {
       nve_initial();
       forward_comm();
       force_passes(-1);
+      post_force();
+      nve_final();
     }
-    post_force();
-    nve_final();
   } catch (...) {
     ok = false;
   }
