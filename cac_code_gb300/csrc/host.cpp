@@ -335,9 +335,11 @@ struct cacg_context {
   long long hgraph_launches = 0;
   const void *hgraph_bufs[4] = {nullptr, nullptr, nullptr, nullptr};
   const void *hlast_bufs[4] = {nullptr, nullptr, nullptr, nullptr};  // the previous call's
-  // neighbor unions staged in shared memory ("tune union yes"): bit-identical
-  // to the direct passes; at C2 they run at 8 warps per SM and lose to the
-  // direct kernels' 32 (1.71 vs 0.77 ms for the density pass), so off by default
+  // neighbor unions staged in shared memory ("tune union yes"): the same pair
+  // arithmetic over the build-order lists (the direct passes walk the
+  // reordered lists, so sums differ in order only); at C2 they run at 8 warps
+  // per SM and lose to the direct kernels (1.71 vs 0.77 ms for the density
+  // pass when measured), so off by default
   bool mixed_union = false;
   long long list_builds = 0, union_of = -1;
   // the atom lists reordered for the mixed EAM passes (in-range entries

@@ -179,3 +179,20 @@ def test_run_host_matches_device_resident_run(cacg_lib, precision, pinned):
     finally:
         a.close()
         b.close()
+
+
+def test_union_variant_agrees_with_direct_passes(cacg_lib):
+    """`tune union yes` stages each warp's neighbor union in shared memory and
+    walks the build-order lists (the direct passes walk the reordered ones, so
+    the FP32 sums differ in order only): forces agree to FP32 rounding, and a
+    short trajectory stays together."""
+    cfg, z = C.load_golden("eam_atoms")
+    m = C.model_from_arrays(z)
+    out = []
+    for u in ("no", "yes"):
+        a, e, c = _run_cull(cacg_lib, cfg, m, "yes", 10, tune=(f"union {u}",))
+        out.append(a)
+    f0, f1 = out[0]["f"], out[1]["f"]
+    scale = np.abs(f0).max()
+    assert np.abs(f0 - f1).max() <= 1e-5 * scale
+    assert np.abs(out[0]["x"] - out[1]["x"]).max() <= 1e-8
