@@ -196,3 +196,18 @@ def test_union_variant_agrees_with_direct_passes(cacg_lib):
     scale = np.abs(f0).max()
     assert np.abs(f0 - f1).max() <= 1e-5 * scale
     assert np.abs(out[0]["x"] - out[1]["x"]).max() <= 1e-8
+
+
+def test_ip_group_sizes_agree(cacg_lib):
+    """The integration-point passes split each row's entries over 4, 8 or 16
+    lanes (`tune ip_group`); the lane sums meet in a fixed order, so the nodal
+    forces of the three widths agree to FP32 rounding."""
+    cfg, z = C.load_golden("eam_cac")
+    m = C.model_from_arrays(z)
+    nodef = []
+    for gsz in (4, 8, 16):
+        a, e, c = _run_cull(cacg_lib, cfg, m, "yes", 0, tune=(f"ip_group {gsz}",))
+        nodef.append(e["nodef"])
+    scale = np.abs(nodef[0]).max()
+    for other in nodef[1:]:
+        assert np.abs(nodef[0] - other).max() <= 1e-5 * scale
