@@ -52,7 +52,7 @@ EXPORTED = [
     "cacg_gemm_bf16_tn", "cacg_surrogate_reference", "cacg_surrogate_samples",
     "cacg_surrogate_attach", "cacg_compute_centro", "cacg_dump_xyz", "cacg_dump_elements",
     "cacg_fix_post_force", "cacg_get_box", "cacg_set_graphs", "cacg_set_group",
-    "cacg_run_host",
+    "cacg_run_host", "cacg_get_kernel_timing",
 ]
 
 
@@ -346,13 +346,13 @@ class System:
 
     # ---- state out ----
     def counts(self) -> Dict[str, int]:
-        c = np.zeros(23, dtype=np.int64)
-        self._ok(self._L.cacg_get_counts(self.h, c.ctypes.data_as(_lp), 23))
+        c = np.zeros(25, dtype=np.int64)
+        self._ok(self._L.cacg_get_counts(self.h, c.ctypes.data_as(_lp), 25))
         keys = ["nlocal", "nghost", "atom_entries", "enlocal", "enghost", "elem_entries",
                 "ip_rows", "ip_entries", "rebuilds", "nstencil", "step", "sites", "launches",
                 "sites_needed", "force_rows", "short_entries", "surrogate_elements",
                 "surrogate_evaluated", "surrogate_accepted", "graph_steps", "density_scan_entries",
-                "ip_scan_entries", "ip_reorders"]
+                "ip_scan_entries", "ip_reorders", "rebuilds_atoms_only", "atom_reorders"]
         return dict(zip(keys, (int(v) for v in c)))
 
     def atoms(self, all_: bool = False) -> Dict[str, np.ndarray]:
@@ -463,6 +463,15 @@ class System:
         ms = np.zeros(8)
         self._ok(self._L.cacg_get_timing(self.h, _d(ms), 8))
         return ms[:7]
+
+    def kernel_timing(self) -> np.ndarray:
+        """Device ms of the main kernels of the last run with timing on (eager
+        steps): [atom pass 1, atom pass 2, element density, element force,
+        surrogate, sites/lines, atom-list reorder, element row preparation,
+        site F'], then the device ms of every rebuild since creation."""
+        ms = np.zeros(10)
+        self._ok(self._L.cacg_get_kernel_timing(self.h, _d(ms), 10))
+        return ms
 
     def put_atoms(self, x, v):
         """Push host-owned owned-atom x, v (float64 [nlocal][3], C order)."""

@@ -227,6 +227,7 @@ struct cacg_context {
   DBuf<unsigned char> d_row_isforce;
   long long elist_builds = 0, epart_of = -1;
   bool ereorders_zeroed = false;  // the reorder counter (d_misc slot 15)
+  bool areorders_zeroed = false;  // the atom-list reorder counter (d_misc slot 16)
   // lanes per integration point ("tune ip_group N"; 0: from the row count, so
   // that rows x lanes reach the GPU's resident threads)
   int mixed_ip_group = 0;
@@ -310,6 +311,18 @@ struct cacg_context {
   bool inited = false, setup_done = false, list_built = false, elists_built = false;
   long long ntimestep = 0, launches = 0;
   int ago = 0, nrebuild = 0;
+  // rebuilds that kept the element lists (atoms alone moved past the trigger)
+  long long nrebuild_atoms = 0;
+  // a rebuild that only atoms triggered keeps the element lists and element
+  // ghosts when no node has moved past the trigger since the element lists
+  // were built and no element needs a periodic wrap: every pair within the
+  // cutoff is then still in the lists (a site moves at most as far as the
+  // farthest node of its element), so forces are unchanged.  Off in the
+  // bit-exact mode, which follows the reference's full rebuild.
+  bool lazy_elists = true;
+  // device time of every rebuild (events around it)
+  cudaEvent_t rb_ev[2] = {nullptr, nullptr};
+  double rebuild_ms_total = 0.0;
   cudaEvent_t ev[10] = {};
   double t_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   bool timing = false;
@@ -368,14 +381,28 @@ struct cacg_context {
   }
   bool capture_plain_step();
   std::vector<cudaEvent_t> pev;  // per-step phase events
-  // with timing on: events around the EAM atom density kernel of each step
+  // with timing on: events around the main kernels of each step; kernel k of
+  // step j is bracketed by events 2 (j KT_N + k) and 2 (j KT_N + k) + 1
+  enum {
+    KT_ATOM1 = 0,   // atom pass 1: LJ forces or EAM densities + F'
+    KT_ATOM2,       // atom pass 2: EAM forces
+    KT_ELEM_RHO,    // nodal densities (EAM element density pass)
+    KT_ELEM_FORCE,  // integration-point forces
+    KT_SUR,         // surrogate: features, ensemble, acceptance
+    KT_SITES,       // element sites (FP64) or lattice lines (mixed)
+    KT_APART,       // mixed atom-list reorder (returns at once unless due)
+    KT_EPREP,       // mixed integration-point rows, reorder and line masks
+    KT_SITE_FP,     // site F'(rho): per site (FP64) or per lattice line (mixed)
+    KT_N
+  };
+  double t_kern[KT_N] = {};
   std::vector<cudaEvent_t> kev;
   std::vector<char> kev_used;
   size_t cur_step = 0;
   bool capturing = false;
-  void kmark(int k) {
+  void kmark(int k, int end) {
     if (!timing || capturing) return;
-    const size_t at = 2 * cur_step + k;
+    const size_t at = 2 * (cur_step * KT_N + (size_t) k) + (size_t) end;
     while (kev.size() <= at) {
       cudaEvent_t e;
       check(cudaEventCreate(&e), "event");
@@ -520,7 +547,9 @@ struct cacg_context {
   void surrogate_attach(cacg_mlp_t *m, double tol, double dist);
   void surrogate_predict(const EamTables &e);
   int decide();
-  void rebuild();
+  void rebuild(int flags = 3);
+  void borders_atoms();
+  void borders_elems();
   void run(int n);
   void force_passes(long long b);  // b: phase-mark base of the step, < 0 for none
   void run_host(int n, double *x, double *v, double *nodex, double *nodev);
@@ -790,6 +819,8 @@ void cacg_context::command(const std::string &raw) {
     // tune cull yes|no: the mixed EAM density pass skips list entries that no
     //   displacement since the list reorder can bring within the cutoff
     // tune streams yes|no: a mixed step's atom and element chains on two streams
+    // tune elists lazy|eager: in the FP64 and mixed modes a rebuild that only
+    //   atoms triggered keeps the element lists and ghosts (lazy, the default)
     if (a.size() != 2) fail(CACG_EINVAL, "Illegal tune command");
     if (a[0] == "block") {
       int b = inumeric(a[1]);
@@ -810,6 +841,9 @@ void cacg_context::command(const std::string &raw) {
       if (a[1] != "yes" && a[1] != "no") fail(CACG_EINVAL, "tune streams takes yes or no");
       two_streams = a[1] == "yes";
       invalidate_graph();
+    } else if (a[0] == "elists") {
+      if (a[1] != "lazy" && a[1] != "eager") fail(CACG_EINVAL, "tune elists takes lazy or eager");
+      lazy_elists = a[1] == "lazy";
     } else {
       fail(CACG_EINVAL, "Illegal tune command");
     }
@@ -1642,7 +1676,7 @@ void cacg_context::mixed_tables() {
 void cacg_context::element_size() {
   if (enlocal == 0) return;
   d_diag.ensure(enlocal, stream);
-  d_misc.ensure(16, stream);
+  d_misc.ensure(32, stream);
   check(cudaMemsetAsync(d_misc.p + 8, 0, sizeof(int), stream), "memset");
   launch_elem_diag(d_nodex.p, d_ex.p, enlocal, d_diag.p, d_misc.p + 8, stream);
   launches++;
@@ -1942,10 +1976,16 @@ void cacg_context::init() {
 
 // ------------------------------------------------------------------ ghosts
 
+// CommBrick::borders (comm_brick.cpp:641-914): atoms, then elements
 void cacg_context::borders() {
+  borders_atoms();
+  borders_elems();
+}
+
+// ghost atoms, swap by swap (comm_brick.cpp:657-801)
+void cacg_context::borders_atoms() {
   cudaStream_t s = stream;
-  d_misc.ensure(16, s);
-  // atoms (comm_brick.cpp:657-801)
+  d_misc.ensure(32, s);
   nghost = 0;
   size_t send_total = 0;
   int nfirst = 0, nlast = 0;
@@ -1980,10 +2020,16 @@ void cacg_context::borders() {
     send_total += cnt;
     nghost += cnt;
   }
-  // elements (comm_brick.cpp:804-905)
+}
+
+// ghost elements, swap by swap (comm_brick.cpp:804-905), and the per-element
+// offsets of their interpolated sites
+void cacg_context::borders_elems() {
+  cudaStream_t s = stream;
+  d_misc.ensure(32, s);
   enghost = 0;
-  send_total = 0;
-  nfirst = nlast = 0;
+  size_t send_total = 0;
+  int nfirst = 0, nlast = 0;
   for (size_t iw = 0; iw < swaps.size(); iw++) {
     SwapDef &w = swaps[iw];
     if (iw == 0 || swaps[iw - 1].dim != w.dim) nlast = 0;
@@ -2092,7 +2138,7 @@ void cacg_context::neighbor_build() {
     list_built = true;
     return;
   }
-  d_misc.ensure(16, s);
+  d_misc.ensure(32, s);
   d_abin.ensure(nall, s);
   check(cudaMemsetAsync(d_misc.p + 1, 0, sizeof(int) * 2, s), "memset");
   launch_coord2bin_atoms(d_x.p, nall, bins, d_abin.p, d_misc.p + 1, s);
@@ -2266,8 +2312,10 @@ void cacg_context::pair_compute_pass(int pass) {
   const int *num = d_snum.p, *lst = d_slist.p;
   if (pair_style == 1) {
     if (pass != 1) return;
+    kmark(KT_ATOM1, 0);
     if (exact) fp64_exact::lj_atoms(d_x.p, d_type.p, num, lst, stride, nlocal, d_ljtab.p, d_f.p, s);
     else fp64_fma::lj_atoms(d_x.p, d_xh.p, d_type.p, num, lst, stride, nlocal, d_ljtab.p, cp, d_f.p, s);
+    kmark(KT_ATOM1, 1);
     launches++;
     return;
   }
@@ -2275,16 +2323,18 @@ void cacg_context::pair_compute_pass(int pass) {
   if (pass == 1) {
     d_rho.ensure(nall, s);
     d_fp.ensure(nall, s);
-    kmark(0);
+    kmark(KT_ATOM1, 0);
     if (exact) fp64_exact::eam_rho_atoms(d_x.p, num, lst, stride, nlocal, e, d_rho.p, d_fp.p, s);
     else fp64_fma::eam_rho_atoms(d_x.p, d_xh.p, num, lst, stride, nlocal, e, cp, d_rho.p, d_fp.p, s);
-    kmark(1);
+    kmark(KT_ATOM1, 1);
     // forward_comm_pair: ghost fp = owner fp (comm_brick.cpp:941-971)
     launch_copy_root(d_fp.p, 1, d_root.p, nlocal, nghost, s);
     launches += 2;
   } else {
+    kmark(KT_ATOM2, 0);
     if (exact) fp64_exact::eam_force_atoms(d_x.p, num, lst, stride, nlocal, e, d_fp.p, d_f.p, s);
     else fp64_fma::eam_force_atoms(d_x.p, d_xh.p, num, lst, stride, nlocal, e, cp, d_fp.p, d_f.p, s);
+    kmark(KT_ATOM2, 1);
     launches++;
   }
 }
@@ -2305,7 +2355,7 @@ void cacg_context::pair_compute_mixed(int pass) {
   pack_grid(l0, g);
   if (pass == 1) {
     d_xh.ensure(nall, s);
-    d_misc.ensure(16, s);
+    d_misc.ensure(32, s);
     if (!oob_zeroed) {
       check(cudaMemsetAsync(d_misc.p + 9, 0, sizeof(int), s), "oob");
       oob_zeroed = true;
@@ -2360,9 +2410,16 @@ void cacg_context::pair_compute_mixed(int pass) {
       d_mlist.ensure((size_t) maxneigh * stride, s);
       d_nnear.ensure(std::max(nlocal, 1), s);
       d_xq_ref.ensure(std::max(nlocal, 1), s);
+      if (!areorders_zeroed) {
+        check(cudaMemsetAsync(d_misc.p + 16, 0, sizeof(int), s), "areorders");
+        areorders_zeroed = true;
+      }
+      kmark(KT_APART, 0);
       mixed::list_partition(d_xh.p, m.qg, d_num.p, d_list.p, stride, nlocal, m.band_hi,
                             (float) std::sqrt(cutforcesq), d_mlist.p, d_nnear.p, d_xq_ref.p,
-                            reinterpret_cast<unsigned *>(d_misc.p + 11), s);
+                            reinterpret_cast<unsigned *>(d_misc.p + 11),
+                            reinterpret_cast<unsigned *>(d_misc.p + 16), s);
+      kmark(KT_APART, 1);
       for (int d = 0; d < 3; d++) ref_l0[d] = l0[d];
       ref_g = g;
       launches++;
@@ -2379,9 +2436,9 @@ void cacg_context::pair_compute_mixed(int pass) {
       mixed::eam_rho_union(m, d_union_j.p, d_union_n.p, d_slot.p, d_sslot.p, d_rhor_val4.p, e,
                            d_fp4.p, d_rho.p, d_fpf.p, s);
     else {
-      kmark(0);
+      kmark(KT_ATOM1, 0);
       mixed::eam_rho_atoms(m, d_rhor_val4.p, e, d_fp4.p, d_rho.p, d_fpf.p, s);
-      kmark(1);
+      kmark(KT_ATOM1, 1);
     }
     launch_copy_root(d_fpf.p, 1, d_root.p, nlocal, nghost, s);
     launches += 2;
@@ -2389,8 +2446,11 @@ void cacg_context::pair_compute_mixed(int pass) {
     if (mixed_union)
       mixed::eam_force_union(m, d_union_j.p, d_union_n.p, d_sslot.p, d_ftab.p, e, d_fpf.p, d_f.p,
                              s);
-    else
+    else {
+      kmark(KT_ATOM2, 0);
       mixed::eam_force_atoms(m, d_ftab.p, e, d_fpf.p, d_f.p, s);
+      kmark(KT_ATOM2, 1);
+    }
     launches++;
   }
 }
@@ -2406,7 +2466,7 @@ void cacg_context::pair_ecompute_mixed() {
                       "the sites per line) lattice lines (element list build)");
   double l0[3], g;
   pack_grid(l0, g);
-  d_misc.ensure(16, s);
+  d_misc.ensure(32, s);
   if (!oob_zeroed) {
     check(cudaMemsetAsync(d_misc.p + 9, 0, sizeof(int), s), "oob");
     oob_zeroed = true;
@@ -2434,15 +2494,18 @@ void cacg_context::pair_ecompute_mixed() {
   }
   check(cudaMemsetAsync(d_misc.p + 13, same_e ? 0 : 0x7F, sizeof(int), s), "edmax");
   check(cudaMemsetAsync(d_misc.p + 14, 0, sizeof(int), s), "ereordered");
+  kmark(KT_SITES, 0);
   mixed::node_split(d_nodex.p, nall, d_node_hl.p, same_e ? d_node_ref.p : nullptr, eflags, s);
   const mixed::Lattice lat{d_nae.p, d_frac.p, fstride, code_kb};
   // the lattice lines that the scanned entries reference (all referenced
   // lines in a step that reorders)
   mixed::lines(d_node_hl.p, d_etype.p, lat, max_nax, d_line_mask.p,
                cull_e ? d_line_mask_n.p : nullptr, eflags, maxlines, pg, nall, d_line_pos.p, s);
+  kmark(KT_SITES, 1);
   d_ip_q.ensure(std::max(nrows, 1), s);
   d_ip_h.ensure(std::max(nrows, 1), s);
   d_ip_l.ensure(std::max(nrows, 1), s);
+  kmark(KT_EPREP, 0);
   mixed::row_q(d_row_elem.p, d_row_jj.p, d_etype.p, d_int_off.p, d_spa_int_hl.p, d_node_hl.p, nrows,
                pg, d_ip_q.p, d_ip_h.p, d_ip_l.p, s);
   const double csq_e = pair_style == 1 ? ljtab.cutsq[1 * (MAXT + 1) + 1] : cutforcesq;
@@ -2451,6 +2514,7 @@ void cacg_context::pair_ecompute_mixed() {
                     d_node_ref.p, eflags, s);
   mixed::line_masks(d_row_start.p, d_ent_near.p, d_nnear_row.p, nrows, lat, d_row_isforce.p,
                     d_line_mask_n.p, d_line_mask_nf.p, nmask, eflags, s);
+  kmark(KT_EPREP, 1);
   launches += 6;
   epart_of = elist_builds;
   const bool use_sur = sur && nfar > 0;
@@ -2491,9 +2555,15 @@ void cacg_context::pair_ecompute_mixed() {
     m.band_lo = m.cutsq_f * (1.0f - eps);
     m.band_hi = m.cutsq_f * (1.0f + eps);
     EamTables e{};
-    if (use_sur) surrogate_predict(eamtab());
+    if (use_sur) {
+      kmark(KT_SUR, 0);
+      surrogate_predict(eamtab());
+      kmark(KT_SUR, 1);
+    }
+    kmark(KT_ELEM_FORCE, 0);
     mixed::ip_pass(m, 0, nullptr, e, (float) ljtab.lj1[a], (float) ljtab.lj2[a], nullptr,
                    d_fipf.p, s);
+    kmark(KT_ELEM_FORCE, 1);
     launches++;
   } else {
     EamTables e = eamtab();
@@ -2503,20 +2573,30 @@ void cacg_context::pair_ecompute_mixed() {
     m.band_hi = m.cutsq_f * (1.0f + eps);
     d_erho.ensure((size_t) NPE * nall, s);
     d_line_rho.ensure(nmask, s);
+    kmark(KT_ELEM_RHO, 0);
     mixed::ip_pass(m, 1, d_rhor_val4.p, e, 0.f, 0.f, d_erho.p, nullptr, s);
+    kmark(KT_ELEM_RHO, 1);
     launch_copy_root(d_erho.p, NPE, d_eroot.p, enlocal, enghost, s);
+    kmark(KT_SITE_FP, 0);
     mixed::line_rho(d_erho.p, d_etype.p, lat, d_line_mask_f.p, cull_e ? d_line_mask_nf.p : nullptr,
                     eflags, maxlines, nall, d_line_rho.p, s);
     d_row_fpf.ensure(std::max(nrows, 1), s);
     mixed::row_fp(d_force_rows.p, nforce, d_row_elem.p, d_row_jj.p, d_etype.p, d_int_off.p,
                   d_spa_int.p, d_erho.p, e, d_row_fpf.p, s);
+    kmark(KT_SITE_FP, 1);
     m.line_rho = d_line_rho.p;
     m.fp4 = d_fp4.p;
     m.nrho = nrho;
     m.rdrho = (float) rdrho;
     m.row_fp = d_row_fpf.p;
-    if (use_sur) surrogate_predict(e);
+    if (use_sur) {
+      kmark(KT_SUR, 0);
+      surrogate_predict(e);
+      kmark(KT_SUR, 1);
+    }
+    kmark(KT_ELEM_FORCE, 0);
     mixed::ip_pass(m, 2, d_ftab.p, e, 0.f, 0.f, nullptr, d_fipf.p, s);
+    kmark(KT_ELEM_FORCE, 1);
     launches += 5;
   }
   mixed::gather_nodef(d_fipf.p, d_etype.p, d_row_first.p, d_numint.p, d_int_off.p, d_wn.p, enlocal,
@@ -2766,8 +2846,10 @@ void cacg_context::pair_ecompute() {
   // with their float copies, then this step's short lists of the rows
   d_site_h.ensure(std::max(nsites, 1), s);
   // contraction-free in both modes: bit-identical to the all-sites kernel
+  kmark(KT_SITES, 0);
   fp64_fma::sites_needed(d_nodex.p, d_etype.p, d_site_base.p, d_need.p, d_need_elem.p, nneed, t,
                          d_site_x.p, d_site_h.p, s);
+  kmark(KT_SITES, 1);
   const double csq = pair_style == 1 ? ljtab.cutsq[1 * (MAXT + 1) + 1] : cutforcesq;
   const float cp = cut_pass(csq);
   d_sipnum.ensure(std::max(nrows, 1), s);
@@ -2778,6 +2860,7 @@ void cacg_context::pair_ecompute() {
   const int *ipn = d_sipnum.p, *ipe = d_sipent.p;
   if (pair_style == 1) {
     int a = 1 * (MAXT + 1) + 1;
+    kmark(KT_ELEM_FORCE, 0);
     if (exact)
       fp64_exact::lj_ip(d_nodex.p, d_etype.p, d_row_elem.p, d_row_jj.p, nrows, ipn, ipe,
                         rowstride, d_site_x.p, t, ljtab.lj1[a], ljtab.lj2[a], ljtab.cutsq[a], d_fip.p, s);
@@ -2785,28 +2868,39 @@ void cacg_context::pair_ecompute() {
       fp64_fma::lj_ip(d_nodex.p, d_etype.p, d_row_elem.p, d_row_jj.p, nforce, ipn, ipe,
                       rowstride, d_site_x.p, d_site_h.p, t, ljtab.lj1[a], ljtab.lj2[a], ljtab.cutsq[a],
                       cp, d_force_rows.p, d_fip.p, s);
+    kmark(KT_ELEM_FORCE, 1);
     launches++;
   } else {
     EamTables e = eamtab();
     d_erho.ensure((size_t) NPE * nall, s);
     d_site_fp.ensure(std::max(nsites, 1), s);
+    kmark(KT_ELEM_RHO, 0);
     if (exact) {
       fp64_exact::eam_erho(d_nodex.p, d_etype.p, d_row_first.p, enlocal, ipn, ipe, rowstride, d_site_x.p, t, e, d_erho.p, s);
     } else {
       fp64_fma::eam_erho(d_nodex.p, d_etype.p, d_row_first.p, enlocal, ipn, ipe, rowstride, d_site_x.p, d_site_h.p, t, e, cp, d_erho.p, s);
     }
+    kmark(KT_ELEM_RHO, 1);
     // eforward_comm_pair: ghost nodal densities from their owners (comm_brick.cpp:978-1010)
     launch_copy_root(d_erho.p, NPE, d_eroot.p, enlocal, enghost, s);
     if (exact) {
+      kmark(KT_SITE_FP, 0);
       fp64_exact::eam_site_fp(d_erho.p, d_etype.p, d_site_base.p, nall, t, e, d_site_fp.p, s);
+      kmark(KT_SITE_FP, 1);
+      kmark(KT_ELEM_FORCE, 0);
       fp64_exact::eam_ip(d_nodex.p, d_erho.p, d_etype.p, d_row_elem.p, d_row_jj.p, nrows, ipn, ipe,
                          rowstride, d_site_x.p, d_site_fp.p, t, e, d_fip.p, s);
+      kmark(KT_ELEM_FORCE, 1);
     } else {
+      kmark(KT_SITE_FP, 0);
       fp64_fma::site_fp_needed(d_erho.p, d_etype.p, d_site_base.p, d_need.p, d_need_elem.p, nneed,
                                t, e, d_site_fp.p, s);
+      kmark(KT_SITE_FP, 1);
+      kmark(KT_ELEM_FORCE, 0);
       fp64_fma::eam_ip(d_nodex.p, d_erho.p, d_etype.p, d_row_elem.p, d_row_jj.p, nforce, ipn, ipe,
                        rowstride, d_site_x.p, d_site_h.p, d_site_fp.p, t, e, cp, d_force_rows.p,
                        d_fip.p, s);
+      kmark(KT_ELEM_FORCE, 1);
     }
     launches += 4;
   }
@@ -2943,14 +3037,21 @@ int cacg_context::decide() {
   ago++;
   if (ago >= delay && ago % every == 0) {
     if (dist_check == 0) return 1;
-    d_misc.ensure(16, stream);
+    d_misc.ensure(32, stream);
     check(cudaMemsetAsync(d_misc.p + 6, 0, sizeof(int), stream), "memset");
-    launch_check_distance(d_x.p, d_xhold.p, nlocal, d_nodex.p, d_nodexhold.p, enlocal, triggersq,
-                          d_misc.p + 6, stream);
+    BoxWrap box{};
+    for (int d = 0; d < 3; d++) {
+      box.lo[d] = lo[d];
+      box.hi[d] = hi[d];
+      box.periodic[d] = periodic[d];
+    }
+    launch_check_distance(d_x.p, d_xhold.p, nlocal, d_nodex.p, d_nodexhold.p, enlocal,
+                          enlocal ? d_ex.p : nullptr, box, triggersq, d_misc.p + 6, stream);
     launches++;
     check(cudaMemcpyAsync(h_pin + 6, d_misc.p + 6, sizeof(int), cudaMemcpyDeviceToHost, stream), "flag");
     sync();
-    return h_pin[6] ? 1 : 0;
+    // a wrap alone needs no rebuild (the reference's check tests distances only)
+    return (h_pin[6] & 3) ? h_pin[6] : 0;
   }
   return 0;
 }
@@ -2967,21 +3068,45 @@ void cacg_context::check_packed_range() {
   }
 }
 
-void cacg_context::rebuild() {
+// A rebuild (Verlet::run's reneighbor branch, verlet.cpp:184-198).  flags are
+// decide()'s bits: with the element lists lazy, a rebuild that atoms alone
+// triggered (bit 1 without bits 2 and 4), in a fixed box, re-bins and re-lists
+// the atoms and keeps the element lists, element ghosts and cutoffs.
+void cacg_context::rebuild(int flags) {
   check_packed_range();
   nrebuild++;
   invalidate_graph();
-  pbc();
-  if (enlocal) element_size();
-  setup_cut();
-  comm_setup();
-  setup_bins();
-  borders();
-  if (nlocal) neighbor_build();
-  if (enlocal) {
-    neighbor_ebuild();
-    neighbor_nbuild();
+  if (!rb_ev[0]) {
+    check(cudaEventCreate(&rb_ev[0]), "event");
+    check(cudaEventCreate(&rb_ev[1]), "event");
   }
+  check(cudaEventRecord(rb_ev[0], stream), "event record");
+  const bool atoms_only = lazy_elists && mode != CACG_FP64_EXACT && !deform_on && elists_built &&
+                          enlocal > 0 && (flags & 6) == 0;
+  if (atoms_only) {
+    nrebuild_atoms++;
+    launch_pbc_atoms(d_x.p, nlocal, lo, hi, prd, periodic, stream);
+    launches++;
+    borders_atoms();
+    if (nlocal) neighbor_build();
+  } else {
+    pbc();
+    if (enlocal) element_size();
+    setup_cut();
+    comm_setup();
+    setup_bins();
+    borders();
+    if (nlocal) neighbor_build();
+    if (enlocal) {
+      neighbor_ebuild();
+      neighbor_nbuild();
+    }
+  }
+  check(cudaEventRecord(rb_ev[1], stream), "event record");
+  check(cudaEventSynchronize(rb_ev[1]), "event sync");
+  float ms = 0.f;
+  check(cudaEventElapsedTime(&ms, rb_ev[0], rb_ev[1]), "elapsed");
+  rebuild_ms_total += ms;
 }
 
 void cacg_context::setup() {
@@ -3009,6 +3134,7 @@ void cacg_context::run(int n) {
   if (!fix_nve) fail(CACG_ESTATE, "run without fix nve");
   ran = ran || n > 0;
   for (int k = 0; k < 8; k++) t_ms[k] = 0.0;
+  for (int k = 0; k < KT_N; k++) t_kern[k] = 0.0;
   std::fill(pev_used.begin(), pev_used.end(), 0);
   for (auto &e : ev)
     if (!e) check(cudaEventCreate(&e), "event");
@@ -3072,7 +3198,7 @@ void cacg_context::run(int n) {
     nve_initial();
     int nflag = decide();
     if (nflag == 0) forward_comm();
-    else rebuild();
+    else rebuild(nflag);
     mark(b + 1);
     force_passes((long long) b);
     post_force();  // verlet.cpp:206
@@ -3105,13 +3231,16 @@ void cacg_context::run(int n) {
         check(cudaEventElapsedTime(&d, pev[b + k], pev[b + k + 1]), "elapsed");
         t_ms[1 + k] += d;
       }
-      // [6]: the EAM atom density kernel alone
-      const size_t kb = 2 * (size_t) step;
-      float d = 0;
-      if (kb + 1 < kev.size() && kev_used[kb] && kev_used[kb + 1]) {
-        check(cudaEventElapsedTime(&d, kev[kb], kev[kb + 1]), "elapsed");
-        t_ms[6] += d;
+      // the main kernels alone; [6]: the atom pass-1 kernel
+      for (int k = 0; k < KT_N; k++) {
+        const size_t kb = 2 * ((size_t) step * KT_N + (size_t) k);
+        float d = 0;
+        if (kb + 1 < kev.size() && kev_used[kb] && kev_used[kb + 1]) {
+          check(cudaEventElapsedTime(&d, kev[kb], kev[kb + 1]), "elapsed");
+          t_kern[k] += d;
+        }
       }
+      t_ms[6] = t_kern[KT_ATOM1];
     }
   }
   cur_step = 0;
@@ -3279,8 +3408,9 @@ void cacg_context::run_host(int n, double *x, double *v, double *nodex, double *
         launches++;
       }
       nve_initial();
-      if (decide() == 0) forward_comm();
-      else rebuild();
+      const int nflag = decide();
+      if (nflag == 0) forward_comm();
+      else rebuild(nflag);
       check(cudaEventRecord(ev_xout, stream), "x final");
       check(cudaEventRecord(ev_nxout, stream), "nodex final");
       force_passes(-1);
@@ -3751,10 +3881,16 @@ int cacg_run_host(cacg_handle h, int nsteps, double *x, double *v, double *nodex
 
 int cacg_get_counts(cacg_handle h, long long *c, int n) {
   API_BEGIN
-  long long v[23] = {h->nlocal, h->nghost, 0, h->enlocal, h->enghost, 0, h->nrows, 0,
+  long long v[25] = {h->nlocal, h->nghost, 0, h->enlocal, h->enghost, 0, h->nrows, 0,
                      h->nrebuild, (long long) h->stencil.size(), h->ntimestep, h->nsites,
                      h->launches, h->nneed, h->nforce, 0, h->sur ? h->nfar : 0, 0, 0,
-                     h->graph_steps, 0, 0, 0};
+                     h->graph_steps, 0, 0, 0, h->nrebuild_atoms, 0};
+  if (h->areorders_zeroed && h->d_misc.p) {
+    unsigned r = 0;
+    check(cudaMemcpyAsync(&r, h->d_misc.p + 16, sizeof(r), cudaMemcpyDeviceToHost, h->stream), "areorders");
+    h->sync();
+    v[24] = r;
+  }
   if (h->sur && h->d_scount.p) {
     unsigned long long c2[2] = {0, 0};
     check(cudaMemcpyAsync(c2, h->d_scount.p, sizeof(c2), cudaMemcpyDeviceToHost, h->stream), "scount");
@@ -3825,7 +3961,7 @@ int cacg_get_counts(cacg_handle h, long long *c, int n) {
       for (const int4 &x : nn) v[21] += level == 1 ? x.x : level == 2 ? x.y : x.z;
     }
   }
-  for (int i = 0; i < n && i < 23; i++) c[i] = v[i];
+  for (int i = 0; i < n && i < 25; i++) c[i] = v[i];
   API_END
 }
 
@@ -4017,6 +4153,13 @@ int cacg_surrogate_samples(cacg_handle h, float *x, float *t, int n) {
 int cacg_surrogate_attach(cacg_handle h, cacg_mlp m, double tol, double dist) {
   API_BEGIN
   h->surrogate_attach(m, tol, dist);
+  API_END
+}
+
+int cacg_get_kernel_timing(cacg_handle h, double *ms, int n) {
+  API_BEGIN
+  for (int i = 0; i < n && i < cacg_context::KT_N; i++) ms[i] = h->t_kern[i];
+  if (n > cacg_context::KT_N) ms[cacg_context::KT_N] = h->rebuild_ms_total;
   API_END
 }
 

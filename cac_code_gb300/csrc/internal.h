@@ -373,7 +373,7 @@ void ip_reorder(const int *row_start, const int *ent, int nrows, const float4 *i
 // sets ref to the positions and dmax2[1] = 1
 void list_partition(const float4 *xq, float g, const int *num, const int *list, int stride,
                     int nlocal, float cut_rsq, float cutoff, int *out, int4 *nnear, float4 *ref,
-                    unsigned *dmax2, cudaStream_t s);
+                    unsigned *dmax2, unsigned *reorders, cudaStream_t s);
 // neighbor unions of 32-atom groups staged in shared memory (EAM atom passes)
 int union_max();
 void union_build(const int *num, const int *list, int stride, int nlocal, int *union_j,
@@ -500,9 +500,17 @@ void launch_viscous(double *f, const double *v, const int *mask, int n, int per_
                     double gamma, cudaStream_t s);
 void launch_nve_nodes_final(double *nodev, const double *nodef, const int *etype,
                             const TypeScale &dtfm, int n, bool fused, cudaStream_t s);
+// the box for the element wrap test of the distance check
+struct BoxWrap {
+  double lo[3], hi[3];
+  int periodic[3];
+};
+// bits of *flag: 1 atoms, 2 nodes moved past the trigger; 4 (with ex) an
+// element centre outside the box in a periodic dimension
 void launch_check_distance(const double4 *x, const double *xhold, int n,
                            const double *nodex, const double *nodexhold, int ne,
-                           double triggersq, int *flag, cudaStream_t s);
+                           const double *ex, const BoxWrap &box, double triggersq, int *flag,
+                           cudaStream_t s);
 void launch_hold_atoms(const double4 *x, double *xhold, int n, cudaStream_t s);
 void launch_elem_diag(const double *nodex, const double *ex, int n, double *diag,
                       int *centre_bad, cudaStream_t s);

@@ -353,20 +353,19 @@ __global__ void k_bin_fill(const int *__restrict__ bin, int n, const int *__rest
 }
 
 // Sort each bin's members ascending (the reference's forward linked order).
-// One warp per bin: rank by counting smaller members, then scatter.
-__global__ void k_bin_sort(const int *__restrict__ start, const int *__restrict__ count,
-                           int mbins, const int *__restrict__ members_in,
+// One thread per member: its rank in its bin is the number of smaller members
+// of that bin.  The work follows the members, not the bins (a long box has far
+// more bins than members).
+__global__ void k_bin_sort(const int *__restrict__ bin, int n, const int *__restrict__ start,
+                           const int *__restrict__ count, const int *__restrict__ members_in,
                            int *__restrict__ members_out) {
-  int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (w >= mbins) return;
-  int s0 = start[w], c = count[w];
-  for (int a = lane; a < c; a += 32) {
-    int me = members_in[s0 + a];
-    int rank = 0;
-    for (int b = 0; b < c; b++) rank += members_in[s0 + b] < me;
-    members_out[s0 + rank] = me;
-  }
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int b = bin[i];
+  const int s0 = start[b], c = count[b];
+  int rank = 0;
+  for (int a = 0; a < c; a++) rank += members_in[s0 + a] < i;
+  members_out[s0 + rank] = i;
 }
 
 __global__ void k_gather_bx_atoms(const int *__restrict__ mem, const double4 *__restrict__ x,
@@ -530,8 +529,7 @@ void build_bins(const int *bin, int n, int mbins, DBuf<int> &count, DBuf<int> &s
   check(cudaMemsetAsync(cursor.p, 0, sizeof(int) * (size_t) mbins, s), "cursor memset");
   if (n > 0) {
     k_bin_fill<<<nblk(n, 256), 256, 0, s>>>(bin, n, start.p, cursor.p, unsorted);
-    k_bin_sort<<<nblk((long long) mbins * 32, 256), 256, 0, s>>>(start.p, cursor.p, mbins,
-                                                                  unsorted, members.p);
+    k_bin_sort<<<nblk(n, 256), 256, 0, s>>>(bin, n, start.p, cursor.p, unsorted, members.p);
   }
   check(cudaGetLastError(), "build_bins");
 }

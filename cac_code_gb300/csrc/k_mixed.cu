@@ -289,10 +289,14 @@ k_eam_rho_atoms(AtomArgs a, const float4 *__restrict__ rhor_val, int nr, float r
 __global__ void k_list_partition(const float4 *__restrict__ xq, float g, const int *__restrict__ num,
                                  const int *__restrict__ list, int stride, int nlocal, float4 lim,
                                  int *__restrict__ out, int4 *__restrict__ nnear,
-                                 float4 *__restrict__ ref, unsigned *__restrict__ dmax2) {
+                                 float4 *__restrict__ ref, unsigned *__restrict__ dmax2,
+                                 unsigned *__restrict__ reorders) {
   // (the gate reads only dmax2[0], which no block of this kernel writes)
   if (moved_little(dmax2)) return;
-  if (blockIdx.x == 0 && threadIdx.x == 0) dmax2[1] = 1u;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    dmax2[1] = 1u;
+    if (reorders) *reorders += 1u;
+  }
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nlocal; i += gridDim.x * blockDim.x) {
     const float4 qi = xq[i];
     ref[i] = qi;
@@ -1369,11 +1373,12 @@ static float4 part_limits(float cut_rsq, float cutoff) {
 
 void list_partition(const float4 *xq, float g, const int *num, const int *list, int stride,
                     int nlocal, float cut_rsq, float cutoff, int *out, int4 *nnear, float4 *ref,
-                    unsigned *dmax2, cudaStream_t s) {
+                    unsigned *dmax2, unsigned *reorders, cudaStream_t s) {
   if (nlocal <= 0) return;
   const int grid = persistent_grid((const void *) k_list_partition, 256, 0, nlocal);
   k_list_partition<<<grid, 256, 0, s>>>(xq, g, num, list, stride, nlocal,
-                                        part_limits(cut_rsq, cutoff), out, nnear, ref, dmax2);
+                                        part_limits(cut_rsq, cutoff), out, nnear, ref, dmax2,
+                                        reorders);
   check(cudaGetLastError(), "list_partition");
 }
 

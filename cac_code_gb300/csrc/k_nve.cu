@@ -104,24 +104,37 @@ __global__ void k_nve_nodes_final(double *__restrict__ nodev, const double *__re
   nodev[t] = madd<FUSED>(nodev[t], type_scale(dtfm_t, etype[i]), nodef[t]);
 }
 
-// Neighbor::check_distance, neighbor.cpp:1176-1217
+// Neighbor::check_distance, neighbor.cpp:1176-1217.  Bits of *flag: 1 an
+// atom moved more than the trigger distance since its list build, 2 a node
+// did since the element list build, 4 an element centre lies outside the box
+// in a periodic dimension (Domain::elepbc would wrap it).
 __global__ void k_check_distance(const double4 *__restrict__ x, const double *__restrict__ xh,
                                  int n, const double *__restrict__ nodex,
-                                 const double *__restrict__ nodexh, int ne, double triggersq,
+                                 const double *__restrict__ nodexh, int ne,
+                                 const double *__restrict__ ex, BoxWrap box, double triggersq,
                                  int *__restrict__ flag) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  bool hit = false;
+  const long long t = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nn = (long long) ne * NPE;
+  int bit = 0;
   if (t < n) {
     double4 p = x[t];
     double dx = p.x - xh[3 * t], dy = p.y - xh[3 * t + 1], dz = p.z - xh[3 * t + 2];
-    hit = dx * dx + dy * dy + dz * dz > triggersq;
-  } else if (t < n + ne * NPE) {
+    if (dx * dx + dy * dy + dz * dz > triggersq) bit = 1;
+  } else if (t < n + nn) {
     size_t k = 3 * (size_t) (t - n);
     double dx = nodex[k] - nodexh[k], dy = nodex[k + 1] - nodexh[k + 1],
            dz = nodex[k + 2] - nodexh[k + 2];
-    hit = dx * dx + dy * dy + dz * dz > triggersq;
+    if (dx * dx + dy * dy + dz * dz > triggersq) bit = 2;
+  } else if (ex && t < n + nn + ne) {
+    const size_t e = (size_t) (t - n - nn);
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      const double c = ex[3 * e + d];
+      if (box.periodic[d] && (c < box.lo[d] || c >= box.hi[d])) bit = 4;
+    }
   }
-  if (__any_sync(0xffffffffu, hit) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+  const unsigned m = __reduce_or_sync(0xffffffffu, (unsigned) bit);
+  if (m && (threadIdx.x & 31) == 0) atomicOr(flag, (int) m);
 }
 
 __global__ void k_hold_atoms(const double4 *__restrict__ x, double *__restrict__ xh, int n) {
@@ -227,10 +240,11 @@ void launch_nve_nodes_final(double *nodev, const double *nodef, const int *etype
 
 void launch_check_distance(const double4 *x, const double *xhold, int n,
                            const double *nodex, const double *nodexhold, int ne,
-                           double triggersq, int *flag, cudaStream_t s) {
-  long long tot = (long long) n + (long long) ne * NPE;
+                           const double *ex, const BoxWrap &box, double triggersq, int *flag,
+                           cudaStream_t s) {
+  long long tot = (long long) n + (long long) ne * NPE + (ex ? ne : 0);
   if (tot <= 0) return;
-  k_check_distance<<<nblk(tot, 256), 256, 0, s>>>(x, xhold, n, nodex, nodexhold, ne,
+  k_check_distance<<<nblk(tot, 256), 256, 0, s>>>(x, xhold, n, nodex, nodexhold, ne, ex, box,
                                                    triggersq, flag);
   check(cudaGetLastError(), "check_distance");
 }

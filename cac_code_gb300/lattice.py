@@ -95,12 +95,18 @@ def fcc_sites(ncell: Sequence[int], a: float, origin=(0.0, 0.0, 0.0)) -> np.ndar
 
 def element_nodes(origin: np.ndarray, nae: int, a: float) -> np.ndarray:
     """Node positions (8, 3) of a rhombohedral element whose node 0 is ``origin``."""
+    return elements_nodes(np.asarray(origin, dtype=np.float64)[None, :], nae, a)[0]
+
+
+def elements_nodes(origins: np.ndarray, nae: int, a: float) -> np.ndarray:
+    """Node positions (n, 8, 3) of rhombohedral elements whose node 0 sits at
+    ``origins`` (n, 3): origin + t0*span0 + t1*span1 + t2*span2, summed left to
+    right, with t the node's parent corner mapped to {0, 1}."""
     span = (nae - 1) * a * PRIMITIVE           # edge vectors along a1, a2, a3
-    nodes = np.empty((8, 3))
-    for k in range(8):
-        t = (NODE_PARENT[k] + 1) // 2
-        nodes[k] = origin + t[0] * span[0] + t[1] * span[1] + t[2] * span[2]
-    return nodes
+    t = (NODE_PARENT + 1) // 2                 # (8, 3)
+    o = np.asarray(origins, dtype=np.float64)[:, None, :]
+    return (o + t[None, :, 0:1] * span[0] + t[None, :, 1:2] * span[1]
+            + t[None, :, 2:3] * span[2])
 
 
 def gauss_intp(nae: int, with_nodes: bool) -> Tuple[np.ndarray, np.ndarray]:
@@ -148,18 +154,18 @@ def tile_elements(nae: int, a: float, base_x: float, layers: int, direction: int
     per = nae * a
     half = 0.5 * per
     ny_, nz_ = int(round(ly / per)), int(round(lz / per))
-    origins = []
-    for k in range(layers):
-        s = direction * k
-        # y = (n1 + s - n2)*half, z = (n1 + n2)*half
-        for u in range(0, 2 * ny_):          # u = n1 + s - n2
-            for w in range(0, 2 * nz_):      # w = n1 + n2
-                if (u + w - s) % 2:
-                    continue
-                origins.append([base_x + s * half, u * half, w * half])
-    if not origins:
+    if layers <= 0 or ny_ <= 0 or nz_ <= 0:
         return np.zeros((0, 3))
-    origins = np.array(origins)
+    # plane k has s = direction*k; y = (n1 + s - n2)*half, z = (n1 + n2)*half,
+    # u = n1 + s - n2 and w = n1 + n2 of equal parity with s
+    s_ = direction * np.arange(layers, dtype=np.int64)
+    uu, ww = np.meshgrid(np.arange(2 * ny_, dtype=np.int64), np.arange(2 * nz_, dtype=np.int64),
+                         indexing="ij")
+    ss = np.broadcast_to(s_[:, None, None], (layers,) + uu.shape)
+    ub = np.broadcast_to(uu[None], ss.shape)
+    wb = np.broadcast_to(ww[None], ss.shape)
+    keep = (ub + wb - ss) % 2 == 0
+    origins = np.stack([base_x + ss[keep] * half, ub[keep] * half, wb[keep] * half], axis=1)
     order = np.lexsort((origins[:, 2], origins[:, 1], origins[:, 0]))
     return origins[order]
 
@@ -182,13 +188,12 @@ def make_slab_model(a: float, mass: float, atom_cells: Tuple[int, int, int], nae
         if abs(ly / per - round(ly / per)) > 1e-9 or abs(lz / per - round(lz / per)) > 1e-9:
             raise ValueError("y,z extent must be a multiple of nae*a")
     atoms = fcc_sites((ax, ay, az), a)
-    nodes_list = []
     if nae > 0 and elem_layers > 0:
         left = tile_elements(nae, a, -nae * a, elem_layers, -1, ly, lz)
         right = tile_elements(nae, a, ax * a, elem_layers, +1, ly, lz)
-        for r in list(left) + list(right):
-            nodes_list.append(element_nodes(r, nae, a))
-    nodex = np.array(nodes_list).reshape(-1, 8, 3)
+        nodex = elements_nodes(np.concatenate([left, right]), nae, a).reshape(-1, 8, 3)
+    else:
+        nodex = np.zeros((0, 8, 3))
     if nodex.shape[0]:
         xmin = min(atoms[:, 0].min(), nodex[:, :, 0].min())
         xmax = max(atoms[:, 0].max(), nodex[:, :, 0].max())
@@ -229,12 +234,12 @@ def thermalize(model: Model, temperature: float, kb: float, mvv2e: float, seed: 
         v -= v.mean(axis=0)
         model.atom_v = v
     if model.nelements:
-        v = np.zeros_like(model.nodex)
-        for e in range(model.nelements):
-            nae = model.etypes[model.elem_type[e] - 1].nae
-            m_node = model.mass * nae[0] * nae[1] * nae[2] / 8.0
-            s = math.sqrt(kb * temperature / (m_node * mvv2e))
-            v[e] = rng.standard_normal((8, 3)) * s
+        # one (8, 3) draw per element in element order, scaled by the element
+        # type's nodal thermal speed
+        sd = np.array([math.sqrt(kb * temperature /
+                                 (model.mass * et.nae[0] * et.nae[1] * et.nae[2] / 8.0 * mvv2e))
+                       for et in model.etypes])
+        v = rng.standard_normal(model.nodex.shape) * sd[np.asarray(model.elem_type) - 1][:, None, None]
         v -= v.reshape(-1, 3).mean(axis=0)
         model.nodev = v
 
@@ -437,17 +442,23 @@ def remap_into_box(model: Model) -> None:
     (element.cpp:478-540), so only centres move here.
     """
     def wrap(x: np.ndarray) -> None:
+        # per coordinate: add the period while below lo, subtract it while at
+        # or above hi, then clamp to lo (the same operations, element-wise)
         for d in range(3):
             if not model.periodic[d]:
                 continue
             lo, hi = float(model.boxlo[d]), float(model.boxhi[d])
             prd = hi - lo
             col = x[:, d]
-            for i in range(col.shape[0]):
-                c = float(col[i])
-                while c < lo:
-                    c += prd
-                while c >= hi:
-                    c -= prd
-                col[i] = max(c, lo)
+            while True:
+                m = col < lo
+                if not m.any():
+                    break
+                col[m] += prd
+            while True:
+                m = col >= hi
+                if not m.any():
+                    break
+                col[m] -= prd
+            np.maximum(col, lo, out=col)
     wrap(model.atom_x)

@@ -39,7 +39,7 @@ def element_box(nae: int, planes: int, ny: int, nz: int, a: float = W.A_CU,
     per = nae * a
     ly, lz = ny * per, nz * per
     origins = L.tile_elements(nae, a, 0.0, planes, +1, ly, lz)
-    nodex = np.array([L.element_nodes(o, nae, a) for o in origins]).reshape(-1, 8, 3)
+    nodex = L.elements_nodes(origins, nae, a).reshape(-1, 8, 3)
     ip, w = L.gauss_intp(nae, True)
     m = L.Model(boxlo=np.zeros(3), boxhi=np.array([planes // 2 * per, ly, lz]),
                 periodic=(True, True, True), mass=mass, atom_x=np.zeros((0, 3)),

@@ -1,16 +1,24 @@
 """The synthetic benchmark configurations, as seeded models plus input commands.
 
-C1  LJ CAC slab (reduced units): 16x16x16-cell atom slab (16,384 atoms) between
-    32+32 rhombohedral elements with 8 sites per edge, 2x2x2 Gauss points,
-    periodic y,z, T* = 0.1, dt = 0.005, neighbor 2.8 bin.
-C2  EAM Cu CAC slab (metal units): 25x100x100-cell atom slab (1,000,000 atoms)
-    between 10,000+10,000 elements with 10 sites per edge (1,000 sites each);
-    integration points = 8 Gauss points + the 8 nodes (weight 0, needed for the
-    EAM nodal densities); periodic y,z, 300 K, dt = 1 fs, neighbor 7.5 bin.
+"An edge of N primitive spacings" is realised as N + 1 lattice sites per
+element edge where the element period then divides the atom slab's y,z extent;
+elements tile the FCC lattice with no shared sites.
 
-"Edge of N spacings" in the configuration text is realised as N lattice sites
-per element edge, so the element period (N lattice constants) divides the
-atom slab's y,z extent and elements tile the FCC lattice without shared sites.
+C1  LJ CAC slab (reduced units): 16x16x16-cell atom slab (16,384 atoms) between
+    32+32 rhombohedral elements with 8 sites per edge (7 spacings: a period of
+    9 sites does not divide the 16-cell slab), 2x2x2 Gauss points, periodic
+    y,z, T* = 0.1, dt = 0.005, neighbor 2.8 bin.
+C2  EAM Cu CAC slab (metal units): 21x110x110-cell atom slab (1,016,400 atoms)
+    between 10,000+10,000 elements with 11 sites per edge (10 spacings, 1,331
+    sites each); integration points = 8 Gauss points + the 8 nodes (weight 0,
+    needed for the EAM nodal densities); periodic y,z, 300 K, dt = 1 fs,
+    neighbor 7.5 bin.
+C3  the C2 model at 83x110x110 cells (4,017,200 atoms) + 500+500 element planes
+    (200,000 elements, 11 sites per edge), for the strain ramp.
+C5  the surrogate configuration: 16x176x176 cells (1,982,464 atoms) + 488+488
+    element planes of 512 (499,712 elements, 11 sites per edge; 3,997,696 Gauss
+    points).
+
 The site-steps/s metric counts atoms plus Gauss integration points; node
 density rows and interpolated neighbor sites are work, not sites.
 """
@@ -38,7 +46,7 @@ def c1_lj(seed: int = 1) -> Tuple[L.Model, dict]:
     return m, cfg
 
 
-def c2_eam(cells=(25, 100, 100), layers: int = 50, nae: int = 10, seed: int = 2,
+def c2_eam(cells=(21, 110, 110), layers: int = 50, nae: int = 11, seed: int = 2,
            temperature: float = 300.0) -> Tuple[L.Model, dict]:
     m = L.make_slab_model(A_CU, L.AnalyticEAM().mass, cells, nae, layers,
                           L.gauss_intp(nae, True))
@@ -50,9 +58,26 @@ def c2_eam(cells=(25, 100, 100), layers: int = 50, nae: int = 10, seed: int = 2,
 
 
 def c2_sample(seed: int = 3) -> Tuple[L.Model, dict]:
-    """A small replica with C2's structure and atom:element ratio (50:1), used for
-    the bounded CPU samples: 8,000 atoms + 160 elements."""
-    return c2_eam(cells=(5, 20, 20), layers=10, seed=seed)
+    """A small replica with C2's structure and about its atom:element ratio
+    (61:1 against 51:1): 9,680 atoms + 160 elements, 11 sites per edge."""
+    return c2_eam(cells=(5, 22, 22), layers=10, seed=seed)
+
+
+def c3_eam(seed: int = 4) -> Tuple[L.Model, dict]:
+    """C3: 4,017,200 atoms + 200,000 elements (11 sites per edge)."""
+    return c2_eam(cells=(83, 110, 110), layers=500, seed=seed)
+
+
+def c5_eam(seed: int = 6) -> Tuple[L.Model, dict]:
+    """C5: 1,982,464 atoms + 499,712 elements (11 sites per edge), the
+    surrogate configuration."""
+    return c2_eam(cells=(16, 176, 176), layers=488, seed=seed)
+
+
+def c5_sample(seed: int = 7) -> Tuple[L.Model, dict]:
+    """A small replica with C5's structure and atom:element ratio (about 4:1):
+    7,744 atoms + 1,936 elements, 11 sites per edge."""
+    return c2_eam(cells=(4, 22, 22), layers=121, seed=seed)
 
 
 def metric_sites(m: L.Model, cfg: dict) -> int:

@@ -10,8 +10,8 @@
  *
  * Each entry point replaces the reference routine named beside it (file:line in
  * fangyuanxiao/CAC_Code).  Where the reference is a C++ virtual (Pair,
- * Neighbor, Fix), the plug-in shim that calls this ABI is shown in
- * INTEGRATION.md.
+ * Neighbor, Fix), a reference-side subclass of that virtual calls these entry
+ * points from its overrides.
  */
 #ifndef CACG_H
 #define CACG_H
@@ -114,7 +114,10 @@ int cacg_run_host(cacg_handle h, int nsteps, double *x, double *v, double *nodex
    captured CUDA graph 20 atom-list entries the last mixed EAM density pass
    scanned (fewer than 2 while displacement culling holds) 21 integration-point
    list entries the last mixed element passes scanned per pass (fewer than 7
-   while culling holds) 22 reorders of the mixed integration-point lists so far */
+   while culling holds) 22 reorders of the mixed integration-point lists so far
+   23 rebuilds that kept the element lists (only atoms had moved past the
+   trigger; "tune elists lazy", FP64 and mixed modes) 24 reorders of the mixed
+   atom lists so far */
 int cacg_get_counts(cacg_handle h, long long *counts, int n);
 /* Atom::x/v/f (atom.h:40); all != 0 includes ghosts for x and tag */
 int cacg_get_atoms(cacg_handle h, int all, double *x, double *v, double *f, int *tag);
@@ -256,6 +259,18 @@ int cacg_set_graphs(cacg_handle h, int enable);
    or rebuild, [2] atom pass 1, [3] atom pass 2, [4] element passes and fixes,
    [5] final integration, [6] the EAM atom density kernel alone.  n <= 8. */
 int cacg_get_timing(cacg_handle h, double *ms, int n);
+/* Device milliseconds of the main kernels in the last cacg_run, from CUDA
+   events around each launch on the handle's stream (recorded only with
+   cacg_set_timing(h, 1), summed over the eagerly run steps): [0] atom pass 1
+   (LJ forces or EAM densities and F'), [1] atom pass 2 (EAM forces), [2]
+   nodal densities (element density pass), [3] integration-point forces, [4]
+   surrogate (features, ensemble, acceptance), [5] element sites (FP64 modes)
+   or lattice lines (mixed), [6] mixed atom-list reorder, [7] mixed
+   integration-point rows, reorder and line masks, [8] site F'(rho); then [9]
+   the device milliseconds of every rebuild since the handle was created
+   (Neighbor::decide -> reneighbor branch of verlet.cpp:184-198, timing on or
+   off).  n <= 10. */
+int cacg_get_kernel_timing(cacg_handle h, double *ms, int n);
 /* Device-time of a FP64 fused-multiply-add loop on this GPU, for the FP64 roof:
    returns achieved FP64 FLOP/s in *flops. */
 int cacg_measure_fp64_peak(cacg_handle h, double *flops);
