@@ -1,21 +1,31 @@
 #!/usr/bin/env python
-"""Benchmark: site-steps/s of the CAC step on the C2 workload (EAM Cu, 1,000,000
-atoms + 20,000 elements) on one GB300 per rank.  The headline mode is mixed
-precision (FP32 pair terms, FP64 accumulation and integration); the plain FP64
-and bit-exact FP64 modes are timed beside it on the same system, with their
-force difference.
+"""Benchmark: site-steps/s of the CAC step on one GB300 per rank.
+
+Default workload: the surrogate configuration, EAM Cu with a 1,982,464-atom
+core between 499,712 rhombohedral elements of 11 sites per edge (10 primitive
+spacings, 1,331 sites each; 8 Gauss points + 8 node rows per element), 300 K,
+dt = 1 fs, neighbor 7.5 bin, every 10 steps with the distance check.  The
+headline mode is mixed precision (FP32 pair terms) with the nodal-force
+surrogate attached at an ensemble-spread tolerance of 1e-4; the plain FP64 and
+bit-exact FP64 paths are timed on the same system, with every mode's force
+difference from the bit-exact forces of one configuration.
 
 A step is one full Verlet step of the reference's loop (verlet.cpp:163-218):
-NVE half-kick and drift of atoms and nodes, rebuild decision (every 10 steps,
-1 A trigger), ghost refresh or rebuild, EAM density + embedding derivative +
-force passes over the atom list, nodal densities and integration-point forces
-over the element lists with the shape-function gather onto the nodes, and the
-final half-kick.  site-steps/s = (atoms + Gauss integration points) * steps / s.
+NVE half-kick and drift of atoms and nodes, rebuild decision (every 10 steps),
+ghost refresh or rebuild, EAM density + embedding derivative + force passes
+over the atom list, nodal densities and integration-point forces over the
+element lists with the shape-function gather onto the nodes, and the final
+half-kick.  site-steps/s = (atoms + Gauss integration points) * steps / s.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--mode fp64|exact|mixed]
+value: the K timed steps' device time, with the rebuilds and list reorders
+that fell inside them replaced by the rates counted over a longer window
+(>= 200 steps) at their event-timed costs, so that neighbor work enters at its
+natural frequency.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--config c5|c2|c5-medium|...]
   python bench.py --impl reference ...   # the reference algorithm on the host cores
 
-Multi-GPU (torchrun): replicas only -- every rank runs its own C2 system, no
+Multi-GPU (torchrun): replicas only -- every rank runs its own system, no
 collective on the data path; value = all ranks' site-steps / max rank time.
 """
 from __future__ import annotations
@@ -37,6 +47,21 @@ sys.path.insert(0, ROOT)
 METRIC = "site-steps/s on 1 GB300: mixed+surrogate vs plain FP64 at ≤1e-4 rel force err"
 UNIT = "site-steps/s"
 
+# (workload builder, label) per --config
+CONFIGS = {
+    "c5": ("c5_eam", "C5: EAM Cu CAC slab, 1,982,464 atoms + 499,712 elements of 11 sites per "
+                     "edge (10 spacings, 1,331 sites), 8 Gauss points + 8 node rows each"),
+    "c5-medium": ("c5_medium", "C5-structured medium slab: EAM Cu 247,808 atoms + 64,000 elements "
+                               "of 11 sites per edge (profiling size)"),
+    "c2": ("c2_eam", "C2: EAM Cu CAC slab, 1,016,400 atoms + 20,000 elements of 11 sites per "
+                     "edge (10 spacings, 1,331 sites), 8 Gauss points + 8 node rows each"),
+    "c2-medium": ("c2_medium", "C2-structured medium slab: EAM Cu 266,200 atoms + 7,200 elements "
+                               "of 11 sites per edge (profiling size)"),
+    "c2-small": ("c2_sample", "C2 sample: EAM Cu 9,680 atoms + 160 elements of 11 sites per edge"),
+}
+SAMPLES = {"c5": "c5_sample", "c5-medium": "c5_sample", "c2": "c2_sample",
+           "c2-medium": "c2_sample", "c2-small": "c2_sample"}
+
 
 def parse():
     p = argparse.ArgumentParser()
@@ -44,19 +69,22 @@ def parse():
     p.add_argument("--steps", type=int, default=50)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--config", default="c5", choices=sorted(CONFIGS))
     p.add_argument("--mode", default="mixed", choices=["fp64", "exact", "mixed"])
     p.add_argument("--no-surrogate", action="store_true",
                    help="mixed mode without the nodal-force surrogate")
     p.add_argument("--sur-tol", type=float, default=1e-4,
                    help="ensemble-spread tolerance (fraction of the rms nodal force)")
-    p.add_argument("--sur-samples", type=int, default=262144)
+    p.add_argument("--sur-samples", type=int, default=2000000)
     p.add_argument("--sur-epochs", type=int, default=10)
+    p.add_argument("--long-steps", type=int, default=200,
+                   help="steps of the window that counts rebuilds and list reorders")
     p.add_argument("--c4-steps", type=int, default=200,
                    help="steps of the batched-replica workload (256 replicas; 0: skip)")
     p.add_argument("--drift-steps", type=int, default=1000,
                    help="NVE steps of the energy-drift run after the timed region (0: skip)")
-    p.add_argument("--size", default="full", choices=["full", "medium", "small"],
-                   help="full C2; medium = 360,000-atom slab (profiling, > L2); small = 8,000 atoms")
+    p.add_argument("--cpu-steps", type=int, default=150,
+                   help="steps of each host-core sample replica of the CPU baseline")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-modes", action="store_true", help="skip timing the other precision modes")
@@ -158,13 +186,13 @@ class ClockSampler:
 # ----------------------------------------------------------------------------- CPU legs
 
 def _cpu_worker(args):
-    """One host core: the CPU restatement of the reference on a C2-structured
-    sample replica (8,000 atoms + 160 elements), timed over ``steps`` steps."""
-    seed, steps, warm, eam = args
+    """One host core: the CPU restatement of the reference on a sample replica
+    of the workload's structure, timed over ``steps`` steps."""
+    sample, seed, steps, warm, eam = args
     sys.path.insert(0, ROOT)
     from cac_code_gb300 import workloads as W
     from oracle import oracle as O
-    m, cfg = W.c2_sample(seed=seed)
+    m, cfg = getattr(W, sample)(seed=seed)
     o = O.Oracle(m, **W.oracle_kwargs(cfg, eam))
     o.setup()
     if m.natoms:
@@ -175,33 +203,80 @@ def _cpu_worker(args):
     t0 = time.perf_counter()
     o.run(steps)
     dt = time.perf_counter() - t0
-    return W.metric_sites(m, cfg) * steps / dt, dt
+    return W.metric_sites(m, cfg) * steps / dt, dt, W.metric_sites(m, cfg), m.natoms, m.nelements
 
 
-def cpu_leg(cores, steps, warm, eam):
+def cpu_leg(sample, cores, steps, warm, eam):
     from oracle import oracle as O
     O.build()
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores) as pool:
-        res = pool.map(_cpu_worker, [(100 + k, steps, warm, eam) for k in range(cores)])
-    return sum(r[0] for r in res), max(r[1] for r in res)
+        res = pool.map(_cpu_worker, [(sample, 100 + k, steps, warm, eam) for k in range(cores)])
+    return sum(r[0] for r in res), max(r[1] for r in res), res[0][2:]
+
+
+# ----------------------------------------------------------------------------- byte models
+
+# The algorithmic bytes of each main kernel per launch (compulsory traffic:
+# every per-item input read once, every output written once, each list entry
+# read once per pass; neighbor gathers count as cache hits).  c: counts after
+# the timed steps; L: lattice lines the lists reference (all rows, force rows).
+
+def kernel_bytes(name, c, mode, lines_all, lines_force, nae_lines):
+    n = c["nlocal"]
+    ne = c["enlocal"]
+    ne_all = ne + c["enghost"]
+    rows_n = 8 * ne                     # node rows (EAM nodal densities)
+    rows_f = c["force_rows"]            # Gauss rows (nonzero weight)
+    scan_e = c["ip_scan_entries"] / max(c["ip_rows"], 1)   # entries scanned per row
+    n_s = c["short_entries"] / max(n, 1)
+    if mode == "mixed":
+        n_scan = c["density_scan_entries"] / max(n, 1)
+        return {
+            # packed x_i 16, count 4, scanned entries 4n, short-list count 4 and
+            # entries 4 n_s written, rho 8, F' 4
+            "atom1": n * (16 + 4 + 4 * n_scan + 4 + 4 * n_s + 8 + 4),
+            # packed x_i 16, short count 4 + entries 4 n_s, F'_i 4, f_i 24
+            "atom2": n * (16 + 4 + 4 * n_s + 4 + 24),
+            # per node row: element index data 8, row start pair 8, culling counts
+            # 16, packed point 16, codes 4 n, nodal density 8; the line data
+            # (48 B a line) of the lines the node rows reference, read once
+            "elem_rho": rows_n * (8 + 8 + 16 + 16 + 4 * scan_e + 8) + lines_all * 48,
+            # per Gauss row: row 4, element 4, row start pair 8, culling counts
+            # 16, packed point 16, F' 4, codes 4 n, force 24; line data 48 and
+            # density line 8 of the force rows' lines
+            "elem_force": rows_f * (4 + 4 + 8 + 16 + 16 + 4 + 4 * scan_e + 24)
+            + lines_force * (48 + 8),
+            # node split (read 192, write 192 per element), lattice lines (node
+            # halves 192 per element, masks 8 per line slot, 48 per formed line)
+            "sites": ne_all * (192 + 192 + 192 + 8 * nae_lines) + lines_all * 48,
+            # density lines: nodal densities 64 per element, masks, 8 per line;
+            # row F': per Gauss row 16 in, 4 out
+            "site_fp": ne_all * (64 + 8 * nae_lines) + lines_force * 8 + rows_f * 20,
+        }
+    # FP64 modes: per atom x_i 24, count 4, short list 4 n_s, rho/F' 16 or fp_i 8 + f_i 24
+    return {
+        "atom1": n * (24 + 4 + 4 * n_s + 16),
+        "atom2": n * (24 + 4 + 4 * n_s + 8 + 24),
+    }
+
+
+# FP64 operations per launch of the plain FP64 path's kernels (a multiply and
+# an add count two; the site kernels run without contraction, so each is one
+# FP64 instruction).  Sites: 8 nodes x 3 coordinates, a multiply and an add
+# each; site F': 8 density products and sums plus the spline derivative (8);
+# atom density pass: difference, squared distance, root, index and cubic per
+# short-list entry (20); atom force pass: 45 per entry (two splines, the
+# derivative terms and the force components).
+
+def fp64_flops(name, c):
+    n = max(c["nlocal"], 1)
+    n_s = c["short_entries"] / n
+    return {"sites": 48.0 * c["sites_needed"], "site_fp": 24.0 * c["sites_needed"],
+            "atom1": 20.0 * c["nlocal"] * n_s, "atom2": 45.0 * c["nlocal"] * n_s}.get(name)
 
 
 # ----------------------------------------------------------------------------- arms
-
-def algorithmic_bytes_force_atoms(natoms, mean_short):
-    """FP64 EAM force pass over the atom short list (bytes per launch): x_i 24 +
-    count 4 + list 4n + fp_i 8 + f_i 24."""
-    return natoms * (24 + 4 + 4 * mean_short + 8 + 24)
-
-
-def algorithmic_bytes_rho_mixed(natoms, mean_scan, mean_short):
-    """Mixed EAM density pass (bytes per launch): packed x_i 16 + count 4 + the
-    scanned list entries 4 n (the near part of each reordered list while
-    displacement culling holds) + short-list count 4 and entries 4 n_s written +
-    rho 8 + F' 4 (FP32)."""
-    return natoms * (16 + 4 + 4 * mean_scan + 4 + 4 * mean_short + 8 + 4)
-
 
 def run_ours(a, ws, rank, local):
     import numpy as np
@@ -210,23 +285,21 @@ def run_ours(a, ws, rank, local):
     build.build_library()
     tmp = tempfile.mkdtemp(prefix="cacbench_")
     eam = W.write_eam(os.path.join(tmp, "Cu_analytic_2000.eam"))
+    builder, label = CONFIGS[a.config]
 
     cpu = None
     if rank == 0 and ws == 1 and not a.no_cpu_baseline:
         # before the first GPU call: spawn the host-core sample
         cores = os.cpu_count() or 1
-        val, wall = cpu_leg(cores, 60, 2, eam)
+        val, wall, (s_sites, s_atoms, s_elems) = cpu_leg(SAMPLES[a.config], cores, a.cpu_steps, 5,
+                                                         eam)
         cpu = {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"{cores} independent 8,000-atom + 160-element C2-structured replicas "
-                         f"(CPU restatement of the reference, oracle/cac_oracle.c, -O3), 60 timed "
-                         f"steps each after 2 warm-up, {wall:.1f} s"}
+               "sample": f"{cores} independent replicas of {s_atoms:,} atoms + {s_elems:,} "
+                         f"elements ({s_sites:,} metric sites, the workload's structure) on the "
+                         f"CPU restatement of the reference (oracle/cac_oracle.c, -O3), "
+                         f"{a.cpu_steps} timed steps each after 5 warm-up, {wall:.1f} s"}
 
-    if a.size == "small":
-        m, cfg = W.c2_sample(seed=5)
-    elif a.size == "medium":
-        m, cfg = W.c2_eam(cells=(25, 60, 60), layers=50)
-    else:
-        m, cfg = W.c2_eam()
+    m, cfg = getattr(W, builder)()
     sites = W.metric_sites(m, cfg)
     s = cacg.System(local)
     W.configure_system(s, m, cfg, eam)
@@ -238,42 +311,52 @@ def run_ours(a, ws, rank, local):
     if m.nelements:
         s.neighbor_ebuild()
         s.neighbor_nbuild()
+    nae = m.etypes[0].nae[0] if m.nelements else 0
+
     # the surrogate: samples from the plain FP64 quadrature on strained,
-    # thermally perturbed periodic element boxes, trained on the GPU, attached
-    # to the elements farther than 2 r_c from the atoms
+    # thermally perturbed periodic element boxes of the workload's element
+    # type, trained on the GPU, attached to the elements farther than 2 r_c
+    # from the atoms
     sur, net = None, None
     use_sur = a.mode == "mixed" and not a.no_surrogate and m.nelements > 0
     if use_sur:
         from cac_code_gb300 import surrogate as S
         t0 = time.perf_counter()
-        xs, ts, info = S.generate(eam, a.sur_samples, seed=11, planes=8, ny=8, nz=8,
-                                  snapshots=4, device=local)
-        xv, tv, _ = S.generate(eam, 16384, seed=12, planes=8, ny=8, nz=8, snapshots=4,
+        xs, ts, info = S.generate(eam, a.sur_samples, seed=11, nae=nae, planes=8, ny=8, nz=8,
+                                  snapshots=16, device=local)
+        xv, tv, _ = S.generate(eam, 32768, seed=12, nae=nae, planes=8, ny=8, nz=8, snapshots=4,
                                device=local)
         t_gen = time.perf_counter() - t0
         t0 = time.perf_counter()
         net, loss = S.train(xs, ts, members=4, epochs=a.sur_epochs, batch=2048, lr=2e-3,
                             device=local)
         t_train = time.perf_counter() - t0
+        del xs, ts
         pm, psp = net.predict(xv)
         fs = net.normalization()[4]
+        err_elem = np.abs(pm - tv).max(axis=1) / fs
         sur = {"tol": a.sur_tol, "distance_A": 11.0, "members": 4,
                "network": "32-256-256-256-24 SiLU, bf16 tensor cores, fp32 accumulation",
                "samples": info, "generate_s": round(t_gen, 2), "train_s": round(t_train, 2),
                "epochs": a.sur_epochs, "train_loss_normalised": loss,
                "heldout_force_error": S.force_errors(pm, tv),
                "heldout_spread_median_rel": float(np.median(psp) / fs),
-               "heldout_fraction_within_tol": float(np.mean(psp <= a.sur_tol * fs))}
+               "heldout_fraction_spread_within_tol": float(np.mean(psp <= a.sur_tol * fs)),
+               "heldout_fraction_error_within_tol": float(np.mean(err_elem <= a.sur_tol))}
         s.surrogate_reference(m.nodex)
         s.surrogate_attach(net, tol=a.sur_tol, dist=11.0)
     c0 = s.counts()
     s.run(max(a.warmup, 3))
     s.set_timing(False)  # steps without a rebuild decision replay a CUDA graph
+    K = a.steps
 
+    # ---- the timed region: exactly K steps
     clocks = ClockSampler(local)
     barrier(ws)
     clocks.start()
-    l0 = s.counts()["launches"]
+    cs = s.counts()
+    l0 = cs["launches"]
+    rb_ms0 = s.kernel_timing()[9]
     t0 = time.perf_counter()
     s.run(a.steps)
     wall = time.perf_counter() - t0
@@ -281,73 +364,55 @@ def run_ours(a, ws, rank, local):
     barrier(ws)
     dev_ms = float(s.timing()[0])
     c1 = s.counts()
+    rb_ms_timed = s.kernel_timing()[9] - rb_ms0
     launches = c1["launches"] - l0
-    graph_steps = c1["graph_steps"] - c0["graph_steps"]
-    # the phase split of the same number of steps, run eagerly with events
+    graph_steps = c1["graph_steps"] - cs["graph_steps"]
+    win = {k: c1[k] - cs[k] for k in ("rebuilds", "rebuilds_atoms_only", "atom_reorders",
+                                      "ip_reorders")}
+
+    # ---- the same number of steps run eagerly with events: phases and kernels
     s.set_graphs(False)
     s.set_timing(True)
     s.run(a.steps)
     tm = s.timing()
+    kt = s.kernel_timing()
     eager_ms = float(tm[0])
     s.set_timing(False)
     s.set_graphs(True)
     if sur is not None:
-        ev = c1["surrogate_evaluated"] - c0["surrogate_evaluated"]
-        ac = c1["surrogate_accepted"] - c0["surrogate_accepted"]
-        sur["far_elements"] = c1["surrogate_elements"]
+        # element-steps of the timed window (warm-up included in c0 .. c1)
+        ev = c1["surrogate_evaluated"] - cs["surrogate_evaluated"]
+        ac = c1["surrogate_accepted"] - cs["surrogate_accepted"]
+        far = c1["surrogate_elements"]
+        sur["far_elements"] = far
         sur["elements"] = c1["enlocal"]
-        sur["accepted_fraction_timed"] = ac / ev if ev else 0.0
-    value, ms_max = aggregate(ws, sites, a.steps, dev_ms)
+        sur["tested_fraction_timed"] = ev / (far * K) if far else 0.0
+        sur["accepted_fraction_of_tests_timed"] = ac / ev if ev else 0.0
+        sur["accepted_fraction_timed"] = ac / (far * K) if far else 0.0
+        sur["retest"] = ("a rejected element is re-tested after 1, 3, 7, then 15 steps (the "
+                         "quadrature evaluates it meanwhile); an accepted one every step")
 
-    # dominant kernel, one launch per step: the FP64 modes' EAM force pass
-    # over the atom list (phase 3); the mixed mode's EAM density pass (phase 2),
-    # which also writes the force pass's short list
-    mean_neigh = c0["atom_entries"] / max(c0["nlocal"], 1)
-    mean_short = c1["short_entries"] / max(c1["nlocal"], 1)
-    phase = {"integrate+comm": tm[1], "atom_rho": tm[2], "atom_force": tm[3],
-             "element": tm[4], "final": tm[5]}
-    mean_scan = mean_neigh
-    if a.mode == "mixed":
-        kname = "mixed k_eam_rho_atoms (EAM density pass over the atom list, emits the short list)"
-        # the kernel alone (events on its stream around each launch), else its phase
-        k_ms = (tm[6] if len(tm) > 6 and tm[6] > 0 else tm[2]) / a.steps
-        mean_scan = c1["density_scan_entries"] / max(c1["nlocal"], 1)
-        abytes = algorithmic_bytes_rho_mixed(c0["nlocal"], mean_scan, mean_short)
-        tkey = "mixed_k_eam_rho_atoms_bytes_per_atom"
-    else:
-        kname = "k_eam_force_atoms (EAM force pass over the atom list)"
-        k_ms = tm[3] / a.steps
-        abytes = algorithmic_bytes_force_atoms(c0["nlocal"], mean_short)
-        tkey = "k_eam_force_atoms_bytes_per_atom"
-    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    peak, peak_src = 6790.0, "fallback 6.8 TB/s"
-    if os.path.exists(peaks_path):
-        try:
-            peak = float(json.load(open(peaks_path))["hbm_gbs"])
-            peak_src = "measured (MEASURED_PEAKS.json hbm_gbs)"
-        except Exception:
-            pass
-    achieved = abytes / (k_ms * 1e-3) / 1e9 if k_ms > 0 else 0.0
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath):
-        try:
-            tj = json.load(open(tpath))
-            per_atom = tj.get(tkey)
-            if per_atom:
-                traffic = per_atom * c0["nlocal"]
-        except Exception:
-            traffic = None
-    fp64_peak = s.fp64_peak()
+    # ---- neighbor work at its natural frequency: rebuilds and list reorders
+    # counted over a longer window; their costs from events (rebuilds) and
+    # from one eager step right after a list build, which reorders every list
+    # (reorders), less the same kernels' time in a step that does not reorder
+    n_long = max(a.long_steps, a.steps)
+    cl0 = s.counts()
+    rbl0 = s.kernel_timing()[9]
+    s.run(n_long)
+    cl1 = s.counts()
+    rb_ms_long = s.kernel_timing()[9] - rbl0
+    lw = {k: cl1[k] - cl0[k] for k in ("rebuilds", "rebuilds_atoms_only", "atom_reorders",
+                                       "ip_reorders")}
+    rb_cost = rb_ms_long / lw["rebuilds"] if lw["rebuilds"] else (
+        rb_ms_timed / win["rebuilds"] if win["rebuilds"] else 0.0)
 
-    # every later measurement starts from the state right after the timed
-    # region (the synthetic configuration is far from equilibrium: left to run,
-    # it changes the neighbor counts the timings depend on)
     st_a = s.atoms()
     st_e = s.elements()
     st = (st_a["x"].copy(), st_a["v"].copy(), st_e["nodex"].copy(), st_e["nodev"].copy())
 
     def restore():
+        """The state right after the long window, lists rebuilt from it."""
         s.put_atoms(st[0], st[1])
         s.put_nodes(st[2], st[3])
         s.neighbor_build()
@@ -355,10 +420,90 @@ def run_ours(a, ws, rank, local):
             s.neighbor_ebuild()
             s.neighbor_nbuild()
 
-    # the other precision modes on the same system: timing, and every mode's
-    # force difference from the bit-exact FP64 forces of one configuration
+    ro_cost_a = ro_cost_e = 0.0
+    if a.mode == "mixed":
+        restore()
+        s.set_graphs(False)
+        s.set_timing(True)
+        s.run(1)   # reorders the atom and integration-point lists
+        k_re = s.kernel_timing()
+        s.run(1)   # reorders nothing
+        k_no = s.kernel_timing()
+        s.set_timing(False)
+        s.set_graphs(True)
+        ro_cost_a = max(k_re[6] - k_no[6], 0.0)
+        ro_cost_e = max(k_re[7] - k_no[7], 0.0)
+    K = a.steps
+    extra = ((lw["rebuilds"] / n_long * K - win["rebuilds"]) * rb_cost
+             + (lw["atom_reorders"] / n_long * K - win["atom_reorders"]) * ro_cost_a
+             + (lw["ip_reorders"] / n_long * K - win["ip_reorders"]) * ro_cost_e)
+    amort_ms = dev_ms + extra
+    value, ms_max = aggregate(ws, sites, K, amort_ms)
+    value_window, _ = aggregate(ws, sites, K, dev_ms)
+    neighbor_work = {
+        "long_window_steps": n_long, "long_window": lw, "timed_window": win,
+        "rebuild_ms_each": rb_cost, "atom_list_reorder_ms_each": ro_cost_a,
+        "ip_list_reorder_ms_each": ro_cost_e,
+        "timed_ms": dev_ms, "amortised_ms": amort_ms,
+        "value_timed_window_unamortised": value_window,
+        "note": "value = sites * K / (timed device ms + (long-window rate * K - events in the "
+                "timed window) * event cost) for rebuilds and both list reorders"}
+
+    # ---- the dominant kernel: largest event-timed share of the eager run
+    names = ["atom1", "atom2", "elem_rho", "elem_force", "sur", "sites", "apart", "eprep",
+             "site_fp"]
+    kms = {nm: float(kt[i]) / K for i, nm in enumerate(names)}
+    lines_all, lines_force = s.referenced_lines() if m.nelements else (0, 0)
+    nae_lines = nae * nae
+    kb = kernel_bytes(None, c1, a.mode, lines_all, lines_force, nae_lines)
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak, peak_src = 6800.0, "fallback 6.8 TB/s"
+    if os.path.exists(peaks_path):
+        try:
+            peak = float(json.load(open(peaks_path))["hbm_gbs"])
+            peak_src = "measured (MEASURED_PEAKS.json hbm_gbs)"
+        except Exception:
+            pass
+    kernels = {}
+    step_ms = eager_ms / K
+    for nm in names:
+        if kms[nm] <= 0:
+            continue
+        e = {"ms": round(kms[nm], 4), "share_of_eager_step": round(kms[nm] / step_ms, 4)}
+        if nm in kb:
+            e["algorithmic_bytes"] = kb[nm]
+            e["achieved_GBps"] = kb[nm] / (kms[nm] * 1e-3) / 1e9
+            e["hbm_frac"] = e["achieved_GBps"] / peak
+        kernels[nm] = e
+    dom = max(kernels, key=lambda k: kernels[k]["ms"])
+    kernel_names = {
+        "atom1": "k_eam_rho_atoms (EAM density pass over the atom list)",
+        "atom2": "k_eam_force_atoms (EAM force pass over the atom list)",
+        "elem_rho": "k_ipg<EAM, density> (nodal densities over the node rows)",
+        "elem_force": "k_ipg<EAM, force> (integration-point forces over the Gauss rows)",
+        "sur": "surrogate (features, k_mlp_ensemble, acceptance)",
+        "sites": "k_node_split + k_lines (lattice lines)",
+        "site_fp": "k_line_rho + k_row_fp",
+    }
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        try:
+            tj = json.load(open(tpath))
+            key = f"{a.config}:{a.mode}:{dom}_bytes_per_unit"
+            if key in tj:
+                unit = {"atom1": c1["nlocal"], "atom2": c1["nlocal"]}.get(dom, c1["enlocal"])
+                traffic = tj[key] * unit
+        except Exception:
+            traffic = None
+    dk = kernels[dom]
+    fp64_peak = s.fp64_peak()
+
+    # ---- the other precision modes on the same system: timing, and every
+    # mode's force difference from the bit-exact FP64 forces of one configuration
     modes = {}
     force_error = None
+    roof64 = None
     if not a.no_modes and ws == 1:
         def forces():
             s.pair_compute()
@@ -376,55 +521,74 @@ def run_ours(a, ws, rank, local):
                     out[key] = {"rms_rel": float(np.sqrt((d ** 2).mean() / (n_ ** 2).mean())),
                                 "max_rel": float(d.max() / n_.max())}
             return out
-        # (name, precision, surrogate tolerance or None)
-        variants = [("exact", cacg.FP64_EXACT, None), ("fp64", cacg.FP64, None),
-                    ("mixed", cacg.MIXED, None)]
+        # (name, precision, surrogate tolerance or None, timed steps)
+        variants = [("exact", cacg.FP64_EXACT, None, min(K, 5)),
+                    ("fp64", cacg.FP64, None, min(K, 10)),
+                    ("mixed", cacg.MIXED, None, K)]
         head = a.mode
         if use_sur:
             head = "mixed+surrogate"
-            variants += [(head, cacg.MIXED, a.sur_tol),
-                         ("mixed+surrogate(tol=1e-2)", cacg.MIXED, 1e-2)]
+            variants += [(head, cacg.MIXED, a.sur_tol, K),
+                         ("mixed+surrogate(tol=1e-2)", cacg.MIXED, 1e-2, K)]
 
         def setv(mcode, tol):
             s.set_precision(mcode)
             if use_sur:
                 s.surrogate_attach(net if tol is not None else None, tol=tol or 0.0, dist=11.0)
-        fs = {}
+        fs_ = {}
         restore()
-        for name, mcode, tol in variants:
+        for name, mcode, tol, _ in variants:
             setv(mcode, tol)
-            fs[name] = forces()
-        errs = {name: rel_err(fs[name], fs["exact"]) for name, _, _ in variants}
+            fs_[name] = forces()
+        errs = {name: rel_err(fs_[name], fs_["exact"]) for name, _, _, _ in variants}
+        del fs_
         force_error = {"vs": "bit-exact FP64 forces at the same configuration", **errs[head]}
-        for name, mcode, tol in variants:
+        for name, mcode, tol, nst in variants:
             if name == head:
                 continue
             setv(mcode, tol)
             restore()
             cs0 = s.counts()
             s.run(2)
-            s.run(a.steps)  # graphs on, as in the headline
+            s.run(nst)  # graphs on, as in the headline
             t_all = s.timing()[0]
             cs1 = s.counts()
             s.set_graphs(False)
             s.set_timing(True)
-            s.run(a.steps)
+            s.run(nst)
             tmm = s.timing()
+            ktm = s.kernel_timing()
             s.set_timing(False)
             s.set_graphs(True)
-            modes[name] = {"value": sites * a.steps / (t_all * 1e-3),
-                           "ms_per_step": t_all / a.steps,
-                           "phase_ms_per_step_eager": [round(v / a.steps, 4) for v in tmm[1:6]],
+            modes[name] = {"value": sites * nst / (t_all * 1e-3), "steps": nst,
+                           "ms_per_step": t_all / nst,
+                           "phase_ms_per_step_eager": [round(v / nst, 4) for v in tmm[1:6]],
+                           "kernel_ms_per_step_eager": {nm: round(float(ktm[i]) / nst, 4)
+                                                        for i, nm in enumerate(names)
+                                                        if ktm[i] > 0},
                            "force_err_vs_exact": errs[name]}
             if tol is not None:
                 ev = cs1["surrogate_evaluated"] - cs0["surrogate_evaluated"]
+                far = cs1["surrogate_elements"]
                 modes[name]["accepted_fraction"] = (
-                    (cs1["surrogate_accepted"] - cs0["surrogate_accepted"]) / ev if ev else 0.0)
+                    (cs1["surrogate_accepted"] - cs0["surrogate_accepted"]) / (far * (nst + 2))
+                    if far else 0.0)
+            if name == "fp64":
+                # the plain FP64 path against the FP64 roof: its dominant kernel's
+                # FP64 operations per launch over its event time
+                k64 = modes[name]["kernel_ms_per_step_eager"]
+                dk64 = max(k64, key=k64.get)
+                fl = fp64_flops(dk64, s.counts())
+                roof64 = {"bound": "fp64", "kernel": dk64, "ms": k64[dk64], "flops_per_launch": fl,
+                          "achieved": fl / (k64[dk64] * 1e-3) if fl else None,
+                          "peak": fp64_peak, "unit": "FLOP/s",
+                          "frac": (fl / (k64[dk64] * 1e-3) / fp64_peak) if fl else None,
+                          "peak_source": "measured FP64 FMA loop on this GPU (cacg_measure_fp64_peak)"}
         setv(mode, a.sur_tol if use_sur else None)
 
-    # e2e through the C ABI with host-resident state: x,v (atoms + nodes) in
-    # from pinned host memory, one step, the new x,v (atoms + nodes) back out,
-    # every step (cacg_run_host)
+    # ---- e2e through the C ABI with host-resident state: x,v (atoms + nodes)
+    # in from pinned host memory, one step, the new x,v (atoms + nodes) back
+    # out, every step (cacg_run_host)
     e2e = None
     if not a.no_e2e:
         try:
@@ -447,8 +611,9 @@ def run_ours(a, ws, rank, local):
         el = s.elements()
         hnx[...] = el["nodex"]
         hnv[...] = el["nodev"]
+        del el
         s.set_timing(False)
-        e_steps = max(10, min(a.steps, 50))
+        e_steps = max(10, min(K, 50))
         # untimed warm-up through the same call (the first steps after the
         # restore re-partition the lists)
         for _ in range(max(a.warmup, 3)):
@@ -465,12 +630,12 @@ def run_ours(a, ws, rank, local):
                "steps": e_steps, "warmup": max(a.warmup, 3),
                "note": "state round trip per step: x, v of atoms and nodes in and out of "
                        "pinned host buffers through cacg_run_host, one call per step (copies "
-                       "overlap the step where the data allow; host<->device copies run at "
-                       "~200 GB/s each way on this box)"}
+                       "overlap the step where the data allow)"}
 
-    # energy drift of the headline mode: FP64 energies before and after an NVE
-    # run (the potential is not smoothed at the cutoff: phi(rc) = -0.0189 eV,
-    # so pairs crossing it make the total jump by that much)
+    # ---- energy drift of the headline mode, atoms and elements apart (they do
+    # not interact): FP64 energies before and after an NVE run.  The potential
+    # is not smoothed at the cutoff (phi(rc) = -0.0189 eV): a pair crossing it
+    # makes the total jump by that much
     drift = None
     if a.drift_steps > 0:
         s.set_timing(False)
@@ -478,66 +643,72 @@ def run_ours(a, ws, rank, local):
         t_a = s.thermo()
         s.run(a.drift_steps)
         t_b = s.thermo()
-        drift = {"steps": a.drift_steps, "mode": a.mode,
-                 "e_start_ev": t_a["etotal"], "e_end_ev": t_b["etotal"],
-                 "ev_per_site": (t_b["etotal"] - t_a["etotal"]) / sites,
-                 "ke_start_ev": t_a["ke_atoms"] + t_a["ke_nodes"]}
+        ea0, ea1 = t_a["pe_atoms"] + t_a["ke_atoms"], t_b["pe_atoms"] + t_b["ke_atoms"]
+        ee0, ee1 = t_a["pe_elements"] + t_a["ke_nodes"], t_b["pe_elements"] + t_b["ke_nodes"]
+        ngp = cfg["gauss_per_element"] * max(c1["enlocal"], 1)
+        drift = {"steps": a.drift_steps, "mode": a.mode + ("+surrogate" if use_sur else ""),
+                 "atoms": {"e_start_ev": ea0, "e_end_ev": ea1,
+                           "ev_per_atom": (ea1 - ea0) / max(c1["nlocal"], 1)},
+                 "elements": {"e_start_ev": ee0, "e_end_ev": ee1,
+                              "ev_per_gauss_point": (ee1 - ee0) / ngp,
+                              "ke_nodes_start_ev": t_a["ke_nodes"],
+                              "ke_nodes_end_ev": t_b["ke_nodes"]},
+                 "ev_per_site": (t_b["etotal"] - t_a["etotal"]) / sites}
 
-    # the batched-replica workload: 256 independent replicas packed by pair
-    # style and size class, autotuned, graph-replayed
+    # ---- the batched-replica workload: 256 independent replicas packed by
+    # pair style and size class, autotuned, graph-replayed
     c4 = None
     if a.c4_steps > 0 and ws == 1:
+        s.close()
+        s = None
         from cac_code_gb300 import batch as B
         t0 = time.perf_counter()
         c4 = B.run_batch(eam, n=256, steps=a.c4_steps, seed=4, tune=True, device=local)
         c4["wall_s"] = round(time.perf_counter() - t0, 1)
-        c4["note"] = ("element kinetic energy grows under the reference's force definition on "
-                      "these synthetic replicas; the step count stays inside the stable window")
 
     if rank == 0:
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps,
-            "warmup": max(a.warmup, 3), "ms_per_step": ms_max / a.steps,
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K,
+            "warmup": max(a.warmup, 3), "ms_per_step": dev_ms / K,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if a.mode != "mixed" else "f32+f64", "data": "synthetic",
             "config": {
-                "workload": {"small": "C2 sample: EAM Cu 8,000 atoms + 160 elements",
-                             "medium": "C2 medium: EAM Cu 360,000 atoms + 7,200 elements",
-                             "full": "C2: EAM Cu CAC slab, 1,000,000 atoms + 20,000 elements "
-                                     "(11 sites/edge, 8 Gauss points each)"}[a.size],
+                "workload": label, "config": a.config,
                 "mode": a.mode + ("+surrogate" if use_sur else ""),
-                "atoms": c0["nlocal"], "ghost_atoms": c0["nghost"],
+                "sites_per_edge": nae, "atoms": c0["nlocal"], "ghost_atoms": c0["nghost"],
                 "elements": c0["enlocal"], "ghost_elements": c0["enghost"],
                 "gauss_points": cfg["gauss_per_element"] * c0["enlocal"],
                 "integration_rows": c0["ip_rows"], "sites": sites,
                 "interpolated_sites": c0["sites"], "sites_referenced": c0["sites_needed"],
-                "atom_list_mean": round(mean_neigh, 2),
-                "density_pass_scan_mean": round(mean_scan, 2),
-                "short_list_mean": round(mean_short, 2),
+                "atom_list_mean": round(c0["atom_entries"] / max(c0["nlocal"], 1), 2),
+                "density_pass_scan_mean": round(c1["density_scan_entries"] / max(c1["nlocal"], 1), 2),
+                "short_list_mean": round(c1["short_entries"] / max(c1["nlocal"], 1), 2),
                 "ip_list_mean": round(c0["ip_entries"] / max(c0["ip_rows"], 1), 2),
-                "rebuild": "every 10 steps if any displacement > skin/2 (check yes)",
-                "rebuilds_in_timed_region": c1["rebuilds"] - c0["rebuilds"],
-                "l2": "inputs larger than L2 (positions+lists >> 129 MB resident)",
+                "ip_scan_mean": round(c1["ip_scan_entries"] / max(c1["ip_rows"], 1), 2),
+                "lattice_lines_referenced": lines_all,
+                "rebuild": "every 10 steps if any displacement > skin/2 (check yes); a rebuild "
+                           "that only atoms trigger keeps the element lists",
+                "neighbor_work": neighbor_work,
+                "l2": "inputs larger than L2 (positions + lists >> 129 MB resident)",
                 "parallelism": f"replicas{ws}",
-                "phase_ms_per_step": {k: round(v / a.steps, 4) for k, v in phase.items()},
-                "phase_note": "phases from an equal eager run (no graphs) right after the timed one",
-                "eager_ms_per_step": round(eager_ms / a.steps, 4),
+                "phase_ms_per_step_eager": {k: round(float(v) / K, 4) for k, v in
+                                            zip(["integrate+comm", "atom_pass1", "atom_pass2",
+                                                 "element", "final"], tm[1:6])},
+                "eager_ms_per_step": round(eager_ms / K, 4),
                 "graph_steps_timed": graph_steps,
                 "wall_s": round(wall, 3)},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic,
-                         "kernel": kname,
-                         "algorithmic_bytes_per_launch": abytes, "kernel_ms": k_ms,
-                         "kernel_ms_source": ("CUDA events around each launch on its stream, "
-                                              "averaged over the equal eager run"
-                                              if a.mode == "mixed" and len(tm) > 6 and tm[6] > 0
-                                              else "the kernel's phase in the equal eager run"),
+            "roofline": {"bound": "hbm", "achieved": dk.get("achieved_GBps"), "peak": peak,
+                         "unit": "GB/s", "frac": dk.get("hbm_frac"), "traffic": traffic,
+                         "kernel": kernel_names.get(dom, dom),
+                         "algorithmic_bytes_per_launch": dk.get("algorithmic_bytes"),
+                         "kernel_ms": dk["ms"],
+                         "kernel_ms_source": "CUDA events around each launch on its stream, "
+                                             "averaged over an equal eager run right after the "
+                                             "timed one",
                          "peak_source": peak_src,
-                         "fp64_peak_flops_measured": fp64_peak,
-                         "note": "FP64 pair math is ALU-bound on GB300 (see fp64_peak); the "
-                                 "mixed passes run no FP64 in their pair loops and are bound "
-                                 "by instruction issue and the latency of neighbor gathers "
-                                 "(L2 hits)"},
+                         "kernels": kernels},
+            "roofline_fp64": roof64,
+            "fp64_peak_flops_measured": fp64_peak,
             "cpu_baseline": cpu,
             "e2e": e2e,
             "clocks": clk,
@@ -551,7 +722,8 @@ def run_ours(a, ws, rank, local):
         if "fp64" in modes:
             line["speedup_vs_plain_fp64"] = value / modes["fp64"]["value"]
         print(json.dumps(line), flush=True)
-    s.close()
+    if s is not None:
+        s.close()
     if net is not None:
         net.close()
 
@@ -564,21 +736,21 @@ def run_reference(a, ws, rank):
     eam = W.write_eam(os.path.join(tmp, "Cu_analytic_2000.eam"))
     cores = os.cpu_count() or 1
     steps = max(1, min(a.steps, 200))
-    warm = max(1, min(a.warmup, 5))
-    val, wall = cpu_leg(cores, steps, warm, eam)
+    warm = max(3, min(a.warmup, 5))
+    val, wall, (s_sites, s_atoms, s_elems) = cpu_leg(SAMPLES[a.config], cores, steps, warm, eam)
     line = {
         "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": ws,
         "steps": steps, "warmup": warm, "ms_per_step": None, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "C2: EAM Cu CAC slab, 1,000,000 atoms + 20,000 elements (11 "
-                               "sites/edge, 8 Gauss points each), sampled on the host cores "
-                               "as independent C2-structured replicas",
-                   "parallelism": f"{cores} host processes"},
+        "config": {"workload": CONFIGS[a.config][1] + ", sampled on the host cores as "
+                                                      "independent replicas of its structure",
+                   "config": a.config, "parallelism": f"{cores} host processes"},
         "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{cores} independent 8,000-atom + 160-element C2-structured "
-                                   f"replicas, {steps} timed steps each, {wall:.1f} s; the "
-                                   f"reference's own binary is x86-only here, so its CPU "
-                                   f"restatement (bit-identical outputs) is timed"},
+                         "sample": f"{cores} independent replicas of {s_atoms:,} atoms + "
+                                   f"{s_elems:,} elements ({s_sites:,} metric sites), {steps} "
+                                   f"timed steps each, {wall:.1f} s; the reference's own binary "
+                                   f"is built for x86 here only, so its CPU restatement "
+                                   f"(bit-identical outputs) is timed"},
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

@@ -228,6 +228,16 @@ struct cacg_context {
   long long elist_builds = 0, epart_of = -1;
   bool ereorders_zeroed = false;  // the reorder counter (d_misc slot 15)
   bool areorders_zeroed = false;  // the atom-list reorder counter (d_misc slot 16)
+  // lattice lines that the integration-point lists reference (all rows; force
+  // rows), counted at each element list build
+  DBuf<unsigned long long> d_nlines;
+  unsigned long long h_nlines[2] = {0, 0};
+  // fused element passes ("tune fused yes|no"): one warp per element when every
+  // list entry references its row's own element (checked at each element list
+  // build) and no type has more than 32 rows of nonzero weight
+  bool fused_on = true, self_contained = false, fused_types_ok = false, fused_used = false;
+  DBuf<int> d_fjj, d_fjj_off;
+  DBuf<int4> d_intp4;  // lattice indices (i, j, k) of every type's rows
   // lanes per integration point ("tune ip_group N"; 0: from the row count, so
   // that rows x lanes reach the GPU's resident threads)
   int mixed_ip_group = 0;
@@ -275,6 +285,10 @@ struct cacg_context {
   DBuf<int> d_far;
   int nfar = 0;
   DBuf<unsigned char> d_skip;
+  // re-test back-off of the far elements: steps to the next test, rejections
+  // in a row; the elements due this step (indices into d_far) and their number
+  DBuf<unsigned char> d_swait, d_sstreak;
+  DBuf<int> d_sdue, d_sdue_n, d_sfar_due;
   DBuf<unsigned short> d_sfeat;  // bf16 features [nfar][64]
   DBuf<float> d_smean, d_sspread, d_sraw;
   DBuf<unsigned long long> d_scount;  // evaluated, accepted element-steps
@@ -819,6 +833,8 @@ void cacg_context::command(const std::string &raw) {
     // tune cull yes|no: the mixed EAM density pass skips list entries that no
     //   displacement since the list reorder can bring within the cutoff
     // tune streams yes|no: a mixed step's atom and element chains on two streams
+    // tune fused yes|no: the mixed element passes one warp per element
+    //   (when every list entry references its row's own element)
     // tune elists lazy|eager: in the FP64 and mixed modes a rebuild that only
     //   atoms triggered keeps the element lists and ghosts (lazy, the default)
     if (a.size() != 2) fail(CACG_EINVAL, "Illegal tune command");
@@ -840,6 +856,10 @@ void cacg_context::command(const std::string &raw) {
     } else if (a[0] == "streams") {
       if (a[1] != "yes" && a[1] != "no") fail(CACG_EINVAL, "tune streams takes yes or no");
       two_streams = a[1] == "yes";
+      invalidate_graph();
+    } else if (a[0] == "fused") {
+      if (a[1] != "yes" && a[1] != "no") fail(CACG_EINVAL, "tune fused takes yes or no");
+      fused_on = a[1] == "yes";
       invalidate_graph();
     } else if (a[0] == "elists") {
       if (a[1] != "lazy" && a[1] != "eager") fail(CACG_EINVAL, "tune elists takes lazy or eager");
@@ -1630,6 +1650,30 @@ void cacg_context::element_tables() {
   for (size_t r = 0; r < w_all.size(); r++)
     for (int q = 0; q < NPE; q++) wn[r * NPE + q] = (float) (w_all[r] * spa_int[r * NPE + q]);
   upload(d_wn, wn, s);
+  // per type, the rows of nonzero weight in ascending order (the fused passes)
+  std::vector<int> fjj, fjj_off(MAXT + 2, 0);
+  fused_types_ok = true;
+  for (int t = 0; t <= MAXT; t++) {
+    fjj_off[t] = (int) fjj.size();
+    if (t < 1 || t > netypes) continue;
+    int nf = 0;
+    for (int jj = 0; jj < numint[t]; jj++)
+      if (w_all[int_off[t] + jj] != 0.0) {
+        fjj.push_back(jj);
+        nf++;
+      }
+    if (nf > 32) fused_types_ok = false;
+  }
+  fjj_off[MAXT + 1] = (int) fjj.size();
+  if (fjj.empty()) fjj.push_back(0);
+  upload(d_fjj, fjj, s);
+  upload(d_fjj_off, fjj_off, s);
+  std::vector<int4> ip4;
+  for (int t = 1; t <= netypes; t++)
+    for (int m = 0; m < numint[t]; m++)
+      ip4.push_back(make_int4(intp[t][3 * m], intp[t][3 * m + 1], intp[t][3 * m + 2], 0));
+  if (ip4.empty()) ip4.push_back(make_int4(0, 0, 0, 0));
+  upload(d_intp4, ip4, s);
   std::vector<float2> sihl(spa_int.size());
   for (size_t k = 0; k < spa_int.size(); k++)
     sihl[k] = make_float2((float) spa_int[k], (float) (spa_int[k] - (double) (float) spa_int[k]));
@@ -2275,7 +2319,13 @@ void cacg_context::neighbor_nbuild() {
     d_line_mask_f.ensure(nmask, s);
     mixed::line_masks(d_row_start.p, d_ent.p, nullptr, nrows, lat, d_row_isforce.p, d_line_mask.p,
                       d_line_mask_f.p, nmask, nullptr, s);
-    launches += 3;
+    d_nlines.ensure(2, s);
+    self_contained = mixed::self_check(d_row_start.p, d_ent.p, d_row_elem.p, nrows, lat, maxlines,
+                                       d_nlines.p, s) == 0;
+    mixed::count_lines(d_line_mask.p, d_line_mask_f.p, nmask, d_nlines.p, s);
+    check(cudaMemcpyAsync(h_nlines, d_nlines.p, sizeof(h_nlines), cudaMemcpyDeviceToHost, s), "nlines");
+    sync();
+    launches += 4;
   }
   elist_builds++;
   elists_built = true;
@@ -2494,20 +2544,27 @@ void cacg_context::pair_ecompute_mixed() {
   }
   check(cudaMemsetAsync(d_misc.p + 13, same_e ? 0 : 0x7F, sizeof(int), s), "edmax");
   check(cudaMemsetAsync(d_misc.p + 14, 0, sizeof(int), s), "ereordered");
+  const EamTables et = pair_style == 2 ? eamtab() : EamTables{};
+  const bool fused = fused_on && self_contained && fused_types_ok &&
+                     mixed::fused_fits(pair_style == 2 ? et.nr : 0, pair_style == 2 ? et.nrho : 0);
+  // the fused passes need the line data and row points only to reorder the lists
+  const unsigned *gate = fused ? eflags : nullptr;
+  fused_used = fused;
   kmark(KT_SITES, 0);
   mixed::node_split(d_nodex.p, nall, d_node_hl.p, same_e ? d_node_ref.p : nullptr, eflags, s);
   const mixed::Lattice lat{d_nae.p, d_frac.p, fstride, code_kb};
   // the lattice lines that the scanned entries reference (all referenced
   // lines in a step that reorders)
   mixed::lines(d_node_hl.p, d_etype.p, lat, max_nax, d_line_mask.p,
-               cull_e ? d_line_mask_n.p : nullptr, eflags, maxlines, pg, nall, d_line_pos.p, s);
+               cull_e ? d_line_mask_n.p : nullptr, eflags, maxlines, pg, nall, d_line_pos.p, s,
+               gate);
   kmark(KT_SITES, 1);
   d_ip_q.ensure(std::max(nrows, 1), s);
   d_ip_h.ensure(std::max(nrows, 1), s);
   d_ip_l.ensure(std::max(nrows, 1), s);
   kmark(KT_EPREP, 0);
   mixed::row_q(d_row_elem.p, d_row_jj.p, d_etype.p, d_int_off.p, d_spa_int_hl.p, d_node_hl.p, nrows,
-               pg, d_ip_q.p, d_ip_h.p, d_ip_l.p, s);
+               pg, d_ip_q.p, d_ip_h.p, d_ip_l.p, s, gate);
   const double csq_e = pair_style == 1 ? ljtab.cutsq[1 * (MAXT + 1) + 1] : cutforcesq;
   mixed::ip_reorder(d_row_start.p, d_ent.p, nrows, d_ip_q.p, d_line_pos.p, lat, pg,
                     (float) std::sqrt(csq_e), d_ent_near.p, d_nnear_row.p, d_node_hl.p, nall,
@@ -2548,6 +2605,53 @@ void cacg_context::pair_ecompute_mixed() {
   m.lat = lat;
   m.pg = pg;
   if (use_sur) m.skip = d_skip.p;
+  if (fused) {
+    mixed::FusedTables ft{d_node_hl.p, d_nodex.p, d_int_off.p, d_inter_off.p, d_intp4.p,
+                          d_spa_int.p, d_spa_inter.p, d_fjj.p, d_fjj_off.p, d_wn.p, maxlines};
+    if (pair_style == 1) {
+      int a = 1 * (MAXT + 1) + 1;
+      m.cutsq = ljtab.cutsq[a];
+      m.cutsq_f = (float) m.cutsq;
+      m.band_lo = m.cutsq_f * (1.0f - eps);
+      m.band_hi = m.cutsq_f * (1.0f + eps);
+      if (use_sur) {
+        kmark(KT_SUR, 0);
+        surrogate_predict(et);
+        kmark(KT_SUR, 1);
+      }
+      kmark(KT_ELEM_FORCE, 0);
+      mixed::elem_fused(m, ft, 0, nullptr, et, (float) ljtab.lj1[a], (float) ljtab.lj2[a], nullptr,
+                        nullptr, d_nodef.p, s);
+      kmark(KT_ELEM_FORCE, 1);
+      launches++;
+    } else {
+      m.cutsq = cutforcesq;
+      m.cutsq_f = (float) cutforcesq;
+      m.band_lo = m.cutsq_f * (1.0f - eps);
+      m.band_hi = m.cutsq_f * (1.0f + eps);
+      m.fp4 = d_fp4.p;
+      m.nrho = nrho;
+      m.rdrho = (float) rdrho;
+      d_erho.ensure((size_t) NPE * nall, s);
+      kmark(KT_ELEM_RHO, 0);
+      mixed::elem_fused(m, ft, 1, d_rhor_val4.p, et, 0.f, 0.f, nullptr, d_erho.p, nullptr, s);
+      kmark(KT_ELEM_RHO, 1);
+      if (use_sur) {
+        kmark(KT_SUR, 0);
+        surrogate_predict(et);
+        kmark(KT_SUR, 1);
+      }
+      kmark(KT_ELEM_FORCE, 0);
+      mixed::elem_fused(m, ft, 2, d_ftab.p, et, 0.f, 0.f, d_erho.p, nullptr, d_nodef.p, s);
+      kmark(KT_ELEM_FORCE, 1);
+      launches += 2;
+    }
+    if (use_sur) {
+      surrogate::write_forces(d_smean.p, d_far.p, d_sdue.p, d_sdue_n.p, nfar, d_skip.p, d_nodef.p, s);
+      launches++;
+    }
+    return;
+  }
   if (pair_style == 1) {
     int a = 1 * (MAXT + 1) + 1;
     m.cutsq = ljtab.cutsq[a];
@@ -2603,7 +2707,7 @@ void cacg_context::pair_ecompute_mixed() {
                       d_nodef.p, s);
   launches++;
   if (use_sur) {
-    surrogate::write_forces(d_smean.p, d_far.p, nfar, d_skip.p, d_nodef.p, s);
+    surrogate::write_forces(d_smean.p, d_far.p, d_sdue.p, d_sdue_n.p, nfar, d_skip.p, d_nodef.p, s);
     launches++;
   }
 }
@@ -2809,6 +2913,12 @@ void cacg_context::surrogate_attach(cacg_mlp_t *m, double tol, double dist) {
   upload(d_far, far.empty() ? std::vector<int>{0} : far, s);
   d_skip.ensure(std::max(enlocal, 1), s);
   check(cudaMemsetAsync(d_skip.p, 0, std::max(enlocal, 1), s), "skip");
+  d_swait.ensure(std::max(nfar, 1), s);
+  d_sstreak.ensure(std::max(nfar, 1), s);
+  check(cudaMemsetAsync(d_swait.p, 0, std::max(nfar, 1), s), "wait");
+  check(cudaMemsetAsync(d_sstreak.p, 0, std::max(nfar, 1), s), "streak");
+  d_sdue.ensure(std::max(nfar, 1), s);
+  d_sdue_n.ensure(1, s);
   d_scount.ensure(2, s);
   check(cudaMemsetAsync(d_scount.p, 0, 2 * sizeof(unsigned long long), s), "scount");
   d_sfeat.ensure((size_t) 64 * std::max(nfar, 1), s);
@@ -2820,15 +2930,22 @@ void cacg_context::surrogate_attach(cacg_mlp_t *m, double tol, double dist) {
   sync();
 }
 
+// The far elements due for a test this step are compacted on the device; their
+// features, the ensemble and the acceptance run on that list (the launches
+// cover every far element and stop at the device count).
 void cacg_context::surrogate_predict(const EamTables &) {
   mlp::Net *net = mlp::net_of(sur);
   cudaStream_t s = stream;
-  surrogate::features(d_nodex.p, d_nodex0.p, pair_style == 2 ? d_erho.p : nullptr, d_far.p, nfar,
-                      mlp::norm_device(net), d_sfeat.p, s);
-  mlp::predict(net, d_sfeat.p, nfar, d_smean.p, d_sspread.p, s);
-  surrogate::accept(d_sspread.p, d_far.p, nfar, (float) (sur_tol * mlp::force_scale(net)), d_skip.p,
+  surrogate::due(nfar, d_far.p, d_swait.p, d_skip.p, d_sdue.p, d_sdue_n.p, s);
+  d_sfar_due.ensure(std::max(nfar, 1), s);
+  surrogate::gather_far(d_far.p, d_sdue.p, d_sdue_n.p, nfar, d_sfar_due.p, s);
+  surrogate::features(d_nodex.p, d_nodex0.p, pair_style == 2 ? d_erho.p : nullptr, d_sfar_due.p,
+                      nfar, d_sdue_n.p, mlp::norm_device(net), d_sfeat.p, s);
+  mlp::predict(net, d_sfeat.p, nfar, d_smean.p, d_sspread.p, s, d_sdue_n.p);
+  surrogate::accept(d_sspread.p, d_far.p, d_sdue.p, d_sdue_n.p, nfar,
+                    (float) (sur_tol * mlp::force_scale(net)), d_skip.p, d_swait.p, d_sstreak.p,
                     d_scount.p, s);
-  launches += 3 + 1 + 3 * mlp::members(net);
+  launches += 6;
 }
 
 void cacg_context::pair_ecompute() {
@@ -3881,10 +3998,12 @@ int cacg_run_host(cacg_handle h, int nsteps, double *x, double *v, double *nodex
 
 int cacg_get_counts(cacg_handle h, long long *c, int n) {
   API_BEGIN
-  long long v[25] = {h->nlocal, h->nghost, 0, h->enlocal, h->enghost, 0, h->nrows, 0,
+  long long v[28] = {h->nlocal, h->nghost, 0, h->enlocal, h->enghost, 0, h->nrows, 0,
                      h->nrebuild, (long long) h->stencil.size(), h->ntimestep, h->nsites,
                      h->launches, h->nneed, h->nforce, 0, h->sur ? h->nfar : 0, 0, 0,
-                     h->graph_steps, 0, 0, 0, h->nrebuild_atoms, 0};
+                     h->graph_steps, 0, 0, 0, h->nrebuild_atoms, 0,
+                     (long long) h->h_nlines[0], (long long) h->h_nlines[1],
+                     h->fused_used ? 1LL : 0LL};
   if (h->areorders_zeroed && h->d_misc.p) {
     unsigned r = 0;
     check(cudaMemcpyAsync(&r, h->d_misc.p + 16, sizeof(r), cudaMemcpyDeviceToHost, h->stream), "areorders");
@@ -3961,7 +4080,7 @@ int cacg_get_counts(cacg_handle h, long long *c, int n) {
       for (const int4 &x : nn) v[21] += level == 1 ? x.x : level == 2 ? x.y : x.z;
     }
   }
-  for (int i = 0; i < n && i < 25; i++) c[i] = v[i];
+  for (int i = 0; i < n && i < 28; i++) c[i] = v[i];
   API_END
 }
 

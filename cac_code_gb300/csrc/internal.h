@@ -345,10 +345,11 @@ void node_split(const double *nodex, int n, float2 *hl, const float2 *ref, unsig
                 cudaStream_t s);
 // Lattice lines: U, D (double-single, relative to l0) of every line that
 // mask (mask_near while culling holds) marks; FP32 nodal-density lines
+// (with gate: only in a step whose node displacement calls for a list reorder)
 void lines(const float2 *node_hl, const int *etype, const Lattice &lat, int max_nax,
            const unsigned long long *mask, const unsigned long long *mask_near,
            const unsigned *eflags, int maxlines, const PackGrid &pg, int nelem, float4 *line_pos,
-           cudaStream_t s);
+           cudaStream_t s, const unsigned *gate = nullptr);
 void line_rho(const double *erho, const int *etype, const Lattice &lat,
               const unsigned long long *mask, const unsigned long long *mask_near,
               const unsigned *eflags, int maxlines, int nelem, float2 *out, cudaStream_t s);
@@ -361,6 +362,33 @@ void line_masks(const int *row_start, const int *ent, const int4 *nnear_row, int
                 const Lattice &lat, const unsigned char *isforce, unsigned long long *mask,
                 unsigned long long *mask_f, long long nmask, const unsigned *gate,
                 cudaStream_t s);
+// the fused element passes (every list entry references its row's own
+// element): per element, one warp evaluates the node rows (pass 1: nodal
+// densities) or the rows of nonzero weight with the nodal gather (pass 2: EAM
+// forces; pass 0: LJ), pair vectors from the element's trilinear coefficient
+// vectors and lattice-index differences; guard-band pairs are decided in FP64
+struct FusedTables {
+  const float2 *node_hl;      // split nodes of this step
+  const double *nodex;        // FP64 nodes
+  const int *int_off, *inter_off;  // first row / site of each type in the per-type tables
+  const int4 *intp;           // lattice indices of the rows, per type
+  const double *spa_int;      // FP64 shape functions of the rows
+  const double *spa_inter;    // FP64 shape functions of the sites
+  const int *fjj, *fjj_off;   // per type: rows of nonzero weight (at most 32), ascending
+  const float *wn;            // weight x shape function per row and node
+  int maxlines;
+};
+bool fused_fits(int nr, int nrho);
+void elem_fused(const MixedElems &m, const FusedTables &t, int pass, const float4 *tab,
+                const EamTables &e, float lj1, float lj2, const double *erho_in,
+                double *erho_out, double *nodef, cudaStream_t s);
+// list entries that reference a site of another element than their row's
+long long self_check(const int *row_start, const int *ent, const int *row_elem, int nrows,
+                     const Lattice &lat, int maxlines, unsigned long long *scratch,
+                     cudaStream_t s);
+// lattice lines with a referenced site: count[0] in mask, count[1] in mask_f
+void count_lines(const unsigned long long *mask, const unsigned long long *mask_f, long long n,
+                 unsigned long long *count, cudaStream_t s);
 // displacement culling of the integration-point lists: reorder (gated on the
 // node displacement in eflags[0]) into ent_near / nnear_row and keep the
 // nodes as the reference (eflags[1] = 1, eflags[2] counts reorders)
@@ -395,7 +423,8 @@ void lj_atoms(const MixedAtoms &m, const int *type, const float *lj1, const floa
 // every row's integration point: packed, and its double-single position
 void row_q(const int *row_elem, const int *row_jj, const int *etype, const int *int_off,
            const float2 *spa_int_hl, const float2 *node_hl, int nrows, const PackGrid &pg,
-           float4 *ip_q, float4 *ip_h, float4 *ip_l, cudaStream_t s);
+           float4 *ip_q, float4 *ip_h, float4 *ip_l, cudaStream_t s,
+           const unsigned *gate = nullptr);
 // FP32 F'(rho) at the rows of nonzero weight, rho in FP64 from the nodal densities
 void row_fp(const int *rows, int nforce, const int *row_elem, const int *row_jj,
             const int *etype, const int *int_off, const double *spa_int, const double *erho,
@@ -448,7 +477,8 @@ void gemm_tn(const void *A, int lda, const void *B, int ldb, int M, int N, int K
 // all members and layers of the surrogate in one launch (k_mlp_ensemble)
 void mlp_ensemble(const void *xf, int n, const void *w1s, const void *w2s, const void *w3s,
                   const void *w4s, const float *bias, int members, const float *norm, float *mean,
-                  float *spread, int *err, cudaStream_t s);
+                  float *spread, int *err, cudaStream_t s,
+                  const int *count = nullptr);
 }  // namespace gemm
 constexpr int MLP_IN = 32, MLP_HIDDEN = 256, MLP_OUT = 24;
 namespace mlp {
@@ -458,19 +488,30 @@ const float *norm_device(const Net *n);  // in_mean[32], in_inv_std[32], out_mea
 double force_scale(const Net *n);
 int members(const Net *n);
 // ensemble prediction on normalised bf16 features [count][64] on the device
-void predict(Net *n, const void *xf, long long count, float *mean, float *spread, cudaStream_t s);
+// count: rows to evaluate (device), or null for all
+void predict(Net *n, const void *xf, long long count, float *mean, float *spread, cudaStream_t s,
+             const int *dcount = nullptr);
 // throws when a bounded wait inside a GEMM ran out (reads a device flag)
 void check_error(Net *n, cudaStream_t s);
 }  // namespace mlp
 namespace surrogate {
+// elems[i] for i < *count (count null: i < n)
 void features(const double *nodex, const double *nodex0, const double *erho, const int *elems,
-              int n, const float *norm, void *xf, cudaStream_t s);
+              int n, const int *count, const float *norm, void *xf, cudaStream_t s);
+// the far elements due for a test this step (indices into far) and their
+// number; wait[i] counts down the steps to a far element's next test
+void due(int nfar, const int *far, unsigned char *wait, unsigned char *skip, int *due_list,
+         int *count, cudaStream_t s);
 void raw_features(const double *nodex, const double *nodex0, const double *erho, int n, float *x,
                   cudaStream_t s);
-void accept(const float *spread, const int *far, int nfar, float thr, unsigned char *skip,
+void accept(const float *spread, const int *far, const int *due_list, const int *count, int nfar,
+            float thr, unsigned char *skip, unsigned char *wait, unsigned char *streak,
             unsigned long long *counters, cudaStream_t s);
-void write_forces(const float *mean, const int *far, int nfar, const unsigned char *skip,
-                  double *nodef, cudaStream_t s);
+void write_forces(const float *mean, const int *far, const int *due_list, const int *count,
+                  int nfar, const unsigned char *skip, double *nodef, cudaStream_t s);
+// out[i] = far[due_list[i]] for i < *count
+void gather_far(const int *far, const int *due_list, const int *count, int nfar, int *out,
+                cudaStream_t s);
 void to_float(const double *src, long long n, float *dst, cudaStream_t s);
 }  // namespace surrogate
 

@@ -335,6 +335,7 @@ struct EnsArgs {
   float *mean, *spread;
   int n, members;
   int *err;
+  const int *count;  // rows to evaluate (device; null: n); CTAs past it return at once
 };
 
 __device__ __forceinline__ void ens_issue(int g, const CUtensorMap *w1, const CUtensorMap *w2,
@@ -368,6 +369,8 @@ k_mlp_ensemble(const __grid_constant__ CUtensorMap tma_x, const __grid_constant_
                const __grid_constant__ CUtensorMap tma_w2, const __grid_constant__ CUtensorMap tma_w3,
                const __grid_constant__ CUtensorMap tma_w4, EnsArgs a) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
+  const int nrows = a.count ? *a.count : a.n;
+  if ((int) blockIdx.x * BM >= nrows) return;  // before any barrier or allocation
   unsigned char *base = reinterpret_cast<unsigned char *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
   unsigned char *sx = base;
@@ -507,7 +510,7 @@ k_mlp_ensemble(const __grid_constant__ CUtensorMap tma_x, const __grid_constant_
     // let the weight copies already issued land before the CTA exits
     for (int t = g; t < issued; t++) mbar_wait(smem_u32(full + t % ENS_STAGES), (t / ENS_STAGES) & 1);
   }
-  if (ok && wg == 0 && m0 + row < a.n) {
+  if (ok && wg == 0 && m0 + row < nrows) {
     const float inv = 1.f / a.members;
     float smax = 0.f;
     float *mo = a.mean + (size_t) (m0 + row) * ENS_OUT;
@@ -608,7 +611,7 @@ void gemm_tn(const void *A, int lda, const void *B, int ldb, int M, int N, int K
 // bias[m][792] (b1, b2, b3, b4).
 void mlp_ensemble(const void *xf, int n, const void *w1s, const void *w2s, const void *w3s,
                   const void *w4s, const float *bias, int members, const float *norm, float *mean,
-                  float *spread, int *err, cudaStream_t s) {
+                  float *spread, int *err, cudaStream_t s, const int *count) {
   if (n <= 0) return;
   if (members < 1 || members > ENS_MAX_MEMBERS)
     throw CudaError{cudaErrorInvalidValue, "mlp_ensemble: 1..4 members"};
@@ -625,7 +628,7 @@ void mlp_ensemble(const void *xf, int n, const void *w1s, const void *w2s, const
           "ensemble smem attribute");
     attr = smem;
   }
-  EnsArgs a{bias, norm, mean, spread, n, members, err};
+  EnsArgs a{bias, norm, mean, spread, n, members, err, count};
   k_mlp_ensemble<<<(n + BM - 1) / BM, ENS_NT, smem, s>>>(tx, t1, t2, t3, t4, a);
   check(cudaGetLastError(), "k_mlp_ensemble");
 }

@@ -865,10 +865,12 @@ __global__ void __launch_bounds__(LCH)
 k_lines(const float2 *__restrict__ node_hl, const int *__restrict__ etype, Lattice lat,
         const unsigned long long *__restrict__ line_mask,
         const unsigned long long *__restrict__ line_mask_near, const unsigned *__restrict__ eflags,
-        int maxlines, PackGrid pg, int nelem, int max_nax, float4 *__restrict__ line_pos) {
+        int maxlines, PackGrid pg, int nelem, int max_nax, float4 *__restrict__ line_pos,
+        const unsigned *__restrict__ gate) {
   // one warp per element: [nax][3][4] P, Q, R, S of the warp's element
   extern __shared__ ds s_cols[];
   __shared__ float2 s_nodes[LCH / 32][24];
+  if (gate && moved_little(gate)) return;  // no list reorder in this step
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int e = blockIdx.x * (LCH / 32) + w;
   if (e >= nelem) return;
@@ -957,6 +959,27 @@ __global__ void k_masks_clear(unsigned long long *__restrict__ mask,
   for (long long t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     mask[t] = 0ull;
     mask_f[t] = 0ull;
+  }
+}
+
+// lattice lines with at least one referenced site, in mask and mask_f
+__global__ void k_count_lines(const unsigned long long *__restrict__ mask,
+                              const unsigned long long *__restrict__ mask_f, long long n,
+                              unsigned long long *__restrict__ count) {
+  unsigned long long a = 0, b = 0;
+  for (long long t = (long long) blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (long long) gridDim.x * blockDim.x) {
+    a += mask[t] != 0ull;
+    b += mask_f[t] != 0ull;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(count, a);
+    atomicAdd(count + 1, b);
   }
 }
 
@@ -1054,7 +1077,9 @@ __global__ void k_row_q(const int *__restrict__ row_elem, const int *__restrict_
                         const int *__restrict__ etype, const int *__restrict__ int_off,
                         const float2 *__restrict__ spa_int_hl, const float2 *__restrict__ node_hl,
                         int nrows, PackGrid pg, float4 *__restrict__ ip_q,
-                        float4 *__restrict__ ip_h, float4 *__restrict__ ip_l) {
+                        float4 *__restrict__ ip_h, float4 *__restrict__ ip_l,
+                        const unsigned *__restrict__ gate) {
+  if (gate && moved_little(gate)) return;  // no list reorder in this step
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nrows) return;
   const int e = row_elem[r], ty = etype[e];
@@ -1135,11 +1160,9 @@ __global__ void k_ip_reorder(const int *__restrict__ row_start, const int *__res
 // integration point's (ip_h + ip_l) and the site's (line data, relative to l0)
 // (arguments by value: a reference to the kernel's arrays would put them in
 // local memory on every iteration of the caller's loop)
-__device__ __noinline__ bool inside_band(const float4 *__restrict__ ip_h,
-                                         const float4 *__restrict__ ip_l, PackGrid pg,
-                                         double cutsq, int r, float x0h, float x0l, float x1h,
-                                         float x1l, float x2h, float x2l) {
-  const float4 h = __ldg(ip_h + r), l = __ldg(ip_l + r);
+__device__ __noinline__ bool inside_band_pt(float4 h, float4 l, PackGrid pg, double cutsq,
+                                            float x0h, float x0l, float x1h, float x1l,
+                                            float x2h, float x2l) {
   const double lx = (double) pg.l0h[0] + pg.l0l[0];
   const double ly = (double) pg.l0h[1] + pg.l0l[1];
   const double lz = (double) pg.l0h[2] + pg.l0l[2];
@@ -1147,6 +1170,14 @@ __device__ __noinline__ bool inside_band(const float4 *__restrict__ ip_h,
   const double dy = (((double) h.y + l.y) - ly) - ((double) x1h + x1l);
   const double dz = (((double) h.z + l.z) - lz) - ((double) x2h + x2l);
   return dx * dx + dy * dy + dz * dz < cutsq;
+}
+
+__device__ __forceinline__ bool inside_band(const float4 *__restrict__ ip_h,
+                                            const float4 *__restrict__ ip_l, PackGrid pg,
+                                            double cutsq, int r, float x0h, float x0l, float x1h,
+                                            float x1l, float x2h, float x2l) {
+  return inside_band_pt(__ldg(ip_h + r), __ldg(ip_l + r), pg, cutsq, x0h, x0l, x1h, x1l, x2h,
+                        x2l);
 }
 
 // G lanes per integration point, each taking every G-th entry of the row's
@@ -1296,6 +1327,402 @@ __global__ void k_gather_nodef_ds(const float2 *__restrict__ fipf, const int *__
     acc.add(__fmul_rn(wq, f.y));
   }
   nodef[tid] = acc.value();
+}
+
+// ---- fused element passes (self-contained elements) ----
+//
+// When every list entry of an element's rows references a site of that same
+// element (the reference's element lists are then empty: no element centre
+// lies within another's neighbor stencil, element_neighbor.cpp:11-75), every
+// pair of the element's rows lies inside the element, and one warp evaluates
+// the element whole, without forming a site position.  The element's
+// trilinear map in its lattice fractions (a, b, c) = (i, j, k) / (n - 1) is
+//   x(a, b, c) = x0 + Ka a + Kb b + Kc c + Kab ab + Kac ac + Kbc bc + Kabc abc
+// (Ka = x1 - x0, Kb = x3 - x0, Kc = x4 - x0, Kab = x0 - x1 + x2 - x3, ...,
+// shape functions of element.cpp:1340-1347); the warp keeps the seven
+// coefficient vectors as FP32, from the double-single nodes.  The pair vector
+// of a row's point p and a site s is sum_m Km (m(p) - m(s)), the monomial
+// differences formed from the integer lattice-index differences: FP32
+// roundings of a few 1e-7 A per pair (the coefficients' own roundings deform
+// the element smoothly, by about 1e-6 A over its length).  The nodal
+// densities enter the same way (rho(a, b, c) with scalar coefficients).
+// Pairs whose FP32 squared distance falls in the 1e-4 guard band around the
+// cutoff are decided in FP64 from the FP64 nodes and shape functions
+// (Spa_inter_ele, Spa_int), so the set of interacting pairs is the FP64 set.
+// Sums: FP32 over chunks of 8 pairs, double-single across chunks and lanes;
+// F'(rho) of the rows in FP64 (k_row_fp), of the sites in FP32.
+constexpr int FG = 4;           // lanes per row: 8 rows per warp
+constexpr int FUSED_MAXF = 32;  // rows of nonzero weight per type, at most
+constexpr int FUSED_BLOCK = 512;
+
+struct FusedArgs {
+  const float2 *node_hl;       // split nodes of this step
+  const double *nodex;         // FP64 nodes (guard-band decisions)
+  const int *etype, *row_first, *node_list, *int_off, *inter_off;
+  const int4 *intp;            // lattice indices (i, j, k) of every type's rows
+  const double *spa_int;       // FP64 shape functions of the rows
+  const double *spa_inter;     // FP64 shape functions of the sites
+  const int *fjj, *fjj_off;    // per type: the rows of nonzero weight, ascending
+  const float *wn;             // weight x shape function per row and node
+  const int *row_start, *ent;  // row-major line codes, culling parts in order
+  const int4 *nnear_row;
+  const unsigned *eflags;
+  int nlocal_e, maxlines;
+  float cutsq_f, band_lo, band_hi;
+  double cutsq;
+  const unsigned char *skip;   // elements the surrogate evaluates
+  Lattice lat;
+  const float4 *fp4;           // FP32 F' spline (sites)
+  int nrho;
+  float rdrho;
+  const double *frho;          // FP64 F spline (rows)
+  double rdrho64;
+};
+
+// the trilinear coefficient vectors of the element: k[3 m + d], m = a, b, c,
+// ab, ac, bc, abc (lanes 0..20), from the double-single nodes
+__device__ __forceinline__ void fused_coeffs(const float2 *__restrict__ node_hl, int e, int lane,
+                                             float *s_k) {
+  if (lane < 21) {
+    const int m = lane / 3, d = lane % 3;
+    const float2 *nx = node_hl + 24 * (size_t) e + d;
+    auto X = [&](int k) { return ds{nx[3 * k].x, nx[3 * k].y}; };
+    ds v;
+    switch (m) {
+      case 0: v = ds_sub(X(1), X(0)); break;
+      case 1: v = ds_sub(X(3), X(0)); break;
+      case 2: v = ds_sub(X(4), X(0)); break;
+      case 3: v = ds_add(ds_sub(X(0), X(1)), ds_sub(X(2), X(3))); break;
+      case 4: v = ds_add(ds_sub(X(0), X(1)), ds_sub(X(5), X(4))); break;
+      case 5: v = ds_add(ds_sub(X(0), X(3)), ds_sub(X(7), X(4))); break;
+      default:
+        v = ds_add(ds_add(ds_sub(X(1), X(0)), ds_sub(X(3), X(2))),
+                   ds_add(ds_sub(X(4), X(5)), ds_sub(X(6), X(7))));
+    }
+    s_k[lane] = v.h + v.l;
+  }
+}
+
+// FP64 cutoff decision of a guard-band pair: the row's point and the site from
+// the FP64 nodes and shape functions
+__device__ __noinline__ bool fused_band64(const double *N, const double *M, const double *x,
+                                          double cutsq) {
+  double rsq = 0.0;
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    double p = 0.0, q = 0.0;
+#pragma unroll
+    for (int k = 0; k < NPE; k++) {
+      p += N[k] * x[3 * k + d];
+      q += M[k] * x[3 * k + d];
+    }
+    rsq += (p - q) * (p - q);
+  }
+  return rsq < cutsq;
+}
+
+// lattice geometry of a type as the kernels use it
+struct FusedLat {
+  int nay, naz;
+  float ia, ib, ic;     // 1 / (n - 1) per axis
+  float inay;           // 1 / nay, for the line's (ii, jj)
+};
+
+// one row of the element, FG lanes: the scan of its culled list, pair vectors
+// from the coefficient vectors k (registers) and the row's lattice indices
+// F'(rho) from the FP32 coefficient table in shared memory (fprime32's arithmetic)
+__device__ __forceinline__ float fprime32_s(float rho, const float4 *s_fp, int nrho, float rdrho) {
+  float p = rho * rdrho + 1.0f;
+  int m = (int) p;
+  m = m < nrho - 1 ? m : nrho - 1;
+  m = 1 > m ? 1 : m;
+  p -= (float) m;
+  p = fminf(p, 1.0f);
+  const float4 c = s_fp[m];
+  return (c.x * p + c.y) * p + c.z;
+}
+
+template <bool EAM, bool DENSITY>
+__device__ __forceinline__ void fused_row(const FusedArgs &a, const FusedLat &g, int e, int ty,
+                                          int jj, int level, int glane, const float (&k)[21],
+                                          const float (&rk)[8], const float4 *s_tab,
+                                          const float4 *s_fp, int nr,
+                                          float rdr, float fpi, float lj1, float lj2, bool live,
+                                          dsacc &acc, dsacc &fx, dsacc &fy, dsacc &fz) {
+  int n = 0, s0 = 0;
+  int ip = 0, jp = 0, kp = 0;
+  if (live) {
+    const int r = a.row_first[e] + jj;
+    s0 = a.row_start[r];
+    n = level < 4 ? culled_count(level, a.nnear_row[r], 0) : a.row_start[r + 1] - s0;
+    const int4 q = a.intp[a.int_off[ty] + jj];
+    ip = q.x;
+    jp = q.y;
+    kp = q.z;
+  }
+  const float ap = (float) ip * g.ia, bp = (float) jp * g.ib, cp = (float) kp * g.ic;
+  const float abp = ap * bp;
+  const int lbase = e * a.maxlines;
+  float part = 0.f, px = 0.f, py = 0.f, pz = 0.f;
+  int cn = 0, cnt = 0;
+  if (glane < n) cn = __ldg(a.ent + s0 + glane);
+  for (int t = glane; t < n; t += FG) {
+    const int code = cn;
+    if (t + FG < n) cn = __ldg(a.ent + s0 + t + FG);
+    const int L = code_line(a.lat, code) - lbase, kk = code_kk(a.lat, code);
+    const int ii = (int) (((float) L + 0.5f) * g.inay);
+    const int js = L - ii * g.nay;
+    // monomial differences m(p) - m(s)
+    const float da = (float) (ip - ii) * g.ia, db = (float) (jp - js) * g.ib,
+                dc = (float) (kp - kk) * g.ic;
+    const float dab = fmaf(ap, db, fmaf(bp, da, -da * db));
+    const float dac = fmaf(ap, dc, fmaf(cp, da, -da * dc));
+    const float dbc = fmaf(bp, dc, fmaf(cp, db, -db * dc));
+    const float dabc = fmaf(abp, dc, fmaf(cp, dab, -dab * dc));
+    float v[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      float w = k[d] * da;
+      w = fmaf(k[3 + d], db, w);
+      w = fmaf(k[6 + d], dc, w);
+      w = fmaf(k[9 + d], dab, w);
+      w = fmaf(k[12 + d], dac, w);
+      w = fmaf(k[15 + d], dbc, w);
+      v[d] = fmaf(k[18 + d], dabc, w);
+    }
+    const float dx = v[0], dy = v[1], dz = v[2];
+    const float rsq = dx * dx + dy * dy + dz * dz;
+    bool in = rsq < a.cutsq_f;
+    if (rsq >= a.band_lo && rsq <= a.band_hi)
+      in = fused_band64(a.spa_int + ((size_t) a.int_off[ty] + jj) * NPE,
+                        a.spa_inter + ((size_t) a.inter_off[ty] + L * g.naz + kk) * NPE,
+                        a.nodex + 24 * (size_t) e, a.cutsq);
+    if (in) {
+      if (EAM) {
+        const float recip = rsqrtf(rsq);
+        const float rr = rsq * recip;
+        float p;
+        const int m = findex(rr, rdr, nr, p);
+        if (DENSITY) {
+          const float4 cc = s_tab[m];
+          part += ((cc.x * p + cc.y) * p + cc.z) * p + cc.w;
+        } else {
+          // the site's density from the nodal densities: rho(p) - sum Rm (m(p) - m(s))
+          float dr = rk[1] * da;
+          dr = fmaf(rk[2], db, dr);
+          dr = fmaf(rk[3], dc, dr);
+          dr = fmaf(rk[4], dab, dr);
+          dr = fmaf(rk[5], dac, dr);
+          dr = fmaf(rk[6], dbc, dr);
+          dr = fmaf(rk[7], dabc, dr);
+          const float fpj = fprime32_s(rk[0] - dr, s_fp, a.nrho, a.rdrho);
+          float rhoip, z2, z2p;
+          force_spline(s_tab, m, p, rdr, rhoip, z2, z2p);
+          const float phi = z2 * recip;
+          const float phip = z2p * recip - phi * recip;
+          const float psip = (fpi + fpj) * rhoip + phip;
+          const float fpair = -psip * recip;
+          px += dx * fpair;
+          py += dy * fpair;
+          pz += dz * fpair;
+        }
+      } else {
+        const float r2inv = __frcp_rn(rsq);
+        const float r6inv = r2inv * r2inv * r2inv;
+        const float fpair = r6inv * (lj1 * r6inv - lj2) * r2inv;
+        px += dx * fpair;
+        py += dy * fpair;
+        pz += dz * fpair;
+      }
+      if ((++cnt & (CHUNK - 1)) == 0) {
+        acc.add(part);
+        fx.add(px);
+        fy.add(py);
+        fz.add(pz);
+        part = px = py = pz = 0.f;
+      }
+    }
+  }
+  if (DENSITY) {
+    acc.add(part);
+    group_sum<FG>(acc);
+  } else {
+    fx.add(px);
+    fy.add(py);
+    fz.add(pz);
+    group_sum<FG>(fx);
+    group_sum<FG>(fy);
+    group_sum<FG>(fz);
+  }
+}
+
+__device__ __forceinline__ FusedLat fused_lat(const Lattice &lat, int ty) {
+  FusedLat g;
+  const int nax = lat.nae[3 * ty], nay = lat.nae[3 * ty + 1], naz = lat.nae[3 * ty + 2];
+  g.nay = nay;
+  g.naz = naz;
+  g.ia = nax > 1 ? 1.0f / (float) (nax - 1) : 0.f;
+  g.ib = nay > 1 ? 1.0f / (float) (nay - 1) : 0.f;
+  g.ic = naz > 1 ? 1.0f / (float) (naz - 1) : 0.f;
+  g.inay = 1.0f / (float) nay;
+  return g;
+}
+
+// per-warp shared memory: coefficient vectors (21), density coefficients (8),
+// row forces (3 per row of nonzero weight)
+constexpr int FUSED_WARP_FLOATS = 32 + 2 * 3 * FUSED_MAXF;
+
+// EAM nodal densities: the element's 8 node rows, one row per FG lanes
+__global__ void __launch_bounds__(FUSED_BLOCK, 1)
+k_elem_rho_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rdr,
+                 double *__restrict__ erho) {
+  extern __shared__ float4 smem[];
+  float4 *s_tab = smem;
+  for (int m = threadIdx.x; m <= nr; m += blockDim.x) s_tab[m] = tab[m];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float *s_k = reinterpret_cast<float *>(smem + nr + 1) + (size_t) w * FUSED_WARP_FLOATS;
+  __syncthreads();
+  const int gw = (int) (((long long) blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int nw = (int) (((long long) gridDim.x * blockDim.x) >> 5);
+  const int level = a.nnear_row ? cull_level(a.eflags) : 4;
+  const int gsub = lane / FG, glane = lane % FG;
+  const float rk[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  for (int e = gw; e < a.nlocal_e; e += nw) {
+    const int ty = a.etype[e];
+    const FusedLat g = fused_lat(a.lat, ty);
+    fused_coeffs(a.node_hl, e, lane, s_k);
+    __syncwarp();
+    float k[21];
+#pragma unroll
+    for (int q = 0; q < 21; q++) k[q] = s_k[q];
+    for (int kb = 0; kb < NPE; kb += 32 / FG) {
+      const int q = kb + gsub;
+      const bool live = q < NPE;
+      const int jj = live ? a.node_list[ty * NPE + q] : 0;
+      dsacc acc, fx, fy, fz;
+      fused_row<true, true>(a, g, e, ty, jj, level, glane, k, rk, s_tab, nullptr, nr, rdr, 0.f,
+                            0.f, 0.f, live, acc, fx, fy, fz);
+      if (live && glane == 0) erho[NPE * (size_t) e + q] = acc.value();
+    }
+    __syncwarp();
+  }
+}
+
+// Forces of the element's rows of nonzero weight and their gather onto the
+// nodes (EAM with the nodal densities and row F'(rho), or LJ)
+template <bool EAM>
+__global__ void __launch_bounds__(FUSED_BLOCK, 1)
+k_elem_force_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rdr, float lj1,
+                   float lj2, const double *__restrict__ erho, double *__restrict__ nodef) {
+  extern __shared__ float4 smem[];
+  float4 *s_tab = smem;
+  const int ntab = EAM ? FTAB_W * (nr + 1) : 0;
+  const int nfp = EAM ? a.nrho + 1 : 0;
+  float4 *s_fp = smem + ntab;
+  for (int m = threadIdx.x; m < ntab; m += blockDim.x) s_tab[m] = tab[m];
+  for (int m = threadIdx.x; m < nfp; m += blockDim.x) s_fp[m] = a.fp4[m];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float *s_k = reinterpret_cast<float *>(smem + ntab + nfp) + (size_t) w * FUSED_WARP_FLOATS;
+  float *s_r = s_k + 24;
+  float2 *s_f = reinterpret_cast<float2 *>(s_k + 32);
+  __syncthreads();
+  const int gw = (int) (((long long) blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int nw = (int) (((long long) gridDim.x * blockDim.x) >> 5);
+  const int level = a.nnear_row ? cull_level(a.eflags) : 4;
+  const int gsub = lane / FG, glane = lane % FG;
+  for (int e = gw; e < a.nlocal_e; e += nw) {
+    if (a.skip && a.skip[e]) continue;  // nodal forces from the surrogate (warp-uniform)
+    const int ty = a.etype[e];
+    const FusedLat g = fused_lat(a.lat, ty);
+    const int f0 = a.fjj_off[ty], nf = a.fjj_off[ty + 1] - f0;
+    fused_coeffs(a.node_hl, e, lane, s_k);
+    if (EAM && lane >= 24) {  // density coefficients from the nodal densities (FP32)
+      const double *er = erho + NPE * (size_t) e;
+      const int m = lane - 24;
+      float v;
+      switch (m) {
+        case 0: v = (float) er[0]; break;
+        case 1: v = (float) (er[1] - er[0]); break;
+        case 2: v = (float) (er[3] - er[0]); break;
+        case 3: v = (float) (er[4] - er[0]); break;
+        case 4: v = (float) ((er[0] - er[1]) + (er[2] - er[3])); break;
+        case 5: v = (float) ((er[0] - er[1]) + (er[5] - er[4])); break;
+        case 6: v = (float) ((er[0] - er[3]) + (er[7] - er[4])); break;
+        default: v = (float) (((er[1] - er[0]) + (er[3] - er[2])) + ((er[4] - er[5]) + (er[6] - er[7])));
+      }
+      s_r[m] = v;
+    }
+    __syncwarp();
+    float k[21];
+#pragma unroll
+    for (int q = 0; q < 21; q++) k[q] = s_k[q];
+    float rk[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int fb = 0; fb < nf; fb += 32 / FG) {
+      const int j = fb + gsub;
+      const bool live = j < nf;
+      const int jj = live ? a.fjj[f0 + j] : 0;
+      float fpi = 0.f;
+      if (EAM) {
+        // F'(rho) at the row, rho in FP64 from the nodal densities (k_row_fp);
+        // the row's density in FP32 for the sites' (rho(p) in rk[0])
+        float rho32 = 0.f;
+        if (live && glane == 0) {
+          const double *N = a.spa_int + ((size_t) a.int_off[ty] + jj) * NPE;
+          double rho = 0.0;
+#pragma unroll
+          for (int q = 0; q < NPE; q++) rho += N[q] * erho[NPE * (size_t) e + q];
+          fpi = (float) fprime64(rho, a.frho, a.nrho, a.rdrho64);
+          rho32 = (float) rho;
+        }
+        fpi = __shfl_sync(0xffffffffu, fpi, lane & ~(FG - 1));
+        rk[0] = __shfl_sync(0xffffffffu, rho32, lane & ~(FG - 1));
+#pragma unroll
+        for (int q = 1; q < 8; q++) rk[q] = s_r[q];
+      }
+      dsacc acc, fx, fy, fz;
+      fused_row<EAM, false>(a, g, e, ty, jj, level, glane, k, rk, s_tab, s_fp, nr, rdr, fpi,
+                            lj1, lj2, live, acc, fx, fy, fz);
+      if (live && glane == 0) {
+        s_f[3 * j] = make_float2(fx.h, fx.l);
+        s_f[3 * j + 1] = make_float2(fy.h, fy.l);
+        s_f[3 * j + 2] = make_float2(fz.h, fz.l);
+      }
+    }
+    __syncwarp();
+    if (lane < 24) {  // the nodal gather (k_gather_nodef_ds), rows in ascending order
+      const int q = lane / 3, c = lane % 3;
+      const float *wt = a.wn + (size_t) a.int_off[ty] * NPE;
+      dsacc acc;
+      for (int j = 0; j < nf; j++) {
+        const float wq = __ldg(wt + a.fjj[f0 + j] * NPE + q);
+        if (wq == 0.f) continue;
+        const float2 f = s_f[3 * j + c];
+        acc.add(__fmul_rn(wq, f.x));
+        acc.add(__fmul_rn(wq, f.y));
+      }
+      nodef[24 * (size_t) e + lane] = acc.value();
+    }
+    __syncwarp();
+  }
+}
+
+// every entry of every row references a site of the row's own element:
+// count the entries that do not
+__global__ void k_self_check(const int *__restrict__ row_start, const int *__restrict__ ent,
+                             const int *__restrict__ row_elem, int nrows, Lattice lat,
+                             int maxlines, unsigned long long *__restrict__ foreign) {
+  unsigned long long c = 0;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += gridDim.x * blockDim.x) {
+    const int e = row_elem[r];
+    const long long lo = (long long) e * maxlines, hi = lo + maxlines;
+    for (int k = row_start[r]; k < row_start[r + 1]; k++) {
+      const long long L = code_line(lat, __ldg(ent + k));
+      c += L < lo || L >= hi;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(foreign, c);
 }
 
 inline int nblk(long long n, int t) { return (int) ((n + t - 1) / t); }
@@ -1463,12 +1890,12 @@ void node_split(const double *nodex, int n, float2 *hl, const float2 *ref, unsig
 void lines(const float2 *node_hl, const int *etype, const Lattice &lat, int max_nax,
            const unsigned long long *mask, const unsigned long long *mask_near,
            const unsigned *eflags, int maxlines, const PackGrid &pg, int nelem, float4 *line_pos,
-           cudaStream_t s) {
+           cudaStream_t s, const unsigned *gate) {
   if (nelem <= 0) return;
   const size_t smem = sizeof(ds) * 12 * (size_t) max_nax * (LCH / 32);
   const int grid = (nelem + LCH / 32 - 1) / (LCH / 32);
   k_lines<<<grid, LCH, smem, s>>>(node_hl, etype, lat, mask, mask_near, eflags, maxlines, pg,
-                                  nelem, max_nax, line_pos);
+                                  nelem, max_nax, line_pos, gate);
   check(cudaGetLastError(), "lines");
 }
 
@@ -1502,6 +1929,15 @@ void line_masks(const int *row_start, const int *ent, const int4 *nnear_row, int
   check(cudaGetLastError(), "line_masks");
 }
 
+void count_lines(const unsigned long long *mask, const unsigned long long *mask_f, long long n,
+                 unsigned long long *count, cudaStream_t s) {
+  check(cudaMemsetAsync(count, 0, 2 * sizeof(unsigned long long), s), "count_lines");
+  if (n <= 0) return;
+  const int g = persistent_grid((const void *) k_count_lines, 256, 0, n);
+  k_count_lines<<<g, 256, 0, s>>>(mask, mask_f, n, count);
+  check(cudaGetLastError(), "count_lines");
+}
+
 void ip_reorder(const int *row_start, const int *ent, int nrows, const float4 *ip_q,
                 const float4 *line_pos, const Lattice &lat, const PackGrid &pg, float cutoff,
                 int *ent_near, int4 *nnear_row, const float2 *node_hl, int nall_e,
@@ -1516,10 +1952,10 @@ void ip_reorder(const int *row_start, const int *ent, int nrows, const float4 *i
 
 void row_q(const int *row_elem, const int *row_jj, const int *etype, const int *int_off,
            const float2 *spa_int_hl, const float2 *node_hl, int nrows, const PackGrid &pg,
-           float4 *ip_q, float4 *ip_h, float4 *ip_l, cudaStream_t s) {
+           float4 *ip_q, float4 *ip_h, float4 *ip_l, cudaStream_t s, const unsigned *gate) {
   if (nrows <= 0) return;
   k_row_q<<<nblk(nrows, 128), 128, 0, s>>>(row_elem, row_jj, etype, int_off, spa_int_hl, node_hl,
-                                          nrows, pg, ip_q, ip_h, ip_l);
+                                          nrows, pg, ip_q, ip_h, ip_l, gate);
   check(cudaGetLastError(), "row_q");
 }
 
@@ -1572,6 +2008,86 @@ void ip_pass(const MixedElems &m, int pass, const float4 *tab, const EamTables &
   else  // EAM forces
     launch_ip<true, false>(a, m.nforce, m.block, m.group, tab, e, 0.f, 0.f, out, outf, s);
   check(cudaGetLastError(), "ip_pass_mixed");
+}
+
+bool fused_fits(int nr, int nrho) {
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const size_t need = sizeof(float4) * (FTAB_W * (size_t) (nr + 1) + (size_t) (nrho + 1)) +
+                      sizeof(float) * FUSED_WARP_FLOATS * (FUSED_BLOCK / 32);
+  return need <= (size_t) optin;
+}
+
+void elem_fused(const MixedElems &m, const FusedTables &t, int pass, const float4 *tab,
+                const EamTables &e, float lj1, float lj2, const double *erho_in, double *erho_out,
+                double *nodef, cudaStream_t s) {
+  if (m.nlocal_e <= 0) return;
+  FusedArgs a{};
+  a.node_hl = t.node_hl;
+  a.nodex = t.nodex;
+  a.etype = m.etype;
+  a.row_first = m.row_first;
+  a.node_list = m.node_list;
+  a.int_off = t.int_off;
+  a.inter_off = t.inter_off;
+  a.intp = t.intp;
+  a.spa_int = t.spa_int;
+  a.spa_inter = t.spa_inter;
+  a.fjj = t.fjj;
+  a.fjj_off = t.fjj_off;
+  a.wn = t.wn;
+  a.row_start = m.row_start;
+  a.ent = m.ent;
+  a.nnear_row = m.nnear_row;
+  a.eflags = m.eflags;
+  a.nlocal_e = m.nlocal_e;
+  a.maxlines = t.maxlines;
+  a.cutsq_f = m.cutsq_f;
+  a.band_lo = m.band_lo;
+  a.band_hi = m.band_hi;
+  a.cutsq = m.cutsq;
+  a.skip = m.skip;
+  a.lat = m.lat;
+  a.fp4 = m.fp4;
+  a.nrho = m.nrho;
+  a.rdrho = m.rdrho;
+  a.frho = e.frho;
+  a.rdrho64 = e.rdrho;
+  const bool force = pass != 1;
+  const bool eam = pass != 0;
+  const size_t table =
+      eam ? sizeof(float4) * ((force ? FTAB_W : 1) * (size_t) (e.nr + 1) + (force ? e.nrho + 1 : 0))
+          : 0;
+  const size_t smem = table + sizeof(float) * FUSED_WARP_FLOATS * (FUSED_BLOCK / 32);
+  const long long items = (long long) m.nlocal_e * 32;
+  if (pass == 1) {
+    const int g = persistent_grid((const void *) k_elem_rho_fused, FUSED_BLOCK, smem, items);
+    k_elem_rho_fused<<<g, FUSED_BLOCK, smem, s>>>(a, tab, e.nr, (float) e.rdr, erho_out);
+  } else if (pass == 2) {
+    const int g = persistent_grid((const void *) k_elem_force_fused<true>, FUSED_BLOCK, smem, items);
+    k_elem_force_fused<true><<<g, FUSED_BLOCK, smem, s>>>(a, tab, e.nr, (float) e.rdr, 0.f, 0.f,
+                                                          erho_in, nodef);
+  } else {
+    const int g = persistent_grid((const void *) k_elem_force_fused<false>, FUSED_BLOCK, smem, items);
+    k_elem_force_fused<false><<<g, FUSED_BLOCK, smem, s>>>(a, nullptr, 0, 0.f, lj1, lj2, nullptr,
+                                                           nodef);
+  }
+  check(cudaGetLastError(), "elem_fused");
+}
+
+long long self_check(const int *row_start, const int *ent, const int *row_elem, int nrows,
+                     const Lattice &lat, int maxlines, unsigned long long *scratch,
+                     cudaStream_t s) {
+  if (nrows <= 0) return 0;
+  check(cudaMemsetAsync(scratch, 0, sizeof(unsigned long long), s), "self_check");
+  const int g = persistent_grid((const void *) k_self_check, 256, 0, nrows);
+  k_self_check<<<g, 256, 0, s>>>(row_start, ent, row_elem, nrows, lat, maxlines, scratch);
+  check(cudaGetLastError(), "self_check");
+  unsigned long long c = 0;
+  check(cudaMemcpyAsync(&c, scratch, sizeof(c), cudaMemcpyDeviceToHost, s), "self_check");
+  check(cudaStreamSynchronize(s), "self_check");
+  return (long long) c;
 }
 
 void gather_nodef(const float2 *fipf, const int *etype, const int *row_first, const int *numint,

@@ -5,6 +5,11 @@
 //   features  -> 24 nodal displacements about their mean, relative to the
 //                ideal node positions, then the 8 nodal densities, normalised
 //                and rounded to bf16 [n][64] (zero padded) for the GEMMs;
+//   due       -> the far elements tested this step: an element whose spread
+//                exceeded the threshold is re-tested after 1, 3, 7, then 15
+//                steps (the quadrature evaluates it meanwhile); an accepted
+//                element is tested every step.  The list is compacted on the
+//                device, with its length in a device counter;
 //   accept    -> skip[e] = (ensemble spread <= threshold); counts evaluated
 //                and accepted elements on the device;
 //   write     -> nodef[e] = ensemble mean for the accepted elements, after the
@@ -39,9 +44,10 @@ __device__ __forceinline__ void element_features(const double *__restrict__ node
 
 __global__ void k_features(const double *__restrict__ nodex, const double *__restrict__ nodex0,
                            const double *__restrict__ erho, const int *__restrict__ elems, int n,
-                           const float *__restrict__ norm, __nv_bfloat16 *__restrict__ out) {
+                           const int *__restrict__ count, const float *__restrict__ norm,
+                           __nv_bfloat16 *__restrict__ out) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= (count ? *count : n)) return;
   float f[MLP_IN];
   element_features(nodex, nodex0, erho, elems[i], f);
   __nv_bfloat16 *o = out + 64 * (size_t) i;
@@ -61,30 +67,69 @@ __global__ void k_raw_features(const double *__restrict__ nodex, const double *_
   for (int c = 0; c < MLP_IN; c++) out[(size_t) e * MLP_IN + c] = f[c];
 }
 
-__global__ void k_accept(const float *__restrict__ spread, const int *__restrict__ far, int nfar,
+// The far elements due for a test this step, compacted into due[] (indices
+// into far) with *count; every far element starts the step on the quadrature
+__global__ void k_due(int nfar, const int *__restrict__ far, unsigned char *__restrict__ wait,
+                      unsigned char *__restrict__ skip, int *__restrict__ due,
+                      int *__restrict__ count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool d = false;
+  if (i < nfar) {
+    skip[far[i]] = 0;
+    const unsigned char w = wait[i];
+    d = w == 0;
+    if (!d) wait[i] = (unsigned char) (w - 1);
+  }
+  const unsigned b = __ballot_sync(0xffffffffu, d);
+  int base = 0;
+  if ((threadIdx.x & 31) == 0 && b) base = atomicAdd(count, __popc(b));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (d) due[base + __popc(b & ((1u << (threadIdx.x & 31)) - 1u))] = i;
+}
+
+// due[] indexes far[]; the features, means and spreads are in due order.  A
+// rejection doubles the element's re-test interval (1, 3, 7, 15 steps), an
+// acceptance resets it
+__global__ void k_accept(const float *__restrict__ spread, const int *__restrict__ far,
+                         const int *__restrict__ due, const int *__restrict__ count, int nfar,
                          float thr, unsigned char *__restrict__ skip,
+                         unsigned char *__restrict__ wait, unsigned char *__restrict__ streak,
                          unsigned long long *__restrict__ counters) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = count ? *count : nfar;
   bool acc = false;
-  if (i < nfar) {
+  if (i < n) {
+    const int f = due ? due[i] : i;
     acc = spread[i] <= thr;
-    skip[far[i]] = acc ? 1 : 0;
+    skip[far[f]] = acc ? 1 : 0;
+    if (wait) {
+      const unsigned char st = acc ? 0 : (unsigned char) min(streak[f] + 1, 4);
+      streak[f] = st;
+      wait[f] = (unsigned char) ((1u << st) - 1u);
+    }
   }
   unsigned b = __ballot_sync(0xffffffffu, acc);
-  unsigned v = __ballot_sync(0xffffffffu, i < nfar);
+  unsigned v = __ballot_sync(0xffffffffu, i < n);
   if ((threadIdx.x & 31) == 0) {
     if (v) atomicAdd(counters, (unsigned long long) __popc(v));
     if (b) atomicAdd(counters + 1, (unsigned long long) __popc(b));
   }
 }
 
-__global__ void k_write(const float *__restrict__ mean, const int *__restrict__ far, int nfar,
+__global__ void k_write(const float *__restrict__ mean, const int *__restrict__ far,
+                        const int *__restrict__ due, const int *__restrict__ count, int nfar,
                         const unsigned char *__restrict__ skip, double *__restrict__ nodef) {
   long i = blockIdx.x * (long) blockDim.x + threadIdx.x;
-  if (i >= (long) nfar * MLP_OUT) return;
+  if (i >= (long) (count ? *count : nfar) * MLP_OUT) return;
   int r = (int) (i / MLP_OUT), c = (int) (i % MLP_OUT);
-  int e = far[r];
+  int e = far[due ? due[r] : r];
   if (skip[e]) nodef[(size_t) MLP_OUT * e + c] = (double) mean[i];
+}
+
+__global__ void k_gather_far(const int *__restrict__ far, const int *__restrict__ due,
+                             const int *__restrict__ count, int *__restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < *count) out[i] = far[due[i]];
 }
 
 __global__ void k_to_float(const double *__restrict__ src, long n, float *__restrict__ dst) {
@@ -95,9 +140,9 @@ __global__ void k_to_float(const double *__restrict__ src, long n, float *__rest
 }  // namespace
 
 void features(const double *nodex, const double *nodex0, const double *erho, const int *elems,
-              int n, const float *norm, void *xf, cudaStream_t s) {
+              int n, const int *count, const float *norm, void *xf, cudaStream_t s) {
   if (n <= 0) return;
-  k_features<<<nblk(n, 128), 128, 0, s>>>(nodex, nodex0, erho, elems, n, norm,
+  k_features<<<nblk(n, 128), 128, 0, s>>>(nodex, nodex0, erho, elems, n, count, norm,
                                           static_cast<__nv_bfloat16 *>(xf));
   check(cudaGetLastError(), "surrogate features");
 }
@@ -109,18 +154,36 @@ void raw_features(const double *nodex, const double *nodex0, const double *erho,
   check(cudaGetLastError(), "surrogate raw features");
 }
 
-void accept(const float *spread, const int *far, int nfar, float thr, unsigned char *skip,
+void due(int nfar, const int *far, unsigned char *wait, unsigned char *skip, int *due_list,
+         int *count, cudaStream_t s) {
+  check(cudaMemsetAsync(count, 0, sizeof(int), s), "surrogate due");
+  if (nfar <= 0) return;
+  k_due<<<nblk(nfar, 256), 256, 0, s>>>(nfar, far, wait, skip, due_list, count);
+  check(cudaGetLastError(), "surrogate due");
+}
+
+void accept(const float *spread, const int *far, const int *due_list, const int *count, int nfar,
+            float thr, unsigned char *skip, unsigned char *wait, unsigned char *streak,
             unsigned long long *counters, cudaStream_t s) {
   if (nfar <= 0) return;
-  k_accept<<<nblk(nfar, 256), 256, 0, s>>>(spread, far, nfar, thr, skip, counters);
+  k_accept<<<nblk(nfar, 256), 256, 0, s>>>(spread, far, due_list, count, nfar, thr, skip, wait,
+                                           streak, counters);
   check(cudaGetLastError(), "surrogate accept");
 }
 
-void write_forces(const float *mean, const int *far, int nfar, const unsigned char *skip,
-                  double *nodef, cudaStream_t s) {
+void write_forces(const float *mean, const int *far, const int *due_list, const int *count,
+                  int nfar, const unsigned char *skip, double *nodef, cudaStream_t s) {
   if (nfar <= 0) return;
-  k_write<<<nblk((long long) nfar * MLP_OUT, 256), 256, 0, s>>>(mean, far, nfar, skip, nodef);
+  k_write<<<nblk((long long) nfar * MLP_OUT, 256), 256, 0, s>>>(mean, far, due_list, count, nfar,
+                                                                 skip, nodef);
   check(cudaGetLastError(), "surrogate write");
+}
+
+void gather_far(const int *far, const int *due_list, const int *count, int nfar, int *out,
+                cudaStream_t s) {
+  if (nfar <= 0) return;
+  k_gather_far<<<nblk(nfar, 256), 256, 0, s>>>(far, due_list, count, out);
+  check(cudaGetLastError(), "surrogate gather_far");
 }
 
 void to_float(const double *src, long long n, float *dst, cudaStream_t s) {

@@ -398,7 +398,8 @@ struct Net {
   // one fused launch over all members and layers (gemm::mlp_ensemble)
   DBuf<bf16> iw2, iw3, iw4;
   DBuf<float> ibias;
-  void predict_device(const bf16 *xf, long long n, float *mean, float *spread, cudaStream_t s) {
+  void predict_device(const bf16 *xf, long long n, float *mean, float *spread, cudaStream_t s,
+                      const int *dcount = nullptr) {
     if (n <= 0) return;
     ensure_err(s);
     if (!stacked) {
@@ -423,7 +424,7 @@ struct Net {
       stacked = true;
     }
     gemm::mlp_ensemble(xf, (int) n, iw1.p, iw2.p, iw3.p, iw4.p, ibias.p, members, d_norm.p, mean,
-                       spread, errflag.p, s);
+                       spread, errflag.p, s, dcount);
   }
 };
 
@@ -431,9 +432,10 @@ Net *net_of(cacg_mlp_t *m);
 const float *norm_device(const Net *n) { return n->d_norm.p; }
 double force_scale(const Net *n) { return n->force_scale; }
 int members(const Net *n) { return n->members; }
-void predict(Net *n, const void *xf, long long count, float *mean, float *spread, cudaStream_t s) {
+void predict(Net *n, const void *xf, long long count, float *mean, float *spread, cudaStream_t s,
+             const int *dcount) {
   n->ensure_err(s);
-  n->predict_device(static_cast<const bf16 *>(xf), count, mean, spread, s);
+  n->predict_device(static_cast<const bf16 *>(xf), count, mean, spread, s, dcount);
 }
 void check_error(Net *n, cudaStream_t s) {
   int v = 0;

@@ -63,7 +63,7 @@ BOX_CFG = dict(units="metal", boundary="p p p", pair="eam", skin=7.5, every=10, 
                check=True, dt=0.001)
 
 
-def generate(eam_file: str, n_samples: int, seed: int = 1, nae: int = 10, planes: int = 8,
+def generate(eam_file: str, n_samples: int, seed: int = 1, nae: int = 11, planes: int = 8,
              ny: int = 8, nz: int = 8, snapshots: int = 16, strain: float = 0.03,
              t_max: float = 500.0, device: int = 0) -> Tuple[np.ndarray, np.ndarray, Dict]:
     """At least ``n_samples`` (features, nodal forces) pairs from the plain FP64

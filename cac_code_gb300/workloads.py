@@ -74,6 +74,16 @@ def c5_eam(seed: int = 6) -> Tuple[L.Model, dict]:
     return c2_eam(cells=(16, 176, 176), layers=488, seed=seed)
 
 
+def c2_medium(seed: int = 2) -> Tuple[L.Model, dict]:
+    """C2's structure at profiling size: 266,200 atoms + 7,200 elements."""
+    return c2_eam(cells=(22, 55, 55), layers=72, seed=seed)
+
+
+def c5_medium(seed: int = 6) -> Tuple[L.Model, dict]:
+    """C5's structure at profiling size: 247,808 atoms + 64,000 elements."""
+    return c2_eam(cells=(8, 88, 88), layers=250, seed=seed)
+
+
 def c5_sample(seed: int = 7) -> Tuple[L.Model, dict]:
     """A small replica with C5's structure and atom:element ratio (about 4:1):
     7,744 atoms + 1,936 elements, 11 sites per edge."""

@@ -1,0 +1,89 @@
+"""Fused element passes (one warp per element: lattice lines as FP32 offsets
+from the element's centre in shared memory, guard-band pairs decided in FP64)
+against the unfused passes and against bit-exact FP64 forces.
+
+The fused path runs when every integration-point list entry references its
+row's own element; the C2 sample's elements (11 sites per edge) are such
+elements, since the reference's element lists find no other element centre
+within their neighbor stencil (element_neighbor.cpp:11-75).
+"""
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+from cac_code_gb300 import cacg
+from cac_code_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+
+
+def rel_err(f, ref):
+    f = np.asarray(f, dtype=np.float64).reshape(-1, 3)
+    ref = np.asarray(ref, dtype=np.float64).reshape(-1, 3)
+    d = np.linalg.norm(f - ref, axis=1)
+    n = np.linalg.norm(ref, axis=1)
+    return float(np.sqrt((d ** 2).mean() / (n ** 2).mean())), float(d.max() / n.max())
+
+
+def _run(mode, fused, steps, vscale, eam):
+    m, cfg = W.c2_sample(seed=13)
+    m.atom_v = m.atom_v * vscale
+    m.nodev = m.nodev * vscale
+    s = cacg.System(0)
+    try:
+        W.configure_system(s, m, cfg, eam)
+        s.set_precision(mode)
+        s.command(f"tune fused {'yes' if fused else 'no'}")
+        s.init()
+        s.setup()
+        s.neighbor_build()
+        s.neighbor_ebuild()
+        s.neighbor_nbuild()
+        s.pair_compute()
+        s.pair_ecompute()
+        c = s.counts()
+        first = (s.atoms()["f"].copy(), s.elements()["nodef"].copy(), c["elem_fused"])
+        s.run(steps)
+        return first, s.atoms(), s.elements(), s.counts()
+    finally:
+        s.close()
+
+
+@pytest.fixture(scope="module")
+def eam_file():
+    return W.write_eam(os.path.join(tempfile.mkdtemp(), "Cu_analytic_2000.eam"))
+
+
+@pytest.mark.parametrize("vscale", [1.0, 40.0])
+def test_fused_passes_match_unfused_and_fp64(cacg_lib, eam_file, vscale):
+    """Nodal forces of one evaluation within 1e-5 of the unfused passes and
+    within 1e-4 of bit-exact FP64; 25 steps (a rebuild decision, and at 40x
+    the thermal speeds list reorders) stay within 1e-6 A of the unfused run."""
+    f0, a0, e0, c0 = _run(cacg.MIXED, False, 25, vscale, eam_file)
+    f1, a1, e1, c1 = _run(cacg.MIXED, True, 25, vscale, eam_file)
+    fx, _, _, _ = _run(cacg.FP64_EXACT, False, 0, vscale, eam_file)
+    assert f0[2] == 0 and f1[2] == 1, "the fused path must run only where asked"
+    assert np.array_equal(f0[0], f1[0])  # atom passes untouched
+    rms, mx = rel_err(f1[1], f0[1])
+    assert rms <= 1e-5 and mx <= 1e-5, (rms, mx)
+    rms, mx = rel_err(f1[1], fx[1])
+    assert rms <= TOL and mx <= TOL, (rms, mx)
+    assert np.abs(e1["nodex"] - e0["nodex"]).max() < 1e-6
+    assert np.abs(a1["x"] - a0["x"]).max() < 1e-6
+    if vscale > 1.0:
+        assert c1["ip_reorders"] >= 2, c1["ip_reorders"]
+
+
+def test_fused_passes_off_for_foreign_entries(cacg_lib):
+    """Lists whose rows reference other elements' sites (a bin size that
+    covers the element cutoff) keep the unfused passes."""
+    import cases as C
+    from gpu_runner import run_gpu
+    cfg, z = C.load_golden("lj_cac_bigbins")
+    m = C.model_from_arrays(z)
+    out = run_gpu(cfg, m, cacg.MIXED, steps=0)
+    assert out["_counts"]["elem_fused"] == 0

@@ -1,5 +1,7 @@
-"""Mixed precision (FP32 pair terms, FP64 accumulation, embedding derivative and
-integration) against the reference's FP64 forces: relative force error <= 1e-4.
+"""Mixed precision against the reference's FP64 forces: relative force error
+<= 1e-4.  Mixed mode evaluates pair terms in FP32, F'(rho) of atoms and element
+sites in FP32 (of integration points in FP64), sums chunks of 8 pairs in FP32
+and the chunks as FP32 double-single pairs, and integrates in FP64.
 
 Errors are measured two ways on every atom and node: RMS of |df| over RMS of |f|
 and max |df| over max |f|.  The neighbor lists are the FP64 lists (identical).

@@ -127,3 +127,45 @@ def test_fallback_and_acceptance_in_the_step(cacg_lib):
     finally:
         s.close()
         net.close()
+
+
+@pytest.mark.gpu
+def test_rejected_elements_back_off(cacg_lib):
+    """An element the ensemble rejects is re-tested after 1, 3, 7, then 15
+    steps: with every far element rejected (tolerance 0), 16 steps test each
+    4 times, and the trajectory equals the one without the surrogate bit for
+    bit (rejected elements take the quadrature)."""
+    from cac_code_gb300 import surrogate as S
+    from cac_code_gb300 import workloads as W
+    eam = _eam_file()
+    x, t, _ = S.generate(eam, 8192, seed=4, planes=8, ny=8, nz=8, snapshots=4)
+    net, _ = S.train(x, t, members=2, epochs=1, batch=1024, lr=2e-3)
+    m, cfg = W.c2_sample(seed=5)
+    out = []
+    try:
+        for attach in (True, False):
+            s = cacg_lib.System(0)
+            try:
+                W.configure_system(s, m, cfg, eam)
+                s.set_precision(cacg_lib.MIXED)
+                s.init()
+                s.setup()
+                s.neighbor_build()
+                s.neighbor_ebuild()
+                s.neighbor_nbuild()
+                if attach:
+                    s.surrogate_reference(m.nodex)
+                    s.surrogate_attach(net, tol=0.0, dist=11.0)
+                c0 = s.counts()
+                s.run(16)
+                c1 = s.counts()
+                out.append((s.elements()["nodex"], c1["surrogate_evaluated"] - c0["surrogate_evaluated"],
+                            c1["surrogate_elements"], c1["surrogate_accepted"]))
+            finally:
+                s.close()
+    finally:
+        net.close()
+    (nx_s, ev, far, acc), (nx_p, _, _, _) = out
+    assert far > 0 and acc == 0
+    assert ev == 4 * far, (ev, far)
+    assert np.array_equal(nx_s.view(np.int64), nx_p.view(np.int64))
