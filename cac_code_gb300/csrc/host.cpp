@@ -236,6 +236,12 @@ struct cacg_context {
   // list entry references its row's own element (checked at each element list
   // build) and no type has more than 32 rows of nonzero weight
   bool fused_on = true, self_contained = false, fused_types_ok = false, fused_used = false;
+  // "tune fused_variant 0|1|2", the kernel arrangement (same arithmetic): the
+  // element's coefficients in registers (0, 512 threads a block), read from
+  // shared memory at every entry (1, 768 threads: more warps per SM; at C5
+  // 2.48 against 3.18 ms for the force pass), or as 1 with two entries in
+  // flight per lane (2)
+  int fused_variant = 1;
   DBuf<int> d_fjj, d_fjj_off;
   DBuf<int4> d_intp4;  // lattice indices (i, j, k) of every type's rows
   // lanes per integration point ("tune ip_group N"; 0: from the row count, so
@@ -856,6 +862,11 @@ void cacg_context::command(const std::string &raw) {
     } else if (a[0] == "streams") {
       if (a[1] != "yes" && a[1] != "no") fail(CACG_EINVAL, "tune streams takes yes or no");
       two_streams = a[1] == "yes";
+      invalidate_graph();
+    } else if (a[0] == "fused_variant") {
+      const int v = inumeric(a[1]);
+      if (v < 0 || v > 2) fail(CACG_EINVAL, "tune fused_variant takes 0, 1 or 2");
+      fused_variant = v;
       invalidate_graph();
     } else if (a[0] == "fused") {
       if (a[1] != "yes" && a[1] != "no") fail(CACG_EINVAL, "tune fused takes yes or no");
@@ -2607,7 +2618,8 @@ void cacg_context::pair_ecompute_mixed() {
   if (use_sur) m.skip = d_skip.p;
   if (fused) {
     mixed::FusedTables ft{d_node_hl.p, d_nodex.p, d_int_off.p, d_inter_off.p, d_intp4.p,
-                          d_spa_int.p, d_spa_inter.p, d_fjj.p, d_fjj_off.p, d_wn.p, maxlines};
+                          d_spa_int.p, d_spa_inter.p, d_fjj.p, d_fjj_off.p, d_wn.p, maxlines,
+                          fused_variant};
     if (pair_style == 1) {
       int a = 1 * (MAXT + 1) + 1;
       m.cutsq = ljtab.cutsq[a];

@@ -377,6 +377,7 @@ struct FusedTables {
   const int *fjj, *fjj_off;   // per type: rows of nonzero weight (at most 32), ascending
   const float *wn;            // weight x shape function per row and node
   int maxlines;
+  int variant;                // 0: coefficients in registers; 1, 2: in shared memory
 };
 bool fused_fits(int nr, int nrho);
 void elem_fused(const MixedElems &m, const FusedTables &t, int pass, const float4 *tab,

@@ -1379,10 +1379,12 @@ struct FusedArgs {
   double rdrho64;
 };
 
-// the trilinear coefficient vectors of the element: k[3 m + d], m = a, b, c,
-// ab, ac, bc, abc (lanes 0..20), from the double-single nodes
+// the trilinear coefficient vectors of the element, m = a, b, c, ab, ac, bc,
+// abc (lanes 0..20), from the double-single nodes: s_k[3 m + d] (kept in
+// registers), or with by_axis s_k[8 d + m] (read from shared memory as two
+// float4 per axis)
 __device__ __forceinline__ void fused_coeffs(const float2 *__restrict__ node_hl, int e, int lane,
-                                             float *s_k) {
+                                             float *s_k, bool by_axis) {
   if (lane < 21) {
     const int m = lane / 3, d = lane % 3;
     const float2 *nx = node_hl + 24 * (size_t) e + d;
@@ -1399,8 +1401,17 @@ __device__ __forceinline__ void fused_coeffs(const float2 *__restrict__ node_hl,
         v = ds_add(ds_add(ds_sub(X(1), X(0)), ds_sub(X(3), X(2))),
                    ds_add(ds_sub(X(4), X(5)), ds_sub(X(6), X(7))));
     }
-    s_k[lane] = v.h + v.l;
+    s_k[by_axis ? 8 * d + m : lane] = v.h + v.l;
   }
+}
+
+// a 16-byte shared-memory load that the compiler keeps inside the loop
+__device__ __forceinline__ float4 lds_v4(const float4 *p) {
+  float4 v;
+  asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "r"((unsigned) __cvta_generic_to_shared(p)));
+  return v;
 }
 
 // FP64 cutoff decision of a guard-band pair: the row's point and the site from
@@ -1442,11 +1453,14 @@ __device__ __forceinline__ float fprime32_s(float rho, const float4 *s_fp, int n
   return (c.x * p + c.y) * p + c.z;
 }
 
-template <bool EAM, bool DENSITY>
+// V = 0: coefficients in registers; V = 1: read from shared memory (sk4:
+// two float4 per axis, then the density coefficients) at every entry, fewer
+// registers; V = 2: as 1, two entries in flight per lane
+template <bool EAM, bool DENSITY, int V>
 __device__ __forceinline__ void fused_row(const FusedArgs &a, const FusedLat &g, int e, int ty,
                                           int jj, int level, int glane, const float (&k)[21],
-                                          const float (&rk)[8], const float4 *s_tab,
-                                          const float4 *s_fp, int nr,
+                                          const float (&rk)[8], const float4 *sk4,
+                                          const float4 *s_tab, const float4 *s_fp, int nr,
                                           float rdr, float fpi, float lj1, float lj2, bool live,
                                           dsacc &acc, dsacc &fx, dsacc &fy, dsacc &fz) {
   int n = 0, s0 = 0;
@@ -1466,6 +1480,7 @@ __device__ __forceinline__ void fused_row(const FusedArgs &a, const FusedLat &g,
   float part = 0.f, px = 0.f, py = 0.f, pz = 0.f;
   int cn = 0, cnt = 0;
   if (glane < n) cn = __ldg(a.ent + s0 + glane);
+#pragma unroll(V == 2 ? 2 : 1)
   for (int t = glane; t < n; t += FG) {
     const int code = cn;
     if (t + FG < n) cn = __ldg(a.ent + s0 + t + FG);
@@ -1480,15 +1495,29 @@ __device__ __forceinline__ void fused_row(const FusedArgs &a, const FusedLat &g,
     const float dbc = fmaf(bp, dc, fmaf(cp, db, -db * dc));
     const float dabc = fmaf(abp, dc, fmaf(cp, dab, -dab * dc));
     float v[3];
+    if (V == 0) {
 #pragma unroll
-    for (int d = 0; d < 3; d++) {
-      float w = k[d] * da;
-      w = fmaf(k[3 + d], db, w);
-      w = fmaf(k[6 + d], dc, w);
-      w = fmaf(k[9 + d], dab, w);
-      w = fmaf(k[12 + d], dac, w);
-      w = fmaf(k[15 + d], dbc, w);
-      v[d] = fmaf(k[18 + d], dabc, w);
+      for (int d = 0; d < 3; d++) {
+        float w = k[d] * da;
+        w = fmaf(k[3 + d], db, w);
+        w = fmaf(k[6 + d], dc, w);
+        w = fmaf(k[9 + d], dab, w);
+        w = fmaf(k[12 + d], dac, w);
+        w = fmaf(k[15 + d], dbc, w);
+        v[d] = fmaf(k[18 + d], dabc, w);
+      }
+    } else {
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        const float4 c0 = lds_v4(sk4 + 2 * d), c1 = lds_v4(sk4 + 2 * d + 1);
+        float w = c0.x * da;
+        w = fmaf(c0.y, db, w);
+        w = fmaf(c0.z, dc, w);
+        w = fmaf(c0.w, dab, w);
+        w = fmaf(c1.x, dac, w);
+        w = fmaf(c1.y, dbc, w);
+        v[d] = fmaf(c1.z, dabc, w);
+      }
     }
     const float dx = v[0], dy = v[1], dz = v[2];
     const float rsq = dx * dx + dy * dy + dz * dz;
@@ -1508,13 +1537,25 @@ __device__ __forceinline__ void fused_row(const FusedArgs &a, const FusedLat &g,
           part += ((cc.x * p + cc.y) * p + cc.z) * p + cc.w;
         } else {
           // the site's density from the nodal densities: rho(p) - sum Rm (m(p) - m(s))
-          float dr = rk[1] * da;
-          dr = fmaf(rk[2], db, dr);
-          dr = fmaf(rk[3], dc, dr);
-          dr = fmaf(rk[4], dab, dr);
-          dr = fmaf(rk[5], dac, dr);
-          dr = fmaf(rk[6], dbc, dr);
-          dr = fmaf(rk[7], dabc, dr);
+          float dr;
+          if (V == 0) {
+            dr = rk[1] * da;
+            dr = fmaf(rk[2], db, dr);
+            dr = fmaf(rk[3], dc, dr);
+            dr = fmaf(rk[4], dab, dr);
+            dr = fmaf(rk[5], dac, dr);
+            dr = fmaf(rk[6], dbc, dr);
+            dr = fmaf(rk[7], dabc, dr);
+          } else {
+            const float4 r0 = lds_v4(sk4 + 6), r1 = lds_v4(sk4 + 7);
+            dr = r0.y * da;
+            dr = fmaf(r0.z, db, dr);
+            dr = fmaf(r0.w, dc, dr);
+            dr = fmaf(r1.x, dab, dr);
+            dr = fmaf(r1.y, dac, dr);
+            dr = fmaf(r1.z, dbc, dr);
+            dr = fmaf(r1.w, dabc, dr);
+          }
           const float fpj = fprime32_s(rk[0] - dr, s_fp, a.nrho, a.rdrho);
           float rhoip, z2, z2p;
           force_spline(s_tab, m, p, rdr, rhoip, z2, z2p);
@@ -1572,8 +1613,12 @@ __device__ __forceinline__ FusedLat fused_lat(const Lattice &lat, int ty) {
 // row forces (3 per row of nonzero weight)
 constexpr int FUSED_WARP_FLOATS = 32 + 2 * 3 * FUSED_MAXF;
 
+// threads per block of each variant (V = 0: coefficients in registers)
+__host__ __device__ constexpr int fused_block(int V) { return V == 0 ? FUSED_BLOCK : 768; }
+
 // EAM nodal densities: the element's 8 node rows, one row per FG lanes
-__global__ void __launch_bounds__(FUSED_BLOCK, 1)
+template <int V>
+__global__ void __launch_bounds__(fused_block(V), 1)
 k_elem_rho_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rdr,
                  double *__restrict__ erho) {
   extern __shared__ float4 smem[];
@@ -1590,18 +1635,21 @@ k_elem_rho_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rdr,
   for (int e = gw; e < a.nlocal_e; e += nw) {
     const int ty = a.etype[e];
     const FusedLat g = fused_lat(a.lat, ty);
-    fused_coeffs(a.node_hl, e, lane, s_k);
+    fused_coeffs(a.node_hl, e, lane, s_k, V != 0);
     __syncwarp();
     float k[21];
+    if (V == 0) {
 #pragma unroll
-    for (int q = 0; q < 21; q++) k[q] = s_k[q];
+      for (int q = 0; q < 21; q++) k[q] = s_k[q];
+    }
     for (int kb = 0; kb < NPE; kb += 32 / FG) {
       const int q = kb + gsub;
       const bool live = q < NPE;
       const int jj = live ? a.node_list[ty * NPE + q] : 0;
       dsacc acc, fx, fy, fz;
-      fused_row<true, true>(a, g, e, ty, jj, level, glane, k, rk, s_tab, nullptr, nr, rdr, 0.f,
-                            0.f, 0.f, live, acc, fx, fy, fz);
+      fused_row<true, true, V>(a, g, e, ty, jj, level, glane, k, rk,
+                               reinterpret_cast<const float4 *>(s_k), s_tab, nullptr, nr, rdr,
+                               0.f, 0.f, 0.f, live, acc, fx, fy, fz);
       if (live && glane == 0) erho[NPE * (size_t) e + q] = acc.value();
     }
     __syncwarp();
@@ -1610,8 +1658,8 @@ k_elem_rho_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rdr,
 
 // Forces of the element's rows of nonzero weight and their gather onto the
 // nodes (EAM with the nodal densities and row F'(rho), or LJ)
-template <bool EAM>
-__global__ void __launch_bounds__(FUSED_BLOCK, 1)
+template <bool EAM, int V>
+__global__ void __launch_bounds__(fused_block(V), 1)
 k_elem_force_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rdr, float lj1,
                    float lj2, const double *__restrict__ erho, double *__restrict__ nodef) {
   extern __shared__ float4 smem[];
@@ -1635,7 +1683,7 @@ k_elem_force_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rd
     const int ty = a.etype[e];
     const FusedLat g = fused_lat(a.lat, ty);
     const int f0 = a.fjj_off[ty], nf = a.fjj_off[ty + 1] - f0;
-    fused_coeffs(a.node_hl, e, lane, s_k);
+    fused_coeffs(a.node_hl, e, lane, s_k, V != 0);
     if (EAM && lane >= 24) {  // density coefficients from the nodal densities (FP32)
       const double *er = erho + NPE * (size_t) e;
       const int m = lane - 24;
@@ -1654,8 +1702,10 @@ k_elem_force_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rd
     }
     __syncwarp();
     float k[21];
+    if (V == 0) {
 #pragma unroll
-    for (int q = 0; q < 21; q++) k[q] = s_k[q];
+      for (int q = 0; q < 21; q++) k[q] = s_k[q];
+    }
     float rk[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     for (int fb = 0; fb < nf; fb += 32 / FG) {
       const int j = fb + gsub;
@@ -1676,12 +1726,15 @@ k_elem_force_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rd
         }
         fpi = __shfl_sync(0xffffffffu, fpi, lane & ~(FG - 1));
         rk[0] = __shfl_sync(0xffffffffu, rho32, lane & ~(FG - 1));
+        if (V == 0) {
 #pragma unroll
-        for (int q = 1; q < 8; q++) rk[q] = s_r[q];
+          for (int q = 1; q < 8; q++) rk[q] = s_r[q];
+        }
       }
       dsacc acc, fx, fy, fz;
-      fused_row<EAM, false>(a, g, e, ty, jj, level, glane, k, rk, s_tab, s_fp, nr, rdr, fpi,
-                            lj1, lj2, live, acc, fx, fy, fz);
+      fused_row<EAM, false, V>(a, g, e, ty, jj, level, glane, k, rk,
+                               reinterpret_cast<const float4 *>(s_k), s_tab, s_fp, nr, rdr, fpi,
+                               lj1, lj2, live, acc, fx, fy, fz);
       if (live && glane == 0) {
         s_f[3 * j] = make_float2(fx.h, fx.l);
         s_f[3 * j + 1] = make_float2(fy.h, fy.l);
@@ -2010,12 +2063,32 @@ void ip_pass(const MixedElems &m, int pass, const float4 *tab, const EamTables &
   check(cudaGetLastError(), "ip_pass_mixed");
 }
 
+template <int V>
+static void launch_fused(const FusedArgs &a, int pass, const float4 *tab, const EamTables &e,
+                         size_t table, float lj1, float lj2, const double *erho_in,
+                         double *erho_out, double *nodef, cudaStream_t s) {
+  constexpr int B = fused_block(V);
+  const size_t smem = table + sizeof(float) * FUSED_WARP_FLOATS * (B / 32);
+  const long long items = (long long) a.nlocal_e * 32;
+  if (pass == 1) {
+    const int g = persistent_grid((const void *) k_elem_rho_fused<V>, B, smem, items);
+    k_elem_rho_fused<V><<<g, B, smem, s>>>(a, tab, e.nr, (float) e.rdr, erho_out);
+  } else if (pass == 2) {
+    const int g = persistent_grid((const void *) k_elem_force_fused<true, V>, B, smem, items);
+    k_elem_force_fused<true, V><<<g, B, smem, s>>>(a, tab, e.nr, (float) e.rdr, 0.f, 0.f,
+                                                   erho_in, nodef);
+  } else {
+    const int g = persistent_grid((const void *) k_elem_force_fused<false, V>, B, smem, items);
+    k_elem_force_fused<false, V><<<g, B, smem, s>>>(a, nullptr, 0, 0.f, lj1, lj2, nullptr, nodef);
+  }
+}
+
 bool fused_fits(int nr, int nrho) {
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   const size_t need = sizeof(float4) * (FTAB_W * (size_t) (nr + 1) + (size_t) (nrho + 1)) +
-                      sizeof(float) * FUSED_WARP_FLOATS * (FUSED_BLOCK / 32);
+                      sizeof(float) * FUSED_WARP_FLOATS * (fused_block(2) / 32);
   return need <= (size_t) optin;
 }
 
@@ -2059,20 +2132,10 @@ void elem_fused(const MixedElems &m, const FusedTables &t, int pass, const float
   const size_t table =
       eam ? sizeof(float4) * ((force ? FTAB_W : 1) * (size_t) (e.nr + 1) + (force ? e.nrho + 1 : 0))
           : 0;
-  const size_t smem = table + sizeof(float) * FUSED_WARP_FLOATS * (FUSED_BLOCK / 32);
-  const long long items = (long long) m.nlocal_e * 32;
-  if (pass == 1) {
-    const int g = persistent_grid((const void *) k_elem_rho_fused, FUSED_BLOCK, smem, items);
-    k_elem_rho_fused<<<g, FUSED_BLOCK, smem, s>>>(a, tab, e.nr, (float) e.rdr, erho_out);
-  } else if (pass == 2) {
-    const int g = persistent_grid((const void *) k_elem_force_fused<true>, FUSED_BLOCK, smem, items);
-    k_elem_force_fused<true><<<g, FUSED_BLOCK, smem, s>>>(a, tab, e.nr, (float) e.rdr, 0.f, 0.f,
-                                                          erho_in, nodef);
-  } else {
-    const int g = persistent_grid((const void *) k_elem_force_fused<false>, FUSED_BLOCK, smem, items);
-    k_elem_force_fused<false><<<g, FUSED_BLOCK, smem, s>>>(a, nullptr, 0, 0.f, lj1, lj2, nullptr,
-                                                           nodef);
-  }
+  if (t.variant == 1) launch_fused<1>(a, pass, tab, e, table, lj1, lj2, erho_in, erho_out, nodef, s);
+  else if (t.variant == 2)
+    launch_fused<2>(a, pass, tab, e, table, lj1, lj2, erho_in, erho_out, nodef, s);
+  else launch_fused<0>(a, pass, tab, e, table, lj1, lj2, erho_in, erho_out, nodef, s);
   check(cudaGetLastError(), "elem_fused");
 }
 

@@ -87,3 +87,28 @@ def test_fused_passes_off_for_foreign_entries(cacg_lib):
     m = C.model_from_arrays(z)
     out = run_gpu(cfg, m, cacg.MIXED, steps=0)
     assert out["_counts"]["elem_fused"] == 0
+
+
+def test_fused_variants_bit_identical(cacg_lib, eam_file):
+    """The three kernel arrangements of the fused passes (coefficients in
+    registers, in shared memory, two entries in flight) give the same bits."""
+    m, cfg = W.c2_sample(seed=13)
+    s = cacg.System(0)
+    try:
+        W.configure_system(s, m, cfg, eam_file)
+        s.set_precision(cacg.MIXED)
+        s.init()
+        s.setup()
+        s.neighbor_build()
+        s.neighbor_ebuild()
+        s.neighbor_nbuild()
+        out = []
+        for v in (0, 1, 2):
+            s.command(f"tune fused_variant {v}")
+            s.pair_ecompute()
+            assert s.counts()["elem_fused"] == 1
+            out.append(s.elements()["nodef"].copy())
+    finally:
+        s.close()
+    for o in out[1:]:
+        assert np.array_equal(o.view(np.int64), out[0].view(np.int64))
