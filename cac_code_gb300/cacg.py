@@ -52,7 +52,7 @@ EXPORTED = [
     "cacg_gemm_bf16_tn", "cacg_surrogate_reference", "cacg_surrogate_samples",
     "cacg_surrogate_attach", "cacg_compute_centro", "cacg_dump_xyz", "cacg_dump_elements",
     "cacg_fix_post_force", "cacg_get_box", "cacg_set_graphs", "cacg_set_group",
-    "cacg_run_host", "cacg_get_kernel_timing",
+    "cacg_run_host", "cacg_get_kernel_timing", "cacg_set_lj", "cacg_set_eam",
 ]
 
 
@@ -261,6 +261,21 @@ class System:
         self._ok(self._L.cacg_set_precision(self.h, mode))
 
     # ---- direct state ----
+    def set_lj(self, lj1, lj2, cutsq):
+        """PairLJCut tables after init_one, [ntypes + 1][ntypes + 1] each."""
+        a = [np.ascontiguousarray(t, dtype=np.float64) for t in (lj1, lj2, cutsq)]
+        nt = int(round(np.sqrt(a[0].size))) - 1
+        self._ok(self._L.cacg_set_lj(self.h, nt, _d(a[0]), _d(a[1]), _d(a[2])))
+
+    def set_eam(self, nr, dr, nrho, drho, frho7, rhor7, z2r7, cutforcesq, mass):
+        """PairEAM splines of the one species ([n + 1][7] each) and grids."""
+        f, r, z = (np.ascontiguousarray(t, dtype=np.float64) for t in (frho7, rhor7, z2r7))
+        L = self._L
+        L.cacg_set_eam.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                   ctypes.c_double, _dp, _dp, _dp, ctypes.c_double, ctypes.c_double]
+        self._ok(L.cacg_set_eam(self.h, int(nr), float(dr), int(nrho), float(drho), _d(f), _d(r),
+                                _d(z), float(cutforcesq), float(mass)))
+
     def set_box(self, lo, hi, periodic):
         lo = np.ascontiguousarray(lo, dtype=np.float64)
         hi = np.ascontiguousarray(hi, dtype=np.float64)

@@ -172,6 +172,10 @@ struct cacg_context {
   double cut_global = 0.0;
   double eps[MAXT + 1][MAXT + 1] = {}, sig[MAXT + 1][MAXT + 1] = {}, cutp[MAXT + 1][MAXT + 1] = {};
   int setflag[MAXT + 1][MAXT + 1] = {};
+  // LJ tables handed over by cacg_set_lj (the caller's PairLJCut after
+  // init_one): used as given instead of forming them from epsilon and sigma
+  bool lj_raw = false;
+  std::vector<double> raw_lj1, raw_lj2, raw_cutsq;  // [(ntypes + 1)^2]
   LJTabHost ljtab;
   // eam
   int nr = 0, nrho = 0;
@@ -762,6 +766,7 @@ void cacg_context::command(const std::string &raw) {
     read_data(a[0]);
   } else if (c == "pair_style") {
     if (a.empty()) fail(CACG_EINVAL, "Illegal pair_style command");
+    lj_raw = false;
     if (a[0] == "lj/cut") {
       if (a.size() != 2) fail(CACG_EINVAL, "Illegal pair_style command");
       pair_style = 1;
@@ -781,6 +786,7 @@ void cacg_context::command(const std::string &raw) {
     int nt = ntypes > 0 ? ntypes : 1;
     if (pair_style == 1) {
       if (a.size() < 4 || a.size() > 5) fail(CACG_EINVAL, "Incorrect args for pair coefficients");
+      lj_raw = false;  // coefficients again, instead of handed-over tables
       bounds(a[0], nt, ilo, ihi);
       bounds(a[1], nt, jlo, jhi);
       double e = numeric(a[2]), s = numeric(a[3]);
@@ -1890,7 +1896,29 @@ void cacg_context::init() {
   triggersq = 0.25 * skin * skin;
 
   // Pair::init -> init_one (pair.cpp:102-155, pair_lj_cut.cpp:140-198)
-  if (pair_style == 1) {
+  if (pair_style == 1 && lj_raw) {
+    // tables as the caller's PairLJCut::init_one made them; lj3 = lj1 / 12
+    // and lj4 = lj2 / 6 (4 eps sigma^12 and 4 eps sigma^6) for the energies
+    memset(&ljtab, 0, sizeof(ljtab));
+    const int T = (MAXT + 1) * (MAXT + 1);
+    std::vector<double> lj5(5 * T, 0.0);
+    for (int i = 1; i <= nt; i++)
+      for (int j = 1; j <= nt; j++) {
+        const int a = i * (MAXT + 1) + j, r = i * (nt + 1) + j;
+        ljtab.lj1[a] = raw_lj1[r];
+        ljtab.lj2[a] = raw_lj2[r];
+        ljtab.cutsq[a] = raw_cutsq[r];
+        lj5[a] = raw_lj1[r];
+        lj5[T + a] = raw_lj2[r];
+        lj5[2 * T + a] = raw_lj1[r] / 12.0;
+        lj5[3 * T + a] = raw_lj2[r] / 6.0;
+        lj5[4 * T + a] = raw_cutsq[r];
+      }
+    d_ljtab.ensure(1, stream);
+    check(cudaMemcpyAsync(d_ljtab.p, &ljtab, sizeof(ljtab), cudaMemcpyHostToDevice, stream), "ljtab");
+    upload(d_lj5, lj5, stream);
+    h_lj5 = lj5;
+  } else if (pair_style == 1) {
     memset(&ljtab, 0, sizeof(ljtab));
     for (int i = 1; i <= nt; i++)
       for (int j = i; j <= nt; j++) {
@@ -3852,6 +3880,57 @@ int cacg_set_box(cacg_handle h, const double *lo, const double *hi, const int *p
     h->periodic[d] = periodic[d] ? 1 : 0;
   }
   h->box_set = true;
+  h->inited = false;
+  API_END
+}
+
+int cacg_set_lj(cacg_handle h, int ntypes, const double *lj1, const double *lj2,
+                const double *cutsq) {
+  API_BEGIN
+  if (h->pair_style != 1) fail(CACG_ESTATE, "cacg_set_lj after pair_style lj/cut");
+  if (ntypes < 1 || ntypes > MAXT || !lj1 || !lj2 || !cutsq) fail(CACG_EINVAL, "bad LJ tables");
+  if (h->ntypes > 0 && ntypes != h->ntypes) fail(CACG_EINVAL, "LJ tables for another type count");
+  const size_t n = (size_t) (ntypes + 1) * (ntypes + 1);
+  h->raw_lj1.assign(lj1, lj1 + n);
+  h->raw_lj2.assign(lj2, lj2 + n);
+  h->raw_cutsq.assign(cutsq, cutsq + n);
+  for (int i = 1; i <= ntypes; i++)
+    for (int j = 1; j <= ntypes; j++) {
+      const size_t r = (size_t) i * (ntypes + 1) + j;
+      if (!(cutsq[r] > 0.0) || !std::isfinite(lj1[r]) || !std::isfinite(lj2[r]))
+        fail(CACG_EINVAL, "bad LJ tables");
+    }
+  for (int i = 1; i <= ntypes; i++)
+    for (int j = i; j <= ntypes; j++) h->setflag[i][j] = 1;
+  h->lj_raw = true;
+  h->inited = false;
+  API_END
+}
+
+int cacg_set_eam(cacg_handle h, int nr, double dr, int nrho, double drho, const double *frho7,
+                 const double *rhor7, const double *z2r7, double cutforcesq, double mass) {
+  API_BEGIN
+  if (h->pair_style != 2) fail(CACG_ESTATE, "cacg_set_eam after pair_style eam");
+  if (nr < 5 || nrho < 5 || !(dr > 0.0) || !(drho > 0.0) || !frho7 || !rhor7 || !z2r7 ||
+      !(cutforcesq > 0.0) || !(mass > 0.0))
+    fail(CACG_EINVAL, "bad EAM tables");
+  h->nr = nr;
+  h->dr = dr;
+  h->rdr = 1.0 / dr;
+  h->nrho = nrho;
+  h->drho = drho;
+  h->rdrho = 1.0 / drho;
+  h->frho_sp.assign(frho7, frho7 + (size_t) (nrho + 1) * 7);
+  h->rhor_sp.assign(rhor7, rhor7 + (size_t) (nr + 1) * 7);
+  h->z2r_sp.assign(z2r7, z2r7 + (size_t) (nr + 1) * 7);
+  h->cutforcesq = cutforcesq;
+  h->eam_cut = std::sqrt(cutforcesq);
+  h->eam_mass = mass;
+  const int nt = std::max(h->ntypes, 1);
+  for (int i = 1; i <= nt; i++) {
+    h->setflag[i][i] = 1;
+    h->amass[i] = mass;  // PairEAM::coeff sets the type mass (pair_eam.cpp:152-161)
+  }
   h->inited = false;
   API_END
 }

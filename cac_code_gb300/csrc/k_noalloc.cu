@@ -24,9 +24,15 @@
 // between them) overwrite each other's partial sums: serialise them on one
 // stream or with events.
 //
-// The scratch address is resolved once per device, with that device current,
-// by cudaGetSymbolAddress on the first call; make that first call (n = 0 is
-// enough) before any stream capture begins.
+// The scratch address is resolved once per device ordinal, with that device
+// current, by cudaGetSymbolAddress on the first call, and cached: it belongs
+// to the device's primary context, so it does not survive cudaDeviceReset and
+// does not serve a caller that made another context current.  Make that first
+// call (n = 0 is enough) before any stream capture begins.
+//
+// A CUDA error left pending by earlier, unrelated work is reported
+// (CACG_ECUDA) and left in place for its owner; the call then launches
+// nothing.
 #include <mutex>
 
 #include "cacg.h"
@@ -81,14 +87,28 @@ k_kinetic_partials(const double *__restrict__ v, const int *__restrict__ type,
   }
 }
 
-// out[k] = mvv2e * (partials of quantity k added in block order)
-__global__ void k_kinetic_finish(const double *__restrict__ part, int nblocks, double mvv2e,
-                                 double *__restrict__ out) {
-  const int k = threadIdx.x;
-  if (k >= NOALLOC_NQ) return;
-  double s = 0.0;
-  for (int b = 0; b < nblocks; b++) s += part[(size_t) b * NOALLOC_NQ + k];
-  out[k] = s * mvv2e;
+// out[k] = mvv2e * (the partials of quantity k summed): one block, each
+// thread sums a stride of the partials, then a tree over the threads
+constexpr int NOALLOC_FINISH = 256;
+
+__global__ void __launch_bounds__(NOALLOC_FINISH)
+k_kinetic_finish(const double *__restrict__ part, int nblocks, double mvv2e,
+                 double *__restrict__ out) {
+  __shared__ double sh[NOALLOC_NQ][NOALLOC_FINISH];
+  double q[NOALLOC_NQ] = {0, 0, 0, 0, 0, 0, 0};
+  for (int b = threadIdx.x; b < nblocks; b += NOALLOC_FINISH)
+#pragma unroll
+    for (int k = 0; k < NOALLOC_NQ; k++) q[k] += part[(size_t) b * NOALLOC_NQ + k];
+#pragma unroll
+  for (int k = 0; k < NOALLOC_NQ; k++) sh[k][threadIdx.x] = q[k];
+  __syncthreads();
+  for (int w = NOALLOC_FINISH / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+#pragma unroll
+      for (int k = 0; k < NOALLOC_NQ; k++) sh[k][threadIdx.x] += sh[k][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x < NOALLOC_NQ) out[threadIdx.x] = sh[threadIdx.x][0] * mvv2e;
 }
 
 // the scratch address on the current device, resolved once per device
@@ -113,6 +133,8 @@ extern "C" int cacg_kinetic_noalloc(const double *v, const int *type, const doub
                                     void *stream) {
   if (n < 0 || per_item < 1 || !out || (n > 0 && (!v || !type || !mass))) return CACG_EINVAL;
   if (n > CACG_NOALLOC_MAX_ITEMS) return CACG_ESCRATCH;
+  // an error pending from earlier work is its owner's: report it, keep it
+  if (cudaPeekAtLastError() != cudaSuccess) return CACG_ECUDA;
   double *part = nullptr;
   int rc = noalloc_scratch(&part);
   if (rc != CACG_OK) return rc;
@@ -120,6 +142,7 @@ extern "C" int cacg_kinetic_noalloc(const double *v, const int *type, const doub
   const int nblocks = (n + NOALLOC_TB - 1) / NOALLOC_TB;
   if (nblocks > 0)
     k_kinetic_partials<<<nblocks, NOALLOC_TB, 0, s>>>(v, type, mass, n, per_item, scale, part);
-  k_kinetic_finish<<<1, 32, 0, s>>>(part, nblocks, mvv2e, out);
+  k_kinetic_finish<<<1, NOALLOC_FINISH, 0, s>>>(part, nblocks, mvv2e, out);
+  // nothing was pending before the launches: an error now is theirs
   return cudaGetLastError() == cudaSuccess ? CACG_OK : CACG_ECUDA;
 }

@@ -68,6 +68,22 @@ int cacg_set_elements(cacg_handle h, int n, const int *etype, const double *cent
                       const double *nodex, const double *nodev);      /* Elements, Nodes */
 int cacg_set_precision(cacg_handle h, int mode);
 
+/* ---- pair tables handed over as the reference built them ----
+   For a Pair subclass whose base already read the potential: after
+   pair_style lj/cut, the PairLJCut tables after init_one
+   (pair_lj_cut.cpp:140-198), lj1, lj2, cutsq as [ntypes + 1][ntypes + 1]
+   (the contiguous memory->create 2-d arrays, row 0 and column 0 unused);
+   they replace pair_coeff's epsilon, sigma and cutoff. */
+int cacg_set_lj(cacg_handle h, int ntypes, const double *lj1, const double *lj2,
+                const double *cutsq);
+/* After pair_style eam: the splines PairEAM::array2spline made for the one
+   species (pair_eam.cpp:527-580), frho_spline[type2frho[1]] [nrho + 1][7],
+   rhor_spline[type2rhor[1][1]] and z2r_spline[type2z2r[1][1]] [nr + 1][7],
+   with the grids nr, dr, nrho, drho, cutforcesq (pair_eam.cpp:274-282) and
+   the potential's mass; they replace pair_coeff's file. */
+int cacg_set_eam(cacg_handle h, int nr, double dr, int nrho, double drho, const double *frho7,
+                 const double *rhor7, const double *z2r7, double cutforcesq, double mass);
+
 /* ---- init and setup ---- */
 int cacg_init(cacg_handle h);       /* CAC::init, cac.cpp:202-213 (tables, cutoffs) */
 int cacg_setup(cacg_handle h);      /* Verlet::setup through comm->borders, verlet.cpp:70-90 */
@@ -160,8 +176,12 @@ int cacg_compute_thermo(cacg_handle h, double *out, int n);
    CACG_NOALLOC_MAX_ITEMS returns CACG_ESCRATCH.  Nothing has to be zeroed
    first.  Calls share that array per device, so calls that can overlap
    race: serialise them.  The first call on a device resolves the array's
-   address (make it, n = 0 is enough, before any stream capture).  Returns
-   CACG_OK once both kernels are queued. */
+   address (make it, n = 0 is enough, before any stream capture) and caches
+   it per device ordinal: the address is the primary context's, so it does
+   not outlive cudaDeviceReset and does not serve another current context.
+   A CUDA error already pending from earlier work is reported as CACG_ECUDA
+   and left pending (nothing is launched).  Returns CACG_OK once both kernels
+   are queued. */
 #define CACG_NOALLOC_MAX_ITEMS (8192 * 256)
 int cacg_kinetic_noalloc(const double *v, const int *type, const double *mass, int n,
                          int per_item, double scale, double mvv2e, double *out, void *stream);

@@ -17,7 +17,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_BIN = os.path.join(HERE, "_ref", "cacref")
-REF_TREE = os.environ.get("CAC_REFERENCE_TREE", "/root/reference")
+# the reference tree: CAC_REFERENCE_TREE, else the directory "reference"
+# beside the repository
+REF_TREE = os.environ.get("CAC_REFERENCE_TREE",
+                          os.path.normpath(os.path.join(HERE, "..", "..", "reference")))
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int)

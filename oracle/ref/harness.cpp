@@ -22,6 +22,11 @@
 //     elem_forces    Pair::ecompute, dump nodef
 //     step N         N steps in Verlet::run order (atoms get Pair::compute too)
 //     state TAG      dump x, v, f, nodex, nodev, nodef with file prefix TAG
+//     eam_tables     after setup: PairEAM's splines of type 1 (frho, rhor, z2r,
+//                    [n + 1][7] each, pair_eam.cpp:527-580) and nr, dr, nrho,
+//                    drho, cutforcesq, mass of type 1
+//     lj_tables      after setup: PairLJCut's lj1, lj2 and cutsq,
+//                    [ntypes + 1][ntypes + 1] each (pair_lj_cut.cpp:140-198)
 //     velocities F   set atom velocities from raw float64 file F (3 per atom, in
 //                    tag order); the data file format has no atom velocities
 //                    (atom_vec_atomic.cpp:70-72 zero them, and ReadData has no
@@ -54,6 +59,8 @@
 #include "output.h"
 #include "node_neigh_list.h"
 #include "pair.h"
+#include "pair_eam.h"
+#include "pair_lj_cut.h"
 #include "update.h"
 
 using namespace CAC_NS;
@@ -511,6 +518,42 @@ int main(int argc, char **argv) {
       }
     } else if (cmd.compare(0, 6, "state ") == 0) {
       h.dump_state(cmd.substr(6));
+    } else if (cmd == "eam_tables") {
+      PairEAM *p = (PairEAM *) h.cac->force->pair;
+      const int f1 = p->type2frho[1], r1 = p->type2rhor[1][1], z1 = p->type2z2r[1][1];
+      std::vector<double> fr, rr, zr;
+      for (int m = 0; m <= p->nrho; m++)
+        for (int k = 0; k < 7; k++) fr.push_back(p->frho_spline[f1][m][k]);
+      for (int m = 0; m <= p->nr; m++)
+        for (int k = 0; k < 7; k++) {
+          rr.push_back(p->rhor_spline[r1][m][k]);
+          zr.push_back(p->z2r_spline[z1][m][k]);
+        }
+      write_f64("eam_frho.f64", fr);
+      write_f64("eam_rhor.f64", rr);
+      write_f64("eam_z2r.f64", zr);
+      std::vector<double> sc(6);
+      sc[0] = p->nr;
+      sc[1] = p->dr;
+      sc[2] = p->nrho;
+      sc[3] = p->drho;
+      sc[4] = p->cutforcesq;
+      sc[5] = h.cac->atom->mass[1];
+      write_f64("eam_scalars.f64", sc);
+    } else if (cmd == "lj_tables") {
+      PairLJCut *p = (PairLJCut *) h.cac->force->pair;
+      const int nt = h.cac->atom->ntypes;
+      std::vector<double> l1, l2, cs;
+      for (int i = 0; i <= nt; i++)
+        for (int j = 0; j <= nt; j++) {
+          const bool set = i >= 1 && j >= 1;
+          l1.push_back(set ? p->lj1[i][j] : 0.0);
+          l2.push_back(set ? p->lj2[i][j] : 0.0);
+          cs.push_back(set ? p->cutsq[i][j] : 0.0);
+        }
+      write_f64("lj_lj1.f64", l1);
+      write_f64("lj_lj2.f64", l2);
+      write_f64("lj_cutsq.f64", cs);
     } else {
       fprintf(stderr, "cacref: unknown directive '%s'\n", cmd.c_str());
       return 2;

@@ -48,6 +48,8 @@ def run_case(name: str, cfg: dict) -> None:
                             **kw)
     cap = 8 * (m.natoms + 64)
     directives = [f"capacity {cap}", "velocities v.bin", "setup"]
+    # the reference's own pair tables after init (raw-table hand-over tests)
+    directives.append("eam_tables" if cfg["pair"] == "eam" else "lj_tables")
     if m.natoms:
         directives += ["atom_list", "centro", "atom_forces"]
     if m.nelements:

@@ -54,10 +54,13 @@ def configure(s, cfg, m, via_files=False, eam_file=C.EAM_FILE, pair_lines=None):
         s.command(line)
 
 
-def run_gpu(cfg, m, mode=cacg.FP64_EXACT, via_files=False, steps=None, pair_lines=None):
+def run_gpu(cfg, m, mode=cacg.FP64_EXACT, via_files=False, steps=None, pair_lines=None,
+            before_init=None):
     s = cacg.System(0)
     try:
         configure(s, cfg, m, via_files=via_files, pair_lines=pair_lines)
+        if before_init is not None:
+            before_init(s)
         s.set_precision(mode)
         s.init()
         s.setup()
