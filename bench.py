@@ -230,6 +230,21 @@ def kernel_bytes(name, c, mode, lines_all, lines_force, nae_lines):
     rows_f = c["force_rows"]            # Gauss rows (nonzero weight)
     scan_e = c["ip_scan_entries"] / max(c["ip_rows"], 1)   # entries scanned per row
     n_s = c["short_entries"] / max(n, 1)
+    if mode == "mixed" and c.get("elem_fused"):
+        # the fused element passes (one warp per element): per element the split
+        # nodes 192 (read in both passes), the nodal densities 64 (written by
+        # the density pass, read by the force pass) and the nodal forces 192;
+        # per row the row start pair 8, culling counts 16, lattice indices 16
+        # and the list codes 4 n.  No line or site data reaches memory.
+        n_scan = c["density_scan_entries"] / max(n, 1)
+        return {
+            "atom1": n * (16 + 4 + 4 * n_scan + 4 + 4 * n_s + 8 + 4),
+            "atom2": n * (16 + 4 + 4 * n_s + 4 + 24),
+            "elem_rho": ne * (192 + 64) + rows_n * (8 + 16 + 16 + 4 * scan_e),
+            "elem_force": ne * (192 + 64 + 192) + rows_f * (8 + 16 + 16 + 4 * scan_e),
+            # node split only (the lines are formed on list-reorder steps alone)
+            "sites": ne_all * (192 + 192),
+        }
     if mode == "mixed":
         n_scan = c["density_scan_entries"] / max(n, 1)
         return {
@@ -479,8 +494,12 @@ def run_ours(a, ws, rank, local):
     kernel_names = {
         "atom1": "k_eam_rho_atoms (EAM density pass over the atom list)",
         "atom2": "k_eam_force_atoms (EAM force pass over the atom list)",
-        "elem_rho": "k_ipg<EAM, density> (nodal densities over the node rows)",
-        "elem_force": "k_ipg<EAM, force> (integration-point forces over the Gauss rows)",
+        "elem_rho": ("k_elem_rho_fused (nodal densities, one warp per element)"
+                     if c1.get("elem_fused") else
+                     "k_ipg<EAM, density> (nodal densities over the node rows)"),
+        "elem_force": ("k_elem_force_fused (integration-point forces and nodal gather, one "
+                       "warp per element)" if c1.get("elem_fused") else
+                       "k_ipg<EAM, force> (integration-point forces over the Gauss rows)"),
         "sur": "surrogate (features, k_mlp_ensemble, acceptance)",
         "sites": "k_node_split + k_lines (lattice lines)",
         "site_fp": "k_line_rho + k_row_fp",

@@ -205,6 +205,7 @@ struct cacg_context {
   // integration-point shape functions, packed site positions and site F'(rho),
   // the referenced sites of each lattice line, lattice sizes per type
   DBuf<float4> d_xl, d_rhor_val4, d_ftab, d_fp4, d_line_pos;
+  DBuf<float2> d_frho_ds;  // F' spline coefficients c0..c2 per knot, double-single
   DBuf<float2> d_node_hl, d_spa_int_hl;
   DBuf<float> d_u, d_ljf, d_fpf;
   DBuf<float2> d_line_rho;
@@ -1721,10 +1722,16 @@ void cacg_context::mixed_tables() {
       ft[2 * m + 1] = make_float4((float) z[4], (float) z[5], (float) z[6], 0.f);
     }
     std::vector<float4> f4(nrho + 1);
+    std::vector<float2> fds(3 * (size_t) (nrho + 1));
     for (int m = 0; m <= nrho; m++) {
       const double *c = &frho_sp[(size_t) m * 7];
       f4[m] = make_float4((float) c[0], (float) c[1], (float) c[2], 0.f);
+      for (int k = 0; k < 3; k++) {  // the F' coefficients as double-single pairs
+        const float h = (float) c[k];
+        fds[3 * (size_t) m + k] = make_float2(h, (float) (c[k] - (double) h));
+      }
     }
+    upload(d_frho_ds, fds, stream);
     upload(d_rhor_val4, val, stream);
     upload(d_ftab, ft, stream);
     upload(d_fp4, f4, stream);
@@ -2647,7 +2654,7 @@ void cacg_context::pair_ecompute_mixed() {
   if (fused) {
     mixed::FusedTables ft{d_node_hl.p, d_nodex.p, d_int_off.p, d_inter_off.p, d_intp4.p,
                           d_spa_int.p, d_spa_inter.p, d_fjj.p, d_fjj_off.p, d_wn.p, maxlines,
-                          fused_variant};
+                          fused_variant, d_spa_int_hl.p, d_frho_ds.p};
     if (pair_style == 1) {
       int a = 1 * (MAXT + 1) + 1;
       m.cutsq = ljtab.cutsq[a];

@@ -378,6 +378,8 @@ struct FusedTables {
   const float *wn;            // weight x shape function per row and node
   int maxlines;
   int variant;                // 0: coefficients in registers; 1, 2: in shared memory
+  const float2 *spa_int_hl;   // the rows' shape functions as double-single pairs
+  const float2 *frho_ds;      // F' spline c0..c2 per knot as double-single pairs
 };
 bool fused_fits(int nr, int nrho);
 void elem_fused(const MixedElems &m, const FusedTables &t, int pass, const float4 *tab,

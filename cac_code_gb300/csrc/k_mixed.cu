@@ -1360,6 +1360,9 @@ struct FusedArgs {
   const double *nodex;         // FP64 nodes (guard-band decisions)
   const int *etype, *row_first, *node_list, *int_off, *inter_off;
   const int4 *intp;            // lattice indices (i, j, k) of every type's rows
+  const float2 *spa_int_hl;    // the rows' shape functions as double-single pairs
+  const float2 *frho_ds;       // F' spline c0..c2 per knot as double-single pairs
+  float2 rdrho_ds;             // 1 / drho as a double-single pair
   const double *spa_int;       // FP64 shape functions of the rows
   const double *spa_inter;     // FP64 shape functions of the sites
   const int *fjj, *fjj_off;    // per type: the rows of nonzero weight, ascending
@@ -1412,6 +1415,32 @@ __device__ __forceinline__ float4 lds_v4(const float4 *p) {
                : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
                : "r"((unsigned) __cvta_generic_to_shared(p)));
   return v;
+}
+
+// F'(rho) at a row, rho = sum_k N_k erho_k, as fprime64 forms it (pair_eam.cpp:
+// 1090-1100, knot index, clamps, cubic) in double-single FP32 arithmetic from
+// the double-single shape functions, nodal densities and spline
+// coefficients: the FP32 value of the FP64 result, without an FP64
+// instruction (also *rho32, rho rounded to FP32)
+__device__ __forceinline__ float row_fprime_ds(const float2 *__restrict__ N,
+                                               const double *__restrict__ er,
+                                               const float2 *__restrict__ c3, int nrho,
+                                               float2 rdrho, float &rho32) {
+  ds rho = ds{0.f, 0.f};
+#pragma unroll
+  for (int k = 0; k < NPE; k++) rho = ds_madd(ds{N[k].x, N[k].y}, ds_of_double(er[k]), rho);
+  rho32 = rho.h + rho.l;
+  ds p = ds_madd(rho, ds{rdrho.x, rdrho.y}, ds{1.f, 0.f});
+  int m = (int) p.h;  // floor of p.h + p.l (p >= 1)
+  if ((float) m == p.h && p.l < 0.f) m -= 1;
+  m = m < nrho - 1 ? m : nrho - 1;
+  m = 1 > m ? 1 : m;
+  p = ds_add(ds{p.h - (float) m, 0.f}, ds{p.l, 0.f});
+  if (p.h + p.l > 1.f) p = ds{1.f, 0.f};
+  const float2 a = c3[3 * m], b = c3[3 * m + 1], c = c3[3 * m + 2];
+  ds q = ds_madd(p, ds{a.x, a.y}, ds{b.x, b.y});
+  q = ds_madd(p, q, ds{c.x, c.y});
+  return q.h + q.l;
 }
 
 // FP64 cutoff decision of a guard-band pair: the row's point and the site from
@@ -1684,21 +1713,25 @@ k_elem_force_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rd
     const FusedLat g = fused_lat(a.lat, ty);
     const int f0 = a.fjj_off[ty], nf = a.fjj_off[ty + 1] - f0;
     fused_coeffs(a.node_hl, e, lane, s_k, V != 0);
-    if (EAM && lane >= 24) {  // density coefficients from the nodal densities (FP32)
+    if (EAM && lane >= 24) {  // density coefficients from the nodal densities (FP32,
+      // formed in double-single from the doubles' bits: no FP64 instruction)
       const double *er = erho + NPE * (size_t) e;
       const int m = lane - 24;
-      float v;
+      auto E = [&](int k) { return ds_of_double(er[k]); };
+      ds v;
       switch (m) {
-        case 0: v = (float) er[0]; break;
-        case 1: v = (float) (er[1] - er[0]); break;
-        case 2: v = (float) (er[3] - er[0]); break;
-        case 3: v = (float) (er[4] - er[0]); break;
-        case 4: v = (float) ((er[0] - er[1]) + (er[2] - er[3])); break;
-        case 5: v = (float) ((er[0] - er[1]) + (er[5] - er[4])); break;
-        case 6: v = (float) ((er[0] - er[3]) + (er[7] - er[4])); break;
-        default: v = (float) (((er[1] - er[0]) + (er[3] - er[2])) + ((er[4] - er[5]) + (er[6] - er[7])));
+        case 0: v = E(0); break;
+        case 1: v = ds_sub(E(1), E(0)); break;
+        case 2: v = ds_sub(E(3), E(0)); break;
+        case 3: v = ds_sub(E(4), E(0)); break;
+        case 4: v = ds_add(ds_sub(E(0), E(1)), ds_sub(E(2), E(3))); break;
+        case 5: v = ds_add(ds_sub(E(0), E(1)), ds_sub(E(5), E(4))); break;
+        case 6: v = ds_add(ds_sub(E(0), E(3)), ds_sub(E(7), E(4))); break;
+        default:
+          v = ds_add(ds_add(ds_sub(E(1), E(0)), ds_sub(E(3), E(2))),
+                     ds_add(ds_sub(E(4), E(5)), ds_sub(E(6), E(7))));
       }
-      s_r[m] = v;
+      s_r[m] = v.h + v.l;
     }
     __syncwarp();
     float k[21];
@@ -1716,16 +1749,10 @@ k_elem_force_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rd
         // F'(rho) at the row, rho in FP64 from the nodal densities (k_row_fp);
         // the row's density in FP32 for the sites' (rho(p) in rk[0])
         float rho32 = 0.f;
-        if (live && glane == 0) {
-          const double *N = a.spa_int + ((size_t) a.int_off[ty] + jj) * NPE;
-          double rho = 0.0;
-#pragma unroll
-          for (int q = 0; q < NPE; q++) rho += N[q] * erho[NPE * (size_t) e + q];
-          fpi = (float) fprime64(rho, a.frho, a.nrho, a.rdrho64);
-          rho32 = (float) rho;
-        }
-        fpi = __shfl_sync(0xffffffffu, fpi, lane & ~(FG - 1));
-        rk[0] = __shfl_sync(0xffffffffu, rho32, lane & ~(FG - 1));
+        if (live)  // every lane of the row's group (no shuffle)
+          fpi = row_fprime_ds(a.spa_int_hl + ((size_t) a.int_off[ty] + jj) * NPE,
+                              erho + NPE * (size_t) e, a.frho_ds, a.nrho, a.rdrho_ds, rho32);
+        rk[0] = rho32;
         if (V == 0) {
 #pragma unroll
           for (int q = 1; q < 8; q++) rk[q] = s_r[q];
@@ -2105,6 +2132,12 @@ void elem_fused(const MixedElems &m, const FusedTables &t, int pass, const float
   a.int_off = t.int_off;
   a.inter_off = t.inter_off;
   a.intp = t.intp;
+  a.spa_int_hl = t.spa_int_hl;
+  a.frho_ds = t.frho_ds;
+  {
+    const float h = (float) e.rdrho;
+    a.rdrho_ds = make_float2(h, (float) (e.rdrho - (double) h));
+  }
   a.spa_int = t.spa_int;
   a.spa_inter = t.spa_inter;
   a.fjj = t.fjj;
