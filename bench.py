@@ -88,6 +88,9 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-modes", action="store_true", help="skip timing the other precision modes")
+    p.add_argument("--study", choices=["strain", "drift", "surrogate"],
+                   help="a longer measurement instead of the benchmark (one JSON line)")
+    p.add_argument("--study-steps", type=int, default=0, help="steps of a study (0: its default)")
     return p.parse_args()
 
 
@@ -775,8 +778,207 @@ def run_reference(a, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+
+
+# ----------------------------------------------------------------------------- studies
+#
+# Longer measurements run on request (--study), one JSON line each; none is
+# part of the default run.
+
+def _system(cacg, W, m, cfg, eam, mode, extra=(), damp_elements=0.0):
+    import numpy as np
+    s = cacg.System(0)
+    W.configure_system(s, m, cfg, eam)
+    for c in extra:
+        s.command(c)
+    if damp_elements > 0.0 and m.nelements:
+        s.set_group("elems", None, np.ones(m.nelements, dtype=np.int32))
+        s.command(f"fix 3 elems viscous {damp_elements!r}")
+    s.set_precision(mode)
+    s.init()
+    s.setup()
+    if m.natoms:
+        s.neighbor_build()
+    if m.nelements:
+        s.neighbor_ebuild()
+        s.neighbor_nbuild()
+    return s
+
+
+def _rel(f, ref):
+    import numpy as np
+    f = np.asarray(f, dtype=np.float64).reshape(-1, 3)
+    ref = np.asarray(ref, dtype=np.float64).reshape(-1, 3)
+    if not ref.size:
+        return None
+    d = np.linalg.norm(f - ref, axis=1)
+    n = np.linalg.norm(ref, axis=1)
+    return {"rms_rel": float(np.sqrt((d ** 2).mean() / (n ** 2).mean())),
+            "max_rel": float(d.max() / n.max())}
+
+
+def study_strain(a):
+    """C3: 4,017,200 atoms + 200,000 elements under the uniaxial ramp
+    (1e8 / s along x = 1e-4 / ps, "fix 2 all deform 1 x erate 1e-4"), run
+    in mixed precision and, side by side, in FP64 (FMA).  Every 100 steps:
+    the mixed forces against an FP64 evaluation of the same state (atoms and
+    nodes), and the two trajectories' energies and virials.  The nodes are
+    damped ("fix 3 elems viscous 100", both runs, a relaxation time of about
+    11 fs for nodes of 1331 / 8 atomic masses): under the reference's element
+    force the isolated elements of this configuration gain kinetic energy
+    without bound (node kinetic energy 8 eV -> 2e6 eV by step 1,400 on a
+    1,452-atom + 24-element slab in the oracle, and likewise here), deform and
+    leave the box; a damping of 10 only delays that to about step 4,000.  The
+    atoms are not damped."""
+    import numpy as np
+    from cac_code_gb300 import build, cacg
+    from cac_code_gb300 import workloads as W
+    build.build_library()
+    eam = W.write_eam(os.path.join(tempfile.mkdtemp(), "Cu_analytic_2000.eam"))
+    m, cfg = W.c3_eam()
+    sites = W.metric_sites(m, cfg)
+    deform = ["fix 2 all deform 1 x erate 1e-4"]
+    t0 = time.perf_counter()
+    A = _system(cacg, W, m, cfg, eam, cacg.MIXED, deform, damp_elements=100.0)
+    B = _system(cacg, W, m, cfg, eam, cacg.FP64, deform, damp_elements=100.0)
+    steps = a.study_steps or 5000
+    rec, err = [], None
+    lo0, hi0 = A.box()
+    L0 = hi0[0] - lo0[0]
+    k = 0
+    try:
+        while True:
+            A.pair_compute()
+            A.pair_ecompute()
+            fm = (A.atoms()["f"].copy(), A.elements()["nodef"].copy())
+            A.set_precision(cacg.FP64)
+            A.pair_compute()
+            A.pair_ecompute()
+            f64 = (A.atoms()["f"].copy(), A.elements()["nodef"].copy())
+            A.set_precision(cacg.MIXED)
+            ta, tb = A.thermo(), B.thermo()
+            lo, hi = A.box()
+            vs = max(np.abs(tb["virial"]).max(), 1e-30)
+            rec.append({"step": k, "strain_x": float((hi[0] - lo[0]) / L0 - 1.0),
+                        "force_err_atoms": _rel(fm[0], f64[0]),
+                        "force_err_nodes": _rel(fm[1], f64[1]),
+                        "e_mixed_ev_per_site": ta["etotal"] / sites,
+                        "e_fp64_ev_per_site": tb["etotal"] / sites,
+                        "de_ev_per_site": (ta["etotal"] - tb["etotal"]) / sites,
+                        "de_atoms_ev_per_atom": ((ta["pe_atoms"] + ta["ke_atoms"]) -
+                                                 (tb["pe_atoms"] + tb["ke_atoms"])) / m.natoms,
+                        "virial_rel_diff": float(np.abs(ta["virial"] - tb["virial"]).max() / vs)})
+            if k >= steps:
+                break
+            A.run(100)
+            B.run(100)
+            k += 100
+    except Exception as ex:  # the synthetic elements can leave the box's range
+        err = f"stopped at step {k}: {ex}"
+    out = {"study": "strain", "workload": "C3: EAM Cu 4,017,200 atoms + 200,000 elements of "
+                                         "11 sites per edge, x ramp 1e8/s, mixed beside FP64, "
+                                         "nodes damped (fix viscous 100)",
+           "steps": k, "records": rec, "error": err,
+           "max_force_err_nodes": max((r["force_err_nodes"]["max_rel"] for r in rec), default=None),
+           "max_force_err_atoms": max((r["force_err_atoms"]["max_rel"] for r in rec), default=None),
+           "wall_s": round(time.perf_counter() - t0, 1),
+           "counts_mixed": A.counts(), "counts_fp64": B.counts()}
+    A.close()
+    B.close()
+    print(json.dumps(out), flush=True)
+
+
+def study_drift(a):
+    """Energy of the atom subsystem over NVE steps (atoms and elements do not
+    interact, so the atoms alone carry the precision question): the C2 atom
+    slab (1,016,400 atoms, free x faces, periodic y, z, 300 K), bit-exact FP64
+    against mixed precision with F'(rho) of the atoms from the FP64 or the FP32
+    spline, with the configuration's potential (not smoothed: phi(r_c) =
+    -0.0189 eV) and with the same potential tapered to zero at the cutoff."""
+    import numpy as np
+    from cac_code_gb300 import build, cacg
+    from cac_code_gb300 import lattice as L
+    from cac_code_gb300 import workloads as W
+    build.build_library()
+    tmp = tempfile.mkdtemp()
+    pots = {"plain": W.write_eam(os.path.join(tmp, "Cu_plain.eam")),
+            "tapered": os.path.join(tmp, "Cu_tapered.eam")}
+    pot = L.AnalyticEAM(taper=1.0)
+    L.write_eam_funcfl(pot, pots["tapered"], nrho=2000, nr=2000, r_max=pot.cut * 1.01)
+    m, cfg = W.c2_eam(cells=(21, 110, 110), layers=0)
+    n = m.natoms
+    steps = a.study_steps or 10000
+    every = 100
+    variants = [("exact", cacg.FP64_EXACT, []), ("mixed", cacg.MIXED, []),
+                ("mixed_fp32_fprime", cacg.MIXED, ["tune fprime fp32"])]
+    out = {"study": "drift", "atoms": n, "steps": steps, "dt_fs": 1.0, "results": {}}
+    t0 = time.perf_counter()
+    for pname, pfile in pots.items():
+        series = {}
+        for name, mode, extra in variants:
+            s = _system(cacg, W, m, cfg, pfile, mode, extra)
+            e = []
+            for k in range(0, steps + 1, every):
+                t = s.thermo()
+                e.append(t["pe_atoms"] + t["ke_atoms"])
+                if k < steps:
+                    s.run(every)
+            series[name] = np.array(e)
+            s.close()
+        res = {}
+        for name, e in series.items():
+            res[name] = {"drift_ev_per_atom": float((e[-1] - e[0]) / n),
+                         "max_excursion_ev_per_atom": float(np.abs(e - e[0]).max() / n),
+                         "max_diff_from_exact_ev_per_atom": float(np.abs(e - series["exact"]).max() / n),
+                         "e_every_100_ev_per_atom": [round(float(v / n), 9) for v in e[::10]]}
+        out["results"][pname] = res
+    out["wall_s"] = round(time.perf_counter() - t0, 1)
+    print(json.dumps(out), flush=True)
+
+
+def study_surrogate(a):
+    """The surrogate's error floor against training-set size, epochs and
+    ensemble size, on held-out elements of 11 sites per edge: rms and max
+    nodal-force error relative to the force scale, the per-element largest
+    error, the ensemble spread, and the fractions within 1e-4."""
+    import numpy as np
+    from cac_code_gb300 import build
+    from cac_code_gb300 import surrogate as S
+    from cac_code_gb300 import workloads as W
+    build.build_library()
+    eam = W.write_eam(os.path.join(tempfile.mkdtemp(), "Cu_analytic_2000.eam"))
+    t0 = time.perf_counter()
+    xs, ts, info = S.generate(eam, 2000000, seed=11, snapshots=16)
+    xv, tv, _ = S.generate(eam, 65536, seed=12, snapshots=4)
+    a_ = np.hstack([xs[:400000], np.ones((400000, 1), np.float32)]).astype(np.float64)
+    coef, *_ = np.linalg.lstsq(a_, ts[:400000].astype(np.float64), rcond=None)
+    lin = np.hstack([xv, np.ones((xv.shape[0], 1))]) @ coef
+    rows = [{"model": "linear least squares (400k samples)", **S.force_errors(lin, tv)}]
+    for nsamp, members, epochs in ((250000, 4, 10), (1000000, 4, 10), (2000000, 4, 10),
+                                   (2000000, 2, 30), (2000000, 4, 30)):
+        t1 = time.perf_counter()
+        net, loss = S.train(xs[:nsamp], ts[:nsamp], members=members, epochs=epochs, batch=2048,
+                            lr=2e-3)
+        tt = time.perf_counter() - t1
+        pm, psp = net.predict(xv)
+        fs = net.normalization()[4]
+        per = np.abs(pm - tv).max(axis=1) / fs
+        rows.append({"samples": nsamp, "members": members, "epochs": epochs,
+                     "train_s": round(tt, 1), "loss": loss, **S.force_errors(pm, tv),
+                     "median_element_max_err_rel": float(np.median(per)),
+                     "spread_median_rel": float(np.median(psp) / fs),
+                     "fraction_err_within_1e-4": float(np.mean(per <= 1e-4)),
+                     "fraction_spread_within_1e-4": float(np.mean(psp <= 1e-4 * fs))})
+        net.close()
+    print(json.dumps({"study": "surrogate", "samples": info, "heldout": int(xv.shape[0]),
+                      "rows": rows, "wall_s": round(time.perf_counter() - t0, 1)}), flush=True)
+
+
 def main():
     a = parse()
+    if a.study:
+        {"strain": study_strain, "drift": study_drift, "surrogate": study_surrogate}[a.study](a)
+        return
     ws, rank, local = dist_init()
     if a.impl == "reference":
         run_reference(a, ws, rank)

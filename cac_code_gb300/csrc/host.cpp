@@ -247,6 +247,9 @@ struct cacg_context {
   // 2.48 against 3.18 ms for the force pass), or as 1 with two entries in
   // flight per lane (2)
   int fused_variant = 1;
+  // "tune fprime fp64|fp32": F'(rho) of the atoms in the mixed density pass
+  // from the FP64 spline at the FP64 density (default), or from the FP32 copy
+  bool fprime64 = true;
   DBuf<int> d_fjj, d_fjj_off;
   DBuf<int4> d_intp4;  // lattice indices (i, j, k) of every type's rows
   // lanes per integration point ("tune ip_group N"; 0: from the row count, so
@@ -846,6 +849,7 @@ void cacg_context::command(const std::string &raw) {
     // tune cull yes|no: the mixed EAM density pass skips list entries that no
     //   displacement since the list reorder can bring within the cutoff
     // tune streams yes|no: a mixed step's atom and element chains on two streams
+    // tune fprime fp64|fp32: F'(rho) of the atoms in the mixed density pass
     // tune fused yes|no: the mixed element passes one warp per element
     //   (when every list entry references its row's own element)
     // tune elists lazy|eager: in the FP64 and mixed modes a rebuild that only
@@ -869,6 +873,10 @@ void cacg_context::command(const std::string &raw) {
     } else if (a[0] == "streams") {
       if (a[1] != "yes" && a[1] != "no") fail(CACG_EINVAL, "tune streams takes yes or no");
       two_streams = a[1] == "yes";
+      invalidate_graph();
+    } else if (a[0] == "fprime") {
+      if (a[1] != "fp64" && a[1] != "fp32") fail(CACG_EINVAL, "tune fprime takes fp64 or fp32");
+      fprime64 = a[1] == "fp64";
       invalidate_graph();
     } else if (a[0] == "fused_variant") {
       const int v = inumeric(a[1]);
@@ -2442,6 +2450,7 @@ void cacg_context::pair_compute_mixed(int pass) {
   const float eps = 1.0e-4f;
   mixed::MixedAtoms m{};
   m.block = mixed_block;
+  m.fprime64 = fprime64;
   m.x = d_x.p;
   m.num = d_num.p;
   m.list = d_list.p;

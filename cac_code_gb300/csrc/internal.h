@@ -273,6 +273,7 @@ struct MixedAtoms {
   const int4 *nnear = nullptr;
   const unsigned *dmax2 = nullptr;
   int block = 512;    // threads per block of the persistent grids (autotuned)
+  bool fprime64 = true;  // F'(rho) of the atoms from the FP64 spline ("tune fprime")
 };
 // Displacement culling of the mixed passes: list entries beyond r_c + d at
 // the last reorder are skipped while twice the largest displacement since

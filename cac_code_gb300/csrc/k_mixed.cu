@@ -150,6 +150,10 @@ struct AtomArgs {
   // plus CULL_MARGIN reaches are skipped
   const int4 *nnear;
   const unsigned *dmax2;  // [0]: squared displacement bits; [1]: reordered in this step
+  // F'(rho) of the density pass: from the FP64 spline at the FP64 density
+  // (fprime64, rounded to FP32 for the force pass), else FP32 (fprime32)
+  const double *frho64 = nullptr;
+  double rdrho64 = 0.0;
 };
 
 __device__ __forceinline__ bool moved_little(const unsigned *dmax2) {
@@ -272,7 +276,8 @@ k_eam_rho_atoms(AtomArgs a, const float4 *__restrict__ rhor_val, int nr, float r
     a.snum[i] = ns;
     acc.add(part);
     rho[i] = acc.value();
-    fp[i] = fprime32(__fadd_rn(acc.h, acc.l), fp4, nrho, rdrho);
+    fp[i] = a.frho64 ? (float) fprime64(acc.value(), a.frho64, nrho, a.rdrho64)
+                     : fprime32(__fadd_rn(acc.h, acc.l), fp4, nrho, rdrho);
   }
 }
 
@@ -452,7 +457,8 @@ k_eam_rho_union(AtomArgs a, UnionArgs u, const float4 *__restrict__ rhor_val, in
       a.snum[i] = ns;
       acc.add(part);
       rho[i] = acc.value();
-      fp[i] = fprime32(__fadd_rn(acc.h, acc.l), fp4, nrho, rdrho);
+      fp[i] = a.frho64 ? (float) fprime64(acc.value(), a.frho64, nrho, a.rdrho64)
+                       : fprime32(__fadd_rn(acc.h, acc.l), fp4, nrho, rdrho);
     }
     __syncwarp();  // the union is overwritten by the warp's next group
   }
@@ -1866,6 +1872,10 @@ void eam_rho_atoms(const MixedAtoms &m, const float4 *rhor_val, const EamTables 
   if (m.nlocal <= 0) return;
   AtomArgs a{m.x, m.xq, m.qg, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
              m.band_hi, m.cutsq, m.snum, m.slist, m.nnear, m.dmax2};
+  if (m.fprime64) {
+    a.frho64 = e.frho;
+    a.rdrho64 = e.rdrho;
+  }
   size_t smem = sizeof(float4) * (e.nr + 1);
   int g = persistent_grid((const void *) k_eam_rho_atoms, m.block, smem, m.nlocal);
   k_eam_rho_atoms<<<g, m.block, smem, s>>>(a, rhor_val, e.nr, (float) e.rdr, fp4, e.nrho,
@@ -1912,6 +1922,10 @@ void eam_rho_union(const MixedAtoms &m, const int *union_j, const int *union_n,
   if (m.nlocal <= 0) return;
   AtomArgs a{m.x, m.xq, m.qg, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
              m.band_hi, m.cutsq, m.snum, m.slist, nullptr, nullptr};
+  if (m.fprime64) {
+    a.frho64 = e.frho;
+    a.rdrho64 = e.rdrho;
+  }
   UnionArgs u{union_j, union_n, slot, sslot};
   size_t smem = sizeof(float4) * ((e.nr + 1) + (size_t) UWARPS * UMAX);
   int g = union_grid((const void *) k_eam_rho_union, smem, m.nlocal);
