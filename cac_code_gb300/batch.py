@@ -8,12 +8,25 @@ class.  The replicas of a class share one handle: they sit side by side along
 the non-periodic x axis, each a slab with the class's periodic y-z cross
 section, separated by gaps wider than the element neighbor cutoff, so that no
 list ever crosses from one replica into another.  Every kernel of a step then
-covers all replicas of the class at once, and steps without a rebuild
-decision replay one captured CUDA graph.
+covers all replicas of the class at once.
 
-Per class an autotuner times the candidate bin sizes (the reference's default
-r_n / 2 and r_n) and thread-block sizes of the persistent mixed-precision
-kernels (256, 512) on a few steps and keeps the fastest.
+Each class runs its steps through the device step loop ("tune loop device"):
+one CUDA graph launch runs step after step, the rebuild decision
+(Neighbor::decide, neighbor.cpp:1150-1163) taken on the device, and returns to
+the host only for a step that needs a rebuild.  The classes run at the same
+time, each handle on its own stream driven by its own host thread.
+
+The nodes are damped (fix viscous): under the reference's element force the
+elements of these slabs gain kinetic energy without bound over some hundreds
+of steps, and the damping keeps 2,000 steps of every replica bounded.
+
+Per class an autotuner searches, on a few steps from the same starting state
+each, the bin size (the reference's default r_n / 2, or r_n) and the threads
+per block of the persistent mixed-precision kernels (128, 256, 512), then, on
+the best of those, one stream or two (atom and element chains) and the
+arrangement of the fused element kernel (coefficients in registers, in shared
+memory, or in shared memory with two entries in flight per lane), and keeps
+the fastest.
 
 The reference runs one system per process; it has no batching.
 """
@@ -21,6 +34,7 @@ from __future__ import annotations
 
 import dataclasses
 import math
+import threading
 import time
 from typing import Dict, List, Tuple
 
@@ -34,13 +48,18 @@ A_LJ = (4.0 / 1.0) ** (1.0 / 3.0)  # FCC at rho* = 1.0
 
 # per pair style: lattice, element size (sites per edge), cross sections (in
 # element periods) of the size classes, gap between replicas, reference commands
+# (damp: fix viscous gamma of the nodes, relaxation times m / gamma of about 8
+# steps for EAM nodes of 1000 / 8 Cu masses and 1.3 steps for LJ nodes of
+# 512 / 8 masses; in the oracle the hottest replica of the smallest class runs
+# 2,000 steps bounded with these, while LJ nodes under gamma 1000 or 5000 gain
+# energy again after 1,000-2,000 steps)
 STYLE = {
     "eam": dict(a=W.A_CU, nae=10, units="metal", skin=7.5, gap=70.0, kb=W.KB["metal"],
-                mvv2e=W.MVV2E["metal"], t_scale=1.0, dt=0.001),
+                mvv2e=W.MVV2E["metal"], t_scale=1.0, dt=0.001, damp=100.0),
     # LJ temperatures: T* = kB T / eps with eps = 0.4 eV (a Cu-like well), so
     # 10-600 K maps to T* = 0.002-0.13, below the LJ melting point
     "lj": dict(a=A_LJ, nae=8, units="lj", skin=2.8, gap=20.0, kb=1.0, mvv2e=1.0,
-               t_scale=8.617343e-5 / 0.4, dt=0.005),
+               t_scale=8.617343e-5 / 0.4, dt=0.005, damp=10000.0),
 }
 SIZE_CLASSES = [(2000, 8000, 1), (8000, 20000, 2), (20000, 60001, 3)]  # sites lo, hi, periods
 
@@ -159,69 +178,156 @@ def _restore(s: cacg.System, snap):
     s.put_nodes(snap[2], snap[3])
 
 
-def autotune(s: cacg.System, skin: float, steps: int = 20) -> Dict:
-    """Fastest (bin size, block size) of the candidates on `steps` steps, each
-    trial from the same starting state."""
-    best, trials = None, []
+def _apply(s: cacg.System, opts: Dict) -> None:
+    b = opts["binsize"]
+    s.command(f"neigh_modify binsize {b!r}" if b else "neigh_modify binsize 0.0")
+    s.command(f"tune block {opts['block']}")
+    if "streams" in opts:
+        s.command(f"tune streams {opts['streams']}")
+    if "fused_variant" in opts:
+        s.command(f"tune fused_variant {opts['fused_variant']}")
+
+
+def autotune(s: cacg.System, skin: float, steps: int = 12) -> Dict:
+    """Fastest options on `steps` steps, each trial from the same starting
+    state: bin size x block size, then streams x fused-kernel arrangement on
+    the best of those (the arrangements only when the element passes run
+    fused)."""
+    trials = []
     snap = _snapshot(s)
-    for binsize in (0.0, skin):  # 0: the reference's default r_n / 2
-        for block in (256, 512):
-            s.command(f"neigh_modify binsize {binsize!r}" if binsize else "neigh_modify binsize 0.0")
-            s.command(f"tune block {block}")
-            _restore(s, snap)
-            _prepare(s)
-            s.run(3)
-            s.run(steps)
-            ms = s.timing()[0] / steps
-            trials.append({"binsize": binsize or "default", "block": block, "ms_per_step": ms})
-            if best is None or ms < best[0]:
-                best = (ms, binsize, block)
-    s.command(f"neigh_modify binsize {best[1]!r}" if best[1] else "neigh_modify binsize 0.0")
-    s.command(f"tune block {best[2]}")
+
+    def trial(opts):
+        _apply(s, opts)
+        _restore(s, snap)
+        _prepare(s)
+        s.run(3)
+        s.run(steps)
+        ms = s.timing()[0] / steps
+        trials.append(dict(opts, binsize=opts["binsize"] or "default", ms_per_step=ms))
+        return ms
+
+    stage1 = [{"binsize": b, "block": k} for b in (0.0, skin) for k in (128, 256, 512)]
+    best = min(stage1, key=trial)
+    fused = s.counts()["elem_fused"] == 1
+    stage2 = [dict(best, streams=st, fused_variant=v)
+              for st in ("yes", "no") for v in ((0, 1, 2) if fused else (1,))]
+    best = min(stage2, key=trial)
+    _apply(s, best)
     _restore(s, snap)
     _prepare(s)
-    return {"chosen": {"binsize": best[1] or "default", "block": best[2]}, "trials": trials}
+    chosen = dict(best, binsize=best["binsize"] or "default")
+    return {"chosen": chosen, "trials": trials}
+
+
+@dataclasses.dataclass
+class _Class:
+    pair: str
+    k: int
+    reps: List[Replica]
+    system: cacg.System
+    sites: int
+    atoms: int
+    elements: int
+    build_s: float
+    tuned: Dict = None
+    ms: float = 0.0
+    wall_s: float = 0.0
+    c0: Dict = None
+    c1: Dict = None
+    error: BaseException = None
+
+
+def _prepare_class(pair: str, k: int, rs: List[Replica], eam_file: str, device: int, mode: int,
+                   tune: bool, loop: str) -> _Class:
+    periods = SIZE_CLASSES[k][2]
+    st = STYLE[pair]
+    t0 = time.perf_counter()
+    big, cla, cle, spans = pack([replica_model(r, periods) for r in rs], st["gap"])
+    t_build = time.perf_counter() - t0
+    cfg = class_config(pair)
+    s = cacg.System(device)
+    try:
+        W.configure_system(s, big, cfg, eam_file)
+        s.set_group("clamp", cla, cle)
+        s.command("fix 2 clamp setforce 0.0 0.0 0.0")
+        if big.nelements:
+            s.set_group("nodes", None, np.ones(big.nelements, dtype=np.int32))
+            s.command(f"fix 3 nodes viscous {st['damp']!r}")
+        s.set_precision(mode)
+        s.command(f"tune loop {loop}")
+        s.init()
+        _prepare(s)
+        c = _Class(pair, k, rs, s, W.metric_sites(big, cfg), big.natoms, big.nelements,
+                   round(t_build, 2))
+        c.tuned = autotune(s, cfg["skin"]) if tune else None
+        s.run(3)
+        return c
+    except BaseException:
+        s.close()
+        raise
+
+
+def _run_class(c: _Class, steps: int) -> None:
+    try:
+        c.c0 = c.system.counts()
+        t0 = time.perf_counter()
+        c.system.run(steps)
+        c.wall_s = time.perf_counter() - t0
+        c.ms = c.system.timing()[0]
+        c.c1 = c.system.counts()
+    except BaseException as ex:  # re-raised by the caller
+        c.error = ex
 
 
 def run_batch(eam_file: str, n: int = 256, steps: int = 2000, seed: int = 4, tune: bool = True,
-              device: int = 0, mode: int = cacg.MIXED) -> Dict:
-    """All replicas, class by class; returns per-class and whole-batch site-steps/s."""
+              device: int = 0, mode: int = cacg.MIXED, loop: str = "device",
+              concurrent: bool = True) -> Dict:
+    """All replicas: the classes prepared (and autotuned) one after another,
+    then timed together, each class's steps on its own stream from its own
+    host thread (concurrent=False: one class after another).  Returns
+    per-class and whole-batch site-steps/s; the whole batch's is the total
+    site-steps over the wall time of the timed run."""
     reps = draw_replicas(n, seed)
-    classes: Dict[Tuple[str, int], List[Replica]] = {}
+    groups: Dict[Tuple[str, int], List[Replica]] = {}
     for r in reps:
-        classes.setdefault((r.pair, size_class(r.sites)), []).append(r)
-    out, tot_sites_steps, tot_ms = [], 0.0, 0.0
-    for (pair, k), rs in sorted(classes.items()):
-        periods = SIZE_CLASSES[k][2]
+        groups.setdefault((r.pair, size_class(r.sites)), []).append(r)
+    classes: List[_Class] = []
+    try:
+        for (pair, k), rs in sorted(groups.items()):
+            classes.append(_prepare_class(pair, k, rs, eam_file, device, mode, tune, loop))
         t0 = time.perf_counter()
-        big, cla, cle, spans = pack([replica_model(r, periods) for r in rs], STYLE[pair]["gap"])
-        t_build = time.perf_counter() - t0
-        cfg = class_config(pair)
-        s = cacg.System(device)
-        try:
-            W.configure_system(s, big, cfg, eam_file)
-            s.set_group("clamp", cla, cle)
-            s.command("fix 2 clamp setforce 0.0 0.0 0.0")
-            s.set_precision(mode)
-            s.init()
-            _prepare(s)
-            tuned = autotune(s, cfg["skin"]) if tune else None
-            sites = W.metric_sites(big, cfg)
-            s.run(3)
-            c0 = s.counts()
-            s.run(steps)
-            ms = s.timing()[0]
-            c1 = s.counts()
-            out.append({"pair": pair, "size_class": list(SIZE_CLASSES[k][:2]), "replicas": len(rs),
-                         "sites": sites, "atoms": big.natoms, "elements": big.nelements,
-                         "cross_section_periods": periods, "steps": steps, "ms": ms,
-                         "site_steps_per_s": sites * steps / (ms * 1e-3),
-                         "graph_steps": c1["graph_steps"] - c0["graph_steps"],
-                         "rebuilds": c1["rebuilds"] - c0["rebuilds"], "build_s": round(t_build, 2),
-                         "autotune": tuned})
-            tot_sites_steps += sites * steps
-            tot_ms += ms
-        finally:
-            s.close()
-    return {"replicas": n, "classes": out, "site_steps_per_s": tot_sites_steps / (tot_ms * 1e-3),
-            "total_sites": int(sum(c["sites"] for c in out)), "steps": steps}
+        if concurrent:
+            threads = [threading.Thread(target=_run_class, args=(c, steps)) for c in classes]
+            for t in threads:
+                t.start()
+            for t in threads:
+                t.join()
+        else:
+            for c in classes:
+                _run_class(c, steps)
+        wall = time.perf_counter() - t0
+        for c in classes:
+            if c.error is not None:
+                raise c.error
+        out = []
+        for c in classes:
+            c0, c1 = c.c0, c.c1
+            out.append({"pair": c.pair, "size_class": list(SIZE_CLASSES[c.k][:2]),
+                        "replicas": len(c.reps), "sites": c.sites, "atoms": c.atoms,
+                        "elements": c.elements, "cross_section_periods": SIZE_CLASSES[c.k][2],
+                        "steps": steps, "ms": c.ms, "wall_s": round(c.wall_s, 3),
+                        "site_steps_per_s": c.sites * steps / (c.ms * 1e-3),
+                        "graph_steps": c1["graph_steps"] - c0["graph_steps"],
+                        "rebuilds": c1["rebuilds"] - c0["rebuilds"],
+                        "loop_launches": c1["loop_launches"] - c0["loop_launches"],
+                        "host_decisions": c1["host_decisions"] - c0["host_decisions"],
+                        "build_s": c.build_s, "autotune": c.tuned})
+        tot = sum(c.sites for c in classes) * steps
+        return {"replicas": n, "classes": out, "steps": steps,
+                "total_sites": int(sum(c.sites for c in classes)),
+                "site_steps_per_s": tot / wall, "wall_s": round(wall, 3),
+                "concurrent": concurrent, "loop": loop,
+                "sum_of_class_ms": round(sum(c.ms for c in classes), 1)}
+    finally:
+        for c in classes:
+            c.system.close()

@@ -402,12 +402,27 @@ struct cacg_context {
   unsigned long long graph_epoch = 0;
   long long graph_launches = 0, graph_steps = 0;
   int eager_since = 0;
+  // device step loop ("tune loop device|host"): one graph launch runs steps
+  // back to back, the rebuild decision taken on the device (a WHILE node
+  // around the step, an IF node around its force passes), until the wanted
+  // steps are done or a step needs a rebuild, which the host then performs
+  std::atomic<unsigned long long> epoch{0};  // allocations made in calls on this handle
+  bool loop_device = false;
+  DBuf<int> d_loop;
+  cudaGraphExec_t lexec = nullptr;
+  bool lgraph_valid = false;
+  unsigned long long lgraph_epoch = 0;
+  long long lgraph_pre = 0, lgraph_post = 0;  // kernels per iteration before / after the decision
+  long long loop_launches = 0, host_decisions = 0;
   void invalidate_graph() {
     graph_valid = false;
     hgraph_valid = false;
+    lgraph_valid = false;
     eager_since = 0;
   }
   bool capture_plain_step();
+  bool capture_loop();
+  int run_loop(int n);
   std::vector<cudaEvent_t> pev;  // per-step phase events
   // with timing on: events around the main kernels of each step; kernel k of
   // step j is bracketed by events 2 (j KT_N + k) and 2 (j KT_N + k) + 1
@@ -659,7 +674,7 @@ cacg_context::~cacg_context() {
                      &d_int_off, &d_inter_off, &d_numint, &d_inter_num, &d_node_list,
                      &d_list_isub, &d_sub_first, &d_flags, &d_pos, &d_scan, &d_misc,
                      &d_snum, &d_slist, &d_sipnum, &d_sipent, &d_force_rows, &d_need,
-                     &d_need_elem, &d_site_flag, &d_site_pos};
+                     &d_need_elem, &d_site_flag, &d_site_pos, &d_loop};
   for (auto *b : bi) b->release();
   d_ljtab.release();
   for (auto &e : ev)
@@ -667,6 +682,7 @@ cacg_context::~cacg_context() {
   for (auto &e : pev) cudaEventDestroy(e);
   for (auto &e : kev) cudaEventDestroy(e);
   if (gexec) cudaGraphExecDestroy(gexec);
+  if (lexec) cudaGraphExecDestroy(lexec);
   if (h_pin) cudaFreeHost(h_pin);
   if (fork_ev) cudaEventDestroy(fork_ev);
   if (hexec) cudaGraphExecDestroy(hexec);
@@ -854,6 +870,10 @@ void cacg_context::command(const std::string &raw) {
     //   (when every list entry references its row's own element)
     // tune elists lazy|eager: in the FP64 and mixed modes a rebuild that only
     //   atoms triggered keeps the element lists and ghosts (lazy, the default)
+    // tune loop device|host: steps run as one graph launch with the rebuild
+    //   decision on the device (with graphs on, no box deformation), or one
+    //   graph launch per step without a decision and eager decision steps
+    //   (host, the default)
     if (a.size() != 2) fail(CACG_EINVAL, "Illegal tune command");
     if (a[0] == "block") {
       int b = inumeric(a[1]);
@@ -890,6 +910,10 @@ void cacg_context::command(const std::string &raw) {
     } else if (a[0] == "elists") {
       if (a[1] != "lazy" && a[1] != "eager") fail(CACG_EINVAL, "tune elists takes lazy or eager");
       lazy_elists = a[1] == "lazy";
+    } else if (a[0] == "loop") {
+      if (a[1] != "device" && a[1] != "host") fail(CACG_EINVAL, "tune loop takes device or host");
+      loop_device = a[1] == "device";
+      invalidate_graph();
     } else {
       fail(CACG_EINVAL, "Illegal tune command");
     }
@@ -3209,6 +3233,7 @@ void cacg_context::nve_final(int which) {
 int cacg_context::decide() {
   ago++;
   if (ago >= delay && ago % every == 0) {
+    host_decisions++;
     if (dist_check == 0) return 1;
     d_misc.ensure(32, stream);
     check(cudaMemsetAsync(d_misc.p + 6, 0, sizeof(int), stream), "memset");
@@ -3315,7 +3340,10 @@ void cacg_context::run(int n) {
   const size_t P = 6;  // phase marks per step
   std::fill(kev_used.begin(), kev_used.end(), 0);
   cur_step = 0;
-  for (int step = 0; step < n; step++) {
+  // the device loop runs the steps it can (all of them unless its capture
+  // fails, which leaves the rest to the loop below)
+  const int step0 = loop_device && use_graphs && graph_ok && !deform_on && n > 0 ? run_loop(n) : 0;
+  for (int step = step0; step < n; step++) {
     size_t b = (size_t) step * P;
     cur_step = (size_t) step;
     ntimestep++;
@@ -3744,6 +3772,188 @@ void cacg_context::run_host(int n, double *x, double *v, double *nodex, double *
   finish();
 }
 
+// The device step loop: a WHILE node whose body is a step's initial
+// integration, the gated distance check and the decision kernel, then an IF
+// node around the step's communication, force passes, post-force fixes and
+// final integration (the body of a plain step).  The decision kernel sets
+// both conditions.  Anything that would allocate or synchronise ends a
+// capture with an error; the steps then run the host way and the device loop
+// stays off for this handle.
+bool cacg_context::capture_loop() {
+  upload_masks();  // host-to-device copies stay outside the capture
+  d_loop.ensure(LOOP_SLOTS, stream);
+  if (!astream && fork_ok()) {  // the second chain's stream exists before the capture
+    int least = 0, greatest = 0;
+    check(cudaDeviceGetStreamPriorityRange(&least, &greatest), "stream priorities");
+    check(cudaStreamCreateWithPriority(&astream, cudaStreamNonBlocking, greatest), "atom stream");
+  }
+  const unsigned long long e0 = dbuf_epoch();
+  const long long l0 = launches;
+  cudaGraph_t top = nullptr;
+  cudaGraphExec_t ex = nullptr;
+  cudaGraphConditionalHandle again = 0, proceed = 0;
+  cudaGraph_t body = nullptr, then = nullptr;
+  long long pre = 0, post = 0;
+  bool ok = cudaGraphCreate(&top, 0) == cudaSuccess &&
+            cudaGraphConditionalHandleCreate(&again, top, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+  if (ok) {
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = again;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    ok = cudaGraphAddNode(&node, top, nullptr, nullptr, 0, &p) == cudaSuccess;
+    if (ok) body = p.conditional.phGraph_out[0];
+  }
+  ok = ok && cudaGraphConditionalHandleCreate(&proceed, body, 0, 0) == cudaSuccess;
+  capturing = true;
+  // the step up to the decision
+  if (ok && cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+    std::vector<cudaGraphNode_t> leaves;
+    try {
+      nve_initial();
+      if (dist_check) {
+        BoxWrap box{};
+        for (int d = 0; d < 3; d++) {
+          box.lo[d] = lo[d];
+          box.hi[d] = hi[d];
+          box.periodic[d] = periodic[d];
+        }
+        launch_loop_check(d_x.p, d_xhold.p, nlocal, d_nodex.p, d_nodexhold.p, enlocal,
+                          enlocal ? d_ex.p : nullptr, box, triggersq, d_loop.p, every, delay, stream);
+        launches++;
+      }
+      launch_loop_decide(d_loop.p, every, delay, dist_check, again, proceed, stream);
+      launches++;
+      cudaStreamCaptureStatus st;
+      const cudaGraphNode_t *deps = nullptr;
+      size_t nd = 0;
+      if (cudaStreamGetCaptureInfo(stream, &st, nullptr, nullptr, &deps, nullptr, &nd) != cudaSuccess)
+        ok = false;
+      else
+        leaves.assign(deps, deps + nd);
+    } catch (...) {
+      ok = false;
+    }
+    cudaGraph_t g = nullptr;
+    if (cudaStreamEndCapture(stream, &g) != cudaSuccess) ok = false;
+    pre = launches - l0;
+    if (ok) {
+      cudaGraphNodeParams p = {};
+      p.type = cudaGraphNodeTypeConditional;
+      p.conditional.handle = proceed;
+      p.conditional.type = cudaGraphCondTypeIf;
+      p.conditional.size = 1;
+      cudaGraphNode_t node = nullptr;
+      ok = cudaGraphAddNode(&node, body, leaves.data(), nullptr, leaves.size(), &p) == cudaSuccess;
+      if (ok) then = p.conditional.phGraph_out[0];
+    }
+  } else {
+    ok = false;
+  }
+  // the rest of the step, as a plain step runs it
+  if (ok && cudaStreamBeginCaptureToGraph(stream, then, nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+    const long long l1 = launches;
+    try {
+      if (fork_ok()) {
+        const bool nodes_done = post_fixes.empty();
+        forked(
+            [&] {
+              forward_comm(1);
+              pair_compute_pass(1);
+              pair_compute_pass(2);
+            },
+            [&] {
+              forward_comm(2);
+              pair_ecompute();
+              if (nodes_done) nve_final(2);
+            });
+        post_force();
+        nve_final(nodes_done ? 1 : 3);
+      } else {
+        forward_comm();
+        force_passes(-1);
+        post_force();
+        nve_final();
+      }
+    } catch (...) {
+      ok = false;
+    }
+    cudaGraph_t g = nullptr;
+    if (cudaStreamEndCapture(stream, &g) != cudaSuccess) ok = false;
+    post = launches - l1;
+  } else {
+    ok = false;
+  }
+  capturing = false;
+  if (ok && dbuf_epoch() != e0) ok = false;
+  if (ok && cudaGraphInstantiate(&ex, top, 0) != cudaSuccess) ok = false;
+  if (top) cudaGraphDestroy(top);
+  cudaGetLastError();  // a failed capture leaves its error behind
+  launches = l0;
+  if (!ok) {
+    if (ex) cudaGraphExecDestroy(ex);
+    loop_device = false;
+    return false;
+  }
+  if (lexec) cudaGraphExecDestroy(lexec);
+  lexec = ex;
+  lgraph_pre = pre;
+  lgraph_post = post;
+  lgraph_epoch = e0;
+  lgraph_valid = true;
+  return true;
+}
+
+// Up to n steps through the device loop; returns the steps taken (n unless a
+// capture failed).  Each launch runs until the wanted steps are done or a
+// step needs a rebuild: that step's initial integration and decision ran on
+// the device, the host rebuilds and finishes it, and the next launch goes on.
+int cacg_context::run_loop(int n) {
+  int done = 0;
+  int *hl = h_pin + 16;
+  while (done < n) {
+    if (!lgraph_valid || lgraph_epoch != dbuf_epoch()) {
+      if (!capture_loop()) return done;
+    }
+    hl[LOOP_AGO] = ago;
+    hl[LOOP_DONE] = 0;
+    hl[LOOP_WANT] = n - done;
+    hl[LOOP_PENDING] = 0;
+    hl[LOOP_ITERS] = 0;
+    hl[LOOP_BITS] = 0;
+    check(cudaMemcpyAsync(d_loop.p, hl, LOOP_SLOTS * sizeof(int), cudaMemcpyHostToDevice, stream), "loop in");
+    check(cudaGraphLaunch(lexec, stream), "loop launch");
+    check(cudaMemcpyAsync(hl, d_loop.p, LOOP_SLOTS * sizeof(int), cudaMemcpyDeviceToHost, stream), "loop out");
+    sync();
+    loop_launches++;
+    const int steps = hl[LOOP_DONE], iters = hl[LOOP_ITERS], flags = hl[LOOP_PENDING];
+    if (steps < 0 || steps > n - done || iters < steps || iters > steps + 1)
+      fail(CACG_ECUDA, "device step loop: %d steps in %d iterations of %d wanted", steps, iters,
+           n - done);
+    ago = hl[LOOP_AGO];
+    done += steps;
+    ntimestep += steps;
+    graph_steps += steps;
+    launches += lgraph_pre * iters + lgraph_post * steps;
+    if (flags) {  // the step after those: initial integration and decision done
+      ntimestep++;
+      cur_step = (size_t) done;
+      rebuild(flags);
+      force_passes(-1);
+      post_force();
+      nve_final();
+      done++;
+    } else if (steps == 0) {
+      fail(CACG_ECUDA, "device step loop made no progress");
+    }
+  }
+  return done;
+}
+
 // The body of a step without a rebuild decision, captured into a CUDA graph.
 // Anything that would allocate or synchronise ends the capture with an error;
 // the step then runs eagerly and graphs stay off for this handle.
@@ -3814,6 +4024,7 @@ bool cacg_context::capture_plain_step() {
 
 #define API_BEGIN                 \
   if (!h) return CACG_EINVAL;     \
+  EpochScope epoch_scope_(&h->epoch);  \
   try {                           \
     check(cudaSetDevice(h->device), "cudaSetDevice");
 #define API_END                                                              \
@@ -4105,12 +4316,12 @@ int cacg_run_host(cacg_handle h, int nsteps, double *x, double *v, double *nodex
 
 int cacg_get_counts(cacg_handle h, long long *c, int n) {
   API_BEGIN
-  long long v[28] = {h->nlocal, h->nghost, 0, h->enlocal, h->enghost, 0, h->nrows, 0,
+  long long v[30] = {h->nlocal, h->nghost, 0, h->enlocal, h->enghost, 0, h->nrows, 0,
                      h->nrebuild, (long long) h->stencil.size(), h->ntimestep, h->nsites,
                      h->launches, h->nneed, h->nforce, 0, h->sur ? h->nfar : 0, 0, 0,
                      h->graph_steps, 0, 0, 0, h->nrebuild_atoms, 0,
                      (long long) h->h_nlines[0], (long long) h->h_nlines[1],
-                     h->fused_used ? 1LL : 0LL};
+                     h->fused_used ? 1LL : 0LL, h->loop_launches, h->host_decisions};
   if (h->areorders_zeroed && h->d_misc.p) {
     unsigned r = 0;
     check(cudaMemcpyAsync(&r, h->d_misc.p + 16, sizeof(r), cudaMemcpyDeviceToHost, h->stream), "areorders");
@@ -4187,7 +4398,7 @@ int cacg_get_counts(cacg_handle h, long long *c, int n) {
       for (const int4 &x : nn) v[21] += level == 1 ? x.x : level == 2 ? x.y : x.z;
     }
   }
-  for (int i = 0; i < n && i < 28; i++) c[i] = v[i];
+  for (int i = 0; i < n && i < 30; i++) c[i] = v[i];
   API_END
 }
 

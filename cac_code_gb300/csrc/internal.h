@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstddef>
 #include <cstdint>
 #include <string>
@@ -26,12 +27,39 @@ inline void check(cudaError_t e, const char *where) {
   if (e != cudaSuccess) throw CudaError{e, where};
 }
 
-// Bumped whenever any device array is allocated or freed: a CUDA graph
-// captured under an older value may hold pointers that are gone.
-inline unsigned long long &dbuf_epoch() {
-  static unsigned long long e = 0;
+// Allocation epochs: bumped whenever a device array is allocated or freed, so
+// that a CUDA graph captured under an older value (it may hold pointers that
+// are gone) is dropped.  An allocation made inside a call on a handle counts
+// in that handle's epoch (the C ABI's entry points install it for the calling
+// thread), any other in the global one; a handle's graphs are checked against
+// the sum of both.  Handles driven from threads of their own thus do not drop
+// each other's graphs.
+inline std::atomic<unsigned long long> &dbuf_global_epoch() {
+  static std::atomic<unsigned long long> e{0};
   return e;
 }
+inline std::atomic<unsigned long long> *&dbuf_epoch_slot() {
+  static thread_local std::atomic<unsigned long long> *p = nullptr;
+  return p;
+}
+inline void dbuf_bump() {
+  if (std::atomic<unsigned long long> *p = dbuf_epoch_slot()) ++*p;
+  else ++dbuf_global_epoch();
+}
+inline unsigned long long dbuf_epoch() {
+  const std::atomic<unsigned long long> *p = dbuf_epoch_slot();
+  return (p ? p->load() : 0ULL) + dbuf_global_epoch().load();
+}
+// installs a handle's epoch for the calling thread for the scope of a call
+struct EpochScope {
+  std::atomic<unsigned long long> *prev;
+  explicit EpochScope(std::atomic<unsigned long long> *e) : prev(dbuf_epoch_slot()) {
+    dbuf_epoch_slot() = e;
+  }
+  ~EpochScope() { dbuf_epoch_slot() = prev; }
+  EpochScope(const EpochScope &) = delete;
+  EpochScope &operator=(const EpochScope &) = delete;
+};
 
 // Growable device array.  Growth keeps contents when asked (ghost appends).
 template <class T>
@@ -40,7 +68,7 @@ struct DBuf {
   size_t cap = 0;
   void ensure(size_t n, cudaStream_t s, bool keep = false) {
     if (n <= cap) return;
-    dbuf_epoch()++;
+    dbuf_bump();
     size_t ncap = cap ? cap : 256;
     while (ncap < n) ncap = ncap + ncap / 2 + 256;
     T *q = nullptr;
@@ -56,7 +84,7 @@ struct DBuf {
   void release() {
     if (p) {
       cudaFree(p);
-      dbuf_epoch()++;
+      dbuf_bump();
     }
     p = nullptr;
     cap = 0;
@@ -556,6 +584,20 @@ void launch_check_distance(const double4 *x, const double *xhold, int n,
                            const double *nodex, const double *nodexhold, int ne,
                            const double *ex, const BoxWrap &box, double triggersq, int *flag,
                            cudaStream_t s);
+// the device step loop's state (int slots): steps since setup, steps done in
+// this launch, steps wanted, flags of a pending rebuild (0: none), loop
+// iterations, check_distance bits of the current step
+enum { LOOP_AGO = 0, LOOP_DONE, LOOP_WANT, LOOP_PENDING, LOOP_ITERS, LOOP_BITS, LOOP_SLOTS };
+// check_distance for the device loop: only on steps that reach a decision,
+// bits into loop[LOOP_BITS]
+void launch_loop_check(const double4 *x, const double *xhold, int n, const double *nodex,
+                       const double *nodexhold, int ne, const double *ex, const BoxWrap &box,
+                       double triggersq, int *loop, int every, int delay, cudaStream_t s);
+// the decision of the device loop: sets the loop's conditions (again: run
+// another iteration; proceed: this step's force passes run)
+void launch_loop_decide(int *loop, int every, int delay, int dist_check,
+                        cudaGraphConditionalHandle again, cudaGraphConditionalHandle proceed,
+                        cudaStream_t s);
 void launch_hold_atoms(const double4 *x, double *xhold, int n, cudaStream_t s);
 void launch_elem_diag(const double *nodex, const double *ex, int n, double *diag,
                       int *centre_bad, cudaStream_t s);

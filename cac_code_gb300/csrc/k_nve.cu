@@ -108,11 +108,18 @@ __global__ void k_nve_nodes_final(double *__restrict__ nodev, const double *__re
 // atom moved more than the trigger distance since its list build, 2 a node
 // did since the element list build, 4 an element centre lies outside the box
 // in a periodic dimension (Domain::elepbc would wrap it).
+// With gate (the device step loop's state, gate[0] = steps since setup before
+// this one), the kernel returns at once unless this step reaches a decision.
 __global__ void k_check_distance(const double4 *__restrict__ x, const double *__restrict__ xh,
                                  int n, const double *__restrict__ nodex,
                                  const double *__restrict__ nodexh, int ne,
                                  const double *__restrict__ ex, BoxWrap box, double triggersq,
-                                 int *__restrict__ flag) {
+                                 int *__restrict__ flag, const int *__restrict__ gate, int every,
+                                 int delay) {
+  if (gate) {
+    const int ago = gate[0] + 1;
+    if (ago < delay || ago % every != 0) return;  // uniform over the grid
+  }
   const long long t = (long long) blockIdx.x * blockDim.x + threadIdx.x;
   const long long nn = (long long) ne * NPE;
   int bit = 0;
@@ -245,8 +252,61 @@ void launch_check_distance(const double4 *x, const double *xhold, int n,
   long long tot = (long long) n + (long long) ne * NPE + (ex ? ne : 0);
   if (tot <= 0) return;
   k_check_distance<<<nblk(tot, 256), 256, 0, s>>>(x, xhold, n, nodex, nodexhold, ne, ex, box,
-                                                   triggersq, flag);
+                                                   triggersq, flag, nullptr, 1, 0);
   check(cudaGetLastError(), "check_distance");
+}
+
+void launch_loop_check(const double4 *x, const double *xhold, int n, const double *nodex,
+                       const double *nodexhold, int ne, const double *ex, const BoxWrap &box,
+                       double triggersq, int *loop, int every, int delay, cudaStream_t s) {
+  long long tot = (long long) n + (long long) ne * NPE + (ex ? ne : 0);
+  if (tot <= 0) return;
+  k_check_distance<<<nblk(tot, 256), 256, 0, s>>>(x, xhold, n, nodex, nodexhold, ne, ex, box,
+                                                   triggersq, loop + LOOP_BITS, loop, every, delay);
+  check(cudaGetLastError(), "loop check");
+}
+
+// Neighbor::decide (neighbor.cpp:1150-1163) inside the device step loop: one
+// thread.  ago counts steps since setup (not reset by a rebuild); a decision
+// step whose check found an atom or a node past the trigger (or any decision
+// step without the check) ends the loop before the step's force passes, with
+// the flags left for the host's rebuild; any other step runs on and counts
+// as done.  The loop also ends when the wanted steps are done, and never runs
+// more iterations than steps wanted.
+__global__ void k_loop_decide(int *__restrict__ loop, int every, int delay, int dist_check,
+                              cudaGraphConditionalHandle again, cudaGraphConditionalHandle proceed) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int ago = loop[LOOP_AGO] + 1;
+  const int it = loop[LOOP_ITERS] + 1;
+  loop[LOOP_AGO] = ago;
+  loop[LOOP_ITERS] = it;
+  int flags = 0;
+  if (ago >= delay && ago % every == 0) {
+    if (!dist_check) {
+      flags = 1;
+    } else {
+      const int b = loop[LOOP_BITS];
+      flags = (b & 3) ? b : 0;  // a wrap alone needs no rebuild
+    }
+    loop[LOOP_BITS] = 0;
+  }
+  if (flags) {
+    loop[LOOP_PENDING] = flags;
+    cudaGraphSetConditional(proceed, 0u);
+    cudaGraphSetConditional(again, 0u);
+    return;
+  }
+  const int done = loop[LOOP_DONE] + 1;
+  loop[LOOP_DONE] = done;
+  cudaGraphSetConditional(proceed, 1u);
+  cudaGraphSetConditional(again, (done < loop[LOOP_WANT] && it < loop[LOOP_WANT]) ? 1u : 0u);
+}
+
+void launch_loop_decide(int *loop, int every, int delay, int dist_check,
+                        cudaGraphConditionalHandle again, cudaGraphConditionalHandle proceed,
+                        cudaStream_t s) {
+  k_loop_decide<<<1, 32, 0, s>>>(loop, every, delay, dist_check, again, proceed);
+  check(cudaGetLastError(), "loop decide");
 }
 
 void launch_hold_atoms(const double4 *x, double *xhold, int n, cudaStream_t s) {

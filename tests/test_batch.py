@@ -82,8 +82,24 @@ def test_small_batched_run_with_autotuner(cacg_lib):
     from cac_code_gb300 import workloads as W
     eam = W.write_eam(os.path.join(tempfile.gettempdir(), "cacg_batch_Cu2000.eam"))
     res = B.run_batch(eam, n=6, steps=30, seed=7, tune=True)
-    assert res["replicas"] == 6 and len(res["classes"]) >= 2
+    assert res["replicas"] == 6 and len(res["classes"]) >= 2 and res["concurrent"]
     for c in res["classes"]:
         assert np.isfinite(c["site_steps_per_s"]) and c["site_steps_per_s"] > 0
-        assert c["graph_steps"] > 0
-        assert c["autotune"]["chosen"]["block"] in (256, 512)
+        # every step without a rebuild ran inside a device-loop graph launch,
+        # and no rebuild decision was taken on the host
+        assert c["graph_steps"] == 30 - c["rebuilds"]
+        assert c["host_decisions"] == 0 and 1 <= c["loop_launches"] <= c["rebuilds"] + 1
+        assert c["autotune"]["chosen"]["block"] in (128, 256, 512)
+        assert len(c["autotune"]["trials"]) >= 8
+
+
+@pytest.mark.gpu
+def test_concurrent_classes_match_one_after_another(cacg_lib):
+    """The classes run from their own threads on their own streams give the
+    same per-class results as the same classes run one after another."""
+    from cac_code_gb300 import workloads as W
+    eam = W.write_eam(os.path.join(tempfile.gettempdir(), "cacg_batch_Cu2000.eam"))
+    a = B.run_batch(eam, n=6, steps=40, seed=7, tune=False, concurrent=True)
+    b = B.run_batch(eam, n=6, steps=40, seed=7, tune=False, concurrent=False)
+    for ca, cb in zip(a["classes"], b["classes"]):
+        assert (ca["pair"], ca["sites"], ca["rebuilds"]) == (cb["pair"], cb["sites"], cb["rebuilds"])
