@@ -2475,6 +2475,7 @@ void cacg_context::pair_compute_mixed(int pass) {
   mixed::MixedAtoms m{};
   m.block = mixed_block;
   m.fprime64 = fprime64;
+  m.frho_ds = d_frho_ds.p;
   m.x = d_x.p;
   m.num = d_num.p;
   m.list = d_list.p;
@@ -3340,10 +3341,18 @@ void cacg_context::run(int n) {
   const size_t P = 6;  // phase marks per step
   std::fill(kev_used.begin(), kev_used.end(), 0);
   cur_step = 0;
-  // the device loop runs the steps it can (all of them unless its capture
-  // fails, which leaves the rest to the loop below)
-  const int step0 = loop_device && use_graphs && graph_ok && !deform_on && n > 0 ? run_loop(n) : 0;
-  for (int step = step0; step < n; step++) {
+  for (int step = 0; step < n; step++) {
+    // the device loop runs the steps it can; it hands back a step that must
+    // run here first (after set-up or a rebuild: first-call allocations and
+    // read-backs stay outside the capture), and all steps once its capture
+    // has failed
+    if (loop_device && use_graphs && graph_ok && !deform_on) {
+      const int k = run_loop(n - step);
+      if (k > 0) {
+        step += k - 1;
+        continue;
+      }
+    }
     size_t b = (size_t) step * P;
     cur_step = (size_t) step;
     ntimestep++;
@@ -3407,6 +3416,7 @@ void cacg_context::run(int n) {
     nve_final();
     deform_step();
     mark(b + 5);
+    if (nflag == 0) eager_since++;  // every pass of a plain step has run eagerly
   }
   // the packed-range counter is read back behind the last step, so that one
   // synchronisation serves both
@@ -3794,6 +3804,11 @@ bool cacg_context::capture_loop() {
   cudaGraphConditionalHandle again = 0, proceed = 0;
   cudaGraph_t body = nullptr, then = nullptr;
   long long pre = 0, post = 0;
+  // a capture into a conditional body that ends invalidated may leave that
+  // body released by the runtime while its node still refers to it: the
+  // whole graph is then left alone (not destroyed), once, as the device loop
+  // goes off for the handle
+  bool destroyable = true;
   bool ok = cudaGraphCreate(&top, 0) == cudaSuccess &&
             cudaGraphConditionalHandleCreate(&again, top, 1, cudaGraphCondAssignDefault) == cudaSuccess;
   if (ok) {
@@ -3838,7 +3853,7 @@ bool cacg_context::capture_loop() {
       ok = false;
     }
     cudaGraph_t g = nullptr;
-    if (cudaStreamEndCapture(stream, &g) != cudaSuccess) ok = false;
+    if (cudaStreamEndCapture(stream, &g) != cudaSuccess) ok = destroyable = false;
     pre = launches - l0;
     if (ok) {
       cudaGraphNodeParams p = {};
@@ -3883,7 +3898,7 @@ bool cacg_context::capture_loop() {
       ok = false;
     }
     cudaGraph_t g = nullptr;
-    if (cudaStreamEndCapture(stream, &g) != cudaSuccess) ok = false;
+    if (cudaStreamEndCapture(stream, &g) != cudaSuccess) ok = destroyable = false;
     post = launches - l1;
   } else {
     ok = false;
@@ -3891,7 +3906,7 @@ bool cacg_context::capture_loop() {
   capturing = false;
   if (ok && dbuf_epoch() != e0) ok = false;
   if (ok && cudaGraphInstantiate(&ex, top, 0) != cudaSuccess) ok = false;
-  if (top) cudaGraphDestroy(top);
+  if (top && destroyable) cudaGraphDestroy(top);
   cudaGetLastError();  // a failed capture leaves its error behind
   launches = l0;
   if (!ok) {
@@ -3908,16 +3923,19 @@ bool cacg_context::capture_loop() {
   return true;
 }
 
-// Up to n steps through the device loop; returns the steps taken (n unless a
-// capture failed).  Each launch runs until the wanted steps are done or a
-// step needs a rebuild: that step's initial integration and decision ran on
-// the device, the host rebuilds and finishes it, and the next launch goes on.
+// Up to n steps through the device loop; returns the steps taken.  Each
+// launch runs until the wanted steps are done or a step needs a rebuild:
+// that step's initial integration and decision ran on the device, the host
+// rebuilds and finishes it, and the next launch goes on.  A capture waits for
+// one eager step since the last set-up, rebuild or change (fewer steps are
+// returned, and the caller runs that step); a failed capture turns the device
+// loop off for the handle.
 int cacg_context::run_loop(int n) {
   int done = 0;
   int *hl = h_pin + 16;
   while (done < n) {
     if (!lgraph_valid || lgraph_epoch != dbuf_epoch()) {
-      if (!capture_loop()) return done;
+      if (eager_since < 1 || !capture_loop()) return done;
     }
     hl[LOOP_AGO] = ago;
     hl[LOOP_DONE] = 0;

@@ -302,6 +302,7 @@ struct MixedAtoms {
   const unsigned *dmax2 = nullptr;
   int block = 512;    // threads per block of the persistent grids (autotuned)
   bool fprime64 = true;  // F'(rho) of the atoms from the FP64 spline ("tune fprime")
+  const float2 *frho_ds = nullptr;  // its F' coefficients as double-single pairs
 };
 // Displacement culling of the mixed passes: list entries beyond r_c + d at
 // the last reorder are skipped while twice the largest displacement since

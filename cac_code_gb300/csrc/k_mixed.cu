@@ -91,6 +91,73 @@ struct dsacc {
   __device__ __forceinline__ double value() const { return (double) h + (double) l; }
 };
 
+// Double-single FP32 arithmetic: a value is an unevaluated sum hi + lo of two
+// floats; products and sums use error-free transformations (TwoProduct via
+// fma, Knuth's TwoSum), about 44 bits without an FP64 instruction.
+struct ds {
+  float h, l;
+};
+
+// fast TwoSum (|s| >= |e|)
+__device__ __forceinline__ ds ds_renorm(float s, float e) {
+  const float h = __fadd_rn(s, e);
+  return ds{h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+
+__device__ __forceinline__ ds ds_add(ds a, ds b) {
+  const float s = __fadd_rn(a.h, b.h);
+  const float v = __fsub_rn(s, a.h);
+  float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, v)), __fsub_rn(b.h, v));
+  e = __fadd_rn(e, __fadd_rn(a.l, b.l));
+  return ds_renorm(s, e);
+}
+
+__device__ __forceinline__ ds ds_sub(ds a, ds b) { return ds_add(a, ds{-b.h, -b.l}); }
+
+// x + a * d, dropping a.l * d.l
+__device__ __forceinline__ ds ds_madd(ds a, ds d, ds x) {
+  const float p = __fmul_rn(a.h, d.h);
+  float pe = __fmaf_rn(a.h, d.h, -p);
+  pe = __fmaf_rn(a.h, d.l, pe);
+  pe = __fmaf_rn(a.l, d.h, pe);
+  return ds_add(x, ds{p, pe});
+}
+
+// A double as a double-single by integer operations on its bits, without an
+// FP64 instruction: hi keeps the sign, the exponent and the top 23 stored
+// mantissa bits (a truncation, exact in FP32), lo the remaining 29 bits
+// scaled by 2^(e-1075) (rounded once).  Zero and values below 2^-74 give 0.
+__device__ __forceinline__ ds ds_of_double(double x) {
+  const unsigned bh = (unsigned) __double2hiint(x), bl = (unsigned) __double2loint(x);
+  const int ex = (int) ((bh >> 20) & 0x7FF);
+  if (ex < 949) return ds{0.f, 0.f};
+  const unsigned sign = bh & 0x80000000u;
+  const float h = __uint_as_float(sign | ((unsigned) (ex - 896) << 23) | ((bh & 0xFFFFFu) << 3) |
+                                  (bl >> 29));
+  const float scale = __uint_as_float((unsigned) (ex - 948) << 23);  // 2^(ex - 1075)
+  const float l = __fmul_rn(__uint2float_rn(bl & 0x1FFFFFFFu), scale);
+  return ds{h, sign ? -l : l};
+}
+
+// F'(rho) as fprime64 forms it (pair_eam.cpp:1090-1100: knot index, clamps,
+// cubic) from the FP64 spline's coefficients as double-single pairs, in
+// double-single arithmetic: the FP32 rounding of the FP64 result, without an
+// FP64 instruction
+__device__ __forceinline__ float fprime_ds(ds rho, const float2 *__restrict__ c3, int nrho,
+                                           float2 rdrho) {
+  ds p = ds_madd(rho, ds{rdrho.x, rdrho.y}, ds{1.f, 0.f});
+  int m = (int) p.h;  // floor of p.h + p.l (p >= 1)
+  if ((float) m == p.h && p.l < 0.f) m -= 1;
+  m = m < nrho - 1 ? m : nrho - 1;
+  m = 1 > m ? 1 : m;
+  p = ds_add(ds{p.h - (float) m, 0.f}, ds{p.l, 0.f});
+  if (p.h + p.l > 1.f) p = ds{1.f, 0.f};
+  const float2 a = c3[3 * m], b = c3[3 * m + 1], c = c3[3 * m + 2];
+  ds q = ds_madd(p, ds{a.x, a.y}, ds{b.x, b.y});
+  q = ds_madd(p, q, ds{c.x, c.y});
+  return q.h + q.l;
+}
+
 // sum of a double-single over each aligned group of G lanes (xor shuffles)
 template <int G>
 __device__ __forceinline__ void group_sum(dsacc &a) {
@@ -150,10 +217,11 @@ struct AtomArgs {
   // plus CULL_MARGIN reaches are skipped
   const int4 *nnear;
   const unsigned *dmax2;  // [0]: squared displacement bits; [1]: reordered in this step
-  // F'(rho) of the density pass: from the FP64 spline at the FP64 density
-  // (fprime64, rounded to FP32 for the force pass), else FP32 (fprime32)
-  const double *frho64 = nullptr;
-  double rdrho64 = 0.0;
+  // F'(rho) of the density pass: from the FP64 spline at the double-single
+  // density (fprime_ds: the FP32 rounding of the FP64 result), else from the
+  // FP32 spline at the FP32 density (fprime32)
+  const float2 *frho_ds = nullptr;
+  float2 rdrho_ds = {0.f, 0.f};
 };
 
 __device__ __forceinline__ bool moved_little(const unsigned *dmax2) {
@@ -276,8 +344,8 @@ k_eam_rho_atoms(AtomArgs a, const float4 *__restrict__ rhor_val, int nr, float r
     a.snum[i] = ns;
     acc.add(part);
     rho[i] = acc.value();
-    fp[i] = a.frho64 ? (float) fprime64(acc.value(), a.frho64, nrho, a.rdrho64)
-                     : fprime32(__fadd_rn(acc.h, acc.l), fp4, nrho, rdrho);
+    fp[i] = a.frho_ds ? fprime_ds(ds_renorm(acc.h, acc.l), a.frho_ds, nrho, a.rdrho_ds)
+                       : fprime32(__fadd_rn(acc.h, acc.l), fp4, nrho, rdrho);
   }
 }
 
@@ -457,8 +525,8 @@ k_eam_rho_union(AtomArgs a, UnionArgs u, const float4 *__restrict__ rhor_val, in
       a.snum[i] = ns;
       acc.add(part);
       rho[i] = acc.value();
-      fp[i] = a.frho64 ? (float) fprime64(acc.value(), a.frho64, nrho, a.rdrho64)
-                       : fprime32(__fadd_rn(acc.h, acc.l), fp4, nrho, rdrho);
+      fp[i] = a.frho_ds ? fprime_ds(ds_renorm(acc.h, acc.l), a.frho_ds, nrho, a.rdrho_ds)
+                        : fprime32(__fadd_rn(acc.h, acc.l), fp4, nrho, rdrho);
     }
     __syncwarp();  // the union is overwritten by the warp's next group
   }
@@ -568,7 +636,10 @@ k_eam_force_atoms(AtomArgs a, const float4 *__restrict__ ftab, int nr, float rdr
     dsacc fx, fy, fz;
     float px = 0.f, py = 0.f, pz = 0.f;
     int cnt = 0;
-    int jn = 0;
+    // software pipeline: the list index two entries ahead and the next
+    // entry's coordinates and F' in flight while this entry is evaluated, so
+    // that no gather waits on a list load issued in the same iteration
+    int jn = 0, jnn = 0;
     float4 qn = qi;
     float fpn = 0.f;
     if (n > 0) {
@@ -576,12 +647,14 @@ k_eam_force_atoms(AtomArgs a, const float4 *__restrict__ ftab, int nr, float rdr
       qn = __ldg(a.xq + jn);
       fpn = __ldg(fp + jn);
     }
+    if (n > 1) jnn = __ldg(a.slist + (size_t) a.stride + i);
     for (int k = 0; k < n; k++) {
       const int j = jn;
       const float4 qj = qn;
       const float fpj = fpn;
-      if (k + 1 < n) {  // next entry's gathers in flight during this one
-        jn = __ldg(a.slist + (size_t) (k + 1) * a.stride + i);
+      jn = jnn;
+      if (k + 2 < n) jnn = __ldg(a.slist + (size_t) (k + 2) * a.stride + i);
+      if (k + 1 < n) {
         qn = __ldg(a.xq + jn);
         fpn = __ldg(fp + jn);
       }
@@ -635,10 +708,22 @@ k_lj_atoms(AtomArgs a, const int *__restrict__ type, const float *__restrict__ l
     const int n = a.num[i];
     dsacc fx, fy, fz;
     float px = 0.f, py = 0.f, pz = 0.f;
+    // the list index two entries ahead, the next coordinates one ahead
+    int jn = 0, jnn = 0;
+    float4 qn = qi;
+    if (n > 0) {
+      jn = __ldg(a.list + i);
+      qn = __ldg(a.xq + jn);
+    }
+    if (n > 1) jnn = __ldg(a.list + (size_t) a.stride + i);
     for (int k = 0; k < n; k++) {
-      int j = __ldg(a.list + (size_t) k * a.stride + i);
+      const int j = jn;
+      const float4 qj = qn;
+      jn = jnn;
+      if (k + 2 < n) jnn = __ldg(a.list + (size_t) (k + 2) * a.stride + i);
+      if (k + 1 < n) qn = __ldg(a.xq + jn);
       float dx, dy, dz;
-      rel_vec(qi, cx, cy, cz, __ldg(a.xq + j), a.qg, dx, dy, dz);
+      rel_vec(qi, cx, cy, cz, qj, a.qg, dx, dy, dz);
       float rsq = dx * dx + dy * dy + dz * dz;
       int ij = it * (MAXT + 1) + type[j];
       float cs = cutsq_t[ij];
@@ -680,57 +765,12 @@ k_lj_atoms(AtomArgs a, const int *__restrict__ type, const float *__restrict__ l
 // (x(i,j,k) = U(i,j) + c_k D(i,j)), so a site costs three double-single
 // multiply-adds.
 
-struct ds {
-  float h, l;
-};
-
-// fast TwoSum (|s| >= |e|)
-__device__ __forceinline__ ds ds_renorm(float s, float e) {
-  const float h = __fadd_rn(s, e);
-  return ds{h, __fsub_rn(e, __fsub_rn(h, s))};
-}
-
-__device__ __forceinline__ ds ds_add(ds a, ds b) {
-  const float s = __fadd_rn(a.h, b.h);
-  const float v = __fsub_rn(s, a.h);
-  float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, v)), __fsub_rn(b.h, v));
-  e = __fadd_rn(e, __fadd_rn(a.l, b.l));
-  return ds_renorm(s, e);
-}
-
-__device__ __forceinline__ ds ds_sub(ds a, ds b) { return ds_add(a, ds{-b.h, -b.l}); }
-
-// x + a * d, dropping a.l * d.l
-__device__ __forceinline__ ds ds_madd(ds a, ds d, ds x) {
-  const float p = __fmul_rn(a.h, d.h);
-  float pe = __fmaf_rn(a.h, d.h, -p);
-  pe = __fmaf_rn(a.h, d.l, pe);
-  pe = __fmaf_rn(a.l, d.h, pe);
-  return ds_add(x, ds{p, pe});
-}
-
 __device__ __forceinline__ ds ds_lerp(ds x, ds y, ds a) { return ds_madd(a, ds_sub(y, x), x); }
 
 // the lattice fraction k / (n - 1) along an axis of a type, as a double-single
 __device__ __forceinline__ ds frac_of(const Lattice &lat, int ty, int axis, int k) {
   const float2 v = __ldg(lat.frac + (size_t) (ty * 3 + axis) * lat.fstride + k);
   return ds{v.x, v.y};
-}
-
-// A double as a double-single by integer operations on its bits, without an
-// FP64 instruction: hi keeps the sign, the exponent and the top 23 stored
-// mantissa bits (a truncation, exact in FP32), lo the remaining 29 bits
-// scaled by 2^(e-1075) (rounded once).  Zero and values below 2^-74 give 0.
-__device__ __forceinline__ ds ds_of_double(double x) {
-  const unsigned bh = (unsigned) __double2hiint(x), bl = (unsigned) __double2loint(x);
-  const int ex = (int) ((bh >> 20) & 0x7FF);
-  if (ex < 949) return ds{0.f, 0.f};
-  const unsigned sign = bh & 0x80000000u;
-  const float h = __uint_as_float(sign | ((unsigned) (ex - 896) << 23) | ((bh & 0xFFFFFu) << 3) |
-                                  (bl >> 29));
-  const float scale = __uint_as_float((unsigned) (ex - 948) << 23);  // 2^(ex - 1075)
-  const float l = __fmul_rn(__uint2float_rn(bl & 0x1FFFFFFFu), scale);
-  return ds{h, sign ? -l : l};
 }
 
 // node coordinates as double-single pairs, once per element and step
@@ -1436,17 +1476,7 @@ __device__ __forceinline__ float row_fprime_ds(const float2 *__restrict__ N,
 #pragma unroll
   for (int k = 0; k < NPE; k++) rho = ds_madd(ds{N[k].x, N[k].y}, ds_of_double(er[k]), rho);
   rho32 = rho.h + rho.l;
-  ds p = ds_madd(rho, ds{rdrho.x, rdrho.y}, ds{1.f, 0.f});
-  int m = (int) p.h;  // floor of p.h + p.l (p >= 1)
-  if ((float) m == p.h && p.l < 0.f) m -= 1;
-  m = m < nrho - 1 ? m : nrho - 1;
-  m = 1 > m ? 1 : m;
-  p = ds_add(ds{p.h - (float) m, 0.f}, ds{p.l, 0.f});
-  if (p.h + p.l > 1.f) p = ds{1.f, 0.f};
-  const float2 a = c3[3 * m], b = c3[3 * m + 1], c = c3[3 * m + 2];
-  ds q = ds_madd(p, ds{a.x, a.y}, ds{b.x, b.y});
-  q = ds_madd(p, q, ds{c.x, c.y});
-  return q.h + q.l;
+  return fprime_ds(rho, c3, nrho, rdrho);
 }
 
 // FP64 cutoff decision of a guard-band pair: the row's point and the site from
@@ -1873,8 +1903,9 @@ void eam_rho_atoms(const MixedAtoms &m, const float4 *rhor_val, const EamTables 
   AtomArgs a{m.x, m.xq, m.qg, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
              m.band_hi, m.cutsq, m.snum, m.slist, m.nnear, m.dmax2};
   if (m.fprime64) {
-    a.frho64 = e.frho;
-    a.rdrho64 = e.rdrho;
+    a.frho_ds = m.frho_ds;
+    const float h = (float) e.rdrho;
+    a.rdrho_ds = make_float2(h, (float) (e.rdrho - (double) h));
   }
   size_t smem = sizeof(float4) * (e.nr + 1);
   int g = persistent_grid((const void *) k_eam_rho_atoms, m.block, smem, m.nlocal);
@@ -1923,8 +1954,9 @@ void eam_rho_union(const MixedAtoms &m, const int *union_j, const int *union_n,
   AtomArgs a{m.x, m.xq, m.qg, m.num, m.list, m.stride, m.nlocal, m.cutsq_f, m.band_lo,
              m.band_hi, m.cutsq, m.snum, m.slist, nullptr, nullptr};
   if (m.fprime64) {
-    a.frho64 = e.frho;
-    a.rdrho64 = e.rdrho;
+    a.frho_ds = m.frho_ds;
+    const float h = (float) e.rdrho;
+    a.rdrho_ds = make_float2(h, (float) (e.rdrho - (double) h));
   }
   UnionArgs u{union_j, union_n, slot, sslot};
   size_t smem = sizeof(float4) * ((e.nr + 1) + (size_t) UWARPS * UMAX);

@@ -88,8 +88,8 @@ __global__ void k_due(int nfar, const int *__restrict__ far, unsigned char *__re
 }
 
 // due[] indexes far[]; the features, means and spreads are in due order.  A
-// rejection doubles the element's re-test interval (1, 3, 7, 15 steps), an
-// acceptance resets it
+// rejection doubles the element's re-test interval (1, 3, 7, ... 127 steps),
+// an acceptance resets it
 __global__ void k_accept(const float *__restrict__ spread, const int *__restrict__ far,
                          const int *__restrict__ due, const int *__restrict__ count, int nfar,
                          float thr, unsigned char *__restrict__ skip,
@@ -103,7 +103,7 @@ __global__ void k_accept(const float *__restrict__ spread, const int *__restrict
     acc = spread[i] <= thr;
     skip[far[f]] = acc ? 1 : 0;
     if (wait) {
-      const unsigned char st = acc ? 0 : (unsigned char) min(streak[f] + 1, 4);
+      const unsigned char st = acc ? 0 : (unsigned char) min(streak[f] + 1, 7);
       streak[f] = st;
       wait[f] = (unsigned char) ((1u << st) - 1u);
     }
