@@ -956,8 +956,11 @@ int orc_atom_list(orc_sys *s) {
   int nall = s->nlocal + s->nghost;
   s->bins = (int *) realloc(s->bins, (size_t) (nall + 1) * sizeof(int));
   for (int i = 0; i < s->mbins; i++) s->binhead[i] = -1;
+  /* the reference bins without a range check (an atom that left the bin
+     grid indexes past binhead); here that is an error, as on the device */
   for (int i = nall - 1; i >= 0; i--) {
     int ib = coord2bin(s, s->x + 3 * i);
+    if (ib < 0 || ib >= s->mbins) return fail(s, "atoms outside the bin grid (lost atoms)");
     s->bins[i] = s->binhead[ib];
     s->binhead[ib] = i;
   }
@@ -998,6 +1001,7 @@ int orc_elem_lists(orc_sys *s) {
   for (int i = 0; i < s->mbins; i++) s->ebinhead[i] = -1;
   for (int i = nall - 1; i >= 0; i--) {
     int ib = coord2bin(s, s->ex + 3 * i);
+    if (ib < 0 || ib >= s->mbins) return fail(s, "elements outside the bin grid (lost elements)");
     s->ebins[i] = s->ebinhead[ib];
     s->ebinhead[ib] = i;
   }
