@@ -918,10 +918,10 @@ k_lines(const float2 *__restrict__ node_hl, const int *__restrict__ etype, Latti
   __shared__ float2 s_nodes[LCH / 32][24];
   if (gate && moved_little(gate)) return;  // no list reorder in this step
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int e = blockIdx.x * (LCH / 32) + w;
-  if (e >= nelem) return;
   ds *s_col = s_cols + (size_t) w * 12 * max_nax;
   float2 *s_nx = s_nodes[w];
+  // a persistent grid (a gated step then costs one short launch)
+  for (int e = blockIdx.x * (LCH / 32) + w; e < nelem; e += gridDim.x * (LCH / 32)) {
   const int ty = etype[e];
   const int *nae = lat.nae;
   const int nax = nae[3 * ty], nay = nae[3 * ty + 1];
@@ -958,6 +958,8 @@ k_lines(const float2 *__restrict__ node_hl, const int *__restrict__ etype, Latti
     out[3 * L] = make_float4(U[0].h, U[0].l, U[1].h, U[1].l);
     out[3 * L + 1] = make_float4(U[2].h, U[2].l, D[0].h, D[0].l);
     out[3 * L + 2] = make_float4(D[1].h, D[1].l, D[2].h, D[2].l);
+  }
+  __syncwarp();  // the warp's shared columns are rewritten for its next element
   }
 }
 
@@ -1126,15 +1128,15 @@ __global__ void k_row_q(const int *__restrict__ row_elem, const int *__restrict_
                         float4 *__restrict__ ip_h, float4 *__restrict__ ip_l,
                         const unsigned *__restrict__ gate) {
   if (gate && moved_little(gate)) return;  // no list reorder in this step
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= nrows) return;
-  const int e = row_elem[r], ty = etype[e];
-  ds x[3];
-  ip_ds(spa_int_hl + ((size_t) int_off[ty] + row_jj[r]) * NPE, node_hl + 24 * (size_t) e, x);
   const ds l0[3] = {{pg.l0h[0], pg.l0l[0]}, {pg.l0h[1], pg.l0l[1]}, {pg.l0h[2], pg.l0l[2]}};
-  ip_q[r] = pack_u(ds_sub(x[0], l0[0]), ds_sub(x[1], l0[1]), ds_sub(x[2], l0[2]), pg);
-  ip_h[r] = make_float4(x[0].h, x[1].h, x[2].h, 0.f);
-  ip_l[r] = make_float4(x[0].l, x[1].l, x[2].l, 0.f);
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += gridDim.x * blockDim.x) {
+    const int e = row_elem[r], ty = etype[e];
+    ds x[3];
+    ip_ds(spa_int_hl + ((size_t) int_off[ty] + row_jj[r]) * NPE, node_hl + 24 * (size_t) e, x);
+    ip_q[r] = pack_u(ds_sub(x[0], l0[0]), ds_sub(x[1], l0[1]), ds_sub(x[2], l0[2]), pg);
+    ip_h[r] = make_float4(x[0].h, x[1].h, x[2].h, 0.f);
+    ip_l[r] = make_float4(x[0].l, x[1].l, x[2].l, 0.f);
+  }
 }
 
 // F'(rho_i) at the rows of nonzero weight, rho_i = sum_k N_k erho_k in FP64
@@ -2019,7 +2021,7 @@ void lines(const float2 *node_hl, const int *etype, const Lattice &lat, int max_
            cudaStream_t s, const unsigned *gate) {
   if (nelem <= 0) return;
   const size_t smem = sizeof(ds) * 12 * (size_t) max_nax * (LCH / 32);
-  const int grid = (nelem + LCH / 32 - 1) / (LCH / 32);
+  const int grid = persistent_grid((const void *) k_lines, LCH, smem, (long long) nelem * 32);
   k_lines<<<grid, LCH, smem, s>>>(node_hl, etype, lat, mask, mask_near, eflags, maxlines, pg,
                                   nelem, max_nax, line_pos, gate);
   check(cudaGetLastError(), "lines");
@@ -2080,8 +2082,9 @@ void row_q(const int *row_elem, const int *row_jj, const int *etype, const int *
            const float2 *spa_int_hl, const float2 *node_hl, int nrows, const PackGrid &pg,
            float4 *ip_q, float4 *ip_h, float4 *ip_l, cudaStream_t s, const unsigned *gate) {
   if (nrows <= 0) return;
-  k_row_q<<<nblk(nrows, 128), 128, 0, s>>>(row_elem, row_jj, etype, int_off, spa_int_hl, node_hl,
-                                          nrows, pg, ip_q, ip_h, ip_l, gate);
+  const int grid = persistent_grid((const void *) k_row_q, 128, 0, nrows);
+  k_row_q<<<grid, 128, 0, s>>>(row_elem, row_jj, etype, int_off, spa_int_hl, node_hl, nrows, pg,
+                               ip_q, ip_h, ip_l, gate);
   check(cudaGetLastError(), "row_q");
 }
 

@@ -6,7 +6,7 @@
 //                ideal node positions, then the 8 nodal densities, normalised
 //                and rounded to bf16 [n][64] (zero padded) for the GEMMs;
 //   due       -> the far elements tested this step: an element whose spread
-//                exceeded the threshold is re-tested after 1, 3, 7, then 15
+//                exceeded the threshold is re-tested after 1, 3, 7, ... 127
 //                steps (the quadrature evaluates it meanwhile); an accepted
 //                element is tested every step.  The list is compacted on the
 //                device, with its length in a device counter;
@@ -16,6 +16,8 @@
 //                quadrature's nodal gather (which skipped their force rows).
 // The reference has no counterpart: it evaluates every element by quadrature.
 #include <cuda_bf16.h>
+
+#include <algorithm>
 
 #include "internal.h"
 
@@ -116,14 +118,17 @@ __global__ void k_accept(const float *__restrict__ spread, const int *__restrict
   }
 }
 
+// a grid-stride loop over the device count (most steps test few elements)
 __global__ void k_write(const float *__restrict__ mean, const int *__restrict__ far,
                         const int *__restrict__ due, const int *__restrict__ count, int nfar,
                         const unsigned char *__restrict__ skip, double *__restrict__ nodef) {
-  long i = blockIdx.x * (long) blockDim.x + threadIdx.x;
-  if (i >= (long) (count ? *count : nfar) * MLP_OUT) return;
-  int r = (int) (i / MLP_OUT), c = (int) (i % MLP_OUT);
-  int e = far[due ? due[r] : r];
-  if (skip[e]) nodef[(size_t) MLP_OUT * e + c] = (double) mean[i];
+  const long n = (long) (count ? *count : nfar) * MLP_OUT;
+  for (long i = blockIdx.x * (long) blockDim.x + threadIdx.x; i < n;
+       i += (long) gridDim.x * blockDim.x) {
+    const int r = (int) (i / MLP_OUT), c = (int) (i % MLP_OUT);
+    const int e = far[due ? due[r] : r];
+    if (skip[e]) nodef[(size_t) MLP_OUT * e + c] = (double) mean[i];
+  }
 }
 
 __global__ void k_gather_far(const int *__restrict__ far, const int *__restrict__ due,
@@ -174,7 +179,11 @@ void accept(const float *spread, const int *far, const int *due_list, const int 
 void write_forces(const float *mean, const int *far, const int *due_list, const int *count,
                   int nfar, const unsigned char *skip, double *nodef, cudaStream_t s) {
   if (nfar <= 0) return;
-  k_write<<<nblk((long long) nfar * MLP_OUT, 256), 256, 0, s>>>(mean, far, due_list, count, nfar,
+  int dev = 0, nsm = 0;
+  check(cudaGetDevice(&dev), "device");
+  check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "sm count");
+  const int grid = std::min(nblk((long long) nfar * MLP_OUT, 256), 8 * nsm);
+  k_write<<<grid, 256, 0, s>>>(mean, far, due_list, count, nfar,
                                                                  skip, nodef);
   check(cudaGetLastError(), "surrogate write");
 }
