@@ -256,15 +256,24 @@ __device__ __forceinline__ int cull_part(float rsq, const float4 &lim) {
 // longer than REORDER_CAP classify again in the second sweep.
 constexpr int REORDER_CAP = 256;
 
-template <class Index, class Rsq, class Put>
-__device__ __forceinline__ int4 reorder_parts(int n, const float4 &lim, Index index, Rsq rsq,
-                                              Put put) {
+// The first sweep keeps the list index two entries ahead and the fetched
+// data of the next entry in flight (fetch(entry) -> what rsq needs), so
+// that no gather waits on a list load issued in the same iteration.
+template <class Index, class Fetch, class Rsq, class Put>
+__device__ __forceinline__ int4 reorder_parts(int n, const float4 &lim, Index index, Fetch fetch,
+                                              Rsq rsq, Put put) {
   unsigned codes[REORDER_CAP / 8];
   const bool keep = n <= REORDER_CAP;
   int c[4] = {0, 0, 0, 0};
   unsigned word = 0u;
+  int en = n > 0 ? index(0) : 0, enn = n > 1 ? index(1) : 0;
+  auto fn = fetch(en);
   for (int k = 0; k < n; k++) {
-    const int p = cull_part(rsq(index(k)), lim);
+    const auto fk = fn;
+    en = enn;
+    if (k + 2 < n) enn = index(k + 2);
+    if (k + 1 < n) fn = fetch(en);
+    const int p = cull_part(rsq(fk), lim);
     if (p < 4) c[p]++;
     if (keep) {
       word |= (unsigned) p << (4 * (k & 7));
@@ -283,7 +292,7 @@ __device__ __forceinline__ int4 reorder_parts(int n, const float4 &lim, Index in
       if ((k & 7) == 0) word = codes[k >> 3];
       p = (int) ((word >> (4 * (k & 7))) & 15u);
     } else {
-      p = cull_part(rsq(e), lim);
+      p = cull_part(rsq(fetch(e)), lim);
     }
     put(m[p]++, e);
   }
@@ -376,13 +385,14 @@ __global__ void k_list_partition(const float4 *__restrict__ xq, float g, const i
     float cx, cy, cz;
     cell_of(qi, cx, cy, cz);
     auto index = [&](int k) { return __ldg(list + (size_t) k * stride + i); };
-    auto rsq = [&](int j) {
+    auto fetch = [&](int j) { return __ldg(xq + j); };
+    auto rsq = [&](const float4 &qj) {
       float dx, dy, dz;
-      rel_vec(qi, cx, cy, cz, __ldg(xq + j), g, dx, dy, dz);
+      rel_vec(qi, cx, cy, cz, qj, g, dx, dy, dz);
       return dx * dx + dy * dy + dz * dz;
     };
     auto put = [&](int at, int j) { out[(size_t) at * stride + i] = j; };
-    nnear[i] = reorder_parts(num[i], lim, index, rsq, put);
+    nnear[i] = reorder_parts(num[i], lim, index, fetch, rsq, put);
   }
 }
 
@@ -1198,7 +1208,8 @@ __global__ void k_ip_reorder(const int *__restrict__ row_start, const int *__res
       return dx * dx + dy * dy + dz * dz;
     };
     auto put = [&](int at, int code) { ent_near[s0 + at] = code; };
-    nnear_row[r] = reorder_parts(row_start[r + 1] - s0, lim, index, rsq, put);
+    auto fetch = [&](int code) { return code; };
+    nnear_row[r] = reorder_parts(row_start[r + 1] - s0, lim, index, fetch, rsq, put);
   }
   for (long long t = blockIdx.x * blockDim.x + threadIdx.x; t < nvals; t += stride)
     node_ref[t] = node_hl[t];
@@ -2217,6 +2228,7 @@ void elem_fused(const MixedElems &m, const FusedTables &t, int pass, const float
   if (t.variant == 1) launch_fused<1>(a, pass, tab, e, table, lj1, lj2, erho_in, erho_out, nodef, s);
   else if (t.variant == 2)
     launch_fused<2>(a, pass, tab, e, table, lj1, lj2, erho_in, erho_out, nodef, s);
+
   else launch_fused<0>(a, pass, tab, e, table, lj1, lj2, erho_in, erho_out, nodef, s);
   check(cudaGetLastError(), "elem_fused");
 }
