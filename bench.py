@@ -730,10 +730,11 @@ def run_ours(a, ws, rank, local):
         t0 = time.perf_counter()
         c4 = B.run_batch(eam, n=256, steps=a.c4_steps, seed=4, tune=True, device=local)
         c4["wall_s_with_setup_and_tuning"] = round(time.perf_counter() - t0, 1)
-        c4["note"] = ("per class one handle (replicas side by side), its steps in device-loop "
-                      "graph launches (rebuild decision on the device; a launch ends only at a "
-                      "rebuild); the classes concurrently on their own streams; site_steps_per_s "
-                      "= all classes' site-steps over the wall time of the timed run")
+        c4["note"] = ("per class one handle (replicas side by side); every class's step loop "
+                      "is a branch of one CUDA graph (rebuild decisions on the device), one "
+                      "launch runs all classes until each is done or needs a rebuild, which the "
+                      "host performs before the next launch; site_steps_per_s = all classes' "
+                      "site-steps over the wall time of the timed run")
 
     if rank == 0:
         line = {

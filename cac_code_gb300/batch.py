@@ -11,10 +11,13 @@ list ever crosses from one replica into another.  Every kernel of a step then
 covers all replicas of the class at once.
 
 Each class runs its steps through the device step loop ("tune loop device"):
-one CUDA graph launch runs step after step, the rebuild decision
-(Neighbor::decide, neighbor.cpp:1150-1163) taken on the device, and returns to
-the host only for a step that needs a rebuild.  The classes run at the same
-time, each handle on its own stream driven by its own host thread.
+step after step inside a CUDA graph, the rebuild decision (Neighbor::decide,
+neighbor.cpp:1150-1163) taken on the device, back to the host only for a step
+that needs a rebuild.  All classes' loops are the branches of one graph
+(cacg_run_batch): one launch runs every replica until each class is done or
+needs a rebuild; the host performs those rebuilds and launches again.  (The
+alternatives: each handle's loop from its own host thread, or one class after
+another.)
 
 The nodes are damped (fix viscous): under the reference's element force the
 elements of these slabs gain kinetic energy without bound over some hundreds
@@ -281,12 +284,14 @@ def _run_class(c: _Class, steps: int) -> None:
 
 def run_batch(eam_file: str, n: int = 256, steps: int = 2000, seed: int = 4, tune: bool = True,
               device: int = 0, mode: int = cacg.MIXED, loop: str = "device",
-              concurrent: bool = True) -> Dict:
+              schedule: str = "graph") -> Dict:
     """All replicas: the classes prepared (and autotuned) one after another,
-    then timed together, each class's steps on its own stream from its own
-    host thread (concurrent=False: one class after another).  Returns
-    per-class and whole-batch site-steps/s; the whole batch's is the total
-    site-steps over the wall time of the timed run."""
+    then timed together: schedule "graph" runs every class's loop as a branch
+    of one CUDA graph (cacg_run_batch), "threads" each class from its own host
+    thread on its own stream, "sequential" one class after another.  Returns
+    per-class counts and the whole batch's site-steps/s (the total site-steps
+    over the wall time of the timed run; per class also site-steps/s over its
+    own run where the class runs alone)."""
     reps = draw_replicas(n, seed)
     groups: Dict[Tuple[str, int], List[Replica]] = {}
     for r in reps:
@@ -296,7 +301,14 @@ def run_batch(eam_file: str, n: int = 256, steps: int = 2000, seed: int = 4, tun
         for (pair, k), rs in sorted(groups.items()):
             classes.append(_prepare_class(pair, k, rs, eam_file, device, mode, tune, loop))
         t0 = time.perf_counter()
-        if concurrent:
+        if schedule == "graph":
+            for c in classes:
+                c.c0 = c.system.counts()
+            cacg.run_batch([c.system for c in classes], steps)
+            for c in classes:
+                c.c1 = c.system.counts()
+                c.ms = float("nan")
+        elif schedule == "threads":
             threads = [threading.Thread(target=_run_class, args=(c, steps)) for c in classes]
             for t in threads:
                 t.start()
@@ -315,8 +327,9 @@ def run_batch(eam_file: str, n: int = 256, steps: int = 2000, seed: int = 4, tun
             out.append({"pair": c.pair, "size_class": list(SIZE_CLASSES[c.k][:2]),
                         "replicas": len(c.reps), "sites": c.sites, "atoms": c.atoms,
                         "elements": c.elements, "cross_section_periods": SIZE_CLASSES[c.k][2],
-                        "steps": steps, "ms": c.ms, "wall_s": round(c.wall_s, 3),
-                        "site_steps_per_s": c.sites * steps / (c.ms * 1e-3),
+                        "steps": steps, "ms": c.ms if schedule != "graph" else None,
+                        "site_steps_per_s": (c.sites * steps / (c.ms * 1e-3)
+                                             if schedule != "graph" else None),
                         "graph_steps": c1["graph_steps"] - c0["graph_steps"],
                         "rebuilds": c1["rebuilds"] - c0["rebuilds"],
                         "loop_launches": c1["loop_launches"] - c0["loop_launches"],
@@ -326,8 +339,7 @@ def run_batch(eam_file: str, n: int = 256, steps: int = 2000, seed: int = 4, tun
         return {"replicas": n, "classes": out, "steps": steps,
                 "total_sites": int(sum(c.sites for c in classes)),
                 "site_steps_per_s": tot / wall, "wall_s": round(wall, 3),
-                "concurrent": concurrent, "loop": loop,
-                "sum_of_class_ms": round(sum(c.ms for c in classes), 1)}
+                "schedule": schedule, "loop": loop}
     finally:
         for c in classes:
             c.system.close()

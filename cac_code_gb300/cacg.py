@@ -53,6 +53,7 @@ EXPORTED = [
     "cacg_surrogate_attach", "cacg_compute_centro", "cacg_dump_xyz", "cacg_dump_elements",
     "cacg_fix_post_force", "cacg_get_box", "cacg_set_graphs", "cacg_set_group",
     "cacg_run_host", "cacg_get_kernel_timing", "cacg_set_lj", "cacg_set_eam",
+    "cacg_run_batch",
 ]
 
 
@@ -88,6 +89,7 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
     lib.cacg_command.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
     lib.cacg_file.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
     lib.cacg_run.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.cacg_run_batch.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int]
     lib.cacg_run_host.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _dp, _dp]
     lib.cacg_set_precision.argtypes = [ctypes.c_void_p, ctypes.c_int]
     lib.cacg_set_timing.argtypes = [ctypes.c_void_p, ctypes.c_int]
@@ -517,3 +519,20 @@ class System:
         v = ctypes.c_double()
         self._ok(self._L.cacg_measure_fp64_peak(self.h, ctypes.byref(v)))
         return v.value
+
+
+def run_batch(systems, n: int) -> None:
+    """n steps on every System of `systems` (one device, "tune loop device")
+    as the branches of one CUDA graph (cacg_run_batch); a failure raises the
+    error of the handle that met it."""
+    if not systems:
+        return
+    L = systems[0]._L
+    arr = (ctypes.c_void_p * len(systems))(*[s.h.value for s in systems])
+    rc = L.cacg_run_batch(arr, len(systems), n)
+    if rc != 0:
+        for s in systems:
+            msg = L.cacg_error(s.h).decode()
+            if msg:
+                raise CacgError(rc, msg)
+        raise CacgError(rc, "cacg_run_batch failed")

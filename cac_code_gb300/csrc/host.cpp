@@ -421,7 +421,11 @@ struct cacg_context {
     eager_since = 0;
   }
   bool capture_plain_step();
+  void loop_prepare();
+  bool add_loop(cudaGraph_t top, long long &pre, long long &post, bool *destroyable);
   bool capture_loop();
+  void loop_arm(int want);
+  int loop_finish(int want, long long pre, long long post);
   int run_loop(int n);
   std::vector<cudaEvent_t> pev;  // per-step phase events
   // with timing on: events around the main kernels of each step; kernel k of
@@ -3789,28 +3793,29 @@ void cacg_context::run_host(int n, double *x, double *v, double *nodex, double *
 // both conditions.  Anything that would allocate or synchronise ends a
 // capture with an error; the steps then run the host way and the device loop
 // stays off for this handle.
-bool cacg_context::capture_loop() {
-  upload_masks();  // host-to-device copies stay outside the capture
+// Prepares the handle for a loop capture: masks uploaded, the loop state and
+// the second chain's stream allocated (nothing of this may happen inside a
+// capture).
+void cacg_context::loop_prepare() {
+  upload_masks();
   d_loop.ensure(LOOP_SLOTS, stream);
-  if (!astream && fork_ok()) {  // the second chain's stream exists before the capture
+  if (!astream && fork_ok()) {
     int least = 0, greatest = 0;
     check(cudaDeviceGetStreamPriorityRange(&least, &greatest), "stream priorities");
     check(cudaStreamCreateWithPriority(&astream, cudaStreamNonBlocking, greatest), "atom stream");
   }
-  const unsigned long long e0 = dbuf_epoch();
+}
+
+// Adds this handle's step loop to `top` as one WHILE node (see capture_loop);
+// pre / post: the kernels of an iteration before and after the decision.  A
+// capture into a conditional body that ends invalidated may leave that body
+// released by the runtime while its node still refers to it: *destroyable is
+// then cleared and the caller leaves the whole graph alone.
+bool cacg_context::add_loop(cudaGraph_t top, long long &pre, long long &post, bool *destroyable) {
   const long long l0 = launches;
-  cudaGraph_t top = nullptr;
-  cudaGraphExec_t ex = nullptr;
   cudaGraphConditionalHandle again = 0, proceed = 0;
   cudaGraph_t body = nullptr, then = nullptr;
-  long long pre = 0, post = 0;
-  // a capture into a conditional body that ends invalidated may leave that
-  // body released by the runtime while its node still refers to it: the
-  // whole graph is then left alone (not destroyed), once, as the device loop
-  // goes off for the handle
-  bool destroyable = true;
-  bool ok = cudaGraphCreate(&top, 0) == cudaSuccess &&
-            cudaGraphConditionalHandleCreate(&again, top, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+  bool ok = cudaGraphConditionalHandleCreate(&again, top, 1, cudaGraphCondAssignDefault) == cudaSuccess;
   if (ok) {
     cudaGraphNodeParams p = {};
     p.type = cudaGraphNodeTypeConditional;
@@ -3853,7 +3858,7 @@ bool cacg_context::capture_loop() {
       ok = false;
     }
     cudaGraph_t g = nullptr;
-    if (cudaStreamEndCapture(stream, &g) != cudaSuccess) ok = destroyable = false;
+    if (cudaStreamEndCapture(stream, &g) != cudaSuccess) ok = *destroyable = false;
     pre = launches - l0;
     if (ok) {
       cudaGraphNodeParams p = {};
@@ -3898,17 +3903,36 @@ bool cacg_context::capture_loop() {
       ok = false;
     }
     cudaGraph_t g = nullptr;
-    if (cudaStreamEndCapture(stream, &g) != cudaSuccess) ok = destroyable = false;
+    if (cudaStreamEndCapture(stream, &g) != cudaSuccess) ok = *destroyable = false;
     post = launches - l1;
   } else {
     ok = false;
   }
   capturing = false;
+  launches = l0;
+  cudaGetLastError();  // a failed capture leaves its error behind
+  return ok;
+}
+
+// The device step loop: a WHILE node whose body is a step's initial
+// integration, the gated distance check and the decision kernel, then an IF
+// node around the step's communication, force passes, post-force fixes and
+// final integration (the body of a plain step).  The decision kernel sets
+// both conditions.  Anything that would allocate or synchronise ends a
+// capture with an error; the steps then run the host way and the device loop
+// stays off for this handle.
+bool cacg_context::capture_loop() {
+  loop_prepare();
+  const unsigned long long e0 = dbuf_epoch();
+  cudaGraph_t top = nullptr;
+  cudaGraphExec_t ex = nullptr;
+  long long pre = 0, post = 0;
+  bool destroyable = true;
+  bool ok = cudaGraphCreate(&top, 0) == cudaSuccess && add_loop(top, pre, post, &destroyable);
   if (ok && dbuf_epoch() != e0) ok = false;
   if (ok && cudaGraphInstantiate(&ex, top, 0) != cudaSuccess) ok = false;
   if (top && destroyable) cudaGraphDestroy(top);
-  cudaGetLastError();  // a failed capture leaves its error behind
-  launches = l0;
+  cudaGetLastError();
   if (!ok) {
     if (ex) cudaGraphExecDestroy(ex);
     loop_device = false;
@@ -3921,6 +3945,43 @@ bool cacg_context::capture_loop() {
   lgraph_epoch = e0;
   lgraph_valid = true;
   return true;
+}
+
+// The loop state of a launch that wanted `want` steps, into the pinned slots
+// (before the launch), and its outcome (after it): the steps done are
+// accounted, and a step that needs a rebuild is rebuilt and finished here.
+// Returns the steps taken, that one included.
+void cacg_context::loop_arm(int want) {
+  int *hl = h_pin + 16;
+  hl[LOOP_AGO] = ago;
+  hl[LOOP_DONE] = 0;
+  hl[LOOP_WANT] = want;
+  hl[LOOP_PENDING] = 0;
+  hl[LOOP_ITERS] = 0;
+  hl[LOOP_BITS] = 0;
+}
+
+int cacg_context::loop_finish(int want, long long pre, long long post) {
+  const int *hl = h_pin + 16;
+  loop_launches++;
+  const int steps = hl[LOOP_DONE], iters = hl[LOOP_ITERS], flags = hl[LOOP_PENDING];
+  if (steps < 0 || steps > want || iters < steps || iters > steps + 1)
+    fail(CACG_ECUDA, "device step loop: %d steps in %d iterations of %d wanted", steps, iters, want);
+  ago = hl[LOOP_AGO];
+  ntimestep += steps;
+  graph_steps += steps;
+  launches += pre * iters + post * steps;
+  if (flags) {  // the step after those: initial integration and decision done
+    ntimestep++;
+    cur_step = (size_t) steps;
+    rebuild(flags);
+    force_passes(-1);
+    post_force();
+    nve_final();
+    return steps + 1;
+  }
+  if (steps == 0) fail(CACG_ECUDA, "device step loop made no progress");
+  return steps;
 }
 
 // Up to n steps through the device loop; returns the steps taken.  Each
@@ -3937,37 +3998,12 @@ int cacg_context::run_loop(int n) {
     if (!lgraph_valid || lgraph_epoch != dbuf_epoch()) {
       if (eager_since < 1 || !capture_loop()) return done;
     }
-    hl[LOOP_AGO] = ago;
-    hl[LOOP_DONE] = 0;
-    hl[LOOP_WANT] = n - done;
-    hl[LOOP_PENDING] = 0;
-    hl[LOOP_ITERS] = 0;
-    hl[LOOP_BITS] = 0;
+    loop_arm(n - done);
     check(cudaMemcpyAsync(d_loop.p, hl, LOOP_SLOTS * sizeof(int), cudaMemcpyHostToDevice, stream), "loop in");
     check(cudaGraphLaunch(lexec, stream), "loop launch");
     check(cudaMemcpyAsync(hl, d_loop.p, LOOP_SLOTS * sizeof(int), cudaMemcpyDeviceToHost, stream), "loop out");
     sync();
-    loop_launches++;
-    const int steps = hl[LOOP_DONE], iters = hl[LOOP_ITERS], flags = hl[LOOP_PENDING];
-    if (steps < 0 || steps > n - done || iters < steps || iters > steps + 1)
-      fail(CACG_ECUDA, "device step loop: %d steps in %d iterations of %d wanted", steps, iters,
-           n - done);
-    ago = hl[LOOP_AGO];
-    done += steps;
-    ntimestep += steps;
-    graph_steps += steps;
-    launches += lgraph_pre * iters + lgraph_post * steps;
-    if (flags) {  // the step after those: initial integration and decision done
-      ntimestep++;
-      cur_step = (size_t) done;
-      rebuild(flags);
-      force_passes(-1);
-      post_force();
-      nve_final();
-      done++;
-    } else if (steps == 0) {
-      fail(CACG_ECUDA, "device step loop made no progress");
-    }
+    done += loop_finish(n - done, lgraph_pre, lgraph_post);
   }
   return done;
 }
@@ -4324,6 +4360,102 @@ int cacg_run(cacg_handle h, int nsteps) {
   API_BEGIN
   h->run(nsteps);
   API_END
+}
+
+// Several handles' step loops as the branches of one CUDA graph: each launch
+// runs every handle until its wanted steps are done or it needs a rebuild;
+// the host performs those rebuilds (then one eager step each, so that the
+// next capture holds no first-call work), captures again and relaunches.  An
+// error is reported on the handle whose call raised it (its cacg_error); the
+// other handles keep the steps they completed.
+int cacg_run_batch(cacg_handle *hs, int nh, int nsteps) {
+  if (!hs || nh < 1 || nsteps < 0) return CACG_EINVAL;
+  for (int k = 0; k < nh; k++)
+    if (!hs[k] || hs[k]->device != hs[0]->device) return CACG_EINVAL;
+  for (int k = 0; k < nh; k++) hs[k]->err.clear();  // only the failing handle reports
+  cacg_handle cur = hs[0];
+  try {
+    check(cudaSetDevice(hs[0]->device), "cudaSetDevice");
+    std::vector<int> left(nh, nsteps);
+    for (int k = 0; k < nh; k++) {
+      cur = hs[k];
+      EpochScope es(&cur->epoch);
+      if (!cur->loop_device || !cur->use_graphs || !cur->graph_ok || cur->deform_on)
+        fail(CACG_ESTATE, "run_batch takes handles with the device loop on (tune loop device), "
+                          "graphs on and no box deformation");
+      cur->run(0);  // set-up and lists, as a run starts
+    }
+    while (true) {
+      std::vector<int> in;
+      for (int k = 0; k < nh; k++) {
+        cur = hs[k];
+        EpochScope es(&cur->epoch);
+        while (left[k] > 0 && cur->eager_since < 1) {  // first-call work outside the capture
+          cur->run(1);
+          left[k]--;
+        }
+        if (left[k] > 0) in.push_back(k);
+      }
+      if (in.empty()) break;
+      cudaGraph_t top = nullptr;
+      cudaGraphExec_t ex = nullptr;
+      check(cudaGraphCreate(&top, 0), "batch graph");
+      std::vector<long long> pre(nh, 0), post(nh, 0);
+      std::vector<unsigned long long> e0(nh, 0);
+      bool ok = true, destroyable = true;
+      for (int k : in) {
+        cur = hs[k];
+        EpochScope es(&cur->epoch);
+        cur->loop_prepare();
+        e0[k] = dbuf_epoch();
+        if (!cur->add_loop(top, pre[k], post[k], &destroyable)) {
+          ok = false;
+          break;
+        }
+      }
+      for (int k : in) {
+        EpochScope es(&hs[k]->epoch);
+        if (dbuf_epoch() != e0[k]) ok = false;
+      }
+      if (ok && cudaGraphInstantiate(&ex, top, 0) != cudaSuccess) ok = false;
+      if (destroyable) cudaGraphDestroy(top);
+      cudaGetLastError();
+      if (!ok) {
+        if (ex) cudaGraphExecDestroy(ex);
+        fail(CACG_ECUDA, "run_batch: the combined step graph could not be built");
+      }
+      const cudaStream_t s0 = hs[in[0]]->stream;
+      for (int k : in) {
+        cur = hs[k];
+        check(cudaStreamSynchronize(cur->stream), "batch in");  // the handle's own work first
+        cur->loop_arm(left[k]);
+        check(cudaMemcpyAsync(cur->d_loop.p, cur->h_pin + 16, LOOP_SLOTS * sizeof(int),
+                              cudaMemcpyHostToDevice, s0), "batch loop in");
+      }
+      cur = hs[in[0]];
+      const cudaError_t le = cudaGraphLaunch(ex, s0);
+      for (int k : in)
+        if (le == cudaSuccess)
+          check(cudaMemcpyAsync(hs[k]->h_pin + 16, hs[k]->d_loop.p, LOOP_SLOTS * sizeof(int),
+                                cudaMemcpyDeviceToHost, s0), "batch loop out");
+      const cudaError_t se = cudaStreamSynchronize(s0);
+      cudaGraphExecDestroy(ex);
+      check(le, "batch launch");
+      check(se, "batch sync");
+      for (int k : in) {
+        cur = hs[k];
+        EpochScope es(&cur->epoch);
+        left[k] -= cur->loop_finish(left[k], pre[k], post[k]);
+      }
+    }
+    return CACG_OK;
+  } catch (const ApiError &e) {
+    cur->err = e.msg;
+    return e.code;
+  } catch (const CudaError &e) {
+    cur->err = std::string(e.where) + ": " + cudaGetErrorString(e.code);
+    return e.code == cudaErrorMemoryAllocation ? CACG_ENOMEM : CACG_ECUDA;
+  }
 }
 
 int cacg_run_host(cacg_handle h, int nsteps, double *x, double *v, double *nodex, double *nodev) {

@@ -103,6 +103,12 @@ int cacg_fix_nve_final_integrate(cacg_handle h);
 
 /* ---- Verlet::run, verlet.cpp:149-219 (atoms also get Pair::compute) ---- */
 int cacg_run(cacg_handle h, int nsteps);
+/* nsteps Verlet steps on each of nh handles (one device, "tune loop device",
+   graphs on, no deformation) as the branches of one CUDA graph: a launch runs
+   every handle until its steps are done or it needs a rebuild, which the host
+   then performs before the next launch (Verlet::run, verlet.cpp:149-219, for
+   independent systems at once).  Results equal cacg_run on each handle. */
+int cacg_run_batch(cacg_handle *hs, int nh, int nsteps);
 
 /* ---- host-owned state in (drop-in callers keep Atom::x/v and Element::nodex/nodev,
    atom.h:40, element.h:25, in host memory and push them every step) ---- */

@@ -82,9 +82,9 @@ def test_small_batched_run_with_autotuner(cacg_lib):
     from cac_code_gb300 import workloads as W
     eam = W.write_eam(os.path.join(tempfile.gettempdir(), "cacg_batch_Cu2000.eam"))
     res = B.run_batch(eam, n=6, steps=30, seed=7, tune=True)
-    assert res["replicas"] == 6 and len(res["classes"]) >= 2 and res["concurrent"]
+    assert res["replicas"] == 6 and len(res["classes"]) >= 2 and res["schedule"] == "graph"
+    assert np.isfinite(res["site_steps_per_s"]) and res["site_steps_per_s"] > 0
     for c in res["classes"]:
-        assert np.isfinite(c["site_steps_per_s"]) and c["site_steps_per_s"] > 0
         # every step but the rebuilds and the eager step after each ran inside
         # a device-loop graph launch, and no rebuild decision was taken on the host
         assert c["graph_steps"] >= 30 - 2 * c["rebuilds"] - 1
@@ -94,12 +94,12 @@ def test_small_batched_run_with_autotuner(cacg_lib):
 
 
 @pytest.mark.gpu
-def test_concurrent_classes_match_one_after_another(cacg_lib):
-    """The classes run from their own threads on their own streams give the
-    same per-class results as the same classes run one after another."""
+def test_schedules_agree(cacg_lib):
+    """One graph for all classes, one host thread per class, and one class
+    after another give the same per-class rebuilds and steps."""
     from cac_code_gb300 import workloads as W
     eam = W.write_eam(os.path.join(tempfile.gettempdir(), "cacg_batch_Cu2000.eam"))
-    a = B.run_batch(eam, n=6, steps=40, seed=7, tune=False, concurrent=True)
-    b = B.run_batch(eam, n=6, steps=40, seed=7, tune=False, concurrent=False)
-    for ca, cb in zip(a["classes"], b["classes"]):
-        assert (ca["pair"], ca["sites"], ca["rebuilds"]) == (cb["pair"], cb["sites"], cb["rebuilds"])
+    runs = [B.run_batch(eam, n=6, steps=40, seed=7, tune=False, schedule=sch)
+            for sch in ("graph", "threads", "sequential")]
+    for cs in zip(*(r["classes"] for r in runs)):
+        assert len({(c["pair"], c["sites"], c["rebuilds"]) for c in cs}) == 1

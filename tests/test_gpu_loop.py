@@ -95,3 +95,50 @@ def test_device_loop_c1_full(cacg_lib):
     assert dev[2]["rebuilds"] == host[2]["rebuilds"] == 5
     assert dev[2]["loop_launches"] == 5
     assert dev[2]["graph_steps"] == 40
+
+
+def test_batch_graph_equals_separate_runs(cacg_lib):
+    """cacg_run_batch: several handles' step loops as branches of one CUDA
+    graph give the same trajectories, bit for bit, as each handle's own run,
+    across rebuilds (handed to the host) and with post-force fixes."""
+    from gpu_runner import configure
+    names = ["eam_cac", "lj_cac_fixes", "lj_cac"]
+    cases = []
+    for nm in names:
+        cfg, z = C.load_golden(nm)
+        cases.append((dict(cfg, every=3, check=True), C.model_from_arrays(z)))
+
+    def make():
+        out = []
+        for cfg, m in cases:
+            s = cacg_lib.System(0)
+            configure(s, cfg, m)
+            s.set_precision(cacg_lib.MIXED)
+            s.command("tune loop device")
+            s.init()
+            s.setup()
+            s.neighbor_build()
+            s.pair_compute()
+            if m.nelements:
+                s.neighbor_ebuild()
+                s.neighbor_nbuild()
+                s.pair_ecompute()
+            out.append(s)
+        return out
+
+    alone, batch = make(), make()
+    try:
+        for s in alone:
+            s.run(45)
+        cacg_lib.run_batch(batch, 45)
+        for a, b in zip(alone, batch):
+            ca, cb = a.counts(), b.counts()
+            assert ca["step"] == cb["step"] and ca["rebuilds"] == cb["rebuilds"]
+            assert cb["host_decisions"] == 0
+            for k in ("x", "v", "f"):
+                assert np.array_equal(a.atoms()[k], b.atoms()[k]), k
+            for k in ("nodex", "nodev", "nodef"):
+                assert np.array_equal(a.elements()[k], b.elements()[k]), k
+    finally:
+        for s in alone + batch:
+            s.close()
