@@ -4365,9 +4365,10 @@ int cacg_run(cacg_handle h, int nsteps) {
 // Several handles' step loops as the branches of one CUDA graph: each launch
 // runs every handle until its wanted steps are done or it needs a rebuild;
 // the host performs those rebuilds (then one eager step each, so that the
-// next capture holds no first-call work), captures again and relaunches.  An
-// error is reported on the handle whose call raised it (its cacg_error); the
-// other handles keep the steps they completed.
+// next capture holds no first-call work), captures again and relaunches.
+// Where the combined graph cannot be built, each handle runs its remaining
+// steps on its own.  An error is reported on the handle whose call raised it
+// (its cacg_error); the other handles keep the steps they completed.
 int cacg_run_batch(cacg_handle *hs, int nh, int nsteps) {
   if (!hs || nh < 1 || nsteps < 0) return CACG_EINVAL;
   for (int k = 0; k < nh; k++)
@@ -4420,9 +4421,15 @@ int cacg_run_batch(cacg_handle *hs, int nh, int nsteps) {
       if (ok && cudaGraphInstantiate(&ex, top, 0) != cudaSuccess) ok = false;
       if (destroyable) cudaGraphDestroy(top);
       cudaGetLastError();
-      if (!ok) {
+      if (!ok) {  // each handle finishes its steps on its own
         if (ex) cudaGraphExecDestroy(ex);
-        fail(CACG_ECUDA, "run_batch: the combined step graph could not be built");
+        for (int k : in) {
+          cur = hs[k];
+          EpochScope es(&cur->epoch);
+          cur->run(left[k]);
+          left[k] = 0;
+        }
+        break;
       }
       const cudaStream_t s0 = hs[in[0]]->stream;
       for (int k : in) {
