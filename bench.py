@@ -92,7 +92,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-modes", action="store_true", help="skip timing the other precision modes")
-    p.add_argument("--study", choices=["strain", "drift", "surrogate"],
+    p.add_argument("--study", choices=["strain", "drift", "surrogate", "c1"],
                    help="a longer measurement instead of the benchmark (one JSON line)")
     p.add_argument("--study-steps", type=int, default=0, help="steps of a study (0: its default)")
     return p.parse_args()
@@ -938,6 +938,43 @@ def study_strain(a):
     print(json.dumps(out), flush=True)
 
 
+def study_c1(a):
+    """C1 in full (LJ, 16,384 atoms + 64 elements) on the GPU in every
+    precision mode: 200 steps (the reference's algorithm stops at step 260,
+    when the growing elements' bin grid no longer holds the atoms), after 10
+    warm-up steps, site-steps/s from CUDA events; the bit-exact mode computes
+    what the reference computes, bit for bit."""
+    from cac_code_gb300 import build, cacg
+    from cac_code_gb300 import workloads as W
+    build.build_library()
+    m, cfg = W.c1_lj()
+    sites = W.metric_sites(m, cfg)
+    steps = a.study_steps or 200
+    out = {"study": "c1", "workload": "C1: LJ, 16,384 atoms + 64 elements of 8 sites per edge, "
+                                      "T* = 0.1, dt = 0.005, neighbor 2.8 bin, every 10 check yes",
+           "sites": sites, "steps": steps, "modes": {}}
+    for name, mode in (("exact", cacg.FP64_EXACT), ("fp64", cacg.FP64), ("mixed", cacg.MIXED)):
+        s = cacg.System(0)
+        try:
+            W.configure_system(s, m, cfg)
+            s.set_precision(mode)
+            s.command("tune loop device")
+            s.init()
+            s.setup()
+            s.neighbor_build()
+            s.neighbor_ebuild()
+            s.neighbor_nbuild()
+            s.run(10)
+            s.run(steps - 10)
+            ms = float(s.timing()[0])
+            c = s.counts()
+            out["modes"][name] = {"site_steps_per_s": sites * (steps - 10) / (ms * 1e-3),
+                                  "ms_per_step": ms / (steps - 10), "rebuilds": c["rebuilds"]}
+        finally:
+            s.close()
+    print(json.dumps(out), flush=True)
+
+
 def study_drift(a):
     """Energy of the atom subsystem over NVE steps (atoms and elements do not
     interact, so the atoms alone carry the precision question): the C2 atom
@@ -1027,7 +1064,8 @@ def study_surrogate(a):
 def main():
     a = parse()
     if a.study:
-        {"strain": study_strain, "drift": study_drift, "surrogate": study_surrogate}[a.study](a)
+        {"strain": study_strain, "drift": study_drift, "surrogate": study_surrogate,
+         "c1": study_c1}[a.study](a)
         return
     ws, rank, local = dist_init()
     if a.impl == "reference":
