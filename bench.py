@@ -677,15 +677,20 @@ def run_ours(a, ws, rank, local):
         for _ in range(max(a.warmup, 3)):
             s.run_host(1, hx, hv, hnx, hnv)
         barrier(ws)
+        ce0 = s.counts()
         t0 = time.perf_counter()
         for _ in range(e_steps):
             s.run_host(1, hx, hv, hnx, hnv)
         e_wall = time.perf_counter() - t0
+        ce1 = s.counts()
         e_wall = allmax(ws, e_wall)
         e2e = {"value": ws * sites * e_steps / e_wall, "unit": UNIT,
                "h2d_bytes_per_step": int(hx.nbytes + hv.nbytes + hnx.nbytes + hnv.nbytes),
                "d2h_bytes_per_step": int(hx.nbytes + hv.nbytes + hnx.nbytes + hnv.nbytes),
                "steps": e_steps, "warmup": max(a.warmup, 3),
+               "graph_replays": ce1["graph_steps"] - ce0["graph_steps"],
+               "atom_reorders": ce1["atom_reorders"] - ce0["atom_reorders"],
+               "surrogate_tests": ce1["surrogate_evaluated"] - ce0["surrogate_evaluated"],
                "note": "state round trip per step: x, v of atoms and nodes in and out of "
                        "pinned host buffers through cacg_run_host, one call per step (copies "
                        "overlap the step where the data allow)"}
