@@ -1442,14 +1442,15 @@ struct FusedArgs {
 };
 
 // the trilinear coefficient vectors of the element, m = a, b, c, ab, ac, bc,
-// abc (lanes 0..20), from the double-single nodes: s_k[3 m + d] (kept in
+// abc (lanes 0..20), from the double-single nodes (staged in the warp's shared
+// memory, s_nx[3 k + d]): s_k[3 m + d] (kept in
 // registers), or with by_axis s_k[8 d + m] (read from shared memory as two
 // float4 per axis)
-__device__ __forceinline__ void fused_coeffs(const float2 *__restrict__ node_hl, int e, int lane,
-                                             float *s_k, bool by_axis) {
+__device__ __forceinline__ void fused_coeffs(const float2 *s_nx, int lane, float *s_k,
+                                             bool by_axis) {
   if (lane < 21) {
     const int m = lane / 3, d = lane % 3;
-    const float2 *nx = node_hl + 24 * (size_t) e + d;
+    const float2 *nx = s_nx + d;
     auto X = [&](int k) { return ds{nx[3 * k].x, nx[3 * k].y}; };
     ds v;
     switch (m) {
@@ -1535,8 +1536,8 @@ __device__ __forceinline__ float fprime32_s(float rho, const float4 *s_fp, int n
 // two float4 per axis, then the density coefficients) at every entry, fewer
 // registers; V = 2: as 1, two entries in flight per lane
 template <bool EAM, bool DENSITY, int V>
-__device__ __forceinline__ void fused_row(const FusedArgs &a, const FusedLat &g, int e, int ty,
-                                          int jj, int level, int glane, const float (&k)[21],
+__device__ __forceinline__ void fused_row(const FusedArgs &a, const FusedLat &g, int e, int rfirst,
+                                          int ty, int jj, int level, int glane, const float (&k)[21],
                                           const float (&rk)[8], const float4 *sk4,
                                           const float4 *s_tab, const float4 *s_fp, int nr,
                                           float rdr, float fpi, float lj1, float lj2, bool live,
@@ -1544,7 +1545,7 @@ __device__ __forceinline__ void fused_row(const FusedArgs &a, const FusedLat &g,
   int n = 0, s0 = 0;
   int ip = 0, jp = 0, kp = 0;
   if (live) {
-    const int r = a.row_first[e] + jj;
+    const int r = rfirst + jj;
     s0 = a.row_start[r];
     n = level < 4 ? culled_count(level, a.nnear_row[r], 0) : a.row_start[r + 1] - s0;
     const int4 q = a.intp[a.int_off[ty] + jj];
@@ -1688,8 +1689,12 @@ __device__ __forceinline__ FusedLat fused_lat(const Lattice &lat, int ty) {
 }
 
 // per-warp shared memory: coefficient vectors (21), density coefficients (8),
-// row forces (3 per row of nonzero weight)
-constexpr int FUSED_WARP_FLOATS = 32 + 2 * 3 * FUSED_MAXF;
+// row forces (3 per row of nonzero weight), then the element's staged nodes
+// (24 float2) and nodal densities (8 double)
+constexpr int FUSED_WARP_FLOATS = 32 + 2 * 3 * FUSED_MAXF + 48 + 16;
+constexpr int FUSED_NX_AT = 32 + 2 * 3 * FUSED_MAXF, FUSED_ER_AT = FUSED_NX_AT + 48;
+static_assert(FUSED_NX_AT % 2 == 0 && FUSED_ER_AT % 2 == 0 && FUSED_WARP_FLOATS % 2 == 0,
+              "8-byte alignment of the staged nodes and densities");
 
 // threads per block of each variant (V = 0: coefficients in registers)
 __host__ __device__ constexpr int fused_block(int V) { return V == 0 ? FUSED_BLOCK : 768; }
@@ -1710,10 +1715,28 @@ k_elem_rho_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rdr,
   const int level = a.nnear_row ? cull_level(a.eflags) : 4;
   const int gsub = lane / FG, glane = lane % FG;
   const float rk[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  float2 *s_nx = reinterpret_cast<float2 *>(s_k + FUSED_NX_AT);
+  // the next element's nodes, type and first row are loaded while this
+  // element's rows run
+  float2 pn = make_float2(0.f, 0.f);
+  int pty = 0, prf = 0;
+  if (gw < a.nlocal_e) {
+    if (lane < 24) pn = __ldg(a.node_hl + 24 * (size_t) gw + lane);
+    pty = __ldg(a.etype + gw);
+    prf = __ldg(a.row_first + gw);
+  }
   for (int e = gw; e < a.nlocal_e; e += nw) {
-    const int ty = a.etype[e];
+    const int ty = pty, rfirst = prf;
+    if (lane < 24) s_nx[lane] = pn;
+    const int en = e + nw;
+    if (en < a.nlocal_e) {
+      if (lane < 24) pn = __ldg(a.node_hl + 24 * (size_t) en + lane);
+      pty = __ldg(a.etype + en);
+      prf = __ldg(a.row_first + en);
+    }
     const FusedLat g = fused_lat(a.lat, ty);
-    fused_coeffs(a.node_hl, e, lane, s_k, V != 0);
+    __syncwarp();
+    fused_coeffs(s_nx, lane, s_k, V != 0);
     __syncwarp();
     float k[21];
     if (V == 0) {
@@ -1725,7 +1748,7 @@ k_elem_rho_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rdr,
       const bool live = q < NPE;
       const int jj = live ? a.node_list[ty * NPE + q] : 0;
       dsacc acc, fx, fy, fz;
-      fused_row<true, true, V>(a, g, e, ty, jj, level, glane, k, rk,
+      fused_row<true, true, V>(a, g, e, rfirst, ty, jj, level, glane, k, rk,
                                reinterpret_cast<const float4 *>(s_k), s_tab, nullptr, nr, rdr,
                                0.f, 0.f, 0.f, live, acc, fx, fy, fz);
       if (live && glane == 0) erho[NPE * (size_t) e + q] = acc.value();
@@ -1756,15 +1779,36 @@ k_elem_force_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rd
   const int nw = (int) (((long long) gridDim.x * blockDim.x) >> 5);
   const int level = a.nnear_row ? cull_level(a.eflags) : 4;
   const int gsub = lane / FG, glane = lane % FG;
+  float2 *s_nx = reinterpret_cast<float2 *>(s_k + FUSED_NX_AT);
+  double *s_er = reinterpret_cast<double *>(s_k + FUSED_ER_AT);
+  // the next element's nodes, type and first row are loaded while this
+  // element's rows run
+  float2 pn = make_float2(0.f, 0.f);
+  int pty = 0, prf = 0;
+  if (gw < a.nlocal_e) {
+    if (lane < 24) pn = __ldg(a.node_hl + 24 * (size_t) gw + lane);
+    pty = __ldg(a.etype + gw);
+    prf = __ldg(a.row_first + gw);
+  }
   for (int e = gw; e < a.nlocal_e; e += nw) {
+    const int ty = pty, rfirst = prf;
+    const float2 cn = pn;
+    const int en = e + nw;
+    if (en < a.nlocal_e) {
+      if (lane < 24) pn = __ldg(a.node_hl + 24 * (size_t) en + lane);
+      pty = __ldg(a.etype + en);
+      prf = __ldg(a.row_first + en);
+    }
     if (a.skip && a.skip[e]) continue;  // nodal forces from the surrogate (warp-uniform)
-    const int ty = a.etype[e];
+    if (lane < 24) s_nx[lane] = cn;
+    else if (EAM) s_er[lane - 24] = __ldg(erho + NPE * (size_t) e + (lane - 24));
     const FusedLat g = fused_lat(a.lat, ty);
     const int f0 = a.fjj_off[ty], nf = a.fjj_off[ty + 1] - f0;
-    fused_coeffs(a.node_hl, e, lane, s_k, V != 0);
+    __syncwarp();
+    fused_coeffs(s_nx, lane, s_k, V != 0);
     if (EAM && lane >= 24) {  // density coefficients from the nodal densities (FP32,
       // formed in double-single from the doubles' bits: no FP64 instruction)
-      const double *er = erho + NPE * (size_t) e;
+      const double *er = s_er;
       const int m = lane - 24;
       auto E = [&](int k) { return ds_of_double(er[k]); };
       ds v;
@@ -1799,8 +1843,8 @@ k_elem_force_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rd
         // the row's density in FP32 for the sites' (rho(p) in rk[0])
         float rho32 = 0.f;
         if (live)  // every lane of the row's group (no shuffle)
-          fpi = row_fprime_ds(a.spa_int_hl + ((size_t) a.int_off[ty] + jj) * NPE,
-                              erho + NPE * (size_t) e, a.frho_ds, a.nrho, a.rdrho_ds, rho32);
+          fpi = row_fprime_ds(a.spa_int_hl + ((size_t) a.int_off[ty] + jj) * NPE, s_er,
+                              a.frho_ds, a.nrho, a.rdrho_ds, rho32);
         rk[0] = rho32;
         if (V == 0) {
 #pragma unroll
@@ -1808,7 +1852,7 @@ k_elem_force_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rd
         }
       }
       dsacc acc, fx, fy, fz;
-      fused_row<EAM, false, V>(a, g, e, ty, jj, level, glane, k, rk,
+      fused_row<EAM, false, V>(a, g, e, rfirst, ty, jj, level, glane, k, rk,
                                reinterpret_cast<const float4 *>(s_k), s_tab, s_fp, nr, rdr, fpi,
                                lj1, lj2, live, acc, fx, fy, fz);
       if (live && glane == 0) {
@@ -2228,6 +2272,7 @@ void elem_fused(const MixedElems &m, const FusedTables &t, int pass, const float
   if (t.variant == 1) launch_fused<1>(a, pass, tab, e, table, lj1, lj2, erho_in, erho_out, nodef, s);
   else if (t.variant == 2)
     launch_fused<2>(a, pass, tab, e, table, lj1, lj2, erho_in, erho_out, nodef, s);
+
 
   else launch_fused<0>(a, pass, tab, e, table, lj1, lj2, erho_in, erho_out, nodef, s);
   check(cudaGetLastError(), "elem_fused");
