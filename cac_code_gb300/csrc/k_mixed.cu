@@ -1441,29 +1441,40 @@ struct FusedArgs {
   double rdrho64;
 };
 
-// the trilinear coefficient vectors of the element, m = a, b, c, ab, ac, bc,
-// abc (lanes 0..20), from the double-single nodes (staged in the warp's shared
-// memory, s_nx[3 k + d]): s_k[3 m + d] (kept in
-// registers), or with by_axis s_k[8 d + m] (read from shared memory as two
-// float4 per axis)
+// The trilinear coefficient vectors of the element, m = a, b, c, ab, ac, bc,
+// abc (lanes 0..20: m = lane / 3, axis d = lane % 3), K_a = x1 - x0,
+// K_b = x3 - x0, K_c = x4 - x0, K_ab = x0 - x1 + x2 - x3, K_ac = x0 - x1 + x5 -
+// x4, K_bc = x0 - x3 + x7 - x4, K_abc = x1 - x0 + x3 - x2 + x4 - x5 + x6 - x7,
+// and the nodal-density coefficients likewise (rho_0, then the same seven
+// monomials), as signed sums over the 8 nodes in node order: bit k of byte m
+// of POS / NEG marks node k added / subtracted.  Every lane runs the same
+// eight double-single additions (no divergent cases).
+constexpr unsigned long long COEF_POS = 0x5A81210510080200ull;  // bytes: a b c ab ac bc abc
+constexpr unsigned long long COEF_NEG = 0xA518120A01010100ull;
+constexpr unsigned long long RHO_POS = 0x5A81210510080201ull;   // bytes: 0 a b c ab ac bc abc
+constexpr unsigned long long RHO_NEG = 0xA518120A01010100ull;
+
+__device__ __forceinline__ ds signed_node_sum(const float2 *v, int stride, unsigned pos,
+                                              unsigned neg) {
+  ds s = ds{0.f, 0.f};
+#pragma unroll
+  for (int k = 0; k < NPE; k++) {
+    const float sg = (float) ((int) ((pos >> k) & 1u) - (int) ((neg >> k) & 1u));
+    const float2 x = v[stride * k];
+    s = ds_add(s, ds{sg * x.x, sg * x.y});
+  }
+  return s;
+}
+
+// K from the double-single nodes staged in the warp's shared memory
+// (s_nx[3 k + d]): s_k[3 m + d] (kept in registers), or with by_axis
+// s_k[8 d + m] (read from shared memory as two float4 per axis)
 __device__ __forceinline__ void fused_coeffs(const float2 *s_nx, int lane, float *s_k,
                                              bool by_axis) {
   if (lane < 21) {
     const int m = lane / 3, d = lane % 3;
-    const float2 *nx = s_nx + d;
-    auto X = [&](int k) { return ds{nx[3 * k].x, nx[3 * k].y}; };
-    ds v;
-    switch (m) {
-      case 0: v = ds_sub(X(1), X(0)); break;
-      case 1: v = ds_sub(X(3), X(0)); break;
-      case 2: v = ds_sub(X(4), X(0)); break;
-      case 3: v = ds_add(ds_sub(X(0), X(1)), ds_sub(X(2), X(3))); break;
-      case 4: v = ds_add(ds_sub(X(0), X(1)), ds_sub(X(5), X(4))); break;
-      case 5: v = ds_add(ds_sub(X(0), X(3)), ds_sub(X(7), X(4))); break;
-      default:
-        v = ds_add(ds_add(ds_sub(X(1), X(0)), ds_sub(X(3), X(2))),
-                   ds_add(ds_sub(X(4), X(5)), ds_sub(X(6), X(7))));
-    }
+    const ds v = signed_node_sum(s_nx + d, 3, (unsigned) (COEF_POS >> (8 * (m + 1))) & 0xFFu,
+                                 (unsigned) (COEF_NEG >> (8 * (m + 1))) & 0xFFu);
     s_k[by_axis ? 8 * d + m : lane] = v.h + v.l;
   }
 }
@@ -1479,16 +1490,17 @@ __device__ __forceinline__ float4 lds_v4(const float4 *p) {
 
 // F'(rho) at a row, rho = sum_k N_k erho_k, as fprime64 forms it (pair_eam.cpp:
 // 1090-1100, knot index, clamps, cubic) in double-single FP32 arithmetic from
-// the double-single shape functions, nodal densities and spline
+// the double-single shape functions, nodal densities (erds) and spline
 // coefficients: the FP32 value of the FP64 result, without an FP64
 // instruction (also *rho32, rho rounded to FP32)
 __device__ __forceinline__ float row_fprime_ds(const float2 *__restrict__ N,
-                                               const double *__restrict__ er,
+                                               const float2 *__restrict__ erds,
                                                const float2 *__restrict__ c3, int nrho,
                                                float2 rdrho, float &rho32) {
   ds rho = ds{0.f, 0.f};
 #pragma unroll
-  for (int k = 0; k < NPE; k++) rho = ds_madd(ds{N[k].x, N[k].y}, ds_of_double(er[k]), rho);
+  for (int k = 0; k < NPE; k++)
+    rho = ds_madd(ds{N[k].x, N[k].y}, ds{erds[k].x, erds[k].y}, rho);
   rho32 = rho.h + rho.l;
   return fprime_ds(rho, c3, nrho, rdrho);
 }
@@ -1690,7 +1702,7 @@ __device__ __forceinline__ FusedLat fused_lat(const Lattice &lat, int ty) {
 
 // per-warp shared memory: coefficient vectors (21), density coefficients (8),
 // row forces (3 per row of nonzero weight), then the element's staged nodes
-// (24 float2) and nodal densities (8 double)
+// (24 float2) and nodal densities (8 double-single float2)
 constexpr int FUSED_WARP_FLOATS = 32 + 2 * 3 * FUSED_MAXF + 48 + 16;
 constexpr int FUSED_NX_AT = 32 + 2 * 3 * FUSED_MAXF, FUSED_ER_AT = FUSED_NX_AT + 48;
 static_assert(FUSED_NX_AT % 2 == 0 && FUSED_ER_AT % 2 == 0 && FUSED_WARP_FLOATS % 2 == 0,
@@ -1780,7 +1792,7 @@ k_elem_force_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rd
   const int level = a.nnear_row ? cull_level(a.eflags) : 4;
   const int gsub = lane / FG, glane = lane % FG;
   float2 *s_nx = reinterpret_cast<float2 *>(s_k + FUSED_NX_AT);
-  double *s_er = reinterpret_cast<double *>(s_k + FUSED_ER_AT);
+  float2 *s_erds = reinterpret_cast<float2 *>(s_k + FUSED_ER_AT);  // nodal densities, ds
   // the next element's nodes, type and first row are loaded while this
   // element's rows run
   float2 pn = make_float2(0.f, 0.f);
@@ -1801,29 +1813,19 @@ k_elem_force_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rd
     }
     if (a.skip && a.skip[e]) continue;  // nodal forces from the surrogate (warp-uniform)
     if (lane < 24) s_nx[lane] = cn;
-    else if (EAM) s_er[lane - 24] = __ldg(erho + NPE * (size_t) e + (lane - 24));
+    else if (EAM) {
+      const ds d = ds_of_double(__ldg(erho + NPE * (size_t) e + (lane - 24)));
+      s_erds[lane - 24] = make_float2(d.h, d.l);
+    }
     const FusedLat g = fused_lat(a.lat, ty);
     const int f0 = a.fjj_off[ty], nf = a.fjj_off[ty + 1] - f0;
     __syncwarp();
     fused_coeffs(s_nx, lane, s_k, V != 0);
     if (EAM && lane >= 24) {  // density coefficients from the nodal densities (FP32,
       // formed in double-single from the doubles' bits: no FP64 instruction)
-      const double *er = s_er;
       const int m = lane - 24;
-      auto E = [&](int k) { return ds_of_double(er[k]); };
-      ds v;
-      switch (m) {
-        case 0: v = E(0); break;
-        case 1: v = ds_sub(E(1), E(0)); break;
-        case 2: v = ds_sub(E(3), E(0)); break;
-        case 3: v = ds_sub(E(4), E(0)); break;
-        case 4: v = ds_add(ds_sub(E(0), E(1)), ds_sub(E(2), E(3))); break;
-        case 5: v = ds_add(ds_sub(E(0), E(1)), ds_sub(E(5), E(4))); break;
-        case 6: v = ds_add(ds_sub(E(0), E(3)), ds_sub(E(7), E(4))); break;
-        default:
-          v = ds_add(ds_add(ds_sub(E(1), E(0)), ds_sub(E(3), E(2))),
-                     ds_add(ds_sub(E(4), E(5)), ds_sub(E(6), E(7))));
-      }
+      const ds v = signed_node_sum(s_erds, 1, (unsigned) (RHO_POS >> (8 * m)) & 0xFFu,
+                                   (unsigned) (RHO_NEG >> (8 * m)) & 0xFFu);
       s_r[m] = v.h + v.l;
     }
     __syncwarp();
@@ -1843,7 +1845,7 @@ k_elem_force_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rd
         // the row's density in FP32 for the sites' (rho(p) in rk[0])
         float rho32 = 0.f;
         if (live)  // every lane of the row's group (no shuffle)
-          fpi = row_fprime_ds(a.spa_int_hl + ((size_t) a.int_off[ty] + jj) * NPE, s_er,
+          fpi = row_fprime_ds(a.spa_int_hl + ((size_t) a.int_off[ty] + jj) * NPE, s_erds,
                               a.frho_ds, a.nrho, a.rdrho_ds, rho32);
         rk[0] = rho32;
         if (V == 0) {
