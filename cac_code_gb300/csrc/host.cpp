@@ -213,6 +213,7 @@ struct cacg_context {
   DBuf<int> d_nae;
   DBuf<float2> d_frac, d_fipf;  // lattice fractions; double-single row forces
   DBuf<float> d_wn;             // weight x shape function per type row and node (FP32)
+  DBuf<float> d_wnf;            // the same for the rows of nonzero weight, per type in order
   int fstride = 1;
   // mixed precision, per row: packed and double-single integration points,
   // F'(rho) of the force rows; the integration-point lists row-major
@@ -632,6 +633,7 @@ cacg_context::~cacg_context() {
   d_frac.release();
   d_fipf.release();
   d_wn.release();
+  d_wnf.release();
   d_ip_q.release();
   d_ip_h.release();
   d_ip_l.release();
@@ -1719,6 +1721,13 @@ void cacg_context::element_tables() {
     if (nf > 32) fused_types_ok = false;
   }
   fjj_off[MAXT + 1] = (int) fjj.size();
+  // their weight x shape function products in the same order (the fused
+  // nodal gather reads them without the row indirection)
+  std::vector<float> wnf(std::max<size_t>(fjj.size(), 1) * NPE, 0.f);
+  for (int t = 1; t <= netypes; t++)
+    for (int j = fjj_off[t]; j < fjj_off[t + 1]; j++)
+      for (int q = 0; q < NPE; q++) wnf[(size_t) j * NPE + q] = wn[((size_t) int_off[t] + fjj[j]) * NPE + q];
+  upload(d_wnf, wnf, s);
   if (fjj.empty()) fjj.push_back(0);
   upload(d_fjj, fjj, s);
   upload(d_fjj_off, fjj_off, s);
@@ -2692,7 +2701,7 @@ void cacg_context::pair_ecompute_mixed() {
   if (fused) {
     mixed::FusedTables ft{d_node_hl.p, d_nodex.p, d_int_off.p, d_inter_off.p, d_intp4.p,
                           d_spa_int.p, d_spa_inter.p, d_fjj.p, d_fjj_off.p, d_wn.p, maxlines,
-                          fused_variant, d_spa_int_hl.p, d_frho_ds.p};
+                          fused_variant, d_spa_int_hl.p, d_frho_ds.p, d_wnf.p};
     if (pair_style == 1) {
       int a = 1 * (MAXT + 1) + 1;
       m.cutsq = ljtab.cutsq[a];

@@ -410,6 +410,7 @@ struct FusedTables {
   int variant;                // 0: coefficients in registers; 1, 2: in shared memory
   const float2 *spa_int_hl;   // the rows' shape functions as double-single pairs
   const float2 *frho_ds;      // F' spline c0..c2 per knot as double-single pairs
+  const float *wnf;           // wn of the rows of nonzero weight, per type in fjj order
 };
 bool fused_fits(int nr, int nrho);
 void elem_fused(const MixedElems &m, const FusedTables &t, int pass, const float4 *tab,

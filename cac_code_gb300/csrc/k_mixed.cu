@@ -1426,6 +1426,7 @@ struct FusedArgs {
   const double *spa_inter;     // FP64 shape functions of the sites
   const int *fjj, *fjj_off;    // per type: the rows of nonzero weight, ascending
   const float *wn;             // weight x shape function per row and node
+  const float *wnf;            // the same for the rows of nonzero weight, per type in order
   const int *row_start, *ent;  // row-major line codes, culling parts in order
   const int4 *nnear_row;
   const unsigned *eflags;
@@ -1866,10 +1867,10 @@ k_elem_force_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rd
     __syncwarp();
     if (lane < 24) {  // the nodal gather (k_gather_nodef_ds), rows in ascending order
       const int q = lane / 3, c = lane % 3;
-      const float *wt = a.wn + (size_t) a.int_off[ty] * NPE;
+      const float *wt = a.wnf + (size_t) f0 * NPE + q;
       dsacc acc;
       for (int j = 0; j < nf; j++) {
-        const float wq = __ldg(wt + a.fjj[f0 + j] * NPE + q);
+        const float wq = __ldg(wt + j * NPE);
         if (wq == 0.f) continue;
         const float2 f = s_f[3 * j + c];
         acc.add(__fmul_rn(wq, f.x));
@@ -2249,6 +2250,7 @@ void elem_fused(const MixedElems &m, const FusedTables &t, int pass, const float
   a.fjj = t.fjj;
   a.fjj_off = t.fjj_off;
   a.wn = t.wn;
+  a.wnf = t.wnf;
   a.row_start = m.row_start;
   a.ent = m.ent;
   a.nnear_row = m.nnear_row;
