@@ -363,15 +363,15 @@ class System:
 
     # ---- state out ----
     def counts(self) -> Dict[str, int]:
-        c = np.zeros(30, dtype=np.int64)
-        self._ok(self._L.cacg_get_counts(self.h, c.ctypes.data_as(_lp), 30))
+        c = np.zeros(31, dtype=np.int64)
+        self._ok(self._L.cacg_get_counts(self.h, c.ctypes.data_as(_lp), 31))
         keys = ["nlocal", "nghost", "atom_entries", "enlocal", "enghost", "elem_entries",
                 "ip_rows", "ip_entries", "rebuilds", "nstencil", "step", "sites", "launches",
                 "sites_needed", "force_rows", "short_entries", "surrogate_elements",
                 "surrogate_evaluated", "surrogate_accepted", "graph_steps", "density_scan_entries",
                 "ip_scan_entries", "ip_reorders", "rebuilds_atoms_only", "atom_reorders",
                 "lines_referenced", "lines_referenced_force", "elem_fused",
-                "loop_launches", "host_decisions"]
+                "loop_launches", "host_decisions", "band_reruns"]
         return dict(zip(keys, (int(v) for v in c)))
 
     def referenced_lines(self):

@@ -214,6 +214,7 @@ struct cacg_context {
   DBuf<float2> d_frac, d_fipf;  // lattice fractions; double-single row forces
   DBuf<float> d_wn;             // weight x shape function per type row and node (FP32)
   DBuf<float> d_wnf;            // the same for the rows of nonzero weight, per type in order
+  DBuf<int> d_band;             // elements with a guard-band pair: count, blocks done, list
   int fstride = 1;
   // mixed precision, per row: packed and double-single integration points,
   // F'(rho) of the force rows; the integration-point lists row-major
@@ -248,6 +249,8 @@ struct cacg_context {
   // 2.48 against 3.18 ms for the force pass), or as 1 with two entries in
   // flight per lane (2)
   int fused_variant = 1;
+  // half-width of the guard band of the mixed cutoff decisions ("tune band")
+  float band_eps = 1.0e-4f;
   // "tune fprime fp64|fp32": F'(rho) of the atoms in the mixed density pass
   // from the FP64 spline at the FP64 density (default), or from the FP32 copy
   bool fprime64 = true;
@@ -634,6 +637,7 @@ cacg_context::~cacg_context() {
   d_fipf.release();
   d_wn.release();
   d_wnf.release();
+  d_band.release();
   d_ip_q.release();
   d_ip_h.release();
   d_ip_l.release();
@@ -880,6 +884,9 @@ void cacg_context::command(const std::string &raw) {
     //   decision on the device (with graphs on, no box deformation), or one
     //   graph launch per step without a decision and eager decision steps
     //   (host, the default)
+    // tune band W: the guard band of the mixed cutoff decisions, cutsq (1 +- W)
+    //   (default 1e-4, at most 0.1); a wider band only moves more pairs to the
+    //   FP64 decision, the decisions and forces stay the same
     if (a.size() != 2) fail(CACG_EINVAL, "Illegal tune command");
     if (a[0] == "block") {
       int b = inumeric(a[1]);
@@ -903,6 +910,11 @@ void cacg_context::command(const std::string &raw) {
     } else if (a[0] == "fprime") {
       if (a[1] != "fp64" && a[1] != "fp32") fail(CACG_EINVAL, "tune fprime takes fp64 or fp32");
       fprime64 = a[1] == "fp64";
+      invalidate_graph();
+    } else if (a[0] == "band") {
+      const double w = numeric(a[1]);
+      if (!(w >= 1.0e-4 && w <= 0.1)) fail(CACG_EINVAL, "tune band takes 1e-4 to 0.1");
+      band_eps = (float) w;
       invalidate_graph();
     } else if (a[0] == "fused_variant") {
       const int v = inumeric(a[1]);
@@ -2484,7 +2496,7 @@ void cacg_context::pair_compute_pass(int pass) {
 void cacg_context::pair_compute_mixed(int pass) {
   cudaStream_t s = stream;
   int nall = nlocal + nghost;
-  const float eps = 1.0e-4f;
+  const float eps = band_eps;
   mixed::MixedAtoms m{};
   m.block = mixed_block;
   m.fprime64 = fprime64;
@@ -2668,7 +2680,7 @@ void cacg_context::pair_ecompute_mixed() {
   launches += 6;
   epart_of = elist_builds;
   const bool use_sur = sur && nfar > 0;
-  const float eps = 1.0e-4f;
+  const float eps = band_eps;
   mixed::MixedElems m{};
   m.block = mixed_block;
   if (mixed_ip_group) {
@@ -2699,9 +2711,13 @@ void cacg_context::pair_ecompute_mixed() {
   m.pg = pg;
   if (use_sur) m.skip = d_skip.p;
   if (fused) {
+    if (d_band.cap < 3 + (size_t) enlocal) {  // outside captures: the eager step allocates
+      d_band.ensure(3 + (size_t) enlocal, s);
+      check(cudaMemsetAsync(d_band.p, 0, 3 * sizeof(int), s), "band list");
+    }
     mixed::FusedTables ft{d_node_hl.p, d_nodex.p, d_int_off.p, d_inter_off.p, d_intp4.p,
                           d_spa_int.p, d_spa_inter.p, d_fjj.p, d_fjj_off.p, d_wn.p, maxlines,
-                          fused_variant, d_spa_int_hl.p, d_frho_ds.p, d_wnf.p};
+                          fused_variant, d_spa_int_hl.p, d_frho_ds.p, d_wnf.p, d_band.p};
     if (pair_style == 1) {
       int a = 1 * (MAXT + 1) + 1;
       m.cutsq = ljtab.cutsq[a];
@@ -2717,7 +2733,7 @@ void cacg_context::pair_ecompute_mixed() {
       mixed::elem_fused(m, ft, 0, nullptr, et, (float) ljtab.lj1[a], (float) ljtab.lj2[a], nullptr,
                         nullptr, d_nodef.p, s);
       kmark(KT_ELEM_FORCE, 1);
-      launches++;
+      launches += 2;  // the pass and its guard-band exact pass
     } else {
       m.cutsq = cutforcesq;
       m.cutsq_f = (float) cutforcesq;
@@ -2738,7 +2754,7 @@ void cacg_context::pair_ecompute_mixed() {
       kmark(KT_ELEM_FORCE, 0);
       mixed::elem_fused(m, ft, 2, d_ftab.p, et, 0.f, 0.f, d_erho.p, nullptr, d_nodef.p, s);
       kmark(KT_ELEM_FORCE, 1);
-      launches += 2;
+      launches += 4;  // two passes, each with its guard-band exact pass
     }
     if (use_sur) {
       surrogate::write_forces(d_smean.p, d_far.p, d_sdue.p, d_sdue_n.p, nfar, d_skip.p, d_nodef.p, s);
@@ -4482,12 +4498,18 @@ int cacg_run_host(cacg_handle h, int nsteps, double *x, double *v, double *nodex
 
 int cacg_get_counts(cacg_handle h, long long *c, int n) {
   API_BEGIN
-  long long v[30] = {h->nlocal, h->nghost, 0, h->enlocal, h->enghost, 0, h->nrows, 0,
+  long long v[31] = {h->nlocal, h->nghost, 0, h->enlocal, h->enghost, 0, h->nrows, 0,
                      h->nrebuild, (long long) h->stencil.size(), h->ntimestep, h->nsites,
                      h->launches, h->nneed, h->nforce, 0, h->sur ? h->nfar : 0, 0, 0,
                      h->graph_steps, 0, 0, 0, h->nrebuild_atoms, 0,
                      (long long) h->h_nlines[0], (long long) h->h_nlines[1],
-                     h->fused_used ? 1LL : 0LL, h->loop_launches, h->host_decisions};
+                     h->fused_used ? 1LL : 0LL, h->loop_launches, h->host_decisions, 0};
+  if (h->d_band.p) {
+    int b = 0;
+    check(cudaMemcpyAsync(&b, h->d_band.p + 2, sizeof(b), cudaMemcpyDeviceToHost, h->stream), "band");
+    h->sync();
+    v[30] = b;
+  }
   if (h->areorders_zeroed && h->d_misc.p) {
     unsigned r = 0;
     check(cudaMemcpyAsync(&r, h->d_misc.p + 16, sizeof(r), cudaMemcpyDeviceToHost, h->stream), "areorders");
@@ -4564,7 +4586,7 @@ int cacg_get_counts(cacg_handle h, long long *c, int n) {
       for (const int4 &x : nn) v[21] += level == 1 ? x.x : level == 2 ? x.y : x.z;
     }
   }
-  for (int i = 0; i < n && i < 30; i++) c[i] = v[i];
+  for (int i = 0; i < n && i < 31; i++) c[i] = v[i];
   API_END
 }
 

@@ -411,6 +411,8 @@ struct FusedTables {
   const float2 *spa_int_hl;   // the rows' shape functions as double-single pairs
   const float2 *frho_ds;      // F' spline c0..c2 per knot as double-single pairs
   const float *wnf;           // wn of the rows of nonzero weight, per type in fjj order
+  int *band;                  // guard-band list: count, blocks done, elements re-run so
+                              // far, then the listed elements (3 + nlocal_e ints, zeroed once)
 };
 bool fused_fits(int nr, int nrho);
 void elem_fused(const MixedElems &m, const FusedTables &t, int pass, const float4 *tab,

@@ -1434,6 +1434,7 @@ struct FusedArgs {
   float cutsq_f, band_lo, band_hi;
   double cutsq;
   const unsigned char *skip;   // elements the surrogate evaluates
+  int *band;                   // the guard-band list (band_list)
   Lattice lat;
   const float4 *fp4;           // FP32 F' spline (sites)
   int nrho;
@@ -1547,9 +1548,13 @@ __device__ __forceinline__ float fprime32_s(float rho, const float4 *s_fp, int n
 
 // V = 0: coefficients in registers; V = 1: read from shared memory (sk4:
 // two float4 per axis, then the density coefficients) at every entry, fewer
-// registers; V = 2: as 1, two entries in flight per lane
-template <bool EAM, bool DENSITY, int V>
-__device__ __forceinline__ void fused_row(const FusedArgs &a, const FusedLat &g, int e, int rfirst,
+// registers; V = 2: as 1, two entries in flight per lane.
+// EXACT: a pair in the guard band is decided in FP64 (fused_band64) in the
+// loop; otherwise the loop only reports that it met one (the return value):
+// the caller lists the element for the exact pass, and the call with its
+// register saves stays out of the common case's loop
+template <bool EAM, bool DENSITY, int V, bool EXACT>
+__device__ __forceinline__ bool fused_row(const FusedArgs &a, const FusedLat &g, int e, int rfirst,
                                           int ty, int jj, int level, int glane, const float (&k)[21],
                                           const float (&rk)[8], const float4 *sk4,
                                           const float4 *s_tab, const float4 *s_fp, int nr,
@@ -1571,6 +1576,7 @@ __device__ __forceinline__ void fused_row(const FusedArgs &a, const FusedLat &g,
   const int lbase = e * a.maxlines;
   float part = 0.f, px = 0.f, py = 0.f, pz = 0.f;
   int cn = 0, cnt = 0;
+  bool band = false;
   if (glane < n) cn = __ldg(a.ent + s0 + glane);
 #pragma unroll(V == 2 ? 2 : 1)
   for (int t = glane; t < n; t += FG) {
@@ -1614,10 +1620,14 @@ __device__ __forceinline__ void fused_row(const FusedArgs &a, const FusedLat &g,
     const float dx = v[0], dy = v[1], dz = v[2];
     const float rsq = dx * dx + dy * dy + dz * dz;
     bool in = rsq < a.cutsq_f;
-    if (rsq >= a.band_lo && rsq <= a.band_hi)
-      in = fused_band64(a.spa_int + ((size_t) a.int_off[ty] + jj) * NPE,
-                        a.spa_inter + ((size_t) a.inter_off[ty] + L * g.naz + kk) * NPE,
-                        a.nodex + 24 * (size_t) e, a.cutsq);
+    if (rsq >= a.band_lo && rsq <= a.band_hi) {
+      if (EXACT)
+        in = fused_band64(a.spa_int + ((size_t) a.int_off[ty] + jj) * NPE,
+                          a.spa_inter + ((size_t) a.inter_off[ty] + L * g.naz + kk) * NPE,
+                          a.nodex + 24 * (size_t) e, a.cutsq);
+      else
+        band = true;
+    }
     if (in) {
       if (EAM) {
         const float recip = rsqrtf(rsq);
@@ -1687,6 +1697,7 @@ __device__ __forceinline__ void fused_row(const FusedArgs &a, const FusedLat &g,
     group_sum<FG>(fy);
     group_sum<FG>(fz);
   }
+  return band;
 }
 
 __device__ __forceinline__ FusedLat fused_lat(const Lattice &lat, int ty) {
@@ -1712,11 +1723,38 @@ static_assert(FUSED_NX_AT % 2 == 0 && FUSED_ER_AT % 2 == 0 && FUSED_WARP_FLOATS 
 // threads per block of each variant (V = 0: coefficients in registers)
 __host__ __device__ constexpr int fused_block(int V) { return V == 0 ? FUSED_BLOCK : 768; }
 
+// The guard-band list (a.band: count, blocks done, elements re-run so far,
+// then the element indices).  A fused pass lists every element in which some
+// pair fell in the guard band; the exact pass (FIX) runs the listed elements
+// again with the FP64 decisions, overwriting their outputs, and its last block
+// to finish resets the list for the next pass.
+constexpr int BAND_LIST = 3;
+
+__device__ __forceinline__ void band_list(int *band, int e, int cap) {
+  const int slot = atomicAdd(band, 1);
+  if (slot < cap) band[BAND_LIST + slot] = e;
+}
+
+__device__ __forceinline__ void band_done(int *band, int ne) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(band + 1, 1) == (int) gridDim.x - 1) {
+      band[2] += ne;
+      band[0] = 0;
+      band[1] = 0;
+    }
+  }
+}
+
 // EAM nodal densities: the element's 8 node rows, one row per FG lanes
-template <int V>
+// (FIX: the listed elements, guard-band pairs decided in FP64)
+template <int V, bool FIX>
 __global__ void __launch_bounds__(fused_block(V), 1)
 k_elem_rho_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rdr,
                  double *__restrict__ erho) {
+  const int ne = FIX ? min(a.band[0], a.nlocal_e) : a.nlocal_e;
+  if (FIX && ne == 0) return;  // the whole grid (the count is the same for every block)
   extern __shared__ float4 smem[];
   float4 *s_tab = smem;
   for (int m = threadIdx.x; m <= nr; m += blockDim.x) s_tab[m] = tab[m];
@@ -1732,17 +1770,20 @@ k_elem_rho_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rdr,
   // the next element's nodes, type and first row are loaded while this
   // element's rows run
   float2 pn = make_float2(0.f, 0.f);
-  int pty = 0, prf = 0;
-  if (gw < a.nlocal_e) {
-    if (lane < 24) pn = __ldg(a.node_hl + 24 * (size_t) gw + lane);
-    pty = __ldg(a.etype + gw);
-    prf = __ldg(a.row_first + gw);
+  int pty = 0, prf = 0, pe = gw;
+  if (gw < ne) {
+    if (FIX) pe = a.band[BAND_LIST + gw];
+    if (lane < 24) pn = __ldg(a.node_hl + 24 * (size_t) pe + lane);
+    pty = __ldg(a.etype + pe);
+    prf = __ldg(a.row_first + pe);
   }
-  for (int e = gw; e < a.nlocal_e; e += nw) {
-    const int ty = pty, rfirst = prf;
+  for (int i = gw; i < ne; i += nw) {
+    const int e = FIX ? pe : i, ty = pty, rfirst = prf;
     if (lane < 24) s_nx[lane] = pn;
-    const int en = e + nw;
-    if (en < a.nlocal_e) {
+    const int in = i + nw;
+    if (in < ne) {
+      const int en = FIX ? a.band[BAND_LIST + in] : in;
+      if (FIX) pe = en;
       if (lane < 24) pn = __ldg(a.node_hl + 24 * (size_t) en + lane);
       pty = __ldg(a.etype + en);
       prf = __ldg(a.row_first + en);
@@ -1756,26 +1797,32 @@ k_elem_rho_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rdr,
 #pragma unroll
       for (int q = 0; q < 21; q++) k[q] = s_k[q];
     }
+    bool band = false;
     for (int kb = 0; kb < NPE; kb += 32 / FG) {
       const int q = kb + gsub;
       const bool live = q < NPE;
       const int jj = live ? a.node_list[ty * NPE + q] : 0;
       dsacc acc, fx, fy, fz;
-      fused_row<true, true, V>(a, g, e, rfirst, ty, jj, level, glane, k, rk,
-                               reinterpret_cast<const float4 *>(s_k), s_tab, nullptr, nr, rdr,
-                               0.f, 0.f, 0.f, live, acc, fx, fy, fz);
+      band |= fused_row<true, true, V, FIX>(a, g, e, rfirst, ty, jj, level, glane, k, rk,
+                                            reinterpret_cast<const float4 *>(s_k), s_tab, nullptr,
+                                            nr, rdr, 0.f, 0.f, 0.f, live, acc, fx, fy, fz);
       if (live && glane == 0) erho[NPE * (size_t) e + q] = acc.value();
     }
+    if (!FIX && __any_sync(0xffffffffu, band) && lane == 0) band_list(a.band, e, a.nlocal_e);
     __syncwarp();
   }
+  if (FIX) band_done(a.band, ne);
 }
 
 // Forces of the element's rows of nonzero weight and their gather onto the
 // nodes (EAM with the nodal densities and row F'(rho), or LJ)
-template <bool EAM, int V>
+// (FIX: the listed elements, guard-band pairs decided in FP64)
+template <bool EAM, int V, bool FIX>
 __global__ void __launch_bounds__(fused_block(V), 1)
 k_elem_force_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rdr, float lj1,
                    float lj2, const double *__restrict__ erho, double *__restrict__ nodef) {
+  const int ne = FIX ? min(a.band[0], a.nlocal_e) : a.nlocal_e;
+  if (FIX && ne == 0) return;  // the whole grid (the count is the same for every block)
   extern __shared__ float4 smem[];
   float4 *s_tab = smem;
   const int ntab = EAM ? FTAB_W * (nr + 1) : 0;
@@ -1797,17 +1844,20 @@ k_elem_force_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rd
   // the next element's nodes, type and first row are loaded while this
   // element's rows run
   float2 pn = make_float2(0.f, 0.f);
-  int pty = 0, prf = 0;
-  if (gw < a.nlocal_e) {
-    if (lane < 24) pn = __ldg(a.node_hl + 24 * (size_t) gw + lane);
-    pty = __ldg(a.etype + gw);
-    prf = __ldg(a.row_first + gw);
+  int pty = 0, prf = 0, pe = gw;
+  if (gw < ne) {
+    if (FIX) pe = a.band[BAND_LIST + gw];
+    if (lane < 24) pn = __ldg(a.node_hl + 24 * (size_t) pe + lane);
+    pty = __ldg(a.etype + pe);
+    prf = __ldg(a.row_first + pe);
   }
-  for (int e = gw; e < a.nlocal_e; e += nw) {
-    const int ty = pty, rfirst = prf;
+  for (int i = gw; i < ne; i += nw) {
+    const int e = FIX ? pe : i, ty = pty, rfirst = prf;
     const float2 cn = pn;
-    const int en = e + nw;
-    if (en < a.nlocal_e) {
+    const int in = i + nw;
+    if (in < ne) {
+      const int en = FIX ? a.band[BAND_LIST + in] : in;
+      if (FIX) pe = en;
       if (lane < 24) pn = __ldg(a.node_hl + 24 * (size_t) en + lane);
       pty = __ldg(a.etype + en);
       prf = __ldg(a.row_first + en);
@@ -1836,6 +1886,7 @@ k_elem_force_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rd
       for (int q = 0; q < 21; q++) k[q] = s_k[q];
     }
     float rk[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    bool band = false;
     for (int fb = 0; fb < nf; fb += 32 / FG) {
       const int j = fb + gsub;
       const bool live = j < nf;
@@ -1855,9 +1906,9 @@ k_elem_force_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rd
         }
       }
       dsacc acc, fx, fy, fz;
-      fused_row<EAM, false, V>(a, g, e, rfirst, ty, jj, level, glane, k, rk,
-                               reinterpret_cast<const float4 *>(s_k), s_tab, s_fp, nr, rdr, fpi,
-                               lj1, lj2, live, acc, fx, fy, fz);
+      band |= fused_row<EAM, false, V, FIX>(a, g, e, rfirst, ty, jj, level, glane, k, rk,
+                                            reinterpret_cast<const float4 *>(s_k), s_tab, s_fp,
+                                            nr, rdr, fpi, lj1, lj2, live, acc, fx, fy, fz);
       if (live && glane == 0) {
         s_f[3 * j] = make_float2(fx.h, fx.l);
         s_f[3 * j + 1] = make_float2(fy.h, fy.l);
@@ -1878,8 +1929,10 @@ k_elem_force_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rd
       }
       nodef[24 * (size_t) e + lane] = acc.value();
     }
+    if (!FIX && __any_sync(0xffffffffu, band) && lane == 0) band_list(a.band, e, a.nlocal_e);
     __syncwarp();
   }
+  if (FIX) band_done(a.band, ne);
 }
 
 // every entry of every row references a site of the row's own element:
@@ -2204,16 +2257,29 @@ static void launch_fused(const FusedArgs &a, int pass, const float4 *tab, const 
   constexpr int B = fused_block(V);
   const size_t smem = table + sizeof(float) * FUSED_WARP_FLOATS * (B / 32);
   const long long items = (long long) a.nlocal_e * 32;
+  // the pass, then the exact pass over the elements it listed (a grid of the
+  // same shape; it returns at once when the list is empty)
   if (pass == 1) {
-    const int g = persistent_grid((const void *) k_elem_rho_fused<V>, B, smem, items);
-    k_elem_rho_fused<V><<<g, B, smem, s>>>(a, tab, e.nr, (float) e.rdr, erho_out);
+    const int g = persistent_grid((const void *) k_elem_rho_fused<V, false>, B, smem, items);
+    k_elem_rho_fused<V, false><<<g, B, smem, s>>>(a, tab, e.nr, (float) e.rdr, erho_out);
+    persistent_grid((const void *) k_elem_rho_fused<V, true>, B, smem, items);
+    k_elem_rho_fused<V, true><<<g, B, smem, s>>>(a, tab, e.nr, (float) e.rdr, erho_out);
   } else if (pass == 2) {
-    const int g = persistent_grid((const void *) k_elem_force_fused<true, V>, B, smem, items);
-    k_elem_force_fused<true, V><<<g, B, smem, s>>>(a, tab, e.nr, (float) e.rdr, 0.f, 0.f,
-                                                   erho_in, nodef);
+    const int g =
+        persistent_grid((const void *) k_elem_force_fused<true, V, false>, B, smem, items);
+    k_elem_force_fused<true, V, false><<<g, B, smem, s>>>(a, tab, e.nr, (float) e.rdr, 0.f, 0.f,
+                                                          erho_in, nodef);
+    persistent_grid((const void *) k_elem_force_fused<true, V, true>, B, smem, items);
+    k_elem_force_fused<true, V, true><<<g, B, smem, s>>>(a, tab, e.nr, (float) e.rdr, 0.f, 0.f,
+                                                         erho_in, nodef);
   } else {
-    const int g = persistent_grid((const void *) k_elem_force_fused<false, V>, B, smem, items);
-    k_elem_force_fused<false, V><<<g, B, smem, s>>>(a, nullptr, 0, 0.f, lj1, lj2, nullptr, nodef);
+    const int g =
+        persistent_grid((const void *) k_elem_force_fused<false, V, false>, B, smem, items);
+    k_elem_force_fused<false, V, false><<<g, B, smem, s>>>(a, nullptr, 0, 0.f, lj1, lj2, nullptr,
+                                                           nodef);
+    persistent_grid((const void *) k_elem_force_fused<false, V, true>, B, smem, items);
+    k_elem_force_fused<false, V, true><<<g, B, smem, s>>>(a, nullptr, 0, 0.f, lj1, lj2, nullptr,
+                                                          nodef);
   }
 }
 
@@ -2262,6 +2328,7 @@ void elem_fused(const MixedElems &m, const FusedTables &t, int pass, const float
   a.band_hi = m.band_hi;
   a.cutsq = m.cutsq;
   a.skip = m.skip;
+  a.band = t.band;
   a.lat = m.lat;
   a.fp4 = m.fp4;
   a.nrho = m.nrho;
@@ -2276,8 +2343,6 @@ void elem_fused(const MixedElems &m, const FusedTables &t, int pass, const float
   if (t.variant == 1) launch_fused<1>(a, pass, tab, e, table, lj1, lj2, erho_in, erho_out, nodef, s);
   else if (t.variant == 2)
     launch_fused<2>(a, pass, tab, e, table, lj1, lj2, erho_in, erho_out, nodef, s);
-
-
   else launch_fused<0>(a, pass, tab, e, table, lj1, lj2, erho_in, erho_out, nodef, s);
   check(cudaGetLastError(), "elem_fused");
 }

@@ -144,7 +144,9 @@ int cacg_run_host(cacg_handle h, int nsteps, double *x, double *v, double *nodex
    nonzero weight 27 1 if the last mixed element pass ran fused (one warp per
    element: every list entry references its row's own element) 28 graph
    launches of the device step loop so far ("tune loop device") 29 rebuild
-   decisions taken on the host so far (the device loop takes its own) */
+   decisions taken on the host so far (the device loop takes its own)
+   30 element passes re-run so far because a pair of the element fell in the
+   guard band of the FP32 cutoff decision (fused passes; decided in FP64) */
 int cacg_get_counts(cacg_handle h, long long *counts, int n);
 /* Atom::x/v/f (atom.h:40); all != 0 includes ghosts for x and tag */
 int cacg_get_atoms(cacg_handle h, int all, double *x, double *v, double *f, int *tag);

@@ -112,3 +112,64 @@ def test_fused_variants_bit_identical(cacg_lib, eam_file):
         s.close()
     for o in out[1:]:
         assert np.array_equal(o.view(np.int64), out[0].view(np.int64))
+
+
+def _band_run(m, cfg, eam_file, band, variant, steps=8, cull=True):
+    s = cacg.System(0)
+    try:
+        W.configure_system(s, m, cfg, eam_file)
+        s.set_precision(cacg.MIXED)
+        s.command(f"tune fused_variant {variant}")
+        s.command(f"tune cull {'yes' if cull else 'no'}")
+        if band is not None:
+            s.command(f"tune band {band}")
+        s.init()
+        s.setup()
+        s.neighbor_build()
+        s.neighbor_ebuild()
+        s.neighbor_nbuild()
+        s.pair_compute()
+        s.pair_ecompute()
+        s.run(steps)
+        return s.atoms(), s.elements(), s.counts()
+    finally:
+        s.close()
+
+
+def _lj_sample():
+    """LJ elements of 11 sites per edge; the skin (2.8) is the whole list
+    cutoff (Neighbor::init sets cutneighmax = skin, neighbor.cpp:297-374), as
+    in C1; no element sees another's sites, so the fused LJ pass runs."""
+    from cac_code_gb300 import lattice as L
+    m = L.make_slab_model(W.A_LJ, 1.0, (6, 22, 22), 11, 4, L.gauss_intp(11, False))
+    L.thermalize(m, 0.1, W.KB["lj"], W.MVV2E["lj"], 5)
+    L.remap_into_box(m)
+    cfg = dict(units="lj", boundary="f p p", pair="lj/cut", lj=(1.0, 1.0, 2.5), skin=2.8,
+               every=4, delay=0, check=True, dt=0.005, gauss_per_element=8)
+    return m, cfg
+
+
+@pytest.mark.parametrize("pot,variant", [("eam", 0), ("eam", 1), ("eam", 2), ("lj", 1)])
+def test_guard_band_reruns_are_exact(cacg_lib, eam_file, pot, variant):
+    """A pair of an element whose FP32 distance falls in the guard band has
+    the element re-run by the exact pass (FP64 decisions).  Widened to
+    cutsq (1 +- 0.1), the band holds a lattice shell (EAM Cu: the sixth at
+    +8 %; LJ: the fifth at +0.8 %, scanned with the displacement culling off),
+    so every element is re-run at every pass; decisions outside the default
+    band agree in FP32 and FP64, so positions and forces stay bit-identical to
+    the default band's over 8 steps."""
+    if pot == "eam":
+        m, cfg = W.c2_sample(seed=13)
+    else:
+        m, cfg = _lj_sample()
+    cull = pot == "eam"
+    a0, e0, c0 = _band_run(m, cfg, eam_file, None, 1, cull=cull)
+    a1, e1, c1 = _band_run(m, cfg, eam_file, 0.1, variant, cull=cull)
+    assert c0["elem_fused"] == 1 and c1["elem_fused"] == 1
+    passes = (2 if pot == "eam" else 1) * (1 + 8)
+    assert c1["band_reruns"] >= passes * c1["enlocal"], (c1["band_reruns"], c1["enlocal"])
+    assert c0["band_reruns"] < c1["band_reruns"]
+    for k in ("x", "v", "f"):
+        assert np.array_equal(a0[k], a1[k]), k
+    for k in ("nodex", "nodev", "nodef"):
+        assert np.array_equal(e0[k], e1[k]), k
