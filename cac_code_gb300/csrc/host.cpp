@@ -251,6 +251,15 @@ struct cacg_context {
   int fused_variant = 1;
   // half-width of the guard band of the mixed cutoff decisions ("tune band")
   float band_eps = 1.0e-4f;
+  // run_host: the fused element force pass in out_parts parts, each part's node
+  // velocities integrated and copied out while the next part's forces run
+  // ("tune out_parts 0..8", 0: 4 parts from 65,536 elements on, else 1);
+  // out_split is set while run_host enqueues such a step, parts_done /
+  // part_bounds report what the force pass did
+  int out_parts = 0, parts_done = 1;
+  bool out_split = false;
+  std::vector<int> part_bounds;
+  cudaEvent_t ev_nvpart[8] = {};
   // "tune fprime fp64|fp32": F'(rho) of the atoms in the mixed density pass
   // from the FP64 spline at the FP64 density (default), or from the FP32 copy
   bool fprime64 = true;
@@ -372,7 +381,8 @@ struct cacg_context {
   // events that order the copies against the step's two chains
   cudaStream_t cin = nullptr, cout_s = nullptr;
   cudaEvent_t ev_ain = nullptr, ev_nin = nullptr, ev_xout = nullptr, ev_nxout = nullptr,
-              ev_nvout = nullptr, ev_end = nullptr, ev_hstart = nullptr, ev_hdone = nullptr;
+              ev_nvout = nullptr, ev_end = nullptr, ev_hstart = nullptr, ev_hdone = nullptr,
+              ev_vout = nullptr;
   // graph of a whole single-step run_host call on pinned buffers
   cudaGraphExec_t hexec = nullptr;
   bool hgraph_valid = false, hgraph_ok = true;
@@ -565,6 +575,7 @@ struct cacg_context {
   void pair_ecompute();
   void nve_initial(int which = 3);
   void nve_final(int which = 3);
+  void nve_nodes_final_range(int b0, int b1);
   void compute_thermo(double *out);
   void compute_centro(double *out);
   void region_cmd(const std::vector<std::string> &a);
@@ -696,7 +707,10 @@ cacg_context::~cacg_context() {
   if (h_pin) cudaFreeHost(h_pin);
   if (fork_ev) cudaEventDestroy(fork_ev);
   if (hexec) cudaGraphExecDestroy(hexec);
-  for (cudaEvent_t e : {ev_ain, ev_nin, ev_xout, ev_nxout, ev_nvout, ev_end, ev_hstart, ev_hdone})
+  for (cudaEvent_t e : ev_nvpart)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e :
+       {ev_ain, ev_nin, ev_xout, ev_nxout, ev_nvout, ev_end, ev_hstart, ev_hdone, ev_vout})
     if (e) cudaEventDestroy(e);
   if (cin) cudaStreamDestroy(cin);
   if (cout_s) cudaStreamDestroy(cout_s);
@@ -884,6 +898,10 @@ void cacg_context::command(const std::string &raw) {
     //   decision on the device (with graphs on, no box deformation), or one
     //   graph launch per step without a decision and eager decision steps
     //   (host, the default)
+    // tune out_parts N: run_host splits the fused element force pass in N parts
+    //   and copies each part's node velocities out while the next part runs
+    //   (1 to 8; 0, the default: 4 from 65,536 elements on, else 1;
+    //   bit-identical)
     // tune band W: the guard band of the mixed cutoff decisions, cutsq (1 +- W)
     //   (default 1e-4, at most 0.1); a wider band only moves more pairs to the
     //   FP64 decision, the decisions and forces stay the same
@@ -915,6 +933,11 @@ void cacg_context::command(const std::string &raw) {
       const double w = numeric(a[1]);
       if (!(w >= 1.0e-4 && w <= 0.1)) fail(CACG_EINVAL, "tune band takes 1e-4 to 0.1");
       band_eps = (float) w;
+      invalidate_graph();
+    } else if (a[0] == "out_parts") {
+      const int v = inumeric(a[1]);
+      if (v < 0 || v > 8) fail(CACG_EINVAL, "tune out_parts takes 0 to 8");
+      out_parts = v;
       invalidate_graph();
     } else if (a[0] == "fused_variant") {
       const int v = inumeric(a[1]);
@@ -2718,6 +2741,30 @@ void cacg_context::pair_ecompute_mixed() {
     mixed::FusedTables ft{d_node_hl.p, d_nodex.p, d_int_off.p, d_inter_off.p, d_intp4.p,
                           d_spa_int.p, d_spa_inter.p, d_fjj.p, d_fjj_off.p, d_wn.p, maxlines,
                           fused_variant, d_spa_int_hl.p, d_frho_ds.p, d_wnf.p, d_band.p};
+    // the surrogate's nodal forces go in before the force pass, which skips
+    // (writes nothing for) the elements the surrogate evaluates
+    auto sur_write = [&] {
+      surrogate::write_forces(d_smean.p, d_far.p, d_sdue.p, d_sdue_n.p, nfar, d_skip.p, d_nodef.p, s);
+      launches++;
+    };
+    // the force pass, in parts when run_host copies the node velocities out
+    // part by part (each part's velocities integrated while the next part's
+    // forces run); the caller integrates the last part
+    auto force_parts = [&](auto pass) {
+      const int want = out_parts ? out_parts : enlocal >= 65536 ? 4 : 1;
+      const int parts = out_split ? std::max(1, std::min(want, enlocal)) : 1;
+      part_bounds.assign(parts + 1, enlocal);
+      for (int p = 0; p < parts; p++) part_bounds[p] = (int) ((long long) enlocal * p / parts);
+      for (int p = 0; p < parts; p++) {
+        pass(part_bounds[p], part_bounds[p + 1]);
+        launches += 2;  // the pass and its guard-band exact pass
+        if (p + 1 < parts) {
+          nve_nodes_final_range(part_bounds[p], part_bounds[p + 1]);
+          check(cudaEventRecord(ev_nvpart[p], s), "nodev part final");
+        }
+      }
+      parts_done = parts;
+    };
     if (pair_style == 1) {
       int a = 1 * (MAXT + 1) + 1;
       m.cutsq = ljtab.cutsq[a];
@@ -2728,12 +2775,14 @@ void cacg_context::pair_ecompute_mixed() {
         kmark(KT_SUR, 0);
         surrogate_predict(et);
         kmark(KT_SUR, 1);
+        sur_write();
       }
       kmark(KT_ELEM_FORCE, 0);
-      mixed::elem_fused(m, ft, 0, nullptr, et, (float) ljtab.lj1[a], (float) ljtab.lj2[a], nullptr,
-                        nullptr, d_nodef.p, s);
+      force_parts([&](int b0, int b1) {
+        mixed::elem_fused(m, ft, 0, nullptr, et, (float) ljtab.lj1[a], (float) ljtab.lj2[a],
+                          nullptr, nullptr, d_nodef.p, s, b0, b1);
+      });
       kmark(KT_ELEM_FORCE, 1);
-      launches += 2;  // the pass and its guard-band exact pass
     } else {
       m.cutsq = cutforcesq;
       m.cutsq_f = (float) cutforcesq;
@@ -2746,19 +2795,19 @@ void cacg_context::pair_ecompute_mixed() {
       kmark(KT_ELEM_RHO, 0);
       mixed::elem_fused(m, ft, 1, d_rhor_val4.p, et, 0.f, 0.f, nullptr, d_erho.p, nullptr, s);
       kmark(KT_ELEM_RHO, 1);
+      launches += 2;  // the pass and its guard-band exact pass
       if (use_sur) {
         kmark(KT_SUR, 0);
         surrogate_predict(et);
         kmark(KT_SUR, 1);
+        sur_write();
       }
       kmark(KT_ELEM_FORCE, 0);
-      mixed::elem_fused(m, ft, 2, d_ftab.p, et, 0.f, 0.f, d_erho.p, nullptr, d_nodef.p, s);
+      force_parts([&](int b0, int b1) {
+        mixed::elem_fused(m, ft, 2, d_ftab.p, et, 0.f, 0.f, d_erho.p, nullptr, d_nodef.p, s, b0,
+                          b1);
+      });
       kmark(KT_ELEM_FORCE, 1);
-      launches += 4;  // two passes, each with its guard-band exact pass
-    }
-    if (use_sur) {
-      surrogate::write_forces(d_smean.p, d_far.p, d_sdue.p, d_sdue_n.p, nfar, d_skip.p, d_nodef.p, s);
-      launches++;
     }
     return;
   }
@@ -3245,6 +3294,15 @@ void cacg_context::nve_initial(int which) {
   }
 }
 
+// the nodes' second half-step of elements [b0, b1)
+void cacg_context::nve_nodes_final_range(int b0, int b1) {
+  TypeScale a, e;
+  nve_scales(a, e);
+  launch_nve_nodes_final(d_nodev.p + 24 * (size_t) b0, d_nodef.p + 24 * (size_t) b0,
+                         d_etype.p + b0, e, b1 - b0, fast(), stream);
+  launches++;
+}
+
 void cacg_context::nve_final(int which) {
   TypeScale a, e;
   nve_scales(a, e);
@@ -3611,10 +3669,15 @@ void cacg_context::run_host(int n, double *x, double *v, double *nodex, double *
   if (!cin) check(cudaStreamCreateWithFlags(&cin, cudaStreamNonBlocking), "copy-in stream");
   if (!cout_s) check(cudaStreamCreateWithFlags(&cout_s, cudaStreamNonBlocking), "copy-out stream");
   for (cudaEvent_t *e : {&ev_ain, &ev_nin, &ev_xout, &ev_nxout, &ev_nvout, &ev_end, &ev_hstart,
-                         &ev_hdone})
+                         &ev_hdone, &ev_vout})
     if (!*e) check(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "copy event");
+  for (cudaEvent_t &e : ev_nvpart)
+    if (!e) check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "copy event");
   const bool early_nodes = last_plain && post_fixes.empty();
   const bool oob_read = d_misc.p && oob_zeroed;
+  // the smaller state goes in first: its chain starts while the other's is in
+  // flight (the link moves ~0.2 TB/s each way, a step's state in is ~1 ms)
+  const bool atoms_first = xb <= nb;
   // inputs, the last step with the copies hooked in, outputs; the copy
   // streams fork from the handle's stream and join it again, so the whole
   // call can be captured as one graph
@@ -3623,14 +3686,23 @@ void cacg_context::run_host(int n, double *x, double *v, double *nodex, double *
     check(cudaStreamWaitEvent(cin, ev_hstart, 0), "copy-in fork");
     check(cudaStreamWaitEvent(cout_s, ev_hstart, 0), "copy-out fork");
     if (pending) {
-      // the element state first, so that the element chain runs while the
-      // atom state (six times larger) is still in flight
-      check(cudaMemcpyAsync(d_nodex.p, nodex, nb, cudaMemcpyHostToDevice, cin), "nodex in");
-      check(cudaMemcpyAsync(d_nodev.p, nodev, nb, cudaMemcpyHostToDevice, cin), "nodev in");
-      check(cudaEventRecord(ev_nin, cin), "nodes in");
-      check(cudaMemcpyAsync(d_stage.p, x, xb, cudaMemcpyHostToDevice, cin), "x in");
-      check(cudaMemcpyAsync(d_v.p, v, xb, cudaMemcpyHostToDevice, cin), "v in");
-      check(cudaEventRecord(ev_ain, cin), "atoms in");
+      auto nodes_in = [&] {
+        check(cudaMemcpyAsync(d_nodex.p, nodex, nb, cudaMemcpyHostToDevice, cin), "nodex in");
+        check(cudaMemcpyAsync(d_nodev.p, nodev, nb, cudaMemcpyHostToDevice, cin), "nodev in");
+        check(cudaEventRecord(ev_nin, cin), "nodes in");
+      };
+      auto atoms_in = [&] {
+        check(cudaMemcpyAsync(d_stage.p, x, xb, cudaMemcpyHostToDevice, cin), "x in");
+        check(cudaMemcpyAsync(d_v.p, v, xb, cudaMemcpyHostToDevice, cin), "v in");
+        check(cudaEventRecord(ev_ain, cin), "atoms in");
+      };
+      if (atoms_first) {
+        atoms_in();
+        nodes_in();
+      } else {
+        nodes_in();
+        atoms_in();
+      }
     } else {
       check(cudaEventRecord(ev_ain, cin), "no inputs");
       check(cudaEventRecord(ev_nin, cin), "no inputs");
@@ -3670,40 +3742,69 @@ void cacg_context::run_host(int n, double *x, double *v, double *nodex, double *
             forward_comm(1);
             pair_compute_pass(1);
             pair_compute_pass(2);
+            if (early_nodes) {  // the atoms' velocities go out while the elements run
+              nve_final(1);
+              check(cudaEventRecord(ev_vout, stream), "v final");
+            }
           },
           [&] {
             check(cudaStreamWaitEvent(stream, ev_nin, 0), "wait nodes in");
             nve_initial(2);
             check(cudaEventRecord(ev_nxout, stream), "nodex final");
             forward_comm(2);
-            pair_ecompute();
+            out_split = early_nodes;
+            parts_done = 1;
+            try {
+              pair_ecompute();
+            } catch (...) {
+              out_split = false;
+              throw;
+            }
+            out_split = false;
             if (early_nodes) {  // no fix acts between the force passes and the integration
-              nve_final(2);
+              if (parts_done > 1) nve_nodes_final_range(part_bounds[parts_done - 1], enlocal);
+              else nve_final(2);
               check(cudaEventRecord(ev_nvout, stream), "nodev final");
             }
           },
           true);
-      if (early_nodes) {
-        nve_final(1);
-      } else {
+      if (!early_nodes) {
         post_force();
         nve_final();
+        check(cudaEventRecord(ev_vout, stream), "v final");
       }
       eager_since++;
     }
     check(cudaEventRecord(ev_end, stream), "step end");
-    // outputs
+    // outputs, once the inputs are in (an early output would share the link
+    // with the inputs the element chain waits for)
+    check(cudaStreamWaitEvent(cout_s, ev_ain, 0), "wait atoms in");
+    check(cudaStreamWaitEvent(cout_s, ev_nin, 0), "wait nodes in");
     check(cudaStreamWaitEvent(cout_s, ev_xout, 0), "wait x final");
     launch_unpack4to3(d_x.p, d_stage.p, nlocal, cout_s);
     check(cudaMemcpyAsync(x, d_stage.p, xb, cudaMemcpyDeviceToHost, cout_s), "x out");
     check(cudaStreamWaitEvent(cout_s, ev_nxout, 0), "wait nodex final");
     check(cudaMemcpyAsync(nodex, d_nodex.p, nb, cudaMemcpyDeviceToHost, cout_s), "nodex out");
+    auto v_out = [&] {
+      check(cudaStreamWaitEvent(cout_s, last_plain ? ev_vout : ev_end, 0), "wait v final");
+      check(cudaMemcpyAsync(v, d_v.p, xb, cudaMemcpyDeviceToHost, cout_s), "v out");
+    };
+    // the chain that ends first has its velocities copied first: the atoms'
+    // when their state went in first
+    if (!early_nodes || atoms_first) v_out();
     if (early_nodes) {
-      check(cudaStreamWaitEvent(cout_s, ev_nvout, 0), "wait nodev final");
-      check(cudaMemcpyAsync(nodev, d_nodev.p, nb, cudaMemcpyDeviceToHost, cout_s), "nodev out");
+      for (int p = 0; p < parts_done; p++) {
+        const size_t b0 = 24 * (size_t) (parts_done > 1 ? part_bounds[p] : 0);
+        const size_t b1 = 24 * (size_t) (p + 1 < parts_done ? part_bounds[p + 1] : enlocal);
+        check(cudaStreamWaitEvent(cout_s, p + 1 < parts_done ? ev_nvpart[p] : ev_nvout, 0),
+              "wait nodev final");
+        check(cudaMemcpyAsync(nodev + b0, d_nodev.p + b0, sizeof(double) * (b1 - b0),
+                              cudaMemcpyDeviceToHost, cout_s),
+              "nodev out");
+      }
+      if (!atoms_first) v_out();
     }
     check(cudaStreamWaitEvent(cout_s, ev_end, 0), "wait step end");
-    check(cudaMemcpyAsync(v, d_v.p, xb, cudaMemcpyDeviceToHost, cout_s), "v out");
     if (!early_nodes)
       check(cudaMemcpyAsync(nodev, d_nodev.p, nb, cudaMemcpyDeviceToHost, cout_s), "nodev out");
     if (oob_read)

@@ -415,9 +415,12 @@ struct FusedTables {
                               // far, then the listed elements (3 + nlocal_e ints, zeroed once)
 };
 bool fused_fits(int nr, int nrho);
+// elements [e_begin, e_end) (e_end < 0: all local elements); the guard-band
+// exact pass runs after each launch
 void elem_fused(const MixedElems &m, const FusedTables &t, int pass, const float4 *tab,
                 const EamTables &e, float lj1, float lj2, const double *erho_in,
-                double *erho_out, double *nodef, cudaStream_t s);
+                double *erho_out, double *nodef, cudaStream_t s, int e_begin = 0,
+                int e_end = -1);
 // list entries that reference a site of another element than their row's
 long long self_check(const int *row_start, const int *ent, const int *row_elem, int nrows,
                      const Lattice &lat, int maxlines, unsigned long long *scratch,

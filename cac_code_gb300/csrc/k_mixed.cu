@@ -1435,6 +1435,7 @@ struct FusedArgs {
   double cutsq;
   const unsigned char *skip;   // elements the surrogate evaluates
   int *band;                   // the guard-band list (band_list)
+  int e_begin, e_end;          // the elements of this launch (the exact pass: the list)
   Lattice lat;
   const float4 *fp4;           // FP32 F' spline (sites)
   int nrho;
@@ -1753,7 +1754,7 @@ template <int V, bool FIX>
 __global__ void __launch_bounds__(fused_block(V), 1)
 k_elem_rho_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rdr,
                  double *__restrict__ erho) {
-  const int ne = FIX ? min(a.band[0], a.nlocal_e) : a.nlocal_e;
+  const int ne = FIX ? min(a.band[0], a.nlocal_e) : a.e_end - a.e_begin;
   if (FIX && ne == 0) return;  // the whole grid (the count is the same for every block)
   extern __shared__ float4 smem[];
   float4 *s_tab = smem;
@@ -1770,7 +1771,7 @@ k_elem_rho_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rdr,
   // the next element's nodes, type and first row are loaded while this
   // element's rows run
   float2 pn = make_float2(0.f, 0.f);
-  int pty = 0, prf = 0, pe = gw;
+  int pty = 0, prf = 0, pe = a.e_begin + gw;
   if (gw < ne) {
     if (FIX) pe = a.band[BAND_LIST + gw];
     if (lane < 24) pn = __ldg(a.node_hl + 24 * (size_t) pe + lane);
@@ -1778,11 +1779,11 @@ k_elem_rho_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rdr,
     prf = __ldg(a.row_first + pe);
   }
   for (int i = gw; i < ne; i += nw) {
-    const int e = FIX ? pe : i, ty = pty, rfirst = prf;
+    const int e = FIX ? pe : a.e_begin + i, ty = pty, rfirst = prf;
     if (lane < 24) s_nx[lane] = pn;
     const int in = i + nw;
     if (in < ne) {
-      const int en = FIX ? a.band[BAND_LIST + in] : in;
+      const int en = FIX ? a.band[BAND_LIST + in] : a.e_begin + in;
       if (FIX) pe = en;
       if (lane < 24) pn = __ldg(a.node_hl + 24 * (size_t) en + lane);
       pty = __ldg(a.etype + en);
@@ -1821,7 +1822,7 @@ template <bool EAM, int V, bool FIX>
 __global__ void __launch_bounds__(fused_block(V), 1)
 k_elem_force_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rdr, float lj1,
                    float lj2, const double *__restrict__ erho, double *__restrict__ nodef) {
-  const int ne = FIX ? min(a.band[0], a.nlocal_e) : a.nlocal_e;
+  const int ne = FIX ? min(a.band[0], a.nlocal_e) : a.e_end - a.e_begin;
   if (FIX && ne == 0) return;  // the whole grid (the count is the same for every block)
   extern __shared__ float4 smem[];
   float4 *s_tab = smem;
@@ -1844,7 +1845,7 @@ k_elem_force_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rd
   // the next element's nodes, type and first row are loaded while this
   // element's rows run
   float2 pn = make_float2(0.f, 0.f);
-  int pty = 0, prf = 0, pe = gw;
+  int pty = 0, prf = 0, pe = a.e_begin + gw;
   if (gw < ne) {
     if (FIX) pe = a.band[BAND_LIST + gw];
     if (lane < 24) pn = __ldg(a.node_hl + 24 * (size_t) pe + lane);
@@ -1852,11 +1853,11 @@ k_elem_force_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rd
     prf = __ldg(a.row_first + pe);
   }
   for (int i = gw; i < ne; i += nw) {
-    const int e = FIX ? pe : i, ty = pty, rfirst = prf;
+    const int e = FIX ? pe : a.e_begin + i, ty = pty, rfirst = prf;
     const float2 cn = pn;
     const int in = i + nw;
     if (in < ne) {
-      const int en = FIX ? a.band[BAND_LIST + in] : in;
+      const int en = FIX ? a.band[BAND_LIST + in] : a.e_begin + in;
       if (FIX) pe = en;
       if (lane < 24) pn = __ldg(a.node_hl + 24 * (size_t) en + lane);
       pty = __ldg(a.etype + en);
@@ -2256,7 +2257,7 @@ static void launch_fused(const FusedArgs &a, int pass, const float4 *tab, const 
                          double *erho_out, double *nodef, cudaStream_t s) {
   constexpr int B = fused_block(V);
   const size_t smem = table + sizeof(float) * FUSED_WARP_FLOATS * (B / 32);
-  const long long items = (long long) a.nlocal_e * 32;
+  const long long items = (long long) (a.e_end - a.e_begin) * 32;
   // the pass, then the exact pass over the elements it listed (a grid of the
   // same shape; it returns at once when the list is empty)
   if (pass == 1) {
@@ -2294,9 +2295,12 @@ bool fused_fits(int nr, int nrho) {
 
 void elem_fused(const MixedElems &m, const FusedTables &t, int pass, const float4 *tab,
                 const EamTables &e, float lj1, float lj2, const double *erho_in, double *erho_out,
-                double *nodef, cudaStream_t s) {
-  if (m.nlocal_e <= 0) return;
+                double *nodef, cudaStream_t s, int e_begin, int e_end) {
+  if (e_end < 0) e_end = m.nlocal_e;
+  if (m.nlocal_e <= 0 || e_begin >= e_end) return;
   FusedArgs a{};
+  a.e_begin = e_begin;
+  a.e_end = e_end;
   a.node_hl = t.node_hl;
   a.nodex = t.nodex;
   a.etype = m.etype;

@@ -183,6 +183,54 @@ def test_run_host_matches_device_resident_run(cacg_lib, precision, pinned):
         b.close()
 
 
+@pytest.mark.parametrize("parts", [1, 3])
+def test_run_host_element_heavy_state(cacg_lib, tmp_path, parts):
+    """As above with more node state than atom state (a slab of two cells
+    between forty element layers a side, the C5 proportions): the atom state
+    goes in first and the atoms' velocities go out while the elements run;
+    with "tune out_parts 3" the element force pass runs in three parts whose
+    node velocities are integrated and copied out part by part.  The
+    trajectory is still the device-resident one bit for bit."""
+    from cac_code_gb300 import workloads as W
+    eam = W.write_eam(str(tmp_path / "Cu.eam"))
+    m, cfg = W.c2_eam(cells=(2, 22, 22), layers=40, seed=7)
+    cfg = dict(cfg, every=10, check=True)
+    assert m.nelements * 192 > m.natoms * 24
+
+    def prepared():
+        s = cacg_lib.System(0)
+        W.configure_system(s, m, cfg, eam)
+        s.set_precision(cacg_lib.MIXED)
+        s.command(f"tune out_parts {parts}")
+        s.init()
+        s.setup()
+        s.neighbor_build()
+        s.pair_compute()
+        s.neighbor_ebuild()
+        s.neighbor_nbuild()
+        s.pair_ecompute()
+        return s
+
+    a, b = prepared(), prepared()
+    try:
+        x0, e0 = a.atoms(), a.elements()
+        hx, hv = _host_array(x0["x"], True), _host_array(x0["v"], True)
+        hnx, hnv = _host_array(e0["nodex"], True), _host_array(e0["nodev"], True)
+        for _ in range(23):
+            a.run_host(1, hx, hv, hnx, hnv)
+        a.run_host(7, hx, hv, hnx, hnv)
+        b.run(30)
+        xb, eb = b.atoms(), b.elements()
+        assert np.array_equal(hx, xb["x"])
+        assert np.array_equal(hv, xb["v"])
+        assert np.array_equal(hnx, eb["nodex"])
+        assert np.array_equal(hnv, eb["nodev"])
+        assert a.counts()["rebuilds"] == b.counts()["rebuilds"]
+    finally:
+        a.close()
+        b.close()
+
+
 def test_union_variant_agrees_with_direct_passes(cacg_lib):
     """`tune union yes` stages each warp's neighbor union in shared memory and
     walks the build-order lists (the direct passes walk the reordered ones, so
