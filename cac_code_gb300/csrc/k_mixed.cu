@@ -1678,12 +1678,16 @@ __device__ __forceinline__ bool fused_row(const FusedArgs &a, const FusedLat &g,
         py += dy * fpair;
         pz += dz * fpair;
       }
-      if ((++cnt & (CHUNK - 1)) == 0) {
-        acc.add(part);
-        fx.add(px);
-        fy.add(py);
-        fz.add(pz);
-        part = px = py = pz = 0.f;
+      if ((++cnt & (CHUNK - 1)) == 0) {  // the pass's own sums only
+        if (DENSITY) {
+          acc.add(part);
+          part = 0.f;
+        } else {
+          fx.add(px);
+          fy.add(py);
+          fz.add(pz);
+          px = py = pz = 0.f;
+        }
       }
     }
   }
