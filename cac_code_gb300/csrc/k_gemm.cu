@@ -121,8 +121,20 @@ __device__ __forceinline__ void tmem_ld16(unsigned taddr, float (&v)[16]) {
   for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
-__device__ __forceinline__ float sigmoidf_(float z) { return __fdividef(1.f, 1.f + __expf(-z)); }
-__device__ __forceinline__ float siluf_(float z) { return __fdividef(z, 1.f + __expf(-z)); }
+// sigma(z) = (1 + tanh(z / 2)) / 2 and silu(z) = z sigma(z) = h + h tanh(h), h = z / 2, on
+// the hardware tanh (tanh.approx.f32: one special-function instruction against two for
+// exp and reciprocal; its error, about 2^-11, is below the bf16 rounding of the
+// activations, 2^-9)
+__device__ __forceinline__ float tanh_approx(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float sigmoidf_(float z) { return fmaf(0.5f, tanh_approx(0.5f * z), 0.5f); }
+__device__ __forceinline__ float siluf_(float z) {
+  const float h = 0.5f * z;
+  return fmaf(h, tanh_approx(h), h);
+}
 
 struct Epi {
   int kind;
