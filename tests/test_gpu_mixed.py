@@ -1,7 +1,9 @@
 """Mixed precision against the reference's FP64 forces: relative force error
-<= 1e-4.  Mixed mode evaluates pair terms in FP32, F'(rho) of atoms and element
-sites in FP32 (of integration points in FP64), sums chunks of 8 pairs in FP32
-and the chunks as FP32 double-single pairs, and integrates in FP64.
+<= 1e-4.  Mixed mode evaluates pair terms in FP32; F'(rho) of atoms from the
+FP64 spline at the FP64 density ("tune fprime fp64", the default; "fp32" takes
+the FP32 spline), of integration points from the FP64 spline arithmetic carried
+out in double-single, of element sites in FP32; it sums chunks of 8 pairs in
+FP32 and the chunks as FP32 double-single pairs, and integrates in FP64.
 
 Errors are measured two ways on every atom and node: RMS of |df| over RMS of |f|
 and max |df| over max |f|.  The neighbor lists are the FP64 lists (identical).
