@@ -215,6 +215,7 @@ struct cacg_context {
   DBuf<float> d_wn;             // weight x shape function per type row and node (FP32)
   DBuf<float> d_wnf;            // the same for the rows of nonzero weight, per type in order
   DBuf<int> d_band;             // elements with a guard-band pair: count, blocks done, list
+  DBuf<float4> d_lat_rec;       // per type 1/(n_a-1), 1/(n_b-1), 1/(n_c-1), 1/n_b
   int fstride = 1;
   // mixed precision, per row: packed and double-single integration points,
   // F'(rho) of the force rows; the integration-point lists row-major
@@ -649,6 +650,7 @@ cacg_context::~cacg_context() {
   d_wn.release();
   d_wnf.release();
   d_band.release();
+  d_lat_rec.release();
   d_ip_q.release();
   d_ip_h.release();
   d_ip_l.release();
@@ -1723,6 +1725,15 @@ void cacg_context::element_tables() {
     max_naz = std::max(max_naz, nae[t][2]);
   }
   upload(d_nae, nae3, s);
+  // per type 1 / (n_a - 1), 1 / (n_b - 1), 1 / (n_c - 1), 1 / n_b for the fused
+  // element passes (FP32 division, correctly rounded, as the kernels would do it)
+  std::vector<float4> rec(MAXT + 1, make_float4(0.f, 0.f, 0.f, 0.f));
+  for (int t = 0; t <= MAXT; t++) {
+    const int na = nae3[3 * t], nb = nae3[3 * t + 1], nc = nae3[3 * t + 2];
+    rec[t] = make_float4(na > 1 ? 1.0f / (float) (na - 1) : 0.f, nb > 1 ? 1.0f / (float) (nb - 1) : 0.f,
+                         nc > 1 ? 1.0f / (float) (nc - 1) : 0.f, 1.0f / (float) nb);
+  }
+  upload(d_lat_rec, rec, s);
   // the fractions k / (n - 1) of each lattice axis as double-single floats
   fstride = 1;
   for (int t = 1; t <= netypes; t++)
@@ -2740,7 +2751,8 @@ void cacg_context::pair_ecompute_mixed() {
     }
     mixed::FusedTables ft{d_node_hl.p, d_nodex.p, d_int_off.p, d_inter_off.p, d_intp4.p,
                           d_spa_int.p, d_spa_inter.p, d_fjj.p, d_fjj_off.p, d_wn.p, maxlines,
-                          fused_variant, d_spa_int_hl.p, d_frho_ds.p, d_wnf.p, d_band.p};
+                          fused_variant, d_spa_int_hl.p, d_frho_ds.p, d_wnf.p, d_band.p,
+                          d_lat_rec.p};
     // the surrogate's nodal forces go in before the force pass, which skips
     // (writes nothing for) the elements the surrogate evaluates
     auto sur_write = [&] {

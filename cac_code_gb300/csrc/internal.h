@@ -413,6 +413,7 @@ struct FusedTables {
   const float *wnf;           // wn of the rows of nonzero weight, per type in fjj order
   int *band;                  // guard-band list: count, blocks done, elements re-run so
                               // far, then the listed elements (3 + nlocal_e ints, zeroed once)
+  const float4 *lat_rec;      // per type 1/(n_a-1), 1/(n_b-1), 1/(n_c-1), 1/n_b
 };
 bool fused_fits(int nr, int nrho);
 // elements [e_begin, e_end) (e_end < 0: all local elements); the guard-band

@@ -1436,6 +1436,7 @@ struct FusedArgs {
   const unsigned char *skip;   // elements the surrogate evaluates
   int *band;                   // the guard-band list (band_list)
   int e_begin, e_end;          // the elements of this launch (the exact pass: the list)
+  const float4 *lat_rec;       // per type 1/(n_a-1), 1/(n_b-1), 1/(n_c-1), 1/n_b
   Lattice lat;
   const float4 *fp4;           // FP32 F' spline (sites)
   int nrho;
@@ -1705,15 +1706,17 @@ __device__ __forceinline__ bool fused_row(const FusedArgs &a, const FusedLat &g,
   return band;
 }
 
-__device__ __forceinline__ FusedLat fused_lat(const Lattice &lat, int ty) {
+// the type's lattice sizes and their reciprocals (from the host's table: no
+// division per element)
+__device__ __forceinline__ FusedLat fused_lat(const Lattice &lat, const float4 *rec, int ty) {
   FusedLat g;
-  const int nax = lat.nae[3 * ty], nay = lat.nae[3 * ty + 1], naz = lat.nae[3 * ty + 2];
-  g.nay = nay;
-  g.naz = naz;
-  g.ia = nax > 1 ? 1.0f / (float) (nax - 1) : 0.f;
-  g.ib = nay > 1 ? 1.0f / (float) (nay - 1) : 0.f;
-  g.ic = naz > 1 ? 1.0f / (float) (naz - 1) : 0.f;
-  g.inay = 1.0f / (float) nay;
+  g.nay = __ldg(lat.nae + 3 * ty + 1);
+  g.naz = __ldg(lat.nae + 3 * ty + 2);
+  const float4 r = __ldg(rec + ty);
+  g.ia = r.x;
+  g.ib = r.y;
+  g.ic = r.z;
+  g.inay = r.w;
   return g;
 }
 
@@ -1793,7 +1796,7 @@ k_elem_rho_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rdr,
       pty = __ldg(a.etype + en);
       prf = __ldg(a.row_first + en);
     }
-    const FusedLat g = fused_lat(a.lat, ty);
+    const FusedLat g = fused_lat(a.lat, a.lat_rec, ty);
     __syncwarp();
     fused_coeffs(s_nx, lane, s_k, V != 0);
     __syncwarp();
@@ -1873,7 +1876,7 @@ k_elem_force_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rd
       const ds d = ds_of_double(__ldg(erho + NPE * (size_t) e + (lane - 24)));
       s_erds[lane - 24] = make_float2(d.h, d.l);
     }
-    const FusedLat g = fused_lat(a.lat, ty);
+    const FusedLat g = fused_lat(a.lat, a.lat_rec, ty);
     const int f0 = a.fjj_off[ty], nf = a.fjj_off[ty + 1] - f0;
     __syncwarp();
     fused_coeffs(s_nx, lane, s_k, V != 0);
@@ -2305,6 +2308,7 @@ void elem_fused(const MixedElems &m, const FusedTables &t, int pass, const float
   FusedArgs a{};
   a.e_begin = e_begin;
   a.e_end = e_end;
+  a.lat_rec = t.lat_rec;
   a.node_hl = t.node_hl;
   a.nodex = t.nodex;
   a.etype = m.etype;
