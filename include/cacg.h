@@ -118,8 +118,11 @@ int cacg_put_nodes(cacg_handle h, const double *nodex, const double *nodev); /* 
    nodex, nodev [enlocal][8][3] are copied in, nsteps steps run, and the new
    state is copied back into the same buffers before the call returns (pinned
    buffers give the full link bandwidth).  In mixed precision the last step's
-   copies overlap its computation (element state in first, positions out once
-   the step's initial integration is done), and a single-step call on pinned
+   copies overlap its computation (the smaller of the atom and node states in
+   first, outputs once every input is in: positions after the step's initial
+   integration, velocities as each chain integrates them, the node velocities
+   part by part behind the element force pass, "tune out_parts"), and a
+   single-step call on pinned
    buffers used in the previous call replays one captured graph of the whole
    call (with cacg_set_graphs on); the results equal cacg_put_atoms +
    cacg_put_nodes + cacg_run + cacg_get_atoms + cacg_get_elements. */
