@@ -3632,16 +3632,18 @@ void cacg_context::force_passes(long long b) {
 // nodev of the owned elements are copied in from the caller's buffers, the
 // steps run, and the new state is copied back before the call returns.  When
 // the last step is a mixed step (two chains), its copies overlap the
-// computation.  In a step without a rebuild decision the element inputs are
-// copied first and the element chain runs on them while the atom inputs are
-// still in flight (at C2 it finishes within that window, and the atom chain
-// then has the GPU to itself); positions go out as soon as the step's initial
+// computation.  In a step without a rebuild decision the smaller of the two
+// states (atoms or nodes) is copied in first and its chain runs while the
+// other is still in flight; outputs start once every input is in (the link
+// carries both directions at once, but an early output slows the input the
+// other chain waits for): positions as soon as the step's initial
 // integration has moved them (nothing later in such a step writes owned
-// positions), node velocities after the element chain's final integration
-// when no fix acts on the forces, atom velocities last.  A step with a
-// rebuild decision waits for all its inputs (the decision reads the new
-// positions on the host) and sends positions out after the decision, while
-// its force passes run.  Otherwise the copies and the steps run in order.
+// positions), atom velocities when the atom chain has integrated them, and,
+// when no fix acts on the forces, node velocities part by part as the
+// element force pass finishes each part of the elements (out_parts).  A step
+// with a rebuild decision waits for all its inputs (the decision reads the
+// new positions on the host) and sends positions out after the decision,
+// while its force passes run.  Otherwise the copies and the steps run in order.
 // Results are those of the same steps run on device-resident state.
 void cacg_context::run_host(int n, double *x, double *v, double *nodex, double *nodev) {
   if (n < 1) fail(CACG_EINVAL, "run_host: at least one step");
