@@ -383,7 +383,7 @@ struct cacg_context {
   cudaStream_t cin = nullptr, cout_s = nullptr;
   cudaEvent_t ev_ain = nullptr, ev_nin = nullptr, ev_xout = nullptr, ev_nxout = nullptr,
               ev_nvout = nullptr, ev_end = nullptr, ev_hstart = nullptr, ev_hdone = nullptr,
-              ev_vout = nullptr;
+              ev_vout = nullptr, ev_acheck = nullptr, ev_apass = nullptr;
   // graph of a whole single-step run_host call on pinned buffers
   cudaGraphExec_t hexec = nullptr;
   bool hgraph_valid = false, hgraph_ok = true;
@@ -711,8 +711,8 @@ cacg_context::~cacg_context() {
   if (hexec) cudaGraphExecDestroy(hexec);
   for (cudaEvent_t e : ev_nvpart)
     if (e) cudaEventDestroy(e);
-  for (cudaEvent_t e :
-       {ev_ain, ev_nin, ev_xout, ev_nxout, ev_nvout, ev_end, ev_hstart, ev_hdone, ev_vout})
+  for (cudaEvent_t e : {ev_ain, ev_nin, ev_xout, ev_nxout, ev_nvout, ev_end, ev_hstart, ev_hdone,
+                        ev_vout, ev_acheck, ev_apass})
     if (e) cudaEventDestroy(e);
   if (cin) cudaStreamDestroy(cin);
   if (cout_s) cudaStreamDestroy(cout_s);
@@ -3683,11 +3683,14 @@ void cacg_context::run_host(int n, double *x, double *v, double *nodex, double *
   if (!cin) check(cudaStreamCreateWithFlags(&cin, cudaStreamNonBlocking), "copy-in stream");
   if (!cout_s) check(cudaStreamCreateWithFlags(&cout_s, cudaStreamNonBlocking), "copy-out stream");
   for (cudaEvent_t *e : {&ev_ain, &ev_nin, &ev_xout, &ev_nxout, &ev_nvout, &ev_end, &ev_hstart,
-                         &ev_hdone, &ev_vout})
+                         &ev_hdone, &ev_vout, &ev_acheck, &ev_apass})
     if (!*e) check(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "copy event");
   for (cudaEvent_t &e : ev_nvpart)
     if (!e) check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "copy event");
   const bool early_nodes = last_plain && post_fixes.empty();
+  // a step with a rebuild decision on distances runs its atom chain ahead of the
+  // decision (see below)
+  const bool ahead = !last_plain && dist_check != 0 && post_fixes.empty();
   const bool oob_read = d_misc.p && oob_zeroed;
   // the smaller state goes in first: its chain starts while the other's is in
   // flight (the link moves ~0.2 TB/s each way, a step's state in is ~1 ms)
@@ -3723,7 +3726,99 @@ void cacg_context::run_host(int n, double *x, double *v, double *nodex, double *
     }
     ran = true;
     ntimestep++;
-    if (!last_plain) {
+    bool early = early_nodes;  // velocities out as each chain integrates them
+    if (ahead) {
+      // Neighbor::decide (neighbor.cpp:1150-1163) on this step's integrated
+      // positions, with the atom chain run ahead of it: the atoms' initial
+      // integration and distance check, then their ghost update and force
+      // passes, go on while the node state is still in flight and the host
+      // waits for the two checks (the main stream only).  Without a rebuild
+      // the step goes on as a plain one; with one, the atoms' ghost update
+      // and forces are discarded (the rebuild re-makes the ghosts, the lists
+      // and every force), so the trajectory is the one decide() gives.
+      ago++;
+      host_decisions++;
+      d_misc.ensure(32, stream);
+      check(cudaMemsetAsync(d_misc.p + 6, 0, sizeof(int), stream), "memset");
+      BoxWrap box{};
+      for (int d = 0; d < 3; d++) {
+        box.lo[d] = lo[d];
+        box.hi[d] = hi[d];
+        box.periodic[d] = periodic[d];
+      }
+      if (!astream) forked([] {}, [] {});  // creates the atom stream and its events
+      check(cudaEventRecord(fork_ev, stream), "fork");
+      check(cudaStreamWaitEvent(astream, fork_ev, 0), "fork wait");
+      const cudaStream_t main_stream = stream;
+      stream = astream;
+      try {
+        check(cudaStreamWaitEvent(stream, ev_ain, 0), "wait atoms in");
+        if (pending) {
+          launch_pack3to4(d_stage.p, d_x.p, nlocal, stream);
+          launches++;
+        }
+        nve_initial(1);
+        launch_check_distance(d_x.p, d_xhold.p, nlocal, nullptr, nullptr, 0, nullptr, box,
+                              triggersq, d_misc.p + 6, stream);
+        check(cudaEventRecord(ev_acheck, stream), "atom check");
+        forward_comm(1);
+        pair_compute_pass(1);
+        pair_compute_pass(2);
+        check(cudaEventRecord(ev_apass, stream), "atom passes");
+      } catch (...) {
+        stream = main_stream;
+        throw;
+      }
+      stream = main_stream;
+      check(cudaStreamWaitEvent(stream, ev_nin, 0), "wait nodes in");
+      nve_initial(2);
+      launch_check_distance(nullptr, nullptr, 0, d_nodex.p, d_nodexhold.p, enlocal,
+                            enlocal ? d_ex.p : nullptr, box, triggersq, d_misc.p + 6, stream);
+      check(cudaStreamWaitEvent(stream, ev_acheck, 0), "wait atom check");
+      check(cudaMemcpyAsync(h_pin + 6, d_misc.p + 6, sizeof(int), cudaMemcpyDeviceToHost, stream),
+            "flag");
+      launches += 2;
+      sync();
+      // a wrap alone needs no rebuild (the reference's check tests distances only)
+      const int nflag = (h_pin[6] & 3) ? h_pin[6] : 0;
+      check(cudaEventRecord(ev_xout, stream), "x final");  // (after the decision)
+      check(cudaEventRecord(ev_nxout, stream), "nodex final");
+      if (nflag == 0) {
+        early = true;
+        forward_comm(2);
+        out_split = true;
+        parts_done = 1;
+        try {
+          pair_ecompute();
+        } catch (...) {
+          out_split = false;
+          throw;
+        }
+        out_split = false;
+        if (parts_done > 1) nve_nodes_final_range(part_bounds[parts_done - 1], enlocal);
+        else nve_final(2);
+        check(cudaEventRecord(ev_nvout, stream), "nodev final");
+        stream = astream;
+        try {
+          nve_final(1);
+          check(cudaEventRecord(ev_vout, stream), "v final");
+          check(cudaEventRecord(join_ev, stream), "join");
+        } catch (...) {
+          stream = main_stream;
+          throw;
+        }
+        stream = main_stream;
+        check(cudaStreamWaitEvent(stream, join_ev, 0), "join wait");
+      } else {
+        check(cudaStreamSynchronize(astream), "atom chain");
+        rebuild(nflag);
+        check(cudaEventRecord(ev_xout, stream), "x final");
+        check(cudaEventRecord(ev_nxout, stream), "nodex final");
+        force_passes(-1);
+        post_force();
+        nve_final();
+      }
+    } else if (!last_plain) {
       // Neighbor::decide reads this step's integrated positions on the host,
       // so the step waits for all its inputs; positions go out after the
       // decision (a rebuild wraps them into the box first)
@@ -3800,13 +3895,13 @@ void cacg_context::run_host(int n, double *x, double *v, double *nodex, double *
     check(cudaStreamWaitEvent(cout_s, ev_nxout, 0), "wait nodex final");
     check(cudaMemcpyAsync(nodex, d_nodex.p, nb, cudaMemcpyDeviceToHost, cout_s), "nodex out");
     auto v_out = [&] {
-      check(cudaStreamWaitEvent(cout_s, last_plain ? ev_vout : ev_end, 0), "wait v final");
+      check(cudaStreamWaitEvent(cout_s, last_plain || early ? ev_vout : ev_end, 0), "wait v final");
       check(cudaMemcpyAsync(v, d_v.p, xb, cudaMemcpyDeviceToHost, cout_s), "v out");
     };
     // the chain that ends first has its velocities copied first: the atoms'
     // when their state went in first
-    if (!early_nodes || atoms_first) v_out();
-    if (early_nodes) {
+    if (!early || atoms_first) v_out();
+    if (early) {
       for (int p = 0; p < parts_done; p++) {
         const size_t b0 = 24 * (size_t) (parts_done > 1 ? part_bounds[p] : 0);
         const size_t b1 = 24 * (size_t) (p + 1 < parts_done ? part_bounds[p + 1] : enlocal);
@@ -3819,7 +3914,7 @@ void cacg_context::run_host(int n, double *x, double *v, double *nodex, double *
       if (!atoms_first) v_out();
     }
     check(cudaStreamWaitEvent(cout_s, ev_end, 0), "wait step end");
-    if (!early_nodes)
+    if (!early)
       check(cudaMemcpyAsync(nodev, d_nodev.p, nb, cudaMemcpyDeviceToHost, cout_s), "nodev out");
     if (oob_read)
       check(cudaMemcpyAsync(h_pin + 9, d_misc.p + 9, sizeof(int), cudaMemcpyDeviceToHost, cout_s),
