@@ -3641,9 +3641,11 @@ void cacg_context::force_passes(long long b) {
 // positions), atom velocities when the atom chain has integrated them, and,
 // when no fix acts on the forces, node velocities part by part as the
 // element force pass finishes each part of the elements (out_parts).  A step
-// with a rebuild decision waits for all its inputs (the decision reads the
-// new positions on the host) and sends positions out after the decision,
-// while its force passes run.  Otherwise the copies and the steps run in order.
+// with a rebuild decision on distances (no post-force fix) runs its atom
+// chain ahead of the host decision and, without a rebuild, goes on as a plain
+// step; other decision steps wait for all their inputs.  Positions go out
+// after the decision (a rebuild wraps them into the box).  Otherwise the
+// copies and the steps run in order.
 // Results are those of the same steps run on device-resident state.
 void cacg_context::run_host(int n, double *x, double *v, double *nodex, double *nodev) {
   if (n < 1) fail(CACG_EINVAL, "run_host: at least one step");
