@@ -143,19 +143,21 @@ def _host_array(a, pinned):
     return h
 
 
-@pytest.mark.parametrize("precision,pinned", [("MIXED", False), ("MIXED", True),
-                                              ("FP64", False)])
-def test_run_host_matches_device_resident_run(cacg_lib, precision, pinned):
+@pytest.mark.parametrize("precision,pinned,vscale", [("MIXED", False, 5.0), ("MIXED", True, 5.0),
+                                                     ("FP64", False, 5.0), ("MIXED", True, 20.0)])
+def test_run_host_matches_device_resident_run(cacg_lib, precision, pinned, vscale):
     """cacg_run_host (state copied in from host buffers, stepped, copied back,
     with the last step's copies overlapping its computation in mixed precision,
     and on reused pinned buffers the whole call replayed as one graph) gives
     the device-resident trajectory bit for bit: one step per call across
-    rebuild decisions, then several steps per call."""
+    rebuild decisions, then several steps per call.  At 20x the velocities a
+    decision step rebuilds (the atom chain that ran ahead of the decision is
+    discarded and the step redone on the new lists)."""
     cfg, z = C.load_golden("eam_cac")
     cfg = dict(cfg, every=10, check=True)
     m = C.model_from_arrays(z)
-    m.atom_v = m.atom_v * 5.0
-    m.nodev = m.nodev * 5.0
+    m.atom_v = m.atom_v * vscale
+    m.nodev = m.nodev * vscale
     prec = getattr(cacg_lib, precision)
     a = _prepared(cacg_lib, cfg, m, prec)
     b = _prepared(cacg_lib, cfg, m, prec)
@@ -178,6 +180,8 @@ def test_run_host_matches_device_resident_run(cacg_lib, precision, pinned):
         assert np.array_equal(hnv, eb["nodev"])
         ca = a.counts()
         assert ca["rebuilds"] == b.counts()["rebuilds"]
+        if vscale > 10.0:
+            assert ca["rebuilds"] >= 1
         if pinned:  # single-step calls replayed the whole-call graph
             assert single_graph_steps > 0
     finally:
