@@ -1879,13 +1879,23 @@ k_elem_force_fused(FusedArgs a, const float4 *__restrict__ tab, int nr, float rd
     const FusedLat g = fused_lat(a.lat, a.lat_rec, ty);
     const int f0 = a.fjj_off[ty], nf = a.fjj_off[ty + 1] - f0;
     __syncwarp();
-    fused_coeffs(s_nx, lane, s_k, V != 0);
-    if (EAM && lane >= 24) {  // density coefficients from the nodal densities (FP32,
-      // formed in double-single from the doubles' bits: no FP64 instruction)
-      const int m = lane - 24;
-      const ds v = signed_node_sum(s_erds, 1, (unsigned) (RHO_POS >> (8 * m)) & 0xFFu,
-                                   (unsigned) (RHO_NEG >> (8 * m)) & 0xFFu);
-      s_r[m] = v.h + v.l;
+    if (EAM) {
+      // the coefficient vectors (lanes 0-20, as fused_coeffs) and the
+      // nodal-density coefficients (lanes 24-31; FP32, formed in double-single
+      // from the doubles' bits: no FP64 instruction) in one pass: the same
+      // eight double-single additions from different sources
+      const bool dens = lane >= 24;
+      if (lane < 21 || dens) {
+        const int m = dens ? lane - 24 : lane / 3, d = lane % 3;
+        const unsigned long long pm = dens ? RHO_POS : COEF_POS, nm = dens ? RHO_NEG : COEF_NEG;
+        const int sh = dens ? 8 * m : 8 * (m + 1);
+        const ds v = signed_node_sum(dens ? s_erds : s_nx + d, dens ? 1 : 3,
+                                     (unsigned) (pm >> sh) & 0xFFu, (unsigned) (nm >> sh) & 0xFFu);
+        if (dens) s_r[m] = v.h + v.l;
+        else s_k[V != 0 ? 8 * d + m : lane] = v.h + v.l;
+      }
+    } else {
+      fused_coeffs(s_nx, lane, s_k, V != 0);
     }
     __syncwarp();
     float k[21];
